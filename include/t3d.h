@@ -1,0 +1,350 @@
+/*
+ * t3d.h -- C ABI of the GB300 vertex stage for Tetra3D.
+ *
+ * This library replaces the software vertex stage that Tetra3D runs inside
+ * Camera.Render: per (model, mesh part) it transforms the mesh by the model's
+ * MVP, rejects triangles (near/far, screen +-0.5, 2D-cross backface), keys and
+ * bucket-sorts the survivors, lights every emitted vertex and writes the
+ * per-corner stream that Tetra3D hands to ebiten.DrawTrianglesShader.
+ *
+ * Reference interface replaced (file:line in SolarLune/tetra3d):
+ *   Camera.Render               camera.go:1269-2114  -> t3d_render / t3d_render_jobs
+ *   render closure              camera.go:1507-1827  -> device phases (vertex, triangle, emit)
+ *   Model.ProcessVertices       model.go:600-995     -> device vertex + triangle phases
+ *   sortingTriangleBucket       sortingTriangles.go  -> device segmented 512-bin counting sort
+ *   ILight.beginModel / Light   light.go:110-663     -> device model-prep + vertex phases
+ *   flush (vertex lists)        camera.go:1829-2048  -> t3d_frame_* (resident device buffers)
+ *
+ * Conventions
+ *  - Matrices are Tetra3D Matrix4 values: 16 floats, row-major, row vectors
+ *    (v' = v * M), translation in row 3 (matrix.go:10, :619-637).
+ *  - Every function returns an int status: T3D_OK (0) or a negative T3D_E_*.
+ *    t3d_last_error() returns a message for the last failure on that context.
+ *    Nothing aborts the process.
+ *  - Host arrays passed in are copied during the call; the library keeps no
+ *    pointer to caller memory (safe for cgo).
+ *  - Device outputs are owned by the context and stay valid until the next
+ *    render on that context.
+ *  - One context per host thread. Calls on one context are not re-entrant.
+ */
+#ifndef T3D_H
+#define T3D_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define T3D_OK          0
+#define T3D_E_INVAL    -1   /* bad argument (index out of range, bad enum, null) */
+#define T3D_E_OOM      -2   /* device or host allocation failed */
+#define T3D_E_ADMIT    -3   /* serving: request does not fit the HBM budget */
+#define T3D_E_TIMEOUT  -4   /* a bounded device wait gave up */
+#define T3D_E_CUDA     -5   /* CUDA runtime error */
+#define T3D_E_NOTFOUND -6   /* unknown handle */
+#define T3D_E_BUSY     -7   /* serving: queue full */
+
+/* ---- enums mirroring material.go / node.go ----------------------------- */
+/* material.go:9-13 */
+#define T3D_SORT_BACK_TO_FRONT 0
+#define T3D_SORT_FRONT_TO_BACK 1
+#define T3D_SORT_NONE          2
+/* material.go:15-28 */
+#define T3D_TRANSPARENCY_AUTO        0
+#define T3D_TRANSPARENCY_OPAQUE      1
+#define T3D_TRANSPARENCY_ALPHA_CLIP  2
+#define T3D_TRANSPARENCY_TRANSPARENT 3
+/* material.go:34-38 */
+#define T3D_LIGHTING_DEFAULT       0
+#define T3D_LIGHTING_FIXED_NORMALS 1
+#define T3D_LIGHTING_DOUBLE_SIDED  2
+/* material.go:50-55 */
+#define T3D_LV_PER_VERTEX              0
+#define T3D_LV_PER_VERTEX_WITH_NORMAL  1
+#define T3D_LV_PER_OBJECT              2
+#define T3D_LV_OFF                     3
+/* light kinds: AmbientLight, PointLight, DirectionalLight, LightVolume (light.go) */
+#define T3D_LIGHT_AMBIENT     0
+#define T3D_LIGHT_POINT       1
+#define T3D_LIGHT_DIRECTIONAL 2
+#define T3D_LIGHT_VOLUME      3
+/* world.go:7-11 */
+#define T3D_FOG_ADD       0
+#define T3D_FOG_SUB       1
+#define T3D_FOG_OVERWRITE 2
+
+/* render modes */
+#define T3D_MODE_PLAIN   0   /* one launch per model (the reference's per-model loop) */
+#define T3D_MODE_BATCHED 1   /* all models of all jobs in one persistent launch */
+
+/* Maximum lights one model may be lit by (length of its light list). */
+#define T3D_MAX_LIGHTS_PER_MODEL 128
+
+/* ---- input descriptors -------------------------------------------------- */
+
+/* Material fields read by the vertex stage (material.go:64-125, defaults :146-167).
+ * present = 0 stands for MeshPart.Material == nil. */
+typedef struct t3d_material {
+    float   color[4];          /* Material.Color */
+    float   tex_w, tex_h;      /* texture size in px if UseTexture && Texture != nil, else 0 */
+    int32_t present;
+    int32_t backface_culling;  /* default 1 */
+    int32_t sort_mode;         /* T3D_SORT_* */
+    int32_t lighting_mode;     /* T3D_LIGHTING_* */
+    int32_t lv_shading_mode;   /* T3D_LV_* */
+    int32_t shadeless;
+    int32_t visible;           /* default 1 */
+    int32_t transparency_mode; /* T3D_TRANSPARENCY_* */
+    int32_t blend_source_over; /* 1 when Blend == ebiten.BlendSourceOver (default) */
+    int32_t render_order;
+} t3d_material;
+
+/* A MeshPart (mesh.go:2183-2190): a contiguous triangle range with one material. */
+typedef struct t3d_part_desc {
+    uint32_t     tri_start;    /* first triangle (mesh-absolute) */
+    uint32_t     tri_count;
+    t3d_material mat;
+} t3d_part_desc;
+
+/* A Mesh (mesh.go:260-302) as SoA vertex streams. Indices are mesh-absolute
+ * (Triangle.VertexIndexA/B/C). colors is the active vertex colour channel,
+ * NULL when VertexActiveColorChannel < 0. */
+typedef struct t3d_mesh_desc {
+    const float*         positions;   /* 3 * num_vertices */
+    const float*         normals;     /* 3 * num_vertices */
+    const float*         uvs;         /* 2 * num_vertices */
+    const float*         colors;      /* 4 * num_vertices or NULL */
+    const uint32_t*      indices;     /* 3 * num_triangles */
+    const t3d_part_desc* parts;
+    uint32_t             num_vertices;
+    uint32_t             num_triangles;
+    uint32_t             num_parts;
+    int32_t              has_dimensions; /* 0: Dimensions computed like Mesh.UpdateDimensions */
+    float                dim_min[3];     /* Mesh.Dimensions when has_dimensions */
+    float                dim_max[3];
+} t3d_mesh_desc;
+
+/* A Model (model.go:20-61). Either `transform` holds Model.Transform() and
+ * `world_rotation` holds Model.WorldRotation() (use_trs = 0), or the library
+ * builds the transform itself every frame as Scale * Rotation * Translate
+ * from position/scale/rotation (use_trs = 1, a parentless node, node.go:572-608).
+ * rotate_step is applied as rotation = rotate_step * rotation before each
+ * animated frame (Node.Rotate, node.go:1039-1047); identity when static. */
+typedef struct t3d_model_desc {
+    uint32_t mesh;             /* index into the scene's mesh array */
+    int32_t  visible;
+    int32_t  frustum_culling;  /* default 1 */
+    int32_t  shadeless;
+    int32_t  light_list;       /* -1: the scene light list (list 0); else LightGroup list index */
+    int32_t  use_trs;
+    float    color[4];         /* Model.Color */
+    float    transform[16];
+    float    world_rotation[16];
+    float    position[3];
+    float    scale[3];
+    float    rotation[16];
+    float    rotate_step[16];
+} t3d_model_desc;
+
+/* A light (light.go). transform = the light node's Transform(), world_rotation =
+ * its WorldRotation(). Volume fields describe a LightVolume (light.go:377-680):
+ * its Dimensions, cell sizes, cell counts (as LightVolumeResize computed them),
+ * offset, light bias and the index of its first cell colour (RGBA) in the
+ * scene's cell table. Nested LightVolumeCell.useLights are not supported. */
+typedef struct t3d_light_desc {
+    int32_t  type;             /* T3D_LIGHT_* */
+    int32_t  cell_count[3];
+    float    color[4];
+    float    energy;
+    float    range;            /* PointLight.Range(); 0 = inverse-square falloff */
+    float    transform[16];
+    float    world_rotation[16];
+    float    vol_min[3];
+    float    vol_max[3];
+    float    cell_size[3];
+    float    offset[3];
+    float    bias[3];
+    uint32_t cell_first;
+} t3d_light_desc;
+
+/* Everything the vertex stage reads from a Scene. Light list 0 is the scene
+ * light list in Render order: [World.AmbientLight if LightingOn and visible] +
+ * visible lights in tree order (camera.go:1275-1303). Lists 1.. are LightGroups
+ * (lightGroup.go), used whole when a model names them. */
+typedef struct t3d_scene_desc {
+    const t3d_mesh_desc*  meshes;
+    const t3d_model_desc* models;
+    const t3d_light_desc* lights;
+    const float*          volume_cells;   /* RGBA per cell */
+    const uint32_t*       list_offsets;   /* num_lists + 1 */
+    const uint32_t*       list_items;     /* light indices */
+    uint32_t              num_meshes;
+    uint32_t              num_models;
+    uint32_t              num_lights;
+    uint32_t              num_volume_cells;
+    uint32_t              num_lists;
+    uint32_t              reserved;
+} t3d_scene_desc;
+
+/* Camera + World settings read by Render (camera.go:256-321, world.go:25-39).
+ * Clear() must have run for the reference; here the basis comes from
+ * world_rotation directly (camera.go:1085-1088). */
+typedef struct t3d_camera_desc {
+    float   transform[16];       /* Camera.Transform() */
+    float   world_rotation[16];  /* Camera.WorldRotation() */
+    int32_t width, height;
+    int32_t perspective;         /* default 1 */
+    int32_t render_depth;        /* default 1 */
+    int32_t perspective_corrected;
+    int32_t lighting_on;         /* World.LightingOn (0 also when World == nil) */
+    int32_t fog_on;              /* World.FogOn */
+    int32_t fog_mode;            /* T3D_FOG_* */
+    float   fov_y;               /* degrees, default 60 */
+    float   near_plane;          /* default 0.1 */
+    float   far_plane;           /* default 100 */
+    float   ortho_scale;         /* default 20 */
+    float   depth_margin;        /* default 0.04 */
+    float   fog_range[2];
+    float   fog_color[4];
+} t3d_camera_desc;
+
+/* One unit of rendering work: one camera over one resident scene, optionally
+ * restricted to a subset of the scene's lights (bit i of light_mask keeps
+ * light i; the mask filters every light list; all ones = no restriction). */
+typedef struct t3d_job_desc {
+    uint32_t        scene;
+    uint32_t        reserved;
+    uint64_t        light_mask[2];   /* lights 0..127 */
+    t3d_camera_desc camera;
+} t3d_job_desc;
+
+/* ---- outputs ------------------------------------------------------------- */
+
+/* The emitted stream. Per visible triangle, 3 corners in reference emit order;
+ * per corner: xyuv = (DstX, DstY, SrcX, SrcY), rgba = colour vertex colour,
+ * depth = depth vertex colour (camera.go:1646-1820). Segments are the render
+ * pairs (model, mesh part) in Render's draw order: solids then transparents
+ * (camera.go:2050-2109). Segment s owns triangles [seg_base[s], seg_base[s] +
+ * seg_capacity[s]) of the stream; its seg_count[s] visible triangles are
+ * written densely from seg_base[s]. All pointers are device pointers. */
+typedef struct t3d_frame_view {
+    float*    xyuv;          /* float4 per corner */
+    float*    rgba;          /* float4 per corner */
+    float*    depth;         /* float per corner */
+    uint32_t* seg_base;      /* first triangle slot per segment */
+    uint32_t* seg_count;     /* visible triangles per segment (device) */
+    uint32_t  num_segments;
+    uint32_t  reserved;
+    uint64_t  capacity_tris; /* total triangle slots */
+} t3d_frame_view;
+
+/* Host-side segment description (same order as the device arrays). */
+typedef struct t3d_segment_info {
+    uint32_t job;
+    uint32_t model;
+    uint32_t part;
+    uint32_t base;           /* triangle slot */
+    uint32_t capacity;       /* triangles in the part */
+    uint32_t count;          /* visible triangles (valid after t3d_frame_sync) */
+} t3d_segment_info;
+
+typedef struct t3d_stats {
+    uint64_t visible_tris;   /* DebugInfo.drawnTris of the last frame */
+    uint64_t total_tris;     /* DebugInfo.totalTris */
+    uint32_t drawn_parts;    /* segments with at least one visible triangle */
+    uint32_t total_parts;
+    uint32_t culled_models;  /* models rejected by SphereInFrustum */
+    uint32_t launches;       /* kernel launches of the last frame */
+    uint64_t algorithmic_bytes; /* 48V+12T of surviving models + 108*visible + 64*models + 48*lights*lit models */
+    uint64_t scratch_bytes;  /* device scratch held by the context */
+} t3d_stats;
+
+typedef struct t3d_ctx t3d_ctx;
+
+/* ---- context --------------------------------------------------------------- */
+int         t3d_create(int device, t3d_ctx** out);
+int         t3d_destroy(t3d_ctx* ctx);
+const char* t3d_last_error(const t3d_ctx* ctx);
+/* Tuning knobs (0 keeps the current value): triangles per tile, vertices per
+ * vertex-phase work item, threads per block. */
+int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint32_t block_threads);
+
+/* ---- resident scenes --------------------------------------------------------- */
+/* Uploads meshes, models and lights to the device. Replaces Tetra3D's
+ * per-frame reads of Mesh/Model/Light state. */
+int t3d_scene_upload(t3d_ctx* ctx, const t3d_scene_desc* desc, uint32_t* scene_out);
+int t3d_scene_release(t3d_ctx* ctx, uint32_t scene);
+/* Per-frame transform update (Node.Transform changes): n model descs'
+ * transform/world_rotation/position/scale/rotation/rotate_step fields,
+ * for models [first, first+n). */
+int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first,
+                         const t3d_model_desc* models, uint32_t n);
+/* Reads back the current (possibly animated) per-model transforms, 16 floats each. */
+int t3d_scene_get_transforms(t3d_ctx* ctx, uint32_t scene, float* transforms_out, uint32_t n);
+/* Device bytes held by a scene's resident data. */
+int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out);
+
+/* ---- rendering --------------------------------------------------------------- */
+/* Camera.Render over one scene: enqueue on `stream` (a cudaStream_t, NULL =
+ * the context's stream). animate = 1 applies every model's rotate_step first. */
+int t3d_render(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam,
+               int mode, int animate, void* stream);
+/* Several independent jobs in one frame (serving, multi-view). */
+int t3d_render_jobs(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t num_jobs,
+                    int mode, int animate, void* stream);
+/* Waits for the last frame and fills the segment counts. */
+int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out);
+int t3d_frame_view_get(t3d_ctx* ctx, t3d_frame_view* view_out);
+int t3d_frame_segments(t3d_ctx* ctx, t3d_segment_info* segs_out, uint32_t max_segs, uint32_t* num_out);
+/* Copies the visible triangles of the last frame to host memory, densely in
+ * segment order (3 corners per triangle; xyuv/rgba 4 floats per corner). */
+int t3d_frame_download(t3d_ctx* ctx, float* xyuv, float* rgba, float* depth, uint64_t max_tris,
+                       uint64_t* tris_out);
+
+/* ---- CUDA graph replay (batched form) ------------------------------------- */
+/* Captures the frame of t3d_render(mode=BATCHED, animate) into a CUDA graph. */
+int t3d_graph_capture(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam, int animate);
+int t3d_graph_replay(t3d_ctx* ctx, uint32_t frames, void* stream);
+
+/* ---- serving: continuous batching ------------------------------------------- */
+typedef struct t3d_server t3d_server;
+typedef struct t3d_request {
+    t3d_job_desc job;
+    uint64_t     id;
+    double       arrival_s;   /* replay mode: arrival time relative to start */
+} t3d_request;
+typedef struct t3d_completion {
+    uint64_t id;
+    int32_t  status;
+    uint32_t reserved;
+    uint64_t visible_tris;
+    double   arrival_s;
+    double   admit_s;
+    double   done_s;
+    uint64_t checksum;        /* order-dependent hash of the emitted stream */
+} t3d_completion;
+
+/* hbm_budget_bytes bounds the device bytes of in-flight requests' outputs and
+ * scratch; max_batch bounds the jobs per launch; streams = launch slots that
+ * run concurrently. */
+int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batch,
+                      uint32_t streams, t3d_server** out);
+int t3d_server_destroy(t3d_server* srv);
+/* Thread-safe submit; returns T3D_E_ADMIT if the request can never fit. */
+int t3d_server_submit(t3d_server* srv, const t3d_request* req);
+/* verify = 1 (default) hashes every request's emitted stream into
+ * t3d_completion.checksum (costs a device-to-host copy per request). */
+int t3d_server_set_verify(t3d_server* srv, int verify);
+/* Non-blocking poll of finished requests. */
+int t3d_server_poll(t3d_server* srv, t3d_completion* out, uint32_t max, uint32_t* n_out);
+/* Replays requests at their arrival_s offsets from a driver thread and blocks
+ * until all complete; completions in id order into out[n]. */
+int t3d_server_replay(t3d_server* srv, const t3d_request* reqs, uint32_t n, t3d_completion* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* T3D_H */

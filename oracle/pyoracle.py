@@ -1,0 +1,144 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front end of the oracle (oracle/t3d_oracle.cpp).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+checker; never by the product path. PARITY UNPINNED by reference tests (see
+t3d_oracle.h).
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+from tetra3d_gb300 import abi  # noqa: E402  (struct layouts shared with include/t3d.h)
+
+LIB_PATH = os.path.join(HERE, "_build", "libt3d_oracle.so")
+
+
+class OracleOut(C.Structure):
+    _fields_ = [("max_segments", C.c_uint32), ("num_segments", C.c_uint32),
+                ("seg_model", C.POINTER(C.c_uint32)), ("seg_part", C.POINTER(C.c_uint32)),
+                ("seg_base", C.POINTER(C.c_uint32)), ("seg_capacity", C.POINTER(C.c_uint32)),
+                ("seg_count", C.POINTER(C.c_uint32)), ("max_tris", C.c_uint64), ("total_slots", C.c_uint64),
+                ("visible_tris", C.c_uint64), ("tri_index", C.POINTER(C.c_uint32)), ("xyuv", C.c_void_p),
+                ("rgba", C.c_void_p), ("depth", C.c_void_p), ("culled_models", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from oracle import build_oracle
+            build_oracle.build()
+        lib = C.CDLL(LIB_PATH)
+        for name in ("t3d_oracle_render_f32", "t3d_oracle_render_f64"):
+            fn = getattr(lib, name)
+            fn.restype = C.c_int
+            fn.argtypes = [C.POINTER(abi.SceneDesc), C.POINTER(abi.CameraDesc), C.POINTER(C.c_uint64), C.c_uint32,
+                           C.c_uint32, C.POINTER(OracleOut)]
+        f = C.POINTER(C.c_float)
+        lib.t3d_oracle_mat_mult.argtypes = [f, f, f]
+        lib.t3d_oracle_mat_inverted.argtypes = [f, f]
+        lib.t3d_oracle_mat_rotate.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, f]
+        lib.t3d_oracle_mat_decompose.argtypes = [f, f, f, f]
+        lib.t3d_oracle_quat_to_mat.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, f]
+        lib.t3d_oracle_vec_unit.argtypes = [f, f]
+        for n in ("t3d_oracle_mat_mult", "t3d_oracle_mat_inverted", "t3d_oracle_mat_rotate",
+                  "t3d_oracle_mat_decompose", "t3d_oracle_quat_to_mat", "t3d_oracle_vec_unit"):
+            getattr(lib, n).restype = None
+        _lib = lib
+    return _lib
+
+
+class OracleFrame:
+    def __init__(self, segs, tri_index, xyuv, rgba, depth, culled):
+        self.segments = segs      # list of dicts model, part, base, capacity, count (draw order)
+        self.tri_index = tri_index  # (n,) mesh-absolute triangle per visible triangle, in emit order
+        self.xyuv, self.rgba, self.depth = xyuv, rgba, depth
+        self.culled_models = culled
+
+    @property
+    def visible_tris(self):
+        return int(self.tri_index.shape[0])
+
+
+def render(scene_data, cam, light_mask=None, animate_frames=0, threads=1, f64=False):
+    """Runs the CPU restatement of Camera.Render on a SceneData and returns an OracleFrame
+    with the visible triangles compacted in draw order (same layout as the GPU download)."""
+    lib = load()
+    sd = scene_data.desc()
+    nseg_max = sum(len(scene_data.meshes[int(m)].parts) for m in scene_data.mv["mesh"]) + 1
+    slots = max(1, scene_data.total_tris())
+    dt = np.float64 if f64 else np.float32
+    seg = {k: np.zeros(nseg_max, np.uint32) for k in ("model", "part", "base", "capacity", "count")}
+    tri = np.zeros(slots, np.uint32)
+    xyuv = np.zeros((slots, 3, 4), dt)
+    rgba = np.zeros((slots, 3, 4), dt)
+    depth = np.zeros((slots, 3), dt)
+    o = OracleOut()
+    o.max_segments = nseg_max
+    u = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
+    o.seg_model, o.seg_part, o.seg_base = u(seg["model"]), u(seg["part"]), u(seg["base"])
+    o.seg_capacity, o.seg_count = u(seg["capacity"]), u(seg["count"])
+    o.max_tris = slots
+    o.tri_index = u(tri)
+    o.xyuv, o.rgba, o.depth = xyuv.ctypes.data, rgba.ctypes.data, depth.ctypes.data
+    mask = None
+    if light_mask is not None:
+        m = (C.c_uint64 * 2)(light_mask & ((1 << 64) - 1), (light_mask >> 64) & ((1 << 64) - 1))
+        mask = C.cast(m, C.POINTER(C.c_uint64))
+    fn = lib.t3d_oracle_render_f64 if f64 else lib.t3d_oracle_render_f32
+    rc = fn(C.byref(sd), C.byref(cam), mask, animate_frames, threads, C.byref(o))
+    if rc != 0:
+        raise RuntimeError(f"oracle render failed: {rc}")
+    n = o.num_segments
+    segs = [dict(model=int(seg["model"][i]), part=int(seg["part"][i]), base=int(seg["base"][i]),
+                 capacity=int(seg["capacity"][i]), count=int(seg["count"][i])) for i in range(n)]
+    sel = np.concatenate([np.arange(s["base"], s["base"] + s["count"]) for s in segs] or [np.zeros(0, np.int64)])
+    sel = sel.astype(np.int64)
+    return OracleFrame(segs, tri[sel], xyuv[sel], rgba[sel], depth[sel], o.culled_models)
+
+
+def mat_inverted(m):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+    out = np.zeros(16, np.float32)
+    lib.t3d_oracle_mat_inverted(a.ctypes.data_as(C.POINTER(C.c_float)), out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out.reshape(4, 4)
+
+
+def mat_mult(a, b):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(a, np.float32).reshape(16))
+    b = np.ascontiguousarray(np.asarray(b, np.float32).reshape(16))
+    out = np.zeros(16, np.float32)
+    p = lambda x: x.ctypes.data_as(C.POINTER(C.c_float))
+    lib.t3d_oracle_mat_mult(p(a), p(b), p(out))
+    return out.reshape(4, 4)
+
+
+def mat_rotate(x, y, z, angle):
+    lib = load()
+    out = np.zeros(16, np.float32)
+    lib.t3d_oracle_mat_rotate(x, y, z, angle, out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out.reshape(4, 4)
+
+
+def quat_to_mat(x, y, z, w):
+    lib = load()
+    out = np.zeros(16, np.float32)
+    lib.t3d_oracle_quat_to_mat(x, y, z, w, out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out.reshape(4, 4)
+
+
+def vec_unit(v):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(v, np.float32).reshape(3))
+    out = np.zeros(3, np.float32)
+    lib.t3d_oracle_vec_unit(a.ctypes.data_as(C.POINTER(C.c_float)), out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out

@@ -1,0 +1,847 @@
+// t3d_oracle.cpp -- TEST INFRASTRUCTURE ONLY (parity checker and CPU baseline).
+//
+// A CPU restatement of Tetra3D's software vertex stage, following the Go
+// reference function by function. Every routine cites the reference file:line it
+// restates. Compile with -ffp-contract=off and without -ffast-math: the parity
+// convention is unfused IEEE binary32 (the Go compiler may fuse x*y+z on arm64;
+// on amd64 it does not).
+//
+// PARITY UNPINNED by reference tests: the reference has no golden vectors for
+// this path and its Go sources cannot be compiled here. See t3d_oracle.h.
+
+#include "t3d_oracle.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- math32 ----
+// math32/math32.go: Sqrt/Tan/Cos/Atan/Round/Abs go through float64.
+template <typename R> inline R m_sqrt(R x) { return (R)std::sqrt((double)x); }   // math32.go:126
+template <typename R> inline R m_tan(R x) { return (R)std::tan((double)x); }     // math32.go:476
+template <typename R> inline R m_cos(R x) { return (R)std::cos((double)x); }     // math32.go:147
+template <typename R> inline R m_atan(R x) { return (R)std::atan((double)x); }   // math32.go:177
+template <typename R> inline R m_round(R x) { return (R)std::round((double)x); } // math32.go:114
+template <typename R> inline R m_abs(R x) { return (R)std::fabs((double)x); }    // math32.go:227
+template <typename R> inline R m_clamp(R v, R lo, R hi) {                         // math32.go:39-47
+    if (v < lo) return lo;
+    else if (v > hi) return hi;
+    return v;
+}
+template <typename R> inline R k(double v) { return (R)v; }
+template <typename R> inline R maxf() { return (R)std::numeric_limits<float>::max(); }
+
+// Go's int(float) for the light-volume cell index: values that cannot be a
+// cell index map to -1 (no cell).
+template <typename R> inline long long to_index(R v) {
+    if (!(v > (R)-2147483648.0 && v < (R)2147483647.0)) return -1;
+    return (long long)v;
+}
+
+template <typename R> struct V3 { R x, y, z; };
+template <typename R> struct V4 { R x, y, z, w; };
+template <typename R> struct M4 { R m[4][4]; };
+template <typename R> struct C4 { R r, g, b, a; };
+
+template <typename R> inline V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <typename R> inline V3<R> add(V3<R> a, V3<R> b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }  // vector.go:86
+template <typename R> inline V3<R> sub(V3<R> a, V3<R> b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }  // vector.go:112
+template <typename R> inline V3<R> hmul(V3<R> a, V3<R> b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); } // vector.go Mult
+template <typename R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }      // vector.go:526
+template <typename R> inline R magnitude(V3<R> a) { return m_sqrt<R>(a.x * a.x + a.y * a.y + a.z * a.z); } // vector.go:191
+template <typename R> inline R dist2(V3<R> a, V3<R> b) {                                                  // vector.go:242
+    R x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
+    return x * x + y * y + z * z;
+}
+template <typename R> inline V3<R> unit(V3<R> a) {                                                        // vector.go:258-266
+    R l = magnitude(a);
+    if (l < k<R>(1e-8) || l == (R)1) return a;
+    return v3(a.x / l, a.y / l, a.z / l);
+}
+template <typename R> inline V4<R> unit4(V4<R> a) {                                                       // vector.go:1869-1877
+    R l = m_sqrt<R>(a.x * a.x + a.y * a.y + a.z * a.z);
+    if (l < k<R>(1e-8) || l == (R)1) return a;
+    return V4<R>{a.x / l, a.y / l, a.z / l, a.w};
+}
+
+template <typename R> inline M4<R> identity() {                                                           // matrix.go:13-23
+    M4<R> r;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) r.m[i][j] = (i == j) ? (R)1 : (R)0;
+    return r;
+}
+template <typename R> inline M4<R> load_m(const float* p) {
+    M4<R> r;
+    for (int i = 0; i < 16; i++) r.m[i / 4][i % 4] = (R)p[i];
+    return r;
+}
+// matrix_none.go:6-32 (and matrix_amd64.s, same order, no fusion)
+template <typename R> inline M4<R> mult(const M4<R>& a, const M4<R>& b) {
+    M4<R> n = identity<R>();
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            n.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j] + a.m[i][3] * b.m[3][j];
+    return n;
+}
+template <typename R> inline M4<R> transposed(const M4<R>& a) {                                          // matrix.go:218-230
+    M4<R> n = identity<R>();
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) n.m[i][j] = a.m[j][i];
+    return n;
+}
+template <typename R> inline V3<R> mult_vec(const M4<R>& m, V3<R> v) {                                   // matrix.go:619-627
+    return v3(m.m[0][0] * v.x + m.m[1][0] * v.y + m.m[2][0] * v.z + m.m[3][0],
+              m.m[0][1] * v.x + m.m[1][1] * v.y + m.m[2][1] * v.z + m.m[3][1],
+              m.m[0][2] * v.x + m.m[1][2] * v.y + m.m[2][2] * v.z + m.m[3][2]);
+}
+template <typename R> inline V4<R> mult_vec_w(const M4<R>& m, V3<R> v) {                                 // matrix.go:630-636, model.go:808-811
+    return V4<R>{m.m[0][0] * v.x + m.m[1][0] * v.y + m.m[2][0] * v.z + m.m[3][0],
+                 m.m[0][1] * v.x + m.m[1][1] * v.y + m.m[2][1] * v.z + m.m[3][1],
+                 m.m[0][2] * v.x + m.m[1][2] * v.y + m.m[2][2] * v.z + m.m[3][2],
+                 m.m[0][3] * v.x + m.m[1][3] * v.y + m.m[2][3] * v.z + m.m[3][3]};
+}
+template <typename R> inline M4<R> translate(R x, R y, R z) {                                            // matrix.go:82-88
+    M4<R> r = identity<R>();
+    r.m[3][0] = x; r.m[3][1] = y; r.m[3][2] = z;
+    return r;
+}
+template <typename R> inline M4<R> scale_m(R x, R y, R z) {                                              // matrix.go:91-97
+    M4<R> r = identity<R>();
+    r.m[0][0] = x; r.m[1][1] = y; r.m[2][2] = z;
+    return r;
+}
+// matrix.go:255-307
+template <typename R> M4<R> inverted(const M4<R>& M) {
+    const R(&m)[4][4] = M.m;
+    R A2323 = m[2][2] * m[3][3] - m[2][3] * m[3][2];
+    R A1323 = m[2][1] * m[3][3] - m[2][3] * m[3][1];
+    R A1223 = m[2][1] * m[3][2] - m[2][2] * m[3][1];
+    R A0323 = m[2][0] * m[3][3] - m[2][3] * m[3][0];
+    R A0223 = m[2][0] * m[3][2] - m[2][2] * m[3][0];
+    R A0123 = m[2][0] * m[3][1] - m[2][1] * m[3][0];
+    R A2313 = m[1][2] * m[3][3] - m[1][3] * m[3][2];
+    R A1313 = m[1][1] * m[3][3] - m[1][3] * m[3][1];
+    R A1213 = m[1][1] * m[3][2] - m[1][2] * m[3][1];
+    R A2312 = m[1][2] * m[2][3] - m[1][3] * m[2][2];
+    R A1312 = m[1][1] * m[2][3] - m[1][3] * m[2][1];
+    R A1212 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+    R A0313 = m[1][0] * m[3][3] - m[1][3] * m[3][0];
+    R A0213 = m[1][0] * m[3][2] - m[1][2] * m[3][0];
+    R A0312 = m[1][0] * m[2][3] - m[1][3] * m[2][0];
+    R A0212 = m[1][0] * m[2][2] - m[1][2] * m[2][0];
+    R A0113 = m[1][0] * m[3][1] - m[1][1] * m[3][0];
+    R A0112 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    R det = m[0][0] * (m[1][1] * A2323 - m[1][2] * A1323 + m[1][3] * A1223) -
+            m[0][1] * (m[1][0] * A2323 - m[1][2] * A0323 + m[1][3] * A0223) +
+            m[0][2] * (m[1][0] * A1323 - m[1][1] * A0323 + m[1][3] * A0123) -
+            m[0][3] * (m[1][0] * A1223 - m[1][1] * A0223 + m[1][2] * A0123);
+    det = (R)1 / det;
+    M4<R> r = identity<R>();
+    r.m[0][0] = det * (m[1][1] * A2323 - m[1][2] * A1323 + m[1][3] * A1223);
+    r.m[0][1] = det * -(m[0][1] * A2323 - m[0][2] * A1323 + m[0][3] * A1223);
+    r.m[0][2] = det * (m[0][1] * A2313 - m[0][2] * A1313 + m[0][3] * A1213);
+    r.m[0][3] = det * -(m[0][1] * A2312 - m[0][2] * A1312 + m[0][3] * A1212);
+    r.m[1][0] = det * -(m[1][0] * A2323 - m[1][2] * A0323 + m[1][3] * A0223);
+    r.m[1][1] = det * (m[0][0] * A2323 - m[0][2] * A0323 + m[0][3] * A0223);
+    r.m[1][2] = det * -(m[0][0] * A2313 - m[0][2] * A0313 + m[0][3] * A0213);
+    r.m[1][3] = det * (m[0][0] * A2312 - m[0][2] * A0312 + m[0][3] * A0212);
+    r.m[2][0] = det * (m[1][0] * A1323 - m[1][1] * A0323 + m[1][3] * A0123);
+    r.m[2][1] = det * -(m[0][0] * A1323 - m[0][1] * A0323 + m[0][3] * A0123);
+    r.m[2][2] = det * (m[0][0] * A1313 - m[0][1] * A0313 + m[0][3] * A0113);
+    r.m[2][3] = det * -(m[0][0] * A1312 - m[0][1] * A0312 + m[0][3] * A0112);
+    r.m[3][0] = det * -(m[1][0] * A1223 - m[1][1] * A0223 + m[1][2] * A0123);
+    r.m[3][1] = det * (m[0][0] * A1223 - m[0][1] * A0223 + m[0][2] * A0123);
+    r.m[3][2] = det * -(m[0][0] * A1213 - m[0][1] * A0213 + m[0][2] * A0113);
+    r.m[3][3] = det * (m[0][0] * A1212 - m[0][1] * A0212 + m[0][2] * A0112);
+    return r;
+}
+// matrix.go:181-196
+template <typename R> void decompose(const M4<R>& M, V3<R>& pos, V3<R>& scl, M4<R>& rot) {
+    pos = v3(M.m[3][0], M.m[3][1], M.m[3][2]);
+    rot = identity<R>();
+    for (int i = 0; i < 3; i++) {
+        V4<R> row = unit4(V4<R>{M.m[i][0], M.m[i][1], M.m[i][2], M.m[i][3]});
+        rot.m[i][0] = row.x; rot.m[i][1] = row.y; rot.m[i][2] = row.z; rot.m[i][3] = row.w;
+    }
+    M4<R> in = mult(M, transposed(rot));
+    scl = v3(magnitude(v3(in.m[0][0], in.m[0][1], in.m[0][2])),
+             magnitude(v3(in.m[1][0], in.m[1][1], in.m[1][2])),
+             magnitude(v3(in.m[2][0], in.m[2][1], in.m[2][2])));
+}
+template <typename R> inline V3<R> row3(const M4<R>& M, int i) { return v3(M.m[i][0], M.m[i][1], M.m[i][2]); }
+template <typename R> inline V3<R> forward(const M4<R>& M) { return unit(row3(M, 2)); }  // matrix.go:169-175
+template <typename R> inline V3<R> right(const M4<R>& M) { return unit(row3(M, 0)); }    // matrix.go:151-157
+template <typename R> inline V3<R> up(const M4<R>& M) { return unit(row3(M, 1)); }       // matrix.go:160-166
+
+// ----------------------------------------------------------------- scene ----
+struct Dims { float mn[3], mx[3]; };
+
+template <typename R> struct Camera {
+    const t3d_camera_desc* d;
+    M4<R> vp;
+    V3<R> pos, fwd, rgt, upv;
+    R sphere_tang, sphere_y, sphere_x, aspect;
+    R near_, far_, W, H, halfW, halfH, margin, spread;
+};
+
+template <typename R> struct LightPrep {  // per frame (beginRender, light.go:110-113, :318-320)
+    int type;
+    V3<R> color;
+    R energy, range, range2;
+    V3<R> wpos;        // WorldPosition
+    V3<R> amb;         // ambient premultiplied result
+    V3<R> fwd;         // directional workingForward
+    const t3d_light_desc* d;
+};
+
+template <typename R> struct ModelState {
+    M4<R> transform, world_rot;
+};
+
+// One render pair: model index + part index + draw-order slot.
+struct Pair { uint32_t model, part; float depth; int32_t order; };
+
+template <typename R> struct Frame {
+    const t3d_scene_desc* sc;
+    Camera<R> cam;
+    std::vector<LightPrep<R>> lights;
+    std::vector<ModelState<R>> models;
+    std::vector<Dims> dims;
+    const uint64_t* mask;
+};
+
+inline bool light_enabled(const uint64_t* mask, uint32_t i) {
+    if (!mask) return true;
+    if (i >= 128) return false;
+    return (mask[i >> 6] >> (i & 63)) & 1ull;
+}
+
+// Mesh.UpdateDimensions (mesh.go:713-748)
+Dims mesh_dims(const t3d_mesh_desc& me) {
+    Dims d;
+    if (me.has_dimensions) {
+        for (int c = 0; c < 3; c++) { d.mn[c] = me.dim_min[c]; d.mx[c] = me.dim_max[c]; }
+        return d;
+    }
+    for (int c = 0; c < 3; c++) { d.mn[c] = std::numeric_limits<float>::max(); d.mx[c] = -std::numeric_limits<float>::max(); }
+    for (uint32_t v = 0; v < me.num_vertices; v++)
+        for (int c = 0; c < 3; c++) {
+            float p = me.positions[3 * v + c];
+            if (d.mn[c] > p) d.mn[c] = p;
+            if (d.mx[c] < p) d.mx[c] = p;
+        }
+    return d;
+}
+
+// Model.isTransparent (model.go:1274-1282)
+bool is_transparent(const t3d_model_desc& m, const t3d_part_desc& p) {
+    const t3d_material& mat = p.mat;
+    if (mat.present) {
+        bool matT = mat.transparency_mode == T3D_TRANSPARENCY_TRANSPARENT || !mat.blend_source_over ||
+                    (mat.transparency_mode == T3D_TRANSPARENCY_AUTO && mat.color[3] < 0.999f);
+        bool modelT = mat.transparency_mode != T3D_TRANSPARENCY_OPAQUE && m.color[3] < 0.999f;
+        return matT || modelT;
+    }
+    return m.color[3] < 0.999f;
+}
+
+// Camera.ViewMatrix / Projection / Clear basis (camera.go:638-679, :1085-1088)
+template <typename R> void setup_camera(Camera<R>& c, const t3d_camera_desc* d) {
+    c.d = d;
+    M4<R> ct = load_m<R>(d->transform);
+    M4<R> cr = load_m<R>(d->world_rotation);
+    c.pos = row3(ct, 3);
+    M4<R> view = mult(translate<R>(-c.pos.x, -c.pos.y, -c.pos.z), transposed(cr));
+    R fov = (R)d->fov_y, nr = (R)d->near_plane, fr = (R)d->far_plane;
+    R W = (R)d->width, H = (R)d->height;
+    c.aspect = W / H;  // AspectRatio, camera.go:992-995
+    R angle = fov * k<R>(3.1415) / (R)360;
+    c.sphere_tang = m_tan<R>(angle);
+    c.sphere_y = (R)1 / m_cos<R>(angle);
+    c.sphere_x = (R)1 / m_cos<R>(m_atan<R>(c.sphere_tang * c.aspect));
+    M4<R> proj;
+    if (d->perspective) {  // matrix.go:588-604
+        R aspect = W / H;
+        R t = m_tan<R>(fov * (R)(float)M_PI / (R)360);
+        R b = -t, r = t * aspect, l = -r;
+        proj = identity<R>();
+        proj.m[0][0] = ((R)2 * nr) / (r - l); proj.m[0][1] = 0; proj.m[0][2] = (r + l) / (r - l); proj.m[0][3] = 0;
+        proj.m[1][0] = 0; proj.m[1][1] = ((R)2 * nr) / (t - b); proj.m[1][2] = (t + b) / (t - b); proj.m[1][3] = 0;
+        proj.m[2][0] = 0; proj.m[2][1] = 0; proj.m[2][2] = -((fr + nr) / (fr - nr)); proj.m[2][3] = -(((R)2 * fr * nr) / (fr - nr));
+        proj.m[3][0] = 0; proj.m[3][1] = 0; proj.m[3][2] = -1; proj.m[3][3] = 0;
+    } else {  // camera.go:670-675, matrix.go:609-616
+        R asr = H / W;
+        R os = (R)d->ortho_scale;
+        R right_ = (R)1 * os, left_ = (R)-1 * os, top = asr * os, bottom = -asr * os;
+        proj = identity<R>();
+        proj.m[0][0] = (R)2 / (right_ - left_);
+        proj.m[1][1] = (R)2 / (top - bottom);
+        proj.m[2][2] = (R)-2 / (fr - nr);
+        proj.m[3][3] = 1;
+    }
+    c.vp = mult(view, proj);
+    c.fwd = forward(cr); c.rgt = right(cr); c.upv = up(cr);
+    c.near_ = nr; c.far_ = fr; c.W = W; c.H = H;
+    c.halfW = W / (R)2; c.halfH = H / (R)2;
+    c.margin = (fr - nr) * (R)d->depth_margin;      // camera.go:1339
+    c.spread = fr - nr + (c.margin * (R)2);         // camera.go:1341
+}
+
+// Camera.SphereInFrustum (camera.go:933-983)
+template <typename R> bool sphere_in_frustum(const Camera<R>& c, V3<R> position, R radius) {
+    V3<R> diff = sub(position, c.pos);
+    V3<R> fi = v3(-c.fwd.x, -c.fwd.y, -c.fwd.z);
+    R pcZ = dot(diff, fi);
+    if (pcZ > c.far_ + radius || pcZ < c.near_ - radius) return false;
+    if (c.d->perspective) {
+        R d = c.sphere_y * radius;
+        pcZ *= c.sphere_tang;
+        R pcY = dot(diff, c.upv);
+        if (pcY > pcZ + d || pcY < -pcZ - d) return false;
+        pcZ *= c.aspect;
+        d = c.sphere_x * radius;
+        R pcX = dot(diff, c.rgt);
+        if (pcX > pcZ + d || pcX < -pcZ - d) return false;
+    } else {
+        R width = (R)c.d->ortho_scale;
+        R height = width / c.aspect;
+        R pcY = dot(diff, c.upv);
+        if (-height / (R)2 - radius > pcY || pcY > height / (R)2 + radius) return false;
+        R pcX = dot(diff, c.rgt);
+        if (-width / (R)2 - radius > pcX || pcX > width / (R)2 + radius) return false;
+    }
+    return true;
+}
+
+// Model.onTransformUpdate (model.go:142-182) + ModelInFrustum (camera.go:986-989)
+template <typename R> bool model_in_frustum(const Camera<R>& c, const M4<R>& transform, const Dims& dm) {
+    V3<R> position, scale; M4<R> rotation;
+    decompose(transform, position, scale, rotation);
+    V3<R> center = v3<R>(((R)dm.mx[0] + (R)dm.mn[0]) / (R)2, ((R)dm.mx[1] + (R)dm.mn[1]) / (R)2,
+                         ((R)dm.mx[2] + (R)dm.mn[2]) / (R)2);
+    center = mult_vec(rotation, center);
+    position.x += center.x * scale.x;
+    position.y += center.y * scale.y;
+    position.z += center.z * scale.z;
+    V3<R> mn = v3<R>((R)dm.mn[0] * scale.x, (R)dm.mn[1] * scale.y, (R)dm.mn[2] * scale.z);
+    V3<R> mx = v3<R>((R)dm.mx[0] * scale.x, (R)dm.mx[1] * scale.y, (R)dm.mx[2] * scale.z);
+    R radius = magnitude(sub(mx, mn)) / (R)2;
+    return sphere_in_frustum(c, position, radius);
+}
+
+// ------------------------------------------------------ per-pair render ----
+template <typename R> struct Scratch {
+    std::vector<V4<R>> clip;               // globalVertexTransforms
+    std::vector<C4<R>> vlight;             // mesh.vertexLights
+    std::vector<std::vector<std::pair<uint32_t, R>>> bins;
+    std::vector<std::pair<uint32_t, R>> unset;
+    Scratch() : bins(512) {}
+};
+
+template <typename R> struct ModelLight {  // beginModel results for one model
+    const LightPrep<R>* l;
+    V3<R> working;          // point workingPosition
+    bool skip;              // model-level point-range skip (camera.go:1625-1629)
+};
+
+// LightVolume helpers (light.go:717-741, :1267-1272)
+template <typename R> bool lv_cell(const t3d_light_desc* d, V3<R> p, long long& idx) {
+    R csx = (R)d->cell_size[0], csy = (R)d->cell_size[1], csz = (R)d->cell_size[2];
+    long long x = to_index<R>(m_round<R>(((p.x - (R)d->offset[0] - (R)d->vol_min[0] - (csx / (R)2)) / csx)));
+    long long y = to_index<R>(m_round<R>(((p.y - (R)d->offset[1] - (R)d->vol_min[1] - (csy / (R)2)) / csy)));
+    long long z = to_index<R>(m_round<R>(((p.z - (R)d->offset[2] - (R)d->vol_min[2] - (csz / (R)2)) / csz)));
+    if (x < 0 || y < 0 || z < 0 || x >= d->cell_count[0] || y >= d->cell_count[1] || z >= d->cell_count[2]) return false;
+    idx = x + (y * d->cell_count[0]) + (z * d->cell_count[0] * d->cell_count[1]);
+    return true;
+}
+
+template <typename R>
+void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_desc& part, const t3d_mesh_desc& me,
+                  const M4<R>& transform, const M4<R>& dir_rot, uint32_t vi, C4<R>& tgt) {
+    const LightPrep<R>& L = *ml.l;
+    const t3d_material& mat = part.mat;
+    V3<R> vpos = v3<R>((R)me.positions[3 * vi], (R)me.positions[3 * vi + 1], (R)me.positions[3 * vi + 2]);
+    V3<R> vnrm = v3<R>((R)me.normals[3 * vi], (R)me.normals[3 * vi + 1], (R)me.normals[3 * vi + 2]);
+    switch (L.type) {
+    case T3D_LIGHT_AMBIENT:  // light.go:115-120
+        tgt.r += L.amb.x; tgt.g += L.amb.y; tgt.b += L.amb.z;
+        break;
+    case T3D_LIGHT_POINT: {  // light.go:191-258
+        R distance = dist2(ml.working, vpos);
+        if (L.range > 0) {
+            if (distance > L.range2) return;
+        } else {
+            if ((R)1 / distance * L.energy < k<R>(0.001)) return;
+        }
+        V3<R> lightVec = unit(sub(ml.working, vpos));
+        V3<R> n = vnrm;
+        if (mat.present && mat.lighting_mode == T3D_LIGHTING_FIXED_NORMALS) n = lightVec;
+        R diffuse = dot(n, lightVec);
+        if (mat.present && mat.lighting_mode == T3D_LIGHTING_DOUBLE_SIDED) diffuse = m_abs<R>(diffuse);
+        if (diffuse > 0) {
+            R diffuseFactor = diffuse * ((R)1 / ((R)1 + (k<R>(0.1) * distance))) * (R)2;
+            if (L.range2 > 0) {
+                R distClamp = m_clamp<R>((L.range2 - distance) / distance, 0, 1);
+                diffuseFactor *= distClamp;
+            }
+            tgt.r += L.color.x * diffuseFactor * L.energy;
+            tgt.g += L.color.y * diffuseFactor * L.energy;
+            tgt.b += L.color.z * diffuseFactor * L.energy;
+        }
+        break;
+    }
+    case T3D_LIGHT_DIRECTIONAL: {  // light.go:332-360
+        V3<R> normal;
+        if (mat.present && mat.lighting_mode == T3D_LIGHTING_FIXED_NORMALS) normal = L.fwd;
+        else normal = mult_vec(dir_rot, vnrm);
+        R diffuseFactor = dot(normal, L.fwd);
+        if (mat.present && mat.lighting_mode == T3D_LIGHTING_DOUBLE_SIDED) diffuseFactor = m_abs<R>(diffuseFactor);
+        if (diffuseFactor <= 0) return;
+        tgt.r += L.color.x * diffuseFactor * L.energy;
+        tgt.g += L.color.y * diffuseFactor * L.energy;
+        tgt.b += L.color.z * diffuseFactor * L.energy;
+        break;
+    }
+    case T3D_LIGHT_VOLUME: {  // light.go:583-663 (+ Light :667-678)
+        if (mat.present && mat.lv_shading_mode == T3D_LV_OFF) return;
+        const t3d_light_desc* d = L.d;
+        int mode = mat.present ? mat.lv_shading_mode : 0;
+        C4<R> cellColor{0, 0, 0, 1};
+        V3<R> cellSize = v3<R>((R)d->cell_size[0] / (R)2, (R)d->cell_size[1] / (R)2, (R)d->cell_size[2] / (R)2);
+        V3<R> bias = v3<R>((R)d->bias[0], (R)d->bias[1], (R)d->bias[2]);
+        long long idx;
+        if (mat.present && mode == T3D_LV_PER_OBJECT) {
+            if (lv_cell(d, row3(transform, 3), idx)) {
+                const float* cc = F.sc->volume_cells + 4 * (size_t)(d->cell_first + idx);
+                cellColor.r = (R)cc[0]; cellColor.g = (R)cc[1]; cellColor.b = (R)cc[2];
+            }
+        } else {
+            V3<R> vertPos = v3<R>(0, 0, 0), vertPosWithNormal = v3<R>(0, 0, 0);
+            if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL)
+                vertPosWithNormal = add(mult_vec(transform, add(vpos, hmul(vnrm, cellSize))), bias);
+            else
+                vertPos = add(mult_vec(transform, vpos), bias);
+            // Dimensions.Contains (mesh.go:82-84)
+            if (!(vertPos.x >= (R)d->vol_min[0] && vertPos.y >= (R)d->vol_min[1] && vertPos.z >= (R)d->vol_min[2] &&
+                  vertPos.x <= (R)d->vol_max[0] && vertPos.y <= (R)d->vol_max[1] && vertPos.z <= (R)d->vol_max[2]))
+                return;
+            cellColor.r = 0; cellColor.g = 0; cellColor.b = 0;
+            if (lv_cell(d, mode == T3D_LV_PER_VERTEX_WITH_NORMAL ? vertPosWithNormal : vertPos, idx)) {
+                const float* cc = F.sc->volume_cells + 4 * (size_t)(d->cell_first + idx);
+                cellColor.r = (R)cc[0]; cellColor.g = (R)cc[1]; cellColor.b = (R)cc[2]; cellColor.a = (R)cc[3];
+            }
+        }
+        tgt.r += L.color.x * cellColor.r * L.energy;
+        tgt.g += L.color.y * cellColor.g * L.energy;
+        tgt.b += L.color.z * cellColor.b * L.energy;
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+// The render closure (camera.go:1507-1827) with Model.ProcessVertices
+// (model.go:600-995) and the bucket sort (sortingTriangles.go:38-125) for one
+// render pair. Writes up to part.tri_count triangles from `slot`.
+template <typename R, typename OutT>
+uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t slot, t3d_oracle_out* out) {
+    const t3d_scene_desc* sc = F.sc;
+    const t3d_model_desc& md = sc->models[rp.model];
+    const t3d_mesh_desc& me = sc->meshes[md.mesh];
+    const t3d_part_desc& part = me.parts[rp.part];
+    const t3d_material& mat = part.mat;
+    const Camera<R>& cam = F.cam;
+    const t3d_camera_desc* cd = cam.d;
+
+    // ---- Model.ProcessVertices ----
+    S.unset.clear();
+    for (auto& b : S.bins) b.clear();
+    if ((md.color[3] == 0 && is_transparent(md, part)) || !md.visible) return 0;  // model.go:604-606
+
+    const M4<R>& modelTransform = F.models[rp.model].transform;
+    V3<R> camPos = cam.pos;
+    V3<R> p, s; M4<R> r;
+    decompose(inverted(modelTransform), p, s, r);  // model.go:629
+    V3<R> invertedCamPos = add(mult_vec(r, camPos), hmul(p, v3<R>((R)1 / s.x, (R)1 / s.y, (R)1 / s.z)));  // :630
+    M4<R> mvp = mult(modelTransform, cam.vp);  // model.go:695
+
+    R minDepth = maxf<R>();   // model.go:710-711
+    R maxDepth = -maxf<R>();
+    R camNear = cam.near_, camFar = cam.far_;
+
+    if (S.clip.size() < me.num_vertices) S.clip.resize(me.num_vertices);
+    uint32_t t_end = part.tri_start + part.tri_count;
+    for (uint32_t t = part.tri_start; t < t_end; t++) {  // model.go:751-979
+        uint32_t vidx[3] = {me.indices[3 * t], me.indices[3 * t + 1], me.indices[3 * t + 2]};
+        for (int vi = 0; vi < 3; vi++) {
+            uint32_t v = vidx[vi];
+            V3<R> vert = v3<R>((R)me.positions[3 * v], (R)me.positions[3 * v + 1], (R)me.positions[3 * v + 2]);
+            S.clip[v] = mult_vec_w(mvp, vert);  // model.go:808-811
+        }
+        bool outOfBounds = true;  // model.go:855-886
+        V3<R> tv[3];
+        for (int i = 0; i < 3; i++) {
+            const V4<R>& c = S.clip[vidx[i]];
+            R w = c.w;
+            if (w < 0) w = k<R>(0.000001);
+            tv[i].x = c.x / w;
+            tv[i].y = c.y / w;
+            if (c.z + (R)1 >= camNear && c.z < camFar) outOfBounds = false;
+        }
+        if (outOfBounds) continue;
+        if ((tv[0].x < k<R>(-0.5) && tv[1].x < k<R>(-0.5) && tv[2].x < k<R>(-0.5)) ||  // model.go:890-898
+            (tv[0].x > k<R>(0.5) && tv[1].x > k<R>(0.5) && tv[2].x > k<R>(0.5)) ||
+            (tv[0].y < k<R>(-0.5) && tv[1].y < k<R>(-0.5) && tv[2].y < k<R>(-0.5)) ||
+            (tv[0].y > k<R>(0.5) && tv[1].y > k<R>(0.5) && tv[2].y > k<R>(0.5)))
+            continue;
+        if (mat.present && mat.backface_culling) {  // model.go:902-925
+            R n0x = tv[0].x - tv[1].x, n0y = tv[0].y - tv[1].y;
+            R n1x = tv[1].x - tv[2].x, n1y = tv[1].y - tv[2].y;
+            R nor = (n0x * n1y) - (n1x * n0y);
+            if (nor < 0) continue;
+        }
+        // tri.Center (mesh.go:1980-1982)
+        const float* pa = me.positions + 3 * (size_t)vidx[0];
+        const float* pb = me.positions + 3 * (size_t)vidx[1];
+        const float* pc = me.positions + 3 * (size_t)vidx[2];
+        V3<R> center = v3<R>(((R)pa[0] + (R)pb[0] + (R)pc[0]) / (R)3, ((R)pa[1] + (R)pb[1] + (R)pc[1]) / (R)3,
+                             ((R)pa[2] + (R)pb[2] + (R)pc[2]) / (R)3);
+        R dx = invertedCamPos.x - center.x, dy = invertedCamPos.y - center.y, dz = invertedCamPos.z - center.z;
+        R depth = dx * dx + dy * dy + dz * dz;  // model.go:950-953
+        if (std::isnan(depth) || std::isinf(depth)) continue;
+        if (depth < minDepth) minDepth = depth;
+        if (depth > maxDepth) maxDepth = depth;
+        S.unset.push_back({t, depth});  // AddTriangle
+    }
+    if (S.unset.empty()) return 0;  // camera.go:1555-1557
+
+    // ---- sortingTriangleBucket.Sort (sortingTriangles.go:38-64) ----
+    int sortMode = mat.present ? mat.sort_mode : T3D_SORT_BACK_TO_FRONT;  // camera.go:1540-1543
+    const int binCount = 512;
+    R minRange = minDepth, maxRange = maxDepth;
+    R rangeDiff = maxRange - minRange;
+    if (rangeDiff == 0) { maxRange += k<R>(0.001); rangeDiff += k<R>(0.001); }
+    for (auto& e : S.unset) {
+        int targetBin = 0;
+        if (sortMode != T3D_SORT_NONE) {
+            R depth = (e.second - minRange) / rangeDiff * (R)binCount;
+            R t = m_clamp<R>(depth, 0, (R)(binCount - 1));
+            targetBin = (int)t;
+        }
+        S.bins[targetBin].push_back(e);
+    }
+    std::vector<uint32_t> order;
+    order.reserve(S.unset.size());
+    if (sortMode == T3D_SORT_BACK_TO_FRONT) {  // ForEach, sortingTriangles.go:93-125
+        for (int b = binCount - 1; b >= 0; b--) for (auto& e : S.bins[b]) order.push_back(e.first);
+    } else {
+        for (int b = 0; b < binCount; b++) for (auto& e : S.bins[b]) order.push_back(e.first);
+    }
+
+    // ---- lighting (camera.go:1521-1528, :1576-1644) ----
+    bool lighting = cd->lighting_on && !(mat.present && mat.shadeless) && !md.shadeless;
+    std::vector<ModelLight<R>> mlights;
+    M4<R> dir_rot = identity<R>();
+    if (lighting) {
+        uint32_t list = md.light_list < 0 ? 0u : (uint32_t)md.light_list;
+        if (list < sc->num_lists) {
+            V3<R> ip, is; M4<R> ir;
+            decompose(inverted(modelTransform), ip, is, ir);  // light.go:177
+            dir_rot = transposed(inverted(F.models[rp.model].world_rot));  // light.go:328
+            Dims dm = F.dims[md.mesh];
+            R maxSpan = magnitude(v3<R>((R)dm.mx[0] - (R)dm.mn[0], (R)dm.mx[1] - (R)dm.mn[1], (R)dm.mx[2] - (R)dm.mn[2]));
+            V3<R> modelPos = row3(modelTransform, 3);
+            for (uint32_t q = sc->list_offsets[list]; q < sc->list_offsets[list + 1]; q++) {
+                uint32_t li = sc->list_items[q];
+                if (li >= F.lights.size() || !light_enabled(F.mask, li)) continue;
+                ModelLight<R> ml;
+                ml.l = &F.lights[li];
+                ml.working = v3<R>(0, 0, 0);
+                ml.skip = false;
+                if (ml.l->type == T3D_LIGHT_POINT) {
+                    ml.working = add(mult_vec(ir, ml.l->wpos), hmul(ip, v3<R>((R)1 / is.x, (R)1 / is.y, (R)1 / is.z)));  // light.go:186
+                    if (ml.l->range > 0) {
+                        R dist = maxSpan + ml.l->range;
+                        if (dist2(modelPos, ml.l->wpos) > dist * dist) ml.skip = true;
+                    }
+                }
+                mlights.push_back(ml);
+            }
+        }
+    }
+    if (lighting) {
+        if (S.vlight.size() < me.num_vertices) S.vlight.resize(me.num_vertices);
+        for (uint32_t t : order) {  // camera.go:1613-1641
+            uint32_t vidx[3] = {me.indices[3 * t], me.indices[3 * t + 1], me.indices[3 * t + 2]};
+            for (int i = 0; i < 3; i++) S.vlight[vidx[i]] = C4<R>{0, 0, 0, 1};
+            for (auto& ml : mlights) {
+                if (ml.skip) continue;
+                for (int i = 0; i < 3; i++)
+                    vertex_light<R>(F, ml, part, me, modelTransform, dir_rot, vidx[i], S.vlight[vidx[i]]);
+            }
+        }
+    }
+
+    // ---- emit (camera.go:1646-1820) ----
+    C4<R> mp{(R)md.color[0], (R)md.color[1], (R)md.color[2], (R)md.color[3]};
+    if (mat.present) { mp.r *= (R)mat.color[0]; mp.g *= (R)mat.color[1]; mp.b *= (R)mat.color[2]; mp.a *= (R)mat.color[3]; }
+    R srcW = mat.present ? (R)mat.tex_w : (R)0, srcH = mat.present ? (R)mat.tex_h : (R)0;
+    OutT* oxyuv = (OutT*)out->xyuv;
+    OutT* orgba = (OutT*)out->rgba;
+    OutT* odepth = (OutT*)out->depth;
+    uint32_t n = 0;
+    for (uint32_t t : order) {
+        size_t s_ = (size_t)slot + n;
+        out->tri_index[s_] = t;
+        for (int vi = 0; vi < 3; vi++) {
+            uint32_t v = me.indices[3 * t + vi];
+            const V4<R>& c = S.clip[v];
+            R w = c.w;
+            if (!cd->perspective) w = (R)1;
+            if (w < 0) w = k<R>(0.001);
+            R dx = (c.x / w) * cam.W + cam.halfW;
+            R dy = (c.y / -w) * cam.H + cam.halfH;
+            R U = (R)me.uvs[2 * v], V = (R)me.uvs[2 * v + 1];
+            R uvU, uvV;
+            if (cd->perspective_corrected) { uvU = (U / w) * srcW; uvV = (((R)1 - V) / w) * srcH; }
+            else { uvU = U * srcW; uvV = ((R)1 - V) * srcH; }
+            C4<R> col;
+            if (me.colors) {
+                const float* vc = me.colors + 4 * (size_t)v;
+                col = C4<R>{(R)vc[0] * mp.r, (R)vc[1] * mp.g, (R)vc[2] * mp.b, (R)vc[3] * mp.a};
+            } else {
+                col = mp;
+            }
+            if (lighting) { col.r *= S.vlight[v].r; col.g *= S.vlight[v].g; col.b *= S.vlight[v].b; }
+            R depthOut = 0;
+            if (cd->render_depth || cd->fog_on) {
+                R depth = (c.z + cam.margin) / cam.spread;
+                if (depth < 0) depth = 0;
+                else if (depth > 1) depth = 1;
+                depthOut = depth;
+                if (!cd->render_depth) {  // fog branch, camera.go:1783-1812
+                    R f0 = (R)cd->fog_range[0], f1 = (R)cd->fog_range[1];
+                    R fd = f0 + ((f1 - f0) * (R)1 - depth);
+                    if (cd->fog_mode == T3D_FOG_ADD) {
+                        col.r += (R)cd->fog_color[0] * fd; col.g += (R)cd->fog_color[1] * fd; col.b += (R)cd->fog_color[2] * fd;
+                    } else if (cd->fog_mode == T3D_FOG_SUB) {
+                        col.r *= (R)cd->fog_color[0] * fd; col.g *= (R)cd->fog_color[1] * fd; col.b *= (R)cd->fog_color[2] * fd;
+                    }
+                }
+            }
+            size_t ci = s_ * 3 + vi;
+            oxyuv[4 * ci] = (OutT)dx; oxyuv[4 * ci + 1] = (OutT)dy; oxyuv[4 * ci + 2] = (OutT)uvU; oxyuv[4 * ci + 3] = (OutT)uvV;
+            orgba[4 * ci] = (OutT)col.r; orgba[4 * ci + 1] = (OutT)col.g; orgba[4 * ci + 2] = (OutT)col.b; orgba[4 * ci + 3] = (OutT)col.a;
+            odepth[ci] = (OutT)depthOut;
+        }
+        n++;
+    }
+    return n;
+}
+
+template <typename R, typename OutT>
+int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* mask, uint32_t animate_frames,
+           uint32_t threads, t3d_oracle_out* out) {
+    if (!sc || !cd || !out) return T3D_E_INVAL;
+    Frame<R> F;
+    F.sc = sc;
+    F.mask = mask;
+    setup_camera(F.cam, cd);
+
+    // models: Node.Transform (node.go:572-608) with optional animation steps
+    F.models.resize(sc->num_models);
+    for (uint32_t i = 0; i < sc->num_models; i++) {
+        const t3d_model_desc& md = sc->models[i];
+        if (md.mesh >= sc->num_meshes) return T3D_E_INVAL;
+        if (md.use_trs) {
+            M4<R> rot = load_m<R>(md.rotation);
+            M4<R> step = load_m<R>(md.rotate_step);
+            for (uint32_t f = 0; f < animate_frames; f++) rot = mult(step, rot);  // Matrix4.Rotated, matrix.go:583-585
+            M4<R> tr = scale_m<R>((R)md.scale[0], (R)md.scale[1], (R)md.scale[2]);
+            tr = mult(tr, rot);
+            tr = mult(tr, translate<R>((R)md.position[0], (R)md.position[1], (R)md.position[2]));
+            F.models[i].transform = tr;
+            F.models[i].world_rot = rot;
+        } else {
+            F.models[i].transform = load_m<R>(md.transform);
+            F.models[i].world_rot = load_m<R>(md.world_rotation);
+        }
+    }
+    F.dims.resize(sc->num_meshes);
+    for (uint32_t m = 0; m < sc->num_meshes; m++) F.dims[m] = mesh_dims(sc->meshes[m]);
+
+    // lights: beginRender (light.go:110-113, :318-320)
+    F.lights.resize(sc->num_lights);
+    for (uint32_t i = 0; i < sc->num_lights; i++) {
+        const t3d_light_desc& d = sc->lights[i];
+        LightPrep<R>& L = F.lights[i];
+        L.d = &d;
+        L.type = d.type;
+        L.color = v3<R>((R)d.color[0], (R)d.color[1], (R)d.color[2]);
+        L.energy = (R)d.energy;
+        L.range = (R)d.range;
+        L.range2 = L.range * L.range;  // PointLight.SetRange, light.go:270-273
+        M4<R> lt = load_m<R>(d.transform);
+        L.wpos = row3(lt, 3);
+        L.amb = v3<R>(L.color.x * L.energy, L.color.y * L.energy, L.color.z * L.energy);
+        L.fwd = forward(load_m<R>(d.world_rotation));
+    }
+
+    // Render pairs (camera.go:1343-1457, :2050-2109). Frustum-culled models
+    // never become pairs in the reference; their removal does not change the
+    // relative draw order of the others (the sorts are stable), so the segment
+    // table keeps them, with zero triangles, to line up with the device layout.
+    std::vector<char> is_culled(sc->num_models, 0);
+    uint32_t culled = 0;
+    std::vector<Pair> solids, transparents;
+    for (uint32_t i = 0; i < sc->num_models; i++) {
+        const t3d_model_desc& md = sc->models[i];
+        if (!md.visible) continue;
+        if (md.frustum_culling && !model_in_frustum(F.cam, F.models[i].transform, F.dims[md.mesh])) {
+            is_culled[i] = 1;
+            culled++;
+        }
+        const t3d_mesh_desc& me = sc->meshes[md.mesh];
+        V3<R> mpos = row3(F.models[i].transform, 3);
+        for (uint32_t p = 0; p < me.num_parts; p++) {
+            const t3d_part_desc& part = me.parts[p];
+            if (part.mat.present && !part.mat.visible) continue;  // MeshPart.isVisible, mesh.go:2402-2407
+            Pair rp{i, p, (float)dist2(F.cam.pos, mpos), part.mat.present ? part.mat.render_order : 0};
+            if (is_transparent(md, part)) transparents.push_back(rp);
+            else solids.push_back(rp);
+        }
+    }
+    auto stable_by = [](std::vector<Pair>& v, auto less) {
+        // bottom-up stable merge sort (any stable sort orders a strict weak ordering identically)
+        std::vector<Pair> tmp(v.size());
+        for (size_t width = 1; width < v.size(); width *= 2) {
+            for (size_t lo = 0; lo < v.size(); lo += 2 * width) {
+                size_t mid = std::min(lo + width, v.size()), hi = std::min(lo + 2 * width, v.size());
+                size_t a = lo, b = mid, o = lo;
+                while (a < mid && b < hi) tmp[o++] = less(v[b], v[a]) ? v[b++] : v[a++];
+                while (a < mid) tmp[o++] = v[a++];
+                while (b < hi) tmp[o++] = v[b++];
+            }
+            v.swap(tmp);
+        }
+    };
+    auto by_order_then_far = [](const Pair& a, const Pair& b) {
+        return a.order != b.order ? a.order < b.order : a.depth > b.depth;
+    };
+    if (!cd->render_depth) stable_by(solids, by_order_then_far);  // camera.go:1461-1470
+    stable_by(transparents, by_order_then_far);                   // camera.go:2050-2055
+    std::vector<Pair> segs(solids);
+    segs.insert(segs.end(), transparents.begin(), transparents.end());
+
+    if (segs.size() > out->max_segments) return T3D_E_INVAL;
+    uint64_t base = 0;
+    for (size_t s = 0; s < segs.size(); s++) {
+        const t3d_mesh_desc& me = sc->meshes[sc->models[segs[s].model].mesh];
+        out->seg_model[s] = segs[s].model;
+        out->seg_part[s] = segs[s].part;
+        out->seg_base[s] = (uint32_t)base;
+        out->seg_capacity[s] = me.parts[segs[s].part].tri_count;
+        out->seg_count[s] = 0;
+        base += me.parts[segs[s].part].tri_count;
+    }
+    out->num_segments = (uint32_t)segs.size();
+    out->total_slots = base;
+    out->culled_models = culled;
+    if (base > out->max_tris) return T3D_E_INVAL;
+
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        Scratch<R> S;
+        for (;;) {
+            size_t s = next.fetch_add(1);
+            if (s >= segs.size()) break;
+            if (is_culled[segs[s].model]) continue;
+            out->seg_count[s] = render_pair<R, OutT>(F, S, segs[s], out->seg_base[s], out);
+        }
+    };
+    if (threads <= 1) {
+        worker();
+    } else {
+        std::vector<std::thread> pool;
+        for (uint32_t t = 0; t < threads; t++) pool.emplace_back(worker);
+        for (auto& th : pool) th.join();
+    }
+    uint64_t vis = 0;
+    for (size_t s = 0; s < segs.size(); s++) vis += out->seg_count[s];
+    out->visible_tris = vis;
+    return T3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int t3d_oracle_render_f32(const t3d_scene_desc* scene, const t3d_camera_desc* cam, const uint64_t* light_mask,
+                          uint32_t animate_frames, uint32_t threads, t3d_oracle_out* out) {
+    return render<float, float>(scene, cam, light_mask, animate_frames, threads, out);
+}
+int t3d_oracle_render_f64(const t3d_scene_desc* scene, const t3d_camera_desc* cam, const uint64_t* light_mask,
+                          uint32_t animate_frames, uint32_t threads, t3d_oracle_out* out) {
+    return render<double, double>(scene, cam, light_mask, animate_frames, threads, out);
+}
+
+void t3d_oracle_mat_mult(const float* a, const float* b, float* out) {
+    M4<float> r = mult(load_m<float>(a), load_m<float>(b));
+    for (int i = 0; i < 16; i++) out[i] = r.m[i / 4][i % 4];
+}
+void t3d_oracle_mat_inverted(const float* m, float* out) {
+    M4<float> r = inverted(load_m<float>(m));
+    for (int i = 0; i < 16; i++) out[i] = r.m[i / 4][i % 4];
+}
+// NewMatrix4Rotate (matrix.go:101-128); Sin/Cos through float64 (math32.go:137-150)
+void t3d_oracle_mat_rotate(float x, float y, float z, float angle, float* out) {
+    if (x == 0 && y == 0 && z == 0) y = 1;
+    M4<float> mat = identity<float>();
+    V3<float> v = unit(v3<float>(x, y, z));
+    float s = (float)std::sin((double)angle);
+    float c = (float)std::cos((double)angle);
+    float m = 1 - c;
+    mat.m[0][0] = m * v.x * v.x + c;
+    mat.m[0][1] = m * v.x * v.y + v.z * s;
+    mat.m[0][2] = m * v.z * v.x - v.y * s;
+    mat.m[1][0] = m * v.x * v.y - v.z * s;
+    mat.m[1][1] = m * v.y * v.y + c;
+    mat.m[1][2] = m * v.y * v.z + v.x * s;
+    mat.m[2][0] = m * v.z * v.x + v.y * s;
+    mat.m[2][1] = m * v.y * v.z - v.x * s;
+    mat.m[2][2] = m * v.z * v.z + c;
+    for (int i = 0; i < 16; i++) out[i] = mat.m[i / 4][i % 4];
+}
+void t3d_oracle_mat_decompose(const float* m, float* pos3, float* scale3, float* rot16) {
+    V3<float> p, s; M4<float> r;
+    decompose(load_m<float>(m), p, s, r);
+    pos3[0] = p.x; pos3[1] = p.y; pos3[2] = p.z;
+    scale3[0] = s.x; scale3[1] = s.y; scale3[2] = s.z;
+    for (int i = 0; i < 16; i++) rot16[i] = r.m[i / 4][i % 4];
+}
+// Quaternion.ToMatrix4 (quaternion.go:135-182)
+void t3d_oracle_quat_to_mat(float x, float y, float z, float w, float* out) {
+    M4<float> m1 = identity<float>(), m2 = identity<float>();
+    m1.m[0][0] = w;  m1.m[0][1] = z;  m1.m[0][2] = -y; m1.m[0][3] = x;
+    m1.m[1][0] = -z; m1.m[1][1] = w;  m1.m[1][2] = x;  m1.m[1][3] = y;
+    m1.m[2][0] = y;  m1.m[2][1] = -x; m1.m[2][2] = w;  m1.m[2][3] = z;
+    m1.m[3][0] = -x; m1.m[3][1] = -y; m1.m[3][2] = -z; m1.m[3][3] = w;
+    m2.m[0][0] = w;  m2.m[0][1] = z;  m2.m[0][2] = -y; m2.m[0][3] = -x;
+    m2.m[1][0] = -z; m2.m[1][1] = w;  m2.m[1][2] = x;  m2.m[1][3] = -y;
+    m2.m[2][0] = y;  m2.m[2][1] = -x; m2.m[2][2] = w;  m2.m[2][3] = -z;
+    m2.m[3][0] = x;  m2.m[3][1] = y;  m2.m[3][2] = z;  m2.m[3][3] = w;
+    M4<float> r = mult(m1, m2);
+    for (int i = 0; i < 16; i++) out[i] = r.m[i / 4][i % 4];
+}
+void t3d_oracle_vec_unit(const float* v, float* o) {
+    V3<float> r = unit(v3<float>(v[0], v[1], v[2]));
+    o[0] = r.x; o[1] = r.y; o[2] = r.z;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+/*
+ * t3d_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of Tetra3D's software vertex stage (Camera.Render minus the
+ * ebiten draw calls) used as the parity checker for the CUDA library and as the
+ * timed CPU baseline. Nothing in the product links or calls this library; only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg do.
+ *
+ * PARITY UNPINNED: the reference (pure Go) publishes no golden vectors for this
+ * path and cannot be compiled here (no Go toolchain). The restatement is pinned
+ * only by the reference's one unit test (TestMatrixInversion, matrix_test.go:36-62)
+ * and by hand-computed known-answer cases in tests/.
+ *
+ * Arithmetic convention: unfused IEEE binary32 (-ffp-contract=off), with
+ * math32.Sqrt/Tan/Cos/Atan/Round evaluated in binary64 and rounded, as
+ * math32/math32.go does. The _f64 twin evaluates everything in binary64 for
+ * error reporting.
+ */
+#ifndef T3D_ORACLE_H
+#define T3D_ORACLE_H
+#include "../include/t3d.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Output in the same segment layout the GPU library uses: render pairs in draw
+ * order, each owning `capacity` triangle slots from `base`; `count` of them are
+ * written. Per slot: the mesh-absolute triangle index and 3 corners. */
+typedef struct t3d_oracle_out {
+    uint32_t  max_segments;
+    uint32_t  num_segments;      /* out */
+    uint32_t* seg_model;         /* [max_segments] */
+    uint32_t* seg_part;
+    uint32_t* seg_base;
+    uint32_t* seg_capacity;
+    uint32_t* seg_count;
+    uint64_t  max_tris;          /* slots available */
+    uint64_t  total_slots;       /* out: sum of capacities */
+    uint64_t  visible_tris;      /* out */
+    uint32_t* tri_index;         /* [max_tris] */
+    void*     xyuv;              /* [max_tris*3*4] float or double */
+    void*     rgba;              /* [max_tris*3*4] */
+    void*     depth;             /* [max_tris*3] */
+    uint32_t  culled_models;     /* out */
+    uint32_t  reserved;
+} t3d_oracle_out;
+
+/* Renders one frame. light_mask may be NULL (all lights). animate_frames
+ * applies each model's rotate_step that many times first. threads > 1 splits
+ * render pairs over host threads (results identical). */
+int t3d_oracle_render_f32(const t3d_scene_desc* scene, const t3d_camera_desc* cam,
+                          const uint64_t* light_mask, uint32_t animate_frames,
+                          uint32_t threads, t3d_oracle_out* out);
+int t3d_oracle_render_f64(const t3d_scene_desc* scene, const t3d_camera_desc* cam,
+                          const uint64_t* light_mask, uint32_t animate_frames,
+                          uint32_t threads, t3d_oracle_out* out);
+
+/* Matrix4 helpers (float32) for pinning against matrix_test.go. */
+void t3d_oracle_mat_mult(const float* a, const float* b, float* out);
+void t3d_oracle_mat_inverted(const float* m, float* out);
+void t3d_oracle_mat_rotate(float x, float y, float z, float angle, float* out);
+void t3d_oracle_mat_decompose(const float* m, float* pos3, float* scale3, float* rot16);
+void t3d_oracle_quat_to_mat(float x, float y, float z, float w, float* out);
+void t3d_oracle_vec_unit(const float* v3, float* out3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,379 @@
+// t3d_capi.cu -- extern "C" entry points of include/t3d.h (context, scenes,
+// frames, CUDA graph replay). Serving lives in t3d_serve.cu.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "t3d_runtime.h"
+
+extern "C" const void* t3d_frame_kernel_ptr();
+extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris);
+
+using namespace t3d;
+
+#define CKR(call)                                                                                       \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            set_err(ctx, "%s failed: %s", #call, cudaGetErrorString(e_));                              \
+            return e_ == cudaErrorMemoryAllocation ? T3D_E_OOM : T3D_E_CUDA;                            \
+        }                                                                                               \
+    } while (0)
+
+namespace t3d {
+int configure(t3d_ctx* ctx) {
+    ctx->smem_bytes = t3d_frame_smem_bytes(ctx->tile_tris);
+    const void* fn = t3d_frame_kernel_ptr();
+    CKR(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
+    int per_sm = 0;
+    CKR(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)ctx->block_threads, ctx->smem_bytes));
+    if (per_sm < 1) {
+        set_err(ctx, "frame kernel does not fit on an SM (block %u, smem %zu)", ctx->block_threads, ctx->smem_bytes);
+        return T3D_E_INVAL;
+    }
+    ctx->max_grid = (uint32_t)(per_sm * ctx->num_sms);
+    return T3D_OK;
+}
+}  // namespace t3d
+
+static void drop_graph(t3d_ctx* ctx) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->graph_exec = nullptr;
+    ctx->graph = nullptr;
+}
+
+extern "C" {
+
+int t3d_create(int device, t3d_ctx** out) {
+    if (!out) return T3D_E_INVAL;
+    *out = nullptr;
+    t3d_ctx* ctx = new (std::nothrow) t3d_ctx();
+    if (!ctx) return T3D_E_OOM;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        delete ctx;
+        return T3D_E_CUDA;
+    }
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming) != cudaSuccess) {
+        delete ctx;
+        return T3D_E_CUDA;
+    }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+    if (!coop) {
+        delete ctx;
+        return T3D_E_CUDA;
+    }
+    if (configure(ctx) != T3D_OK) {
+        delete ctx;
+        return T3D_E_CUDA;
+    }
+    *out = ctx;
+    return T3D_OK;
+}
+
+int t3d_destroy(t3d_ctx* ctx) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    for (auto& kv : ctx->scenes) kv.second->release();
+    ctx->scenes.clear();
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->light_work, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax,
+                      &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth})
+        b->release();
+    ctx->table_host.release();
+    ctx->readback.release();
+    if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return T3D_OK;
+}
+
+const char* t3d_last_error(const t3d_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint32_t block_threads) {
+    if (!ctx) return T3D_E_INVAL;
+    uint32_t T = tile_tris ? tile_tris : ctx->tile_tris;
+    uint32_t V = vertex_chunk ? vertex_chunk : ctx->vchunk;
+    uint32_t B = block_threads ? block_threads : ctx->block_threads;
+    if (T < 256 || T > (uint32_t)kTileMax || (T & (T - 1)) || V < 32 || V > (1u << 20) || (B != 128 && B != 256 && B != 512)) {
+        set_err(ctx, "set_tuning: tile %u (256..%d, power of two), chunk %u, block %u (128/256/512)", T, kTileMax, V, B);
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    uint32_t oT = ctx->tile_tris, oV = ctx->vchunk, oB = ctx->block_threads;
+    ctx->tile_tris = T;
+    ctx->vchunk = V;
+    ctx->block_threads = B;
+    int rc = configure(ctx);
+    if (rc) {
+        ctx->tile_tris = oT; ctx->vchunk = oV; ctx->block_threads = oB;
+        configure(ctx);
+        return rc;
+    }
+    drop_graph(ctx);
+    ctx->frame_valid = false;
+    return T3D_OK;
+}
+
+int t3d_scene_upload(t3d_ctx* ctx, const t3d_scene_desc* desc, uint32_t* scene_out) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    return scene_upload(ctx, desc, scene_out);
+}
+
+int t3d_scene_release(t3d_ctx* ctx, uint32_t scene) {
+    if (!ctx) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
+    drop_graph(ctx);
+    ctx->frame_valid = false;
+    it->second->release();
+    ctx->scenes.erase(it);
+    return T3D_OK;
+}
+
+int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d_model_desc* models, uint32_t n) {
+    if (!ctx || (n && !models)) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    Scene* sc = it->second.get();
+    if ((uint64_t)first + n > sc->models.size()) {
+        set_err(ctx, "set_models: range [%u, %u) beyond %zu models", first, first + n, sc->models.size());
+        return T3D_E_INVAL;
+    }
+    for (uint32_t i = 0; i < n; i++)
+        if (models[i].mesh >= sc->meshes.size() || models[i].light_list >= (int32_t)sc->lists.size()) {
+            set_err(ctx, "set_models: model %u has a bad mesh or light list", first + i);
+            return T3D_E_INVAL;
+        }
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
+    return scene_write_models(ctx, sc, first, models, n);
+}
+
+int t3d_scene_get_transforms(t3d_ctx* ctx, uint32_t scene, float* out, uint32_t n) {
+    if (!ctx || !out) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    Scene* sc = it->second.get();
+    n = std::min<uint32_t>(n, (uint32_t)sc->models.size());
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    std::vector<DevModel> dm(n);
+    if (n) CKR(cudaMemcpy(dm.data(), sc->dmodels.ptr, sizeof(DevModel) * n, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < n; i++) {
+        const DevModel& m = dm[i];
+        if (m.flags & MOD_TRS) {
+            m4 M = trs(mk3(m.position[0], m.position[1], m.position[2]), mk3(m.scale[0], m.scale[1], m.scale[2]),
+                       load16(m.rotation));
+            store16(M, out + 16 * (size_t)i);
+        } else {
+            memcpy(out + 16 * (size_t)i, m.transform, 64);
+        }
+    }
+    return T3D_OK;
+}
+
+int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out) {
+    if (!ctx || !bytes_out) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    *bytes_out = it->second->device_bytes();
+    return T3D_OK;
+}
+
+int t3d_render_jobs(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t num_jobs, int mode, int animate, void* stream) {
+    if (!ctx || (num_jobs && !jobs) || (mode != T3D_MODE_PLAIN && mode != T3D_MODE_BATCHED)) return T3D_E_INVAL;
+    if (animate) {
+        for (uint32_t a = 0; a < num_jobs; a++)
+            for (uint32_t b = a + 1; b < num_jobs; b++)
+                if (jobs[a].scene == jobs[b].scene) {
+                    set_err(ctx, "animate: scene %u appears in more than one job", jobs[a].scene);
+                    return T3D_E_INVAL;
+                }
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    if (ctx->last_stream && ctx->last_stream != st) CKR(cudaStreamSynchronize(ctx->last_stream));
+    ctx->frame_valid = false;
+    int rc = build_frame(ctx, jobs, num_jobs, animate);
+    if (rc) return rc;
+    // The table arena is reused: the previous frame must have consumed it.
+    if ((rc = upload_frame(ctx, st))) return rc;
+    if ((rc = launch_frame(ctx, mode, st))) return rc;
+    ctx->last_stream = st;
+    ctx->frame_pending = true;
+    return T3D_OK;
+}
+
+int t3d_render(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam, int mode, int animate, void* stream) {
+    if (!ctx || !cam) return T3D_E_INVAL;
+    t3d_job_desc job;
+    memset(&job, 0, sizeof job);
+    job.scene = scene;
+    job.light_mask[0] = job.light_mask[1] = ~0ull;
+    job.camera = *cam;
+    return t3d_render_jobs(ctx, &job, 1, mode, animate, stream);
+}
+
+int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    if (!ctx->frame_pending && !ctx->frame_valid) {
+        set_err(ctx, "frame_sync: no frame rendered");
+        return T3D_E_INVAL;
+    }
+    cudaStream_t st = ctx->last_stream ? ctx->last_stream : ctx->stream;
+    FrameTables& F = ctx->tables;
+    const size_t nseg = F.segs.size();
+    const size_t rb = 4 * nseg + sizeof(Ctl) * ctx->nctl + 64;
+    if (ctx->readback.ensure(rb)) { set_err(ctx, "pinned readback alloc failed"); return T3D_E_OOM; }
+    uint32_t* counts = (uint32_t*)ctx->readback.ptr;
+    Ctl* ctls = (Ctl*)((char*)ctx->readback.ptr + ((4 * nseg + 63) & ~(size_t)63));
+    if (nseg) CKR(cudaMemcpyAsync(counts, ctx->seg_count.ptr, 4 * nseg, cudaMemcpyDeviceToHost, st));
+    if (ctx->nctl) CKR(cudaMemcpyAsync(ctls, ctx->ctl.ptr, sizeof(Ctl) * ctx->nctl, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    ctx->frame_pending = false;
+    t3d_stats s;
+    memset(&s, 0, sizeof s);
+    for (uint32_t i = 0; i < ctx->nctl; i++) {
+        if (ctls[i].err) {
+            set_err(ctx, "frame kernel reported error %d (launch %u)", ctls[i].err, i);
+            ctx->frame_valid = false;
+            return ctls[i].err == ERR_BARRIER_TIMEOUT ? T3D_E_TIMEOUT : T3D_E_CUDA;
+        }
+        s.algorithmic_bytes += ctls[i].bytes;
+        s.culled_models += ctls[i].culled;
+    }
+    for (size_t k = 0; k < nseg; k++) {
+        F.seg_info[k].count = counts[k];
+        s.visible_tris += counts[k];
+        s.total_tris += F.seg_info[k].capacity;
+        if (counts[k]) s.drawn_parts++;
+    }
+    s.total_parts = (uint32_t)nseg;
+    s.algorithmic_bytes += 108ull * s.visible_tris;
+    s.launches = ctx->launches;
+    size_t scratch = 0;
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->light_work, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
+        scratch += b->cap;
+    s.scratch_bytes = scratch;
+    ctx->stats = s;
+    ctx->frame_valid = true;
+    if (stats_out) *stats_out = s;
+    return T3D_OK;
+}
+
+int t3d_frame_view_get(t3d_ctx* ctx, t3d_frame_view* v) {
+    if (!ctx || !v) return T3D_E_INVAL;
+    v->xyuv = (float*)ctx->out_xyuv.ptr;
+    v->rgba = (float*)ctx->out_rgba.ptr;
+    v->depth = (float*)ctx->out_depth.ptr;
+    v->seg_base = nullptr;
+    v->seg_count = (uint32_t*)ctx->seg_count.ptr;
+    v->num_segments = (uint32_t)ctx->tables.segs.size();
+    v->reserved = 0;
+    v->capacity_tris = ctx->tables.nslots;
+    return T3D_OK;
+}
+
+int t3d_frame_segments(t3d_ctx* ctx, t3d_segment_info* segs, uint32_t max_segs, uint32_t* num_out) {
+    if (!ctx || !num_out) return T3D_E_INVAL;
+    const auto& info = ctx->tables.seg_info;
+    *num_out = (uint32_t)info.size();
+    if (segs) memcpy(segs, info.data(), sizeof(t3d_segment_info) * std::min<size_t>(max_segs, info.size()));
+    return T3D_OK;
+}
+
+int t3d_frame_download(t3d_ctx* ctx, float* xyuv, float* rgba, float* depth, uint64_t max_tris, uint64_t* tris_out) {
+    if (!ctx) return T3D_E_INVAL;
+    if (!ctx->frame_valid) {
+        set_err(ctx, "frame_download: call t3d_frame_sync first");
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    uint64_t n = 0;
+    for (const auto& si : ctx->tables.seg_info) {
+        if (!si.count) continue;
+        if (n + si.count > max_tris) {
+            set_err(ctx, "frame_download: %llu triangles do not fit %llu", (unsigned long long)(n + si.count),
+                    (unsigned long long)max_tris);
+            return T3D_E_INVAL;
+        }
+        if (xyuv) CKR(cudaMemcpy(xyuv + 12 * n, (char*)ctx->out_xyuv.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost));
+        if (rgba) CKR(cudaMemcpy(rgba + 12 * n, (char*)ctx->out_rgba.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost));
+        if (depth) CKR(cudaMemcpy(depth + 3 * n, (char*)ctx->out_depth.ptr + 12ull * si.base, 12ull * si.count, cudaMemcpyDeviceToHost));
+        n += si.count;
+    }
+    if (tris_out) *tris_out = n;
+    return T3D_OK;
+}
+
+int t3d_graph_capture(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam, int animate) {
+    if (!ctx || !cam) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    drop_graph(ctx);
+    t3d_job_desc job;
+    memset(&job, 0, sizeof job);
+    job.scene = scene;
+    job.light_mask[0] = job.light_mask[1] = ~0ull;
+    job.camera = *cam;
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    int rc = build_frame(ctx, &job, 1, animate);
+    if (rc) return rc;
+    if ((rc = upload_frame(ctx, ctx->stream))) return rc;
+    CKR(cudaStreamSynchronize(ctx->stream));
+    CKR(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = launch_frame(ctx, T3D_MODE_BATCHED, ctx->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) {
+        set_err(ctx, "graph capture: %s", cudaGetErrorString(e));
+        return T3D_E_CUDA;
+    }
+    ctx->graph = g;
+    e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+    if (e != cudaSuccess) {
+        set_err(ctx, "graph instantiate: %s", cudaGetErrorString(e));
+        drop_graph(ctx);
+        return T3D_E_CUDA;
+    }
+    ctx->frame_valid = false;
+    ctx->frame_pending = false;
+    return T3D_OK;
+}
+
+int t3d_graph_replay(t3d_ctx* ctx, uint32_t frames, void* stream) {
+    if (!ctx || !ctx->graph_exec) {
+        if (ctx) set_err(ctx, "graph_replay: no captured graph");
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    for (uint32_t f = 0; f < frames; f++) CKR(cudaGraphLaunch(ctx->graph_exec, st));
+    ctx->last_stream = st;
+    ctx->frame_pending = true;
+    return T3D_OK;
+}
+
+}  // extern "C"

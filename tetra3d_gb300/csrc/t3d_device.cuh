@@ -1,0 +1,188 @@
+// t3d_device.cuh -- layouts shared by the host runtime and the frame kernel.
+//
+// HBM layout of one resident scene (SoA vertex streams, 16-byte records so a
+// warp moves whole 128-bit words):
+//   va[v] = (px, py, pz, nx)   vb[v] = (ny, nz, u, v)   vc[v] = (r, g, b, a)
+//   idx[3t..3t+2]              mesh-absolute vertex indices per triangle
+// Per frame the host builds job / instance / segment / work-item tables; the
+// kernel writes per-vertex scratch (vcull, vxyuv, vrgba), per-tile visible
+// lists and the resident output stream.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/t3d.h"
+#include "t3d_math.cuh"
+
+namespace t3d {
+
+constexpr int kBins = 512;          // sortingTriangleBucket.Resize(512), sortingTriangles.go:166-168
+constexpr int kTileMax = 4096;      // largest triangle tile the kernel supports
+constexpr int kMaxLights = 128;     // per model light list
+constexpr int kMaxWarps = 16;       // block of at most 512 threads
+
+// segment flags
+enum : uint32_t {
+    SEG_SKIP = 1u << 0,         // ProcessVertices early-out (model.go:604-606)
+    SEG_LIT = 1u << 1,          // lighting on for this pair (camera.go:1521-1528)
+    SEG_BACKFACE = 1u << 2,     // Material.BackfaceCulling with a material
+    SEG_COLORS = 1u << 3,       // mesh has an active vertex colour channel
+    SEG_MAT = 1u << 4,          // MeshPart.Material != nil
+    SEG_MULTI = 1u << 5,        // segment spans more than one tile
+};
+__host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }
+__host__ __device__ inline uint32_t seg_light_mode(uint32_t f) { return (f >> 10) & 3u; }
+__host__ __device__ inline uint32_t seg_lv_mode(uint32_t f) { return (f >> 12) & 3u; }
+
+// model flags
+enum : int32_t { MOD_VISIBLE = 1, MOD_FRUSTUM = 2, MOD_SHADELESS = 4, MOD_TRS = 8 };
+
+struct DevMesh {
+    uint32_t vbase;      // first vertex in the scene pool
+    uint32_t tbase;      // first triangle in the scene pool
+    uint32_t nverts, ntris;
+    float dmin[3], dmax[3];  // Mesh.Dimensions
+};
+
+// Resident, animatable model state.
+struct DevModel {
+    float transform[16];
+    float world_rot[16];
+    float position[4];
+    float scale[4];
+    float rotation[16];
+    float rotate_step[16];
+    float color[4];
+    uint32_t mesh;
+    int32_t flags;
+    uint32_t pad[2];
+};
+
+// A light as one job sees it: beginRender results plus LightVolume geometry.
+struct DevLight {
+    int32_t type;
+    int32_t cnt[3];
+    float color[4];
+    float energy, range, range2, pad0;
+    float wpos[4];     // WorldPosition
+    float amb[4];      // AmbientLight.result (color * energy)
+    float fwd[4];      // DirectionalLight.workingForward
+    float vmin[4], vmax[4], cell[4], offset[4], bias[4];
+    uint32_t cell_first;
+    uint32_t pad1[3];
+};
+
+// Camera block per job (camera.go:638-679, :933-983, :1085-1088, :1337-1341).
+struct JobCam {
+    float vp[16];
+    float pos[4], fwd[4], rgt[4], up[4];
+    float sphere_tang, sphere_y, sphere_x, aspect;
+    float near_, far_, W, H;
+    float halfW, halfH, margin, spread;
+    float ortho_scale, pad0;
+    float fog_range[2];
+    float fog_color[4];
+    int32_t perspective, render_depth, persp_correct, fog_on;
+    int32_t fog_mode, pad1[3];
+};
+
+struct DevJob {
+    JobCam cam;
+    const float4* va;
+    const float4* vb;
+    const float4* vc;
+    const uint32_t* idx;
+    const DevMesh* meshes;
+    DevModel* models;
+    const float* cells;
+    const DevLight* lights;
+};
+
+// One (job, model) pair.
+struct DevInst {
+    uint32_t job, model;
+    uint32_t light_off, light_cnt;  // into inst_light_idx / inst_light_work
+    uint32_t animate;               // apply rotate_step in this launch
+    uint32_t pad;
+    uint64_t bytes;                 // algorithmic bytes if the model survives culling
+};
+
+// Phase-0 output per instance.
+struct DevPrep {
+    float mvp[16];
+    float M[16];
+    float dirrot[16];   // DirectionalLight.workingModelRotation (light.go:328)
+    float invcam[4];    // model-space camera position (model.go:630)
+    uint32_t culled;
+    uint32_t pad[3];
+};
+
+// One render pair (model, mesh part) of one job.
+struct DevSeg {
+    uint32_t inst, job, mesh, flags;
+    uint32_t tri_start, tri_count;   // mesh-absolute
+    uint32_t vmin, vcount;           // mesh-absolute vertex range the triangles use
+    uint32_t vscratch;               // first per-vertex scratch record
+    uint32_t out_base;               // first output triangle slot
+    uint32_t tile_first, ntiles;     // global tile numbers
+    uint32_t mt_first;               // first multi-tile tile number (SEG_MULTI)
+    uint32_t pad[3];
+    float mp[4];                     // Model.Color * Material.Color (camera.go:1597-1601)
+    float tex_w, tex_h, pad2[2];
+};
+
+// Launch control block (zeroed before every launch).
+struct Ctl {
+    uint32_t bar_count;
+    uint32_t bar_gen;
+    uint32_t queue[8];
+    int32_t err;
+    uint32_t err_info;
+    unsigned long long bytes;       // algorithmic bytes of surviving models
+    uint32_t culled;
+    uint32_t pad[3];
+};
+
+enum : int32_t { ERR_NONE = 0, ERR_BARRIER_TIMEOUT = 1, ERR_BAD_INDEX = 2, ERR_LIGHTS = 3 };
+
+struct FrameParams {
+    const DevJob* jobs;
+    const DevInst* insts;
+    DevPrep* preps;
+    const uint32_t* inst_light_idx;
+    float4* inst_light_work;      // (wx, wy, wz, skip) per instance light slot
+    const DevSeg* segs;
+    const uint32_t* vitem_seg;    // vertex work item -> segment
+    const uint32_t* vitem_chunk;  // vertex work item -> chunk within the segment
+    const uint32_t* tile_seg;     // tile -> segment
+    const uint32_t* mt_tiles;     // multi-tile tiles (global tile numbers)
+    const uint32_t* mt_segs;      // multi-tile segments
+    // scratch
+    float4* vcull;                // (cx, cy, clipZ, depth01)
+    float4* vxyuv;
+    float4* vrgba;
+    uint32_t* vis_idx;            // per multi-tile tile: kTile visible entries
+    float* vis_depth;
+    uint32_t* tile_count;         // visible per multi-tile tile
+    uint32_t* tile_hist;          // per multi-tile tile: kBins counters, then bases
+    uint32_t* seg_minmax;         // 2 per segment: min bits, max bits
+    uint32_t* seg_count;          // visible per segment (output)
+    // output stream
+    float4* out_xyuv;
+    float4* out_rgba;
+    float* out_depth;
+    Ctl* ctl;
+    // ranges processed by this launch
+    uint32_t inst_begin, inst_end;
+    uint32_t seg_begin, seg_end;
+    uint32_t vitem_begin, vitem_end;
+    uint32_t tile_begin, tile_end;
+    uint32_t mt_tile_begin, mt_tile_end;
+    uint32_t mt_seg_begin, mt_seg_end;
+    uint32_t tile_tris;           // triangles per tile
+    uint32_t vchunk;              // vertices per vertex work item
+    uint32_t has_multi;           // any multi-tile segment in range
+    uint32_t pad;
+};
+
+}  // namespace t3d

@@ -1,0 +1,701 @@
+// t3d_runtime.cu -- host side of the C ABI declared in include/t3d.h.
+//
+// Owns resident scenes in HBM, builds the per-frame job / instance / segment /
+// work-item tables (the part of Camera.Render that decides what to draw and in
+// which order, camera.go:1269-1503 and :2050-2109), launches the persistent
+// frame kernel (one launch for all models, or one launch per render pair) and
+// reads back the per-segment visible counts.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "t3d_device.cuh"
+#include "t3d_runtime.h"
+
+extern "C" const void* t3d_frame_kernel_ptr();
+extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris);
+
+namespace t3d {
+
+// ------------------------------------------------------------ utilities ----
+void set_err(t3d_ctx* c, const char* fmt, ...) {
+    if (!c) return;
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+}
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            set_err(ctx, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? T3D_E_OOM : T3D_E_CUDA;            \
+        }                                                                               \
+    } while (0)
+
+int DevBuf::ensure(t3d_ctx* ctx, size_t bytes) {
+    if (bytes <= cap) return T3D_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, (size_t)256);
+    want = want + want / 4;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        set_err(ctx, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+        return T3D_E_OOM;
+    }
+    cap = want;
+    return T3D_OK;
+}
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+int HostBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return T3D_OK;
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, (size_t)256);
+    want = want + want / 4;
+    if (cudaMallocHost(&ptr, want) != cudaSuccess) {
+        ptr = nullptr;
+        return T3D_E_OOM;
+    }
+    cap = want;
+    return T3D_OK;
+}
+void HostBuf::release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+static bool light_enabled(const uint64_t* mask, uint32_t i) {
+    if (i >= 128) return false;
+    return (mask[i >> 6] >> (i & 63)) & 1ull;
+}
+
+// Model.isTransparent (model.go:1274-1282)
+static bool is_transparent(const float* model_color, const t3d_material& mat) {
+    if (mat.present) {
+        bool matT = mat.transparency_mode == T3D_TRANSPARENCY_TRANSPARENT || !mat.blend_source_over ||
+                    (mat.transparency_mode == T3D_TRANSPARENCY_AUTO && mat.color[3] < 0.999f);
+        bool modelT = mat.transparency_mode != T3D_TRANSPARENCY_OPAQUE && model_color[3] < 0.999f;
+        return matT || modelT;
+    }
+    return model_color[3] < 0.999f;
+}
+
+// Camera.ViewMatrix, Projection, sphere factors, Clear basis and the depth
+// margin (camera.go:638-679, :1085-1088, :1337-1341; matrix.go:588-616).
+void build_camera(const t3d_camera_desc& d, JobCam& c) {
+    memset(&c, 0, sizeof c);
+    m4 ct = load16(d.transform), cr = load16(d.world_rotation);
+    f3 pos = row3(ct, 3);
+    m4 view = mult(translate(-pos.x, -pos.y, -pos.z), transposed(cr));
+    float fov = d.fov_y, nr = d.near_plane, fr = d.far_plane;
+    float W = (float)d.width, H = (float)d.height;
+    float aspect = W / H;
+    float angle = fov * 3.1415f / 360.0f;
+    c.sphere_tang = (float)std::tan((double)angle);
+    c.sphere_y = 1.0f / (float)std::cos((double)angle);
+    c.sphere_x = 1.0f / (float)std::cos((double)(float)std::atan((double)(c.sphere_tang * aspect)));
+    c.aspect = aspect;
+    m4 proj = ident();
+    if (d.perspective) {
+        float t = (float)std::tan((double)(fov * (float)M_PI / 360.0f));
+        float b = -t, r = t * aspect, l = -r;
+        proj.m[0][0] = (2.0f * nr) / (r - l); proj.m[0][1] = 0; proj.m[0][2] = (r + l) / (r - l); proj.m[0][3] = 0;
+        proj.m[1][0] = 0; proj.m[1][1] = (2.0f * nr) / (t - b); proj.m[1][2] = (t + b) / (t - b); proj.m[1][3] = 0;
+        proj.m[2][0] = 0; proj.m[2][1] = 0; proj.m[2][2] = -((fr + nr) / (fr - nr)); proj.m[2][3] = -((2.0f * fr * nr) / (fr - nr));
+        proj.m[3][0] = 0; proj.m[3][1] = 0; proj.m[3][2] = -1; proj.m[3][3] = 0;
+    } else {
+        float asr = H / W;
+        float os = d.ortho_scale;
+        float right = 1.0f * os, left = -1.0f * os, top = asr * os, bottom = -asr * os;
+        proj.m[0][0] = 2.0f / (right - left);
+        proj.m[1][1] = 2.0f / (top - bottom);
+        proj.m[2][2] = -2.0f / (fr - nr);
+        proj.m[3][3] = 1.0f;
+    }
+    store16(mult(view, proj), c.vp);
+    f3 fw = unit3(row3(cr, 2)), rg = unit3(row3(cr, 0)), upv = unit3(row3(cr, 1));
+    c.pos[0] = pos.x; c.pos[1] = pos.y; c.pos[2] = pos.z;
+    c.fwd[0] = fw.x; c.fwd[1] = fw.y; c.fwd[2] = fw.z;
+    c.rgt[0] = rg.x; c.rgt[1] = rg.y; c.rgt[2] = rg.z;
+    c.up[0] = upv.x; c.up[1] = upv.y; c.up[2] = upv.z;
+    c.near_ = nr; c.far_ = fr; c.W = W; c.H = H;
+    c.halfW = W / 2.0f; c.halfH = H / 2.0f;
+    c.margin = (fr - nr) * d.depth_margin;
+    c.spread = fr - nr + (c.margin * 2.0f);
+    c.ortho_scale = d.ortho_scale;
+    c.fog_range[0] = d.fog_range[0]; c.fog_range[1] = d.fog_range[1];
+    for (int i = 0; i < 4; i++) c.fog_color[i] = d.fog_color[i];
+    c.perspective = d.perspective; c.render_depth = d.render_depth; c.persp_correct = d.perspective_corrected;
+    c.fog_on = d.fog_on; c.fog_mode = d.fog_mode;
+}
+
+// beginRender (light.go:110-113, :318-320): per frame, per light.
+static void build_light(const t3d_light_desc& d, DevLight& L) {
+    memset(&L, 0, sizeof L);
+    L.type = d.type;
+    for (int i = 0; i < 3; i++) {
+        L.cnt[i] = d.cell_count[i];
+        L.color[i] = d.color[i];
+        L.vmin[i] = d.vol_min[i]; L.vmax[i] = d.vol_max[i]; L.cell[i] = d.cell_size[i];
+        L.offset[i] = d.offset[i]; L.bias[i] = d.bias[i];
+    }
+    L.color[3] = d.color[3];
+    L.energy = d.energy;
+    L.range = d.range;
+    L.range2 = d.range * d.range;
+    m4 t = load16(d.transform);
+    f3 wp = row3(t, 3);
+    L.wpos[0] = wp.x; L.wpos[1] = wp.y; L.wpos[2] = wp.z;
+    L.amb[0] = d.color[0] * d.energy; L.amb[1] = d.color[1] * d.energy; L.amb[2] = d.color[2] * d.energy;
+    f3 fw = unit3(row3(load16(d.world_rotation), 2));
+    L.fwd[0] = fw.x; L.fwd[1] = fw.y; L.fwd[2] = fw.z;
+    L.cell_first = d.cell_first;
+}
+
+// Host mirror of a model's world transform (for draw-order distances).
+static m4 host_transform(const SceneModel& m) {
+    if (m.d.use_trs)
+        return trs(mk3(m.d.position[0], m.d.position[1], m.d.position[2]),
+                   mk3(m.d.scale[0], m.d.scale[1], m.d.scale[2]), load16(m.d.rotation));
+    return load16(m.d.transform);
+}
+
+// ------------------------------------------------------------ scenes ----
+int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
+    if (!d || !out || (d->num_meshes && !d->meshes) || (d->num_models && !d->models) ||
+        (d->num_lights && !d->lights) || (d->num_volume_cells && !d->volume_cells)) {
+        set_err(ctx, "scene_upload: null array");
+        return T3D_E_INVAL;
+    }
+    if (d->num_lists == 0 || !d->list_offsets || (d->list_offsets[d->num_lists] && !d->list_items)) {
+        set_err(ctx, "scene_upload: light list 0 (the scene list) is required");
+        return T3D_E_INVAL;
+    }
+    auto sc = std::make_unique<Scene>();
+    uint64_t nv = 0, nt = 0;
+    for (uint32_t m = 0; m < d->num_meshes; m++) {
+        const t3d_mesh_desc& me = d->meshes[m];
+        if (!me.positions || !me.normals || !me.uvs || !me.indices || (me.num_parts && !me.parts)) {
+            set_err(ctx, "mesh %u: null stream", m);
+            return T3D_E_INVAL;
+        }
+        SceneMesh sm;
+        sm.vbase = (uint32_t)nv;
+        sm.tbase = (uint32_t)nt;
+        sm.nverts = me.num_vertices;
+        sm.ntris = me.num_triangles;
+        sm.colors = me.colors != nullptr;
+        for (uint32_t t = 0; t < 3ull * me.num_triangles; t++)
+            if (me.indices[t] >= me.num_vertices) {
+                set_err(ctx, "mesh %u: index %u out of range (%u vertices)", m, me.indices[t], me.num_vertices);
+                return T3D_E_INVAL;
+            }
+        // Mesh.Dimensions (UpdateDimensions, mesh.go:713-748)
+        if (me.has_dimensions) {
+            for (int c = 0; c < 3; c++) { sm.dmin[c] = me.dim_min[c]; sm.dmax[c] = me.dim_max[c]; }
+        } else {
+            for (int c = 0; c < 3; c++) { sm.dmin[c] = 3.402823466e38f; sm.dmax[c] = -3.402823466e38f; }
+            for (uint32_t v = 0; v < me.num_vertices; v++)
+                for (int c = 0; c < 3; c++) {
+                    float p = me.positions[3 * (size_t)v + c];
+                    if (sm.dmin[c] > p) sm.dmin[c] = p;
+                    if (sm.dmax[c] < p) sm.dmax[c] = p;
+                }
+        }
+        for (uint32_t p = 0; p < me.num_parts; p++) {
+            const t3d_part_desc& pd = me.parts[p];
+            if ((uint64_t)pd.tri_start + pd.tri_count > me.num_triangles) {
+                set_err(ctx, "mesh %u part %u: triangle range out of bounds", m, p);
+                return T3D_E_INVAL;
+            }
+            const t3d_material& mt = pd.mat;
+            if (mt.present && (mt.sort_mode < 0 || mt.sort_mode > 2 || mt.lighting_mode < 0 || mt.lighting_mode > 2 ||
+                               mt.lv_shading_mode < 0 || mt.lv_shading_mode > 3)) {
+                set_err(ctx, "mesh %u part %u: bad material enum", m, p);
+                return T3D_E_INVAL;
+            }
+            ScenePart sp;
+            sp.d = pd;
+            uint32_t vmin = 0xFFFFFFFFu, vmax = 0;
+            for (uint64_t t = pd.tri_start; t < (uint64_t)pd.tri_start + pd.tri_count; t++)
+                for (int c = 0; c < 3; c++) {
+                    uint32_t v = me.indices[3 * t + c];
+                    vmin = std::min(vmin, v);
+                    vmax = std::max(vmax, v);
+                }
+            sp.vmin = pd.tri_count ? vmin : 0;
+            sp.vcount = pd.tri_count ? vmax - vmin + 1 : 0;
+            sm.parts.push_back(sp);
+        }
+        nv += me.num_vertices;
+        nt += me.num_triangles;
+        if (nv > 0xFFFFFFF0ull || nt > 0x50000000ull) {
+            set_err(ctx, "scene too large for 32-bit vertex/triangle indexing");
+            return T3D_E_INVAL;
+        }
+        sc->meshes.push_back(std::move(sm));
+    }
+    for (uint32_t i = 0; i < d->num_models; i++) {
+        const t3d_model_desc& md = d->models[i];
+        if (md.mesh >= d->num_meshes) {
+            set_err(ctx, "model %u: mesh %u out of range", i, md.mesh);
+            return T3D_E_INVAL;
+        }
+        if (md.light_list >= (int32_t)d->num_lists) {
+            set_err(ctx, "model %u: light list %d out of range", i, md.light_list);
+            return T3D_E_INVAL;
+        }
+        SceneModel sm;
+        sm.d = md;
+        sc->models.push_back(sm);
+    }
+    for (uint32_t i = 0; i < d->num_lights; i++) {
+        const t3d_light_desc& l = d->lights[i];
+        if (l.type < 0 || l.type > 3) {
+            set_err(ctx, "light %u: bad type %d", i, l.type);
+            return T3D_E_INVAL;
+        }
+        if (l.type == T3D_LIGHT_VOLUME) {
+            uint64_t cells = (uint64_t)std::max(0, l.cell_count[0]) * std::max(0, l.cell_count[1]) * std::max(0, l.cell_count[2]);
+            if ((uint64_t)l.cell_first + cells > d->num_volume_cells) {
+                set_err(ctx, "light %u: volume cells out of range", i);
+                return T3D_E_INVAL;
+            }
+        }
+        sc->lights.push_back(l);
+    }
+    sc->lists.resize(d->num_lists);
+    for (uint32_t L = 0; L < d->num_lists; L++) {
+        for (uint32_t q = d->list_offsets[L]; q < d->list_offsets[L + 1]; q++) {
+            if (d->list_items[q] >= d->num_lights) {
+                set_err(ctx, "light list %u: light %u out of range", L, d->list_items[q]);
+                return T3D_E_INVAL;
+            }
+            sc->lists[L].push_back(d->list_items[q]);
+        }
+    }
+    sc->nverts = nv;
+    sc->ntris = nt;
+    // device pools
+    int rc;
+    if ((rc = sc->va.ensure(ctx, nv * 16)) || (rc = sc->vb.ensure(ctx, nv * 16)) || (rc = sc->vc.ensure(ctx, nv * 16)) ||
+        (rc = sc->idx.ensure(ctx, nt * 12)) || (rc = sc->dmeshes.ensure(ctx, sizeof(DevMesh) * std::max<size_t>(1, d->num_meshes))) ||
+        (rc = sc->dmodels.ensure(ctx, sizeof(DevModel) * std::max<size_t>(1, d->num_models))) ||
+        (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))))
+        return rc;
+    std::vector<float4> a, b, c;
+    std::vector<uint32_t> ix;
+    for (uint32_t m = 0; m < d->num_meshes; m++) {
+        const t3d_mesh_desc& me = d->meshes[m];
+        a.resize(me.num_vertices); b.resize(me.num_vertices); c.resize(me.num_vertices);
+        for (uint32_t v = 0; v < me.num_vertices; v++) {
+            const float* p = me.positions + 3 * (size_t)v;
+            const float* n = me.normals + 3 * (size_t)v;
+            const float* u = me.uvs + 2 * (size_t)v;
+            a[v] = make_float4(p[0], p[1], p[2], n[0]);
+            b[v] = make_float4(n[1], n[2], u[0], u[1]);
+            if (me.colors) {
+                const float* k = me.colors + 4 * (size_t)v;
+                c[v] = make_float4(k[0], k[1], k[2], k[3]);
+            } else {
+                c[v] = make_float4(1.f, 1.f, 1.f, 1.f);
+            }
+        }
+        size_t off = (size_t)sc->meshes[m].vbase * 16;
+        CK(cudaMemcpy((char*)sc->va.ptr + off, a.data(), me.num_vertices * 16ull, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((char*)sc->vb.ptr + off, b.data(), me.num_vertices * 16ull, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((char*)sc->vc.ptr + off, c.data(), me.num_vertices * 16ull, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((char*)sc->idx.ptr + (size_t)sc->meshes[m].tbase * 12, me.indices, me.num_triangles * 12ull,
+                      cudaMemcpyHostToDevice));
+    }
+    std::vector<DevMesh> dm(d->num_meshes);
+    for (uint32_t m = 0; m < d->num_meshes; m++) {
+        const SceneMesh& sm = sc->meshes[m];
+        dm[m].vbase = sm.vbase; dm[m].tbase = sm.tbase; dm[m].nverts = sm.nverts; dm[m].ntris = sm.ntris;
+        for (int k = 0; k < 3; k++) { dm[m].dmin[k] = sm.dmin[k]; dm[m].dmax[k] = sm.dmax[k]; }
+    }
+    if (d->num_meshes) CK(cudaMemcpy(sc->dmeshes.ptr, dm.data(), sizeof(DevMesh) * dm.size(), cudaMemcpyHostToDevice));
+    if (d->num_volume_cells)
+        CK(cudaMemcpy(sc->cells.ptr, d->volume_cells, 16ull * d->num_volume_cells, cudaMemcpyHostToDevice));
+    rc = scene_write_models(ctx, sc.get(), 0, d->models, d->num_models);
+    if (rc) return rc;
+    CK(cudaDeviceSynchronize());
+    uint32_t id = ctx->next_scene++;
+    *out = id;
+    ctx->scenes[id] = std::move(sc);
+    return T3D_OK;
+}
+
+int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n) {
+    if (n == 0) return T3D_OK;
+    std::vector<DevModel> dv(n);
+    for (uint32_t i = 0; i < n; i++) {
+        const t3d_model_desc& md = models[i];
+        DevModel& m = dv[i];
+        memset(&m, 0, sizeof m);
+        memcpy(m.transform, md.transform, 64);
+        memcpy(m.world_rot, md.world_rotation, 64);
+        memcpy(m.position, md.position, 12);
+        memcpy(m.scale, md.scale, 12);
+        memcpy(m.rotation, md.rotation, 64);
+        memcpy(m.rotate_step, md.rotate_step, 64);
+        memcpy(m.color, md.color, 16);
+        m.mesh = md.mesh;
+        m.flags = (md.visible ? MOD_VISIBLE : 0) | (md.frustum_culling ? MOD_FRUSTUM : 0) | (md.shadeless ? MOD_SHADELESS : 0) |
+                  (md.use_trs ? MOD_TRS : 0);
+        sc->models[first + i].d = md;
+    }
+    CK(cudaMemcpy((char*)sc->dmodels.ptr + sizeof(DevModel) * first, dv.data(), sizeof(DevModel) * n, cudaMemcpyHostToDevice));
+    return T3D_OK;
+}
+
+// ------------------------------------------------------------ frames ----
+// Builds the tables of one frame. Instances and segments are laid out per job.
+int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate) {
+    FrameTables& F = ctx->tables;
+    F.clear();
+    const uint32_t T = ctx->tile_tris, VC = ctx->vchunk;
+    for (uint32_t j = 0; j < njobs; j++) {
+        auto it = ctx->scene_map().find(jobs[j].scene);
+        if (it == ctx->scene_map().end()) {
+            set_err(ctx, "job %u: unknown scene %u", j, jobs[j].scene);
+            return T3D_E_NOTFOUND;
+        }
+        if (jobs[j].camera.width <= 0 || jobs[j].camera.height <= 0) {
+            set_err(ctx, "job %u: bad camera size", j);
+            return T3D_E_INVAL;
+        }
+        Scene* sc = it->second.get();
+        DevJob dj;
+        memset(&dj, 0, sizeof dj);
+        build_camera(jobs[j].camera, dj.cam);
+        dj.va = (const float4*)sc->va.ptr;
+        dj.vb = (const float4*)sc->vb.ptr;
+        dj.vc = (const float4*)sc->vc.ptr;
+        dj.idx = (const uint32_t*)sc->idx.ptr;
+        dj.meshes = (const DevMesh*)sc->dmeshes.ptr;
+        dj.models = (DevModel*)sc->dmodels.ptr;
+        dj.cells = (const float*)sc->cells.ptr;
+        const uint32_t light_base = (uint32_t)F.lights.size();
+        for (const auto& l : sc->lights) {
+            DevLight L;
+            build_light(l, L);
+            F.lights.push_back(L);
+        }
+        F.job_light_base.push_back(light_base);
+        F.jobs.push_back(dj);
+        F.job_scene.push_back(sc);
+
+        const t3d_camera_desc& cd = jobs[j].camera;
+        f3 campos = row3(load16(cd.transform), 3);
+        struct Pair { uint32_t model, part; float depth; int32_t order; };
+        std::vector<Pair> solids, transparents;
+        std::vector<uint32_t> inst_of(sc->models.size(), 0xFFFFFFFFu);
+        for (uint32_t mi = 0; mi < sc->models.size(); mi++) {
+            SceneModel& m = sc->models[mi];
+            if (!m.d.visible) continue;
+            // instance
+            DevInst in;
+            memset(&in, 0, sizeof in);
+            in.job = j;
+            in.model = mi;
+            in.animate = animate ? 1u : 0u;
+            in.light_off = (uint32_t)F.inst_light_idx.size();
+            uint32_t list = m.d.light_list < 0 ? 0u : (uint32_t)m.d.light_list;
+            uint32_t cnt = 0;
+            for (uint32_t li : sc->lists[list]) {
+                if (!light_enabled(jobs[j].light_mask, li)) continue;
+                F.inst_light_idx.push_back(light_base + li);
+                cnt++;
+            }
+            if (cnt > (uint32_t)kMaxLights) {
+                set_err(ctx, "model %u: %u lights exceed the per-model maximum %d", mi, cnt, kMaxLights);
+                return T3D_E_INVAL;
+            }
+            in.light_cnt = cnt;
+            const SceneMesh& me = sc->meshes[m.d.mesh];
+            in.bytes = (uint64_t)(me.colors ? 48 : 32) * me.nverts + 12ull * me.ntris + 64 + 48ull * cnt;
+            inst_of[mi] = (uint32_t)F.insts.size();
+            F.insts.push_back(in);
+            if (animate && m.d.use_trs) {  // host mirror of the device animation step
+                m4 rot = mult(load16(m.d.rotate_step), load16(m.d.rotation));
+                store16(rot, m.d.rotation);
+            }
+            m4 M = host_transform(m);
+            float depth = dist2(campos, row3(M, 3));  // camera.go:1381
+            for (uint32_t p = 0; p < me.parts.size(); p++) {
+                const t3d_material& mat = me.parts[p].d.mat;
+                if (mat.present && !mat.visible) continue;
+                Pair rp{mi, p, depth, mat.present ? mat.render_order : 0};
+                if (is_transparent(m.d.color, mat)) transparents.push_back(rp);
+                else solids.push_back(rp);
+            }
+        }
+        auto by_order_then_far = [](const Pair& a, const Pair& b) {
+            return a.order != b.order ? a.order < b.order : a.depth > b.depth;
+        };
+        if (!cd.render_depth) std::stable_sort(solids.begin(), solids.end(), by_order_then_far);
+        std::stable_sort(transparents.begin(), transparents.end(), by_order_then_far);
+        solids.insert(solids.end(), transparents.begin(), transparents.end());
+        for (const Pair& rp : solids) {
+            const SceneModel& m = sc->models[rp.model];
+            const SceneMesh& me = sc->meshes[m.d.mesh];
+            const ScenePart& part = me.parts[rp.part];
+            const t3d_material& mat = part.d.mat;
+            DevSeg sg;
+            memset(&sg, 0, sizeof sg);
+            sg.inst = inst_of[rp.model];
+            sg.job = j;
+            sg.mesh = m.d.mesh;
+            sg.tri_start = part.d.tri_start;
+            sg.tri_count = part.d.tri_count;
+            sg.vmin = part.vmin;
+            sg.vcount = part.vcount;
+            uint32_t flags = 0;
+            if ((m.d.color[3] == 0 && is_transparent(m.d.color, mat)) || part.d.tri_count == 0) flags |= SEG_SKIP;
+            bool lit = cd.lighting_on && !(mat.present && mat.shadeless) && !m.d.shadeless;
+            if (lit) flags |= SEG_LIT;
+            if (mat.present && mat.backface_culling) flags |= SEG_BACKFACE;
+            if (me.colors) flags |= SEG_COLORS;
+            if (mat.present) flags |= SEG_MAT;
+            uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
+            flags |= sort_mode << 8;
+            flags |= (uint32_t)(mat.present ? mat.lighting_mode : 0) << 10;
+            flags |= (uint32_t)(mat.present ? mat.lv_shading_mode : 0) << 12;
+            sg.mp[0] = m.d.color[0]; sg.mp[1] = m.d.color[1]; sg.mp[2] = m.d.color[2]; sg.mp[3] = m.d.color[3];
+            if (mat.present) {
+                sg.mp[0] *= mat.color[0]; sg.mp[1] *= mat.color[1]; sg.mp[2] *= mat.color[2]; sg.mp[3] *= mat.color[3];
+                sg.tex_w = mat.tex_w; sg.tex_h = mat.tex_h;
+            }
+            sg.vscratch = (uint32_t)F.nscratch;
+            F.nscratch += sg.vcount;
+            sg.out_base = (uint32_t)F.nslots;
+            F.nslots += sg.tri_count;
+            uint32_t ntiles = (sg.tri_count + T - 1) / T;
+            if (ntiles == 0) ntiles = 1;
+            sg.tile_first = (uint32_t)F.tile_seg.size();
+            sg.ntiles = ntiles;
+            const uint32_t s = (uint32_t)F.segs.size();
+            if (ntiles > 1) {
+                flags |= SEG_MULTI;
+                sg.mt_first = (uint32_t)F.mt_tiles.size();
+                for (uint32_t t = 0; t < ntiles; t++) F.mt_tiles.push_back(sg.tile_first + t);
+                F.mt_segs.push_back(s);
+            }
+            for (uint32_t t = 0; t < ntiles; t++) F.tile_seg.push_back(s);
+            uint32_t nch = (sg.vcount + VC - 1) / VC;
+            F.seg_vitem_first.push_back((uint32_t)F.vitem_seg.size());
+            for (uint32_t c = 0; c < nch; c++) { F.vitem_seg.push_back(s); F.vitem_chunk.push_back(c); }
+            sg.flags = flags;
+            F.segs.push_back(sg);
+            t3d_segment_info si;
+            si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
+            F.seg_info.push_back(si);
+            F.seg_mt_seg.push_back(ntiles > 1 ? (uint32_t)F.mt_segs.size() - 1 : 0xFFFFFFFFu);
+        }
+        F.job_seg_end.push_back((uint32_t)F.segs.size());
+    }
+    if (F.nslots > 0xFFFFFFF0ull || F.nscratch > 0xFFFFFFF0ull) {
+        set_err(ctx, "frame too large for 32-bit slots");
+        return T3D_E_INVAL;
+    }
+    // point the jobs at their light tables (device address known after upload)
+    return T3D_OK;
+}
+
+template <typename T> static size_t bytes_of(const std::vector<T>& v) { return v.size() * sizeof(T); }
+
+// Uploads the tables into one device arena and the scratch buffers.
+int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
+    FrameTables& F = ctx->tables;
+    struct Piece { const void* src; size_t bytes; size_t off; };
+    std::vector<Piece> pieces;
+    size_t off = 0;
+    auto add = [&](const void* p, size_t b) {
+        size_t o = (off + 255) & ~(size_t)255;
+        pieces.push_back({p, b, o});
+        off = o + b;
+        return o;
+    };
+    size_t o_lights = add(F.lights.data(), bytes_of(F.lights));
+    // jobs reference the light table: patch after we know the arena base
+    size_t o_jobs = add(F.jobs.data(), bytes_of(F.jobs));
+    size_t o_insts = add(F.insts.data(), bytes_of(F.insts));
+    size_t o_ili = add(F.inst_light_idx.data(), bytes_of(F.inst_light_idx));
+    size_t o_segs = add(F.segs.data(), bytes_of(F.segs));
+    size_t o_vis = add(F.vitem_seg.data(), bytes_of(F.vitem_seg));
+    size_t o_vic = add(F.vitem_chunk.data(), bytes_of(F.vitem_chunk));
+    size_t o_ts = add(F.tile_seg.data(), bytes_of(F.tile_seg));
+    size_t o_mtt = add(F.mt_tiles.data(), bytes_of(F.mt_tiles));
+    size_t o_mts = add(F.mt_segs.data(), bytes_of(F.mt_segs));
+    std::vector<DevInst> noanim(F.insts);
+    for (auto& in : noanim) in.animate = 0;
+    size_t o_noanim = add(noanim.data(), bytes_of(noanim));
+    int rc;
+    if ((rc = ctx->table_host.ensure(off + 256))) { set_err(ctx, "pinned table alloc failed"); return rc; }
+    if ((rc = ctx->table_dev.ensure(ctx, off + 256))) return rc;
+    char* hb = (char*)ctx->table_host.ptr;
+    char* db = (char*)ctx->table_dev.ptr;
+    for (auto& p : pieces)
+        if (p.bytes) memcpy(hb + p.off, p.src, p.bytes);
+    DevJob* hj = (DevJob*)(hb + o_jobs);
+    for (size_t j = 0; j < F.jobs.size(); j++) hj[j].lights = (const DevLight*)(db + o_lights) + F.job_light_base[j];
+    if (off) {
+        cudaError_t e = cudaMemcpyAsync(db, hb, off, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) { set_err(ctx, "table upload: %s", cudaGetErrorString(e)); return T3D_E_CUDA; }
+    }
+    FrameParams& P = ctx->params;
+    memset(&P, 0, sizeof P);
+    P.jobs = (const DevJob*)(db + o_jobs);
+    P.insts = (const DevInst*)(db + o_insts);
+    P.inst_light_idx = (const uint32_t*)(db + o_ili);
+    P.segs = (const DevSeg*)(db + o_segs);
+    P.vitem_seg = (const uint32_t*)(db + o_vis);
+    P.vitem_chunk = (const uint32_t*)(db + o_vic);
+    P.tile_seg = (const uint32_t*)(db + o_ts);
+    P.mt_tiles = (const uint32_t*)(db + o_mtt);
+    P.mt_segs = (const uint32_t*)(db + o_mts);
+    ctx->insts_noanim = (const DevInst*)(db + o_noanim);
+    // scratch
+    const size_t ninst = std::max<size_t>(1, F.insts.size()), nseg = std::max<size_t>(1, F.segs.size());
+    const size_t nmt = std::max<size_t>(1, F.mt_tiles.size()), nsc = std::max<uint64_t>(1, F.nscratch);
+    const size_t nslots = std::max<uint64_t>(1, F.nslots);
+    if ((rc = ctx->preps.ensure(ctx, sizeof(DevPrep) * ninst)) ||
+        (rc = ctx->light_work.ensure(ctx, 16 * std::max<size_t>(1, F.inst_light_idx.size()))) ||
+        (rc = ctx->vcull.ensure(ctx, 16 * nsc)) || (rc = ctx->vxyuv.ensure(ctx, 16 * nsc)) ||
+        (rc = ctx->vrgba.ensure(ctx, 16 * nsc)) || (rc = ctx->vis_idx.ensure(ctx, 4ull * nmt * ctx->tile_tris)) ||
+        (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) || (rc = ctx->tile_count.ensure(ctx, 4 * nmt)) ||
+        (rc = ctx->tile_hist.ensure(ctx, 4ull * kBins * nmt)) || (rc = ctx->seg_minmax.ensure(ctx, 8 * nseg)) ||
+        (rc = ctx->seg_count.ensure(ctx, 4 * nseg)) || (rc = ctx->out_xyuv.ensure(ctx, 48 * nslots)) ||
+        (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
+        return rc;
+    P.preps = (DevPrep*)ctx->preps.ptr;
+    P.inst_light_work = (float4*)ctx->light_work.ptr;
+    P.vcull = (float4*)ctx->vcull.ptr;
+    P.vxyuv = (float4*)ctx->vxyuv.ptr;
+    P.vrgba = (float4*)ctx->vrgba.ptr;
+    P.vis_idx = (uint32_t*)ctx->vis_idx.ptr;
+    P.vis_depth = (float*)ctx->vis_depth.ptr;
+    P.tile_count = (uint32_t*)ctx->tile_count.ptr;
+    P.tile_hist = (uint32_t*)ctx->tile_hist.ptr;
+    P.seg_minmax = (uint32_t*)ctx->seg_minmax.ptr;
+    P.seg_count = (uint32_t*)ctx->seg_count.ptr;
+    P.out_xyuv = (float4*)ctx->out_xyuv.ptr;
+    P.out_rgba = (float4*)ctx->out_rgba.ptr;
+    P.out_depth = (float*)ctx->out_depth.ptr;
+    P.tile_tris = ctx->tile_tris;
+    P.vchunk = ctx->vchunk;
+    return T3D_OK;
+}
+
+static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items, cudaStream_t st) {
+    P.ctl = ctl;
+    uint32_t grid = std::max(1u, std::min(ctx->max_grid, max_items));
+    const void* fn = t3d_frame_kernel_ptr();
+    void* args[] = {&P};
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(ctx->block_threads);
+    cfg.dynamicSmemBytes = ctx->smem_bytes;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
+    if (e != cudaSuccess) {
+        set_err(ctx, "frame kernel launch failed: %s (grid %u, block %u, smem %zu)", cudaGetErrorString(e), grid,
+                ctx->block_threads, ctx->smem_bytes);
+        return T3D_E_CUDA;
+    }
+    ctx->launches++;
+    return T3D_OK;
+}
+
+int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
+    FrameTables& F = ctx->tables;
+    const FrameParams& P0 = ctx->params;
+    ctx->launches = 0;
+    const size_t nlaunch = (mode == T3D_MODE_BATCHED) ? 1 : std::max<size_t>(1, F.segs.size());
+    int rc;
+    if ((rc = ctx->ctl.ensure(ctx, sizeof(Ctl) * nlaunch))) return rc;
+    cudaError_t e = cudaMemsetAsync(ctx->ctl.ptr, 0, sizeof(Ctl) * nlaunch, st);
+    if (e != cudaSuccess) { set_err(ctx, "ctl memset: %s", cudaGetErrorString(e)); return T3D_E_CUDA; }
+    Ctl* ctl = (Ctl*)ctx->ctl.ptr;
+    ctx->nctl = (uint32_t)nlaunch;
+    if (F.segs.empty() && F.insts.empty()) return T3D_OK;
+    if (mode == T3D_MODE_BATCHED) {
+        FrameParams P = P0;
+        P.inst_begin = 0; P.inst_end = (uint32_t)F.insts.size();
+        P.seg_begin = 0; P.seg_end = (uint32_t)F.segs.size();
+        P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
+        P.tile_begin = 0; P.tile_end = (uint32_t)F.tile_seg.size();
+        P.mt_tile_begin = 0; P.mt_tile_end = (uint32_t)F.mt_tiles.size();
+        P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
+        P.has_multi = F.mt_segs.empty() ? 0u : 1u;
+        uint32_t items = (uint32_t)std::max({F.vitem_seg.size(), F.tile_seg.size(), F.mt_tiles.size(),
+                                             (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
+        return launch_one(ctx, P, ctl, items, st);
+    }
+    // Plain: one launch per render pair, in draw order (render + flush per pair,
+    // camera.go:2061-2106). A model's prep (and animation step) runs with its
+    // first pair; its later pairs recompute the same prep without animating.
+    std::vector<char> animated(F.insts.size(), 0);
+    for (size_t s = 0; s < F.segs.size(); s++) {
+        const DevSeg& sg = F.segs[s];
+        FrameParams P = P0;
+        P.inst_begin = sg.inst; P.inst_end = sg.inst + 1;
+        P.seg_begin = (uint32_t)s; P.seg_end = (uint32_t)s + 1;
+        P.vitem_begin = F.seg_vitem_first[s];
+        P.vitem_end = (s + 1 < F.segs.size()) ? F.seg_vitem_first[s + 1] : (uint32_t)F.vitem_seg.size();
+        P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
+        if (sg.flags & SEG_MULTI) {
+            P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles;
+            P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;
+            P.has_multi = 1;
+        } else {
+            P.mt_tile_begin = P.mt_tile_end = 0; P.mt_seg_begin = P.mt_seg_end = 0; P.has_multi = 0;
+        }
+        // animation must be applied once: host tables carry the flag on the instance,
+        // so later pairs of the same model use a copy without it.
+        if (F.insts[sg.inst].animate && animated[sg.inst]) {
+            // re-point the instance range to the no-animate shadow copy
+            P.insts = ctx->insts_noanim;
+        }
+        animated[sg.inst] = 1;
+        uint32_t items = std::max({P.vitem_end - P.vitem_begin, sg.ntiles, 1u});
+        if ((rc = launch_one(ctx, P, ctl + s, items, st))) return rc;
+    }
+    return T3D_OK;
+}
+
+}  // namespace t3d

@@ -1,0 +1,121 @@
+// t3d_runtime.h -- host-side state behind the C ABI (include/t3d.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "t3d_device.cuh"
+
+namespace t3d {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t cap = 0;
+    int ensure(t3d_ctx* ctx, size_t bytes);
+    void release();
+};
+// Grow-only pinned host buffer.
+struct HostBuf {
+    void* ptr = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+};
+
+struct ScenePart {
+    t3d_part_desc d;
+    uint32_t vmin = 0, vcount = 0;  // vertex range referenced by the part's triangles
+};
+struct SceneMesh {
+    uint32_t vbase = 0, tbase = 0, nverts = 0, ntris = 0;
+    bool colors = false;
+    float dmin[3], dmax[3];
+    std::vector<ScenePart> parts;
+};
+struct SceneModel {
+    t3d_model_desc d;  // host mirror (rotation advanced with every animated frame)
+};
+struct Scene {
+    std::vector<SceneMesh> meshes;
+    std::vector<SceneModel> models;
+    std::vector<t3d_light_desc> lights;
+    std::vector<std::vector<uint32_t>> lists;
+    uint64_t nverts = 0, ntris = 0;
+    DevBuf va, vb, vc, idx, dmeshes, dmodels, cells;
+    uint64_t device_bytes() const {
+        return va.cap + vb.cap + vc.cap + idx.cap + dmeshes.cap + dmodels.cap + cells.cap;
+    }
+    void release() {
+        va.release(); vb.release(); vc.release(); idx.release();
+        dmeshes.release(); dmodels.release(); cells.release();
+    }
+};
+
+// Tables of one frame (host side).
+struct FrameTables {
+    std::vector<DevJob> jobs;
+    std::vector<Scene*> job_scene;
+    std::vector<uint32_t> job_light_base, job_seg_end;
+    std::vector<DevLight> lights;
+    std::vector<DevInst> insts;
+    std::vector<uint32_t> inst_light_idx;
+    std::vector<DevSeg> segs;
+    std::vector<t3d_segment_info> seg_info;
+    std::vector<uint32_t> seg_vitem_first, seg_mt_seg;
+    std::vector<uint32_t> vitem_seg, vitem_chunk, tile_seg, mt_tiles, mt_segs;
+    uint64_t nscratch = 0, nslots = 0;
+    void clear() {
+        jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
+        insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear(); seg_vitem_first.clear();
+        seg_mt_seg.clear(); vitem_seg.clear(); vitem_chunk.clear(); tile_seg.clear(); mt_tiles.clear(); mt_segs.clear();
+        nscratch = 0; nslots = 0;
+    }
+};
+
+}  // namespace t3d
+
+struct t3d_ctx {
+    int device = 0;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    cudaStream_t last_stream = nullptr;
+    int num_sms = 0;
+    uint32_t tile_tris = 2048, vchunk = 1024, block_threads = 256;
+    uint32_t max_grid = 0;   // co-resident blocks for the current tuning
+    size_t smem_bytes = 0;
+    uint32_t next_scene = 1;
+    std::map<uint32_t, std::unique_ptr<t3d::Scene>> scenes;
+    t3d_ctx* scene_owner = nullptr;  // serving slots render the parent context's scenes
+    std::map<uint32_t, std::unique_ptr<t3d::Scene>>& scene_map() { return scene_owner ? scene_owner->scenes : scenes; }
+    t3d::FrameTables tables;
+    t3d::FrameParams params;
+    const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
+    t3d::HostBuf table_host, readback;
+    t3d::DevBuf table_dev, ctl, preps, light_work, vcull, vxyuv, vrgba, vis_idx, vis_depth, tile_count, tile_hist,
+        seg_minmax, seg_count, out_xyuv, out_rgba, out_depth;
+    uint32_t nctl = 0;
+    uint32_t launches = 0;
+    bool frame_pending = false;
+    bool frame_valid = false;
+    t3d_stats stats{};
+    // CUDA graph of one batched frame
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaEvent_t ev_done = nullptr;
+};
+
+namespace t3d {
+void set_err(t3d_ctx* c, const char* fmt, ...);
+void build_camera(const t3d_camera_desc& d, JobCam& c);
+int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out);
+int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n);
+int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate);
+int upload_frame(t3d_ctx* ctx, cudaStream_t st);
+int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st);
+int configure(t3d_ctx* ctx);
+}  // namespace t3d

@@ -1,0 +1,330 @@
+// t3d_serve.cu -- render-request serving with continuous batching.
+//
+// Requests (scene id + camera + light subset) queue in arrival order. A
+// scheduler thread owns `streams` launch slots; each slot is a private frame
+// context (its own stream, tables, scratch and output buffers) over the
+// parent context's resident scenes. Whenever a slot is free it admits queued
+// requests in FIFO order while the batch has room (max_batch) and the device
+// bytes of everything in flight stay within the HBM budget, then launches all
+// admitted jobs in one persistent-kernel launch. Slots run concurrently, so
+// requests arriving while others are on the GPU are admitted as soon as a slot
+// and memory free up. Each request's output is written only by its own job's
+// segments, so its result does not depend on what it was batched with.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "t3d_runtime.h"
+
+using namespace t3d;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct Pending {
+    t3d_request req;
+    double arrival_abs;  // seconds since server start
+    double admit_abs = 0;
+    uint64_t bytes = 0;
+};
+
+struct Slot {
+    t3d_ctx* ctx = nullptr;
+    cudaEvent_t ev = nullptr;
+    bool busy = false;
+    std::vector<Pending> batch;
+    uint64_t bytes = 0;
+};
+
+// FNV-1a over the raw bytes of a request's emitted stream, in emit order.
+uint64_t fnv(const void* p, size_t n, uint64_t h) {
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t i = 0; i < n; i++) {
+        h ^= b[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+}  // namespace
+
+struct t3d_server {
+    t3d_ctx* owner = nullptr;
+    uint64_t budget = 0;
+    uint32_t max_batch = 1;
+    std::vector<Slot> slots;
+    std::thread sched;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Pending> queue;
+    std::vector<t3d_completion> done;
+    std::atomic<bool> stop{false};
+    uint64_t inflight = 0;
+    Clock::time_point t0;
+    bool verify = true;
+    std::string err;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+    uint64_t request_bytes(const t3d_request& r) {
+        auto it = owner->scenes.find(r.job.scene);
+        if (it == owner->scenes.end()) return 0;
+        const Scene* sc = it->second.get();
+        // outputs (108 B per slot), per-vertex scratch (48 B), visible lists and tables
+        return 116ull * sc->ntris + 48ull * sc->nverts + 1024ull * (sc->models.size() + 4);
+    }
+
+    void finish(Slot& s) {
+        t3d_stats st;
+        int rc = t3d_frame_sync(s.ctx, &st);
+        double t = now();
+        const auto& info = s.ctx->tables.seg_info;
+        std::vector<uint64_t> vis(s.batch.size(), 0), sum(s.batch.size(), 1469598103934665603ull);
+        std::vector<float> buf;
+        for (const auto& si : info) {
+            if (si.job >= s.batch.size()) continue;
+            vis[si.job] += si.count;
+            if (verify && rc == T3D_OK && si.count) {
+                buf.resize(12ull * si.count);
+                cudaMemcpy(buf.data(), (char*)s.ctx->out_xyuv.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
+                sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
+                cudaMemcpy(buf.data(), (char*)s.ctx->out_rgba.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
+                sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
+                cudaMemcpy(buf.data(), (char*)s.ctx->out_depth.ptr + 12ull * si.base, 12ull * si.count, cudaMemcpyDeviceToHost);
+                sum[si.job] = fnv(buf.data(), 12ull * si.count, sum[si.job]);
+            }
+        }
+        std::lock_guard<std::mutex> g(mu);
+        for (size_t k = 0; k < s.batch.size(); k++) {
+            t3d_completion c;
+            memset(&c, 0, sizeof c);
+            c.id = s.batch[k].req.id;
+            c.status = rc;
+            c.visible_tris = vis[k];
+            c.arrival_s = s.batch[k].arrival_abs;
+            c.admit_s = s.batch[k].admit_abs;
+            c.done_s = t;
+            c.checksum = verify ? sum[k] : 0;
+            done.push_back(c);
+        }
+        inflight -= s.bytes;
+        s.bytes = 0;
+        s.batch.clear();
+        s.busy = false;
+    }
+
+    // Admits queued requests into a free slot (called with mu held).
+    bool admit(Slot& s, std::vector<Pending>& out) {
+        double t = now();
+        while (!queue.empty() && out.size() < max_batch) {
+            Pending& p = queue.front();
+            if (p.arrival_abs > t) break;  // replay: not arrived yet
+            if (p.bytes > budget) {         // can never fit
+                t3d_completion c;
+                memset(&c, 0, sizeof c);
+                c.id = p.req.id;
+                c.status = T3D_E_ADMIT;
+                c.arrival_s = p.arrival_abs;
+                c.done_s = t;
+                done.push_back(c);
+                queue.pop_front();
+                continue;
+            }
+            if (inflight + s.bytes + p.bytes > budget) break;  // wait for memory
+            p.admit_abs = t;
+            s.bytes += p.bytes;
+            out.push_back(p);
+            queue.pop_front();
+        }
+        (void)s;
+        return !out.empty();
+    }
+
+    void loop() {
+        cudaSetDevice(owner->device);
+        while (true) {
+            bool progress = false;
+            for (Slot& s : slots)
+                if (s.busy && cudaEventQuery(s.ev) == cudaSuccess) {
+                    finish(s);
+                    progress = true;
+                }
+            for (Slot& s : slots) {
+                if (s.busy) continue;
+                std::vector<Pending> batch;
+                {
+                    std::lock_guard<std::mutex> g(mu);
+                    if (!admit(s, batch)) continue;
+                    inflight += s.bytes;
+                }
+                std::vector<t3d_job_desc> jobs(batch.size());
+                for (size_t k = 0; k < batch.size(); k++) jobs[k] = batch[k].req.job;
+                int rc = t3d_render_jobs(s.ctx, jobs.data(), (uint32_t)jobs.size(), T3D_MODE_BATCHED, 0, nullptr);
+                s.batch = std::move(batch);
+                if (rc == T3D_OK) rc = cudaEventRecord(s.ev, s.ctx->stream) == cudaSuccess ? T3D_OK : T3D_E_CUDA;
+                if (rc != T3D_OK) {
+                    std::lock_guard<std::mutex> g(mu);
+                    err = s.ctx->err;
+                    double t = now();
+                    for (auto& p : s.batch) {
+                        t3d_completion c;
+                        memset(&c, 0, sizeof c);
+                        c.id = p.req.id;
+                        c.status = rc;
+                        c.arrival_s = p.arrival_abs;
+                        c.admit_s = p.admit_abs;
+                        c.done_s = t;
+                        done.push_back(c);
+                    }
+                    inflight -= s.bytes;
+                    s.bytes = 0;
+                    s.batch.clear();
+                    continue;
+                }
+                s.busy = true;
+                progress = true;
+            }
+            bool any_busy = false;
+            for (Slot& s : slots) any_busy |= s.busy;
+            if (stop.load() && !any_busy) {
+                std::lock_guard<std::mutex> g(mu);
+                if (queue.empty()) break;
+            }
+            if (!progress) {
+                std::unique_lock<std::mutex> g(mu);
+                cv.wait_for(g, std::chrono::microseconds(any_busy ? 20 : 200));
+            }
+        }
+    }
+};
+
+extern "C" {
+
+int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batch, uint32_t streams, t3d_server** out) {
+    if (!ctx || !out || max_batch == 0 || streams == 0 || streams > 16 || hbm_budget_bytes == 0) return T3D_E_INVAL;
+    *out = nullptr;
+    t3d_server* s = new (std::nothrow) t3d_server();
+    if (!s) return T3D_E_OOM;
+    s->owner = ctx;
+    s->budget = hbm_budget_bytes;
+    s->max_batch = max_batch;
+    s->t0 = Clock::now();
+    for (uint32_t i = 0; i < streams; i++) {
+        Slot sl;
+        int rc = t3d_create(ctx->device, &sl.ctx);
+        if (rc != T3D_OK) {
+            for (auto& x : s->slots) { cudaEventDestroy(x.ev); t3d_destroy(x.ctx); }
+            delete s;
+            return rc;
+        }
+        sl.ctx->scene_owner = ctx;
+        sl.ctx->tile_tris = ctx->tile_tris;
+        sl.ctx->vchunk = ctx->vchunk;
+        sl.ctx->block_threads = ctx->block_threads;
+        configure(sl.ctx);
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
+        s->slots.push_back(sl);
+    }
+    s->sched = std::thread([s] { s->loop(); });
+    *out = s;
+    return T3D_OK;
+}
+
+int t3d_server_destroy(t3d_server* s) {
+    if (!s) return T3D_E_INVAL;
+    s->stop = true;
+    s->cv.notify_all();
+    if (s->sched.joinable()) s->sched.join();
+    for (auto& x : s->slots) {
+        cudaEventDestroy(x.ev);
+        t3d_destroy(x.ctx);
+    }
+    delete s;
+    return T3D_OK;
+}
+
+int t3d_server_set_verify(t3d_server* s, int verify) {
+    if (!s) return T3D_E_INVAL;
+    std::lock_guard<std::mutex> g(s->mu);
+    s->verify = verify != 0;
+    return T3D_OK;
+}
+
+int t3d_server_submit(t3d_server* s, const t3d_request* req) {
+    if (!s || !req) return T3D_E_INVAL;
+    if (s->owner->scenes.find(req->job.scene) == s->owner->scenes.end()) return T3D_E_NOTFOUND;
+    if (req->job.camera.width <= 0 || req->job.camera.height <= 0) return T3D_E_INVAL;
+    Pending p;
+    p.req = *req;
+    p.bytes = s->request_bytes(*req);
+    if (p.bytes > s->budget) return T3D_E_ADMIT;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        p.arrival_abs = s->now();
+        s->queue.push_back(p);
+    }
+    s->cv.notify_all();
+    return T3D_OK;
+}
+
+int t3d_server_poll(t3d_server* s, t3d_completion* out, uint32_t max, uint32_t* n_out) {
+    if (!s || !n_out || (max && !out)) return T3D_E_INVAL;
+    std::lock_guard<std::mutex> g(s->mu);
+    uint32_t n = (uint32_t)std::min<size_t>(max, s->done.size());
+    if (n) memcpy(out, s->done.data(), sizeof(t3d_completion) * n);
+    s->done.erase(s->done.begin(), s->done.begin() + n);
+    *n_out = n;
+    return T3D_OK;
+}
+
+int t3d_server_replay(t3d_server* s, const t3d_request* reqs, uint32_t n, t3d_completion* out) {
+    if (!s || (n && (!reqs || !out))) return T3D_E_INVAL;
+    for (uint32_t i = 0; i < n; i++) {
+        if (s->owner->scenes.find(reqs[i].job.scene) == s->owner->scenes.end()) return T3D_E_NOTFOUND;
+        if (reqs[i].job.camera.width <= 0 || reqs[i].job.camera.height <= 0) return T3D_E_INVAL;
+    }
+    // Enqueue everything with future arrival times; the scheduler admits each
+    // request only once its arrival time has passed.
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        double base = s->now() + 0.002;
+        for (uint32_t i = 0; i < n; i++) {
+            Pending p;
+            p.req = reqs[i];
+            p.arrival_abs = base + reqs[i].arrival_s;
+            p.bytes = s->request_bytes(reqs[i]);
+            s->queue.push_back(p);
+        }
+        std::stable_sort(s->queue.begin(), s->queue.end(),
+                         [](const Pending& a, const Pending& b) { return a.arrival_abs < b.arrival_abs; });
+    }
+    s->cv.notify_all();
+    std::vector<t3d_completion> got;
+    got.reserve(n);
+    while (got.size() < n) {
+        std::vector<t3d_completion> tmp(256);
+        uint32_t k = 0;
+        t3d_server_poll(s, tmp.data(), (uint32_t)tmp.size(), &k);
+        got.insert(got.end(), tmp.begin(), tmp.begin() + k);
+        if (k == 0) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    std::map<uint64_t, size_t> pos;
+    for (uint32_t i = 0; i < n; i++) pos[reqs[i].id] = i;
+    for (auto& c : got) {
+        auto it = pos.find(c.id);
+        if (it != pos.end()) out[it->second] = c;
+    }
+    return T3D_OK;
+}
+
+}  // extern "C"

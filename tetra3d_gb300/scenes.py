@@ -1,0 +1,611 @@
+"""Seeded synthetic scenes for the vertex stage and their C descriptors.
+
+Every array is float32 and every derived matrix is computed with Tetra3D's
+binary32 operation order (no fused multiply-add), so the same SceneData fed to
+the CUDA library and to the oracle describes bit-identical inputs.
+
+Workloads (sizes as named in the benchmark configuration):
+  uv_sphere_scene   one UV sphere, 32 segments x 16 rings (544 V / 960 T)
+  cubes_scene       1000 unit cubes (24 V / 12 T each), 8 point lights
+  terrain_scene     1024x1024-vertex value-noise grid split into 4 quadrant
+                    models with 4 light groups, 16 point + 1 directional + 2 box lights
+  batched_scene     4096 models, vertex counts log-uniform in [24, 65536]
+  serving scenes    64 resident scenes drawn from the three above
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import abi
+
+F32 = np.float32
+PI32 = F32(math.pi)  # math32.Pi = float32(math.Pi)
+
+
+# --------------------------------------------------------------- matrices ----
+def ident(n=None):
+    if n is None:
+        return np.eye(4, dtype=F32)
+    return np.broadcast_to(np.eye(4, dtype=F32), (n, 4, 4)).copy()
+
+
+def mult(a, b):
+    """Matrix4.Mult with the reference's left-to-right sums (matrix_none.go:6-32), batched."""
+    a = np.asarray(a, F32)
+    b = np.asarray(b, F32)
+    out = np.empty(np.broadcast_shapes(a.shape, b.shape), F32)
+    for i in range(4):
+        for j in range(4):
+            s = a[..., i, 0] * b[..., 0, j]
+            s = s + a[..., i, 1] * b[..., 1, j]
+            s = s + a[..., i, 2] * b[..., 2, j]
+            s = s + a[..., i, 3] * b[..., 3, j]
+            out[..., i, j] = s
+    return out
+
+
+def translate(x, y, z):
+    m = ident()
+    m[3, 0], m[3, 1], m[3, 2] = F32(x), F32(y), F32(z)
+    return m
+
+
+def scale_m(x, y, z):
+    m = ident()
+    m[0, 0], m[1, 1], m[2, 2] = F32(x), F32(y), F32(z)
+    return m
+
+
+def unit3(v):
+    """Vector3.Unit (vector.go:258-266) on float32 (..., 3)."""
+    v = np.asarray(v, F32)
+    ln = (v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1] + v[..., 2] * v[..., 2]).astype(F32)
+    ln = np.sqrt(ln.astype(np.float64)).astype(F32)
+    keep = (ln < F32(1e-8)) | (ln == F32(1))
+    safe = np.where(keep, F32(1), ln)
+    out = (v / safe[..., None]).astype(F32)
+    return np.where(keep[..., None], v, out).astype(F32)
+
+
+def rotate(x, y, z, angle):
+    """NewMatrix4Rotate (matrix.go:101-128); Sin/Cos in float64 like math32."""
+    if x == 0 and y == 0 and z == 0:
+        y = 1
+    v = unit3(np.array([x, y, z], F32))
+    s = F32(math.sin(float(F32(angle))))
+    c = F32(math.cos(float(F32(angle))))
+    m = F32(1) - c
+    X, Y, Z = v
+    r = ident()
+    r[0, 0] = m * X * X + c
+    r[0, 1] = m * X * Y + Z * s
+    r[0, 2] = m * Z * X - Y * s
+    r[1, 0] = m * X * Y - Z * s
+    r[1, 1] = m * Y * Y + c
+    r[1, 2] = m * Y * Z + X * s
+    r[2, 0] = m * Z * X + Y * s
+    r[2, 1] = m * Y * Z - X * s
+    r[2, 2] = m * Z * Z + c
+    return r
+
+
+def quat_to_mat(q):
+    """Quaternion.ToMatrix4 (quaternion.go:135-182), batched over (n, 4) = (x, y, z, w)."""
+    q = np.asarray(q, F32).reshape(-1, 4)
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    n = q.shape[0]
+    m1 = ident(n)
+    m2 = ident(n)
+    m1[:, 0] = np.stack([w, z, -y, x], 1)
+    m1[:, 1] = np.stack([-z, w, x, y], 1)
+    m1[:, 2] = np.stack([y, -x, w, z], 1)
+    m1[:, 3] = np.stack([-x, -y, -z, w], 1)
+    m2[:, 0] = np.stack([w, z, -y, -x], 1)
+    m2[:, 1] = np.stack([-z, w, x, -y], 1)
+    m2[:, 2] = np.stack([y, -x, w, -z], 1)
+    m2[:, 3] = np.stack([x, y, z, w], 1)
+    return mult(m1, m2)
+
+
+def random_quats(rng, n):
+    """Uniformly distributed unit quaternions (Shoemake's subgroup method)."""
+    u = rng.random((n, 3))
+    a = np.sqrt(1 - u[:, 0])
+    b = np.sqrt(u[:, 0])
+    q = np.stack([a * np.sin(2 * np.pi * u[:, 1]), a * np.cos(2 * np.pi * u[:, 1]),
+                  b * np.sin(2 * np.pi * u[:, 2]), b * np.cos(2 * np.pi * u[:, 2])], 1)
+    return q.astype(F32)
+
+
+def trs(pos, scl, rot):
+    """Node.Transform of a parentless node: Scale * Rotation * Translate (node.go:583-585), batched."""
+    pos = np.asarray(pos, F32).reshape(-1, 3)
+    scl = np.asarray(scl, F32).reshape(-1, 3)
+    rot = np.asarray(rot, F32).reshape(-1, 4, 4)
+    n = max(pos.shape[0], scl.shape[0], rot.shape[0])
+    S = ident(n)
+    S[:, 0, 0], S[:, 1, 1], S[:, 2, 2] = scl[:, 0], scl[:, 1], scl[:, 2]
+    T = ident(n)
+    T[:, 3, 0], T[:, 3, 1], T[:, 3, 2] = pos[:, 0], pos[:, 1], pos[:, 2]
+    return mult(mult(S, rot), T)
+
+
+def look_rotation(forward_row):
+    """A rotation whose row 2 (Forward) is the given unit vector; rows 0/1 complete a right-handed basis."""
+    z = unit3(np.asarray(forward_row, F32))
+    up = np.array([0, 1, 0], F32) if abs(float(z[1])) < 0.99 else np.array([1, 0, 0], F32)
+    x = unit3(np.cross(up, z).astype(F32))
+    y = np.cross(z, x).astype(F32)
+    r = ident()
+    r[0, :3], r[1, :3], r[2, :3] = x, y, z
+    return r
+
+
+# ------------------------------------------------------------------ meshes ----
+def default_material(**kw):
+    m = dict(color=(1, 1, 1, 1), tex_w=0.0, tex_h=0.0, present=1, backface_culling=1,
+             sort_mode=abi.SORT_BACK_TO_FRONT, lighting_mode=abi.LIGHTING_DEFAULT, lv_shading_mode=abi.LV_PER_VERTEX,
+             shadeless=0, visible=1, transparency_mode=abi.TRANSPARENCY_AUTO, blend_source_over=1, render_order=0)
+    m.update(kw)
+    return m
+
+
+class MeshData:
+    def __init__(self, positions, normals, uvs, indices, colors=None, parts=None, dims=None):
+        self.positions = np.ascontiguousarray(positions, F32).reshape(-1, 3)
+        self.normals = np.ascontiguousarray(normals, F32).reshape(-1, 3)
+        self.uvs = np.ascontiguousarray(uvs, F32).reshape(-1, 2)
+        self.colors = None if colors is None else np.ascontiguousarray(colors, F32).reshape(-1, 4)
+        self.indices = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        T = self.indices.shape[0]
+        self.parts = parts if parts is not None else [dict(tri_start=0, tri_count=T, mat=default_material())]
+        self.dims = dims  # None: UpdateDimensions
+
+    @property
+    def nverts(self):
+        return self.positions.shape[0]
+
+    @property
+    def ntris(self):
+        return self.indices.shape[0]
+
+
+def flat_normals_like_autonormal(positions, indices):
+    """Mesh.AutoNormal (mesh.go:755-764): every vertex of a triangle gets the triangle normal, in triangle order."""
+    p = positions.astype(F32)
+    n = np.zeros_like(p)
+    a, b, c = p[indices[:, 0]], p[indices[:, 1]], p[indices[:, 2]]
+    v0 = (b - a).astype(F32)
+    v1 = (c - b).astype(F32)
+    cr = np.stack([v0[:, 1] * v1[:, 2] - v1[:, 1] * v0[:, 2],
+                   v0[:, 2] * v1[:, 0] - v1[:, 2] * v0[:, 0],
+                   v0[:, 0] * v1[:, 1] - v1[:, 0] * v0[:, 1]], 1).astype(F32)
+    tn = unit3(cr)
+    for k in range(3):  # later triangles overwrite earlier ones, as in the reference loop
+        n[indices[:, k]] = tn
+    # vectorised assignment keeps the last writer per vertex only within one column; redo exactly in order
+    for t in range(indices.shape[0]):
+        for k in range(3):
+            n[indices[t, k]] = tn[t]
+    return n
+
+
+def cube_mesh(w=1.0, h=1.0, d=1.0):
+    """NewCubeMesh (mesh.go:1251-1342): 24 vertices, 12 triangles, flat normals."""
+    w, h, d = F32(w) / F32(2), F32(h) / F32(2), F32(d) / F32(2)
+    v = [(-w, h, -d, 0, 0), (w, h, d, 1, 1), (w, h, -d, 1, 0), (-w, h, d, 0, 1),
+         (w, -h, -d, 1, 0), (w, -h, d, 1, 1), (-w, -h, -d, 0, 0), (-w, -h, d, 0, 1),
+         (-w, h, d, 0, 0), (w, -h, d, 1, 1), (w, h, d, 1, 0), (-w, -h, d, 0, 1),
+         (w, h, -d, 1, 0), (w, -h, -d, 1, 1), (-w, h, -d, 0, 0), (-w, -h, -d, 0, 1),
+         (w, h, -d, 1, 0), (w, h, d, 1, 1), (w, -h, -d, 0, 0), (w, -h, d, 0, 1),
+         (-w, -h, -d, 0, 0), (-w, h, d, 1, 1), (-w, h, -d, 1, 0), (-w, -h, d, 0, 1)]
+    arr = np.array(v, F32)
+    idx = np.array([0, 1, 2, 3, 1, 0, 4, 5, 6, 6, 5, 7, 8, 9, 10, 11, 9, 8,
+                    12, 13, 14, 14, 13, 15, 16, 17, 18, 18, 17, 19, 20, 21, 22, 23, 21, 20], np.uint32).reshape(-1, 3)
+    pos = arr[:, :3]
+    nrm = flat_normals_like_autonormal(pos, idx)
+    return MeshData(pos, nrm, arr[:, 3:5], idx)
+
+
+def _orient_outward(pos, idx, center=None):
+    """Flips triangles whose geometric normal points towards `center` so outward faces wind CCW."""
+    c = np.zeros(3, F32) if center is None else np.asarray(center, F32)
+    a, b, cc = pos[idx[:, 0]], pos[idx[:, 1]], pos[idx[:, 2]]
+    nrm = np.cross(b - a, cc - b)
+    out = ((a + b + cc) / 3 - c)
+    flip = (nrm * out).sum(1) < 0
+    idx = idx.copy()
+    idx[flip, 1], idx[flip, 2] = idx[flip, 2].copy(), idx[flip, 1].copy()
+    return idx
+
+
+def uv_sphere(segments=32, rings=16, radius=1.0):
+    """A UV sphere built with the NewMesh/AddVertices/AddTriangles recipe (mesh.go:1230-1248):
+    (rings+1) x segments vertices, smooth normals, poles as single triangles."""
+    r = np.arange(rings + 1)[:, None]
+    s = np.arange(segments)[None, :]
+    th = np.pi * r / rings + 0 * s
+    ph = 2 * np.pi * s / segments + 0 * r
+    pos = np.stack([np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)], -1).reshape(-1, 3)
+    pos = (pos * radius).astype(F32)
+    nrm = unit3(pos)
+    uv = np.stack([(s / segments + 0 * r), (r / rings + 0 * s)], -1).reshape(-1, 2).astype(F32)
+    tris = []
+    for i in range(rings):
+        for j in range(segments):
+            a = i * segments + j
+            b = i * segments + (j + 1) % segments
+            c = (i + 1) * segments + j
+            d = (i + 1) * segments + (j + 1) % segments
+            if i != 0:
+                tris.append((a, b, c))
+            if i != rings - 1:
+                tris.append((b, d, c))
+    idx = _orient_outward(pos, np.array(tris, np.uint32))
+    return MeshData(pos, nrm, uv, idx)
+
+
+def icosphere(level):
+    """Icosahedron subdivided `level` times, vertices pushed to the unit sphere, flat normals (AutoNormal)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(v, np.float64) for v in verts]
+    for _ in range(level):
+        cache = {}
+
+        def mid(i, j):
+            key = (min(i, j), max(i, j))
+            if key not in cache:
+                verts.append((verts[i] + verts[j]) / 2)
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    pos = np.array(verts)
+    pos = (pos / np.linalg.norm(pos, axis=1, keepdims=True)).astype(F32)
+    idx = _orient_outward(pos, np.array(faces, np.uint32))
+    nrm = flat_normals_like_autonormal(pos, idx) if len(faces) < 4096 else unit3(pos)
+    uv = np.zeros((pos.shape[0], 2), F32)
+    uv[1::3, 0] = 1
+    uv[2::3, 1] = 1
+    return MeshData(pos, nrm, uv, idx)
+
+
+def value_noise(rng_seed, x, z, octaves=4):
+    """Seeded 2D value noise: random lattice values, smoothstep-bilinear, `octaves` octaves (float64)."""
+    total = np.zeros_like(x, dtype=np.float64)
+    amp, freq, norm = 1.0, 1.0, 0.0
+    for o in range(octaves):
+        rng = np.random.Generator(np.random.PCG64([rng_seed, o]))
+        xs, zs = x * freq, z * freq
+        x0, z0 = np.floor(xs).astype(np.int64), np.floor(zs).astype(np.int64)
+        gx0, gz0 = x0.min(), z0.min()
+        lat = rng.random((int(x0.max() - gx0) + 2, int(z0.max() - gz0) + 2)) * 2 - 1
+        fx, fz = xs - x0, zs - z0
+        sx, sz = fx * fx * (3 - 2 * fx), fz * fz * (3 - 2 * fz)
+        i, j = x0 - gx0, z0 - gz0
+        v00, v10, v01, v11 = lat[i, j], lat[i + 1, j], lat[i, j + 1], lat[i + 1, j + 1]
+        total += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sz) + (v01 * (1 - sx) + v11 * sx) * sz)
+        norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    return total / norm
+
+
+def grid_mesh(nx, nz, extent_x, extent_z, heights, x0=0.0, z0=0.0):
+    """A grid of nx x nz vertices (row-major in z), NewPlaneMesh's triangle order (mesh.go:1533-1589)."""
+    xs = (x0 + np.arange(nx) * (extent_x / max(nx - 1, 1))).astype(np.float64)
+    zs = (z0 + np.arange(nz) * (extent_z / max(nz - 1, 1))).astype(np.float64)
+    X, Z = np.meshgrid(xs, zs)
+    H = heights(X, Z)
+    pos = np.stack([X, H, Z], -1).reshape(-1, 3).astype(F32)
+    # central finite differences
+    dx, dz = extent_x / max(nx - 1, 1), extent_z / max(nz - 1, 1)
+    hp = np.pad(H, 1, mode="edge")
+    gx = (hp[1:-1, 2:] - hp[1:-1, :-2]) / (2 * dx)
+    gz = (hp[2:, 1:-1] - hp[:-2, 1:-1]) / (2 * dz)
+    nrm = np.stack([-gx, np.ones_like(gx), -gz], -1)
+    nrm = (nrm / np.linalg.norm(nrm, axis=-1, keepdims=True)).reshape(-1, 3).astype(F32)
+    uv = np.stack([(X - X.min()) / max(extent_x, 1e-9), (Z - Z.min()) / max(extent_z, 1e-9)], -1).reshape(-1, 2).astype(F32)
+    q = (np.arange(nz - 1)[:, None] * nx + np.arange(nx - 1)[None, :]).reshape(-1)
+    idx = np.stack([q + 1, q + nx, q + nx + 1, q, q + nx, q + 1], 1).reshape(-1, 3).astype(np.uint32)
+    return MeshData(pos, nrm, uv, idx)
+
+
+# ------------------------------------------------------------------ scenes ----
+class SceneData:
+    """Meshes, models, lights and light lists of one scene plus a default camera.
+
+    light list 0 is the scene light list in Render order; lists 1.. are LightGroups.
+    """
+
+    def __init__(self, meshes, nmodels, lights, lists, cells=None, name=""):
+        self.name = name
+        self.meshes = meshes
+        self.models = (abi.ModelDesc * max(1, nmodels))()
+        self.nmodels = nmodels
+        self.mv = np.ctypeslib.as_array(self.models)[:nmodels]
+        self.lights = (abi.LightDesc * max(1, len(lights)))(*lights)
+        self.nlights = len(lights)
+        self.lists = [list(map(int, l)) for l in lists]
+        self.cells = np.zeros((1, 4), F32) if cells is None or len(cells) == 0 else np.ascontiguousarray(cells, F32)
+        self.ncells = 0 if cells is None else len(cells)
+        self.camera = None
+        self.meta = {}
+        self._keep = []
+
+    def desc(self):
+        keep = []
+        md = (abi.MeshDesc * max(1, len(self.meshes)))()
+        for i, m in enumerate(self.meshes):
+            pa = (abi.PartDesc * max(1, len(m.parts)))()
+            for k, p in enumerate(m.parts):
+                pa[k].tri_start = p["tri_start"]
+                pa[k].tri_count = p["tri_count"]
+                mat = p["mat"]
+                for f, v in mat.items():
+                    if f == "color":
+                        pa[k].mat.color[:] = [float(c) for c in v]
+                    else:
+                        setattr(pa[k].mat, f, v)
+            keep.append(pa)
+            d = md[i]
+            d.positions, d.normals, d.uvs = abi.fptr(m.positions), abi.fptr(m.normals), abi.fptr(m.uvs)
+            d.colors = abi.fptr(m.colors) if m.colors is not None else None
+            d.indices = abi.uptr(m.indices)
+            d.parts = C.cast(pa, C.POINTER(abi.PartDesc))
+            d.num_vertices, d.num_triangles, d.num_parts = m.nverts, m.ntris, len(m.parts)
+            if m.dims is not None:
+                d.has_dimensions = 1
+                d.dim_min[:] = [float(x) for x in m.dims[0]]
+                d.dim_max[:] = [float(x) for x in m.dims[1]]
+        offs = np.zeros(len(self.lists) + 1, np.uint32)
+        for i, l in enumerate(self.lists):
+            offs[i + 1] = offs[i] + len(l)
+        items = np.array([x for l in self.lists for x in l] or [0], np.uint32)
+        keep += [md, offs, items]
+        sd = abi.SceneDesc()
+        sd.meshes = C.cast(md, C.POINTER(abi.MeshDesc))
+        sd.models = C.cast(self.models, C.POINTER(abi.ModelDesc))
+        sd.lights = C.cast(self.lights, C.POINTER(abi.LightDesc))
+        sd.volume_cells = abi.fptr(self.cells)
+        sd.list_offsets = abi.uptr(offs)
+        sd.list_items = abi.uptr(items)
+        sd.num_meshes, sd.num_models, sd.num_lights = len(self.meshes), self.nmodels, self.nlights
+        sd.num_volume_cells, sd.num_lists = self.ncells, len(self.lists)
+        self._keep = keep
+        return sd
+
+    def total_tris(self):
+        return sum(self.meshes[int(m)].ntris for m in self.mv["mesh"])
+
+    def total_verts(self):
+        return sum(self.meshes[int(m)].nverts for m in self.mv["mesh"])
+
+
+def set_models_trs(sd, mesh, pos, scl, rot, color=(1, 1, 1, 1), light_list=-1, frustum=1, step=None):
+    n = sd.nmodels
+    mv = sd.mv
+    mv["mesh"] = np.asarray(mesh, np.uint32).reshape(-1) if np.ndim(mesh) else mesh
+    mv["visible"] = 1
+    mv["frustum_culling"] = frustum
+    mv["shadeless"] = 0
+    mv["light_list"] = light_list
+    mv["use_trs"] = 1
+    mv["color"] = np.broadcast_to(np.asarray(color, F32), (n, 4))
+    rot = np.asarray(rot, F32).reshape(n, 4, 4)
+    pos = np.asarray(pos, F32).reshape(n, 3)
+    scl = np.asarray(scl, F32).reshape(n, 3)
+    mv["position"] = pos
+    mv["scale"] = scl
+    mv["rotation"] = rot.reshape(n, 16)
+    M = trs(pos, scl, rot)
+    mv["transform"] = M.reshape(n, 16)
+    mv["world_rotation"] = rot.reshape(n, 16)
+    mv["rotate_step"] = (ident(n) if step is None else np.asarray(step, F32).reshape(n, 4, 4)).reshape(n, 16)
+
+
+def light(kind, color=(1, 1, 1), energy=1.0, rng_=0.0, pos=(0, 0, 0), rot=None, vol=None):
+    L = abi.LightDesc()
+    L.type = kind
+    L.color[:] = [float(color[0]), float(color[1]), float(color[2]), 1.0]
+    L.energy = float(energy)
+    L.range = float(rng_)
+    r = ident() if rot is None else np.asarray(rot, F32)
+    M = mult(r, translate(*pos))
+    L.transform[:] = M.reshape(16).tolist()
+    L.world_rotation[:] = r.reshape(16).tolist()
+    if vol is not None:
+        vmin, vmax, cell, counts, first = vol
+        L.vol_min[:] = [float(x) for x in vmin]
+        L.vol_max[:] = [float(x) for x in vmax]
+        L.cell_size[:] = [float(x) for x in cell]
+        L.cell_count[:] = [int(x) for x in counts]
+        L.cell_first = first
+    return L
+
+
+def light_volume_counts(vmin, vmax, cell):
+    """LightVolumeResize's cell counts (light.go:485-513): float32 accumulation loops."""
+    counts = []
+    for a in range(3):
+        lo, hi, cs = F32(vmin[a]), F32(vmax[a]), F32(cell[a])
+        k = 0
+        x = lo + F32(cs / F32(2))
+        while x <= hi - F32(cs / F32(2)):
+            k += 1
+            x = F32(x + cs)
+        counts.append(k)
+    return counts
+
+
+def camera(pos=(0, 0, 0), rot=None, w=640, h=360, fov=60.0, near=0.1, far=100.0, perspective=1,
+           render_depth=1, lighting_on=1, fog_on=1, fog_mode=abi.FOG_ADD, ortho_scale=20.0):
+    c = abi.CameraDesc()
+    r = ident() if rot is None else np.asarray(rot, F32)
+    M = trs(np.asarray(pos, F32), np.ones(3, F32), r)[0]
+    c.transform[:] = M.reshape(16).tolist()
+    c.world_rotation[:] = r.reshape(16).tolist()
+    c.width, c.height = int(w), int(h)
+    c.perspective, c.render_depth, c.perspective_corrected = perspective, render_depth, 0
+    c.lighting_on, c.fog_on, c.fog_mode = lighting_on, fog_on, fog_mode
+    c.fov_y, c.near_plane, c.far_plane = float(fov), float(near), float(far)
+    c.ortho_scale, c.depth_margin = float(ortho_scale), 0.04
+    c.fog_range[:] = [0.0, 1.0]
+    c.fog_color[:] = [0.0, 0.0, 0.0, 0.0]
+    return c
+
+
+def deg2rad(deg):
+    """math32.ToRadians (math32.go:14-16)."""
+    return F32(math.pi) * F32(deg) / F32(180)
+
+
+# ------------------------------------------------------------- workloads ----
+def uv_sphere_scene(seed=1, w=640, h=360):
+    """One UV sphere (radius 1, 32 x 16), RGBA vertex colours in [0.5, 1], random rotation at (0,0,-5);
+    640x360 FOV 75, ambient 0.2, a directional light along -(1,1,1), a point light at (2,2,-3)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    me = uv_sphere(32, 16, 1.0)
+    me.colors = rng.uniform(0.5, 1.0, (me.nverts, 4)).astype(F32)
+    lights = [light(abi.LIGHT_AMBIENT, energy=0.2),
+              light(abi.LIGHT_DIRECTIONAL, energy=1.0, rot=look_rotation(unit3(np.array([1, 1, 1], F32)))),
+              light(abi.LIGHT_POINT, energy=2.0, rng_=10.0, pos=(2, 2, -3))]
+    sd = SceneData([me], 1, lights, [[0, 1, 2]], name="uv_sphere")
+    set_models_trs(sd, 0, [(0, 0, -5)], [(1, 1, 1)], quat_to_mat(random_quats(rng, 1)))
+    sd.camera = camera(w=w, h=h, fov=75.0)
+    return sd
+
+
+def cubes_scene(seed=2, n=1000, w=1920, h=1080, nlights=8):
+    """n unit cubes (shared mesh), positions U[-50,50]^3, random rotations, scales U[0.5,2];
+    1920x1080 FOV 60 at the origin looking -Z; 8 coloured point lights, ambient 0.1."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    me = cube_mesh(1, 1, 1)
+    pos = rng.uniform(-50, 50, (n, 3)).astype(F32)
+    s = rng.uniform(0.5, 2.0, n).astype(F32)
+    rot = quat_to_mat(random_quats(rng, n))
+    lights = [light(abi.LIGHT_AMBIENT, energy=0.1)]
+    for i in range(nlights):
+        lights.append(light(abi.LIGHT_POINT, color=rng.uniform(0, 1, 3), energy=rng.uniform(0.5, 2.0),
+                            rng_=rng.uniform(5, 20), pos=rng.uniform(-50, 50, 3)))
+    sd = SceneData([me], n, lights, [list(range(len(lights)))], name="cubes")
+    set_models_trs(sd, np.zeros(n, np.uint32), pos, np.repeat(s[:, None], 3, 1), rot)
+    sd.camera = camera(w=w, h=h, fov=60.0)
+    return sd
+
+
+def terrain_scene(seed=3, n=1024, extent=200.0, w=3840, h=2160):
+    """A value-noise grid of n x n vertices (4 octaves, amplitude 5) split into 4 quadrant models, each
+    lit by its own LightGroup (ambient + directional + 4 of the 16 point lights + 2 box lights).
+    3840x2160 FOV 70, camera 30 units up pitched -35 degrees, front-to-back sort."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    half = n // 2
+    heights = lambda X, Z: 5.0 * value_noise(seed, X / 25.0, Z / 25.0, 4)
+    step = extent / (n - 1)
+    meshes = []
+    for qz in range(2):
+        for qx in range(2):
+            i0, i1 = (0, half + 1) if qx == 0 else (half, n)
+            j0, j1 = (0, half + 1) if qz == 0 else (half, n)
+            me = grid_mesh(i1 - i0, j1 - j0, step * (i1 - i0 - 1), step * (j1 - j0 - 1), heights,
+                           x0=-extent / 2 + i0 * step, z0=-extent / 2 + j0 * step)
+            me.parts[0]["mat"] = default_material(sort_mode=abi.SORT_FRONT_TO_BACK)
+            meshes.append(me)
+    lights = [light(abi.LIGHT_AMBIENT, energy=0.15),
+              light(abi.LIGHT_DIRECTIONAL, color=rng.uniform(0.5, 1, 3), energy=0.8,
+                    rot=look_rotation(unit3(np.array([0.3, 1.0, 0.2], F32))))]
+    for i in range(16):
+        lights.append(light(abi.LIGHT_POINT, color=rng.uniform(0, 1, 3), energy=rng.uniform(0.5, 2.0),
+                            rng_=rng.uniform(10, 40),
+                            pos=(rng.uniform(-extent / 2, extent / 2), rng.uniform(2, 20), rng.uniform(-extent / 2, extent / 2))))
+    cells = []
+    for b in range(2):
+        c = np.round(rng.uniform(-extent / 4, extent / 4, 3) * 4) / 4
+        c[1] = 0.0
+        vmin, vmax, cs = (c - 10).astype(F32), (c + 10).astype(F32), np.array([20, 20, 20], F32)
+        counts = light_volume_counts(vmin, vmax, cs)
+        first = len(cells)
+        for _ in range(int(np.prod(counts))):
+            cells.append(list(rng.uniform(0.2, 1.0, 3)) + [1.0])
+        lights.append(light(abi.LIGHT_VOLUME, energy=1.0, vol=(vmin, vmax, cs, counts, first)))
+    ambient, sun, points, boxes = 0, 1, list(range(2, 18)), [18, 19]
+    lists = [list(range(len(lights)))]
+    for g in range(4):
+        lists.append([ambient, sun] + points[4 * g:4 * g + 4] + boxes)
+    sd = SceneData(meshes, 4, lights, lists, cells=np.array(cells, F32), name="terrain")
+    set_models_trs(sd, np.arange(4, dtype=np.uint32), np.zeros((4, 3)), np.ones((4, 3)), ident(4),
+                   light_list=np.arange(1, 5))
+    rot = rotate(1, 0, 0, deg2rad(-35.0))
+    sd.camera = camera(pos=(0, 30, 0), rot=rot, w=w, h=h, fov=70.0)
+    return sd
+
+
+def batched_scene(seed=4, n=4096, vmin=24, vmax=65536, nlights=32, box=200.0, w=1920, h=1080, max_levels=6):
+    """n models with log-uniform vertex counts in [vmin, vmax] (half noise-displaced grids of the exact
+    count, half icospheres of the nearest level), transforms in [-box, box]^3, 32 point lights + ambient,
+    a random LightGroup (ambient + random subset of the point lights) per model, random angular velocity
+    steps for animation. Camera 1920x1080 at (0, 0, 1.5*box) looking -Z, far 3*box."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    targets = np.exp(rng.uniform(math.log(vmin), math.log(vmax), n)).astype(np.int64)
+    ico = {}
+    meshes, mesh_of = [], np.zeros(n, np.uint32)
+    ico_levels = [icosphere(L) for L in range(max_levels + 1)]
+    ico_counts = np.array([m.nverts for m in ico_levels])
+    for i in range(n):
+        if i % 2 == 0:
+            lvl = int(np.argmin(np.abs(np.log(ico_counts) - math.log(targets[i]))))
+            if lvl not in ico:
+                ico[lvl] = len(meshes)
+                meshes.append(ico_levels[lvl])
+            mesh_of[i] = ico[lvl]
+        else:
+            side = max(5, int(round(math.sqrt(targets[i]))))
+            nx, nz = side, max(5, int(targets[i] // side))
+            sseed = int(rng.integers(1 << 30))
+            me = grid_mesh(nx, nz, 4.0, 4.0 * nz / nx, lambda X, Z, s=sseed: 0.4 * value_noise(s, X, Z, 3),
+                           x0=-2.0, z0=-2.0 * nz / nx)
+            mesh_of[i] = len(meshes)
+            meshes.append(me)
+    pos = rng.uniform(-box, box, (n, 3)).astype(F32)
+    scl = np.repeat(rng.uniform(1.0, 6.0, (n, 1)), 3, 1).astype(F32)
+    rot = quat_to_mat(random_quats(rng, n))
+    lights = [light(abi.LIGHT_AMBIENT, energy=0.1)]
+    for _ in range(nlights):
+        lights.append(light(abi.LIGHT_POINT, color=rng.uniform(0, 1, 3), energy=rng.uniform(0.5, 2.0),
+                            rng_=rng.uniform(20, 80), pos=rng.uniform(-box, box, 3)))
+    lists = [list(range(len(lights)))]
+    groups = np.zeros(n, np.int32)
+    for i in range(n):
+        mask = rng.random(nlights) < 0.5
+        lists.append([0] + [1 + k for k in range(nlights) if mask[k]])
+        groups[i] = len(lists) - 1
+    omega = rng.uniform(-1, 1, (n, 3)).astype(F32)
+    dt = F32(1.0 / 60.0)
+    steps = np.stack([rotate(*omega[i], float(np.linalg.norm(omega[i].astype(np.float64))) * dt) for i in range(n)])
+    sd = SceneData(meshes, n, lights, lists, name="batched")
+    set_models_trs(sd, mesh_of, pos, scl, rot, light_list=groups, step=steps)
+    sd.camera = camera(pos=(0, 0, 1.5 * box), w=w, h=h, fov=60.0, near=0.1, far=3.0 * box)
+    return sd
+
+
+def small_variant(kind, seed):
+    """Reduced-size versions of the workloads for oracle comparisons."""
+    if kind == "sphere":
+        return uv_sphere_scene(seed)
+    if kind == "cubes":
+        return cubes_scene(seed, n=200)
+    if kind == "terrain":
+        return terrain_scene(seed, n=96, extent=60.0, w=1280, h=720)
+    if kind == "batched":
+        return batched_scene(seed, n=48, vmin=24, vmax=6000, nlights=8, box=40.0, max_levels=4)
+    raise ValueError(kind)
