@@ -1,0 +1,365 @@
+"""Benchmark of the GB300 vertex stage (visible triangles per second).
+
+Default workload: the batched form -- 4096 models with log-uniform vertex
+counts in [24, 65536] (35.1M vertices, 69.7M triangles), 32 point lights +
+ambient with a random LightGroup per model, 1920x1080 camera, animated
+transforms -- rendered as one persistent-kernel launch per frame and replayed
+from a captured CUDA graph. A step is one frame over all 4096 models.
+
+  value  visible triangles/s with the scene resident in HBM (graph replay)
+  e2e    the same metric through the public C ABI with host buffers: per step
+         the host pushes every model transform (t3d_scene_set_models), renders
+         (t3d_render, batched) and reads the per-pair visible counts back
+         (t3d_frame_sync)
+  plain  one launch per render pair (the reference's render + flush loop)
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                [--workload batched|terrain|cubes|sphere|serving]
+Under torchrun (N > 1) every rank renders its own replica (replicas only: the
+stage has no cross-GPU exchange); rank 0 prints the JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "visible_tris_per_s"
+UNIT = "tris/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(workload):
+    """DRAM bytes per launch of the frame kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"t3d_frame_kernel_{workload}.md")
+    if not os.path.exists(p):
+        return None, None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                v = line.split(":", 1)[1].strip().split()[0]
+                return float(v), p
+    return None, p
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def make_scene(workload):
+    from tetra3d_gb300 import scenes
+    if workload == "batched":
+        return scenes.batched_scene(4)
+    if workload == "terrain":
+        return scenes.terrain_scene(3)
+    if workload == "cubes":
+        return scenes.cubes_scene(2)
+    if workload == "sphere":
+        return scenes.uv_sphere_scene(1)
+    raise ValueError(workload)
+
+
+def workload_config(workload, sd):
+    c = sd.camera
+    base = {"workload": {"batched": "batched_4096_models", "terrain": "terrain_grid_1024x1024",
+                         "cubes": "cubes_1000", "sphere": "uv_sphere_32x16"}[workload],
+            "models": int(sd.nmodels), "vertices": int(sd.total_verts()), "triangles": int(sd.total_tris()),
+            "camera": f"{c.width}x{c.height} fov{c.fov_y:g}", "lights": int(sd.nlights),
+            "l2": "inputs larger than L2 (129 MB), no flush" if sd.total_verts() * 48 > 256e6 else
+                  "small scene: L2-resident across steps (no flush)"}
+    return base
+
+
+def cpu_sample(sd, workload):
+    """Bounded sample of the workload for the CPU arms: every k-th model."""
+    from tetra3d_gb300 import scenes
+    if workload == "batched":
+        idx = np.arange(0, sd.nmodels, 16)
+        return scenes.subset(sd, idx), f"{len(idx)} of {sd.nmodels} models (every 16th), 1 frame"
+    return sd, "full scene, 1 frame"
+
+
+def time_cpu(sd_sample, cam, threads, min_seconds=10.0, max_reps=50):
+    from oracle import pyoracle
+    reps, vis, t0 = 0, 0, time.perf_counter()
+    while True:
+        f = pyoracle.render(sd_sample, cam, threads=threads)
+        vis += f.visible_tris
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or reps >= max_reps:
+            break
+    return vis / el, reps, el
+
+
+# ----------------------------------------------------------------- ours ----
+def run_ours(args, rank, world, local_rank):
+    import ctypes as C
+
+    import torch
+    import __graft_entry__
+    from tetra3d_gb300 import abi, scenes
+    from tetra3d_gb300.runtime import Context
+
+    __graft_entry__.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    sd = make_scene(args.workload)
+    ctx = Context(local_rank)
+    sid = ctx.upload(sd)
+    cam = sd.camera
+    animate = args.workload == "batched"
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    # ---- device-resident value: captured CUDA graph of the batched frame ----
+    ctx.graph_capture(sid, cam, animate=animate)
+    ctx.graph_replay(args.warmup, stream=sh)
+    torch.cuda.synchronize()
+    v0, b0 = ctx.counters()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        ev0.record(stream)
+        ctx.graph_replay(args.steps, stream=sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    v1, b1 = ctx.counters()
+    vis = v1 - v0
+    alg_bytes = (b1 - b0) + 108 * vis
+    if dist is not None:
+        t = torch.tensor([ms, float(vis), float(alg_bytes)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms, vis, alg_bytes = float(mx[0]), float(t[1]), float(t[2])
+    value = vis / (ms / 1e3)
+    ms_per_step = ms / args.steps
+    st_last = ctx.sync()
+
+    # ---- plain path: one launch per render pair ----
+    plain = None
+    if rank == 0 and not args.no_plain:
+        pf = max(1, min(3, args.steps))
+        ctx.render(sid, cam, mode=abi.MODE_PLAIN, animate=False, stream=sh)
+        ctx.sync()
+        pv0, _ = ctx.counters()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(pf):
+            ctx.render(sid, cam, mode=abi.MODE_PLAIN, animate=False, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pst = ctx.sync()
+        pv1, _ = ctx.counters()
+        pms = e0.elapsed_time(e1) / pf
+        plain = {"tris_per_s": (pv1 - pv0) / (pms * pf / 1e3), "ms_per_frame": pms,
+                 "launches_per_frame": int(pst.launches), "frames": pf}
+
+    # ---- e2e through the public API with host buffers ----
+    e2e = None
+    if rank == 0:
+        n = sd.nmodels
+        rot = sd.mv["rotation"].reshape(n, 4, 4).copy()
+        step = sd.mv["rotate_step"].reshape(n, 4, 4).copy()
+        ek = max(3, min(args.steps, 30))
+        # warm
+        ctx.set_models(sid, sd)
+        ctx.render(sid, cam, mode=abi.MODE_BATCHED, stream=sh)
+        ctx.sync()
+        ev, eb = 0, 0
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for _ in range(ek):
+            if animate:  # the game loop advances Node.Rotate on the host
+                rot = scenes.mult(step, rot)
+                sd.mv["rotation"] = rot.reshape(n, 16)
+            ctx.set_models(sid, sd)
+            ctx.render(sid, cam, mode=abi.MODE_BATCHED, stream=sh)
+            st = ctx.sync()
+            ev += st.visible_tris
+            h2d += n * C.sizeof(abi.ModelDesc) + st.h2d_bytes
+            d2h += st.d2h_bytes
+        el = time.perf_counter() - t0
+        e2e = {"value": ev / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d // ek),
+               "d2h_bytes_per_step": int(d2h // ek), "ms_per_step": el / ek * 1e3, "steps": ek}
+
+    # ---- CPU baseline (oracle port, 1 thread) ----
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sample, desc = cpu_sample(sd, args.workload)
+        rate, reps, el = time_cpu(sample, cam, threads=1, min_seconds=args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{desc}; {reps} repetitions in {el:.1f} s, static transforms"}
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        achieved = alg_bytes / (ms / 1e3) / 1e9 / max(1, world)
+        traffic, tsrc = profile_traffic(args.workload)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": dict(workload_config(args.workload, sd), form="batched persistent kernel, CUDA graph replay",
+                           animated=animate, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_step": alg_bytes / args.steps / max(1, world),
+                         "traffic_source": tsrc},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk.summary(),
+            "gpu_launches": int(args.steps),
+            "visible_tris_per_step": vis / args.steps / max(1, world),
+            "culled_models_last_frame": int(st_last.culled_models),
+            "plain": plain,
+            "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------ reference ----
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sd = make_scene(args.workload)
+    sample, desc = cpu_sample(sd, args.workload)
+    from oracle import pyoracle
+    from tetra3d_gb300 import scenes
+    threads = os.cpu_count() or 1
+    # size each step so the whole run stays within about two minutes
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    stride = 16
+    while True:
+        t0 = time.perf_counter()
+        pyoracle.render(sample, sd.camera, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt <= budget or args.workload != "batched" or stride >= 1024:
+            break
+        stride *= 2
+        idx = np.arange(0, sd.nmodels, stride)
+        sample, desc = scenes.subset(sd, idx), f"{len(idx)} of {sd.nmodels} models (every {stride}th), 1 frame"
+    for _ in range(args.warmup):
+        pyoracle.render(sample, sd.camera, threads=threads)
+    vis = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vis += pyoracle.render(sample, sd.camera, threads=threads).visible_tris
+    el = time.perf_counter() - t0
+    value = vis / el
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": dict(workload_config(args.workload, sd), form="CPU restatement of Camera.Render"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{desc} per step, render pairs split over {threads} host threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=240)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "terrain", "cubes", "sphere", "serving"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if args.workload == "serving":
+        import bench_serving
+        bench_serving.main(args)
+        return
+    run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -260,6 +260,8 @@ typedef struct t3d_stats {
     uint32_t launches;       /* kernel launches of the last frame */
     uint64_t algorithmic_bytes; /* 48V+12T of surviving models + 108*visible + 64*models + 48*lights*lit models */
     uint64_t scratch_bytes;  /* device scratch held by the context */
+    uint64_t h2d_bytes;      /* host-to-device bytes of the last render call (tables) */
+    uint64_t d2h_bytes;      /* device-to-host bytes of the last t3d_frame_sync */
 } t3d_stats;
 
 typedef struct t3d_ctx t3d_ctx;
@@ -297,6 +299,10 @@ int t3d_render_jobs(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t num_jobs,
                     int mode, int animate, void* stream);
 /* Waits for the last frame and fills the segment counts. */
 int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out);
+/* Cumulative counters since t3d_create over every frame (graph replays
+ * included): visible triangles and the 48V+12T+64+48L bytes of models that
+ * survived frustum culling. Waits for the last frame. */
+int t3d_frame_counters(t3d_ctx* ctx, uint64_t* visible_total, uint64_t* model_bytes_total);
 int t3d_frame_view_get(t3d_ctx* ctx, t3d_frame_view* view_out);
 int t3d_frame_segments(t3d_ctx* ctx, t3d_segment_info* segs_out, uint32_t max_segs, uint32_t* num_out);
 /* Copies the visible triangles of the last frame to host memory, densely in

@@ -102,7 +102,8 @@ class SegmentInfo(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("visible_tris", C.c_uint64), ("total_tris", C.c_uint64), ("drawn_parts", C.c_uint32),
                 ("total_parts", C.c_uint32), ("culled_models", C.c_uint32), ("launches", C.c_uint32),
-                ("algorithmic_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64)]
+                ("algorithmic_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("h2d_bytes", C.c_uint64),
+                ("d2h_bytes", C.c_uint64)]
 
 
 class Request(C.Structure):
@@ -130,6 +131,7 @@ SIGNATURES = {
     "t3d_render": (C.c_int, [_VP, C.c_uint32, C.POINTER(CameraDesc), C.c_int, C.c_int, _VP]),
     "t3d_render_jobs": (C.c_int, [_VP, C.POINTER(JobDesc), C.c_uint32, C.c_int, C.c_int, _VP]),
     "t3d_frame_sync": (C.c_int, [_VP, C.POINTER(Stats)]),
+    "t3d_frame_counters": (C.c_int, [_VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "t3d_frame_view_get": (C.c_int, [_VP, C.POINTER(FrameView)]),
     "t3d_frame_segments": (C.c_int, [_VP, C.POINTER(SegmentInfo), C.c_uint32, C.POINTER(C.c_uint32)]),
     "t3d_frame_download": (C.c_int, [_VP, f32p, f32p, f32p, C.c_uint64, C.POINTER(C.c_uint64)]),

@@ -72,7 +72,8 @@ int t3d_create(int device, t3d_ctx** out) {
         delete ctx;
         return T3D_E_CUDA;
     }
-    if (configure(ctx) != T3D_OK) {
+    if (configure(ctx) != T3D_OK || ctx->accum.ensure(ctx, 64) != T3D_OK ||
+        cudaMemset(ctx->accum.ptr, 0, ctx->accum.cap) != cudaSuccess) {
         delete ctx;
         return T3D_E_CUDA;
     }
@@ -89,7 +90,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     ctx->scenes.clear();
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->light_work, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax,
-                      &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth})
+                      &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum})
         b->release();
     ctx->table_host.release();
     ctx->readback.release();
@@ -274,9 +275,22 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
         scratch += b->cap;
     s.scratch_bytes = scratch;
+    s.h2d_bytes = ctx->last_h2d;
+    s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl;
     ctx->stats = s;
     ctx->frame_valid = true;
     if (stats_out) *stats_out = s;
+    return T3D_OK;
+}
+
+int t3d_frame_counters(t3d_ctx* ctx, uint64_t* visible_total, uint64_t* model_bytes_total) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    unsigned long long h[2] = {0, 0};
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    CKR(cudaMemcpy(h, ctx->accum.ptr, sizeof h, cudaMemcpyDeviceToHost));
+    if (visible_total) *visible_total = h[0];
+    if (model_bytes_total) *model_bytes_total = h[1];
     return T3D_OK;
 }
 
@@ -338,6 +352,7 @@ int t3d_graph_capture(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam, 
     int rc = build_frame(ctx, &job, 1, animate);
     if (rc) return rc;
     if ((rc = upload_frame(ctx, ctx->stream))) return rc;
+    if ((rc = ctx->ctl.ensure(ctx, sizeof(Ctl)))) return rc;  // no allocation may happen while capturing
     CKR(cudaStreamSynchronize(ctx->stream));
     CKR(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     rc = launch_frame(ctx, T3D_MODE_BATCHED, ctx->stream);

@@ -172,6 +172,7 @@ struct FrameParams {
     float4* out_rgba;
     float* out_depth;
     Ctl* ctl;
+    unsigned long long* accum;    // [0] visible triangles, [1] model bytes; cumulative across frames
     // ranges processed by this launch
     uint32_t inst_begin, inst_end;
     uint32_t seg_begin, seg_end;

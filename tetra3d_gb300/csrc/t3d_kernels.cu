@@ -149,8 +149,12 @@ __device__ void phase_prep(const FrameParams& P) {
         store16(transposed(inverted(WR)), pr.dirrot);  // light.go:326-330
         bool culled = (md->flags & MOD_FRUSTUM) && !model_in_frustum(cam, M, me);
         pr.culled = culled ? 1u : 0u;
-        if (culled) atomicAdd(&P.ctl->culled, 1u);
-        else atomicAdd(&P.ctl->bytes, (unsigned long long)in.bytes);
+        if (culled) {
+            atomicAdd(&P.ctl->culled, 1u);
+        } else {
+            atomicAdd(&P.ctl->bytes, (unsigned long long)in.bytes);
+            atomicAdd(&P.accum[1], (unsigned long long)in.bytes);
+        }
         // PointLight.beginModel (light.go:175-189) and the model-level range skip (camera.go:1625-1629)
         f3 dspan = mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]);
         float maxSpan = mag3(dspan);
@@ -630,7 +634,10 @@ __device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
                 scan_bins(sm);
                 rank_and_emit(P, seg, J, smem, T, t0, n, sort_mode);
             }
-            if (threadIdx.x == 0) P.seg_count[s] = n;
+            if (threadIdx.x == 0) {
+                P.seg_count[s] = n;
+                if (n) atomicAdd(&P.accum[0], (unsigned long long)n);
+            }
         } else {
             uint32_t* gi = P.vis_idx + (size_t)mt * T;
             float* gd = P.vis_depth + (size_t)mt * T;
@@ -641,6 +648,7 @@ __device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
                     atomicMin(&P.seg_minmax[2 * s], __float_as_uint(mn));
                     atomicMax(&P.seg_minmax[2 * s + 1], __float_as_uint(mx));
                     atomicAdd(&P.seg_count[s], n);
+                    atomicAdd(&P.accum[0], (unsigned long long)n);
                 }
             }
         }

@@ -567,6 +567,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         if (p.bytes) memcpy(hb + p.off, p.src, p.bytes);
     DevJob* hj = (DevJob*)(hb + o_jobs);
     for (size_t j = 0; j < F.jobs.size(); j++) hj[j].lights = (const DevLight*)(db + o_lights) + F.job_light_base[j];
+    ctx->last_h2d = off;
     if (off) {
         cudaError_t e = cudaMemcpyAsync(db, hb, off, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) { set_err(ctx, "table upload: %s", cudaGetErrorString(e)); return T3D_E_CUDA; }
@@ -610,6 +611,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.out_xyuv = (float4*)ctx->out_xyuv.ptr;
     P.out_rgba = (float4*)ctx->out_rgba.ptr;
     P.out_depth = (float*)ctx->out_depth.ptr;
+    P.accum = (unsigned long long*)ctx->accum.ptr;
     P.tile_tris = ctx->tile_tris;
     P.vchunk = ctx->vchunk;
     return T3D_OK;

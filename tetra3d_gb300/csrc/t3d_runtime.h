@@ -97,8 +97,9 @@ struct t3d_ctx {
     const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
     t3d::HostBuf table_host, readback;
     t3d::DevBuf table_dev, ctl, preps, light_work, vcull, vxyuv, vrgba, vis_idx, vis_depth, tile_count, tile_hist,
-        seg_minmax, seg_count, out_xyuv, out_rgba, out_depth;
+        seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
+    uint64_t last_h2d = 0;
     uint32_t launches = 0;
     bool frame_pending = false;
     bool frame_valid = false;

@@ -107,6 +107,11 @@ class Context:
                                                 C.byref(got)), "frame_download")
         return Frame(xyuv[:n], rgba[:n], depth[:n], self.segments(), st)
 
+    def counters(self):
+        v, b = C.c_uint64(), C.c_uint64()
+        self._check(self.lib.t3d_frame_counters(self.h, C.byref(v), C.byref(b)), "frame_counters")
+        return v.value, b.value
+
     def view(self):
         v = abi.FrameView()
         self._check(self.lib.t3d_frame_view_get(self.h, C.byref(v)), "frame_view_get")

@@ -609,3 +609,13 @@ def small_variant(kind, seed):
     if kind == "batched":
         return batched_scene(seed, n=48, vmin=24, vmax=6000, nlights=8, box=40.0, max_levels=4)
     raise ValueError(kind)
+
+
+def subset(sd, models):
+    """A SceneData with only the given models (meshes, lights and light lists shared)."""
+    models = np.asarray(models, np.int64)
+    out = SceneData(sd.meshes, len(models), [sd.lights[i] for i in range(sd.nlights)], sd.lists,
+                    cells=sd.cells[:sd.ncells] if sd.ncells else None, name=sd.name + f"[{len(models)}]")
+    out.mv[:] = sd.mv[models]
+    out.camera = sd.camera
+    return out
