@@ -108,10 +108,10 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def make_scene(workload):
+def make_scene(workload, models=4096):
     from tetra3d_gb300 import scenes
     if workload == "batched":
-        return scenes.batched_scene(4)
+        return scenes.batched_scene(4, n=models)
     if workload == "terrain":
         return scenes.terrain_scene(3)
     if workload == "cubes":
@@ -123,7 +123,7 @@ def make_scene(workload):
 
 def workload_config(workload, sd):
     c = sd.camera
-    base = {"workload": {"batched": "batched_4096_models", "terrain": "terrain_grid_1024x1024",
+    base = {"workload": {"batched": f"batched_{sd.nmodels}_models", "terrain": "terrain_grid_1024x1024",
                          "cubes": "cubes_1000", "sphere": "uv_sphere_32x16"}[workload],
             "models": int(sd.nmodels), "vertices": int(sd.total_verts()), "triangles": int(sd.total_tris()),
             "camera": f"{c.width}x{c.height} fov{c.fov_y:g}", "lights": int(sd.nlights),
@@ -170,7 +170,7 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    sd = make_scene(args.workload)
+    sd = make_scene(args.workload, args.models)
     ctx = Context(local_rank)
     sid = ctx.upload(sd)
     cam = sd.camera
@@ -286,6 +286,8 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": int(args.steps),
             "visible_tris_per_step": vis / args.steps / max(1, world),
             "culled_models_last_frame": int(st_last.culled_models),
+            "phase_us_last_frame": {k: round(float(v), 1) for k, v in
+                                    zip(("prep", "triangles", "hist", "scan", "rank", "emit"), st_last.phase_us)},
             "plain": plain,
             "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,
         }
@@ -299,7 +301,7 @@ def run_ours(args, rank, world, local_rank):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    sd = make_scene(args.workload)
+    sd = make_scene(args.workload, args.models)
     sample, desc = cpu_sample(sd, args.workload)
     from oracle import pyoracle
     from tetra3d_gb300 import scenes
@@ -342,6 +344,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "terrain", "cubes", "sphere", "serving"])
+    ap.add_argument("--models", type=int, default=4096, help="models in the batched scene (4096 = the full workload)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

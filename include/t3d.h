@@ -262,6 +262,7 @@ typedef struct t3d_stats {
     uint64_t scratch_bytes;  /* device scratch held by the context */
     uint64_t h2d_bytes;      /* host-to-device bytes of the last render call (tables) */
     uint64_t d2h_bytes;      /* device-to-host bytes of the last t3d_frame_sync */
+    double   phase_us[6];    /* batched launch: model prep, triangles, histogram, scan, rank, emit */
 } t3d_stats;
 
 typedef struct t3d_ctx t3d_ctx;
@@ -270,8 +271,8 @@ typedef struct t3d_ctx t3d_ctx;
 int         t3d_create(int device, t3d_ctx** out);
 int         t3d_destroy(t3d_ctx* ctx);
 const char* t3d_last_error(const t3d_ctx* ctx);
-/* Tuning knobs (0 keeps the current value): triangles per tile, vertices per
- * vertex-phase work item, threads per block. */
+/* Tuning knobs (0 keeps the current value): triangles per tile (power of two,
+ * 256..4096), a reserved value, threads per block (128 or 256). */
 int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint32_t block_threads);
 
 /* ---- resident scenes --------------------------------------------------------- */

@@ -10,7 +10,7 @@
 #include "t3d_runtime.h"
 
 extern "C" const void* t3d_frame_kernel_ptr();
-extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris);
+extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads);
 
 using namespace t3d;
 
@@ -25,7 +25,7 @@ using namespace t3d;
 
 namespace t3d {
 int configure(t3d_ctx* ctx) {
-    ctx->smem_bytes = t3d_frame_smem_bytes(ctx->tile_tris);
+    ctx->smem_bytes = t3d_frame_smem_bytes(ctx->tile_tris, ctx->block_threads);
     const void* fn = t3d_frame_kernel_ptr();
     CKR(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
     int per_sm = 0;
@@ -88,7 +88,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     drop_graph(ctx);
     for (auto& kv : ctx->scenes) kv.second->release();
     ctx->scenes.clear();
-    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->light_work, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->order,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum})
         b->release();
@@ -107,8 +107,8 @@ int t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint
     uint32_t T = tile_tris ? tile_tris : ctx->tile_tris;
     uint32_t V = vertex_chunk ? vertex_chunk : ctx->vchunk;
     uint32_t B = block_threads ? block_threads : ctx->block_threads;
-    if (T < 256 || T > (uint32_t)kTileMax || (T & (T - 1)) || V < 32 || V > (1u << 20) || (B != 128 && B != 256 && B != 512)) {
-        set_err(ctx, "set_tuning: tile %u (256..%d, power of two), chunk %u, block %u (128/256/512)", T, kTileMax, V, B);
+    if (T < 256 || T > (uint32_t)kTileMax || (T & (T - 1)) || V < 32 || V > (1u << 20) || (B != 128 && B != 256)) {
+        set_err(ctx, "set_tuning: tile %u (256..%d, power of two), chunk %u, block %u (128/256)", T, kTileMax, V, B);
         return T3D_E_INVAL;
     }
     cudaSetDevice(ctx->device);
@@ -271,11 +271,21 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.algorithmic_bytes += 108ull * s.visible_tris;
     s.launches = ctx->launches;
     size_t scratch = 0;
-    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->light_work, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->order,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
         scratch += b->cap;
     s.scratch_bytes = scratch;
     s.h2d_bytes = ctx->last_h2d;
+    if (ctx->nctl == 1) {
+        const Ctl& c = ctls[0];
+        unsigned long long prev = c.t_end[7];
+        for (int k = 0; k < 6; k++) {
+            if (c.t_end[k] >= prev && prev) {
+                s.phase_us[k] = (double)(c.t_end[k] - prev) / 1e3;
+                prev = c.t_end[k];
+            }
+        }
+    }
     s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl;
     ctx->stats = s;
     ctx->frame_valid = true;

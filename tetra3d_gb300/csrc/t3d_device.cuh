@@ -4,9 +4,10 @@
 // warp moves whole 128-bit words):
 //   va[v] = (px, py, pz, nx)   vb[v] = (ny, nz, u, v)   vc[v] = (r, g, b, a)
 //   idx[3t..3t+2]              mesh-absolute vertex indices per triangle
-// Per frame the host builds job / instance / segment / work-item tables; the
-// kernel writes per-vertex scratch (vcull, vxyuv, vrgba), per-tile visible
-// lists and the resident output stream.
+// Per frame the host builds job / instance / segment / tile tables; the kernel
+// writes per-model prep records, per-tile visible lists (multi-tile segments
+// only) and the resident output stream. No per-vertex scratch: every emitted
+// corner is computed from the vertex streams when it is written.
 #pragma once
 
 #include <stdint.h>
@@ -19,7 +20,7 @@ namespace t3d {
 constexpr int kBins = 512;          // sortingTriangleBucket.Resize(512), sortingTriangles.go:166-168
 constexpr int kTileMax = 4096;      // largest triangle tile the kernel supports
 constexpr int kMaxLights = 128;     // per model light list
-constexpr int kMaxWarps = 16;       // block of at most 512 threads
+constexpr int kMaxWarps = 8;        // block of at most 256 threads
 
 // segment flags
 enum : uint32_t {
@@ -101,7 +102,7 @@ struct DevJob {
 // One (job, model) pair.
 struct DevInst {
     uint32_t job, model;
-    uint32_t light_off, light_cnt;  // into inst_light_idx / inst_light_work
+    uint32_t light_off, light_cnt;  // into inst_light_idx
     uint32_t animate;               // apply rotate_step in this launch
     uint32_t pad;
     uint64_t bytes;                 // algorithmic bytes if the model survives culling
@@ -113,8 +114,10 @@ struct DevPrep {
     float M[16];
     float dirrot[16];   // DirectionalLight.workingModelRotation (light.go:328)
     float invcam[4];    // model-space camera position (model.go:630)
+    float inv_r[16];    // Decompose(Inverted(M)): rotation rows 0..3 (cols 0..2) and p * (1/s) in column 3
+    float maxspan;      // Mesh.Dimensions.MaxSpan()
     uint32_t culled;
-    uint32_t pad[3];
+    uint32_t pad[2];
 };
 
 // One render pair (model, mesh part) of one job.
@@ -122,7 +125,7 @@ struct DevSeg {
     uint32_t inst, job, mesh, flags;
     uint32_t tri_start, tri_count;   // mesh-absolute
     uint32_t vmin, vcount;           // mesh-absolute vertex range the triangles use
-    uint32_t vscratch;               // first per-vertex scratch record
+    uint32_t reserved0;
     uint32_t out_base;               // first output triangle slot
     uint32_t tile_first, ntiles;     // global tile numbers
     uint32_t mt_first;               // first multi-tile tile number (SEG_MULTI)
@@ -141,6 +144,7 @@ struct Ctl {
     unsigned long long bytes;       // algorithmic bytes of surviving models
     uint32_t culled;
     uint32_t pad[3];
+    unsigned long long t_end[8];    // globaltimer when the last block finished phase k; [7] = kernel start
 };
 
 enum : int32_t { ERR_NONE = 0, ERR_BARRIER_TIMEOUT = 1, ERR_BAD_INDEX = 2, ERR_LIGHTS = 3 };
@@ -150,23 +154,20 @@ struct FrameParams {
     const DevInst* insts;
     DevPrep* preps;
     const uint32_t* inst_light_idx;
-    float4* inst_light_work;      // (wx, wy, wz, skip) per instance light slot
     const DevSeg* segs;
-    const uint32_t* vitem_seg;    // vertex work item -> segment
-    const uint32_t* vitem_chunk;  // vertex work item -> chunk within the segment
     const uint32_t* tile_seg;     // tile -> segment
     const uint32_t* mt_tiles;     // multi-tile tiles (global tile numbers)
     const uint32_t* mt_segs;      // multi-tile segments
+    const uint32_t* emit_seg;     // emit work item -> multi-tile segment
+    const uint32_t* emit_chunk;   // emit work item -> chunk of tile_tris output slots
     // scratch
-    float4* vcull;                // (cx, cy, clipZ, depth01)
-    float4* vxyuv;
-    float4* vrgba;
-    uint32_t* vis_idx;            // per multi-tile tile: kTile visible entries
+    uint16_t* vis_idx;            // per multi-tile tile: up to tile_tris visible entries
     float* vis_depth;
     uint32_t* tile_count;         // visible per multi-tile tile
     uint32_t* tile_hist;          // per multi-tile tile: kBins counters, then bases
     uint32_t* seg_minmax;         // 2 per segment: min bits, max bits
     uint32_t* seg_count;          // visible per segment (output)
+    uint32_t* order;              // multi-tile segments: segment-relative triangle per output slot
     // output stream
     float4* out_xyuv;
     float4* out_rgba;
@@ -176,12 +177,12 @@ struct FrameParams {
     // ranges processed by this launch
     uint32_t inst_begin, inst_end;
     uint32_t seg_begin, seg_end;
-    uint32_t vitem_begin, vitem_end;
     uint32_t tile_begin, tile_end;
     uint32_t mt_tile_begin, mt_tile_end;
     uint32_t mt_seg_begin, mt_seg_end;
+    uint32_t emit_begin, emit_end;
     uint32_t tile_tris;           // triangles per tile
-    uint32_t vchunk;              // vertices per vertex work item
+    uint32_t vchunk;              // unused (kept for tuning compatibility)
     uint32_t has_multi;           // any multi-tile segment in range
     uint32_t pad;
 };

@@ -110,11 +110,11 @@ __device__ bool model_in_frustum(const JobCam& c, const m4& M, const DevMesh& me
     return true;
 }
 
-__device__ void phase_prep(const FrameParams& P) {
+__device__ __noinline__ void phase_prep(const FrameParams& P) {
     const uint32_t n = P.inst_end - P.inst_begin;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    for (uint32_t k = g; k < n; k += stride) {
+    // model k runs on block k % grid: the serial per-model chains spread over every SM
+    for (uint32_t k = blockIdx.x + gridDim.x * threadIdx.x; k < n; k += stride) {
         const uint32_t i = P.inst_begin + k;
         const DevInst in = P.insts[i];
         const DevJob& J = P.jobs[in.job];
@@ -146,6 +146,10 @@ __device__ void phase_prep(const FrameParams& P) {
         InvFrame inv = inv_frame(M);   // model.go:629
         f3 ic = to_model_space(inv, mk3(cam.pos[0], cam.pos[1], cam.pos[2]));  // model.go:630
         pr.invcam[0] = ic.x; pr.invcam[1] = ic.y; pr.invcam[2] = ic.z; pr.invcam[3] = 0.0f;
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 3; c++) pr.inv_r[4 * r + c] = inv.r.m[r][c];
+        const f3 off = hmul3(inv.p, inv.inv_s);
+        pr.inv_r[3] = off.x; pr.inv_r[7] = off.y; pr.inv_r[11] = off.z; pr.inv_r[15] = 0.0f;
         store16(transposed(inverted(WR)), pr.dirrot);  // light.go:326-330
         bool culled = (md->flags & MOD_FRUSTUM) && !model_in_frustum(cam, M, me);
         pr.culled = culled ? 1u : 0u;
@@ -155,28 +159,11 @@ __device__ void phase_prep(const FrameParams& P) {
             atomicAdd(&P.ctl->bytes, (unsigned long long)in.bytes);
             atomicAdd(&P.accum[1], (unsigned long long)in.bytes);
         }
-        // PointLight.beginModel (light.go:175-189) and the model-level range skip (camera.go:1625-1629)
-        f3 dspan = mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]);
-        float maxSpan = mag3(dspan);
-        f3 modelPos = row3(M, 3);
-        for (uint32_t s = 0; s < in.light_cnt; s++) {
-            const uint32_t li = P.inst_light_idx[in.light_off + s];
-            const DevLight& L = J.lights[li];
-            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (L.type == T3D_LIGHT_POINT) {
-                f3 lp = mk3(L.wpos[0], L.wpos[1], L.wpos[2]);
-                f3 wp = to_model_space(inv, lp);
-                w.x = wp.x; w.y = wp.y; w.z = wp.z;
-                if (L.range > 0.0f) {
-                    float dist = maxSpan + L.range;
-                    if (dist2(modelPos, lp) > dist * dist) w.w = 1.0f;
-                }
-            }
-            P.inst_light_work[in.light_off + s] = w;
-        }
+        // Mesh.Dimensions.MaxSpan for the model-level point-light skip (camera.go:1625-1629)
+        pr.maxspan = mag3(mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]));
     }
     const uint32_t ns = P.seg_end - P.seg_begin;
-    for (uint32_t k = g; k < ns; k += stride) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += stride) {
         const uint32_t s = P.seg_begin + k;
         P.seg_minmax[2 * s] = 0xFFFFFFFFu;
         P.seg_minmax[2 * s + 1] = 0u;
@@ -185,24 +172,14 @@ __device__ void phase_prep(const FrameParams& P) {
 }
 
 // ------------------------------------------------------------------ P1 ----
+// One light of the model's list as the emit loop reads it (48 bytes).
+// x, y, z: point = model-space workingPosition, ambient = result,
+// directional = workingForward. Volume geometry is read from `vol`.
 struct SLight {
     int32_t type, skip;
-    int32_t cnt[3];
-    uint32_t cell_first;
     float cr, cg, cb, energy, range, range2;
-    float wx, wy, wz;    // point: model-space workingPosition
-    float ax, ay, az;    // ambient result
-    float fx, fy, fz;    // directional workingForward
-    float vmin[3], vmax[3], cell[3], off[3], bias[3];
-};
-
-struct VertexSmem {
-    SLight lights[kMaxLights];
-    float mvp[16];
-    float M[16];
-    float dirrot[16];
-    uint32_t nlights;
-    uint32_t item;
+    float x, y, z;
+    const DevLight* vol;
 };
 
 // LightVolume.convertToXYZIndices + getLightCell (light.go:717-741, :1267-1272)
@@ -210,28 +187,35 @@ __device__ __forceinline__ int lv_index(float v) {
     if (!(v > -2147483648.0f && v < 2147483647.0f)) return -1;
     return (int)v;
 }
-__device__ bool lv_cell(const SLight& L, f3 p, uint32_t& idx) {
+__device__ bool lv_cell(const DevLight& L, f3 p, uint32_t& idx) {
     float csx = L.cell[0], csy = L.cell[1], csz = L.cell[2];
-    int x = lv_index(roundf(((p.x - L.off[0] - L.vmin[0] - (csx / 2.0f)) / csx)));
-    int y = lv_index(roundf(((p.y - L.off[1] - L.vmin[1] - (csy / 2.0f)) / csy)));
-    int z = lv_index(roundf(((p.z - L.off[2] - L.vmin[2] - (csz / 2.0f)) / csz)));
+    int x = lv_index(roundf(((p.x - L.offset[0] - L.vmin[0] - (csx / 2.0f)) / csx)));
+    int y = lv_index(roundf(((p.y - L.offset[1] - L.vmin[1] - (csy / 2.0f)) / csy)));
+    int z = lv_index(roundf(((p.z - L.offset[2] - L.vmin[2] - (csz / 2.0f)) / csz)));
     if (x < 0 || y < 0 || z < 0 || x >= L.cnt[0] || y >= L.cnt[1] || z >= L.cnt[2]) return false;
     idx = (uint32_t)(x + (y * L.cnt[0]) + (z * L.cnt[0] * L.cnt[1]));
     return true;
 }
 
+// Matrix4.MultVec with the matrix read from shared memory (row-major 16 floats).
+__device__ __forceinline__ f3 mult_vec_s(const float* m, f3 v) {
+    return mk3(m[0] * v.x + m[4] * v.y + m[8] * v.z + m[12], m[1] * v.x + m[5] * v.y + m[9] * v.z + m[13],
+               m[2] * v.x + m[6] * v.y + m[10] * v.z + m[14]);
+}
+
 // One light's contribution to one vertex (ILight.VertexLight, light.go:115-663).
-__device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3 vpos, f3 vnrm, const m4& M,
-                                             const m4& dirrot, const float* __restrict__ cells, float& r, float& g,
+// M (model transform) and dirrot (workingModelRotation) live in shared memory.
+__device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3 vpos, f3 vnrm, const float* M,
+                                             const float* dirrot, const float* __restrict__ cells, float& r, float& g,
                                              float& b) {
     const bool mat = flags & SEG_MAT;
     const uint32_t lmode = seg_light_mode(flags);
     switch (L.type) {
     case T3D_LIGHT_AMBIENT:
-        r += L.ax; g += L.ay; b += L.az;
+        r += L.x; g += L.y; b += L.z;
         break;
     case T3D_LIGHT_POINT: {
-        f3 work = mk3(L.wx, L.wy, L.wz);
+        f3 work = mk3(L.x, L.y, L.z);
         float distance = dist2(work, vpos);
         if (L.range > 0.0f) {
             if (distance > L.range2) return;
@@ -255,8 +239,8 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
         break;
     }
     case T3D_LIGHT_DIRECTIONAL: {
-        f3 fwd = mk3(L.fx, L.fy, L.fz);
-        f3 normal = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? fwd : mult_vec(dirrot, vnrm);
+        f3 fwd = mk3(L.x, L.y, L.z);
+        f3 normal = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? fwd : mult_vec_s(dirrot, vnrm);
         float df = dot3(normal, fwd);
         if (mat && lmode == T3D_LIGHTING_DOUBLE_SIDED) df = fabsf(df);
         if (df <= 0.0f) return;
@@ -268,24 +252,25 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
     case T3D_LIGHT_VOLUME: {
         const uint32_t mode = mat ? seg_lv_mode(flags) : 0u;
         if (mat && mode == T3D_LV_OFF) return;
+        const DevLight& G = *L.vol;
         float cr = 0.0f, cg = 0.0f, cb = 0.0f;
         uint32_t idx;
         if (mat && mode == T3D_LV_PER_OBJECT) {
-            if (lv_cell(L, row3(M, 3), idx)) {
-                const float* c = cells + 4 * (size_t)(L.cell_first + idx);
+            if (lv_cell(G, mk3(M[12], M[13], M[14]), idx)) {
+                const float* c = cells + 4 * (size_t)(G.cell_first + idx);
                 cr = c[0]; cg = c[1]; cb = c[2];
             }
         } else {
-            f3 cs = mk3(L.cell[0] / 2.0f, L.cell[1] / 2.0f, L.cell[2] / 2.0f);
-            f3 bias = mk3(L.bias[0], L.bias[1], L.bias[2]);
+            f3 cs = mk3(G.cell[0] / 2.0f, G.cell[1] / 2.0f, G.cell[2] / 2.0f);
+            f3 bias = mk3(G.bias[0], G.bias[1], G.bias[2]);
             f3 vertPos = mk3(0.f, 0.f, 0.f), vertPosN = mk3(0.f, 0.f, 0.f);
-            if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) vertPosN = add3(mult_vec(M, add3(vpos, hmul3(vnrm, cs))), bias);
-            else vertPos = add3(mult_vec(M, vpos), bias);
-            if (!(vertPos.x >= L.vmin[0] && vertPos.y >= L.vmin[1] && vertPos.z >= L.vmin[2] && vertPos.x <= L.vmax[0] &&
-                  vertPos.y <= L.vmax[1] && vertPos.z <= L.vmax[2]))
+            if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) vertPosN = add3(mult_vec_s(M, add3(vpos, hmul3(vnrm, cs))), bias);
+            else vertPos = add3(mult_vec_s(M, vpos), bias);
+            if (!(vertPos.x >= G.vmin[0] && vertPos.y >= G.vmin[1] && vertPos.z >= G.vmin[2] && vertPos.x <= G.vmax[0] &&
+                  vertPos.y <= G.vmax[1] && vertPos.z <= G.vmax[2]))
                 return;
-            if (lv_cell(L, mode == T3D_LV_PER_VERTEX_WITH_NORMAL ? vertPosN : vertPos, idx)) {
-                const float* c = cells + 4 * (size_t)(L.cell_first + idx);
+            if (lv_cell(G, mode == T3D_LV_PER_VERTEX_WITH_NORMAL ? vertPosN : vertPos, idx)) {
+                const float* c = cells + 4 * (size_t)(G.cell_first + idx);
                 cr = c[0]; cg = c[1]; cb = c[2];
             }
         }
@@ -299,135 +284,225 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
     }
 }
 
-__device__ void phase_vertex(const FrameParams& P, unsigned char* smem_raw) {
-    VertexSmem& sm = *reinterpret_cast<VertexSmem*>(smem_raw);
-    for (;;) {
-        const uint32_t item = P.vitem_begin + next_item(P.ctl, 1, &sm.item);
-        if (item >= P.vitem_end) break;
-        const uint32_t s = P.vitem_seg[item];
-        const DevSeg seg = P.segs[s];
-        if (seg.flags & SEG_SKIP) continue;
-        const DevPrep& pr = P.preps[seg.inst];
-        if (pr.culled) continue;
-        const DevJob& J = P.jobs[seg.job];
-        const DevInst& in = P.insts[seg.inst];
-        const bool lit = seg.flags & SEG_LIT;
-        // stage the model's matrices and light list
-        for (uint32_t k = threadIdx.x; k < 48; k += blockDim.x) {
-            if (k < 16) sm.mvp[k] = pr.mvp[k];
-            else if (k < 32) sm.M[k - 16] = pr.M[k - 16];
-            else sm.dirrot[k - 32] = pr.dirrot[k - 32];
-        }
-        const uint32_t nl = lit ? min(in.light_cnt, (uint32_t)kMaxLights) : 0u;
-        for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
-            const DevLight& L = J.lights[P.inst_light_idx[in.light_off + k]];
-            const float4 w = P.inst_light_work[in.light_off + k];
-            SLight& d = sm.lights[k];
-            d.type = L.type;
-            d.skip = (L.type == T3D_LIGHT_POINT && w.w != 0.0f) ? 1 : 0;
-            d.cnt[0] = L.cnt[0]; d.cnt[1] = L.cnt[1]; d.cnt[2] = L.cnt[2];
-            d.cell_first = L.cell_first;
-            d.cr = L.color[0]; d.cg = L.color[1]; d.cb = L.color[2];
-            d.energy = L.energy; d.range = L.range; d.range2 = L.range2;
-            d.wx = w.x; d.wy = w.y; d.wz = w.z;
-            d.ax = L.amb[0]; d.ay = L.amb[1]; d.az = L.amb[2];
-            d.fx = L.fwd[0]; d.fy = L.fwd[1]; d.fz = L.fwd[2];
-            for (int c = 0; c < 3; c++) {
-                d.vmin[c] = L.vmin[c]; d.vmax[c] = L.vmax[c]; d.cell[c] = L.cell[c];
-                d.off[c] = L.offset[c]; d.bias[c] = L.bias[c];
-            }
-        }
-        __syncthreads();
-        const m4 mvp = load16(sm.mvp);
-        const m4 M = load16(sm.M);
-        const m4 dirrot = load16(sm.dirrot);
+// ------------------------------------------------------- tile phases ----
+// Shared memory of one block while it works on a tile:
+//   ModelSmem | TileSmem | whist[nwarps][kBins] | lidx u16[T] | depth f32[T] | bin u16[T]
+// Per work item constants of the emit path (camera, segment and stream bases).
+enum : uint32_t { EC_PERSP = 1, EC_PCORRECT = 2, EC_DEPTH = 4, EC_RDEPTH = 8, EC_FOG_ADD = 16, EC_FOG_SUB = 32,
+                  EC_LIT = 64, EC_COLORS = 128 };
+struct EmitConst {
+    float W, H, halfW, halfH;
+    float margin, spread, tex_w, tex_h;
+    float mp[4];
+    float fog0, fogspan, fog_r, fog_g;
+    float fog_b;
+    uint32_t flags, seg_flags, pad;
+    const float4* va;        // vertex streams of the mesh (mesh vertex 0)
+    const float4* vb;
+    const float4* vc;
+    const uint32_t* idx;     // triangle 0 of the mesh
+    const float* cells;
+};
+
+struct ModelSmem {
+    SLight lights[kMaxLights];  // active lights only (model-level skips removed), in list order
+    float4 mvpc[4];   // MVP columns: clip.x = dot(mvpc[0], (x, y, z, 1)) in the reference's order
+    float M[16];
+    float dirrot[16];
+    EmitConst ec;
+    uint32_t nl;
+    uint32_t pad[3];
+};
+
+struct TileSmem {
+    uint32_t item, nvis, warp_tot[kMaxWarps], scan_tmp[kMaxWarps];
+    uint32_t wlo[kMaxWarps], whi[kMaxWarps];  // per-warp range of the visible list
+    float wmin[kMaxWarps], wmax[kMaxWarps];
+    uint32_t bins_walk[kBins];  // per-bin counts / bases in walk order
+};
+
+struct SmemLayout {
+    ModelSmem* ms;
+    TileSmem* ts;
+    uint32_t* whist;
+    uint16_t* lidx;
+    float* depth;
+    uint16_t* bin;
+    uint16_t* perm;   // single-tile segments: list entry of each output position
+};
+
+__device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t tile) {
+    SmemLayout L;
+    size_t o = 0;
+    L.ms = (ModelSmem*)(smem + o);
+    o += sizeof(ModelSmem);
+    L.ts = (TileSmem*)(smem + o);
+    o += sizeof(TileSmem);
+    L.whist = (uint32_t*)(smem + o);
+    o += sizeof(uint32_t) * (blockDim.x >> 5) * kBins;
+    L.depth = (float*)(smem + o);
+    o += 4 * (size_t)tile;
+    L.lidx = (uint16_t*)(smem + o);
+    o += 2 * (size_t)tile;
+    L.bin = (uint16_t*)(smem + o);
+    o += 2 * (size_t)tile;
+    L.perm = (uint16_t*)(smem + o);
+    return L;
+}
+
+// Stages the model's matrices and (if lit) its light list in shared memory;
+// each thread runs ILight.beginModel for one light (light.go:175-189) and the
+// model-level point-range skip (camera.go:1625-1629).
+__device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJob& J, ModelSmem& ms) {
+    const DevPrep& pr = P.preps[seg.inst];
+    const DevInst& in = P.insts[seg.inst];
+    float* mvpc = reinterpret_cast<float*>(ms.mvpc);
+    for (uint32_t k = threadIdx.x; k < 48; k += blockDim.x) {
+        if (k < 16) mvpc[4 * (k & 3) + (k >> 2)] = pr.mvp[k];
+        else if (k < 32) ms.M[k - 16] = pr.M[k - 16];
+        else ms.dirrot[k - 32] = pr.dirrot[k - 32];
+    }
+    const uint32_t nl = (seg.flags & SEG_LIT) ? min(in.light_cnt, (uint32_t)kMaxLights) : 0u;
+    if (threadIdx.x == 0) {
         const JobCam& cam = J.cam;
-        const float nearp = cam.near_;
-        (void)nearp;
-        const float W = cam.W, H = cam.H, halfW = cam.halfW, halfH = cam.halfH;
-        const bool persp = cam.perspective != 0, pc = cam.persp_correct != 0;
-        const bool want_depth = cam.render_depth || cam.fog_on;
-        const uint32_t vbase = J.meshes[seg.mesh].vbase;
-        const uint32_t v0 = P.vitem_chunk[item] * P.vchunk;
-        const uint32_t v1 = min(seg.vcount, v0 + P.vchunk);
-        for (uint32_t lv = v0 + threadIdx.x; lv < v1; lv += blockDim.x) {
-            const uint32_t gv = vbase + seg.vmin + lv;
-            const float4 a = J.va[gv];
-            const float4 b = J.vb[gv];
-            const f3 vert = mk3(a.x, a.y, a.z);
-            // MultVecW (model.go:808-811)
-            const float X = mvp.m[0][0] * vert.x + mvp.m[1][0] * vert.y + mvp.m[2][0] * vert.z + mvp.m[3][0];
-            const float Y = mvp.m[0][1] * vert.x + mvp.m[1][1] * vert.y + mvp.m[2][1] * vert.z + mvp.m[3][1];
-            const float Z = mvp.m[0][2] * vert.x + mvp.m[1][2] * vert.y + mvp.m[2][2] * vert.z + mvp.m[3][2];
-            const float Wc = mvp.m[0][3] * vert.x + mvp.m[1][3] * vert.y + mvp.m[2][3] * vert.z + mvp.m[3][3];
-            // cull record (model.go:862-873)
-            float w1 = Wc;
-            if (w1 < 0.0f) w1 = 0.000001f;
-            const float cx = X / w1, cy = Y / w1;
-            // emit (camera.go:1655-1742)
-            float w = Wc;
-            if (!persp) w = 1.0f;
-            if (w < 0.0f) w = 0.001f;
-            const float dx = (X / w) * W + halfW;
-            const float dy = (Y / -w) * H + halfH;
-            const float U = b.z, Vv = b.w;
-            float uvU, uvV;
-            if (pc) { uvU = (U / w) * seg.tex_w; uvV = ((1.0f - Vv) / w) * seg.tex_h; }
-            else { uvU = U * seg.tex_w; uvV = (1.0f - Vv) * seg.tex_h; }
-            float cr, cg, cb, ca;
-            if (seg.flags & SEG_COLORS) {
-                const float4 c = J.vc[gv];
-                cr = c.x * seg.mp[0]; cg = c.y * seg.mp[1]; cb = c.z * seg.mp[2]; ca = c.w * seg.mp[3];
-            } else {
-                cr = seg.mp[0]; cg = seg.mp[1]; cb = seg.mp[2]; ca = seg.mp[3];
+        const DevMesh& me = J.meshes[seg.mesh];
+        EmitConst& e = ms.ec;
+        e.W = cam.W; e.H = cam.H; e.halfW = cam.halfW; e.halfH = cam.halfH;
+        e.margin = cam.margin; e.spread = cam.spread; e.tex_w = seg.tex_w; e.tex_h = seg.tex_h;
+        for (int c = 0; c < 4; c++) e.mp[c] = seg.mp[c];
+        e.fog0 = cam.fog_range[0];
+        e.fogspan = cam.fog_range[1] - cam.fog_range[0];
+        e.fog_r = cam.fog_color[0]; e.fog_g = cam.fog_color[1]; e.fog_b = cam.fog_color[2];
+        uint32_t f = 0;
+        if (cam.perspective) f |= EC_PERSP;
+        if (cam.persp_correct) f |= EC_PCORRECT;
+        if (cam.render_depth || cam.fog_on) f |= EC_DEPTH;
+        if (cam.render_depth) f |= EC_RDEPTH;
+        if (!cam.render_depth && cam.fog_on && cam.fog_mode == T3D_FOG_ADD) f |= EC_FOG_ADD;
+        if (!cam.render_depth && cam.fog_on && cam.fog_mode == T3D_FOG_SUB) f |= EC_FOG_SUB;
+        if (seg.flags & SEG_LIT) f |= EC_LIT;
+        if (seg.flags & SEG_COLORS) f |= EC_COLORS;
+        e.flags = f;
+        e.seg_flags = seg.flags;
+        e.va = J.va + me.vbase;
+        e.vb = J.vb + me.vbase;
+        e.vc = J.vc + me.vbase;
+        e.idx = J.idx + 3 * (size_t)me.tbase;
+        e.cells = J.cells;
+    }
+    for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
+        const DevLight& L = J.lights[P.inst_light_idx[in.light_off + k]];
+        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (L.type == T3D_LIGHT_POINT) {
+            const f3 lp = mk3(L.wpos[0], L.wpos[1], L.wpos[2]);
+            const float* r = pr.inv_r;
+            // Decompose(Inverted(M)): r.MultVec(lp) + p * (1/s)
+            const f3 q = mk3(r[0] * lp.x + r[4] * lp.y + r[8] * lp.z + r[12], r[1] * lp.x + r[5] * lp.y + r[9] * lp.z + r[13],
+                             r[2] * lp.x + r[6] * lp.y + r[10] * lp.z + r[14]);
+            w.x = q.x + r[3]; w.y = q.y + r[7]; w.z = q.z + r[11];
+            if (L.range > 0.0f) {
+                const float dist = pr.maxspan + L.range;
+                if (dist2(mk3(pr.M[12], pr.M[13], pr.M[14]), lp) > dist * dist) w.w = 1.0f;
             }
-            if (lit) {
-                const f3 vnrm = mk3(a.w, b.x, b.y);
-                float lr = 0.0f, lg = 0.0f, lb = 0.0f;
-                for (uint32_t k = 0; k < nl; k++) {
-                    const SLight& L = sm.lights[k];
-                    if (L.skip) continue;
-                    light_vertex(L, seg.flags, vert, vnrm, M, dirrot, J.cells, lr, lg, lb);
-                }
-                cr *= lr; cg *= lg; cb *= lb;
-            }
-            float depth = 0.0f;
-            if (want_depth) {  // camera.go:1744-1812
-                depth = (Z + cam.margin) / cam.spread;
-                if (depth < 0.0f) depth = 0.0f;
-                else if (depth > 1.0f) depth = 1.0f;
-                if (!cam.render_depth) {
-                    const float fd = cam.fog_range[0] + ((cam.fog_range[1] - cam.fog_range[0]) * 1.0f - depth);
-                    if (cam.fog_mode == T3D_FOG_ADD) {
-                        cr += cam.fog_color[0] * fd; cg += cam.fog_color[1] * fd; cb += cam.fog_color[2] * fd;
-                    } else if (cam.fog_mode == T3D_FOG_SUB) {
-                        cr *= cam.fog_color[0] * fd; cg *= cam.fog_color[1] * fd; cb *= cam.fog_color[2] * fd;
-                    }
-                }
-            }
-            const uint32_t o = seg.vscratch + lv;
-            P.vcull[o] = make_float4(cx, cy, Z, depth);
-            P.vxyuv[o] = make_float4(dx, dy, uvU, uvV);
-            P.vrgba[o] = make_float4(cr, cg, cb, ca);
         }
+        SLight& d = ms.lights[k];
+        d.type = L.type;
+        d.skip = (L.type == T3D_LIGHT_POINT && w.w != 0.0f) ? 1 : 0;
+        d.cr = L.color[0]; d.cg = L.color[1]; d.cb = L.color[2];
+        d.energy = L.energy; d.range = L.range; d.range2 = L.range2;
+        if (L.type == T3D_LIGHT_POINT) { d.x = w.x; d.y = w.y; d.z = w.z; }
+        else if (L.type == T3D_LIGHT_AMBIENT) { d.x = L.amb[0]; d.y = L.amb[1]; d.z = L.amb[2]; }
+        else { d.x = L.fwd[0]; d.y = L.fwd[1]; d.z = L.fwd[2]; }
+        d.vol = &L;
+    }
+    // drop model-level skipped point lights, keeping list order (the per-vertex
+    // sums run over the remaining lights in the same sequence)
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const uint32_t lane = threadIdx.x;
+        uint32_t out = 0;
+        for (uint32_t k0 = 0; k0 < nl; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            SLight rec;
+            bool keep = false;
+            if (k < nl) {
+                rec = ms.lights[k];
+                keep = !rec.skip;
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+            __syncwarp();
+            if (keep) ms.lights[out + __popc(bal & ((1u << lane) - 1u))] = rec;
+            out += __popc(bal);
+            __syncwarp();
+        }
+        if (lane == 0) ms.nl = out;
     }
 }
 
-// --------------------------------------------------------- P2 .. P5 ----
-struct TileSmem {
-    uint32_t item, nvis, warp_tot[kMaxWarps], scan_tmp[kMaxWarps];
-    float wmin[kMaxWarps], wmax[kMaxWarps];
-    uint32_t bins_walk[kBins];     // per-bin counts / bases in walk order
-    uint32_t whist[kMaxWarps * kBins];
-    // followed by: uint16 lidx[tile], float depth[tile], uint16 bin[tile]
-};
-
-__device__ __forceinline__ uint16_t* tile_lidx(unsigned char* smem) { return (uint16_t*)(smem + sizeof(TileSmem)); }
-__device__ __forceinline__ float* tile_depth(unsigned char* smem, uint32_t tile) {
-    return (float*)(smem + sizeof(TileSmem) + 2 * (size_t)tile);
+// MultVecW (model.go:808-811) of one model-space vertex by the staged MVP columns.
+__device__ __forceinline__ float4 clip_of(const float4* mc, float x, float y, float z) {
+    float4 c;
+    const float4 a = mc[0], b = mc[1], d = mc[2], e = mc[3];
+    c.x = a.x * x + a.y * y + a.z * z + a.w;
+    c.y = b.x * x + b.y * y + b.z * z + b.w;
+    c.z = d.x * x + d.y * y + d.z * z + d.w;
+    c.w = e.x * x + e.y * y + e.z * z + e.w;
+    return c;
 }
-__device__ __forceinline__ uint16_t* tile_bin(unsigned char* smem, uint32_t tile) {
-    return (uint16_t*)(smem + sizeof(TileSmem) + 6 * (size_t)tile);
+
+// The emitted corner of one vertex (camera.go:1655-1812): screen position,
+// UV, colour (vertex colour * model/material colour * light) and depth.
+__device__ __forceinline__ void emit_corner(const ModelSmem& ms, uint32_t v, float4& xyuv, float4& rgba,
+                                            float& depth_out) {
+    const EmitConst& e = ms.ec;
+    const uint32_t f = e.flags;
+    const float4 a = e.va[v];
+    const float4 b = e.vb[v];
+    const float4 c = clip_of(ms.mvpc, a.x, a.y, a.z);
+    float w = c.w;
+    if (!(f & EC_PERSP)) w = 1.0f;
+    if (w < 0.0f) w = 0.001f;
+    xyuv.x = (c.x / w) * e.W + e.halfW;
+    xyuv.y = (c.y / -w) * e.H + e.halfH;
+    if (f & EC_PCORRECT) {
+        xyuv.z = (b.z / w) * e.tex_w;
+        xyuv.w = ((1.0f - b.w) / w) * e.tex_h;
+    } else {
+        xyuv.z = b.z * e.tex_w;
+        xyuv.w = (1.0f - b.w) * e.tex_h;
+    }
+    float cr, cg, cb, ca;
+    if (f & EC_COLORS) {
+        const float4 k = e.vc[v];
+        cr = k.x * e.mp[0]; cg = k.y * e.mp[1]; cb = k.z * e.mp[2]; ca = k.w * e.mp[3];
+    } else {
+        cr = e.mp[0]; cg = e.mp[1]; cb = e.mp[2]; ca = e.mp[3];
+    }
+    if (f & EC_LIT) {
+        const f3 vert = mk3(a.x, a.y, a.z);
+        const f3 vnrm = mk3(a.w, b.x, b.y);
+        float lr = 0.0f, lg = 0.0f, lb = 0.0f;
+        const uint32_t nl = ms.nl;
+        for (uint32_t k = 0; k < nl; k++)
+            light_vertex(ms.lights[k], e.seg_flags, vert, vnrm, ms.M, ms.dirrot, e.cells, lr, lg, lb);
+        cr *= lr; cg *= lg; cb *= lb;
+    }
+    float depth = 0.0f;
+    if (f & EC_DEPTH) {
+        depth = (c.z + e.margin) / e.spread;
+        if (depth < 0.0f) depth = 0.0f;
+        else if (depth > 1.0f) depth = 1.0f;
+        if (f & (EC_FOG_ADD | EC_FOG_SUB)) {
+            const float fd = e.fog0 + (e.fogspan * 1.0f - depth);
+            if (f & EC_FOG_ADD) {
+                cr += e.fog_r * fd; cg += e.fog_g * fd; cb += e.fog_b * fd;
+            } else {
+                cr *= e.fog_r * fd; cg *= e.fog_g * fd; cb *= e.fog_b * fd;
+            }
+        }
+    }
+    rgba = make_float4(cr, cg, cb, ca);
+    depth_out = depth;
 }
 
 __device__ __forceinline__ uint32_t walk_pos(uint32_t b, uint32_t sort_mode) {
@@ -447,7 +522,7 @@ __device__ __forceinline__ float range_of(float mn, float mx) {
     return r;
 }
 
-// In-place exclusive scan of bins_walk[0..kBins) by the whole block.
+// In-place exclusive scan of ts.bins_walk[0..kBins) by the whole block.
 __device__ void scan_bins(TileSmem& sm) {
     __syncthreads();
     const uint32_t per = (kBins + blockDim.x - 1) / blockDim.x;
@@ -472,31 +547,45 @@ __device__ void scan_bins(TileSmem& sm) {
     __syncthreads();
 }
 
-// Stable placement of a tile's n visible triangles (in triangle order in smem)
-// and their emission. bins_walk holds, in walk order, the first output
-// position of each bin for this tile (within the segment).
-__device__ void rank_and_emit(const FrameParams& P, const DevSeg& seg, const DevJob& J, unsigned char* smem,
-                              uint32_t tile_tris, uint32_t t0, uint32_t n, uint32_t sort_mode) {
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem);
-    const uint16_t* lidx = tile_lidx(smem);
-    const uint16_t* bins = tile_bin(smem, tile_tris);
+// Stable placement of a tile's n visible triangles (in triangle order in
+// shared memory, bins already computed) and their emission. bins_walk holds,
+// in walk order, the first output position of each bin for this tile.
+// Corner c of triangle t written to output corner 3*slot + c (camera.go:1646-1820).
+// One thread per corner: consecutive threads write consecutive corners.
+__device__ __forceinline__ void emit_corner_at(const FrameParams& P, const ModelSmem& ms, uint32_t t, uint32_t c,
+                                               size_t corner) {
+    const uint32_t v = ms.ec.idx[3 * t + c];
+    float4 x, r;
+    float d;
+    emit_corner(ms, v, x, r, d);
+    P.out_xyuv[corner] = x;
+    P.out_rgba[corner] = r;
+    P.out_depth[corner] = d;
+}
+
+// Stable ranking of a tile's visible list (bins computed, in triangle order).
+// Warp w owns entries [ts.wlo[w], ts.whi[w]); the ranges follow each other in
+// triangle order. bins_walk holds, in walk order, the first output position of
+// each bin for this tile. Single-tile segments record perm[pos] = entry;
+// multi-tile segments record order[out_base + pos] = segment-relative triangle.
+__device__ void rank_tile(const FrameParams& P, const DevSeg& seg, const SmemLayout& L, uint32_t sort_mode,
+                          bool single, uint32_t tile_off) {
+    TileSmem& sm = *L.ts;
     const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t chunk = (n + nw - 1) / nw;
-    const uint32_t lo = min(n, wid * chunk), hi = min(n, lo + chunk);
-    for (uint32_t i = threadIdx.x; i < nw * kBins; i += blockDim.x) sm.whist[i] = 0u;
+    const uint32_t lo = sm.wlo[wid], hi = sm.whi[wid];
+    for (uint32_t i = threadIdx.x; i < nw * kBins; i += blockDim.x) L.whist[i] = 0u;
     __syncthreads();
-    for (uint32_t j = lo + lane; j < hi; j += 32) atomicAdd(&sm.whist[wid * kBins + bins[j]], 1u);
+    for (uint32_t j = lo + lane; j < hi; j += 32) atomicAdd(&L.whist[wid * kBins + L.bin[j]], 1u);
     __syncthreads();
     for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
         uint32_t run = sm.bins_walk[walk_pos(b, sort_mode)];
         for (uint32_t w = 0; w < nw; w++) {
-            uint32_t t = sm.whist[w * kBins + b];
-            sm.whist[w * kBins + b] = run;
+            uint32_t t = L.whist[w * kBins + b];
+            L.whist[w * kBins + b] = run;
             run += t;
         }
     }
     __syncthreads();
-    const uint32_t mesh_tbase = J.meshes[seg.mesh].tbase;
     const uint32_t lt = (1u << lane) - 1u;
     for (uint32_t j0 = lo; j0 < hi; j0 += 32) {
         const uint32_t j = j0 + lane;
@@ -504,37 +593,66 @@ __device__ void rank_and_emit(const FrameParams& P, const DevSeg& seg, const Dev
         const uint32_t mask = __ballot_sync(0xffffffffu, active);
         uint32_t b = 0, peers = 0, pos = 0;
         if (active) {
-            b = bins[j];
+            b = L.bin[j];
             peers = __match_any_sync(mask, b);
-            pos = sm.whist[wid * kBins + b] + __popc(peers & lt);
+            pos = L.whist[wid * kBins + b] + __popc(peers & lt);
         }
         __syncwarp();
-        if (active && lane == (uint32_t)(__ffs(peers) - 1)) sm.whist[wid * kBins + b] += __popc(peers);
+        if (active && lane == (uint32_t)(__ffs(peers) - 1)) L.whist[wid * kBins + b] += __popc(peers);
         __syncwarp();
         if (active) {
-            const uint32_t t = t0 + lidx[j];  // mesh-absolute triangle
-            const uint32_t* ip = J.idx + 3 * (size_t)(mesh_tbase + t);
-            const size_t slot = (size_t)seg.out_base + pos;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const uint32_t o = seg.vscratch + (ip[c] - seg.vmin);
-                P.out_xyuv[3 * slot + c] = P.vxyuv[o];
-                P.out_rgba[3 * slot + c] = P.vrgba[o];
-                P.out_depth[3 * slot + c] = P.vcull[o].w;
-            }
+            if (single) L.perm[pos] = (uint16_t)j;
+            else P.order[(size_t)seg.out_base + pos] = tile_off + L.lidx[j];
         }
     }
+    __syncthreads();
 }
 
-__device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem);
+// ProcessVertices' rejection tests and depth key for one triangle whose
+// model-space corners are a, b, c (model.go:855-969).
+__device__ __forceinline__ bool tri_visible(const float4* mvp, float nearp, float farp, bool backface, f3 ic, float4 pa,
+                                            float4 pb, float4 pc, float& depth) {
+    const float4 c0 = clip_of(mvp, pa.x, pa.y, pa.z);
+    const float4 c1 = clip_of(mvp, pb.x, pb.y, pb.z);
+    const float4 c2 = clip_of(mvp, pc.x, pc.y, pc.z);
+    // near/far: some corner with Z + 1 >= near && Z < far (model.go:855-886)
+    if (!((c0.z + 1.0f >= nearp && c0.z < farp) || (c1.z + 1.0f >= nearp && c1.z < farp) ||
+          (c2.z + 1.0f >= nearp && c2.z < farp)))
+        return false;
+    const float w0 = c0.w < 0.0f ? 0.000001f : c0.w;
+    const float w1 = c1.w < 0.0f ? 0.000001f : c1.w;
+    const float w2 = c2.w < 0.0f ? 0.000001f : c2.w;
+    const float x0 = c0.x / w0, y0 = c0.y / w0;
+    const float x1 = c1.x / w1, y1 = c1.y / w1;
+    const float x2 = c2.x / w2, y2 = c2.y / w2;
+    // wholly off one side of the screen (model.go:890-898)
+    if ((x0 < -0.5f && x1 < -0.5f && x2 < -0.5f) || (x0 > 0.5f && x1 > 0.5f && x2 > 0.5f) ||
+        (y0 < -0.5f && y1 < -0.5f && y2 < -0.5f) || (y0 > 0.5f && y1 > 0.5f && y2 > 0.5f))
+        return false;
+    if (backface) {  // 2D cross product (model.go:902-925)
+        const float n0x = x0 - x1, n0y = y0 - y1;
+        const float n1x = x1 - x2, n1y = y1 - y2;
+        const float nor = (n0x * n1y) - (n1x * n0y);
+        if (nor < 0.0f) return false;
+    }
+    // tri.Center (mesh.go:1980-1982) and the squared distance key (model.go:950-953)
+    const float cxx = (pa.x + pb.x + pc.x) / 3.0f;
+    const float cyy = (pa.y + pb.y + pc.y) / 3.0f;
+    const float czz = (pa.z + pb.z + pc.z) / 3.0f;
+    const float ddx = ic.x - cxx, ddy = ic.y - cyy, ddz = ic.z - czz;
+    depth = ddx * ddx + ddy * ddy + ddz * ddz;
+    return !(isnan(depth) || isinf(depth));
+}
+
+// P1: visibility and depth keys per tile; single-tile segments are sorted and
+// emitted right here, multi-tile segments leave their visible list in HBM.
+__device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
-    uint16_t* lidx = tile_lidx(smem);
-    float* dep = tile_depth(smem, T);
-    uint16_t* bins = tile_bin(smem, T);
+    const SmemLayout L = smem_layout(smem, T);
+    TileSmem& sm = *L.ts;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (;;) {
-        const uint32_t item = P.tile_begin + next_item(P.ctl, 2, &sm.item);
+        const uint32_t item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
         if (item >= P.tile_end) break;
         const uint32_t s = P.tile_seg[item];
         const DevSeg seg = P.segs[s];
@@ -547,6 +665,7 @@ __device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
             continue;
         }
         const DevJob& J = P.jobs[seg.job];
+        stage_model(P, seg, J, *L.ms);
         const JobCam& cam = J.cam;
         const float nearp = cam.near_, farp = cam.far_;
         const bool backface = seg.flags & SEG_BACKFACE;
@@ -554,70 +673,62 @@ __device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
         const DevMesh me = J.meshes[seg.mesh];
         const uint32_t t0 = seg.tri_start + tile * T;
         const uint32_t t1 = min(seg.tri_start + seg.tri_count, t0 + T);
-        if (threadIdx.x == 0) sm.nvis = 0u;
         float lmin = 3.402823466e38f, lmax = 0.0f;
         __syncthreads();
-        for (uint32_t base = t0; base < t1; base += blockDim.x) {
-            const uint32_t t = base + threadIdx.x;
-            bool vis = false;
-            float depth = 0.0f;
-            if (t < t1) {
-                const uint32_t* ip = J.idx + 3 * (size_t)(me.tbase + t);
-                const uint32_t i0 = ip[0], i1 = ip[1], i2 = ip[2];
-                const float4 c0 = P.vcull[seg.vscratch + (i0 - seg.vmin)];
-                const float4 c1 = P.vcull[seg.vscratch + (i1 - seg.vmin)];
-                const float4 c2 = P.vcull[seg.vscratch + (i2 - seg.vmin)];
-                // model.go:857-925
-                const bool inb = (c0.z + 1.0f >= nearp && c0.z < farp) || (c1.z + 1.0f >= nearp && c1.z < farp) ||
-                                 (c2.z + 1.0f >= nearp && c2.z < farp);
-                vis = inb;
-                if (vis && ((c0.x < -0.5f && c1.x < -0.5f && c2.x < -0.5f) || (c0.x > 0.5f && c1.x > 0.5f && c2.x > 0.5f) ||
-                            (c0.y < -0.5f && c1.y < -0.5f && c2.y < -0.5f) || (c0.y > 0.5f && c1.y > 0.5f && c2.y > 0.5f)))
-                    vis = false;
-                if (vis && backface) {
-                    const float n0x = c0.x - c1.x, n0y = c0.y - c1.y;
-                    const float n1x = c1.x - c2.x, n1y = c1.y - c2.y;
-                    const float nor = (n0x * n1y) - (n1x * n0y);
-                    if (nor < 0.0f) vis = false;
-                }
-                if (vis) {  // tri.Center (mesh.go:1980-1982) and the depth key (model.go:950-953)
-                    const float4 pa = J.va[me.vbase + i0];
-                    const float4 pb = J.va[me.vbase + i1];
-                    const float4 pc = J.va[me.vbase + i2];
-                    const float cxx = (pa.x + pb.x + pc.x) / 3.0f;
-                    const float cyy = (pa.y + pb.y + pc.y) / 3.0f;
-                    const float czz = (pa.z + pb.z + pc.z) / 3.0f;
-                    const float ddx = ic.x - cxx, ddy = ic.y - cyy, ddz = ic.z - czz;
-                    depth = ddx * ddx + ddy * ddy + ddz * ddz;
-                    if (isnan(depth) || isinf(depth)) vis = false;
-                }
+        const float4* mvp = L.ms->mvpc;
+        // each warp compacts its own contiguous quarter/eighth of the tile
+        const uint32_t per = T / nw;
+        const uint32_t wt0 = t0 + wid * per, wt1 = min(t1, wt0 + per);
+        const uint32_t wbase = wid * per;
+        uint32_t cnt = 0;
+        const uint32_t lt = (1u << lane) - 1u;
+        // two triangles per lane per step (t and t + 32): both gathers are in flight together
+        for (uint32_t tb = wt0; tb < wt1; tb += 64) {
+            const uint32_t ta = tb + lane, tb2 = tb + 32 + lane;
+            const bool ha = ta < wt1, hb = tb2 < wt1;
+            uint32_t ia0 = 0, ia1 = 0, ia2 = 0, ib0 = 0, ib1 = 0, ib2 = 0;
+            if (ha) { const uint32_t* ip = J.idx + 3 * (size_t)(me.tbase + ta); ia0 = ip[0]; ia1 = ip[1]; ia2 = ip[2]; }
+            if (hb) { const uint32_t* ip = J.idx + 3 * (size_t)(me.tbase + tb2); ib0 = ip[0]; ib1 = ip[1]; ib2 = ip[2]; }
+            float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f), pa1 = pa0, pa2 = pa0, pb0 = pa0, pb1 = pa0, pb2 = pa0;
+            if (ha) { pa0 = J.va[me.vbase + ia0]; pa1 = J.va[me.vbase + ia1]; pa2 = J.va[me.vbase + ia2]; }
+            if (hb) { pb0 = J.va[me.vbase + ib0]; pb1 = J.va[me.vbase + ib1]; pb2 = J.va[me.vbase + ib2]; }
+            float da = 0.0f, db = 0.0f;
+            const bool va_ = ha && tri_visible(mvp, nearp, farp, backface, ic, pa0, pa1, pa2, da);
+            const bool vb_ = hb && tri_visible(mvp, nearp, farp, backface, ic, pb0, pb1, pb2, db);
+            const uint32_t bala = __ballot_sync(0xffffffffu, va_);
+            const uint32_t balb = __ballot_sync(0xffffffffu, vb_);
+            if (va_) {
+                const uint32_t p = wbase + cnt + __popc(bala & lt);
+                L.lidx[p] = (uint16_t)(ta - t0);
+                L.depth[p] = da;
+                lmin = fminf(lmin, da);
+                lmax = fmaxf(lmax, da);
             }
-            // stable compaction in triangle order
-            const uint32_t bal = __ballot_sync(0xffffffffu, vis);
-            if (lane == 0) sm.warp_tot[wid] = __popc(bal);
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                uint32_t run = sm.nvis;
-                for (uint32_t w = 0; w < nw; w++) { uint32_t c = sm.warp_tot[w]; sm.scan_tmp[w] = run; run += c; }
-                sm.nvis = run;
+            cnt += __popc(bala);
+            if (vb_) {
+                const uint32_t p = wbase + cnt + __popc(balb & lt);
+                L.lidx[p] = (uint16_t)(tb2 - t0);
+                L.depth[p] = db;
+                lmin = fminf(lmin, db);
+                lmax = fmaxf(lmax, db);
             }
-            __syncthreads();
-            if (vis) {
-                const uint32_t p = sm.scan_tmp[wid] + __popc(bal & ((1u << lane) - 1u));
-                lidx[p] = (uint16_t)(t - t0);
-                dep[p] = depth;
-                lmin = fminf(lmin, depth);
-                lmax = fmaxf(lmax, depth);
-            }
+            cnt += __popc(balb);
         }
         // block min / max of the visible depths
         for (int o = 16; o > 0; o >>= 1) {
             lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
             lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
         }
-        if (lane == 0) { sm.wmin[wid] = lmin; sm.wmax[wid] = lmax; }
+        if (lane == 0) {
+            sm.wmin[wid] = lmin;
+            sm.wmax[wid] = lmax;
+            sm.wlo[wid] = wbase;
+            sm.whi[wid] = wbase + cnt;
+            sm.warp_tot[wid] = cnt;
+        }
         __syncthreads();
-        const uint32_t n = sm.nvis;
+        uint32_t n = 0;
+        for (uint32_t w = 0; w < nw; w++) n += sm.warp_tot[w];
         float mn = sm.wmin[0], mx = sm.wmax[0];
         for (uint32_t w = 1; w < nw; w++) { mn = fminf(mn, sm.wmin[w]); mx = fmaxf(mx, sm.wmax[w]); }
         const uint32_t sort_mode = seg_sort_mode(seg.flags);
@@ -626,22 +737,29 @@ __device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
                 const float range = range_of(mn, mx);
                 for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) sm.bins_walk[b] = 0u;
                 __syncthreads();
-                for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-                    const uint32_t b = bin_of(dep[j], mn, range, sort_mode);
-                    bins[j] = (uint16_t)b;
+                for (uint32_t j = wbase + lane; j < wbase + cnt; j += 32) {
+                    const uint32_t b = bin_of(L.depth[j], mn, range, sort_mode);
+                    L.bin[j] = (uint16_t)b;
                     atomicAdd(&sm.bins_walk[walk_pos(b, sort_mode)], 1u);
                 }
                 scan_bins(sm);
-                rank_and_emit(P, seg, J, smem, T, t0, n, sort_mode);
+                rank_tile(P, seg, L, sort_mode, true, 0);
+                const size_t base = 3 * (size_t)seg.out_base;
+                for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {
+                    const uint32_t r = q / 3u, c = q - 3u * r;
+                    emit_corner_at(P, *L.ms, t0 + L.lidx[L.perm[r]], c, base + q);
+                }
             }
             if (threadIdx.x == 0) {
                 P.seg_count[s] = n;
                 if (n) atomicAdd(&P.accum[0], (unsigned long long)n);
             }
         } else {
-            uint32_t* gi = P.vis_idx + (size_t)mt * T;
+            uint16_t* gi = P.vis_idx + (size_t)mt * T;
             float* gd = P.vis_depth + (size_t)mt * T;
-            for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) { gi[j] = lidx[j]; gd[j] = dep[j]; }
+            uint32_t off = 0;
+            for (uint32_t w = 0; w < wid; w++) off += sm.warp_tot[w];
+            for (uint32_t k = lane; k < cnt; k += 32) { gi[off + k] = L.lidx[wbase + k]; gd[off + k] = L.depth[wbase + k]; }
             if (threadIdx.x == 0) {
                 P.tile_count[mt] = n;
                 if (n > 0) {
@@ -656,15 +774,17 @@ __device__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
     }
 }
 
-__device__ void phase_hist(const FrameParams& P, unsigned char* smem) {
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem);
+// P2: bin histograms of the tiles of multi-tile segments.
+__device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
+    const SmemLayout L = smem_layout(smem, T);
+    TileSmem& sm = *L.ts;
     for (;;) {
-        const uint32_t i = P.mt_tile_begin + next_item(P.ctl, 3, &sm.item);
+        const uint32_t i = P.mt_tile_begin + next_item(P.ctl, 2, &sm.item);
         if (i >= P.mt_tile_end) break;
         const uint32_t g = P.mt_tiles[i];
         const uint32_t s = P.tile_seg[g];
-        const DevSeg seg = P.segs[s];
+        const uint32_t flags = P.segs[s].flags;
         const uint32_t n = __ldcg(&P.tile_count[i]);
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) sm.bins_walk[b] = 0u;
         __syncthreads();
@@ -672,8 +792,9 @@ __device__ void phase_hist(const FrameParams& P, unsigned char* smem) {
             const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
             const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
             const float range = range_of(mn, mx);
-            const uint32_t sort_mode = seg_sort_mode(seg.flags);
+            const uint32_t sort_mode = seg_sort_mode(flags);
             const float* gd = P.vis_depth + (size_t)i * T;
+#pragma unroll 4
             for (uint32_t j = threadIdx.x; j < n; j += blockDim.x)
                 atomicAdd(&sm.bins_walk[bin_of(__ldcg(&gd[j]), mn, range, sort_mode)], 1u);
         }
@@ -682,88 +803,150 @@ __device__ void phase_hist(const FrameParams& P, unsigned char* smem) {
     }
 }
 
-__device__ void phase_scan(const FrameParams& P, unsigned char* smem) {
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem);
+// P3: per multi-tile segment, turn tile histograms into per-tile bin bases.
+__device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* smem) {
+    const SmemLayout L = smem_layout(smem, P.tile_tris);
+    TileSmem& sm = *L.ts;
     for (;;) {
-        const uint32_t k = P.mt_seg_begin + next_item(P.ctl, 4, &sm.item);
+        const uint32_t k = P.mt_seg_begin + next_item(P.ctl, 3, &sm.item);
         if (k >= P.mt_seg_end) break;
         const uint32_t s = P.mt_segs[k];
         const DevSeg seg = P.segs[s];
         const uint32_t sort_mode = seg_sort_mode(seg.flags);
+        const uint32_t* hbase = P.tile_hist + (size_t)seg.mt_first * kBins;
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
             uint32_t tot = 0;
-            for (uint32_t t = 0; t < seg.ntiles; t++) tot += __ldcg(&P.tile_hist[(size_t)(seg.mt_first + t) * kBins + b]);
+            uint32_t t = 0;
+            for (; t + 8 <= seg.ntiles; t += 8) {  // 8 independent loads in flight
+                uint32_t v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) v[u] = __ldcg(&hbase[(size_t)(t + u) * kBins + b]);
+#pragma unroll
+                for (int u = 0; u < 8; u++) tot += v[u];
+            }
+            for (; t < seg.ntiles; t++) tot += __ldcg(&hbase[(size_t)t * kBins + b]);
             sm.bins_walk[walk_pos(b, sort_mode)] = tot;
         }
         scan_bins(sm);
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
             uint32_t run = sm.bins_walk[walk_pos(b, sort_mode)];
-            for (uint32_t t = 0; t < seg.ntiles; t++) {
-                uint32_t* h = &P.tile_hist[(size_t)(seg.mt_first + t) * kBins + b];
-                uint32_t c = __ldcg(h);
-                *h = run;
+            uint32_t t = 0;
+            uint32_t* h = P.tile_hist + (size_t)seg.mt_first * kBins + b;
+            for (; t + 8 <= seg.ntiles; t += 8) {
+                uint32_t v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) v[u] = __ldcg(&h[(size_t)(t + u) * kBins]);
+#pragma unroll
+                for (int u = 0; u < 8; u++) { h[(size_t)(t + u) * kBins] = run; run += v[u]; }
+            }
+            for (; t < seg.ntiles; t++) {
+                const uint32_t c = __ldcg(&h[(size_t)t * kBins]);
+                h[(size_t)t * kBins] = run;
                 run += c;
             }
         }
     }
 }
 
-__device__ void phase_emit_multi(const FrameParams& P, unsigned char* smem) {
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem);
+// P4: stable rank of the tiles of multi-tile segments into the order array.
+__device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
-    uint16_t* lidx = tile_lidx(smem);
-    uint16_t* bins = tile_bin(smem, T);
+    const SmemLayout L = smem_layout(smem, T);
+    TileSmem& sm = *L.ts;
     for (;;) {
-        const uint32_t i = P.mt_tile_begin + next_item(P.ctl, 5, &sm.item);
+        const uint32_t i = P.mt_tile_begin + next_item(P.ctl, 4, &sm.item);
         if (i >= P.mt_tile_end) break;
         const uint32_t g = P.mt_tiles[i];
         const uint32_t s = P.tile_seg[g];
         const DevSeg seg = P.segs[s];
         const uint32_t n = __ldcg(&P.tile_count[i]);
         if (n == 0) continue;
-        const DevJob& J = P.jobs[seg.job];
         const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
         const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
         const float range = range_of(mn, mx);
         const uint32_t sort_mode = seg_sort_mode(seg.flags);
-        const uint32_t* gi = P.vis_idx + (size_t)i * T;
+        const uint16_t* gi = P.vis_idx + (size_t)i * T;
         const float* gd = P.vis_depth + (size_t)i * T;
         for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            lidx[j] = (uint16_t)__ldcg(&gi[j]);
-            bins[j] = (uint16_t)bin_of(__ldcg(&gd[j]), mn, range, sort_mode);
+            L.lidx[j] = __ldcg(&gi[j]);
+            L.bin[j] = (uint16_t)bin_of(__ldcg(&gd[j]), mn, range, sort_mode);
         }
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x)
             sm.bins_walk[walk_pos(b, sort_mode)] = __ldcg(&P.tile_hist[(size_t)i * kBins + b]);
+        if (threadIdx.x < (blockDim.x >> 5)) {
+            const uint32_t chunk = (n + (blockDim.x >> 5) - 1) / (blockDim.x >> 5);
+            sm.wlo[threadIdx.x] = min(n, threadIdx.x * chunk);
+            sm.whi[threadIdx.x] = min(n, threadIdx.x * chunk + chunk);
+        }
         __syncthreads();
-        const uint32_t tile = g - seg.tile_first;
-        rank_and_emit(P, seg, J, smem, T, seg.tri_start + tile * T, n, sort_mode);
+        rank_tile(P, seg, L, sort_mode, false, (g - seg.tile_first) * T);
     }
 }
 
-__global__ void __launch_bounds__(512) t3d_frame_kernel(const FrameParams P) {
+// P5: emit multi-tile segments in output order, tile_tris slots per work item.
+__device__ __noinline__ void phase_emit_multi(const FrameParams& P, unsigned char* smem) {
+    const uint32_t E = P.tile_tris;
+    const SmemLayout L = smem_layout(smem, E);
+    TileSmem& sm = *L.ts;
+    for (;;) {
+        const uint32_t k = P.emit_begin + next_item(P.ctl, 5, &sm.item);
+        if (k >= P.emit_end) break;
+        const uint32_t s = P.emit_seg[k];
+        const uint32_t r0 = P.emit_chunk[k] * E;
+        const uint32_t n = __ldcg(&P.seg_count[s]);
+        if (r0 >= n) continue;
+        const DevSeg seg = P.segs[s];
+        const DevJob& J = P.jobs[seg.job];
+        stage_model(P, seg, J, *L.ms);
+        __syncthreads();
+        const uint32_t r1 = min(n, r0 + E);
+        const uint32_t* __restrict__ ord = P.order + seg.out_base;
+        const size_t base = 3 * (size_t)seg.out_base;
+        for (uint32_t q = 3 * r0 + threadIdx.x; q < 3 * r1; q += blockDim.x) {
+            const uint32_t r = q / 3u, c = q - 3u * r;
+            emit_corner_at(P, *L.ms, seg.tri_start + __ldcg(&ord[r]), c, base + q);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Records when the last block finished phase k (kernel start in slot 7).
+__device__ __forceinline__ void phase_done(Ctl* ctl, int k) {
+    if (threadIdx.x == 0) atomicMax(&ctl->t_end[k], global_ns());
+}
+
+__global__ void __launch_bounds__(256, 4) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl->t_end[7] = global_ns();
     phase_prep(P);
-    if (!grid_barrier(P.ctl)) return;
-    phase_vertex(P, smem);
+    phase_done(P.ctl, 0);
     if (!grid_barrier(P.ctl)) return;
     phase_triangles(P, smem);
+    phase_done(P.ctl, 1);
     if (!P.has_multi) return;
     if (!grid_barrier(P.ctl)) return;
     phase_hist(P, smem);
+    phase_done(P.ctl, 2);
     if (!grid_barrier(P.ctl)) return;
     phase_scan(P, smem);
+    phase_done(P.ctl, 3);
+    if (!grid_barrier(P.ctl)) return;
+    phase_rank_multi(P, smem);
+    phase_done(P.ctl, 4);
     if (!grid_barrier(P.ctl)) return;
     phase_emit_multi(P, smem);
+    phase_done(P.ctl, 5);
 }
-
-size_t tile_smem_bytes(uint32_t tile_tris) { return sizeof(TileSmem) + 8 * (size_t)tile_tris; }
-size_t vertex_smem_bytes() { return sizeof(VertexSmem); }
 
 }  // namespace t3d
 
 // Launch entry used by the runtime (same translation-unit linkage).
 extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel; }
-extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris) {
-    size_t a = t3d::tile_smem_bytes(tile_tris), b = t3d::vertex_smem_bytes();
-    return a > b ? a : b;
+extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads) {
+    return sizeof(t3d::ModelSmem) + sizeof(t3d::TileSmem) + 4ull * (block_threads / 32) * t3d::kBins +
+           10ull * tile_tris + 16;
 }

@@ -25,7 +25,7 @@
 #include "t3d_runtime.h"
 
 extern "C" const void* t3d_frame_kernel_ptr();
-extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris);
+extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads);
 
 namespace t3d {
 
@@ -381,7 +381,7 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
 int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate) {
     FrameTables& F = ctx->tables;
     F.clear();
-    const uint32_t T = ctx->tile_tris, VC = ctx->vchunk;
+    const uint32_t T = ctx->tile_tris;
     for (uint32_t j = 0; j < njobs; j++) {
         auto it = ctx->scene_map().find(jobs[j].scene);
         if (it == ctx->scene_map().end()) {
@@ -494,8 +494,6 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 sg.mp[0] *= mat.color[0]; sg.mp[1] *= mat.color[1]; sg.mp[2] *= mat.color[2]; sg.mp[3] *= mat.color[3];
                 sg.tex_w = mat.tex_w; sg.tex_h = mat.tex_h;
             }
-            sg.vscratch = (uint32_t)F.nscratch;
-            F.nscratch += sg.vcount;
             sg.out_base = (uint32_t)F.nslots;
             F.nslots += sg.tri_count;
             uint32_t ntiles = (sg.tri_count + T - 1) / T;
@@ -510,9 +508,9 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 F.mt_segs.push_back(s);
             }
             for (uint32_t t = 0; t < ntiles; t++) F.tile_seg.push_back(s);
-            uint32_t nch = (sg.vcount + VC - 1) / VC;
-            F.seg_vitem_first.push_back((uint32_t)F.vitem_seg.size());
-            for (uint32_t c = 0; c < nch; c++) { F.vitem_seg.push_back(s); F.vitem_chunk.push_back(c); }
+            F.seg_emit_first.push_back((uint32_t)F.emit_seg.size());
+            if (ntiles > 1)
+                for (uint32_t c = 0; c < ntiles; c++) { F.emit_seg.push_back(s); F.emit_chunk.push_back(c); }
             sg.flags = flags;
             F.segs.push_back(sg);
             t3d_segment_info si;
@@ -550,11 +548,11 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     size_t o_insts = add(F.insts.data(), bytes_of(F.insts));
     size_t o_ili = add(F.inst_light_idx.data(), bytes_of(F.inst_light_idx));
     size_t o_segs = add(F.segs.data(), bytes_of(F.segs));
-    size_t o_vis = add(F.vitem_seg.data(), bytes_of(F.vitem_seg));
-    size_t o_vic = add(F.vitem_chunk.data(), bytes_of(F.vitem_chunk));
     size_t o_ts = add(F.tile_seg.data(), bytes_of(F.tile_seg));
     size_t o_mtt = add(F.mt_tiles.data(), bytes_of(F.mt_tiles));
     size_t o_mts = add(F.mt_segs.data(), bytes_of(F.mt_segs));
+    size_t o_es = add(F.emit_seg.data(), bytes_of(F.emit_seg));
+    size_t o_ec = add(F.emit_chunk.data(), bytes_of(F.emit_chunk));
     std::vector<DevInst> noanim(F.insts);
     for (auto& in : noanim) in.animate = 0;
     size_t o_noanim = add(noanim.data(), bytes_of(noanim));
@@ -578,31 +576,27 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.insts = (const DevInst*)(db + o_insts);
     P.inst_light_idx = (const uint32_t*)(db + o_ili);
     P.segs = (const DevSeg*)(db + o_segs);
-    P.vitem_seg = (const uint32_t*)(db + o_vis);
-    P.vitem_chunk = (const uint32_t*)(db + o_vic);
     P.tile_seg = (const uint32_t*)(db + o_ts);
     P.mt_tiles = (const uint32_t*)(db + o_mtt);
     P.mt_segs = (const uint32_t*)(db + o_mts);
+    P.emit_seg = (const uint32_t*)(db + o_es);
+    P.emit_chunk = (const uint32_t*)(db + o_ec);
     ctx->insts_noanim = (const DevInst*)(db + o_noanim);
     // scratch
     const size_t ninst = std::max<size_t>(1, F.insts.size()), nseg = std::max<size_t>(1, F.segs.size());
-    const size_t nmt = std::max<size_t>(1, F.mt_tiles.size()), nsc = std::max<uint64_t>(1, F.nscratch);
+    const size_t nmt = std::max<size_t>(1, F.mt_tiles.size());
     const size_t nslots = std::max<uint64_t>(1, F.nslots);
     if ((rc = ctx->preps.ensure(ctx, sizeof(DevPrep) * ninst)) ||
-        (rc = ctx->light_work.ensure(ctx, 16 * std::max<size_t>(1, F.inst_light_idx.size()))) ||
-        (rc = ctx->vcull.ensure(ctx, 16 * nsc)) || (rc = ctx->vxyuv.ensure(ctx, 16 * nsc)) ||
-        (rc = ctx->vrgba.ensure(ctx, 16 * nsc)) || (rc = ctx->vis_idx.ensure(ctx, 4ull * nmt * ctx->tile_tris)) ||
+        (rc = ctx->order.ensure(ctx, 4 * nslots)) ||
+        (rc = ctx->vis_idx.ensure(ctx, 2ull * nmt * ctx->tile_tris)) ||
         (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) || (rc = ctx->tile_count.ensure(ctx, 4 * nmt)) ||
         (rc = ctx->tile_hist.ensure(ctx, 4ull * kBins * nmt)) || (rc = ctx->seg_minmax.ensure(ctx, 8 * nseg)) ||
         (rc = ctx->seg_count.ensure(ctx, 4 * nseg)) || (rc = ctx->out_xyuv.ensure(ctx, 48 * nslots)) ||
         (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
         return rc;
     P.preps = (DevPrep*)ctx->preps.ptr;
-    P.inst_light_work = (float4*)ctx->light_work.ptr;
-    P.vcull = (float4*)ctx->vcull.ptr;
-    P.vxyuv = (float4*)ctx->vxyuv.ptr;
-    P.vrgba = (float4*)ctx->vrgba.ptr;
-    P.vis_idx = (uint32_t*)ctx->vis_idx.ptr;
+    P.order = (uint32_t*)ctx->order.ptr;
+    P.vis_idx = (uint16_t*)ctx->vis_idx.ptr;
     P.vis_depth = (float*)ctx->vis_depth.ptr;
     P.tile_count = (uint32_t*)ctx->tile_count.ptr;
     P.tile_hist = (uint32_t*)ctx->tile_hist.ptr;
@@ -659,12 +653,12 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         FrameParams P = P0;
         P.inst_begin = 0; P.inst_end = (uint32_t)F.insts.size();
         P.seg_begin = 0; P.seg_end = (uint32_t)F.segs.size();
-        P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
         P.tile_begin = 0; P.tile_end = (uint32_t)F.tile_seg.size();
         P.mt_tile_begin = 0; P.mt_tile_end = (uint32_t)F.mt_tiles.size();
         P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
+        P.emit_begin = 0; P.emit_end = (uint32_t)F.emit_seg.size();
         P.has_multi = F.mt_segs.empty() ? 0u : 1u;
-        uint32_t items = (uint32_t)std::max({F.vitem_seg.size(), F.tile_seg.size(), F.mt_tiles.size(),
+        uint32_t items = (uint32_t)std::max({F.tile_seg.size(), F.mt_tiles.size(),
                                              (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
         return launch_one(ctx, P, ctl, items, st);
     }
@@ -677,15 +671,15 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         FrameParams P = P0;
         P.inst_begin = sg.inst; P.inst_end = sg.inst + 1;
         P.seg_begin = (uint32_t)s; P.seg_end = (uint32_t)s + 1;
-        P.vitem_begin = F.seg_vitem_first[s];
-        P.vitem_end = (s + 1 < F.segs.size()) ? F.seg_vitem_first[s + 1] : (uint32_t)F.vitem_seg.size();
         P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
         if (sg.flags & SEG_MULTI) {
             P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles;
             P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;
+            P.emit_begin = F.seg_emit_first[s]; P.emit_end = F.seg_emit_first[s] + sg.ntiles;
             P.has_multi = 1;
         } else {
             P.mt_tile_begin = P.mt_tile_end = 0; P.mt_seg_begin = P.mt_seg_end = 0; P.has_multi = 0;
+            P.emit_begin = P.emit_end = 0;
         }
         // animation must be applied once: host tables carry the flag on the instance,
         // so later pairs of the same model use a copy without it.
@@ -694,7 +688,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
             P.insts = ctx->insts_noanim;
         }
         animated[sg.inst] = 1;
-        uint32_t items = std::max({P.vitem_end - P.vitem_begin, sg.ntiles, 1u});
+        uint32_t items = std::max(sg.ntiles, 1u);
         if ((rc = launch_one(ctx, P, ctl + s, items, st))) return rc;
     }
     return T3D_OK;

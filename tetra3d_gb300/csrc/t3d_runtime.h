@@ -66,13 +66,14 @@ struct FrameTables {
     std::vector<uint32_t> inst_light_idx;
     std::vector<DevSeg> segs;
     std::vector<t3d_segment_info> seg_info;
-    std::vector<uint32_t> seg_vitem_first, seg_mt_seg;
-    std::vector<uint32_t> vitem_seg, vitem_chunk, tile_seg, mt_tiles, mt_segs;
+    std::vector<uint32_t> seg_mt_seg;
+    std::vector<uint32_t> tile_seg, mt_tiles, mt_segs, emit_seg, emit_chunk, seg_emit_first;
     uint64_t nscratch = 0, nslots = 0;
     void clear() {
         jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
-        insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear(); seg_vitem_first.clear();
-        seg_mt_seg.clear(); vitem_seg.clear(); vitem_chunk.clear(); tile_seg.clear(); mt_tiles.clear(); mt_segs.clear();
+        insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
+        seg_mt_seg.clear(); tile_seg.clear(); mt_tiles.clear(); mt_segs.clear();
+        emit_seg.clear(); emit_chunk.clear(); seg_emit_first.clear();
         nscratch = 0; nslots = 0;
     }
 };
@@ -96,7 +97,7 @@ struct t3d_ctx {
     t3d::FrameParams params;
     const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
     t3d::HostBuf table_host, readback;
-    t3d::DevBuf table_dev, ctl, preps, light_work, vcull, vxyuv, vrgba, vis_idx, vis_depth, tile_count, tile_hist,
+    t3d::DevBuf table_dev, ctl, preps, order, vis_idx, vis_depth, tile_count, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
     uint64_t last_h2d = 0;
