@@ -184,6 +184,13 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
             torch.cuda.synchronize()
 
+    tuned = None
+    if args.tune:
+        from tetra3d_gb300 import autotune
+        best, res = autotune.tune(ctx, sid, cam, frames=5, animate=False)
+        tuned = {"tile_tris": best[0], "block_threads": best[1],
+                 "sweep_ms": {f"{t}x{b}": round(v, 4) for (t, b), v in res.items()}}
+        ctx.set_models(sid, sd)  # restore the initial transforms after the sweep
     # ---- device-resident value: captured CUDA graph of the batched frame ----
     ctx.graph_capture(sid, cam, animate=animate)
     ctx.graph_replay(args.warmup, stream=sh)
@@ -289,6 +296,7 @@ def run_ours(args, rank, world, local_rank):
             "phase_us_last_frame": {k: round(float(v), 1) for k, v in
                                     zip(("prep", "triangles", "hist", "scan", "rank", "emit"), st_last.phase_us)},
             "plain": plain,
+            "autotune": tuned,
             "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,
         }
         print(json.dumps(line))
@@ -346,6 +354,7 @@ def main():
     ap.add_argument("--workload", default="batched", choices=["batched", "terrain", "cubes", "sphere", "serving"])
     ap.add_argument("--models", type=int, default=4096, help="models in the batched scene (4096 = the full workload)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--tune", action="store_true", help="run the autotuner before the timed region")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()

@@ -452,12 +452,11 @@ __device__ __forceinline__ float4 clip_of(const float4* mc, float x, float y, fl
 
 // The emitted corner of one vertex (camera.go:1655-1812): screen position,
 // UV, colour (vertex colour * model/material colour * light) and depth.
-__device__ __forceinline__ void emit_corner(const ModelSmem& ms, uint32_t v, float4& xyuv, float4& rgba,
-                                            float& depth_out) {
+// a = (px, py, pz, nx), b = (ny, nz, u, v) of mesh vertex v.
+__device__ __forceinline__ void emit_corner(const ModelSmem& ms, uint32_t v, const float4 a, const float4 b, float4& xyuv,
+                                            float4& rgba, float& depth_out) {
     const EmitConst& e = ms.ec;
     const uint32_t f = e.flags;
-    const float4 a = e.va[v];
-    const float4 b = e.vb[v];
     const float4 c = clip_of(ms.mvpc, a.x, a.y, a.z);
     float w = c.w;
     if (!(f & EC_PERSP)) w = 1.0f;
@@ -550,17 +549,42 @@ __device__ void scan_bins(TileSmem& sm) {
 // Stable placement of a tile's n visible triangles (in triangle order in
 // shared memory, bins already computed) and their emission. bins_walk holds,
 // in walk order, the first output position of each bin for this tile.
-// Corner c of triangle t written to output corner 3*slot + c (camera.go:1646-1820).
-// One thread per corner: consecutive threads write consecutive corners.
-__device__ __forceinline__ void emit_corner_at(const FrameParams& P, const ModelSmem& ms, uint32_t t, uint32_t c,
-                                               size_t corner) {
-    const uint32_t v = ms.ec.idx[3 * t + c];
+// Writes one emitted corner (camera.go:1646-1820) at output corner index `corner`.
+__device__ __forceinline__ void store_corner(const FrameParams& P, const ModelSmem& ms, uint32_t v, const float4 a,
+                                             const float4 b, size_t corner) {
     float4 x, r;
     float d;
-    emit_corner(ms, v, x, r, d);
+    emit_corner(ms, v, a, b, x, r, d);
     P.out_xyuv[corner] = x;
     P.out_rgba[corner] = r;
     P.out_depth[corner] = d;
+}
+
+// Emits output corners [q0, q1) of a segment, one thread per corner and two
+// corners per thread per step so both dependent gather chains (triangle ->
+// vertex index -> vertex streams) are in flight together. tri_of(r) gives the
+// mesh triangle of output triangle r.
+template <typename TriOf>
+__device__ __forceinline__ void emit_corners(const FrameParams& P, const ModelSmem& ms, uint32_t q0, uint32_t q1,
+                                             size_t base, TriOf tri_of) {
+    const uint32_t* __restrict__ idx = ms.ec.idx;
+    const float4* __restrict__ va = ms.ec.va;
+    const float4* __restrict__ vb = ms.ec.vb;
+    for (uint32_t q = q0 + threadIdx.x; q < q1; q += 2 * blockDim.x) {
+        const uint32_t q2 = q + blockDim.x;
+        const bool h2 = q2 < q1;
+        const uint32_t r1 = q / 3u, c1 = q - 3u * r1;
+        const uint32_t r2 = q2 / 3u, c2 = q2 - 3u * r2;
+        const uint32_t t1 = tri_of(r1);
+        const uint32_t t2 = h2 ? tri_of(r2) : 0u;
+        const uint32_t v1 = idx[3 * t1 + c1];
+        const uint32_t v2 = h2 ? idx[3 * t2 + c2] : 0u;
+        const float4 a1 = va[v1], b1 = vb[v1];
+        float4 a2 = a1, b2 = b1;
+        if (h2) { a2 = va[v2]; b2 = vb[v2]; }
+        store_corner(P, ms, v1, a1, b1, base + q);
+        if (h2) store_corner(P, ms, v2, a2, b2, base + q2);
+    }
 }
 
 // Stable ranking of a tile's visible list (bins computed, in triangle order).
@@ -744,11 +768,10 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
                 }
                 scan_bins(sm);
                 rank_tile(P, seg, L, sort_mode, true, 0);
-                const size_t base = 3 * (size_t)seg.out_base;
-                for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {
-                    const uint32_t r = q / 3u, c = q - 3u * r;
-                    emit_corner_at(P, *L.ms, t0 + L.lidx[L.perm[r]], c, base + q);
-                }
+                const uint16_t* lidx = L.lidx;
+                const uint16_t* perm = L.perm;
+                emit_corners(P, *L.ms, 0, 3 * n, 3 * (size_t)seg.out_base,
+                             [&](uint32_t r) { return t0 + lidx[perm[r]]; });
             }
             if (threadIdx.x == 0) {
                 P.seg_count[s] = n;
@@ -901,11 +924,9 @@ __device__ __noinline__ void phase_emit_multi(const FrameParams& P, unsigned cha
         __syncthreads();
         const uint32_t r1 = min(n, r0 + E);
         const uint32_t* __restrict__ ord = P.order + seg.out_base;
-        const size_t base = 3 * (size_t)seg.out_base;
-        for (uint32_t q = 3 * r0 + threadIdx.x; q < 3 * r1; q += blockDim.x) {
-            const uint32_t r = q / 3u, c = q - 3u * r;
-            emit_corner_at(P, *L.ms, seg.tri_start + __ldcg(&ord[r]), c, base + q);
-        }
+        const uint32_t ts = seg.tri_start;
+        emit_corners(P, *L.ms, 3 * r0, 3 * r1, 3 * (size_t)seg.out_base,
+                     [&](uint32_t r) { return ts + __ldcg(&ord[r]); });
     }
 }
 
