@@ -294,7 +294,10 @@ def run_ours(args, rank, world, local_rank):
             "visible_tris_per_step": vis / args.steps / max(1, world),
             "culled_models_last_frame": int(st_last.culled_models),
             "phase_us_last_frame": {k: round(float(v), 1) for k, v in
-                                    zip(("prep", "triangles", "hist", "scan", "rank", "emit"), st_last.phase_us)},
+                                    zip(("prep", "vertex", "triangles", "hist", "scan", "rank_emit"), st_last.phase_us)},
+            "phase_busy_us_last_frame": {k: round(float(v), 1) for k, v in
+                                         zip(("prep", "vertex", "triangles", "hist", "scan", "rank_emit"),
+                                             st_last.phase_busy)},
             "plain": plain,
             "autotune": tuned,
             "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,

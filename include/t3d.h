@@ -262,7 +262,8 @@ typedef struct t3d_stats {
     uint64_t scratch_bytes;  /* device scratch held by the context */
     uint64_t h2d_bytes;      /* host-to-device bytes of the last render call (tables) */
     uint64_t d2h_bytes;      /* device-to-host bytes of the last t3d_frame_sync */
-    double   phase_us[6];    /* batched launch: model prep, triangles, histogram, scan, rank, emit */
+    double   phase_us[7];    /* batched launch: model prep, vertex, triangles, histogram, scan, rank + emit, (unused) */
+    double   phase_busy[7];  /* same phases: mean time a block spent working in the phase (us) */
 } t3d_stats;
 
 typedef struct t3d_ctx t3d_ctx;

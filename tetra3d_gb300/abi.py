@@ -103,7 +103,7 @@ class Stats(C.Structure):
     _fields_ = [("visible_tris", C.c_uint64), ("total_tris", C.c_uint64), ("drawn_parts", C.c_uint32),
                 ("total_parts", C.c_uint32), ("culled_models", C.c_uint32), ("launches", C.c_uint32),
                 ("algorithmic_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("h2d_bytes", C.c_uint64),
-                ("d2h_bytes", C.c_uint64), ("phase_us", C.c_double * 6)]
+                ("d2h_bytes", C.c_uint64), ("phase_us", C.c_double * 7), ("phase_busy", C.c_double * 7)]
 
 
 class Request(C.Structure):

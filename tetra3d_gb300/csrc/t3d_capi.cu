@@ -88,7 +88,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     drop_graph(ctx);
     for (auto& kv : ctx->scenes) kv.second->release();
     ctx->scenes.clear();
-    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->order,
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum})
         b->release();
@@ -271,7 +271,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.algorithmic_bytes += 108ull * s.visible_tris;
     s.launches = ctx->launches;
     size_t scratch = 0;
-    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->order,
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
         scratch += b->cap;
     s.scratch_bytes = scratch;
@@ -279,11 +279,14 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     if (ctx->nctl == 1) {
         const Ctl& c = ctls[0];
         unsigned long long prev = c.t_end[7];
-        for (int k = 0; k < 6; k++) {
-            if (c.t_end[k] >= prev && prev) {
-                s.phase_us[k] = (double)(c.t_end[k] - prev) / 1e3;
-                prev = c.t_end[k];
+        const int order[6] = {0, 6, 1, 2, 3, 4};  // prep, vertex, triangles, hist, scan, rank + emit
+        for (int i = 0; i < 6; i++) {
+            const unsigned long long t = c.t_end[order[i]];
+            if (t >= prev && prev) {
+                s.phase_us[i] = (double)(t - prev) / 1e3;
+                prev = t;
             }
+            s.phase_busy[i] = ctx->last_grid ? (double)c.busy[order[i]] / 1e3 / ctx->last_grid : 0.0;
         }
     }
     s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl;

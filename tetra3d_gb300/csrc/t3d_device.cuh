@@ -5,9 +5,9 @@
 //   va[v] = (px, py, pz, nx)   vb[v] = (ny, nz, u, v)   vc[v] = (r, g, b, a)
 //   idx[3t..3t+2]              mesh-absolute vertex indices per triangle
 // Per frame the host builds job / instance / segment / tile tables; the kernel
-// writes per-model prep records, per-tile visible lists (multi-tile segments
-// only) and the resident output stream. No per-vertex scratch: every emitted
-// corner is computed from the vertex streams when it is written.
+// writes per-model prep records, one record per (render pair, vertex) with the
+// cull and emitted attributes, per-tile visible lists (multi-tile segments
+// only) and the resident output stream.
 #pragma once
 
 #include <stdint.h>
@@ -93,6 +93,7 @@ struct DevJob {
     const float4* vb;
     const float4* vc;
     const uint32_t* idx;
+    const float* centers;   // tri.Center per pool triangle (3 floats)
     const DevMesh* meshes;
     DevModel* models;
     const float* cells;
@@ -125,7 +126,7 @@ struct DevSeg {
     uint32_t inst, job, mesh, flags;
     uint32_t tri_start, tri_count;   // mesh-absolute
     uint32_t vmin, vcount;           // mesh-absolute vertex range the triangles use
-    uint32_t reserved0;
+    uint32_t vscratch;               // first per-vertex record of this segment
     uint32_t out_base;               // first output triangle slot
     uint32_t tile_first, ntiles;     // global tile numbers
     uint32_t mt_first;               // first multi-tile tile number (SEG_MULTI)
@@ -145,6 +146,7 @@ struct Ctl {
     uint32_t culled;
     uint32_t pad[3];
     unsigned long long t_end[8];    // globaltimer when the last block finished phase k; [7] = kernel start
+    unsigned long long busy[8];     // sum over blocks of the time spent inside phase k (ns)
 };
 
 enum : int32_t { ERR_NONE = 0, ERR_BARRIER_TIMEOUT = 1, ERR_BAD_INDEX = 2, ERR_LIGHTS = 3 };
@@ -158,16 +160,18 @@ struct FrameParams {
     const uint32_t* tile_seg;     // tile -> segment
     const uint32_t* mt_tiles;     // multi-tile tiles (global tile numbers)
     const uint32_t* mt_segs;      // multi-tile segments
-    const uint32_t* emit_seg;     // emit work item -> multi-tile segment
-    const uint32_t* emit_chunk;   // emit work item -> chunk of tile_tris output slots
+    const uint32_t* vitem_seg;    // vertex work item -> segment
+    const uint32_t* vitem_chunk;  // vertex work item -> chunk of vchunk vertices
     // scratch
+    float4* vcull;                // per-vertex records: (cx, cy, clipZ, depth)
+    float4* vxyuv;                // emitted screen position + UV
+    float4* vrgba;                // emitted colour
     uint16_t* vis_idx;            // per multi-tile tile: up to tile_tris visible entries
     float* vis_depth;
     uint32_t* tile_count;         // visible per multi-tile tile
     uint32_t* tile_hist;          // per multi-tile tile: kBins counters, then bases
     uint32_t* seg_minmax;         // 2 per segment: min bits, max bits
     uint32_t* seg_count;          // visible per segment (output)
-    uint32_t* order;              // multi-tile segments: segment-relative triangle per output slot
     // output stream
     float4* out_xyuv;
     float4* out_rgba;
@@ -180,9 +184,9 @@ struct FrameParams {
     uint32_t tile_begin, tile_end;
     uint32_t mt_tile_begin, mt_tile_end;
     uint32_t mt_seg_begin, mt_seg_end;
-    uint32_t emit_begin, emit_end;
+    uint32_t vitem_begin, vitem_end;
     uint32_t tile_tris;           // triangles per tile
-    uint32_t vchunk;              // unused (kept for tuning compatibility)
+    uint32_t vchunk;              // vertices per vertex work item
     uint32_t has_multi;           // any multi-tile segment in range
     uint32_t pad;
 };

@@ -318,11 +318,11 @@ struct TileSmem {
     uint32_t item, nvis, warp_tot[kMaxWarps], scan_tmp[kMaxWarps];
     uint32_t wlo[kMaxWarps], whi[kMaxWarps];  // per-warp range of the visible list
     float wmin[kMaxWarps], wmax[kMaxWarps];
-    uint32_t bins_walk[kBins];  // per-bin counts / bases in walk order
+    uint32_t bins_walk[kBins];  // per-bin first output position of this tile in the segment (walk order)
+    uint32_t loc_walk[kBins];   // per-bin first position within this tile's own output order (walk order)
 };
 
 struct SmemLayout {
-    ModelSmem* ms;
     TileSmem* ts;
     uint32_t* whist;
     uint16_t* lidx;
@@ -334,8 +334,6 @@ struct SmemLayout {
 __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t tile) {
     SmemLayout L;
     size_t o = 0;
-    L.ms = (ModelSmem*)(smem + o);
-    o += sizeof(ModelSmem);
     L.ts = (TileSmem*)(smem + o);
     o += sizeof(TileSmem);
     L.whist = (uint32_t*)(smem + o);
@@ -452,17 +450,34 @@ __device__ __forceinline__ float4 clip_of(const float4* mc, float x, float y, fl
 
 // The emitted corner of one vertex (camera.go:1655-1812): screen position,
 // UV, colour (vertex colour * model/material colour * light) and depth.
-// a = (px, py, pz, nx), b = (ny, nz, u, v) of mesh vertex v.
-__device__ __forceinline__ void emit_corner(const ModelSmem& ms, uint32_t v, const float4 a, const float4 b, float4& xyuv,
-                                            float4& rgba, float& depth_out) {
+// The per-vertex results of one (model, mesh part) for mesh vertex v with
+// a = (px, py, pz, nx), b = (ny, nz, u, v):
+//   cull  = (X/w, Y/w, Z, depth) with w<0 -> 1e-6 (model.go:862-873) and the
+//           depth vertex colour (camera.go:1744-1779)
+//   xyuv  = screen position and texture coordinate with w<0 -> 0.001 (camera.go:1655-1708)
+//   rgba  = vertex colour * model/material colour * light (camera.go:1726-1742)
+// Every value depends only on the vertex, the model, the part and the camera, so
+// computing it once per vertex gives the reference's per-corner values bit for bit.
+__device__ __forceinline__ void vertex_record(const ModelSmem& ms, uint32_t v, const float4 a, const float4 b,
+                                              float4& cull, float4& xyuv, float4& rgba) {
     const EmitConst& e = ms.ec;
     const uint32_t f = e.flags;
     const float4 c = clip_of(ms.mvpc, a.x, a.y, a.z);
+    const float w1 = c.w < 0.0f ? 0.000001f : c.w;
+    const float cx = c.x / w1, cy = c.y / w1;
     float w = c.w;
     if (!(f & EC_PERSP)) w = 1.0f;
     if (w < 0.0f) w = 0.001f;
-    xyuv.x = (c.x / w) * e.W + e.halfW;
-    xyuv.y = (c.y / -w) * e.H + e.halfH;
+    float qx, qy;
+    if (w == w1) {  // same divisor: RN(Y / -w) == -RN(Y / w)
+        qx = cx;
+        qy = -cy;
+    } else {
+        qx = c.x / w;
+        qy = c.y / -w;
+    }
+    xyuv.x = qx * e.W + e.halfW;
+    xyuv.y = qy * e.H + e.halfH;
     if (f & EC_PCORRECT) {
         xyuv.z = (b.z / w) * e.tex_w;
         xyuv.w = ((1.0f - b.w) / w) * e.tex_h;
@@ -500,8 +515,8 @@ __device__ __forceinline__ void emit_corner(const ModelSmem& ms, uint32_t v, con
             }
         }
     }
+    cull = make_float4(cx, cy, c.z, depth);
     rgba = make_float4(cr, cg, cb, ca);
-    depth_out = depth;
 }
 
 __device__ __forceinline__ uint32_t walk_pos(uint32_t b, uint32_t sort_mode) {
@@ -521,13 +536,13 @@ __device__ __forceinline__ float range_of(float mn, float mx) {
     return r;
 }
 
-// In-place exclusive scan of ts.bins_walk[0..kBins) by the whole block.
-__device__ void scan_bins(TileSmem& sm) {
+// In-place exclusive scan of arr[0..kBins) by the whole block.
+__device__ void scan_bins(TileSmem& sm, uint32_t* arr) {
     __syncthreads();
     const uint32_t per = (kBins + blockDim.x - 1) / blockDim.x;
     const uint32_t lo = threadIdx.x * per, hi = min((uint32_t)kBins, lo + per);
     uint32_t sum = 0;
-    for (uint32_t i = lo; i < hi; i++) sum += sm.bins_walk[i];
+    for (uint32_t i = lo; i < hi; i++) sum += arr[i];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t incl = sum;
     for (int o = 1; o < 32; o <<= 1) {
@@ -542,58 +557,18 @@ __device__ void scan_bins(TileSmem& sm) {
     }
     __syncthreads();
     uint32_t run = sm.scan_tmp[wid] + incl - sum;
-    for (uint32_t i = lo; i < hi; i++) { uint32_t t = sm.bins_walk[i]; sm.bins_walk[i] = run; run += t; }
+    for (uint32_t i = lo; i < hi; i++) { uint32_t t = arr[i]; arr[i] = run; run += t; }
     __syncthreads();
 }
 
-// Stable placement of a tile's n visible triangles (in triangle order in
-// shared memory, bins already computed) and their emission. bins_walk holds,
-// in walk order, the first output position of each bin for this tile.
-// Writes one emitted corner (camera.go:1646-1820) at output corner index `corner`.
-__device__ __forceinline__ void store_corner(const FrameParams& P, const ModelSmem& ms, uint32_t v, const float4 a,
-                                             const float4 b, size_t corner) {
-    float4 x, r;
-    float d;
-    emit_corner(ms, v, a, b, x, r, d);
-    P.out_xyuv[corner] = x;
-    P.out_rgba[corner] = r;
-    P.out_depth[corner] = d;
-}
-
-// Emits output corners [q0, q1) of a segment, one thread per corner and two
-// corners per thread per step so both dependent gather chains (triangle ->
-// vertex index -> vertex streams) are in flight together. tri_of(r) gives the
-// mesh triangle of output triangle r.
-template <typename TriOf>
-__device__ __forceinline__ void emit_corners(const FrameParams& P, const ModelSmem& ms, uint32_t q0, uint32_t q1,
-                                             size_t base, TriOf tri_of) {
-    const uint32_t* __restrict__ idx = ms.ec.idx;
-    const float4* __restrict__ va = ms.ec.va;
-    const float4* __restrict__ vb = ms.ec.vb;
-    for (uint32_t q = q0 + threadIdx.x; q < q1; q += 2 * blockDim.x) {
-        const uint32_t q2 = q + blockDim.x;
-        const bool h2 = q2 < q1;
-        const uint32_t r1 = q / 3u, c1 = q - 3u * r1;
-        const uint32_t r2 = q2 / 3u, c2 = q2 - 3u * r2;
-        const uint32_t t1 = tri_of(r1);
-        const uint32_t t2 = h2 ? tri_of(r2) : 0u;
-        const uint32_t v1 = idx[3 * t1 + c1];
-        const uint32_t v2 = h2 ? idx[3 * t2 + c2] : 0u;
-        const float4 a1 = va[v1], b1 = vb[v1];
-        float4 a2 = a1, b2 = b1;
-        if (h2) { a2 = va[v2]; b2 = vb[v2]; }
-        store_corner(P, ms, v1, a1, b1, base + q);
-        if (h2) store_corner(P, ms, v2, a2, b2, base + q2);
-    }
-}
-
-// Stable ranking of a tile's visible list (bins computed, in triangle order).
-// Warp w owns entries [ts.wlo[w], ts.whi[w]); the ranges follow each other in
-// triangle order. bins_walk holds, in walk order, the first output position of
-// each bin for this tile. Single-tile segments record perm[pos] = entry;
-// multi-tile segments record order[out_base + pos] = segment-relative triangle.
-__device__ void rank_tile(const FrameParams& P, const DevSeg& seg, const SmemLayout& L, uint32_t sort_mode,
-                          bool single, uint32_t tile_off) {
+// Stable ranking of a tile's visible list (bins computed, entries in triangle
+// order). Warp w owns entries [ts.wlo[w], ts.whi[w]); the ranges follow each
+// other in triangle order. Produces the tile's own output order:
+// perm[r] = list entry of the tile's r-th output triangle, and loc_walk[] =
+// first local rank of each bin (walk order). The tile's output triangles of a
+// bin are contiguous in the segment: local ranks loc_walk[w] .. map to
+// positions bins_walk[w] ..
+__device__ void rank_tile(const SmemLayout& L, uint32_t sort_mode) {
     TileSmem& sm = *L.ts;
     const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t lo = sm.wlo[wid], hi = sm.whi[wid];
@@ -602,7 +577,13 @@ __device__ void rank_tile(const FrameParams& P, const DevSeg& seg, const SmemLay
     for (uint32_t j = lo + lane; j < hi; j += 32) atomicAdd(&L.whist[wid * kBins + L.bin[j]], 1u);
     __syncthreads();
     for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
-        uint32_t run = sm.bins_walk[walk_pos(b, sort_mode)];
+        uint32_t tot = 0;
+        for (uint32_t w = 0; w < nw; w++) tot += L.whist[w * kBins + b];
+        sm.loc_walk[walk_pos(b, sort_mode)] = tot;
+    }
+    scan_bins(sm, sm.loc_walk);
+    for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
+        uint32_t run = sm.loc_walk[walk_pos(b, sort_mode)];
         for (uint32_t w = 0; w < nw; w++) {
             uint32_t t = L.whist[w * kBins + b];
             L.whist[w * kBins + b] = run;
@@ -615,40 +596,57 @@ __device__ void rank_tile(const FrameParams& P, const DevSeg& seg, const SmemLay
         const uint32_t j = j0 + lane;
         const bool active = j < hi;
         const uint32_t mask = __ballot_sync(0xffffffffu, active);
-        uint32_t b = 0, peers = 0, pos = 0;
+        uint32_t b = 0, peers = 0, r = 0;
         if (active) {
             b = L.bin[j];
             peers = __match_any_sync(mask, b);
-            pos = L.whist[wid * kBins + b] + __popc(peers & lt);
+            r = L.whist[wid * kBins + b] + __popc(peers & lt);
         }
         __syncwarp();
         if (active && lane == (uint32_t)(__ffs(peers) - 1)) L.whist[wid * kBins + b] += __popc(peers);
         __syncwarp();
-        if (active) {
-            if (single) L.perm[pos] = (uint16_t)j;
-            else P.order[(size_t)seg.out_base + pos] = tile_off + L.lidx[j];
-        }
+        if (active) L.perm[r] = (uint16_t)j;
     }
     __syncthreads();
 }
 
-// ProcessVertices' rejection tests and depth key for one triangle whose
-// model-space corners are a, b, c (model.go:855-969).
-__device__ __forceinline__ bool tri_visible(const float4* mvp, float nearp, float farp, bool backface, f3 ic, float4 pa,
-                                            float4 pb, float4 pc, float& depth) {
-    const float4 c0 = clip_of(mvp, pa.x, pa.y, pa.z);
-    const float4 c1 = clip_of(mvp, pb.x, pb.y, pb.z);
-    const float4 c2 = clip_of(mvp, pc.x, pc.y, pc.z);
+// Emits a ranked tile by copying per-vertex records: one thread per output
+// corner in the tile's output order, so consecutive threads read vertices of
+// the same tile and write consecutive corners of one bin run.
+__device__ void tile_emit(const FrameParams& P, const DevSeg& seg, const SmemLayout& L, const uint32_t* __restrict__ midx,
+                          uint32_t t0, uint32_t n, uint32_t sort_mode, bool single) {
+    const TileSmem& sm = *L.ts;
+    const size_t base = 3 * (size_t)seg.out_base;
+    const uint32_t vs = seg.vscratch, vm = seg.vmin;
+    for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {
+        const uint32_t r = q / 3u, c = q - 3u * r;
+        const uint32_t j = L.perm[r];
+        uint32_t pos = r;
+        if (!single) {
+            const uint32_t w = walk_pos(L.bin[j], sort_mode);
+            pos = sm.bins_walk[w] + (r - sm.loc_walk[w]);
+        }
+        const uint32_t t = t0 + L.lidx[j];
+        const uint32_t o = vs + (midx[3 * t + c] - vm);
+        const float4 x = __ldcg(&P.vxyuv[o]);
+        const float4 k = __ldcg(&P.vrgba[o]);
+        const float d = __ldcg(&P.vcull[o].w);
+        const size_t oc = base + 3 * (size_t)pos + c;
+        P.out_xyuv[oc] = x;
+        P.out_rgba[oc] = k;
+        P.out_depth[oc] = d;
+    }
+}
+
+// ProcessVertices' rejection tests and depth key for one triangle from its
+// corners' cull records (cx, cy, Z) and its model-space centre (model.go:855-969).
+__device__ __forceinline__ bool tri_visible(float nearp, float farp, bool backface, f3 ic, float4 c0, float4 c1,
+                                            float4 c2, f3 ctr, float& depth) {
     // near/far: some corner with Z + 1 >= near && Z < far (model.go:855-886)
     if (!((c0.z + 1.0f >= nearp && c0.z < farp) || (c1.z + 1.0f >= nearp && c1.z < farp) ||
           (c2.z + 1.0f >= nearp && c2.z < farp)))
         return false;
-    const float w0 = c0.w < 0.0f ? 0.000001f : c0.w;
-    const float w1 = c1.w < 0.0f ? 0.000001f : c1.w;
-    const float w2 = c2.w < 0.0f ? 0.000001f : c2.w;
-    const float x0 = c0.x / w0, y0 = c0.y / w0;
-    const float x1 = c1.x / w1, y1 = c1.y / w1;
-    const float x2 = c2.x / w2, y2 = c2.y / w2;
+    const float x0 = c0.x, y0 = c0.y, x1 = c1.x, y1 = c1.y, x2 = c2.x, y2 = c2.y;
     // wholly off one side of the screen (model.go:890-898)
     if ((x0 < -0.5f && x1 < -0.5f && x2 < -0.5f) || (x0 > 0.5f && x1 > 0.5f && x2 > 0.5f) ||
         (y0 < -0.5f && y1 < -0.5f && y2 < -0.5f) || (y0 > 0.5f && y1 > 0.5f && y2 > 0.5f))
@@ -659,13 +657,41 @@ __device__ __forceinline__ bool tri_visible(const float4* mvp, float nearp, floa
         const float nor = (n0x * n1y) - (n1x * n0y);
         if (nor < 0.0f) return false;
     }
-    // tri.Center (mesh.go:1980-1982) and the squared distance key (model.go:950-953)
-    const float cxx = (pa.x + pb.x + pc.x) / 3.0f;
-    const float cyy = (pa.y + pb.y + pc.y) / 3.0f;
-    const float czz = (pa.z + pb.z + pc.z) / 3.0f;
-    const float ddx = ic.x - cxx, ddy = ic.y - cyy, ddz = ic.z - czz;
+    // squared distance from the model-space camera to tri.Center (model.go:950-953)
+    const float ddx = ic.x - ctr.x, ddy = ic.y - ctr.y, ddz = ic.z - ctr.z;
     depth = ddx * ddx + ddy * ddy + ddz * ddz;
     return !(isnan(depth) || isinf(depth));
+}
+
+// PV: per (segment, vertex chunk) the vertex records of every vertex the
+// part's triangles use.
+__device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* smem) {
+    ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
+    uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
+    for (;;) {
+        const uint32_t item = P.vitem_begin + next_item(P.ctl, 6, s_item);
+        if (item >= P.vitem_end) break;
+        const uint32_t s = P.vitem_seg[item];
+        const DevSeg seg = P.segs[s];
+        if ((seg.flags & SEG_SKIP) || P.preps[seg.inst].culled) continue;
+        const DevJob& J = P.jobs[seg.job];
+        stage_model(P, seg, J, ms);
+        __syncthreads();
+        const uint32_t v0 = P.vitem_chunk[item] * P.vchunk;
+        const uint32_t v1 = min(seg.vcount, v0 + P.vchunk);
+        const float4* __restrict__ va = ms.ec.va;
+        const float4* __restrict__ vb = ms.ec.vb;
+        for (uint32_t lv = v0 + threadIdx.x; lv < v1; lv += blockDim.x) {
+            const uint32_t v = seg.vmin + lv;
+            const float4 a = va[v], b = vb[v];
+            float4 cull, xyuv, rgba;
+            vertex_record(ms, v, a, b, cull, xyuv, rgba);
+            const uint32_t o = seg.vscratch + lv;
+            P.vcull[o] = cull;
+            P.vxyuv[o] = xyuv;
+            P.vrgba[o] = rgba;
+        }
+    }
 }
 
 // P1: visibility and depth keys per tile; single-tile segments are sorted and
@@ -689,17 +715,18 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
             continue;
         }
         const DevJob& J = P.jobs[seg.job];
-        stage_model(P, seg, J, *L.ms);
         const JobCam& cam = J.cam;
         const float nearp = cam.near_, farp = cam.far_;
         const bool backface = seg.flags & SEG_BACKFACE;
         const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
         const DevMesh me = J.meshes[seg.mesh];
+        const uint32_t* __restrict__ midx = J.idx + 3 * (size_t)me.tbase;
+        const float* __restrict__ mctr = J.centers + 3 * (size_t)me.tbase;
+        const float4* __restrict__ vcull = P.vcull + seg.vscratch;
+        const uint32_t vm = seg.vmin;
         const uint32_t t0 = seg.tri_start + tile * T;
         const uint32_t t1 = min(seg.tri_start + seg.tri_count, t0 + T);
         float lmin = 3.402823466e38f, lmax = 0.0f;
-        __syncthreads();
-        const float4* mvp = L.ms->mvpc;
         // each warp compacts its own contiguous quarter/eighth of the tile
         const uint32_t per = T / nw;
         const uint32_t wt0 = t0 + wid * per, wt1 = min(t1, wt0 + per);
@@ -710,15 +737,22 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
         for (uint32_t tb = wt0; tb < wt1; tb += 64) {
             const uint32_t ta = tb + lane, tb2 = tb + 32 + lane;
             const bool ha = ta < wt1, hb = tb2 < wt1;
-            uint32_t ia0 = 0, ia1 = 0, ia2 = 0, ib0 = 0, ib1 = 0, ib2 = 0;
-            if (ha) { const uint32_t* ip = J.idx + 3 * (size_t)(me.tbase + ta); ia0 = ip[0]; ia1 = ip[1]; ia2 = ip[2]; }
-            if (hb) { const uint32_t* ip = J.idx + 3 * (size_t)(me.tbase + tb2); ib0 = ip[0]; ib1 = ip[1]; ib2 = ip[2]; }
+            uint32_t ia0 = vm, ia1 = vm, ia2 = vm, ib0 = vm, ib1 = vm, ib2 = vm;
+            f3 ca = mk3(0.f, 0.f, 0.f), cb = ca;
+            if (ha) {
+                ia0 = midx[3 * ta]; ia1 = midx[3 * ta + 1]; ia2 = midx[3 * ta + 2];
+                ca = mk3(mctr[3 * ta], mctr[3 * ta + 1], mctr[3 * ta + 2]);
+            }
+            if (hb) {
+                ib0 = midx[3 * tb2]; ib1 = midx[3 * tb2 + 1]; ib2 = midx[3 * tb2 + 2];
+                cb = mk3(mctr[3 * tb2], mctr[3 * tb2 + 1], mctr[3 * tb2 + 2]);
+            }
             float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f), pa1 = pa0, pa2 = pa0, pb0 = pa0, pb1 = pa0, pb2 = pa0;
-            if (ha) { pa0 = J.va[me.vbase + ia0]; pa1 = J.va[me.vbase + ia1]; pa2 = J.va[me.vbase + ia2]; }
-            if (hb) { pb0 = J.va[me.vbase + ib0]; pb1 = J.va[me.vbase + ib1]; pb2 = J.va[me.vbase + ib2]; }
+            if (ha) { pa0 = __ldcg(&vcull[ia0 - vm]); pa1 = __ldcg(&vcull[ia1 - vm]); pa2 = __ldcg(&vcull[ia2 - vm]); }
+            if (hb) { pb0 = __ldcg(&vcull[ib0 - vm]); pb1 = __ldcg(&vcull[ib1 - vm]); pb2 = __ldcg(&vcull[ib2 - vm]); }
             float da = 0.0f, db = 0.0f;
-            const bool va_ = ha && tri_visible(mvp, nearp, farp, backface, ic, pa0, pa1, pa2, da);
-            const bool vb_ = hb && tri_visible(mvp, nearp, farp, backface, ic, pb0, pb1, pb2, db);
+            const bool va_ = ha && tri_visible(nearp, farp, backface, ic, pa0, pa1, pa2, ca, da);
+            const bool vb_ = hb && tri_visible(nearp, farp, backface, ic, pb0, pb1, pb2, cb, db);
             const uint32_t bala = __ballot_sync(0xffffffffu, va_);
             const uint32_t balb = __ballot_sync(0xffffffffu, vb_);
             if (va_) {
@@ -759,19 +793,10 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
         if (!multi) {
             if (n > 0) {
                 const float range = range_of(mn, mx);
-                for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) sm.bins_walk[b] = 0u;
-                __syncthreads();
-                for (uint32_t j = wbase + lane; j < wbase + cnt; j += 32) {
-                    const uint32_t b = bin_of(L.depth[j], mn, range, sort_mode);
-                    L.bin[j] = (uint16_t)b;
-                    atomicAdd(&sm.bins_walk[walk_pos(b, sort_mode)], 1u);
-                }
-                scan_bins(sm);
-                rank_tile(P, seg, L, sort_mode, true, 0);
-                const uint16_t* lidx = L.lidx;
-                const uint16_t* perm = L.perm;
-                emit_corners(P, *L.ms, 0, 3 * n, 3 * (size_t)seg.out_base,
-                             [&](uint32_t r) { return t0 + lidx[perm[r]]; });
+                for (uint32_t j = wbase + lane; j < wbase + cnt; j += 32)
+                    L.bin[j] = (uint16_t)bin_of(L.depth[j], mn, range, sort_mode);
+                rank_tile(L, sort_mode);
+                tile_emit(P, seg, L, midx, t0, n, sort_mode, true);
             }
             if (threadIdx.x == 0) {
                 P.seg_count[s] = n;
@@ -797,20 +822,24 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
     }
 }
 
-// P2: bin histograms of the tiles of multi-tile segments.
+// P2: bin histograms of the tiles of multi-tile segments, one warp per tile
+// (each warp pulls its own tiles and owns a kBins-counter region of shared memory).
 __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
-    TileSmem& sm = *L.ts;
+    const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* wh = L.whist + wid * kBins;
     for (;;) {
-        const uint32_t i = P.mt_tile_begin + next_item(P.ctl, 2, &sm.item);
+        uint32_t i = 0;
+        if (lane == 0) i = atomicAdd(&P.ctl->queue[2], 1u);
+        i = P.mt_tile_begin + __shfl_sync(0xffffffffu, i, 0);
         if (i >= P.mt_tile_end) break;
         const uint32_t g = P.mt_tiles[i];
         const uint32_t s = P.tile_seg[g];
         const uint32_t flags = P.segs[s].flags;
         const uint32_t n = __ldcg(&P.tile_count[i]);
-        for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) sm.bins_walk[b] = 0u;
-        __syncthreads();
+        for (uint32_t b = lane; b < kBins; b += 32) wh[b] = 0u;
+        __syncwarp();
         if (n > 0) {
             const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
             const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
@@ -818,11 +847,12 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
             const uint32_t sort_mode = seg_sort_mode(flags);
             const float* gd = P.vis_depth + (size_t)i * T;
 #pragma unroll 4
-            for (uint32_t j = threadIdx.x; j < n; j += blockDim.x)
-                atomicAdd(&sm.bins_walk[bin_of(__ldcg(&gd[j]), mn, range, sort_mode)], 1u);
+            for (uint32_t j = lane; j < n; j += 32) atomicAdd(&wh[bin_of(__ldcg(&gd[j]), mn, range, sort_mode)], 1u);
         }
-        __syncthreads();
-        for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) P.tile_hist[(size_t)i * kBins + b] = sm.bins_walk[b];
+        __syncwarp();
+        uint32_t* out = P.tile_hist + (size_t)i * kBins;
+        for (uint32_t b = lane; b < kBins; b += 32) out[b] = wh[b];
+        __syncwarp();
     }
 }
 
@@ -850,7 +880,7 @@ __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* sme
             for (; t < seg.ntiles; t++) tot += __ldcg(&hbase[(size_t)t * kBins + b]);
             sm.bins_walk[walk_pos(b, sort_mode)] = tot;
         }
-        scan_bins(sm);
+        scan_bins(sm, sm.bins_walk);
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
             uint32_t run = sm.bins_walk[walk_pos(b, sort_mode)];
             uint32_t t = 0;
@@ -871,7 +901,7 @@ __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* sme
     }
 }
 
-// P4: stable rank of the tiles of multi-tile segments into the order array.
+// P4: stable rank and emission of the tiles of multi-tile segments.
 __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
@@ -884,6 +914,9 @@ __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned cha
         const DevSeg seg = P.segs[s];
         const uint32_t n = __ldcg(&P.tile_count[i]);
         if (n == 0) continue;
+        const DevJob& J = P.jobs[seg.job];
+        const uint32_t* __restrict__ midx = J.idx + 3 * (size_t)J.meshes[seg.mesh].tbase;
+        const uint32_t t0 = seg.tri_start + (g - seg.tile_first) * T;
         const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
         const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
         const float range = range_of(mn, mx);
@@ -902,31 +935,8 @@ __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned cha
             sm.whi[threadIdx.x] = min(n, threadIdx.x * chunk + chunk);
         }
         __syncthreads();
-        rank_tile(P, seg, L, sort_mode, false, (g - seg.tile_first) * T);
-    }
-}
-
-// P5: emit multi-tile segments in output order, tile_tris slots per work item.
-__device__ __noinline__ void phase_emit_multi(const FrameParams& P, unsigned char* smem) {
-    const uint32_t E = P.tile_tris;
-    const SmemLayout L = smem_layout(smem, E);
-    TileSmem& sm = *L.ts;
-    for (;;) {
-        const uint32_t k = P.emit_begin + next_item(P.ctl, 5, &sm.item);
-        if (k >= P.emit_end) break;
-        const uint32_t s = P.emit_seg[k];
-        const uint32_t r0 = P.emit_chunk[k] * E;
-        const uint32_t n = __ldcg(&P.seg_count[s]);
-        if (r0 >= n) continue;
-        const DevSeg seg = P.segs[s];
-        const DevJob& J = P.jobs[seg.job];
-        stage_model(P, seg, J, *L.ms);
-        __syncthreads();
-        const uint32_t r1 = min(n, r0 + E);
-        const uint32_t* __restrict__ ord = P.order + seg.out_base;
-        const uint32_t ts = seg.tri_start;
-        emit_corners(P, *L.ms, 3 * r0, 3 * r1, 3 * (size_t)seg.out_base,
-                     [&](uint32_t r) { return ts + __ldcg(&ord[r]); });
+        rank_tile(L, sort_mode);
+        tile_emit(P, seg, L, midx, t0, n, sort_mode, false);
     }
 }
 
@@ -935,32 +945,47 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// Records when the last block finished phase k (kernel start in slot 7).
-__device__ __forceinline__ void phase_done(Ctl* ctl, int k) {
-    if (threadIdx.x == 0) atomicMax(&ctl->t_end[k], global_ns());
+// Records when the last block finished phase k (kernel start in slot 7) and the
+// time this block spent inside the phase (from `since`).
+__device__ __forceinline__ void phase_done(Ctl* ctl, int k, unsigned long long& since) {
+    if (threadIdx.x == 0) {
+        const unsigned long long now = global_ns();
+        atomicMax(&ctl->t_end[k], now);
+        atomicAdd(&ctl->busy[k], now - since);
+    }
+}
+__device__ __forceinline__ void phase_start(unsigned long long& since) {
+    if (threadIdx.x == 0) since = global_ns();
 }
 
 __global__ void __launch_bounds__(256, 4) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long since = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl->t_end[7] = global_ns();
+    phase_start(since);
     phase_prep(P);
-    phase_done(P.ctl, 0);
+    phase_done(P.ctl, 0, since);
     if (!grid_barrier(P.ctl)) return;
+    phase_start(since);
+    phase_vertex(P, smem);
+    phase_done(P.ctl, 6, since);
+    if (!grid_barrier(P.ctl)) return;
+    phase_start(since);
     phase_triangles(P, smem);
-    phase_done(P.ctl, 1);
+    phase_done(P.ctl, 1, since);
     if (!P.has_multi) return;
     if (!grid_barrier(P.ctl)) return;
+    phase_start(since);
     phase_hist(P, smem);
-    phase_done(P.ctl, 2);
+    phase_done(P.ctl, 2, since);
     if (!grid_barrier(P.ctl)) return;
+    phase_start(since);
     phase_scan(P, smem);
-    phase_done(P.ctl, 3);
+    phase_done(P.ctl, 3, since);
     if (!grid_barrier(P.ctl)) return;
+    phase_start(since);
     phase_rank_multi(P, smem);
-    phase_done(P.ctl, 4);
-    if (!grid_barrier(P.ctl)) return;
-    phase_emit_multi(P, smem);
-    phase_done(P.ctl, 5);
+    phase_done(P.ctl, 4, since);
 }
 
 }  // namespace t3d
@@ -968,6 +993,7 @@ __global__ void __launch_bounds__(256, 4) t3d_frame_kernel(const __grid_constant
 // Launch entry used by the runtime (same translation-unit linkage).
 extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel; }
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads) {
-    return sizeof(t3d::ModelSmem) + sizeof(t3d::TileSmem) + 4ull * (block_threads / 32) * t3d::kBins +
-           10ull * tile_tris + 16;
+    const size_t tiles = sizeof(t3d::TileSmem) + 4ull * (block_threads / 32) * t3d::kBins + 10ull * tile_tris + 16;
+    const size_t verts = sizeof(t3d::ModelSmem) + 16;
+    return tiles > verts ? tiles : verts;
 }

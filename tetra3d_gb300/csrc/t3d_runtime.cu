@@ -306,12 +306,13 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     // device pools
     int rc;
     if ((rc = sc->va.ensure(ctx, nv * 16)) || (rc = sc->vb.ensure(ctx, nv * 16)) || (rc = sc->vc.ensure(ctx, nv * 16)) ||
-        (rc = sc->idx.ensure(ctx, nt * 12)) || (rc = sc->dmeshes.ensure(ctx, sizeof(DevMesh) * std::max<size_t>(1, d->num_meshes))) ||
+        (rc = sc->idx.ensure(ctx, nt * 12)) || (rc = sc->centers.ensure(ctx, nt * 12)) ||
+        (rc = sc->dmeshes.ensure(ctx, sizeof(DevMesh) * std::max<size_t>(1, d->num_meshes))) ||
         (rc = sc->dmodels.ensure(ctx, sizeof(DevModel) * std::max<size_t>(1, d->num_models))) ||
         (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))))
         return rc;
     std::vector<float4> a, b, c;
-    std::vector<uint32_t> ix;
+    std::vector<float> ctr;
     for (uint32_t m = 0; m < d->num_meshes; m++) {
         const t3d_mesh_desc& me = d->meshes[m];
         a.resize(me.num_vertices); b.resize(me.num_vertices); c.resize(me.num_vertices);
@@ -333,6 +334,16 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         CK(cudaMemcpy((char*)sc->vb.ptr + off, b.data(), me.num_vertices * 16ull, cudaMemcpyHostToDevice));
         CK(cudaMemcpy((char*)sc->vc.ptr + off, c.data(), me.num_vertices * 16ull, cudaMemcpyHostToDevice));
         CK(cudaMemcpy((char*)sc->idx.ptr + (size_t)sc->meshes[m].tbase * 12, me.indices, me.num_triangles * 12ull,
+                      cudaMemcpyHostToDevice));
+        // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis in binary32
+        ctr.resize(3ull * me.num_triangles);
+        for (uint32_t t = 0; t < me.num_triangles; t++) {
+            const float* pa = me.positions + 3 * (size_t)me.indices[3 * (size_t)t];
+            const float* pb = me.positions + 3 * (size_t)me.indices[3 * (size_t)t + 1];
+            const float* pc = me.positions + 3 * (size_t)me.indices[3 * (size_t)t + 2];
+            for (int k = 0; k < 3; k++) ctr[3 * (size_t)t + k] = (pa[k] + pb[k] + pc[k]) / 3.0f;
+        }
+        CK(cudaMemcpy((char*)sc->centers.ptr + (size_t)sc->meshes[m].tbase * 12, ctr.data(), me.num_triangles * 12ull,
                       cudaMemcpyHostToDevice));
     }
     std::vector<DevMesh> dm(d->num_meshes);
@@ -400,6 +411,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.vb = (const float4*)sc->vb.ptr;
         dj.vc = (const float4*)sc->vc.ptr;
         dj.idx = (const uint32_t*)sc->idx.ptr;
+        dj.centers = (const float*)sc->centers.ptr;
         dj.meshes = (const DevMesh*)sc->dmeshes.ptr;
         dj.models = (DevModel*)sc->dmodels.ptr;
         dj.cells = (const float*)sc->cells.ptr;
@@ -494,6 +506,13 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 sg.mp[0] *= mat.color[0]; sg.mp[1] *= mat.color[1]; sg.mp[2] *= mat.color[2]; sg.mp[3] *= mat.color[3];
                 sg.tex_w = mat.tex_w; sg.tex_h = mat.tex_h;
             }
+            sg.vscratch = (uint32_t)F.nscratch;
+            F.nscratch += sg.vcount;
+            F.seg_vitem_first.push_back((uint32_t)F.vitem_seg.size());
+            {
+                const uint32_t nch = (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
+                for (uint32_t c = 0; c < nch; c++) { F.vitem_seg.push_back((uint32_t)F.segs.size()); F.vitem_chunk.push_back(c); }
+            }
             sg.out_base = (uint32_t)F.nslots;
             F.nslots += sg.tri_count;
             uint32_t ntiles = (sg.tri_count + T - 1) / T;
@@ -508,9 +527,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 F.mt_segs.push_back(s);
             }
             for (uint32_t t = 0; t < ntiles; t++) F.tile_seg.push_back(s);
-            F.seg_emit_first.push_back((uint32_t)F.emit_seg.size());
-            if (ntiles > 1)
-                for (uint32_t c = 0; c < ntiles; c++) { F.emit_seg.push_back(s); F.emit_chunk.push_back(c); }
+
             sg.flags = flags;
             F.segs.push_back(sg);
             t3d_segment_info si;
@@ -551,8 +568,9 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     size_t o_ts = add(F.tile_seg.data(), bytes_of(F.tile_seg));
     size_t o_mtt = add(F.mt_tiles.data(), bytes_of(F.mt_tiles));
     size_t o_mts = add(F.mt_segs.data(), bytes_of(F.mt_segs));
-    size_t o_es = add(F.emit_seg.data(), bytes_of(F.emit_seg));
-    size_t o_ec = add(F.emit_chunk.data(), bytes_of(F.emit_chunk));
+    size_t o_vs = add(F.vitem_seg.data(), bytes_of(F.vitem_seg));
+    size_t o_vc = add(F.vitem_chunk.data(), bytes_of(F.vitem_chunk));
+
     std::vector<DevInst> noanim(F.insts);
     for (auto& in : noanim) in.animate = 0;
     size_t o_noanim = add(noanim.data(), bytes_of(noanim));
@@ -579,15 +597,18 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.tile_seg = (const uint32_t*)(db + o_ts);
     P.mt_tiles = (const uint32_t*)(db + o_mtt);
     P.mt_segs = (const uint32_t*)(db + o_mts);
-    P.emit_seg = (const uint32_t*)(db + o_es);
-    P.emit_chunk = (const uint32_t*)(db + o_ec);
+    P.vitem_seg = (const uint32_t*)(db + o_vs);
+    P.vitem_chunk = (const uint32_t*)(db + o_vc);
+
     ctx->insts_noanim = (const DevInst*)(db + o_noanim);
     // scratch
     const size_t ninst = std::max<size_t>(1, F.insts.size()), nseg = std::max<size_t>(1, F.segs.size());
     const size_t nmt = std::max<size_t>(1, F.mt_tiles.size());
+    const size_t nsc = std::max<uint64_t>(1, F.nscratch);
     const size_t nslots = std::max<uint64_t>(1, F.nslots);
     if ((rc = ctx->preps.ensure(ctx, sizeof(DevPrep) * ninst)) ||
-        (rc = ctx->order.ensure(ctx, 4 * nslots)) ||
+(rc = ctx->vcull.ensure(ctx, 16 * nsc)) ||
+        (rc = ctx->vxyuv.ensure(ctx, 16 * nsc)) || (rc = ctx->vrgba.ensure(ctx, 16 * nsc)) ||
         (rc = ctx->vis_idx.ensure(ctx, 2ull * nmt * ctx->tile_tris)) ||
         (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) || (rc = ctx->tile_count.ensure(ctx, 4 * nmt)) ||
         (rc = ctx->tile_hist.ensure(ctx, 4ull * kBins * nmt)) || (rc = ctx->seg_minmax.ensure(ctx, 8 * nseg)) ||
@@ -595,7 +616,10 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
         return rc;
     P.preps = (DevPrep*)ctx->preps.ptr;
-    P.order = (uint32_t*)ctx->order.ptr;
+
+    P.vcull = (float4*)ctx->vcull.ptr;
+    P.vxyuv = (float4*)ctx->vxyuv.ptr;
+    P.vrgba = (float4*)ctx->vrgba.ptr;
     P.vis_idx = (uint16_t*)ctx->vis_idx.ptr;
     P.vis_depth = (float*)ctx->vis_depth.ptr;
     P.tile_count = (uint32_t*)ctx->tile_count.ptr;
@@ -634,6 +658,7 @@ static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items,
         return T3D_E_CUDA;
     }
     ctx->launches++;
+    ctx->last_grid = grid;
     return T3D_OK;
 }
 
@@ -656,9 +681,10 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.tile_begin = 0; P.tile_end = (uint32_t)F.tile_seg.size();
         P.mt_tile_begin = 0; P.mt_tile_end = (uint32_t)F.mt_tiles.size();
         P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
-        P.emit_begin = 0; P.emit_end = (uint32_t)F.emit_seg.size();
+
+        P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
         P.has_multi = F.mt_segs.empty() ? 0u : 1u;
-        uint32_t items = (uint32_t)std::max({F.tile_seg.size(), F.mt_tiles.size(),
+        uint32_t items = (uint32_t)std::max({F.tile_seg.size(), F.mt_tiles.size(), F.vitem_seg.size(),
                                              (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
         return launch_one(ctx, P, ctl, items, st);
     }
@@ -672,14 +698,16 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.inst_begin = sg.inst; P.inst_end = sg.inst + 1;
         P.seg_begin = (uint32_t)s; P.seg_end = (uint32_t)s + 1;
         P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
+        P.vitem_begin = F.seg_vitem_first[s];
+        P.vitem_end = (s + 1 < F.segs.size()) ? F.seg_vitem_first[s + 1] : (uint32_t)F.vitem_seg.size();
         if (sg.flags & SEG_MULTI) {
             P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles;
             P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;
-            P.emit_begin = F.seg_emit_first[s]; P.emit_end = F.seg_emit_first[s] + sg.ntiles;
+
             P.has_multi = 1;
         } else {
             P.mt_tile_begin = P.mt_tile_end = 0; P.mt_seg_begin = P.mt_seg_end = 0; P.has_multi = 0;
-            P.emit_begin = P.emit_end = 0;
+
         }
         // animation must be applied once: host tables carry the flag on the instance,
         // so later pairs of the same model use a copy without it.
@@ -688,7 +716,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
             P.insts = ctx->insts_noanim;
         }
         animated[sg.inst] = 1;
-        uint32_t items = std::max(sg.ntiles, 1u);
+        uint32_t items = std::max({sg.ntiles, P.vitem_end - P.vitem_begin, 1u});
         if ((rc = launch_one(ctx, P, ctl + s, items, st))) return rc;
     }
     return T3D_OK;

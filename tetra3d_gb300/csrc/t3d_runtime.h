@@ -46,12 +46,12 @@ struct Scene {
     std::vector<t3d_light_desc> lights;
     std::vector<std::vector<uint32_t>> lists;
     uint64_t nverts = 0, ntris = 0;
-    DevBuf va, vb, vc, idx, dmeshes, dmodels, cells;
+    DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     uint64_t device_bytes() const {
-        return va.cap + vb.cap + vc.cap + idx.cap + dmeshes.cap + dmodels.cap + cells.cap;
+        return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap;
     }
     void release() {
-        va.release(); vb.release(); vc.release(); idx.release();
+        va.release(); vb.release(); vc.release(); idx.release(); centers.release();
         dmeshes.release(); dmodels.release(); cells.release();
     }
 };
@@ -67,13 +67,14 @@ struct FrameTables {
     std::vector<DevSeg> segs;
     std::vector<t3d_segment_info> seg_info;
     std::vector<uint32_t> seg_mt_seg;
-    std::vector<uint32_t> tile_seg, mt_tiles, mt_segs, emit_seg, emit_chunk, seg_emit_first;
+    std::vector<uint32_t> tile_seg, mt_tiles, mt_segs;
+    std::vector<uint32_t> vitem_seg, vitem_chunk, seg_vitem_first;
     uint64_t nscratch = 0, nslots = 0;
     void clear() {
         jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
         insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
         seg_mt_seg.clear(); tile_seg.clear(); mt_tiles.clear(); mt_segs.clear();
-        emit_seg.clear(); emit_chunk.clear(); seg_emit_first.clear();
+        vitem_seg.clear(); vitem_chunk.clear(); seg_vitem_first.clear();
         nscratch = 0; nslots = 0;
     }
 };
@@ -97,11 +98,12 @@ struct t3d_ctx {
     t3d::FrameParams params;
     const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
     t3d::HostBuf table_host, readback;
-    t3d::DevBuf table_dev, ctl, preps, order, vis_idx, vis_depth, tile_count, tile_hist,
+    t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, tile_count, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
     uint64_t last_h2d = 0;
     uint32_t launches = 0;
+    uint32_t last_grid = 0;
     bool frame_pending = false;
     bool frame_valid = false;
     t3d_stats stats{};
