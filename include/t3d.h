@@ -352,6 +352,52 @@ int t3d_server_poll(t3d_server* srv, t3d_completion* out, uint32_t max, uint32_t
  * until all complete; completions in id order into out[n]. */
 int t3d_server_replay(t3d_server* srv, const t3d_request* reqs, uint32_t n, t3d_completion* out);
 
+/* ---- rendering without allocation ------------------------------------------ */
+/* For callers that cannot allocate device memory while they render -- an engine
+ * or rasteriser that owns the device memory budget through its own allocator, a
+ * real-time render thread where cudaMalloc/cudaFree would synchronise the device,
+ * or code already short of memory. This entry point has no counterpart in the
+ * reference: it renders one render pair (one model, one mesh part) from mesh and
+ * output buffers the caller owns in device memory, and keeps every intermediate
+ * in a fixed 16 MiB __device__ array inside the library (held on every GPU that
+ * loads the library until the process exits). It allocates nothing.
+ * Limits per call: 65536 vertices, 131072 mesh triangles, T3D_MAX_LIGHTS_PER_MODEL
+ * lights; larger requests return T3D_E_INVAL with a message in `error`.
+ * All calls share that array: calls that overlap on the GPU race and corrupt each
+ * other, so serialise them. The first call on a device sets the library up for it
+ * (symbol address, kernel attributes); make it before any stream capture. The call
+ * waits for `stream` before returning its status. Output: out_count visible
+ * triangles, written densely from slot 0, 3 corners each, in draw order. */
+typedef struct t3d_noalloc_args {
+    /* mesh streams in device memory, SoA as in t3d_mesh_desc (colors may be NULL) */
+    const float*          positions;
+    const float*          normals;
+    const float*          uvs;
+    const float*          colors;
+    const uint32_t*       indices;       /* 3 * num_triangles, mesh-absolute */
+    const float*          volume_cells;  /* device RGBA cells for volume lights, or NULL */
+    /* outputs in device memory, room for tri_count triangles */
+    float*                out_xyuv;      /* 3 * 4 floats per triangle */
+    float*                out_rgba;      /* 3 * 4 floats per triangle */
+    float*                out_depth;     /* 3 floats per triangle */
+    uint32_t*             out_count;     /* visible triangles */
+    /* host descriptors */
+    const t3d_model_desc*  model;        /* `mesh` and `light_list` are ignored */
+    const t3d_light_desc*  lights;       /* the model's lights in list order */
+    const t3d_camera_desc* camera;
+    uint32_t              num_vertices;
+    uint32_t              num_triangles;
+    uint32_t              tri_start;     /* the part: triangles [tri_start, tri_start + tri_count) */
+    uint32_t              tri_count;
+    uint32_t              num_lights;
+    uint32_t              reserved;
+    float                 dim_min[3];    /* Mesh.Dimensions */
+    float                 dim_max[3];
+    t3d_material          mat;
+    char                  error[128];    /* out: message when the call fails */
+} t3d_noalloc_args;
+int t3d_render_part_noalloc(int device, t3d_noalloc_args* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -116,6 +116,16 @@ class Completion(C.Structure):
                 ("done_s", C.c_double), ("checksum", C.c_uint64)]
 
 
+class NoallocArgs(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p), ("colors", C.c_void_p),
+                ("indices", C.c_void_p), ("volume_cells", C.c_void_p), ("out_xyuv", C.c_void_p),
+                ("out_rgba", C.c_void_p), ("out_depth", C.c_void_p), ("out_count", C.c_void_p),
+                ("model", C.POINTER(ModelDesc)), ("lights", C.POINTER(LightDesc)), ("camera", C.POINTER(CameraDesc)),
+                ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32), ("tri_start", C.c_uint32),
+                ("tri_count", C.c_uint32), ("num_lights", C.c_uint32), ("reserved", C.c_uint32),
+                ("dim_min", C.c_float * 3), ("dim_max", C.c_float * 3), ("mat", Material), ("error", C.c_char * 128)]
+
+
 # name -> (restype, argtypes) for every entry point of include/t3d.h
 _VP = C.c_void_p
 SIGNATURES = {
@@ -143,6 +153,7 @@ SIGNATURES = {
     "t3d_server_submit": (C.c_int, [_VP, C.POINTER(Request)]),
     "t3d_server_poll": (C.c_int, [_VP, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),
     "t3d_server_replay": (C.c_int, [_VP, C.POINTER(Request), C.c_uint32, C.POINTER(Completion)]),
+    "t3d_render_part_noalloc": (C.c_int, [C.c_int, C.POINTER(NoallocArgs), _VP]),
 }
 
 _lib = None

@@ -157,7 +157,7 @@ void build_camera(const t3d_camera_desc& d, JobCam& c) {
 }
 
 // beginRender (light.go:110-113, :318-320): per frame, per light.
-static void build_light(const t3d_light_desc& d, DevLight& L) {
+void build_light(const t3d_light_desc& d, DevLight& L) {
     memset(&L, 0, sizeof L);
     L.type = d.type;
     for (int i = 0; i < 3; i++) {

@@ -116,6 +116,7 @@ struct t3d_ctx {
 namespace t3d {
 void set_err(t3d_ctx* c, const char* fmt, ...);
 void build_camera(const t3d_camera_desc& d, JobCam& c);
+void build_light(const t3d_light_desc& d, DevLight& L);
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out);
 int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n);
 int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate);
