@@ -160,7 +160,7 @@ def run_ours(args, rank, world, local_rank):
 
     import torch
     import __graft_entry__
-    from tetra3d_gb300 import abi, scenes
+    from tetra3d_gb300 import abi, replicas, scenes
     from tetra3d_gb300.runtime import Context
 
     __graft_entry__.build()
@@ -208,12 +208,7 @@ def run_ours(args, rank, world, local_rank):
     v1, b1 = ctx.counters()
     vis = v1 - v0
     alg_bytes = (b1 - b0) + 108 * vis
-    if dist is not None:
-        t = torch.tensor([ms, float(vis), float(alg_bytes)], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms, vis, alg_bytes = float(mx[0]), float(t[1]), float(t[2])
+    ms, vis, alg_bytes = replicas.combine(ms, vis, alg_bytes, dist, device="cuda")
     value = vis / (ms / 1e3)
     ms_per_step = ms / args.steps
     st_last = ctx.sync()

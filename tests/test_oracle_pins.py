@@ -1,0 +1,150 @@
+"""Pins the oracle (CPU restatement) to what the reference itself checks and to
+independently computed known answers. No GPU needed."""
+import ctypes as C
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from tetra3d_gb300 import abi, scenes
+from oracle import pyoracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+F = np.float32
+
+
+def go_equals(a, b, eps=1e-4):
+    """Matrix4.Equals (matrix.go:486-497): |a-b| > eps fails; NaN compares false, so it passes."""
+    d = np.abs(a.astype(np.float32) - b.astype(np.float32))
+    return not np.any(d > eps)
+
+
+def test_matrix_inversion_reference_test():
+    """TestMatrixInversion (matrix_test.go:36-62): M * M.Inverted() is the identity for the
+    reference's four matrices (the singular fourth passes through NaN comparisons, as in Go)."""
+    T = lambda x, y, z: scenes.translate(x, y, z)
+    S = lambda x, y, z: scenes.scale_m(x, y, z)
+    R = lambda x, y, z, a: pyoracle.mat_rotate(x, y, z, a)
+    mats = [
+        R(0, 1, 0, 0.1),
+        T(-10, 0.1, 3232.1976),
+        S(10, 0.1, -0.45),
+        pyoracle.mat_mult(pyoracle.mat_mult(T(-1, -1, -1), R(1, 0, 0.1, 0.334)), S(10, 1, 0)),
+    ]
+    ident = np.eye(4, dtype=np.float32)
+    for i, m in enumerate(mats):
+        prod = pyoracle.mat_mult(m, pyoracle.mat_inverted(m))
+        assert go_equals(prod, ident), f"matrix #{i}"
+
+
+def test_mult_two_restatements_agree():
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        a = rng.uniform(-100, 100, (4, 4)).astype(F)
+        b = rng.uniform(-100, 100, (4, 4)).astype(F)
+        assert np.array_equal(scenes.mult(a, b).view(np.uint32), pyoracle.mat_mult(a, b).view(np.uint32))
+
+
+def test_rotate_quaternion_unit_restatements_agree():
+    rng = np.random.default_rng(1)
+    for _ in range(100):
+        x, y, z = rng.uniform(-1, 1, 3).astype(F)
+        ang = F(rng.uniform(-3, 3))
+        assert np.array_equal(scenes.rotate(x, y, z, ang).view(np.uint32),
+                              pyoracle.mat_rotate(float(x), float(y), float(z), float(ang)).view(np.uint32))
+        q = scenes.random_quats(rng, 1)[0]
+        assert np.array_equal(scenes.quat_to_mat(q)[0].view(np.uint32),
+                              pyoracle.quat_to_mat(*[float(c) for c in q]).view(np.uint32))
+        v = rng.uniform(-5, 5, 3).astype(F)
+        assert np.array_equal(scenes.unit3(v).view(np.uint32), pyoracle.vec_unit(v).view(np.uint32))
+    # Vector3.Unit leaves unit-length and near-zero vectors unchanged (vector.go:258-266)
+    assert np.array_equal(pyoracle.vec_unit([1, 0, 0]), np.array([1, 0, 0], F))
+    assert np.array_equal(pyoracle.vec_unit([1e-9, 0, 0]), np.array([1e-9, 0, 0], F))
+
+
+def _kat_scene(case, cam, tex):
+    pos = np.array(case["positions"], F)
+    nrm = np.tile(np.array([0, 0, 1], F), (3, 1))
+    uv = np.array([[0.25, 0.75], [0.5, 0.5], [1.0, 0.0]], F)
+    # no light: a shadeless material (Material.Shadeless) keeps the colour unlit (camera.go:1521-1528)
+    mat = scenes.default_material(tex_w=float(tex[0]), tex_h=float(tex[1]), shadeless=int(case["light"] is None))
+    me = scenes.MeshData(pos, nrm, uv, np.array([[0, 1, 2]], np.uint32),
+                         parts=[dict(tri_start=0, tri_count=1, mat=mat)])
+    lights, lists = [], [[]]
+    L = case["light"]
+    if L is not None:
+        if L["type"] == "ambient":
+            lights = [scenes.light(abi.LIGHT_AMBIENT, energy=L["energy"])]
+        else:
+            lights = [scenes.light(abi.LIGHT_POINT, energy=L["energy"], rng_=L["range"], pos=L["pos"])]
+        lists = [[0]]
+    sd = scenes.SceneData([me], 1, lights, lists)
+    scenes.set_models_trs(sd, 0, [(0, 0, 0)], [(1, 1, 1)], scenes.ident()[None], frustum=0)
+    sd.camera = scenes.camera(w=cam["w"], h=cam["h"], fov=cam["fov"], near=cam["near"], far=cam["far"])
+    return sd
+
+
+def test_oracle_known_answers():
+    with open(os.path.join(HERE, "golden", "kat_single_triangles.json")) as fh:
+        kat = json.load(fh)
+    for case in kat["cases"]:
+        sd = _kat_scene(case, kat["camera"], kat["texture"])
+        got = pyoracle.render(sd, sd.camera)
+        assert (got.visible_tris == 1) == case["visible"], case["name"]
+        if not case["visible"]:
+            continue
+        want = np.array(case["corners"], F)  # (3, 9): x y u v r g b a depth
+        have = np.concatenate([got.xyuv[0], got.rgba[0], got.depth[0][:, None]], axis=1).astype(F)
+        assert np.array_equal(have.view(np.uint32), want.view(np.uint32)), (case["name"], have, want)
+
+
+def test_f64_twin_agrees_within_tolerance():
+    sd = scenes.uv_sphere_scene(3)
+    f32 = pyoracle.render(sd, sd.camera)
+    f64 = pyoracle.render(sd, sd.camera, f64=True)
+    # the visible sets may differ only at boundaries; the sphere has none near the edges
+    assert abs(f32.visible_tris - f64.visible_tris) <= 2
+    if f32.visible_tris == f64.visible_tris:
+        rel = np.abs(f32.xyuv.astype(np.float64) - f64.xyuv) / np.maximum(np.abs(f64.xyuv), 1.0)
+        assert rel.max() < 1e-5
+        rel = np.abs(f32.rgba.astype(np.float64) - f64.rgba) / np.maximum(np.abs(f64.rgba), 1e-3)
+        assert rel.max() < 1e-4
+
+
+def test_oracle_threads_do_not_change_results():
+    sd = scenes.small_variant("batched", 7)
+    a = pyoracle.render(sd, sd.camera, threads=1)
+    b = pyoracle.render(sd, sd.camera, threads=4)
+    assert a.segments == b.segments
+    assert np.array_equal(a.xyuv.view(np.uint32), b.xyuv.view(np.uint32))
+    assert np.array_equal(a.rgba.view(np.uint32), b.rgba.view(np.uint32))
+
+
+def test_bucket_sort_semantics_back_to_front():
+    """The 512-bin bucket sort (sortingTriangles.go:38-125): back-to-front walks bins 511..0 and keeps
+    triangle order inside a bin; keys are squared distances from the model-space camera."""
+    sd = scenes.uv_sphere_scene(4)
+    f = pyoracle.render(sd, sd.camera)
+    me = sd.meshes[0]
+    M = scenes.trs(sd.mv["position"][0], sd.mv["scale"][0], sd.mv["rotation"][0].reshape(4, 4))[0]
+    inv = pyoracle.mat_inverted(M)
+    p, s, r = np.zeros(3, F), np.zeros(3, F), np.zeros(16, F)
+    lib = pyoracle.load()
+    fp = lambda x: x.ctypes.data_as(C.POINTER(C.c_float))
+    inv = np.ascontiguousarray(inv, F)
+    lib.t3d_oracle_mat_decompose(fp(inv), fp(p), fp(s), fp(r))
+    r = r.reshape(4, 4)
+    cam = np.array(sd.camera.transform, F).reshape(4, 4)[3, :3]
+    ic = [((r[0, c] * cam[0] + r[1, c] * cam[1]) + r[2, c] * cam[2]) + r[3, c] + p[c] * (F(1) / s[c]) for c in range(3)]
+    tri = f.tri_index
+    ctr = ((me.positions[me.indices[tri, 0]] + me.positions[me.indices[tri, 1]]) + me.positions[me.indices[tri, 2]]) / F(3)
+    d = [((F(ic[0]) - c[0]) ** 2 + (F(ic[1]) - c[1]) ** 2) + (F(ic[2]) - c[2]) ** 2 for c in ctr.astype(F)]
+    d = np.array(d, F)
+    mn, mx = d.min(), d.max()
+    bins = np.clip((d - mn) / (mx - mn) * F(512), 0, 511).astype(np.int64)
+    assert np.all(np.diff(bins) <= 0), "back-to-front: bins must not increase"
+    for b in np.unique(bins):
+        sel = tri[bins == b]
+        assert np.all(np.diff(sel.astype(np.int64)) > 0), "triangle order inside a bin"

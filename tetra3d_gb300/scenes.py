@@ -598,6 +598,122 @@ def batched_scene(seed=4, n=4096, vmin=24, vmax=65536, nlights=32, box=200.0, w=
     return sd
 
 
+def _random_material(rng):
+    """One mesh part's Material with every option drawn at random (material.go:40-120)."""
+    alpha = 1.0 if rng.random() < 0.75 else float(rng.uniform(0.3, 0.9))
+    tex = [0.0, 64.0, 256.0][int(rng.integers(3))]
+    return default_material(
+        color=(float(rng.uniform(0.5, 1)), float(rng.uniform(0.5, 1)), float(rng.uniform(0.5, 1)), alpha),
+        tex_w=tex, tex_h=tex / 2, present=int(rng.random() < 0.95), backface_culling=int(rng.random() < 0.8),
+        sort_mode=int(rng.integers(3)), lighting_mode=int(rng.integers(3)), lv_shading_mode=int(rng.integers(4)),
+        shadeless=int(rng.random() < 0.1), visible=int(rng.random() < 0.95),
+        transparency_mode=[abi.TRANSPARENCY_AUTO, abi.TRANSPARENCY_AUTO, abi.TRANSPARENCY_OPAQUE,
+                           abi.TRANSPARENCY_ALPHA_CLIP, abi.TRANSPARENCY_TRANSPARENT][int(rng.integers(5))],
+        blend_source_over=int(rng.random() < 0.9), render_order=[0, 0, 0, 1, -1][int(rng.integers(5))])
+
+
+def feature_scene(seed=5, n=48, w=1280, h=720):
+    """Small meshes under every material, model and light option of the vertex stage.
+
+    Meshes: icospheres (flat normals, vertex colours) and noise grids split into 1-3 parts, cubes and a UV
+    sphere without a colour channel; each mesh copy gets random part materials (sort mode, backface culling,
+    lighting mode, light-volume shading mode, shadeless, visibility, transparency mode, additive blending,
+    render order, material alpha, texture size, nil material). Models: random transforms in front of the
+    camera plus a few behind it and beyond the far plane, random tint and alpha (one fully transparent),
+    invisible and shadeless models, frustum culling switched off on some. Lights: ambient, three point, two
+    directional and two volume lights; the scene list plus three LightGroups.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    bases = []
+    for lvl in (1, 2):
+        me = icosphere(lvl)
+        me.colors = rng.uniform(0.4, 1.0, (me.nverts, 4)).astype(F32)
+        bases.append(me)
+    for k in range(2):
+        sseed = int(rng.integers(1 << 30))
+        me = grid_mesh(14, 10, 4.0, 3.0, lambda X, Z, s=sseed: 0.5 * value_noise(s, X, Z, 2), x0=-2.0, z0=-1.5)
+        me.colors = rng.uniform(0.4, 1.0, (me.nverts, 4)).astype(F32)
+        bases.append(me)
+    bases.append(cube_mesh(1.5, 1.0, 2.0))
+    bases.append(uv_sphere(16, 8, 1.2))
+    meshes = []
+    for k in range(16):
+        b = bases[k % len(bases)]
+        T = b.ntris
+        nparts = 1 if T < 24 else int(rng.integers(1, 4))
+        cuts = sorted(set([0, T] + [int(c) for c in rng.integers(1, T, nparts - 1)]))
+        parts = [dict(tri_start=cuts[i], tri_count=cuts[i + 1] - cuts[i], mat=_random_material(rng))
+                 for i in range(len(cuts) - 1)]
+        meshes.append(MeshData(b.positions, b.normals, b.uvs, b.indices, colors=b.colors, parts=parts))
+    pos = np.stack([rng.uniform(-14, 14, n), rng.uniform(-8, 8, n), rng.uniform(-45, -4, n)], 1).astype(F32)
+    pos[0] = (0, 0, 150)    # far behind the camera: outside the frustum sphere
+    pos[1] = (2, 0, -90)    # beyond the far plane, frustum culling off below
+    scl = np.repeat(rng.uniform(0.5, 3.0, (n, 1)), 3, 1).astype(F32)
+    scl[2] = (1.0, 2.0, 0.5)  # non-uniform scale
+    rot = quat_to_mat(random_quats(rng, n))
+    cells = []
+    lights = [light(abi.LIGHT_AMBIENT, color=(0.9, 0.95, 1.0), energy=0.25)]
+    for _ in range(3):
+        lights.append(light(abi.LIGHT_POINT, color=rng.uniform(0.3, 1, 3), energy=rng.uniform(1, 4),
+                            rng_=rng.uniform(8, 30), pos=(rng.uniform(-12, 12), rng.uniform(-6, 6), rng.uniform(-40, -5))))
+    for d in ([0.3, 1.0, 0.2], [-0.7, -0.2, 0.6]):
+        lights.append(light(abi.LIGHT_DIRECTIONAL, color=rng.uniform(0.5, 1, 3), energy=rng.uniform(0.4, 1.2),
+                            rot=look_rotation(unit3(np.array(d, F32)))))
+    for c in ((-6.0, 0.0, -20.0), (7.0, 2.0, -30.0)):
+        c = np.asarray(c, F32)
+        vmin, vmax, cs = c - F32(9), c + F32(9), np.array([4.5, 6.0, 3.0], F32)
+        counts = light_volume_counts(vmin, vmax, cs)
+        first = len(cells)
+        for _ in range(int(np.prod(counts))):
+            cells.append(list(rng.uniform(0.1, 1.0, 3)) + [1.0])
+        lights.append(light(abi.LIGHT_VOLUME, energy=float(rng.uniform(0.5, 1.5)), vol=(vmin, vmax, cs, counts, first)))
+    lists = [list(range(len(lights))), [0, 1, 4], [0, 2, 3, 6], [5, 7, 1]]
+    groups = np.where(rng.random(n) < 0.5, -1, rng.integers(1, 4, n)).astype(np.int32)
+    mesh_of = rng.integers(0, len(meshes), n).astype(np.uint32)
+    colors = np.ones((n, 4), F32)
+    tint = rng.random(n) < 0.3
+    colors[tint, :3] = rng.uniform(0.3, 1.0, (int(tint.sum()), 3))
+    half = rng.random(n) < 0.15
+    colors[half, 3] = 0.5
+    colors[3, 3] = 0.0      # fully transparent model: skipped
+    sd = SceneData(meshes, n, lights, lists, cells=np.array(cells, F32), name=f"features{seed}")
+    set_models_trs(sd, mesh_of, pos, scl, rot, light_list=groups)
+    sd.mv["color"] = colors
+    sd.mv["frustum_culling"] = (rng.random(n) < 0.85).astype(np.int32)
+    sd.mv["frustum_culling"][0] = 1  # culled by SphereInFrustum
+    sd.mv["frustum_culling"][1] = 0  # reaches the per-triangle far-plane test
+    sd.mv["visible"][:2] = 1
+    sd.mv["visible"] = (rng.random(n) < 0.95).astype(np.int32)
+    sd.mv["shadeless"] = (rng.random(n) < 0.1).astype(np.int32)
+    sd.camera = feature_camera("persp", w, h)
+    return sd
+
+
+FEATURE_CAMERAS = ["persp", "ortho", "unlit", "fog_add", "fog_sub", "fog_overwrite", "corrected", "tilted"]
+
+
+def feature_camera(variant, w=1280, h=720):
+    """Camera options of camera.go: perspective / orthographic, lighting off, fog modes with depth
+    rendering off, perspective-corrected UVs, a rotated and moved camera."""
+    kw = dict(w=w, h=h, fov=65.0, near=0.1, far=60.0)
+    if variant == "ortho":
+        kw.update(perspective=0, ortho_scale=40.0)
+    elif variant == "unlit":
+        kw.update(lighting_on=0)
+    elif variant.startswith("fog_"):
+        kw.update(render_depth=0, fog_on=1,
+                  fog_mode={"fog_add": abi.FOG_ADD, "fog_sub": abi.FOG_SUB, "fog_overwrite": abi.FOG_OVERWRITE}[variant])
+    elif variant == "tilted":
+        kw.update(pos=(3.0, 4.0, 2.0), rot=mult(rotate(1, 0, 0, deg2rad(-12.0)), rotate(0, 1, 0, deg2rad(8.0))))
+    c = camera(**kw)
+    if variant.startswith("fog_"):
+        c.fog_range[:] = [0.15, 0.85]
+        c.fog_color[:] = [0.4, 0.5, 0.9, 1.0]
+    if variant == "corrected":
+        c.perspective_corrected = 1
+    return c
+
+
 def small_variant(kind, seed):
     """Reduced-size versions of the workloads for oracle comparisons."""
     if kind == "sphere":
