@@ -260,6 +260,14 @@ def run_ours(args, rank, world, local_rank):
         e2e = {"value": ev / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d // ek),
                "d2h_bytes_per_step": int(d2h // ek), "ms_per_step": el / ek * 1e3, "steps": ek}
 
+    # ---- serving sweep (continuous batching over 64 resident scenes) ----
+    serve = None
+    if rank == 0 and not args.no_serving and args.workload == "batched":
+        ctx.release(sid)
+        sid = None
+        serve = serving_sweep(ctx, [int(r) for r in args.rates.split(",")], args.serve_seconds,
+                              args.serve_max_requests)
+
     # ---- CPU baseline (oracle port, 1 thread) ----
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -296,11 +304,85 @@ def run_ours(args, rank, world, local_rank):
             "plain": plain,
             "autotune": tuned,
             "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,
+            "serving": serve,
         }
         print(json.dumps(line))
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+# -------------------------------------------------------------- serving ----
+def serving_sweep(ctx, rates, seconds, max_requests, seed=7, baseline_requests=1000):
+    """Continuous-batching server over 64 resident scenes at Poisson rates; then the same requests
+    rendered one request per launch, synchronously (the plain request loop)."""
+    from tetra3d_gb300 import serving
+    from tetra3d_gb300.runtime import Server
+    t0 = time.perf_counter()
+    sds, centres = serving.serving_scenes(64)
+    gen_s = time.perf_counter() - t0
+    sids = [ctx.upload(sd) for sd in sds]
+    tris = [sd.total_tris() for sd in sds]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    srv = Server(ctx, hbm_budget_bytes=150 << 30, max_batch=64, streams=4, verify=False)
+    out = {"scenes": len(sds), "scene_tris_min": int(min(tris)), "scene_tris_max": int(max(tris)),
+           "scene_tris_total": int(sum(tris)), "hbm_budget_gb": 150, "max_batch": 64, "slots": 4,
+           "scene_gen_s": round(gen_s, 2), "rates": []}
+    try:
+        jobs, arr = serving.poisson_requests(rng, sids, sds, centres, 2000.0, 128)  # warm-up
+        srv.replay(jobs, arr)
+        for rate in rates:
+            n = int(min(max_requests, max(200, rate * seconds)))
+            jobs, arr = serving.poisson_requests(rng, sids, sds, centres, float(rate), n)
+            w0 = time.perf_counter()
+            comps = srv.replay(jobs, arr)
+            wall = time.perf_counter() - w0
+            row = dict(rate_req_s=rate, **serving.latency_summary(comps), wall_s=round(wall, 3))
+            out["rates"].append(row)
+        # one request per launch, synchronously, over the last rate's requests
+        jobs = jobs[:baseline_requests]
+        lat, vis = [], 0
+        b0 = time.perf_counter()
+        for j in jobs:
+            s0 = time.perf_counter()
+            ctx.render_jobs([j], mode=1)
+            vis += int(ctx.sync().visible_tris)
+            lat.append((time.perf_counter() - s0) * 1e3)
+        el = time.perf_counter() - b0
+        out["one_request_per_launch"] = {"requests": len(jobs), "tris_per_s": vis / el, "req_per_s": len(jobs) / el,
+                                         "p50_ms": float(np.percentile(lat, 50)),
+                                         "p99_ms": float(np.percentile(lat, 99))}
+    finally:
+        srv.close()
+        for s in sids:
+            ctx.release(s)
+    return out
+
+
+def run_serving(args, rank, world, local_rank):
+    import torch
+    import __graft_entry__
+    from tetra3d_gb300.runtime import Context
+    __graft_entry__.build()
+    torch.cuda.set_device(local_rank)
+    if rank != 0:
+        return
+    ctx = Context(local_rank)
+    rates = [int(r) for r in args.rates.split(",")]
+    with ClockSampler(local_rank) as clk:
+        sv = serving_sweep(ctx, rates, args.serve_seconds, args.serve_max_requests)
+    top = max(sv["rates"], key=lambda r: r["tris_per_s"])
+    line = {"metric": METRIC, "value": top["tris_per_s"], "unit": UNIT, "n_gpus": world, "steps": len(rates),
+            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "serving_64_scenes_poisson", "rates_req_s": rates,
+                       "form": "continuous batching server (t3d_server), requests via the C ABI"},
+            "serving": sv, "clocks": clk.summary(),
+            "e2e": {"value": top["tris_per_s"], "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                    "note": "requests enter through t3d_server_replay from host memory; completions are read back"},
+            "served_over_one_request_per_launch": top["tris_per_s"] / sv["one_request_per_launch"]["tris_per_s"]}
+    print(json.dumps(line))
+    ctx.close()
 
 
 # ------------------------------------------------------------ reference ----
@@ -355,6 +437,10 @@ def main():
     ap.add_argument("--tune", action="store_true", help="run the autotuner before the timed region")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep in the default run")
+    ap.add_argument("--rates", default="100,1000,5000,20000", help="serving request rates (req/s)")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival span per serving rate")
+    ap.add_argument("--serve-max-requests", type=int, default=8000)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
@@ -365,8 +451,7 @@ def main():
         run_reference(args, rank, world)
         return
     if args.workload == "serving":
-        import bench_serving
-        bench_serving.main(args)
+        run_serving(args, rank, world, local_rank)
         return
     run_ours(args, rank, world, local_rank)
 

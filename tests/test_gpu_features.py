@@ -1,0 +1,238 @@
+"""GPU vs oracle, bit for bit, through the C ABI, over every option of the stage:
+material / model / light options (feature scenes) under every camera option, both
+forms; several jobs with light masks in one launch; animation inside the launch and
+through CUDA graph replay; transform read-back; serving (same bits alone and in a
+mix); argument errors."""
+import ctypes as C
+import time
+
+import numpy as np
+import pytest
+
+from tetra3d_gb300 import abi, scenes
+from tetra3d_gb300.runtime import Server, job
+from oracle import pyoracle
+from tests.parity import assert_frames_equal, bits
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("variant", scenes.FEATURE_CAMERAS)
+@pytest.mark.parametrize("mode", [abi.MODE_BATCHED, abi.MODE_PLAIN])
+def test_feature_scenes_match_oracle(ctx, variant, mode):
+    for seed in (5, 6):
+        sd = scenes.feature_scene(seed)
+        cam = scenes.feature_camera(variant)
+        sid = ctx.upload(sd)
+        try:
+            ctx.render(sid, cam, mode=mode)
+            got = ctx.download()
+        finally:
+            ctx.release(sid)
+        ref = pyoracle.render(sd, cam)
+        assert ref.visible_tris > 0
+        assert_frames_equal(got, ref, f"features{seed}/{variant}/mode{mode}")
+
+
+class _JobFrame:
+    def __init__(self, segments, xyuv, rgba, depth):
+        self.segments, self.xyuv, self.rgba, self.depth = segments, xyuv, rgba, depth
+        self.visible_tris = int(xyuv.shape[0])
+
+
+def split_jobs(frame, njobs):
+    """Per-job views of a multi-job download (compacted in segment order)."""
+    out, b = [], 0
+    per = [[] for _ in range(njobs)]
+    for s in frame.segments:
+        per[s["job"]].append((s, b))
+        b += s["count"]
+    for j in range(njobs):
+        idx = np.concatenate([np.arange(b0, b0 + s["count"]) for s, b0 in per[j]] or [np.zeros(0, np.int64)])
+        idx = idx.astype(np.int64)
+        out.append(_JobFrame([s for s, _ in per[j]], frame.xyuv[idx], frame.rgba[idx], frame.depth[idx]))
+    return out
+
+
+def test_jobs_with_light_masks_in_one_launch(ctx):
+    a = scenes.feature_scene(5)
+    b = scenes.small_variant("batched", 12)
+    sa, sb = ctx.upload(a), ctx.upload(b)
+    try:
+        specs = [(sa, a, scenes.feature_camera("persp"), None),
+                 (sa, a, scenes.feature_camera("tilted"), ((1 << 128) - 1) & ~((1 << 1) | (1 << 6))),
+                 (sb, b, scenes.feature_camera("fog_sub"), ((1 << 128) - 1) & ~(1 << 3)),
+                 (sb, b, b.camera, None)]
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render_jobs([job(s, cam, mask) for s, _, cam, mask in specs], mode=mode)
+            parts = split_jobs(ctx.download(), len(specs))
+            for j, (s, sd, cam, mask) in enumerate(specs):
+                assert_frames_equal(parts[j], pyoracle.render(sd, cam, light_mask=mask), f"job{j}/mode{mode}")
+    finally:
+        ctx.release(sa)
+        ctx.release(sb)
+
+
+def _host_transforms(sd, k):
+    n = sd.nmodels
+    rot = sd.mv["rotation"].reshape(n, 4, 4).copy()
+    step = sd.mv["rotate_step"].reshape(n, 4, 4)
+    for _ in range(k):
+        rot = scenes.mult(step, rot)
+    return scenes.trs(sd.mv["position"], sd.mv["scale"], rot)
+
+
+def test_animation_in_launch_matches_oracle(ctx):
+    sd = scenes.small_variant("batched", 8)
+    sid = ctx.upload(sd)
+    try:
+        for k in (1, 2, 3):
+            ctx.render(sid, sd.camera, mode=abi.MODE_BATCHED, animate=True)
+            assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera, animate_frames=k), f"animate {k}")
+        T = ctx.transforms(sid, sd.nmodels)
+        assert np.array_equal(bits(T), bits(_host_transforms(sd, 3)))
+    finally:
+        ctx.release(sid)
+
+
+def test_graph_replay_matches_oracle(ctx):
+    sd = scenes.small_variant("batched", 9)
+    sid = ctx.upload(sd)
+    try:
+        ctx.graph_capture(sid, sd.camera, animate=True)
+        ctx.graph_replay(4)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera, animate_frames=4), "graph x4")
+        ctx.graph_replay(1)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera, animate_frames=5), "graph x5")
+        assert np.array_equal(bits(ctx.transforms(sid, sd.nmodels)), bits(_host_transforms(sd, 5)))
+        # static capture: replays give the same frame every time
+        ctx.set_models(sid, sd)
+        ctx.graph_capture(sid, sd.camera, animate=False)
+        ctx.graph_replay(3)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "static graph")
+    finally:
+        ctx.release(sid)
+
+
+def test_set_models_between_frames(ctx):
+    sd = scenes.feature_scene(6)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, sd.camera)
+        ctx.sync()
+        sd.mv["position"][:, 0] += np.float32(1.5)
+        sd.mv["transform"] = scenes.trs(sd.mv["position"], sd.mv["scale"],
+                                        sd.mv["rotation"].reshape(-1, 4, 4)).reshape(-1, 16)
+        ctx.set_models(sid, sd, first=4, n=sd.nmodels - 4)  # the first four keep their old place
+        moved = scenes.feature_scene(6)
+        moved.mv[4:] = sd.mv[4:]
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), pyoracle.render(moved, sd.camera), "partial set_models")
+    finally:
+        ctx.release(sid)
+
+
+def _fnv_frame(f):
+    """FNV-1a over xyuv, rgba, depth bytes of each segment in emit order (the server's checksum)."""
+    h = 1469598103934665603
+    b = 0
+    for s in f.segments:
+        n = s["count"]
+        if not n:
+            continue
+        for arr in (f.xyuv[b:b + n], f.rgba[b:b + n], f.depth[b:b + n]):
+            for byte in np.ascontiguousarray(arr, np.float32).tobytes():
+                h = ((h ^ byte) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+        b += n
+    return h
+
+
+def _drain(srv, n, timeout=60.0):
+    got, t0 = {}, time.time()
+    while len(got) < n and time.time() - t0 < timeout:
+        for c in srv.poll():
+            got[c.id] = c
+        time.sleep(0.002)
+    assert len(got) == n, f"{len(got)} of {n} completions"
+    return got
+
+
+def test_serving_same_bits_alone_and_in_mix(ctx):
+    sds = [scenes.feature_scene(s) for s in (5, 6, 7)] + [scenes.small_variant("batched", 13)]
+    sids = [ctx.upload(sd) for sd in sds]
+    cams = [scenes.feature_camera(v) for v in ("persp", "tilted", "fog_add", "ortho")]
+    reqs = [(i, sids[i % 4], sds[i % 4], cams[(i // 4) % 4]) for i in range(12)]
+    srv = Server(ctx, hbm_budget_bytes=8 << 30, max_batch=8, streams=2, verify=True)
+    try:
+        alone = {}
+        for rid, sid, sd, cam in reqs:
+            assert srv.submit(job(sid, cam), rid) == abi.T3D_OK
+            c = _drain(srv, 1)[rid]
+            assert c.status == abi.T3D_OK
+            alone[rid] = (c.checksum, c.visible_tris)
+        for rid, sid, sd, cam in reqs:
+            assert srv.submit(job(sid, cam), 100 + rid) == abi.T3D_OK
+        mix = _drain(srv, len(reqs))
+        for rid, sid, sd, cam in reqs:
+            c = mix[100 + rid]
+            assert c.status == abi.T3D_OK
+            assert (c.checksum, c.visible_tris) == alone[rid], f"request {rid} differs in the mix"
+            assert c.admit_s >= c.arrival_s and c.done_s >= c.admit_s
+        for rid, sid, sd, cam in reqs[:4]:  # the checksum is over the oracle's bits
+            ref = pyoracle.render(sd, cam)
+            assert alone[rid] == (_fnv_frame(ref), ref.visible_tris)
+    finally:
+        srv.close()
+        for s in sids:
+            ctx.release(s)
+
+
+def test_serving_admission(ctx):
+    sd = scenes.small_variant("batched", 14)
+    sid = ctx.upload(sd)
+    srv = Server(ctx, hbm_budget_bytes=1 << 10, max_batch=4, streams=1, verify=False)
+    try:
+        assert srv.submit(job(sid, sd.camera), 1) == abi.T3D_E_ADMIT  # larger than the whole budget
+        assert srv.submit(job(12345, sd.camera), 2) == abi.T3D_E_NOTFOUND
+    finally:
+        srv.close()
+        ctx.release(sid)
+
+
+def test_argument_errors(ctx):
+    lib = ctx.lib
+    sd = scenes.uv_sphere_scene(1)
+    sid = ctx.upload(sd)
+    try:
+        assert lib.t3d_scene_release(ctx.h, 999999) == abi.T3D_E_NOTFOUND
+        assert lib.t3d_render(ctx.h, 999999, C.byref(sd.camera), abi.MODE_BATCHED, 0, None) == abi.T3D_E_NOTFOUND
+        assert lib.t3d_render(ctx.h, sid, C.byref(sd.camera), 7, 0, None) == abi.T3D_E_INVAL
+        j = (abi.JobDesc * 2)(job(sid, sd.camera), job(sid, sd.camera))
+        assert lib.t3d_render_jobs(ctx.h, j, 2, abi.MODE_BATCHED, 1, None) == abi.T3D_E_INVAL  # animate twice
+        fresh = C.c_void_p()
+        assert lib.t3d_create(0, C.byref(fresh)) == abi.T3D_OK
+        assert lib.t3d_graph_replay(fresh, 1, None) == abi.T3D_E_INVAL
+        lib.t3d_destroy(fresh)
+        bad = scenes.uv_sphere_scene(1)
+        bad.mv["mesh"][0] = 5
+        d = bad.desc()
+        out = C.c_uint32()
+        assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+        assert b"mesh" in lib.t3d_last_error(ctx.h)
+        bad = scenes.uv_sphere_scene(1)
+        bad.meshes[0].parts[0]["mat"]["sort_mode"] = 9
+        d = bad.desc()
+        assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+        bad = scenes.uv_sphere_scene(1)
+        bad.meshes[0].indices[3, 1] = bad.meshes[0].nverts  # index past the vertex array
+        d = bad.desc()
+        assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+        bad = scenes.uv_sphere_scene(1)
+        bad.mv["light_list"][0] = 3
+        d = bad.desc()
+        assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+        # the context still works after rejected calls
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "after errors")
+    finally:
+        ctx.release(sid)

@@ -444,7 +444,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             uint32_t cnt = 0;
             for (uint32_t li : sc->lists[list]) {
                 if (!light_enabled(jobs[j].light_mask, li)) continue;
-                F.inst_light_idx.push_back(light_base + li);
+                F.inst_light_idx.push_back(li);  // relative to the job's light table (DevJob.lights)
                 cnt++;
             }
             if (cnt > (uint32_t)kMaxLights) {
