@@ -89,7 +89,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     for (auto& kv : ctx->scenes) kv.second->release();
     ctx->scenes.clear();
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
-                      &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax,
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum})
         b->release();
     ctx->table_host.release();
@@ -272,7 +272,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.launches = ctx->launches;
     size_t scratch = 0;
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
-                      &ctx->vis_idx, &ctx->vis_depth, &ctx->tile_count, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
         scratch += b->cap;
     s.scratch_bytes = scratch;
     s.h2d_bytes = ctx->last_h2d;

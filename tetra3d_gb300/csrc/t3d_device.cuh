@@ -30,7 +30,9 @@ enum : uint32_t {
     SEG_COLORS = 1u << 3,       // mesh has an active vertex colour channel
     SEG_MAT = 1u << 4,          // MeshPart.Material != nil
     SEG_MULTI = 1u << 5,        // segment spans more than one tile
+    SEG_WIDE = 1u << 6,         // vertex range above 65536: local vertex offsets do not fit 16 bits
 };
+constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }
 __host__ __device__ inline uint32_t seg_light_mode(uint32_t f) { return (f >> 10) & 3u; }
 __host__ __device__ inline uint32_t seg_lv_mode(uint32_t f) { return (f >> 12) & 3u; }
@@ -135,6 +137,19 @@ struct DevSeg {
     float tex_w, tex_h, pad2[2];
 };
 
+// Everything the triangle, histogram and rank phases need about one tile, in
+// one 64-byte record so a work item starts after a single dependent load.
+struct TileDesc {
+    uint32_t seg, inst, job, flags;     // render pair, instance, job, segment flags
+    uint32_t t0, t1;                    // mesh-absolute triangle range of the tile
+    uint32_t tbase;                     // the mesh's first triangle in the scene pool
+    uint32_t vmin, vscratch, out_base;  // segment: first vertex, first record, first output slot
+    uint32_t mt;                        // multi-tile tile number (SEG_MULTI), else 0
+    uint32_t pad0;
+    float nearp, farp;                  // job camera near / far planes
+    uint32_t pad1[2];
+};
+
 // Launch control block (zeroed before every launch).
 struct Ctl {
     uint32_t bar_count;
@@ -157,8 +172,8 @@ struct FrameParams {
     DevPrep* preps;
     const uint32_t* inst_light_idx;
     const DevSeg* segs;
-    const uint32_t* tile_seg;     // tile -> segment
-    const uint32_t* mt_tiles;     // multi-tile tiles (global tile numbers)
+    const TileDesc* tiles;        // per tile
+    const TileDesc* mt_desc;      // per multi-tile tile (a copy of its tile's record)
     const uint32_t* mt_segs;      // multi-tile segments
     const uint32_t* vitem_seg;    // vertex work item -> segment
     const uint32_t* vitem_chunk;  // vertex work item -> chunk of vchunk vertices
@@ -166,9 +181,13 @@ struct FrameParams {
     float4* vcull;                // per-vertex records: (cx, cy, clipZ, depth)
     float4* vxyuv;                // emitted screen position + UV
     float4* vrgba;                // emitted colour
-    uint16_t* vis_idx;            // per multi-tile tile: up to tile_tris visible entries
-    float* vis_depth;
+    // per multi-tile tile, tile_tris entries in blockDim/32 regions (one per warp of the
+    // triangle phase, tile_tris/(blockDim/32) entries each, filled from the front)
+    uint16_t* vis_idx;            // triangle within the tile (SEG_WIDE only)
+    float* vis_depth;             // depth key
+    uint16_t* vis_vloc;           // 3 vertex offsets within the segment's range (not SEG_WIDE)
     uint32_t* tile_count;         // visible per multi-tile tile
+    uint32_t* tile_wcnt;          // per multi-tile tile, kMaxWarps counts: entries in each warp's list region
     uint32_t* tile_hist;          // per multi-tile tile: kBins counters, then bases
     uint32_t* seg_minmax;         // 2 per segment: min bits, max bits
     uint32_t* seg_count;          // visible per segment (output)

@@ -55,6 +55,22 @@ __device__ bool grid_barrier(Ctl* ctl) {
     return vload(&ctl->err) == 0;
 }
 
+// Loads of per-vertex records. The records are written only in the vertex
+// phase, before the first grid barrier, and every read comes after it; no SM
+// can hold a stale L1 line of them (L1 starts empty each launch), so the reads
+// may use L1, where the corners of one tile find their shared vertices.
+#ifndef T3D_REC_L1
+#define T3D_REC_L1 1
+#endif
+template <typename V>
+__device__ __forceinline__ V rec_load(const V* p) {
+#if T3D_REC_L1
+    return *p;
+#else
+    return __ldcg(p);
+#endif
+}
+
 __device__ __forceinline__ uint32_t next_item(Ctl* ctl, int q, uint32_t* s_item) {
     __syncthreads();
     if (threadIdx.x == 0) *s_item = atomicAdd(&ctl->queue[q], 1u);
@@ -328,14 +344,15 @@ struct SmemLayout {
     uint16_t* lidx;
     float* depth;
     uint16_t* bin;
-    uint16_t* perm;   // single-tile segments: list entry of each output position
+    uint16_t* perm;   // list entry of each output position of the tile
+    uint16_t* vloc;   // rank phase: 3 vertex offsets per list entry (aliases depth + lidx, unused there)
 };
 
 __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t tile) {
     SmemLayout L;
     size_t o = 0;
     L.ts = (TileSmem*)(smem + o);
-    o += sizeof(TileSmem);
+    o += (sizeof(TileSmem) + 15) & ~(size_t)15;  // 16-byte alignment for the vector accesses below
     L.whist = (uint32_t*)(smem + o);
     o += sizeof(uint32_t) * (blockDim.x >> 5) * kBins;
     L.depth = (float*)(smem + o);
@@ -345,6 +362,7 @@ __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t 
     L.bin = (uint16_t*)(smem + o);
     o += 2 * (size_t)tile;
     L.perm = (uint16_t*)(smem + o);
+    L.vloc = (uint16_t*)L.depth;  // 6 bytes per entry = the depth (4) and lidx (2) arrays
     return L;
 }
 
@@ -458,7 +476,7 @@ __device__ __forceinline__ float4 clip_of(const float4* mc, float x, float y, fl
 //   rgba  = vertex colour * model/material colour * light (camera.go:1726-1742)
 // Every value depends only on the vertex, the model, the part and the camera, so
 // computing it once per vertex gives the reference's per-corner values bit for bit.
-__device__ __forceinline__ void vertex_record(const ModelSmem& ms, uint32_t v, const float4 a, const float4 b,
+__device__ __forceinline__ void vertex_record(const ModelSmem& ms, const float4 a, const float4 b, const float4 k,
                                               float4& cull, float4& xyuv, float4& rgba) {
     const EmitConst& e = ms.ec;
     const uint32_t f = e.flags;
@@ -487,7 +505,6 @@ __device__ __forceinline__ void vertex_record(const ModelSmem& ms, uint32_t v, c
     }
     float cr, cg, cb, ca;
     if (f & EC_COLORS) {
-        const float4 k = e.vc[v];
         cr = k.x * e.mp[0]; cg = k.y * e.mp[1]; cb = k.z * e.mp[2]; ca = k.w * e.mp[3];
     } else {
         cr = e.mp[0]; cg = e.mp[1]; cb = e.mp[2]; ca = e.mp[3];
@@ -612,29 +629,74 @@ __device__ void rank_tile(const SmemLayout& L, uint32_t sort_mode) {
 
 // Emits a ranked tile by copying per-vertex records: one thread per output
 // corner in the tile's output order, so consecutive threads read vertices of
-// the same tile and write consecutive corners of one bin run.
-__device__ void tile_emit(const FrameParams& P, const DevSeg& seg, const SmemLayout& L, const uint32_t* __restrict__ midx,
-                          uint32_t t0, uint32_t n, uint32_t sort_mode, bool single) {
+// the same tile and write consecutive corners of one bin run. Each thread keeps
+// kEmitILP corners in flight: their record addresses first, then all loads,
+// then all stores.
+#ifndef T3D_STREAM_STORES
+#define T3D_STREAM_STORES 0  // write-back stores: a tile writes short bin runs that L2 merges into full lines
+#endif
+#ifndef T3D_EMIT_ILP
+#define T3D_EMIT_ILP 1
+#endif
+constexpr int kEmitILP = T3D_EMIT_ILP;
+#ifndef T3D_EMIT_ILP_SINGLE
+#define T3D_EMIT_ILP_SINGLE 1  // single-tile segments, emitted inside the register-heavy triangle phase
+#endif
+constexpr int kEmitILPSingle = T3D_EMIT_ILP_SINGLE;
+template <int kILP>
+__device__ void tile_emit(const FrameParams& P, const TileDesc& td, const SmemLayout& L, const uint32_t* __restrict__ midx,
+                          uint32_t n, uint32_t sort_mode, bool single, bool use_vloc) {
     const TileSmem& sm = *L.ts;
-    const size_t base = 3 * (size_t)seg.out_base;
-    const uint32_t vs = seg.vscratch, vm = seg.vmin;
-    for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {
-        const uint32_t r = q / 3u, c = q - 3u * r;
-        const uint32_t j = L.perm[r];
-        uint32_t pos = r;
-        if (!single) {
-            const uint32_t w = walk_pos(L.bin[j], sort_mode);
-            pos = sm.bins_walk[w] + (r - sm.loc_walk[w]);
+    float4* __restrict__ oxyuv = P.out_xyuv + 3 * (size_t)td.out_base;
+    float4* __restrict__ orgba = P.out_rgba + 3 * (size_t)td.out_base;
+    float* __restrict__ odepth = P.out_depth + 3 * (size_t)td.out_base;
+    const uint32_t vs = td.vscratch, vm = td.vmin, t0 = td.t0;
+    const uint32_t total = 3 * n, B = blockDim.x;
+    for (uint32_t q0 = threadIdx.x; q0 < total; q0 += kILP * B) {
+        uint32_t o[kILP], oc[kILP];
+        bool ok[kILP];
+#pragma unroll
+        for (int u = 0; u < kILP; u++) {
+            const uint32_t q = q0 + u * B;
+            ok[u] = q < total;
+            o[u] = vs;
+            oc[u] = 0;
+            if (ok[u]) {
+                const uint32_t r = q / 3u, c = q - 3u * r;
+                const uint32_t j = L.perm[r];
+                uint32_t pos = r;
+                if (!single) {
+                    const uint32_t w = walk_pos(L.bin[j], sort_mode);
+                    pos = sm.bins_walk[w] + (r - sm.loc_walk[w]);
+                }
+                o[u] = vs + (use_vloc ? (uint32_t)L.vloc[3 * j + c] : midx[3 * (t0 + L.lidx[j]) + c] - vm);
+                oc[u] = 3 * pos + c;
+            }
         }
-        const uint32_t t = t0 + L.lidx[j];
-        const uint32_t o = vs + (midx[3 * t + c] - vm);
-        const float4 x = __ldcg(&P.vxyuv[o]);
-        const float4 k = __ldcg(&P.vrgba[o]);
-        const float d = __ldcg(&P.vcull[o].w);
-        const size_t oc = base + 3 * (size_t)pos + c;
-        P.out_xyuv[oc] = x;
-        P.out_rgba[oc] = k;
-        P.out_depth[oc] = d;
+        float4 x[kILP], k[kILP];
+        float d[kILP];
+#pragma unroll
+        for (int u = 0; u < kILP; u++) {
+            if (ok[u]) {
+                x[u] = rec_load(&P.vxyuv[o[u]]);
+                k[u] = rec_load(&P.vrgba[o[u]]);
+                d[u] = rec_load(&P.vcull[o[u]].w);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kILP; u++) {
+            if (ok[u]) {
+#if T3D_STREAM_STORES
+                __stcs(&oxyuv[oc[u]], x[u]);
+                __stcs(&orgba[oc[u]], k[u]);
+                __stcs(&odepth[oc[u]], d[u]);
+#else
+                oxyuv[oc[u]] = x[u];
+                orgba[oc[u]] = k[u];
+                odepth[oc[u]] = d[u];
+#endif
+            }
+        }
     }
 }
 
@@ -668,29 +730,51 @@ __device__ __forceinline__ bool tri_visible(float nearp, float farp, bool backfa
 __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* smem) {
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
-    for (;;) {
-        const uint32_t item = P.vitem_begin + next_item(P.ctl, 6, s_item);
-        if (item >= P.vitem_end) break;
+    uint32_t item = P.vitem_begin + next_item(P.ctl, 6, s_item);
+    while (item < P.vitem_end) {
+        // the next item's queue slot is fetched now and read at the end of this one
         const uint32_t s = P.vitem_seg[item];
         const DevSeg seg = P.segs[s];
-        if ((seg.flags & SEG_SKIP) || P.preps[seg.inst].culled) continue;
+        if (!((seg.flags & SEG_SKIP) || P.preps[seg.inst].culled)) {
         const DevJob& J = P.jobs[seg.job];
         stage_model(P, seg, J, ms);
         __syncthreads();
         const uint32_t v0 = P.vitem_chunk[item] * P.vchunk;
         const uint32_t v1 = min(seg.vcount, v0 + P.vchunk);
-        const float4* __restrict__ va = ms.ec.va;
-        const float4* __restrict__ vb = ms.ec.vb;
-        for (uint32_t lv = v0 + threadIdx.x; lv < v1; lv += blockDim.x) {
-            const uint32_t v = seg.vmin + lv;
-            const float4 a = va[v], b = vb[v];
+        const float4* __restrict__ va = ms.ec.va + seg.vmin;
+        const float4* __restrict__ vb = ms.ec.vb + seg.vmin;
+        const float4* __restrict__ vc = ms.ec.vc + seg.vmin;
+        const bool colors = ms.ec.flags & EC_COLORS;
+        // software pipeline: the next vertex's streams load while this one computes
+        uint32_t lv = v0 + threadIdx.x;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 a = zero, b = zero, k = zero;
+        if (lv < v1) {
+            a = va[lv];
+            b = vb[lv];
+            if (colors) k = vc[lv];
+        }
+        while (lv < v1) {
+            const uint32_t nlv = lv + blockDim.x;
+            float4 na = zero, nb = zero, nk = zero;
+            if (nlv < v1) {
+                na = va[nlv];
+                nb = vb[nlv];
+                if (colors) nk = vc[nlv];
+            }
             float4 cull, xyuv, rgba;
-            vertex_record(ms, v, a, b, cull, xyuv, rgba);
+            vertex_record(ms, a, b, k, cull, xyuv, rgba);
             const uint32_t o = seg.vscratch + lv;
             P.vcull[o] = cull;
             P.vxyuv[o] = xyuv;
             P.vrgba[o] = rgba;
+            a = na;
+            b = nb;
+            k = nk;
+            lv = nlv;
         }
+        }
+        item = P.vitem_begin + next_item(P.ctl, 6, s_item);
     }
 }
 
@@ -701,31 +785,30 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
     const SmemLayout L = smem_layout(smem, T);
     TileSmem& sm = *L.ts;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (;;) {
-        const uint32_t item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
-        if (item >= P.tile_end) break;
-        const uint32_t s = P.tile_seg[item];
-        const DevSeg seg = P.segs[s];
-        const uint32_t tile = item - seg.tile_first;
-        const bool multi = seg.flags & SEG_MULTI;
-        const uint32_t mt = seg.mt_first + tile;
-        const DevPrep& pr = P.preps[seg.inst];
-        if ((seg.flags & SEG_SKIP) || pr.culled) {
-            if (multi && threadIdx.x == 0) P.tile_count[mt] = 0u;
-            continue;
-        }
-        const DevJob& J = P.jobs[seg.job];
-        const JobCam& cam = J.cam;
-        const float nearp = cam.near_, farp = cam.far_;
-        const bool backface = seg.flags & SEG_BACKFACE;
+    uint32_t item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
+    while (item < P.tile_end) {
+        // the next item's queue slot is fetched now and read at the end of this one
+        const TileDesc td = P.tiles[item];
+        const uint32_t s = td.seg;
+        const bool multi = td.flags & SEG_MULTI;
+        const uint32_t mt = td.mt;
+        const DevPrep& pr = P.preps[td.inst];
+        // multi-tile segments: entries go straight to the tile's list in HBM, each warp into its own region
+        uint16_t* __restrict__ gi = P.vis_idx + (size_t)mt * T;
+        float* __restrict__ gd = P.vis_depth + (size_t)mt * T;
+        uint16_t* __restrict__ gv = P.vis_vloc + (size_t)mt * 3 * T;
+        if (!((td.flags & SEG_SKIP) || pr.culled)) {
+        const DevJob& J = P.jobs[td.job];
+        const float nearp = td.nearp, farp = td.farp;
+        const bool backface = td.flags & SEG_BACKFACE;
         const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
-        const DevMesh me = J.meshes[seg.mesh];
-        const uint32_t* __restrict__ midx = J.idx + 3 * (size_t)me.tbase;
-        const float* __restrict__ mctr = J.centers + 3 * (size_t)me.tbase;
-        const float4* __restrict__ vcull = P.vcull + seg.vscratch;
-        const uint32_t vm = seg.vmin;
-        const uint32_t t0 = seg.tri_start + tile * T;
-        const uint32_t t1 = min(seg.tri_start + seg.tri_count, t0 + T);
+        const uint32_t* __restrict__ midx = J.idx + 3 * (size_t)td.tbase;
+        const float* __restrict__ mctr = J.centers + 3 * (size_t)td.tbase;
+        const float4* __restrict__ vcull = P.vcull + td.vscratch;
+        const uint32_t vm = td.vmin;
+        const bool wide = td.flags & SEG_WIDE;
+        const uint32_t t0 = td.t0;
+        const uint32_t t1 = td.t1;
         float lmin = 3.402823466e38f, lmax = 0.0f;
         // each warp compacts its own contiguous quarter/eighth of the tile
         const uint32_t per = T / nw;
@@ -748,8 +831,8 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
                 cb = mk3(mctr[3 * tb2], mctr[3 * tb2 + 1], mctr[3 * tb2 + 2]);
             }
             float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f), pa1 = pa0, pa2 = pa0, pb0 = pa0, pb1 = pa0, pb2 = pa0;
-            if (ha) { pa0 = __ldcg(&vcull[ia0 - vm]); pa1 = __ldcg(&vcull[ia1 - vm]); pa2 = __ldcg(&vcull[ia2 - vm]); }
-            if (hb) { pb0 = __ldcg(&vcull[ib0 - vm]); pb1 = __ldcg(&vcull[ib1 - vm]); pb2 = __ldcg(&vcull[ib2 - vm]); }
+            if (ha) { pa0 = rec_load(&vcull[ia0 - vm]); pa1 = rec_load(&vcull[ia1 - vm]); pa2 = rec_load(&vcull[ia2 - vm]); }
+            if (hb) { pb0 = rec_load(&vcull[ib0 - vm]); pb1 = rec_load(&vcull[ib1 - vm]); pb2 = rec_load(&vcull[ib2 - vm]); }
             float da = 0.0f, db = 0.0f;
             const bool va_ = ha && tri_visible(nearp, farp, backface, ic, pa0, pa1, pa2, ca, da);
             const bool vb_ = hb && tri_visible(nearp, farp, backface, ic, pb0, pb1, pb2, cb, db);
@@ -757,16 +840,38 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
             const uint32_t balb = __ballot_sync(0xffffffffu, vb_);
             if (va_) {
                 const uint32_t p = wbase + cnt + __popc(bala & lt);
-                L.lidx[p] = (uint16_t)(ta - t0);
-                L.depth[p] = da;
+                if (!multi) {
+                    L.lidx[p] = (uint16_t)(ta - t0);
+                    L.depth[p] = da;
+                } else {
+                    gd[p] = da;
+                    if (wide) {
+                        gi[p] = (uint16_t)(ta - t0);
+                    } else {
+                        gv[3 * p] = (uint16_t)(ia0 - vm);
+                        gv[3 * p + 1] = (uint16_t)(ia1 - vm);
+                        gv[3 * p + 2] = (uint16_t)(ia2 - vm);
+                    }
+                }
                 lmin = fminf(lmin, da);
                 lmax = fmaxf(lmax, da);
             }
             cnt += __popc(bala);
             if (vb_) {
                 const uint32_t p = wbase + cnt + __popc(balb & lt);
-                L.lidx[p] = (uint16_t)(tb2 - t0);
-                L.depth[p] = db;
+                if (!multi) {
+                    L.lidx[p] = (uint16_t)(tb2 - t0);
+                    L.depth[p] = db;
+                } else {
+                    gd[p] = db;
+                    if (wide) {
+                        gi[p] = (uint16_t)(tb2 - t0);
+                    } else {
+                        gv[3 * p] = (uint16_t)(ib0 - vm);
+                        gv[3 * p + 1] = (uint16_t)(ib1 - vm);
+                        gv[3 * p + 2] = (uint16_t)(ib2 - vm);
+                    }
+                }
                 lmin = fminf(lmin, db);
                 lmax = fmaxf(lmax, db);
             }
@@ -783,31 +888,27 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
             sm.wlo[wid] = wbase;
             sm.whi[wid] = wbase + cnt;
             sm.warp_tot[wid] = cnt;
+            if (multi) P.tile_wcnt[(size_t)mt * kMaxWarps + wid] = cnt;
         }
         __syncthreads();
         uint32_t n = 0;
         for (uint32_t w = 0; w < nw; w++) n += sm.warp_tot[w];
         float mn = sm.wmin[0], mx = sm.wmax[0];
         for (uint32_t w = 1; w < nw; w++) { mn = fminf(mn, sm.wmin[w]); mx = fmaxf(mx, sm.wmax[w]); }
-        const uint32_t sort_mode = seg_sort_mode(seg.flags);
+        const uint32_t sort_mode = seg_sort_mode(td.flags);
         if (!multi) {
             if (n > 0) {
                 const float range = range_of(mn, mx);
                 for (uint32_t j = wbase + lane; j < wbase + cnt; j += 32)
                     L.bin[j] = (uint16_t)bin_of(L.depth[j], mn, range, sort_mode);
                 rank_tile(L, sort_mode);
-                tile_emit(P, seg, L, midx, t0, n, sort_mode, true);
+                tile_emit<kEmitILPSingle>(P, td, L, midx, n, sort_mode, true, false);
             }
             if (threadIdx.x == 0) {
                 P.seg_count[s] = n;
                 if (n) atomicAdd(&P.accum[0], (unsigned long long)n);
             }
         } else {
-            uint16_t* gi = P.vis_idx + (size_t)mt * T;
-            float* gd = P.vis_depth + (size_t)mt * T;
-            uint32_t off = 0;
-            for (uint32_t w = 0; w < wid; w++) off += sm.warp_tot[w];
-            for (uint32_t k = lane; k < cnt; k += 32) { gi[off + k] = L.lidx[wbase + k]; gd[off + k] = L.depth[wbase + k]; }
             if (threadIdx.x == 0) {
                 P.tile_count[mt] = n;
                 if (n > 0) {
@@ -818,7 +919,10 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
                 }
             }
         }
-        __syncthreads();
+        } else if (multi && threadIdx.x == 0) {
+            P.tile_count[mt] = 0u;
+        }
+        item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
     }
 }
 
@@ -827,16 +931,15 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
 __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
-    const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t per = T / nw;
     uint32_t* wh = L.whist + wid * kBins;
-    for (;;) {
-        uint32_t i = 0;
-        if (lane == 0) i = atomicAdd(&P.ctl->queue[2], 1u);
-        i = P.mt_tile_begin + __shfl_sync(0xffffffffu, i, 0);
-        if (i >= P.mt_tile_end) break;
-        const uint32_t g = P.mt_tiles[i];
-        const uint32_t s = P.tile_seg[g];
-        const uint32_t flags = P.segs[s].flags;
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(&P.ctl->queue[2], 1u);
+    i = P.mt_tile_begin + __shfl_sync(0xffffffffu, i, 0);
+    while (i < P.mt_tile_end) {
+        const TileDesc& td = P.mt_desc[i];
+        const uint32_t s = td.seg;
         const uint32_t n = __ldcg(&P.tile_count[i]);
         for (uint32_t b = lane; b < kBins; b += 32) wh[b] = 0u;
         __syncwarp();
@@ -844,15 +947,28 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
             const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
             const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
             const float range = range_of(mn, mx);
-            const uint32_t sort_mode = seg_sort_mode(flags);
-            const float* gd = P.vis_depth + (size_t)i * T;
-#pragma unroll 4
-            for (uint32_t j = lane; j < n; j += 32) atomicAdd(&wh[bin_of(__ldcg(&gd[j]), mn, range, sort_mode)], 1u);
+            const uint32_t sort_mode = seg_sort_mode(td.flags);
+            // the tile's list regions (one per warp of the triangle phase), 4 keys per load
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t c = __ldcg(&P.tile_wcnt[(size_t)i * kMaxWarps + w]);
+                const float4* rd = reinterpret_cast<const float4*>(P.vis_depth + (size_t)i * T + w * per);
+                for (uint32_t k = lane; 4 * k < c; k += 32) {
+                    const float4 v = __ldcg(&rd[k]);
+                    const uint32_t j = 4 * k;
+                    atomicAdd(&wh[bin_of(v.x, mn, range, sort_mode)], 1u);
+                    if (j + 1 < c) atomicAdd(&wh[bin_of(v.y, mn, range, sort_mode)], 1u);
+                    if (j + 2 < c) atomicAdd(&wh[bin_of(v.z, mn, range, sort_mode)], 1u);
+                    if (j + 3 < c) atomicAdd(&wh[bin_of(v.w, mn, range, sort_mode)], 1u);
+                }
+            }
         }
         __syncwarp();
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
         for (uint32_t b = lane; b < kBins; b += 32) out[b] = wh[b];
         __syncwarp();
+        uint32_t nx = 0;
+        if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
+        i = P.mt_tile_begin + __shfl_sync(0xffffffffu, nx, 0);
     }
 }
 
@@ -906,37 +1022,54 @@ __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned cha
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
     TileSmem& sm = *L.ts;
-    for (;;) {
-        const uint32_t i = P.mt_tile_begin + next_item(P.ctl, 4, &sm.item);
-        if (i >= P.mt_tile_end) break;
-        const uint32_t g = P.mt_tiles[i];
-        const uint32_t s = P.tile_seg[g];
-        const DevSeg seg = P.segs[s];
+    const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t per = T / nw, r0 = wid * per;
+    uint32_t i = P.mt_tile_begin + next_item(P.ctl, 4, &sm.item);
+    while (i < P.mt_tile_end) {
+        const TileDesc td = P.mt_desc[i];
         const uint32_t n = __ldcg(&P.tile_count[i]);
-        if (n == 0) continue;
-        const DevJob& J = P.jobs[seg.job];
-        const uint32_t* __restrict__ midx = J.idx + 3 * (size_t)J.meshes[seg.mesh].tbase;
-        const uint32_t t0 = seg.tri_start + (g - seg.tile_first) * T;
+        if (n > 0) {
+        const uint32_t s = td.seg;
+        const uint32_t c = __ldcg(&P.tile_wcnt[(size_t)i * kMaxWarps + wid]);
         const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
         const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
         const float range = range_of(mn, mx);
-        const uint32_t sort_mode = seg_sort_mode(seg.flags);
-        const uint16_t* gi = P.vis_idx + (size_t)i * T;
-        const float* gd = P.vis_depth + (size_t)i * T;
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            L.lidx[j] = __ldcg(&gi[j]);
-            L.bin[j] = (uint16_t)bin_of(__ldcg(&gd[j]), mn, range, sort_mode);
+        const uint32_t sort_mode = seg_sort_mode(td.flags);
+        const bool wide = td.flags & SEG_WIDE;
+        // each warp loads the list region its namesake warp wrote in the triangle phase
+        // (same block size), with 16-byte loads all in flight together
+        {
+            const float4* rd = reinterpret_cast<const float4*>(P.vis_depth + (size_t)i * T + r0);
+            for (uint32_t k = lane; 4 * k < c; k += 32) {
+                const float4 v = __ldcg(&rd[k]);
+                const uint32_t j = r0 + 4 * k;
+                L.bin[j] = (uint16_t)bin_of(v.x, mn, range, sort_mode);
+                L.bin[j + 1] = (uint16_t)bin_of(v.y, mn, range, sort_mode);
+                L.bin[j + 2] = (uint16_t)bin_of(v.z, mn, range, sort_mode);
+                L.bin[j + 3] = (uint16_t)bin_of(v.w, mn, range, sort_mode);
+            }
+            if (!wide) {  // 3 offsets per entry, 8 per load
+                const uint4* rv = reinterpret_cast<const uint4*>(P.vis_vloc + (size_t)i * 3 * T + 3 * r0);
+                uint4* sv = reinterpret_cast<uint4*>(L.vloc + 3 * r0);
+                for (uint32_t k = lane; 8 * k < 3 * c; k += 32) sv[k] = __ldcg(&rv[k]);
+            } else {  // 8 triangle numbers per load
+                const uint4* ri = reinterpret_cast<const uint4*>(P.vis_idx + (size_t)i * T + r0);
+                uint4* si = reinterpret_cast<uint4*>(L.lidx + r0);
+                for (uint32_t k = lane; 8 * k < c; k += 32) si[k] = __ldcg(&ri[k]);
+            }
+        }
+        if (lane == 0) {
+            sm.wlo[wid] = r0;
+            sm.whi[wid] = r0 + c;
         }
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x)
             sm.bins_walk[walk_pos(b, sort_mode)] = __ldcg(&P.tile_hist[(size_t)i * kBins + b]);
-        if (threadIdx.x < (blockDim.x >> 5)) {
-            const uint32_t chunk = (n + (blockDim.x >> 5) - 1) / (blockDim.x >> 5);
-            sm.wlo[threadIdx.x] = min(n, threadIdx.x * chunk);
-            sm.whi[threadIdx.x] = min(n, threadIdx.x * chunk + chunk);
-        }
         __syncthreads();
         rank_tile(L, sort_mode);
-        tile_emit(P, seg, L, midx, t0, n, sort_mode, false);
+        const uint32_t* __restrict__ midx = P.jobs[td.job].idx + 3 * (size_t)td.tbase;
+        tile_emit<kEmitILP>(P, td, L, midx, n, sort_mode, false, !wide);
+        }
+        i = P.mt_tile_begin + next_item(P.ctl, 4, &sm.item);  // its barriers also fence the shared arrays
     }
 }
 
@@ -958,7 +1091,10 @@ __device__ __forceinline__ void phase_start(unsigned long long& since) {
     if (threadIdx.x == 0) since = global_ns();
 }
 
-__global__ void __launch_bounds__(256, 4) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
+#ifndef T3D_MIN_BLOCKS
+#define T3D_MIN_BLOCKS 4  // resident blocks of 256 threads per SM the register budget is sized for
+#endif
+__global__ void __launch_bounds__(256, T3D_MIN_BLOCKS) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long since = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl->t_end[7] = global_ns();
@@ -993,7 +1129,8 @@ __global__ void __launch_bounds__(256, 4) t3d_frame_kernel(const __grid_constant
 // Launch entry used by the runtime (same translation-unit linkage).
 extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel; }
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads) {
-    const size_t tiles = sizeof(t3d::TileSmem) + 4ull * (block_threads / 32) * t3d::kBins + 10ull * tile_tris + 16;
+    const size_t tiles = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + 4ull * (block_threads / 32) * t3d::kBins +
+                         10ull * tile_tris + 16;
     const size_t verts = sizeof(t3d::ModelSmem) + 16;
     return tiles > verts ? tiles : verts;
 }

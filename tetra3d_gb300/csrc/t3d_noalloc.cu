@@ -60,8 +60,10 @@ constexpr size_t O_VXYUV = O_VCULL + al(16ull * kNaMaxV);
 constexpr size_t O_VRGBA = O_VXYUV + al(16ull * kNaMaxV);
 constexpr size_t O_VISI = O_VRGBA + al(16ull * kNaMaxV);
 constexpr size_t O_VISD = O_VISI + al(2ull * kNaMaxT);
-constexpr size_t O_TCNT = O_VISD + al(4ull * kNaMaxT);
-constexpr size_t O_THIST = O_TCNT + al(4ull * kNaMaxTiles);
+constexpr size_t O_VISV = O_VISD + al(4ull * kNaMaxT);
+constexpr size_t O_TCNT = O_VISV + al(6ull * kNaMaxT);
+constexpr size_t O_TWC = O_TCNT + al(4ull * kNaMaxTiles);
+constexpr size_t O_THIST = O_TWC + al(4ull * kMaxWarps * kNaMaxTiles);
 constexpr size_t O_MINMAX = O_THIST + al(4ull * kBins * kNaMaxTiles);
 constexpr size_t O_PREP = O_MINMAX + al(8);
 constexpr size_t O_ACCUM = O_PREP + al(sizeof(DevPrep));
@@ -76,9 +78,9 @@ constexpr size_t T_MESH = T_SEG + al(sizeof(DevSeg));
 constexpr size_t T_MODEL = T_MESH + al(sizeof(DevMesh));
 constexpr size_t T_LIGHTS = T_MODEL + al(sizeof(DevModel));
 constexpr size_t T_LIDX = T_LIGHTS + al(sizeof(DevLight) * kNaMaxL);
-constexpr size_t T_TSEG = T_LIDX + al(4ull * kNaMaxL);
-constexpr size_t T_MTT = T_TSEG + al(4ull * kNaMaxTiles);
-constexpr size_t T_MTS = T_MTT + al(4ull * kNaMaxTiles);
+constexpr size_t T_TILES = T_LIDX + al(4ull * kNaMaxL);
+constexpr size_t T_MTD = T_TILES + al(sizeof(TileDesc) * kNaMaxTiles);
+constexpr size_t T_MTS = T_MTD + al(sizeof(TileDesc) * kNaMaxTiles);
 constexpr size_t T_VSEG = T_MTS + al(4);
 constexpr size_t T_VCH = T_VSEG + al(4ull * kNaMaxChunks);
 constexpr size_t T_END = T_VCH + al(4ull * kNaMaxChunks);
@@ -314,11 +316,20 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     for (int k = 0; k < 4; k++) sg.mp[k] = mat.present ? md.color[k] * mat.color[k] : md.color[k];
     sg.tex_w = mat.present ? mat.tex_w : 0.0f;
     sg.tex_h = mat.present ? mat.tex_h : 0.0f;
-    uint32_t* tseg = reinterpret_cast<uint32_t*>(H + T_TSEG);
-    uint32_t* mtt = reinterpret_cast<uint32_t*>(H + T_MTT);
+    TileDesc* tds = reinterpret_cast<TileDesc*>(H + T_TILES);
+    TileDesc* mtd = reinterpret_cast<TileDesc*>(H + T_MTD);
     uint32_t* vseg = reinterpret_cast<uint32_t*>(H + T_VSEG);
     uint32_t* vch = reinterpret_cast<uint32_t*>(H + T_VCH);
-    for (uint32_t t = 0; t < ntiles; t++) { tseg[t] = 0; mtt[t] = t; }
+    for (uint32_t t = 0; t < ntiles; t++) {
+        TileDesc& td = tds[t];
+        td.seg = 0; td.inst = 0; td.job = 0; td.flags = flags;
+        td.t0 = a->tri_start + t * kNaTile;
+        td.t1 = std::min(a->tri_start + a->tri_count, td.t0 + kNaTile);
+        td.tbase = 0; td.vmin = 0; td.vscratch = 0; td.out_base = 0;
+        td.mt = ntiles > 1 ? t : 0u;
+        td.nearp = job.cam.near_; td.farp = job.cam.far_;
+        mtd[t] = td;
+    }
     for (uint32_t c = 0; c < nchunks; c++) { vseg[c] = 0; vch[c] = c; }
 
     // ---- uploads (no allocation: plain copies into the static array) ----
@@ -338,8 +349,8 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     P.preps = (DevPrep*)(S + O_PREP);
     P.inst_light_idx = (const uint32_t*)(S + O_TABLES + T_LIDX);
     P.segs = (const DevSeg*)(S + O_TABLES + T_SEG);
-    P.tile_seg = (const uint32_t*)(S + O_TABLES + T_TSEG);
-    P.mt_tiles = (const uint32_t*)(S + O_TABLES + T_MTT);
+    P.tiles = (const TileDesc*)(S + O_TABLES + T_TILES);
+    P.mt_desc = (const TileDesc*)(S + O_TABLES + T_MTD);
     P.mt_segs = (const uint32_t*)(S + O_TABLES + T_MTS);
     P.vitem_seg = (const uint32_t*)(S + O_TABLES + T_VSEG);
     P.vitem_chunk = (const uint32_t*)(S + O_TABLES + T_VCH);
@@ -348,7 +359,9 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     P.vrgba = (float4*)(S + O_VRGBA);
     P.vis_idx = (uint16_t*)(S + O_VISI);
     P.vis_depth = (float*)(S + O_VISD);
+    P.vis_vloc = (uint16_t*)(S + O_VISV);
     P.tile_count = (uint32_t*)(S + O_TCNT);
+    P.tile_wcnt = (uint32_t*)(S + O_TWC);
     P.tile_hist = (uint32_t*)(S + O_THIST);
     P.seg_minmax = (uint32_t*)(S + O_MINMAX);
     P.seg_count = a->out_count;

@@ -497,6 +497,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (mat.present && mat.backface_culling) flags |= SEG_BACKFACE;
             if (me.colors) flags |= SEG_COLORS;
             if (mat.present) flags |= SEG_MAT;
+            if (part.vcount > kLocalVerts) flags |= SEG_WIDE;
             uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
             flags |= sort_mode << 8;
             flags |= (uint32_t)(mat.present ? mat.lighting_mode : 0) << 10;
@@ -517,18 +518,29 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             F.nslots += sg.tri_count;
             uint32_t ntiles = (sg.tri_count + T - 1) / T;
             if (ntiles == 0) ntiles = 1;
-            sg.tile_first = (uint32_t)F.tile_seg.size();
+            sg.tile_first = (uint32_t)F.tiles.size();
             sg.ntiles = ntiles;
             const uint32_t s = (uint32_t)F.segs.size();
             if (ntiles > 1) {
                 flags |= SEG_MULTI;
-                sg.mt_first = (uint32_t)F.mt_tiles.size();
-                for (uint32_t t = 0; t < ntiles; t++) F.mt_tiles.push_back(sg.tile_first + t);
+                sg.mt_first = (uint32_t)F.mt_desc.size();
                 F.mt_segs.push_back(s);
             }
-            for (uint32_t t = 0; t < ntiles; t++) F.tile_seg.push_back(s);
-
             sg.flags = flags;
+            for (uint32_t t = 0; t < ntiles; t++) {
+                TileDesc td;
+                memset(&td, 0, sizeof td);
+                td.seg = s; td.inst = sg.inst; td.job = j; td.flags = flags;
+                td.t0 = sg.tri_start + t * T;
+                td.t1 = std::min(sg.tri_start + sg.tri_count, td.t0 + T);
+                td.tbase = me.tbase;
+                td.vmin = sg.vmin; td.vscratch = sg.vscratch; td.out_base = sg.out_base;
+                td.mt = ntiles > 1 ? sg.mt_first + t : 0u;
+                td.nearp = dj.cam.near_; td.farp = dj.cam.far_;
+                F.tiles.push_back(td);
+                if (ntiles > 1) F.mt_desc.push_back(td);
+            }
+
             F.segs.push_back(sg);
             t3d_segment_info si;
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
@@ -565,8 +577,8 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     size_t o_insts = add(F.insts.data(), bytes_of(F.insts));
     size_t o_ili = add(F.inst_light_idx.data(), bytes_of(F.inst_light_idx));
     size_t o_segs = add(F.segs.data(), bytes_of(F.segs));
-    size_t o_ts = add(F.tile_seg.data(), bytes_of(F.tile_seg));
-    size_t o_mtt = add(F.mt_tiles.data(), bytes_of(F.mt_tiles));
+    size_t o_ts = add(F.tiles.data(), bytes_of(F.tiles));
+    size_t o_mtt = add(F.mt_desc.data(), bytes_of(F.mt_desc));
     size_t o_mts = add(F.mt_segs.data(), bytes_of(F.mt_segs));
     size_t o_vs = add(F.vitem_seg.data(), bytes_of(F.vitem_seg));
     size_t o_vc = add(F.vitem_chunk.data(), bytes_of(F.vitem_chunk));
@@ -594,8 +606,8 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.insts = (const DevInst*)(db + o_insts);
     P.inst_light_idx = (const uint32_t*)(db + o_ili);
     P.segs = (const DevSeg*)(db + o_segs);
-    P.tile_seg = (const uint32_t*)(db + o_ts);
-    P.mt_tiles = (const uint32_t*)(db + o_mtt);
+    P.tiles = (const TileDesc*)(db + o_ts);
+    P.mt_desc = (const TileDesc*)(db + o_mtt);
     P.mt_segs = (const uint32_t*)(db + o_mts);
     P.vitem_seg = (const uint32_t*)(db + o_vs);
     P.vitem_chunk = (const uint32_t*)(db + o_vc);
@@ -603,14 +615,16 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     ctx->insts_noanim = (const DevInst*)(db + o_noanim);
     // scratch
     const size_t ninst = std::max<size_t>(1, F.insts.size()), nseg = std::max<size_t>(1, F.segs.size());
-    const size_t nmt = std::max<size_t>(1, F.mt_tiles.size());
+    const size_t nmt = std::max<size_t>(1, F.mt_desc.size());
     const size_t nsc = std::max<uint64_t>(1, F.nscratch);
     const size_t nslots = std::max<uint64_t>(1, F.nslots);
     if ((rc = ctx->preps.ensure(ctx, sizeof(DevPrep) * ninst)) ||
 (rc = ctx->vcull.ensure(ctx, 16 * nsc)) ||
         (rc = ctx->vxyuv.ensure(ctx, 16 * nsc)) || (rc = ctx->vrgba.ensure(ctx, 16 * nsc)) ||
         (rc = ctx->vis_idx.ensure(ctx, 2ull * nmt * ctx->tile_tris)) ||
-        (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) || (rc = ctx->tile_count.ensure(ctx, 4 * nmt)) ||
+        (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) ||
+        (rc = ctx->vis_vloc.ensure(ctx, 6ull * nmt * ctx->tile_tris)) || (rc = ctx->tile_count.ensure(ctx, 4 * nmt)) ||
+        (rc = ctx->tile_wcnt.ensure(ctx, 4ull * kMaxWarps * nmt)) ||
         (rc = ctx->tile_hist.ensure(ctx, 4ull * kBins * nmt)) || (rc = ctx->seg_minmax.ensure(ctx, 8 * nseg)) ||
         (rc = ctx->seg_count.ensure(ctx, 4 * nseg)) || (rc = ctx->out_xyuv.ensure(ctx, 48 * nslots)) ||
         (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
@@ -622,6 +636,8 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.vrgba = (float4*)ctx->vrgba.ptr;
     P.vis_idx = (uint16_t*)ctx->vis_idx.ptr;
     P.vis_depth = (float*)ctx->vis_depth.ptr;
+    P.vis_vloc = (uint16_t*)ctx->vis_vloc.ptr;
+    P.tile_wcnt = (uint32_t*)ctx->tile_wcnt.ptr;
     P.tile_count = (uint32_t*)ctx->tile_count.ptr;
     P.tile_hist = (uint32_t*)ctx->tile_hist.ptr;
     P.seg_minmax = (uint32_t*)ctx->seg_minmax.ptr;
@@ -678,13 +694,13 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         FrameParams P = P0;
         P.inst_begin = 0; P.inst_end = (uint32_t)F.insts.size();
         P.seg_begin = 0; P.seg_end = (uint32_t)F.segs.size();
-        P.tile_begin = 0; P.tile_end = (uint32_t)F.tile_seg.size();
-        P.mt_tile_begin = 0; P.mt_tile_end = (uint32_t)F.mt_tiles.size();
+        P.tile_begin = 0; P.tile_end = (uint32_t)F.tiles.size();
+        P.mt_tile_begin = 0; P.mt_tile_end = (uint32_t)F.mt_desc.size();
         P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
 
         P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
         P.has_multi = F.mt_segs.empty() ? 0u : 1u;
-        uint32_t items = (uint32_t)std::max({F.tile_seg.size(), F.mt_tiles.size(), F.vitem_seg.size(),
+        uint32_t items = (uint32_t)std::max({F.tiles.size(), F.mt_desc.size(), F.vitem_seg.size(),
                                              (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
         return launch_one(ctx, P, ctl, items, st);
     }

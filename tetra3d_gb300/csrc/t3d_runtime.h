@@ -67,13 +67,14 @@ struct FrameTables {
     std::vector<DevSeg> segs;
     std::vector<t3d_segment_info> seg_info;
     std::vector<uint32_t> seg_mt_seg;
-    std::vector<uint32_t> tile_seg, mt_tiles, mt_segs;
+    std::vector<TileDesc> tiles, mt_desc;
+    std::vector<uint32_t> mt_segs;
     std::vector<uint32_t> vitem_seg, vitem_chunk, seg_vitem_first;
     uint64_t nscratch = 0, nslots = 0;
     void clear() {
         jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
         insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
-        seg_mt_seg.clear(); tile_seg.clear(); mt_tiles.clear(); mt_segs.clear();
+        seg_mt_seg.clear(); tiles.clear(); mt_desc.clear(); mt_segs.clear();
         vitem_seg.clear(); vitem_chunk.clear(); seg_vitem_first.clear();
         nscratch = 0; nslots = 0;
     }
@@ -87,7 +88,7 @@ struct t3d_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t last_stream = nullptr;
     int num_sms = 0;
-    uint32_t tile_tris = 2048, vchunk = 1024, block_threads = 256;
+    uint32_t tile_tris = 2048, vchunk = 4096, block_threads = 256;
     uint32_t max_grid = 0;   // co-resident blocks for the current tuning
     size_t smem_bytes = 0;
     uint32_t next_scene = 1;
@@ -98,7 +99,7 @@ struct t3d_ctx {
     t3d::FrameParams params;
     const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
     t3d::HostBuf table_host, readback;
-    t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, tile_count, tile_hist,
+    t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
     uint64_t last_h2d = 0;
