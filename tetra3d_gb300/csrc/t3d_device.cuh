@@ -145,10 +145,12 @@ struct TileDesc {
     uint32_t tbase;                     // the mesh's first triangle in the scene pool
     uint32_t vmin, vscratch, out_base;  // segment: first vertex, first record, first output slot
     uint32_t mt;                        // multi-tile tile number (SEG_MULTI), else 0
-    uint32_t pad0;
+    uint32_t vlo;                       // records [vlo, vhi) cover every vertex of the tile's triangles
     float nearp, farp;                  // job camera near / far planes
-    uint32_t pad1[2];
+    uint32_t vhi;
+    uint32_t pad1;
 };
+constexpr uint32_t kChunkTris = 256;    // triangles per entry of a mesh's vertex-range table
 
 // Launch control block (zeroed before every launch).
 struct Ctl {

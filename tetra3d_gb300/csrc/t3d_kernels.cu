@@ -71,6 +71,18 @@ __device__ __forceinline__ V rec_load(const V* p) {
 #endif
 }
 
+// Asynchronous L2 prefetch of a byte range (cp.async.bulk.prefetch.L2): the
+// start is rounded down and the end up to 16 bytes (the pools carry slack for
+// that), and ranges above kPrefetchMax are left to demand loads.
+constexpr uint32_t kPrefetchMax = 256u << 10;
+
+__device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes) {
+    const uintptr_t a = (uintptr_t)p & ~(uintptr_t)15;
+    const uintptr_t e = ((uintptr_t)p + bytes + 15) & ~(uintptr_t)15;
+    if (e > a && e - a <= kPrefetchMax)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)) : "memory");
+}
+
 __device__ __forceinline__ uint32_t next_item(Ctl* ctl, int q, uint32_t* s_item) {
     __syncthreads();
     if (threadIdx.x == 0) *s_item = atomicAdd(&ctl->queue[q], 1u);
@@ -778,6 +790,20 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
     }
 }
 
+// The triangle phase works one grid-width ahead in L2: when a block starts
+// item i, one lane asks L2 for what item i + gridDim.x will read (the item some
+// block is likely to take next), so its loads hit L2 instead of HBM. (The same
+// for the rank phase measured slower: the issuing warp's descriptor loads delay
+// its block more than the prefetch saves.)
+__device__ __noinline__ void prefetch_triangle_tile(const FrameParams& P, uint32_t item) {
+    const TileDesc td = P.tiles[item];
+    if ((td.flags & SEG_SKIP) || P.preps[td.inst].culled) return;
+    const DevJob& J = P.jobs[td.job];
+    const size_t t0 = (size_t)td.tbase + td.t0, nt = td.t1 - td.t0;
+    l2_prefetch(J.idx + 3 * t0, 12 * nt);
+    l2_prefetch(J.centers + 3 * t0, 12 * nt);
+    if (td.vhi > td.vlo) l2_prefetch(P.vcull + td.vlo, 16ull * (td.vhi - td.vlo));
+}
 // P1: visibility and depth keys per tile; single-tile segments are sorted and
 // emitted right here, multi-tile segments leave their visible list in HBM.
 __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
@@ -787,6 +813,7 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint32_t item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
     while (item < P.tile_end) {
+        if (threadIdx.x == blockDim.x - 32 && item + gridDim.x < P.tile_end) prefetch_triangle_tile(P, item + gridDim.x);
         // the next item's queue slot is fetched now and read at the end of this one
         const TileDesc td = P.tiles[item];
         const uint32_t s = td.seg;

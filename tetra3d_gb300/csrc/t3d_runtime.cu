@@ -306,7 +306,8 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     // device pools
     int rc;
     if ((rc = sc->va.ensure(ctx, nv * 16)) || (rc = sc->vb.ensure(ctx, nv * 16)) || (rc = sc->vc.ensure(ctx, nv * 16)) ||
-        (rc = sc->idx.ensure(ctx, nt * 12)) || (rc = sc->centers.ensure(ctx, nt * 12)) ||
+        // 256 bytes of slack: L2 prefetches round their ranges out to 16 bytes
+        (rc = sc->idx.ensure(ctx, nt * 12 + 256)) || (rc = sc->centers.ensure(ctx, nt * 12 + 256)) ||
         (rc = sc->dmeshes.ensure(ctx, sizeof(DevMesh) * std::max<size_t>(1, d->num_meshes))) ||
         (rc = sc->dmodels.ensure(ctx, sizeof(DevModel) * std::max<size_t>(1, d->num_models))) ||
         (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))))
@@ -345,6 +346,16 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         }
         CK(cudaMemcpy((char*)sc->centers.ptr + (size_t)sc->meshes[m].tbase * 12, ctr.data(), me.num_triangles * 12ull,
                       cudaMemcpyHostToDevice));
+        SceneMesh& smh = sc->meshes[m];
+        const uint32_t nch = (me.num_triangles + kChunkTris - 1) / kChunkTris;
+        smh.chunk_lo.assign(nch, 0xFFFFFFFFu);
+        smh.chunk_hi.assign(nch, 0u);
+        for (uint32_t t = 0; t < me.num_triangles; t++)
+            for (int k = 0; k < 3; k++) {
+                const uint32_t v = me.indices[3 * (size_t)t + k];
+                smh.chunk_lo[t / kChunkTris] = std::min(smh.chunk_lo[t / kChunkTris], v);
+                smh.chunk_hi[t / kChunkTris] = std::max(smh.chunk_hi[t / kChunkTris], v);
+            }
     }
     std::vector<DevMesh> dm(d->num_meshes);
     for (uint32_t m = 0; m < d->num_meshes; m++) {
@@ -537,6 +548,16 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 td.vmin = sg.vmin; td.vscratch = sg.vscratch; td.out_base = sg.out_base;
                 td.mt = ntiles > 1 ? sg.mt_first + t : 0u;
                 td.nearp = dj.cam.near_; td.farp = dj.cam.far_;
+                if (td.t1 > td.t0 && sg.vcount) {  // vertex range of the tile from the chunk table
+                    uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+                    for (uint32_t c = td.t0 / kChunkTris; c <= (td.t1 - 1) / kChunkTris; c++) {
+                        lo = std::min(lo, me.chunk_lo[c]);
+                        hi = std::max(hi, me.chunk_hi[c]);
+                    }
+                    lo = std::max(lo, sg.vmin);
+                    hi = std::min(hi, sg.vmin + sg.vcount - 1);
+                    if (hi >= lo) { td.vlo = sg.vscratch + (lo - sg.vmin); td.vhi = sg.vscratch + (hi - sg.vmin) + 1; }
+                }
                 F.tiles.push_back(td);
                 if (ntiles > 1) F.mt_desc.push_back(td);
             }

@@ -36,6 +36,8 @@ struct SceneMesh {
     bool colors = false;
     float dmin[3], dmax[3];
     std::vector<ScenePart> parts;
+    // per kChunkTris triangles: smallest and largest vertex index they use (prefetch ranges)
+    std::vector<uint32_t> chunk_lo, chunk_hi;
 };
 struct SceneModel {
     t3d_model_desc d;  // host mirror (rotation advanced with every animated frame)
