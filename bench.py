@@ -54,8 +54,8 @@ def profile_traffic(workload):
         for line in f:
             if line.startswith("traffic_bytes_per_launch:"):
                 v = line.split(":", 1)[1].strip().split()[0]
-                return float(v), p
-    return None, p
+                return float(v), os.path.relpath(p, ROOT)
+    return None, os.path.relpath(p, ROOT)
 
 
 class ClockSampler:
