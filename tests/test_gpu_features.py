@@ -236,3 +236,41 @@ def test_argument_errors(ctx):
         assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "after errors")
     finally:
         ctx.release(sid)
+
+
+def test_reused_launch_tables_follow_model_updates(ctx):
+    """Renders that change only transforms of an opaque scene reuse the launch tables; changes
+    that alter the tables (colour -> transparency, visibility) rebuild them. Every frame must
+    match the oracle."""
+    sd = scenes.small_variant("batched", 15)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "first")
+        n = sd.nmodels
+        for k in range(3):  # transforms only: tables reused
+            rot = scenes.mult(sd.mv["rotate_step"].reshape(n, 4, 4), sd.mv["rotation"].reshape(n, 4, 4))
+            sd.mv["rotation"] = rot.reshape(n, 16)
+            sd.mv["position"][:, 1] += np.float32(0.25)
+            sd.mv["transform"] = scenes.trs(sd.mv["position"], sd.mv["scale"], rot).reshape(n, 16)
+            sd.mv["world_rotation"] = rot.reshape(n, 16)
+            ctx.set_models(sid, sd)
+            ctx.render(sid, sd.camera)
+            st = ctx.sync()
+            assert st.h2d_bytes == 0, "launch tables were rebuilt for a transform-only update"
+            assert_frames_equal(ctx.download(st), pyoracle.render(sd, sd.camera), f"transforms {k}")
+        sd.mv["color"][::3, 3] = np.float32(0.5)   # some models become transparent
+        sd.mv["visible"][1] = 0
+        ctx.set_models(sid, sd)
+        ctx.render(sid, sd.camera)
+        st = ctx.sync()
+        assert st.h2d_bytes > 0
+        assert_frames_equal(ctx.download(st), pyoracle.render(sd, sd.camera), "structure change")
+        sd.mv["position"][:, 0] -= np.float32(0.5)  # transparents present: the draw order follows transforms
+        sd.mv["transform"] = scenes.trs(sd.mv["position"], sd.mv["scale"],
+                                        sd.mv["rotation"].reshape(n, 4, 4)).reshape(n, 16)
+        ctx.set_models(sid, sd)
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "transparent reorder")
+    finally:
+        ctx.release(sid)

@@ -61,7 +61,8 @@ int t3d_create(int device, t3d_ctx** out) {
     }
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming) != cudaSuccess) {
         delete ctx;
         return T3D_E_CUDA;
     }
@@ -95,6 +96,8 @@ int t3d_destroy(t3d_ctx* ctx) {
     ctx->table_host.release();
     ctx->readback.release();
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
+    if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
+    ctx->model_host.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return T3D_OK;
@@ -117,6 +120,7 @@ int t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint
     ctx->tile_tris = T;
     ctx->vchunk = V;
     ctx->block_threads = B;
+    ctx->tables_ok = false;
     int rc = configure(ctx);
     if (rc) {
         ctx->tile_tris = oT; ctx->vchunk = oV; ctx->block_threads = oB;
@@ -212,10 +216,37 @@ int t3d_render_jobs(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t num_jobs, i
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     if (ctx->last_stream && ctx->last_stream != st) CKR(cudaStreamSynchronize(ctx->last_stream));
     ctx->frame_valid = false;
-    int rc = build_frame(ctx, jobs, num_jobs, animate);
-    if (rc) return rc;
-    // The table arena is reused: the previous frame must have consumed it.
-    if ((rc = upload_frame(ctx, st))) return rc;
+    // The launch tables depend on the jobs, the tuning and the scenes' structure,
+    // and on model transforms only through the draw order of transparent pairs (or
+    // of all pairs when depth rendering is off). A render that changes none of
+    // these reuses the tables already in the device arena.
+    std::vector<unsigned char> sig;
+    std::vector<uint64_t> mvers;
+    auto put = [&sig](const void* p, size_t n) { sig.insert(sig.end(), (const unsigned char*)p, (const unsigned char*)p + n); };
+    const uint32_t knobs[6] = {(uint32_t)mode, (uint32_t)animate, ctx->tile_tris, ctx->vchunk, ctx->block_threads, ctx->max_grid};
+    put(knobs, sizeof knobs);
+    if (num_jobs) put(jobs, sizeof(t3d_job_desc) * num_jobs);
+    bool known = true;
+    for (uint32_t j = 0; j < num_jobs; j++) {
+        auto it = ctx->scene_map().find(jobs[j].scene);
+        if (it == ctx->scene_map().end()) { known = false; break; }
+        put(&it->second->struct_ver, sizeof(uint64_t));
+        mvers.push_back(it->second->model_ver);
+    }
+    const bool reuse = known && !animate && ctx->tables_ok && sig == ctx->table_sig &&
+                       (!ctx->order_dep || mvers == ctx->table_model_vers);
+    int rc;
+    if (!reuse) {
+        drop_graph(ctx);  // a captured graph reads the arena that is rewritten now
+        if ((rc = build_frame(ctx, jobs, num_jobs, animate))) return rc;
+        // The table arena is reused: the previous frame must have consumed it.
+        if ((rc = upload_frame(ctx, st))) return rc;
+        ctx->table_sig.swap(sig);
+        ctx->table_model_vers.swap(mvers);
+        ctx->tables_ok = true;
+    } else {
+        ctx->last_h2d = 0;
+    }
     if ((rc = launch_frame(ctx, mode, st))) return rc;
     ctx->last_stream = st;
     ctx->frame_pending = true;
@@ -362,9 +393,11 @@ int t3d_graph_capture(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam, 
     job.light_mask[0] = job.light_mask[1] = ~0ull;
     job.camera = *cam;
     if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    ctx->tables_ok = false;  // the arena now holds the captured frame's tables
     int rc = build_frame(ctx, &job, 1, animate);
     if (rc) return rc;
     if ((rc = upload_frame(ctx, ctx->stream))) return rc;
+    ctx->tables_ok = false;
     if ((rc = ctx->ctl.ensure(ctx, sizeof(Ctl)))) return rc;  // no allocation may happen while capturing
     CKR(cudaStreamSynchronize(ctx->stream));
     CKR(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));

@@ -375,9 +375,26 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     return T3D_OK;
 }
 
+uint64_t next_version() {
+    static std::atomic<uint64_t> v{1};
+    return v.fetch_add(1);
+}
+
+// Fields of a model that the launch tables are built from, other than its transform.
+static bool same_model_structure(const t3d_model_desc& a, const t3d_model_desc& b) {
+    return a.mesh == b.mesh && a.visible == b.visible && a.frustum_culling == b.frustum_culling &&
+           a.shadeless == b.shadeless && a.light_list == b.light_list && a.use_trs == b.use_trs &&
+           memcmp(a.color, b.color, sizeof a.color) == 0;
+}
+
 int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n) {
     if (n == 0) return T3D_OK;
-    std::vector<DevModel> dv(n);
+    if (ctx->model_host.ensure(sizeof(DevModel) * n)) {
+        set_err(ctx, "pinned model staging alloc failed");
+        return T3D_E_OOM;
+    }
+    DevModel* dv = (DevModel*)ctx->model_host.ptr;
+    bool structure = sc->struct_ver == 0;
     for (uint32_t i = 0; i < n; i++) {
         const t3d_model_desc& md = models[i];
         DevModel& m = dv[i];
@@ -392,9 +409,14 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
         m.mesh = md.mesh;
         m.flags = (md.visible ? MOD_VISIBLE : 0) | (md.frustum_culling ? MOD_FRUSTUM : 0) | (md.shadeless ? MOD_SHADELESS : 0) |
                   (md.use_trs ? MOD_TRS : 0);
+        if (!structure && !same_model_structure(sc->models[first + i].d, md)) structure = true;
         sc->models[first + i].d = md;
     }
-    CK(cudaMemcpy((char*)sc->dmodels.ptr + sizeof(DevModel) * first, dv.data(), sizeof(DevModel) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync((char*)sc->dmodels.ptr + sizeof(DevModel) * first, dv, sizeof(DevModel) * n,
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (structure) sc->struct_ver = next_version();
+    sc->model_ver = next_version();
     return T3D_OK;
 }
 
@@ -403,6 +425,8 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
 int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate) {
     FrameTables& F = ctx->tables;
     F.clear();
+    ctx->tables_ok = false;
+    ctx->order_dep = false;
     const uint32_t T = ctx->tile_tris;
     for (uint32_t j = 0; j < njobs; j++) {
         auto it = ctx->scene_map().find(jobs[j].scene);
@@ -479,6 +503,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 Pair rp{mi, p, depth, mat.present ? mat.render_order : 0};
                 if (is_transparent(m.d.color, mat)) transparents.push_back(rp);
                 else solids.push_back(rp);
+                if (is_transparent(m.d.color, mat) || !cd.render_depth) ctx->order_dep = true;
             }
         }
         auto by_order_then_far = [](const Pair& a, const Pair& b) {
@@ -608,6 +633,8 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     for (auto& in : noanim) in.animate = 0;
     size_t o_noanim = add(noanim.data(), bytes_of(noanim));
     int rc;
+    // the previous upload must have left the staging buffer before it is rewritten
+    if (ctx->ev_upload) CK(cudaEventSynchronize(ctx->ev_upload));
     if ((rc = ctx->table_host.ensure(off + 256))) { set_err(ctx, "pinned table alloc failed"); return rc; }
     if ((rc = ctx->table_dev.ensure(ctx, off + 256))) return rc;
     char* hb = (char*)ctx->table_host.ptr;
@@ -620,6 +647,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     if (off) {
         cudaError_t e = cudaMemcpyAsync(db, hb, off, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) { set_err(ctx, "table upload: %s", cudaGetErrorString(e)); return T3D_E_CUDA; }
+        if (ctx->ev_upload) CK(cudaEventRecord(ctx->ev_upload, st));
     }
     FrameParams& P = ctx->params;
     memset(&P, 0, sizeof P);

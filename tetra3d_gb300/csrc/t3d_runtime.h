@@ -48,6 +48,9 @@ struct Scene {
     std::vector<t3d_light_desc> lights;
     std::vector<std::vector<uint32_t>> lists;
     uint64_t nverts = 0, ntris = 0;
+    // versions (unique across scenes): struct_ver changes with anything the launch
+    // tables are built from except transforms; model_ver with any model write
+    uint64_t struct_ver = 0, model_ver = 0;
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     uint64_t device_bytes() const {
         return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap;
@@ -100,7 +103,13 @@ struct t3d_ctx {
     t3d::FrameTables tables;
     t3d::FrameParams params;
     const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
-    t3d::HostBuf table_host, readback;
+    t3d::HostBuf table_host, readback, model_host;
+    // launch tables of the last render (reused while nothing they depend on changed)
+    std::vector<unsigned char> table_sig;
+    std::vector<uint64_t> table_model_vers;
+    bool tables_ok = false;
+    bool order_dep = true;   // the draw order depends on model transforms (transparents, depth off)
+    cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
