@@ -359,6 +359,10 @@ def serving_sweep(ctx, rates, seconds, max_requests, seed=7, baseline_requests=1
             wall = time.perf_counter() - w0
             row = dict(rate_req_s=rate, **serving.latency_summary(comps), wall_s=round(wall, 3))
             out["rates"].append(row)
+        # saturation: the last rate's requests all arrive at once (the server's capacity)
+        w0 = time.perf_counter()
+        comps = srv.replay(jobs, np.zeros(len(jobs)))
+        out["burst"] = dict(**serving.latency_summary(comps), wall_s=round(time.perf_counter() - w0, 3))
         # one request per launch, synchronously, over the last rate's requests
         jobs = jobs[:baseline_requests]
         lat, vis = [], 0
@@ -400,7 +404,8 @@ def run_serving(args, rank, world, local_rank):
             "serving": sv, "clocks": clk.summary(),
             "e2e": {"value": top["tris_per_s"], "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                     "note": "requests enter through t3d_server_replay from host memory; completions are read back"},
-            "served_over_one_request_per_launch": top["tris_per_s"] / sv["one_request_per_launch"]["tris_per_s"]}
+            "served_over_one_request_per_launch": top["tris_per_s"] / sv["one_request_per_launch"]["tris_per_s"],
+            "burst_over_one_request_per_launch": sv["burst"]["tris_per_s"] / sv["one_request_per_launch"]["tris_per_s"]}
     print(json.dumps(line))
     ctx.close()
 

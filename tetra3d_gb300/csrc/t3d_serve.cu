@@ -1,15 +1,18 @@
 // t3d_serve.cu -- render-request serving with continuous batching.
 //
-// Requests (scene id + camera + light subset) queue in arrival order. A
-// scheduler thread owns `streams` launch slots; each slot is a private frame
-// context (its own stream, tables, scratch and output buffers) over the
-// parent context's resident scenes. Whenever a slot is free it admits queued
+// Requests (scene id + camera + light subset) queue in arrival order. The
+// server owns `streams` launch slots; each slot is a private frame context (its
+// own stream, tables, scratch and output buffers) over the parent context's
+// resident scenes, driven by its own host thread. A free slot admits queued
 // requests in FIFO order while the batch has room (max_batch) and the device
-// bytes of everything in flight stay within the HBM budget, then launches all
-// admitted jobs in one persistent-kernel launch. Slots run concurrently, so
-// requests arriving while others are on the GPU are admitted as soon as a slot
-// and memory free up. Each request's output is written only by its own job's
+// bytes of everything in flight stay within the HBM budget, builds the batch's
+// launch tables, launches all admitted jobs in one persistent-kernel launch,
+// waits for it and posts the completions. Slots run concurrently -- their table
+// builds overlap each other and the GPU work of the other slots -- so requests
+// arriving while others are on the GPU are admitted as soon as a slot and
+// memory free up. Each request's output is written only by its own job's
 // segments, so its result does not depend on what it was batched with.
+// Scenes must not be uploaded or released while a server runs.
 
 #include <cuda_runtime.h>
 
@@ -41,7 +44,7 @@ struct Pending {
 struct Slot {
     t3d_ctx* ctx = nullptr;
     cudaEvent_t ev = nullptr;
-    bool busy = false;
+    std::thread worker;
     std::vector<Pending> batch;
     uint64_t bytes = 0;
 };
@@ -63,7 +66,6 @@ struct t3d_server {
     uint64_t budget = 0;
     uint32_t max_batch = 1;
     std::vector<Slot> slots;
-    std::thread sched;
     std::mutex mu;
     std::condition_variable cv;
     std::deque<Pending> queue;
@@ -84,49 +86,52 @@ struct t3d_server {
         return 116ull * sc->ntris + 48ull * sc->nverts + 1024ull * (sc->models.size() + 4);
     }
 
-    void finish(Slot& s) {
+    // Completions of the slot's finished launch (called without the lock held).
+    void finish(Slot& s, int rc) {
         t3d_stats st;
-        int rc = t3d_frame_sync(s.ctx, &st);
-        double t = now();
-        const auto& info = s.ctx->tables.seg_info;
+        if (rc == T3D_OK) rc = t3d_frame_sync(s.ctx, &st);
+        const double t = now();
         std::vector<uint64_t> vis(s.batch.size(), 0), sum(s.batch.size(), 1469598103934665603ull);
-        std::vector<float> buf;
-        for (const auto& si : info) {
-            if (si.job >= s.batch.size()) continue;
-            vis[si.job] += si.count;
-            if (verify && rc == T3D_OK && si.count) {
-                buf.resize(12ull * si.count);
-                cudaMemcpy(buf.data(), (char*)s.ctx->out_xyuv.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
-                sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
-                cudaMemcpy(buf.data(), (char*)s.ctx->out_rgba.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
-                sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
-                cudaMemcpy(buf.data(), (char*)s.ctx->out_depth.ptr + 12ull * si.base, 12ull * si.count, cudaMemcpyDeviceToHost);
-                sum[si.job] = fnv(buf.data(), 12ull * si.count, sum[si.job]);
+        if (rc == T3D_OK) {
+            const auto& info = s.ctx->tables.seg_info;
+            std::vector<float> buf;
+            for (const auto& si : info) {
+                if (si.job >= s.batch.size()) continue;
+                vis[si.job] += si.count;
+                if (verify && si.count) {
+                    buf.resize(12ull * si.count);
+                    cudaMemcpy(buf.data(), (char*)s.ctx->out_xyuv.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
+                    sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
+                    cudaMemcpy(buf.data(), (char*)s.ctx->out_rgba.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
+                    sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
+                    cudaMemcpy(buf.data(), (char*)s.ctx->out_depth.ptr + 12ull * si.base, 12ull * si.count, cudaMemcpyDeviceToHost);
+                    sum[si.job] = fnv(buf.data(), 12ull * si.count, sum[si.job]);
+                }
             }
         }
         std::lock_guard<std::mutex> g(mu);
+        if (rc != T3D_OK && err.empty()) err = s.ctx->err;
         for (size_t k = 0; k < s.batch.size(); k++) {
             t3d_completion c;
             memset(&c, 0, sizeof c);
             c.id = s.batch[k].req.id;
             c.status = rc;
-            c.visible_tris = vis[k];
+            c.visible_tris = rc == T3D_OK ? vis[k] : 0;
             c.arrival_s = s.batch[k].arrival_abs;
             c.admit_s = s.batch[k].admit_abs;
             c.done_s = t;
-            c.checksum = verify ? sum[k] : 0;
+            c.checksum = (verify && rc == T3D_OK) ? sum[k] : 0;
             done.push_back(c);
         }
         inflight -= s.bytes;
         s.bytes = 0;
         s.batch.clear();
-        s.busy = false;
     }
 
-    // Admits queued requests into a free slot (called with mu held).
-    bool admit(Slot& s, std::vector<Pending>& out) {
+    // Admits queued requests into the slot's batch (called with mu held).
+    bool admit(Slot& s) {
         double t = now();
-        while (!queue.empty() && out.size() < max_batch) {
+        while (!queue.empty() && s.batch.size() < max_batch) {
             Pending& p = queue.front();
             if (p.arrival_abs > t) break;  // replay: not arrived yet
             if (p.bytes > budget) {         // can never fit
@@ -143,67 +148,35 @@ struct t3d_server {
             if (inflight + s.bytes + p.bytes > budget) break;  // wait for memory
             p.admit_abs = t;
             s.bytes += p.bytes;
-            out.push_back(p);
+            s.batch.push_back(p);
             queue.pop_front();
         }
-        (void)s;
-        return !out.empty();
+        return !s.batch.empty();
     }
 
-    void loop() {
+    // One slot's worker: admit, build + launch, wait, complete.
+    void slot_loop(Slot& s) {
         cudaSetDevice(owner->device);
+        std::vector<t3d_job_desc> jobs;
         while (true) {
-            bool progress = false;
-            for (Slot& s : slots)
-                if (s.busy && cudaEventQuery(s.ev) == cudaSuccess) {
-                    finish(s);
-                    progress = true;
-                }
-            for (Slot& s : slots) {
-                if (s.busy) continue;
-                std::vector<Pending> batch;
-                {
-                    std::lock_guard<std::mutex> g(mu);
-                    if (!admit(s, batch)) continue;
-                    inflight += s.bytes;
-                }
-                std::vector<t3d_job_desc> jobs(batch.size());
-                for (size_t k = 0; k < batch.size(); k++) jobs[k] = batch[k].req.job;
-                int rc = t3d_render_jobs(s.ctx, jobs.data(), (uint32_t)jobs.size(), T3D_MODE_BATCHED, 0, nullptr);
-                s.batch = std::move(batch);
-                if (rc == T3D_OK) rc = cudaEventRecord(s.ev, s.ctx->stream) == cudaSuccess ? T3D_OK : T3D_E_CUDA;
-                if (rc != T3D_OK) {
-                    std::lock_guard<std::mutex> g(mu);
-                    err = s.ctx->err;
-                    double t = now();
-                    for (auto& p : s.batch) {
-                        t3d_completion c;
-                        memset(&c, 0, sizeof c);
-                        c.id = p.req.id;
-                        c.status = rc;
-                        c.arrival_s = p.arrival_abs;
-                        c.admit_s = p.admit_abs;
-                        c.done_s = t;
-                        done.push_back(c);
-                    }
-                    inflight -= s.bytes;
-                    s.bytes = 0;
-                    s.batch.clear();
-                    continue;
-                }
-                s.busy = true;
-                progress = true;
-            }
-            bool any_busy = false;
-            for (Slot& s : slots) any_busy |= s.busy;
-            if (stop.load() && !any_busy) {
-                std::lock_guard<std::mutex> g(mu);
-                if (queue.empty()) break;
-            }
-            if (!progress) {
+            {
                 std::unique_lock<std::mutex> g(mu);
-                cv.wait_for(g, std::chrono::microseconds(any_busy ? 20 : 200));
+                while (!admit(s)) {
+                    if (stop.load() && queue.empty()) return;
+                    // sleep until a submit, a completion, or the next replayed arrival
+                    double wait_s = 200e-6;
+                    if (!queue.empty()) wait_s = std::min(wait_s, std::max(10e-6, queue.front().arrival_abs - now()));
+                    cv.wait_for(g, std::chrono::duration<double>(wait_s));
+                }
+                inflight += s.bytes;
             }
+            jobs.resize(s.batch.size());
+            for (size_t k = 0; k < s.batch.size(); k++) jobs[k] = s.batch[k].req.job;
+            int rc = t3d_render_jobs(s.ctx, jobs.data(), (uint32_t)jobs.size(), T3D_MODE_BATCHED, 0, nullptr);
+            if (rc == T3D_OK) rc = cudaEventRecord(s.ev, s.ctx->stream) == cudaSuccess ? T3D_OK : T3D_E_CUDA;
+            if (rc == T3D_OK) rc = cudaEventSynchronize(s.ev) == cudaSuccess ? T3D_OK : T3D_E_CUDA;
+            finish(s, rc);
+            cv.notify_all();  // memory and the slot are free again
         }
     }
 };
@@ -219,11 +192,12 @@ int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batc
     s->budget = hbm_budget_bytes;
     s->max_batch = max_batch;
     s->t0 = Clock::now();
+    s->slots.resize(streams);
     for (uint32_t i = 0; i < streams; i++) {
-        Slot sl;
+        Slot& sl = s->slots[i];
         int rc = t3d_create(ctx->device, &sl.ctx);
         if (rc != T3D_OK) {
-            for (auto& x : s->slots) { cudaEventDestroy(x.ev); t3d_destroy(x.ctx); }
+            for (uint32_t k = 0; k < i; k++) { cudaEventDestroy(s->slots[k].ev); t3d_destroy(s->slots[k].ctx); }
             delete s;
             return rc;
         }
@@ -233,9 +207,8 @@ int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batc
         sl.ctx->block_threads = ctx->block_threads;
         configure(sl.ctx);
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
-        s->slots.push_back(sl);
     }
-    s->sched = std::thread([s] { s->loop(); });
+    for (auto& sl : s->slots) sl.worker = std::thread([s, &sl] { s->slot_loop(sl); });
     *out = s;
     return T3D_OK;
 }
@@ -244,7 +217,8 @@ int t3d_server_destroy(t3d_server* s) {
     if (!s) return T3D_E_INVAL;
     s->stop = true;
     s->cv.notify_all();
-    if (s->sched.joinable()) s->sched.join();
+    for (auto& x : s->slots)
+        if (x.worker.joinable()) x.worker.join();
     for (auto& x : s->slots) {
         cudaEventDestroy(x.ev);
         t3d_destroy(x.ctx);
