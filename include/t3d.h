@@ -352,6 +352,31 @@ int t3d_server_poll(t3d_server* srv, t3d_completion* out, uint32_t max, uint32_t
  * until all complete; completions in id order into out[n]. */
 int t3d_server_replay(t3d_server* srv, const t3d_request* reqs, uint32_t n, t3d_completion* out);
 
+/* ---- rasterising the emitted stream ----------------------------------------- */
+/* The colour and depth passes of flush (camera.go:1829-2048) over one job of the
+ * last rendered frame, on the device: per render pair in draw order, the depth pass
+ * (camera.go:350-383: encodeDepth into an RGBA8 intermediate, tested against the depth
+ * texture of the pairs before, composited into it unless the pair is transparent) and
+ * the colour pass (shaders/base3d.kage: vertex colour times the default white texture,
+ * alpha premultiplied, fog by the pair's depth with FogCurve and dithering, source-over
+ * blending); with RenderDepth off, the plain source-over triangle draw. The camera's
+ * fog settings are the World's (FogOn, FogMode, FogRange, FogColor). Images are RGBA8,
+ * premultiplied, row-major, camera width x height, cleared to 0 first, like ebiten
+ * images. Coverage: pixel centres, top-left fill rule; attributes interpolated linearly
+ * in screen space. Textures other than the default image, blend modes other than
+ * source-over and custom fragment shaders are not supported. No reference counterpart
+ * runs on the device: the reference hands these passes to ebiten. */
+typedef struct t3d_raster_opts {
+    int32_t fog_curve;     /* World.FogCurve: 0 linear, 1 out-circ, 2 in-circ */
+    float   dither_size;   /* World.DitheredFogSize: > 0 enables Bayer-dithered fog */
+    int32_t fogless;       /* Material.Fogless, for every pair */
+    int32_t reserved;
+} t3d_raster_opts;
+/* Rasterises job `job` (0-based, in the order given to t3d_render_jobs) of the last frame. */
+int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, void* stream);
+/* Copies the last rasterised images (4 * width * height bytes each; either may be NULL). */
+int t3d_frame_images(t3d_ctx* ctx, uint8_t* color_rgba8, uint8_t* depth_rgba8, int32_t* width, int32_t* height);
+
 /* ---- rendering without allocation ------------------------------------------ */
 /* For callers that cannot allocate device memory while they render -- an engine
  * or rasteriser that owns the device memory budget through its own allocator, a

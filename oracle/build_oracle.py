@@ -11,8 +11,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libt3d_oracle.so")
-SRC = os.path.join(HERE, "t3d_oracle.cpp")
-DEPS = [SRC, os.path.join(HERE, "t3d_oracle.h"), os.path.join(HERE, "..", "include", "t3d.h")]
+SRCS = [os.path.join(HERE, "t3d_oracle.cpp"), os.path.join(HERE, "t3d_oracle_raster.cpp")]
+DEPS = SRCS + [os.path.join(HERE, "t3d_oracle.h"), os.path.join(HERE, "..", "include", "t3d.h")]
 
 
 def build(force=False):
@@ -20,7 +20,7 @@ def build(force=False):
     if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in DEPS):
         return LIB
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
-           "-o", LIB, SRC]
+           "-o", LIB, *SRCS]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)

@@ -142,3 +142,52 @@ def vec_unit(v):
     out = np.zeros(3, np.float32)
     lib.t3d_oracle_vec_unit(a.ctypes.data_as(C.POINTER(C.c_float)), out.ctypes.data_as(C.POINTER(C.c_float)))
     return out
+
+
+def is_transparent(model_row, mat):
+    """Model.isTransparent for one mesh part (model.go:1086-1107, material.go:192-207)."""
+    F = np.float32
+    if mat["present"]:
+        mat_t = (mat["transparency_mode"] == abi.TRANSPARENCY_TRANSPARENT or not mat["blend_source_over"]
+                 or (mat["transparency_mode"] == abi.TRANSPARENCY_AUTO and F(mat["color"][3]) < F(0.999)))
+        model_t = mat["transparency_mode"] != abi.TRANSPARENCY_OPAQUE and F(model_row["color"][3]) < F(0.999)
+        return bool(mat_t or model_t)
+    return bool(F(model_row["color"][3]) < F(0.999))
+
+
+def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, transparent=None):
+    """Oracle of t3d_frame_raster for a one-job frame (an OracleFrame or a downloaded frame, both
+    compacted in draw order with .segments). Returns (colour, depth) RGBA8 (height, width, 4).
+    `transparent` (one flag per segment) replaces the flags derived from scene_data."""
+    lib = load()
+    fn = lib.t3d_oracle_raster
+    u32p, f32p = C.POINTER(C.c_uint32), C.POINTER(C.c_float)
+    fn.restype = C.c_int
+    fn.argtypes = [C.POINTER(abi.CameraDesc), C.c_int32, C.c_float, C.c_int32, C.c_uint32, f32p, f32p, f32p, u32p,
+                   C.POINTER(C.c_uint8), u32p, u32p]
+    n = int(frame.xyuv.shape[0])
+    pair = np.zeros(max(1, n), np.uint32)
+    given = transparent
+    transparent = np.zeros(max(1, len(frame.segments)), np.uint8)
+    b = 0
+    for k, s in enumerate(frame.segments):
+        pair[b:b + s["count"]] = k
+        b += s["count"]
+        if given is not None:
+            transparent[k] = bool(given[k])
+        else:
+            md = scene_data.mv[s["model"]]
+            mat = scene_data.meshes[int(md["mesh"])].parts[s["part"]]["mat"]
+            transparent[k] = is_transparent(md, mat)
+    xyuv = np.ascontiguousarray(frame.xyuv, np.float32).reshape(-1)
+    rgba = np.ascontiguousarray(frame.rgba, np.float32).reshape(-1)
+    depth = np.ascontiguousarray(frame.depth, np.float32).reshape(-1)
+    W, H = cam.width, cam.height
+    col = np.zeros(W * H, np.uint32)
+    dep = np.zeros(W * H, np.uint32)
+    rc = fn(C.byref(cam), fog_curve, dither_size, fogless, n, xyuv.ctypes.data_as(f32p), rgba.ctypes.data_as(f32p),
+            depth.ctypes.data_as(f32p), pair.ctypes.data_as(u32p), transparent.ctypes.data_as(C.POINTER(C.c_uint8)),
+            col.ctypes.data_as(u32p), dep.ctypes.data_as(u32p))
+    if rc != 0:
+        raise RuntimeError(f"oracle raster failed: {rc}")
+    return col.view(np.uint8).reshape(H, W, 4), dep.view(np.uint8).reshape(H, W, 4)

@@ -56,6 +56,14 @@ int t3d_oracle_render_f64(const t3d_scene_desc* scene, const t3d_camera_desc* ca
                           const uint64_t* light_mask, uint32_t animate_frames,
                           uint32_t threads, t3d_oracle_out* out);
 
+/* Rasterises n triangles of one job in draw order (3 corners each: xyuv, rgba, depth as
+ * t3d_frame_download writes them) into RGBA8 colour and depth images of the camera size
+ * (pixel = r | g << 8 | b << 16 | a << 24); tri_pair = render pair of each triangle,
+ * pair_transparent indexed by that id. See t3d_oracle_raster.cpp. */
+int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, float dither, int32_t fogless, uint32_t n,
+                      const float* xyuv, const float* rgba, const float* depth, const uint32_t* tri_pair,
+                      const uint8_t* pair_transparent, uint32_t* color_out, uint32_t* depth_out);
+
 /* Matrix4 helpers (float32) for pinning against matrix_test.go. */
 void t3d_oracle_mat_mult(const float* a, const float* b, float* out);
 void t3d_oracle_mat_inverted(const float* m, float* out);

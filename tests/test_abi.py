@@ -18,7 +18,7 @@ STRUCTS = {
     "t3d_model_desc": abi.ModelDesc, "t3d_light_desc": abi.LightDesc, "t3d_scene_desc": abi.SceneDesc,
     "t3d_camera_desc": abi.CameraDesc, "t3d_job_desc": abi.JobDesc, "t3d_frame_view": abi.FrameView,
     "t3d_segment_info": abi.SegmentInfo, "t3d_stats": abi.Stats, "t3d_request": abi.Request,
-    "t3d_completion": abi.Completion, "t3d_noalloc_args": abi.NoallocArgs,
+    "t3d_completion": abi.Completion, "t3d_noalloc_args": abi.NoallocArgs, "t3d_raster_opts": abi.RasterOpts,
 }
 
 

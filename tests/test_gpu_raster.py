@@ -1,0 +1,69 @@
+"""t3d_frame_raster (the colour and depth passes of flush on the device) against its oracle,
+bit for bit, on the emitted stream of real frames: opaque and transparent pairs, depth rendering
+on and off, fog in the colour pass with every curve and with dithering, several jobs."""
+import numpy as np
+import pytest
+
+from tetra3d_gb300 import abi, scenes
+from tetra3d_gb300.runtime import job
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _fog_depth_camera(variant):
+    """Depth rendering on with World fog: the colour pass applies the fog (base3d.kage)."""
+    c = scenes.feature_camera("persp")
+    c.fog_on, c.fog_mode = 1, {"add": abi.FOG_ADD, "sub": abi.FOG_SUB, "over": abi.FOG_OVERWRITE}[variant]
+    c.fog_range[:] = [0.2, 0.9]
+    c.fog_color[:] = [0.3, 0.5, 0.9, 1.0]
+    return c
+
+
+CASES = [
+    ("sphere", lambda: (scenes.uv_sphere_scene(1), None), {}),
+    ("cubes", lambda: (scenes.small_variant("cubes", 3), None), {}),
+    ("terrain", lambda: (scenes.small_variant("terrain", 3), None), {}),
+    ("features_persp", lambda: (scenes.feature_scene(5), scenes.feature_camera("persp")), {}),
+    ("features_tilted", lambda: (scenes.feature_scene(6), scenes.feature_camera("tilted")), {}),
+    ("features_no_depth_fog", lambda: (scenes.feature_scene(5), scenes.feature_camera("fog_add")), {}),
+    ("features_ortho", lambda: (scenes.feature_scene(7), scenes.feature_camera("ortho")), {}),
+    ("fog_add_linear", lambda: (scenes.feature_scene(5), _fog_depth_camera("add")), {}),
+    ("fog_sub_outcirc", lambda: (scenes.feature_scene(6), _fog_depth_camera("sub")), {"fog_curve": 1}),
+    ("fog_over_incirc_dither", lambda: (scenes.feature_scene(7), _fog_depth_camera("over")),
+     {"fog_curve": 2, "dither_size": 2.0}),
+    ("fogless", lambda: (scenes.feature_scene(5), _fog_depth_camera("add")), {"fogless": 1}),
+]
+
+
+@pytest.mark.parametrize("name,make,opts", CASES, ids=[c[0] for c in CASES])
+def test_raster_matches_oracle(ctx, name, make, opts):
+    sd, cam = make()
+    cam = cam if cam is not None else sd.camera
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        col, dep = ctx.raster(**opts)
+    finally:
+        ctx.release(sid)
+    f = pyoracle.render(sd, cam)
+    ocol, odep = pyoracle.raster(f, sd, cam, **opts)
+    assert (ocol[..., 3] > 0).sum() > 100, "the scene covers pixels"
+    bad = np.argwhere(np.any(col != ocol, axis=-1))
+    assert bad.size == 0, f"{name}: colour differs at {len(bad)} pixels, first {bad[:3].tolist()}: " \
+                          f"gpu {col[tuple(bad[0])]} oracle {ocol[tuple(bad[0])]}"
+    assert np.array_equal(dep, odep), f"{name}: depth image differs"
+
+
+def test_raster_second_job(ctx):
+    a, b = scenes.feature_scene(5), scenes.uv_sphere_scene(2)
+    sa, sb = ctx.upload(a), ctx.upload(b)
+    try:
+        cam_b = b.camera
+        ctx.render_jobs([job(sa, scenes.feature_camera("persp")), job(sb, cam_b)])
+        col, dep = ctx.raster(job=1)
+    finally:
+        ctx.release(sa)
+        ctx.release(sb)
+    ocol, odep = pyoracle.raster(pyoracle.render(b, cam_b), b, cam_b)
+    assert np.array_equal(col, ocol) and np.array_equal(dep, odep)

@@ -126,6 +126,10 @@ class NoallocArgs(C.Structure):
                 ("dim_min", C.c_float * 3), ("dim_max", C.c_float * 3), ("mat", Material), ("error", C.c_char * 128)]
 
 
+class RasterOpts(C.Structure):
+    _fields_ = [("fog_curve", C.c_int32), ("dither_size", C.c_float), ("fogless", C.c_int32), ("reserved", C.c_int32)]
+
+
 # name -> (restype, argtypes) for every entry point of include/t3d.h
 _VP = C.c_void_p
 SIGNATURES = {
@@ -154,6 +158,9 @@ SIGNATURES = {
     "t3d_server_poll": (C.c_int, [_VP, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),
     "t3d_server_replay": (C.c_int, [_VP, C.POINTER(Request), C.c_uint32, C.POINTER(Completion)]),
     "t3d_render_part_noalloc": (C.c_int, [C.c_int, C.POINTER(NoallocArgs), _VP]),
+    "t3d_frame_raster": (C.c_int, [_VP, C.c_uint32, C.POINTER(RasterOpts), _VP]),
+    "t3d_frame_images": (C.c_int, [_VP, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32)]),
 }
 
 _lib = None

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libt3d.so")
-SOURCES = ["t3d_kernels.cu", "t3d_runtime.cu", "t3d_capi.cu", "t3d_serve.cu", "t3d_noalloc.cu"]
+SOURCES = ["t3d_kernels.cu", "t3d_runtime.cu", "t3d_capi.cu", "t3d_serve.cu", "t3d_noalloc.cu", "t3d_raster.cu"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

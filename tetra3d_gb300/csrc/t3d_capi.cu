@@ -97,6 +97,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     ctx->readback.release();
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
+    t3d_raster_release(ctx);
     ctx->model_host.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

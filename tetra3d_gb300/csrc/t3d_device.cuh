@@ -31,6 +31,7 @@ enum : uint32_t {
     SEG_MAT = 1u << 4,          // MeshPart.Material != nil
     SEG_MULTI = 1u << 5,        // segment spans more than one tile
     SEG_WIDE = 1u << 6,         // vertex range above 65536: local vertex offsets do not fit 16 bits
+    SEG_TRANSPARENT = 1u << 7,  // drawn in the transparent pass (no depth composite when rasterised)
 };
 constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }

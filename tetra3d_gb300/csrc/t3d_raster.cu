@@ -1,0 +1,580 @@
+// t3d_raster.cu -- rasterising the emitted triangle stream on the device.
+//
+// Restates the two passes Tetra3D's flush runs per render pair through ebiten
+// (camera.go:1829-2048): the depth pass (camera.go:350-383: encodeDepth into an
+// RGBA8 intermediate, tested against the depth texture of the pairs drawn
+// before, composited into it unless the pair is transparent) and the colour
+// pass (shaders/base3d.kage:67-145: vertex colour times the default white
+// texture (tetra3d.go:12, :38), alpha premultiplied, fog by the intermediate
+// depth with FogCurve and Bayer dithering (camera.go:1257-1262), source-over
+// blending); with RenderDepth off, ebiten's plain triangle draw with
+// straight-alpha vertex colours. ebiten (v2.9.7) conventions restated: RGBA8
+// premultiplied images cleared to 0, fragments at pixel centres, the top-left
+// fill rule, attributes interpolated linearly in screen space, unorm8 writes
+// rounded to nearest after clamping to [0, 1].
+//
+// Device work: every visible triangle of the job lists the pixels it covers
+// (fragments, written in draw order), a stable radix sort groups fragments by
+// pixel, and one thread per pixel replays its fragments in draw order with the
+// per-pair depth and colour logic.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "t3d_runtime.h"
+
+using namespace t3d;
+
+#define CKR(call)                                                                                       \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            set_err(ctx, "%s failed: %s", #call, cudaGetErrorString(e_));                              \
+            return e_ == cudaErrorMemoryAllocation ? T3D_E_OOM : T3D_E_CUDA;                            \
+        }                                                                                               \
+    } while (0)
+
+namespace {
+
+constexpr int kSortBits = 8;
+constexpr int kSortDigits = 1 << kSortBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortPerThread = 16;
+constexpr int kSortChunk = kSortThreads * kSortPerThread;
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+
+__constant__ float kBayer[16] = {1.0f / 17.0f,  9.0f / 17.0f, 3.0f / 17.0f,  11.0f / 17.0f,
+                                 13.0f / 17.0f, 5.0f / 17.0f, 15.0f / 17.0f, 7.0f / 17.0f,
+                                 4.0f / 17.0f,  12.0f / 17.0f, 2.0f / 17.0f,  10.0f / 17.0f,
+                                 16.0f / 17.0f, 8.0f / 17.0f, 14.0f / 17.0f, 6.0f / 17.0f};
+
+struct RasterJob {
+    const float4* xyuv;
+    const float4* rgba;
+    const float* depth;
+    const uint32_t* tri_slot;   // compacted triangle -> output slot
+    const uint32_t* tri_seg;    // compacted triangle -> render pair
+    const DevSeg* segs;
+    int32_t W, H;
+    int32_t render_depth;
+    int32_t fog_mode;           // -1 off, 0 add, 1 sub, 2 overwrite
+    float fog_r, fog_g, fog_b, fog0, fog1;
+    int32_t fog_curve, fogless;
+    float dither;
+};
+
+// ---- fragments ---------------------------------------------------------------
+struct TriScreen {
+    float ax, ay, bx, by, cx, cy, area;
+    int x0, x1, y0, y1;
+    bool ok;
+};
+
+__device__ __forceinline__ TriScreen tri_screen(const RasterJob& J, uint32_t slot) {
+    TriScreen t;
+    const float4 a = J.xyuv[3 * (size_t)slot], b = J.xyuv[3 * (size_t)slot + 1], c = J.xyuv[3 * (size_t)slot + 2];
+    t.ax = a.x; t.ay = a.y; t.bx = b.x; t.by = b.y; t.cx = c.x; t.cy = c.y;
+    t.area = (t.bx - t.ax) * (t.cy - t.ay) - (t.by - t.ay) * (t.cx - t.ax);
+    t.ok = t.area != 0.0f && isfinite(t.area);
+    const float mnx = fminf(fminf(t.ax, t.bx), t.cx), mxx = fmaxf(fmaxf(t.ax, t.bx), t.cx);
+    const float mny = fminf(fminf(t.ay, t.by), t.cy), mxy = fmaxf(fmaxf(t.ay, t.by), t.cy);
+    // pixels whose centre (x + 0.5) lies in [mn, mx]
+    t.x0 = (int)fminf(fmaxf(0.0f, ceilf(mnx - 0.5f)), (float)J.W);
+    t.x1 = (int)fmaxf(fminf((float)J.W - 1.0f, floorf(mxx - 0.5f)), -1.0f);
+    t.y0 = (int)fminf(fmaxf(0.0f, ceilf(mny - 0.5f)), (float)J.H);
+    t.y1 = (int)fmaxf(fminf((float)J.H - 1.0f, floorf(mxy - 0.5f)), -1.0f);
+    if (!(mnx == mnx) || !(mny == mny) || !(mxx == mxx) || !(mxy == mxy)) t.ok = false;
+    return t;
+}
+
+// Edge weights of pixel centre (x, y): w_c for edge a->b, w_a for b->c, w_b for c->a.
+// Inside: every weight of the positively oriented triangle > 0, or == 0 on a top-left edge.
+__device__ __forceinline__ bool tl_edge(float dx, float dy) { return dy < 0.0f || (dy == 0.0f && dx > 0.0f); }
+__device__ __forceinline__ bool covers(const TriScreen& t, float x, float y, float& wa, float& wb, float& wc) {
+    wc = (t.bx - t.ax) * (y - t.ay) - (t.by - t.ay) * (x - t.ax);
+    wa = (t.cx - t.bx) * (y - t.by) - (t.cy - t.by) * (x - t.bx);
+    wb = (t.ax - t.cx) * (y - t.cy) - (t.ay - t.cy) * (x - t.cx);
+    const float s = t.area > 0.0f ? 1.0f : -1.0f;
+    const float ea = s * wa, eb = s * wb, ec = s * wc;
+    const bool ia = ea > 0.0f || (ea == 0.0f && tl_edge(s * (t.cx - t.bx), s * (t.cy - t.by)));
+    const bool ib = eb > 0.0f || (eb == 0.0f && tl_edge(s * (t.ax - t.cx), s * (t.ay - t.cy)));
+    const bool ic = ec > 0.0f || (ec == 0.0f && tl_edge(s * (t.bx - t.ax), s * (t.by - t.ay)));
+    return ia && ib && ic;
+}
+
+__global__ void k_seg_bases(const uint32_t* __restrict__ seg_count, uint32_t seg_lo, uint32_t nseg, uint32_t* cbase) {
+    // one block: exclusive prefix of the job's per-pair visible counts, cbase[nseg] = total
+    __shared__ uint32_t warp_sum[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < nseg; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nseg ? seg_count[seg_lo + i] : 0u;
+        uint32_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((threadIdx.x & 31) >= (uint32_t)o) incl += u;
+        }
+        if ((threadIdx.x & 31) == 31) warp_sum[threadIdx.x >> 5] = incl;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const uint32_t nw = blockDim.x >> 5;
+            uint32_t w = threadIdx.x < nw ? warp_sum[threadIdx.x] : 0u, wi = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, wi, o);
+                if (threadIdx.x >= (uint32_t)o) wi += u;
+            }
+            if (threadIdx.x < nw) warp_sum[threadIdx.x] = wi - w;
+        }
+        __syncthreads();
+        if (i < nseg) cbase[i] = carry + warp_sum[threadIdx.x >> 5] + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += warp_sum[threadIdx.x >> 5] + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cbase[nseg] = carry;
+}
+
+__global__ void k_tri_lists(const DevSeg* __restrict__ segs, const uint32_t* __restrict__ seg_count, uint32_t seg_lo,
+                            uint32_t nseg, const uint32_t* __restrict__ cbase, uint32_t* tri_slot, uint32_t* tri_seg) {
+    // one warp per render pair
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nseg) return;
+    const uint32_t s = seg_lo + w, n = seg_count[s], b = cbase[w], ob = segs[s].out_base;
+    for (uint32_t i = lane; i < n; i += 32) {
+        tri_slot[b + i] = ob + i;
+        tri_seg[b + i] = s;
+    }
+}
+
+__global__ void k_frag_count(RasterJob J, uint32_t n, uint32_t* fcount) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const TriScreen t = tri_screen(J, J.tri_slot[c]);
+    uint32_t k = 0;
+    if (t.ok)
+        for (int y = t.y0; y <= t.y1; y++)
+            for (int x = t.x0; x <= t.x1; x++) {
+                float wa, wb, wc;
+                if (covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc)) k++;
+            }
+    fcount[c] = k;
+}
+
+__global__ void k_frag_write(RasterJob J, uint32_t n, const uint32_t* __restrict__ foff, uint32_t* keys, uint32_t* vals) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const TriScreen t = tri_screen(J, J.tri_slot[c]);
+    uint32_t o = foff[c];
+    if (t.ok)
+        for (int y = t.y0; y <= t.y1; y++)
+            for (int x = t.x0; x <= t.x1; x++) {
+                float wa, wb, wc;
+                if (covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc)) {
+                    keys[o] = (uint32_t)y * (uint32_t)J.W + (uint32_t)x;
+                    vals[o] = c;
+                    o++;
+                }
+            }
+}
+
+// ---- device-wide exclusive scan of uint32 ------------------------------------
+__device__ uint32_t block_exclusive(uint32_t v, uint32_t* sh, uint32_t& total) {
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += u;
+    }
+    if (lane == 31) sh[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = lane < nw ? sh[lane] : 0u, wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (uint32_t)o) wi += u;
+        }
+        if (lane < nw) sh[lane] = wi - w;
+        if (lane == nw - 1) sh[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t r = sh[wid] + incl - v;
+    total = sh[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_scan_local(const uint32_t* __restrict__ in, uint32_t* out, uint32_t n, uint32_t* partial) {
+    __shared__ uint32_t sh[33];
+    const size_t base = (size_t)blockIdx.x * kScanChunk + (size_t)threadIdx.x * kScanPer;
+    uint32_t v[kScanPer], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        v[k] = base + k < n ? in[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive(s, sh, total);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = total;
+}
+
+__global__ void k_scan_add(uint32_t* out, uint32_t n, const uint32_t* __restrict__ partial_scanned) {
+    const size_t base = (size_t)blockIdx.x * kScanChunk + (size_t)threadIdx.x * kScanPer;
+    const uint32_t add = partial_scanned[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++)
+        if (base + k < n) out[base + k] += add;
+}
+
+// ---- stable LSD radix sort of (key, value) pairs by kSortBits-bit digits --------
+__global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t nblocks, uint32_t* counts) {
+    __shared__ uint32_t h[kSortDigits];
+    for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) h[d] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kSortChunk;
+    for (int k = 0; k < kSortPerThread; k++) {
+        const size_t i = base + (size_t)k * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kSortDigits - 1)], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) counts[(size_t)d * nblocks + blockIdx.x] = h[d];
+}
+
+__global__ void k_sort_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, int shift,
+                               uint32_t nblocks, const uint32_t* __restrict__ offsets, uint32_t* okeys, uint32_t* ovals) {
+    constexpr int kWarps = kSortThreads / 32;
+    __shared__ uint32_t running[kSortDigits];
+    __shared__ uint32_t wcount[kWarps][kSortDigits];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) running[d] = offsets[(size_t)d * nblocks + blockIdx.x];
+    const size_t base = (size_t)blockIdx.x * kSortChunk;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int k = 0; k < kSortPerThread; k++) {
+        for (int q = threadIdx.x; q < kWarps * kSortDigits; q += blockDim.x) (&wcount[0][0])[q] = 0u;
+        __syncthreads();
+        // entries in order: round k covers [base + 256k, base + 256k + 256), warp w its 32-entry slice
+        const size_t i = base + (size_t)k * kSortThreads + threadIdx.x;
+        const bool active = i < n;
+        const uint32_t mask = __ballot_sync(0xffffffffu, active);
+        uint32_t key = 0, val = 0, d = 0, peers = 0;
+        if (active) {
+            key = keys[i];
+            val = vals[i];
+            d = (key >> shift) & (kSortDigits - 1);
+            peers = __match_any_sync(mask, d);
+            if (lane == (uint32_t)(__ffs(peers) - 1)) wcount[wid][d] = __popc(peers);
+        }
+        __syncthreads();
+        // per digit: exclusive prefix over warps (thread d owns digit d)
+        for (int dd = threadIdx.x; dd < kSortDigits; dd += blockDim.x) {
+            uint32_t run = running[dd];
+            for (int w = 0; w < kWarps; w++) {
+                const uint32_t t = wcount[w][dd];
+                wcount[w][dd] = run;
+                run += t;
+            }
+            running[dd] = run;
+        }
+        __syncthreads();
+        if (active) {
+            const uint32_t pos = wcount[wid][d] + __popc(peers & lt);
+            okeys[pos] = key;
+            ovals[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- per-pixel replay --------------------------------------------------------
+__device__ __forceinline__ float clamp01(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
+__device__ __forceinline__ uint32_t q8(float v) { return (uint32_t)floorf(clamp01(v) * 255.0f + 0.5f); }
+__device__ __forceinline__ float u8f(uint32_t p, int k) { return (float)((p >> (8 * k)) & 255u) / 255.0f; }
+__device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {
+    return r | (g << 8) | (b << 16) | (a << 24);
+}
+__device__ __forceinline__ float fractf(float v) { return v - floorf(v); }
+// encodeDepth (camera.go:356-361) written to RGBA8
+__device__ __forceinline__ uint32_t encode_depth(float d) {
+    const float r = floorf(d * 255.0f) / 255.0f;
+    const float g = floorf(fractf(d * 255.0f) * 255.0f) / 255.0f;
+    const float b = fractf(d * 255.0f * 255.0f);
+    return pack(q8(r), q8(g), q8(b), 255u);
+}
+// decodeDepth (camera.go:363-365)
+__device__ __forceinline__ float decode_depth(uint32_t p) { return u8f(p, 0) + (u8f(p, 1) / 255.0f) + (u8f(p, 2) / 65025.0f); }
+__device__ __forceinline__ float smoothstep(float e0, float e1, float x) {
+    const float t = clamp01((x - e0) / (e1 - e0));
+    return t * t * (3.0f - 2.0f * t);
+}
+// source-over onto a premultiplied RGBA8 pixel
+__device__ __forceinline__ uint32_t blend_over(uint32_t dst, float r, float g, float b, float a) {
+    r = clamp01(r); g = clamp01(g); b = clamp01(b); a = clamp01(a);
+    const float k = 1.0f - a;
+    return pack(q8(r + u8f(dst, 0) * k), q8(g + u8f(dst, 1) * k), q8(b + u8f(dst, 2) * k), q8(a + u8f(dst, 3) * k));
+}
+
+struct Frag {
+    float d, r, g, b, a;
+};
+__device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t c, float x, float y) {
+    const uint32_t slot = J.tri_slot[c];
+    const TriScreen t = tri_screen(J, slot);
+    float wa, wb, wc;
+    covers(t, x, y, wa, wb, wc);
+    const float4 ka = J.rgba[3 * (size_t)slot], kb = J.rgba[3 * (size_t)slot + 1], kc = J.rgba[3 * (size_t)slot + 2];
+    const float da = J.depth[3 * (size_t)slot], db = J.depth[3 * (size_t)slot + 1], dc = J.depth[3 * (size_t)slot + 2];
+    Frag f;
+    f.d = ((wa * da + wb * db) + wc * dc) / t.area;
+    f.r = ((wa * ka.x + wb * kb.x) + wc * kc.x) / t.area;
+    f.g = ((wa * ka.y + wb * kb.y) + wc * kc.y) / t.area;
+    f.b = ((wa * ka.z + wb * kb.z) + wc * kc.z) / t.area;
+    f.a = ((wa * ka.w + wb * kb.w) + wc * kc.w) / t.area;
+    return f;
+}
+
+__global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ fvals,
+                         uint32_t* color, uint32_t* depth) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)(J.W * J.H)) return;
+    const float x = (float)(p % (uint32_t)J.W) + 0.5f, y = (float)(p / (uint32_t)J.W) + 0.5f;
+    uint32_t rc = 0u, rd = 0u;
+    const uint32_t f0 = pstart[p], f1 = pstart[p + 1];
+    uint32_t i = f0;
+    while (i < f1) {
+        const uint32_t s = J.tri_seg[fvals[i]];
+        uint32_t e = i + 1;
+        while (e < f1 && J.tri_seg[fvals[e]] == s) e++;  // this pair's fragments
+        if (J.render_depth) {
+            uint32_t inter = 0u;
+            for (uint32_t q = i; q < e; q++) {  // depth pass (camera.go:1882-1931)
+                const Frag f = fragment(J, fvals[q], x, y);
+                if ((rd >> 24) == 0u || decode_depth(rd) > f.d) inter = encode_depth(f.d);
+            }
+            if ((inter >> 24) != 0u) {
+                for (uint32_t q = i; q < e; q++) {  // colour pass (base3d.kage:67-145)
+                    const Frag f = fragment(J, fvals[q], x, y);
+                    float r = f.r, g = f.g, b = f.b;
+                    const float a = f.a;
+                    r *= a; g *= a; b *= a;
+                    if (!J.fogless && J.fog_mode >= 0 && J.fog_mode <= 2) {
+                        const float dd = decode_depth(inter);
+                        float v = dd;
+                        if (J.fog_curve == 1) v = sqrtf(1.0f - (dd - 1.0f) * (dd - 1.0f));
+                        else if (J.fog_curve == 2) v = 1.0f - sqrtf(1.0f - dd * dd);
+                        float m = smoothstep(J.fog0, J.fog1, v);
+                        if (J.dither > 0.0f) {
+                            const int yc = (int)(y / J.dither) % 4, xc = (int)(x / J.dither) % 4;
+                            m = (m - kBayer[yc * 4 + xc]) < 0.0f ? 0.0f : 1.0f;
+                        }
+                        if (J.fog_mode == 0) {
+                            r += J.fog_r * m * a; g += J.fog_g * m * a; b += J.fog_b * m * a;
+                        } else if (J.fog_mode == 1) {
+                            r -= J.fog_r * m * a; g -= J.fog_g * m * a; b -= J.fog_b * m * a;
+                        } else {
+                            r = (r * (1.0f - m) + J.fog_r * m) * a;
+                            g = (g * (1.0f - m) + J.fog_g * m) * a;
+                            b = (b * (1.0f - m) + J.fog_b * m) * a;
+                        }
+                    }
+                    rc = blend_over(rc, r, g, b, a);
+                }
+                if (!(J.segs[s].flags & SEG_TRANSPARENT)) rd = inter;  // depth composite
+            }
+        } else {
+            for (uint32_t q = i; q < e; q++) {  // plain draw, straight-alpha vertex colours
+                const Frag f = fragment(J, fvals[q], x, y);
+                rc = blend_over(rc, f.r * f.a, f.g * f.a, f.b * f.a, f.a);
+            }
+        }
+        i = e;
+    }
+    color[p] = rc;
+    depth[p] = rd;
+}
+
+__global__ void k_pixel_count(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* pcount) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&pcount[keys[i]], 1u);
+}
+
+struct RasterScratch {
+    DevBuf cbase, tri_slot, tri_seg, fcount, foff, keys, vals, keys2, vals2, counts, offsets, partial[3], pstart, pcount,
+        color, depth;
+};
+
+}  // namespace
+
+struct t3d_raster_state {
+    RasterScratch S;
+    int32_t W = 0, H = 0;
+    bool valid = false;
+};
+
+namespace {
+
+int scan_u32(t3d_ctx* ctx, RasterScratch& S, const uint32_t* in, uint32_t* out, uint32_t n, cudaStream_t st, int level = 0) {
+    if (n == 0) return T3D_OK;
+    const uint32_t nb = (n + kScanChunk - 1) / kScanChunk;
+    if (level > 2) {
+        set_err(ctx, "raster: scan too large");
+        return T3D_E_INVAL;
+    }
+    int rc;
+    if ((rc = S.partial[level].ensure(ctx, 4ull * (nb + 1)))) return rc;
+    uint32_t* part = (uint32_t*)S.partial[level].ptr;
+    k_scan_local<<<nb, kScanThreads, 0, st>>>(in, out, n, part);
+    if (nb > 1) {
+        if ((rc = scan_u32(ctx, S, part, part, nb, st, level + 1))) return rc;
+        k_scan_add<<<nb, kScanThreads, 0, st>>>(out, n, part);
+    }
+    CKR(cudaGetLastError());
+    return T3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, void* stream) {
+    if (!ctx) return T3D_E_INVAL;
+    FrameTables& F = ctx->tables;
+    if ((!ctx->frame_valid && !ctx->frame_pending) || job >= F.jobs.size()) {
+        set_err(ctx, "frame_raster: no rendered frame or job %u out of range", job);
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : (ctx->last_stream ? ctx->last_stream : ctx->stream);
+    if (ctx->last_stream && ctx->last_stream != st) CKR(cudaStreamSynchronize(ctx->last_stream));
+    if (!ctx->raster) ctx->raster = new t3d_raster_state();
+    t3d_raster_state& R = *ctx->raster;
+    RasterScratch& S = R.S;
+    const uint32_t seg_lo = job ? F.job_seg_end[job - 1] : 0u, seg_hi = F.job_seg_end[job];
+    const uint32_t nseg = seg_hi - seg_lo;
+    const JobCam& cam = F.jobs[job].cam;
+    RasterJob J;
+    memset(&J, 0, sizeof J);
+    J.W = (int32_t)cam.W;
+    J.H = (int32_t)cam.H;
+    if (J.W <= 0 || J.H <= 0 || (uint64_t)J.W * J.H >= (1ull << 31)) {
+        set_err(ctx, "frame_raster: bad image size %d x %d", J.W, J.H);
+        return T3D_E_INVAL;
+    }
+    J.render_depth = cam.render_depth;
+    J.fog_mode = cam.fog_on ? cam.fog_mode : -1;
+    J.fog_r = cam.fog_color[0]; J.fog_g = cam.fog_color[1]; J.fog_b = cam.fog_color[2];
+    J.fog0 = cam.fog_range[0]; J.fog1 = cam.fog_range[1];
+    J.fog_curve = opts ? opts->fog_curve : 0;
+    J.fogless = opts ? opts->fogless : 0;
+    J.dither = opts ? opts->dither_size : 0.0f;
+    J.xyuv = (const float4*)ctx->out_xyuv.ptr;
+    J.rgba = (const float4*)ctx->out_rgba.ptr;
+    J.depth = (const float*)ctx->out_depth.ptr;
+    J.segs = ctx->params.segs;
+    uint64_t cap = 0;
+    for (uint32_t s = seg_lo; s < seg_hi; s++) cap += F.segs[s].tri_count;
+    const uint64_t npx = (uint64_t)J.W * J.H;
+    int rc;
+    if ((rc = S.cbase.ensure(ctx, 4ull * (nseg + 1))) || (rc = S.tri_slot.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
+        (rc = S.tri_seg.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
+        (rc = S.fcount.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
+        (rc = S.foff.ensure(ctx, 4 * std::max<uint64_t>(1, cap) + 4)) || (rc = S.pstart.ensure(ctx, 4 * (npx + 1))) ||
+        (rc = S.pcount.ensure(ctx, 4 * npx)) || (rc = S.color.ensure(ctx, 4 * npx)) || (rc = S.depth.ensure(ctx, 4 * npx)))
+        return rc;
+    J.tri_slot = (const uint32_t*)S.tri_slot.ptr;
+    J.tri_seg = (const uint32_t*)S.tri_seg.ptr;
+    // 1. visible triangles of the job, compacted in draw order
+    k_seg_bases<<<1, 1024, 0, st>>>((const uint32_t*)ctx->seg_count.ptr, seg_lo, nseg, (uint32_t*)S.cbase.ptr);
+    if (nseg)
+        k_tri_lists<<<(nseg * 32 + 255) / 256, 256, 0, st>>>(ctx->params.segs, (const uint32_t*)ctx->seg_count.ptr, seg_lo,
+                                                             nseg, (const uint32_t*)S.cbase.ptr, (uint32_t*)S.tri_slot.ptr,
+                                                             (uint32_t*)S.tri_seg.ptr);
+    uint32_t n = 0;
+    CKR(cudaMemcpyAsync(&n, (const uint32_t*)S.cbase.ptr + nseg, 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    // 2. fragments in draw order
+    uint32_t nf = 0;
+    if (n) {
+        k_frag_count<<<(n + 255) / 256, 256, 0, st>>>(J, n, (uint32_t*)S.fcount.ptr);
+        if ((rc = scan_u32(ctx, S, (const uint32_t*)S.fcount.ptr, (uint32_t*)S.foff.ptr, n, st))) return rc;
+        uint32_t last[2];
+        CKR(cudaMemcpyAsync(&last[0], (const uint32_t*)S.foff.ptr + n - 1, 4, cudaMemcpyDeviceToHost, st));
+        CKR(cudaMemcpyAsync(&last[1], (const uint32_t*)S.fcount.ptr + n - 1, 4, cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+        nf = last[0] + last[1];
+    }
+    const uint32_t nsb = std::max(1u, (nf + kSortChunk - 1) / kSortChunk);
+    if ((rc = S.keys.ensure(ctx, 4ull * std::max(1u, nf))) || (rc = S.vals.ensure(ctx, 4ull * std::max(1u, nf))) ||
+        (rc = S.keys2.ensure(ctx, 4ull * std::max(1u, nf))) || (rc = S.vals2.ensure(ctx, 4ull * std::max(1u, nf))) ||
+        (rc = S.counts.ensure(ctx, 4ull * kSortDigits * nsb)) || (rc = S.offsets.ensure(ctx, 4ull * kSortDigits * nsb)))
+        return rc;
+    uint32_t *kin = (uint32_t*)S.keys.ptr, *vin = (uint32_t*)S.vals.ptr;
+    uint32_t *kout = (uint32_t*)S.keys2.ptr, *vout = (uint32_t*)S.vals2.ptr;
+    if (nf) {
+        k_frag_write<<<(n + 255) / 256, 256, 0, st>>>(J, n, (const uint32_t*)S.foff.ptr, kin, vin);
+        // 3. stable sort by pixel
+        int bits = 1;
+        while ((1ull << bits) < npx) bits++;
+        for (int shift = 0; shift < bits; shift += kSortBits) {
+            k_sort_hist<<<nsb, kSortThreads, 0, st>>>(kin, nf, shift, nsb, (uint32_t*)S.counts.ptr);
+            if ((rc = scan_u32(ctx, S, (const uint32_t*)S.counts.ptr, (uint32_t*)S.offsets.ptr, kSortDigits * nsb, st)))
+                return rc;
+            k_sort_scatter<<<nsb, kSortThreads, 0, st>>>(kin, vin, nf, shift, nsb, (const uint32_t*)S.offsets.ptr, kout, vout);
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+        }
+    }
+    // 4. per-pixel fragment ranges
+    CKR(cudaMemsetAsync(S.pcount.ptr, 0, 4 * npx, st));
+    if (nf) k_pixel_count<<<(nf + 255) / 256, 256, 0, st>>>(kin, nf, (uint32_t*)S.pcount.ptr);
+    if ((rc = scan_u32(ctx, S, (const uint32_t*)S.pcount.ptr, (uint32_t*)S.pstart.ptr, (uint32_t)npx, st))) return rc;
+    CKR(cudaMemcpyAsync((uint32_t*)S.pstart.ptr + npx, &nf, 4, cudaMemcpyHostToDevice, st));
+    // 5. replay per pixel
+    k_pixels<<<(uint32_t)((npx + 255) / 256), 256, 0, st>>>(J, (const uint32_t*)S.pstart.ptr, vin, (uint32_t*)S.color.ptr,
+                                                           (uint32_t*)S.depth.ptr);
+    CKR(cudaGetLastError());
+    CKR(cudaStreamSynchronize(st));
+    R.W = J.W;
+    R.H = J.H;
+    R.valid = true;
+    return T3D_OK;
+}
+
+int t3d_frame_images(t3d_ctx* ctx, uint8_t* color_rgba8, uint8_t* depth_rgba8, int32_t* width, int32_t* height) {
+    if (!ctx) return T3D_E_INVAL;
+    if (!ctx->raster || !ctx->raster->valid) {
+        set_err(ctx, "frame_images: nothing rasterised");
+        return T3D_E_INVAL;
+    }
+    t3d_raster_state& R = *ctx->raster;
+    if (width) *width = R.W;
+    if (height) *height = R.H;
+    cudaSetDevice(ctx->device);
+    const size_t bytes = 4ull * R.W * R.H;
+    if (color_rgba8) CKR(cudaMemcpy(color_rgba8, R.S.color.ptr, bytes, cudaMemcpyDeviceToHost));
+    if (depth_rgba8) CKR(cudaMemcpy(depth_rgba8, R.S.depth.ptr, bytes, cudaMemcpyDeviceToHost));
+    return T3D_OK;
+}
+
+}  // extern "C"
+
+void t3d_raster_release(t3d_ctx* ctx) {
+    if (!ctx->raster) return;
+    RasterScratch& S = ctx->raster->S;
+    for (DevBuf* b : {&S.cbase, &S.tri_slot, &S.tri_seg, &S.fcount, &S.foff, &S.keys, &S.vals, &S.keys2, &S.vals2,
+                      &S.counts, &S.offsets, &S.partial[0], &S.partial[1], &S.partial[2], &S.pstart, &S.pcount, &S.color,
+                      &S.depth})
+        b->release();
+    delete ctx->raster;
+    ctx->raster = nullptr;
+}

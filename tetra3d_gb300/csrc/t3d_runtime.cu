@@ -534,6 +534,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (me.colors) flags |= SEG_COLORS;
             if (mat.present) flags |= SEG_MAT;
             if (part.vcount > kLocalVerts) flags |= SEG_WIDE;
+            if (is_transparent(m.d.color, mat)) flags |= SEG_TRANSPARENT;
             uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
             flags |= sort_mode << 8;
             flags |= (uint32_t)(mat.present ? mat.lighting_mode : 0) << 10;

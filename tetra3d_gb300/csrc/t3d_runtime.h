@@ -87,6 +87,9 @@ struct FrameTables {
 
 }  // namespace t3d
 
+struct t3d_raster_state;
+void t3d_raster_release(struct t3d_ctx* ctx);
+
 struct t3d_ctx {
     int device = 0;
     std::string err;
@@ -110,6 +113,7 @@ struct t3d_ctx {
     bool tables_ok = false;
     bool order_dep = true;   // the draw order depends on model transforms (transparents, depth off)
     cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
+    struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
