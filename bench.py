@@ -280,6 +280,21 @@ def run_ours(args, rank, world, local_rank):
                "d2h_bytes_per_step": int(d2h // ek), "ms_per_step": el / ek * 1e3, "steps": ek,
                "host_ms_per_step": {k: round(v / ek * 1e3, 3) for k, v in tm.items()}}
 
+    # ---- rasterising the last frame's stream (colour + depth passes of flush) ----
+    raster = None
+    if rank == 0 and not args.no_raster:
+        ctx.render(sid, cam, mode=abi.MODE_BATCHED, stream=sh)
+        rst = ctx.sync()
+        col, dep = ctx.raster()
+        reps, r0 = 3, time.perf_counter()
+        for _ in range(reps):
+            ctx.raster(download=False)
+        rms = (time.perf_counter() - r0) / reps * 1e3
+        raster = {"ms_per_frame": rms, "image": f"{cam.width}x{cam.height}",
+                  "visible_tris": int(rst.visible_tris), "tris_per_s": int(rst.visible_tris) / (rms / 1e3),
+                  "covered_pixels": int((col[..., 3] > 0).sum()),
+                  "note": "wall time of t3d_frame_raster (fragments, stable sort by pixel, per-pixel passes) incl. its host syncs"}
+
     # ---- serving sweep (continuous batching over 64 resident scenes) ----
     serve = None
     if rank == 0 and not args.no_serving and args.workload == "batched":
@@ -325,6 +340,7 @@ def run_ours(args, rank, world, local_rank):
             "autotune": tuned,
             "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,
             "serving": serve,
+            "raster": raster,
         }
         print(json.dumps(line))
     ctx.close()
@@ -463,6 +479,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep in the default run")
+    ap.add_argument("--no-raster", action="store_true", help="skip rasterising the last frame")
     ap.add_argument("--rates", default="100,1000,5000,20000", help="serving request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival span per serving rate")
     ap.add_argument("--serve-max-requests", type=int, default=8000)

@@ -117,11 +117,14 @@ class Context:
         self._check(self.lib.t3d_frame_view_get(self.h, C.byref(v)), "frame_view_get")
         return v
 
-    def raster(self, job=0, fog_curve=0, dither_size=0.0, fogless=0, stream=None):
+    def raster(self, job=0, fog_curve=0, dither_size=0.0, fogless=0, stream=None, download=True):
         """Rasterises one job of the last frame (the colour and depth passes of flush) and returns
-        (colour, depth) RGBA8 images of shape (height, width, 4), premultiplied."""
+        (colour, depth) RGBA8 images of shape (height, width, 4), premultiplied (None, None without
+        download: the images stay on the device)."""
         o = abi.RasterOpts(fog_curve, float(dither_size), fogless, 0)
         self._check(self.lib.t3d_frame_raster(self.h, job, C.byref(o), stream), "frame_raster")
+        if not download:
+            return None, None
         w, h = C.c_int32(), C.c_int32()
         self._check(self.lib.t3d_frame_images(self.h, None, None, C.byref(w), C.byref(h)), "frame_images")
         col = np.zeros((h.value, w.value, 4), np.uint8)
