@@ -209,6 +209,13 @@ typedef struct t3d_camera_desc {
     float   depth_margin;        /* default 0.04 */
     float   fog_range[2];
     float   fog_color[4];
+    /* Camera.MaxLightCount (camera.go:1474-1497): > 0 keeps that many lights of the scene
+     * list (list 0) after a stable sort by kind (ambient, directional) then squared
+     * distance to the focus point; LightGroups are not affected. 0 = all lights. */
+    int32_t max_light_count;
+    int32_t focus_set;           /* MaxLightCountFocusPoint != nil */
+    float   focus[3];            /* its WorldPosition(); otherwise the camera's is used */
+    float   reserved;
 } t3d_camera_desc;
 
 /* One unit of rendering work: one camera over one resident scene, optionally

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <limits>
 #include <thread>
+#include <functional>
 #include <vector>
 
 namespace {
@@ -213,6 +214,7 @@ template <typename R> struct Frame {
     std::vector<ModelState<R>> models;
     std::vector<Dims> dims;
     const uint64_t* mask;
+    std::vector<uint32_t> scene_lights;  // list 0 after the light mask and Camera.MaxLightCount
 };
 
 inline bool light_enabled(const uint64_t* mask, uint32_t i) {
@@ -220,6 +222,64 @@ inline bool light_enabled(const uint64_t* mask, uint32_t i) {
     if (i >= 128) return false;
     return (mask[i >> 6] >> (i & 63)) & 1ull;
 }
+
+// sort.SliceStable of Go's standard library (sort/zsortfunc.go): insertionSort over
+// 20-element blocks, then symMerge of doubling runs (Kim & Kutzner's SymMerge with
+// rotations by block swaps). Camera.Render (camera.go:1482-1495) sorts the scene lights
+// with it under a comparator that is not a strict weak order, so its exact steps matter.
+struct GoSort {
+    std::vector<uint32_t>& v;
+    std::function<bool(uint32_t, uint32_t)> less;
+    bool lt(int i, int j) const { return less(v[i], v[j]); }
+    void sw(int i, int j) { std::swap(v[i], v[j]); }
+    void insertion_sort(int a, int b) {
+        for (int i = a + 1; i < b; i++)
+            for (int j = i; j > a && lt(j, j - 1); j--) sw(j, j - 1);
+    }
+    void swap_range(int a, int b, int n) {
+        for (int i = 0; i < n; i++) sw(a + i, b + i);
+    }
+    void rotate(int a, int m, int b) {
+        int i = m - a, j = b - m;
+        while (i != j) {
+            if (i > j) { swap_range(m - i, m, j); i -= j; }
+            else { swap_range(m - i, m + j - i, i); j -= i; }
+        }
+        swap_range(m - i, m, i);
+    }
+    void sym_merge(int a, int m, int b) {
+        if (m - a == 1) {  // insert v[a] into v[m:b]
+            int i = m, j = b;
+            while (i < j) { int h = (int)((unsigned)(i + j) >> 1); if (lt(h, a)) i = h + 1; else j = h; }
+            for (int k = a; k < i - 1; k++) sw(k, k + 1);
+            return;
+        }
+        if (b - m == 1) {  // insert v[m] into v[a:m]
+            int i = a, j = m;
+            while (i < j) { int h = (int)((unsigned)(i + j) >> 1); if (!lt(m, h)) i = h + 1; else j = h; }
+            for (int k = m; k > i; k--) sw(k, k - 1);
+            return;
+        }
+        int mid = (int)((unsigned)(a + b) >> 1), n = mid + m, start, r;
+        if (m > mid) { start = n - b; r = mid; } else { start = a; r = m; }
+        int p = n - 1;
+        while (start < r) { int c = (int)((unsigned)(start + r) >> 1); if (!lt(p - c, c)) start = c + 1; else r = c; }
+        int end = n - start;
+        if (start < m && m < end) rotate(start, m, end);
+        if (a < start && start < mid) sym_merge(a, start, mid);
+        if (mid < end && end < b) sym_merge(mid, end, b);
+    }
+    void run() {
+        int n = (int)v.size(), bs = 20, a = 0, b = bs;
+        for (; b <= n; a = b, b += bs) insertion_sort(a, b);
+        insertion_sort(a, n);
+        for (; bs < n; bs *= 2) {
+            a = 0; b = 2 * bs;
+            for (; b <= n; a = b, b += 2 * bs) sym_merge(a, a + bs, b);
+            if (a + bs < n) sym_merge(a, a + bs, n);
+        }
+    }
+};
 
 // Mesh.UpdateDimensions (mesh.go:713-748)
 Dims mesh_dims(const t3d_mesh_desc& me) {
@@ -557,8 +617,10 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
             Dims dm = F.dims[md.mesh];
             R maxSpan = magnitude(v3<R>((R)dm.mx[0] - (R)dm.mn[0], (R)dm.mx[1] - (R)dm.mn[1], (R)dm.mx[2] - (R)dm.mn[2]));
             V3<R> modelPos = row3(modelTransform, 3);
-            for (uint32_t q = sc->list_offsets[list]; q < sc->list_offsets[list + 1]; q++) {
-                uint32_t li = sc->list_items[q];
+            std::vector<uint32_t> items;
+            if (list == 0) items = F.scene_lights;
+            else for (uint32_t q = sc->list_offsets[list]; q < sc->list_offsets[list + 1]; q++) items.push_back(sc->list_items[q]);
+            for (uint32_t li : items) {
                 if (li >= F.lights.size() || !light_enabled(F.mask, li)) continue;
                 ModelLight<R> ml;
                 ml.l = &F.lights[li];
@@ -652,6 +714,31 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
     Frame<R> F;
     F.sc = sc;
     F.mask = mask;
+    // the scene light list after the mask, then Camera.MaxLightCount (camera.go:1474-1497)
+    if (sc->num_lists > 0)
+        for (uint32_t q = sc->list_offsets[0]; q < sc->list_offsets[1]; q++)
+            if (sc->list_items[q] < sc->num_lights && light_enabled(mask, sc->list_items[q]))
+                F.scene_lights.push_back(sc->list_items[q]);
+    if (cd->max_light_count > 0) {
+        const float fx = cd->focus_set ? cd->focus[0] : cd->transform[12];
+        const float fy = cd->focus_set ? cd->focus[1] : cd->transform[13];
+        const float fz = cd->focus_set ? cd->focus[2] : cd->transform[14];
+        auto dist2_to = [&](uint32_t li) {  // Vector3.DistanceSquaredTo, vector.go:242-247
+            const float* t = sc->lights[li].transform;
+            float x = fx - t[12], y = fy - t[13], z = fz - t[14];
+            return x * x + y * y + z * z;
+        };
+        GoSort gs{F.scene_lights, [&](uint32_t i, uint32_t j) {
+                      const int a = sc->lights[i].type, b = sc->lights[j].type;
+                      if (a == T3D_LIGHT_AMBIENT) return true;
+                      if (b == T3D_LIGHT_AMBIENT) return false;
+                      if (a == T3D_LIGHT_DIRECTIONAL) return true;
+                      if (b == T3D_LIGHT_DIRECTIONAL) return false;
+                      return dist2_to(i) < dist2_to(j);
+                  }};
+        gs.run();
+        if (F.scene_lights.size() > (size_t)cd->max_light_count) F.scene_lights.resize((size_t)cd->max_light_count);
+    }
     setup_camera(F.cam, cd);
 
     // models: Node.Transform (node.go:572-608) with optional animation steps

@@ -274,3 +274,33 @@ def test_reused_launch_tables_follow_model_updates(ctx):
         assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "transparent reorder")
     finally:
         ctx.release(sid)
+
+
+def _max_light_scene(nlights, seed=21):
+    sd = scenes.batched_scene(seed, n=24, vmin=24, vmax=1500, nlights=nlights, box=40.0, max_levels=3)
+    sd.mv["light_list"] = -1
+    return sd
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_max_light_count_matches_oracle(ctx, mixed):
+    """Camera.MaxLightCount on the device path against the oracle; `mixed` adds extra ambient and
+    directional lights, where the reference's comparator is not a strict order and the result is
+    that of Go's stable sort algorithm."""
+    sd = _max_light_scene(40)
+    if mixed:
+        for i in (7, 19, 33):
+            sd.lights[i].type = abi.LIGHT_DIRECTIONAL
+        sd.lights[25].type = abi.LIGHT_AMBIENT
+    for keep, focus in ((25, None), (30, (10.0, -5.0, 20.0)), (3, None)):
+        cam = sd.camera
+        cam.max_light_count = keep
+        cam.focus_set = int(focus is not None)
+        if focus is not None:
+            cam.focus[:] = list(focus)
+        sid = ctx.upload(sd)
+        try:
+            ctx.render(sid, cam)
+            assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), f"keep {keep} mixed {mixed}")
+        finally:
+            ctx.release(sid)

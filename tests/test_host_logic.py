@@ -140,3 +140,49 @@ def test_workload_sizes():
     assert c.nmodels == 1000 and c.total_tris() == 12000
     s = scenes.uv_sphere_scene(1)
     assert s.total_verts() == 17 * 32
+
+
+def _scene_list_scene(nlights, seed=21):
+    sd = scenes.batched_scene(seed, n=24, vmin=24, vmax=1500, nlights=nlights, box=40.0, max_levels=3)
+    sd.mv["light_list"] = -1  # every model lit by the scene list (list 0)
+    return sd
+
+
+@pytest.mark.parametrize("nlights,keep", [(8, 4), (40, 25), (40, 1)])
+def test_max_light_count_keeps_the_nearest_scene_lights(nlights, keep):
+    """Camera.MaxLightCount (camera.go:1474-1497): ambient first, then lights by squared distance
+    from the camera; 40 lights run Go's stable sort past its 20-element insertion blocks."""
+    sd = _scene_list_scene(nlights)
+    cam = sd.camera
+    cam.max_light_count = keep
+    culled = pyoracle.render(sd, cam)
+    campos = np.array(cam.transform, F).reshape(4, 4)[3, :3]
+    lights = [sd.lights[i] for i in sd.lists[0]]
+    def d2(L):
+        p = np.array(L.transform, F).reshape(4, 4)[3, :3]
+        d = campos - p
+        return F(F(d[0] * d[0]) + F(d[1] * d[1])) + F(d[2] * d[2])
+    order = sorted(sd.lists[0], key=lambda i: (0, 0.0) if sd.lights[i].type == abi.LIGHT_AMBIENT else (1, float(d2(sd.lights[i]))))
+    explicit = _scene_list_scene(nlights)
+    explicit.lists[0] = order[:keep]
+    ref = pyoracle.render(explicit, explicit.camera)
+    assert culled.segments == ref.segments
+    assert np.array_equal(culled.rgba.view(np.uint32), ref.rgba.view(np.uint32))
+    full = pyoracle.render(_scene_list_scene(nlights), _scene_list_scene(nlights).camera)
+    assert not np.array_equal(full.rgba, culled.rgba)
+
+
+def test_max_light_count_focus_point_and_groups():
+    sd = _scene_list_scene(12)
+    cam = sd.camera
+    cam.max_light_count = 3
+    cam.focus_set = 1
+    cam.focus[:] = [30.0, 0.0, 0.0]
+    a = pyoracle.render(sd, cam)
+    cam.focus[:] = [-30.0, 0.0, 0.0]
+    b = pyoracle.render(sd, cam)
+    assert not np.array_equal(a.rgba, b.rgba)
+    g = scenes.small_variant("batched", 3)  # every model in a LightGroup: MaxLightCount does not apply
+    base = pyoracle.render(g, g.camera)
+    g.camera.max_light_count = 1
+    assert np.array_equal(pyoracle.render(g, g.camera).rgba.view(np.uint32), base.rgba.view(np.uint32))

@@ -97,6 +97,123 @@ static bool light_enabled(const uint64_t* mask, uint32_t i) {
 }
 
 // Model.isTransparent (model.go:1274-1282)
+// Go's sort.SliceStable (sort/zsortfunc.go: insertion sort of 20-element blocks, then
+// SymMerge passes, Kim & Kutzner), restated because Camera.Render sorts the scene lights
+// with a comparator that is not a strict weak order (two ambient or two directional
+// lights are each "less" than the other): the order it produces is the algorithm's.
+namespace gosort {
+template <typename Less> void insertion(std::vector<uint32_t>& d, int a, int b, Less less) {
+    for (int i = a + 1; i < b; i++)
+        for (int j = i; j > a && less(d[j], d[j - 1]); j--) std::swap(d[j], d[j - 1]);
+}
+inline void swap_range(std::vector<uint32_t>& d, int a, int b, int n) {
+    for (int i = 0; i < n; i++) std::swap(d[a + i], d[b + i]);
+}
+inline void rotate(std::vector<uint32_t>& d, int a, int m, int b) {
+    int i = m - a, j = b - m;
+    while (i != j) {
+        if (i > j) {
+            swap_range(d, m - i, m, j);
+            i -= j;
+        } else {
+            swap_range(d, m - i, m + j - i, i);
+            j -= i;
+        }
+    }
+    swap_range(d, m - i, m, i);
+}
+template <typename Less> void sym_merge(std::vector<uint32_t>& d, int a, int m, int b, Less less) {
+    if (m - a == 1) {
+        int i = m, j = b;
+        while (i < j) {
+            const int h = (int)((unsigned)(i + j) >> 1);
+            if (less(d[h], d[a])) i = h + 1;
+            else j = h;
+        }
+        for (int k = a; k < i - 1; k++) std::swap(d[k], d[k + 1]);
+        return;
+    }
+    if (b - m == 1) {
+        int i = a, j = m;
+        while (i < j) {
+            const int h = (int)((unsigned)(i + j) >> 1);
+            if (!less(d[m], d[h])) i = h + 1;
+            else j = h;
+        }
+        for (int k = m; k > i; k--) std::swap(d[k], d[k - 1]);
+        return;
+    }
+    const int mid = (int)((unsigned)(a + b) >> 1), n = mid + m;
+    int start, r;
+    if (m > mid) {
+        start = n - b;
+        r = mid;
+    } else {
+        start = a;
+        r = m;
+    }
+    const int p = n - 1;
+    while (start < r) {
+        const int c = (int)((unsigned)(start + r) >> 1);
+        if (!less(d[p - c], d[c])) start = c + 1;
+        else r = c;
+    }
+    const int end = n - start;
+    if (start < m && m < end) rotate(d, start, m, end);
+    if (a < start && start < mid) sym_merge(d, a, start, mid, less);
+    if (mid < end && end < b) sym_merge(d, mid, end, b, less);
+}
+template <typename Less> void stable(std::vector<uint32_t>& d, Less less) {
+    const int n = (int)d.size();
+    int block = 20, a = 0, b = block;
+    while (b <= n) {
+        insertion(d, a, b, less);
+        a = b;
+        b += block;
+    }
+    insertion(d, a, n, less);
+    while (block < n) {
+        a = 0;
+        b = 2 * block;
+        while (b <= n) {
+            sym_merge(d, a, a + block, b, less);
+            a = b;
+            b += 2 * block;
+        }
+        if (a + block < n) sym_merge(d, a, a + block, n, less);
+        block *= 2;
+    }
+}
+}  // namespace gosort
+
+// Camera.MaxLightCount (camera.go:1474-1497) over the job's scene light list.
+static std::vector<uint32_t> culled_scene_lights(const Scene* sc, const t3d_job_desc& job) {
+    std::vector<uint32_t> l;
+    for (uint32_t li : sc->lists[0])
+        if (light_enabled(job.light_mask, li)) l.push_back(li);
+    const t3d_camera_desc& cd = job.camera;
+    if (cd.max_light_count <= 0) return l;
+    const float px = cd.focus_set ? cd.focus[0] : cd.transform[12];
+    const float py = cd.focus_set ? cd.focus[1] : cd.transform[13];
+    const float pz = cd.focus_set ? cd.focus[2] : cd.transform[14];
+    auto d2 = [&](uint32_t li) {  // Vector3.DistanceSquaredTo (vector.go:242-247)
+        const float* t = sc->lights[li].transform;
+        const float x = px - t[12], y = py - t[13], z = pz - t[14];
+        return x * x + y * y + z * z;
+    };
+    auto less = [&](uint32_t i, uint32_t j) {
+        const int ti = sc->lights[i].type, tj = sc->lights[j].type;
+        if (ti == T3D_LIGHT_AMBIENT) return true;
+        if (tj == T3D_LIGHT_AMBIENT) return false;
+        if (ti == T3D_LIGHT_DIRECTIONAL) return true;
+        if (tj == T3D_LIGHT_DIRECTIONAL) return false;
+        return d2(i) < d2(j);
+    };
+    gosort::stable(l, less);
+    if (l.size() > (size_t)cd.max_light_count) l.resize((size_t)cd.max_light_count);
+    return l;
+}
+
 static bool is_transparent(const float* model_color, const t3d_material& mat) {
     if (mat.present) {
         bool matT = mat.transparency_mode == T3D_TRANSPARENCY_TRANSPARENT || !mat.blend_source_over ||
@@ -465,6 +582,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         struct Pair { uint32_t model, part; float depth; int32_t order; };
         std::vector<Pair> solids, transparents;
         std::vector<uint32_t> inst_of(sc->models.size(), 0xFFFFFFFFu);
+        const std::vector<uint32_t> scene_lights = culled_scene_lights(sc, jobs[j]);
         for (uint32_t mi = 0; mi < sc->models.size(); mi++) {
             SceneModel& m = sc->models[mi];
             if (!m.d.visible) continue;
@@ -477,7 +595,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             in.light_off = (uint32_t)F.inst_light_idx.size();
             uint32_t list = m.d.light_list < 0 ? 0u : (uint32_t)m.d.light_list;
             uint32_t cnt = 0;
-            for (uint32_t li : sc->lists[list]) {
+            for (uint32_t li : list == 0 ? scene_lights : sc->lists[list]) {
                 if (!light_enabled(jobs[j].light_mask, li)) continue;
                 F.inst_light_idx.push_back(li);  // relative to the job's light table (DevJob.lights)
                 cnt++;
