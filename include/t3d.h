@@ -66,6 +66,12 @@ extern "C" {
 #define T3D_LV_PER_VERTEX_WITH_NORMAL  1
 #define T3D_LV_PER_OBJECT              2
 #define T3D_LV_OFF                     3
+/* BillboardUpDirection, material.go:29-32 */
+#define T3D_BILLBOARD_UP_GLOBAL_Y 0
+#define T3D_BILLBOARD_UP_CAMERA_Y 1
+/* BillboardedDepthMode, material.go:45-48 */
+#define T3D_DEPTH_DEFAULT        0
+#define T3D_DEPTH_UNBILLBOARDED  1
 /* light kinds: AmbientLight, PointLight, DirectionalLight, LightVolume (light.go) */
 #define T3D_LIGHT_AMBIENT     0
 #define T3D_LIGHT_POINT       1
@@ -100,6 +106,14 @@ typedef struct t3d_material {
     int32_t transparency_mode; /* T3D_TRANSPARENCY_* */
     int32_t blend_source_over; /* 1 when Blend == ebiten.BlendSourceOver (default) */
     int32_t render_order;
+    /* Billboarding (model.go:634-688): the part turns to face the camera
+     * (NewMatrix4LookAt from the model's world position), optionally with
+     * axes locked; with T3D_DEPTH_UNBILLBOARDED the depth written when
+     * RenderDepth is on is that of the unturned part (model.go:698-803). */
+    int32_t billboard;         /* Material.BillboardEnabled */
+    int32_t billboard_lock[3]; /* BillboardLockX, BillboardLockY, BillboardLockZ */
+    int32_t billboard_up;      /* T3D_BILLBOARD_UP_* */
+    int32_t billboard_depth;   /* T3D_DEPTH_* */
 } t3d_material;
 
 /* A MeshPart (mesh.go:2183-2190): a contiguous triangle range with one material. */
@@ -125,6 +139,20 @@ typedef struct t3d_mesh_desc {
     int32_t              has_dimensions; /* 0: Dimensions computed like Mesh.UpdateDimensions */
     float                dim_min[3];     /* Mesh.Dimensions when has_dimensions */
     float                dim_max[3];
+    /* Shape keys (Mesh.VertexPositionWithShapeKeys / VertexNormalWithShapeKeys,
+     * mesh.go:796-822): per key, a position and a normal delta per vertex, added
+     * key by key times the key's weight (t3d_scene_set_shape_weights; initial
+     * weights here). NULL / 0 when the mesh has none. */
+    const float*         shape_positions; /* 3 * num_vertices * num_shape_keys */
+    const float*         shape_normals;   /* 3 * num_vertices * num_shape_keys */
+    const float*         shape_weights;   /* num_shape_keys */
+    uint32_t             num_shape_keys;
+    /* Skinning (Model.skinVertex, model.go:559-596): four joint slots per vertex and
+     * their weights (Mesh.VertexWeights); a skinned model maps joint j to scene bone
+     * bone_first + j. NULL when no model skins this mesh. */
+    uint32_t             reserved;
+    const uint32_t*      joints;          /* 4 * num_vertices */
+    const float*         weights;         /* 4 * num_vertices */
 } t3d_mesh_desc;
 
 /* A Model (model.go:20-61). Either `transform` holds Model.Transform() and
@@ -147,6 +175,11 @@ typedef struct t3d_model_desc {
     float    scale[3];
     float    rotation[16];
     float    rotate_step[16];
+    /* Model.skinned: vertices are skinned by the scene's bone influences (Node.boneInfluence,
+     * set with t3d_scene_set_bones) instead of transformed by the model matrix; the model
+     * transform still places its frustum sphere and its point-light range test. */
+    int32_t  skinned;
+    uint32_t bone_first;       /* the mesh's joint j uses scene bone bone_first + j */
 } t3d_model_desc;
 
 /* A light (light.go). transform = the light node's Transform(), world_rotation =
@@ -186,7 +219,8 @@ typedef struct t3d_scene_desc {
     uint32_t              num_lights;
     uint32_t              num_volume_cells;
     uint32_t              num_lists;
-    uint32_t              reserved;
+    uint32_t              num_bones;
+    const float*          bones;          /* 16 per bone: initial Node.boneInfluence matrices */
 } t3d_scene_desc;
 
 /* Camera + World settings read by Render (camera.go:256-321, world.go:25-39).
@@ -297,6 +331,11 @@ int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first,
 int t3d_scene_get_transforms(t3d_ctx* ctx, uint32_t scene, float* transforms_out, uint32_t n);
 /* Device bytes held by a scene's resident data. */
 int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out);
+/* Bone influence matrices [first, first + n) of a scene (16 floats each, Node.boneInfluence,
+ * node.go), as an animation player updates them every frame. */
+int t3d_scene_set_bones(t3d_ctx* ctx, uint32_t scene, uint32_t first, const float* influences, uint32_t n);
+/* Shape-key weights of one mesh of a scene (ShapeKey.weight, mesh.go). */
+int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, const float* weights, uint32_t n);
 
 /* ---- rendering --------------------------------------------------------------- */
 /* Camera.Render over one scene: enqueue on `stream` (a cudaStream_t, NULL =

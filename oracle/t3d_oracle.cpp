@@ -378,12 +378,15 @@ template <typename R> bool sphere_in_frustum(const Camera<R>& c, V3<R> position,
     return true;
 }
 
-// Model.onTransformUpdate (model.go:142-182) + ModelInFrustum (camera.go:986-989)
-template <typename R> bool model_in_frustum(const Camera<R>& c, const M4<R>& transform, const Dims& dm) {
+// Model.onTransformUpdate (model.go:142-182) + ModelInFrustum (camera.go:986-989);
+// a skinned model's sphere has no mesh-centre offset (model.go:158-161)
+template <typename R> bool model_in_frustum(const Camera<R>& c, const M4<R>& transform, const Dims& dm, bool skinned) {
     V3<R> position, scale; M4<R> rotation;
     decompose(transform, position, scale, rotation);
-    V3<R> center = v3<R>(((R)dm.mx[0] + (R)dm.mn[0]) / (R)2, ((R)dm.mx[1] + (R)dm.mn[1]) / (R)2,
-                         ((R)dm.mx[2] + (R)dm.mn[2]) / (R)2);
+    V3<R> center = v3<R>(0, 0, 0);
+    if (!skinned)
+        center = v3<R>(((R)dm.mx[0] + (R)dm.mn[0]) / (R)2, ((R)dm.mx[1] + (R)dm.mn[1]) / (R)2,
+                       ((R)dm.mx[2] + (R)dm.mn[2]) / (R)2);
     center = mult_vec(rotation, center);
     position.x += center.x * scale.x;
     position.y += center.y * scale.y;
@@ -394,9 +397,70 @@ template <typename R> bool model_in_frustum(const Camera<R>& c, const M4<R>& tra
     return sphere_in_frustum(c, position, radius);
 }
 
+// ---------------------------------------------------------- billboards ----
+template <typename R> inline bool vequals(V3<R> a, V3<R> b) {  // Vector3.Equals, vector.go:415-425
+    const R eps = k<R>(1e-4);
+    return !(m_abs<R>(a.x - b.x) > eps || m_abs<R>(a.y - b.y) > eps || m_abs<R>(a.z - b.z) > eps);
+}
+template <typename R> inline V3<R> cross(V3<R> a, V3<R> b) {  // Vector3.Cross, vector.go:164-175
+    R z = a.x * b.y - b.x * a.y;
+    R y = a.z * b.x - b.z * a.x;
+    R x = a.y * b.z - b.y * a.z;
+    return v3(x, y, z);
+}
+template <typename R> M4<R> look_at(V3<R> from, V3<R> to, V3<R> up) {  // NewMatrix4LookAt, matrix.go:788-815
+    if (vequals(from, to)) return identity<R>();
+    V3<R> z = unit(sub(to, from));
+    up = unit(up);
+    if (vequals(z, up) || vequals(z, v3<R>(-up.x, -up.y, -up.z))) {
+        if (!vequals(up, v3<R>(1, 0, 0))) up = v3<R>(1, 0, 0);
+        else up = v3<R>(0, 0, 1);
+    }
+    V3<R> x = unit(cross(up, z));
+    V3<R> y = cross(z, x);
+    M4<R> m = identity<R>();
+    m.m[0][0] = x.x; m.m[0][1] = x.y; m.m[0][2] = x.z; m.m[0][3] = 0;
+    m.m[1][0] = y.x; m.m[1][1] = y.y; m.m[1][2] = y.z; m.m[1][3] = 0;
+    m.m[2][0] = z.x; m.m[2][1] = z.y; m.m[2][2] = z.z; m.m[2][3] = 0;
+    return m;
+}
+template <typename R> inline V4<R> row4(const M4<R>& m, int i) { return V4<R>{m.m[i][0], m.m[i][1], m.m[i][2], m.m[i][3]}; }
+template <typename R> inline void set_row(M4<R>& m, int i, V4<R> v) {  // Matrix4.SetRow, matrix.go:564-569
+    m.m[i][0] = v.x; m.m[i][1] = v.y; m.m[i][2] = v.z; m.m[i][3] = v.w;
+}
+// The billboarded `base` of ProcessVertices (model.go:634-688).
+template <typename R>
+M4<R> billboard_base(const M4<R>& modelTransform, const Camera<R>& cam, const t3d_material& mat) {
+    V3<R> up = v3<R>(0, 1, 0);  // WorldUp
+    if (mat.billboard_up == T3D_BILLBOARD_UP_CAMERA_Y) up = cam.upv;
+    M4<R> lookat = look_at(row3(modelTransform, 3), cam.pos, up);
+    if (mat.billboard_lock[0]) {
+        set_row(lookat, 0, V4<R>{1, 0, 0, 0});
+        V4<R> row = row4(lookat, 1); row.x = 0; set_row(lookat, 1, unit4(row));
+        row = row4(lookat, 2); row.x = 0; set_row(lookat, 2, unit4(row));
+    }
+    if (mat.billboard_lock[1]) {
+        set_row(lookat, 1, V4<R>{0, 1, 0, 0});
+        V4<R> row = row4(lookat, 0); row.y = 0; set_row(lookat, 0, unit4(row));
+        row = row4(lookat, 2); row.y = 0; set_row(lookat, 2, unit4(row));
+    }
+    if (mat.billboard_lock[2]) {
+        set_row(lookat, 2, V4<R>{0, 0, 1, 0});
+        V4<R> row = row4(lookat, 0); row.z = 0; set_row(lookat, 0, unit4(row));
+        row = row4(lookat, 1); row.z = 0; set_row(lookat, 1, unit4(row));
+    }
+    V3<R> p, s; M4<R> r;
+    decompose(modelTransform, p, s, r);
+    M4<R> base = mult(mult(r, scale_m<R>(s.x, s.y, s.z)), lookat);
+    set_row(base, 3, V4<R>{p.x, p.y, p.z, 1});
+    return base;
+}
+
 // ------------------------------------------------------ per-pair render ----
 template <typename R> struct Scratch {
     std::vector<V4<R>> clip;               // globalVertexTransforms
+    std::vector<V3<R>> apos, anrm;         // globalMeshAlteredVertexPositions / Normals
+    std::vector<R> udepth;                 // globalVertexDepthUnbillboarded
     std::vector<C4<R>> vlight;             // mesh.vertexLights
     std::vector<std::vector<std::pair<uint32_t, R>>> bins;
     std::vector<std::pair<uint32_t, R>> unset;
@@ -420,13 +484,12 @@ template <typename R> bool lv_cell(const t3d_light_desc* d, V3<R> p, long long& 
     return true;
 }
 
+// vpos / vnrm: the altered vertex (model space, or world space when skinned).
 template <typename R>
-void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_desc& part, const t3d_mesh_desc& me,
-                  const M4<R>& transform, const M4<R>& dir_rot, uint32_t vi, C4<R>& tgt) {
+void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_desc& part, bool skinned,
+                  const M4<R>& transform, const M4<R>& dir_rot, V3<R> vpos, V3<R> vnrm, C4<R>& tgt) {
     const LightPrep<R>& L = *ml.l;
     const t3d_material& mat = part.mat;
-    V3<R> vpos = v3<R>((R)me.positions[3 * vi], (R)me.positions[3 * vi + 1], (R)me.positions[3 * vi + 2]);
-    V3<R> vnrm = v3<R>((R)me.normals[3 * vi], (R)me.normals[3 * vi + 1], (R)me.normals[3 * vi + 2]);
     switch (L.type) {
     case T3D_LIGHT_AMBIENT:  // light.go:115-120
         tgt.r += L.amb.x; tgt.g += L.amb.y; tgt.b += L.amb.z;
@@ -458,6 +521,7 @@ void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_des
     case T3D_LIGHT_DIRECTIONAL: {  // light.go:332-360
         V3<R> normal;
         if (mat.present && mat.lighting_mode == T3D_LIGHTING_FIXED_NORMALS) normal = L.fwd;
+        else if (skinned) normal = vnrm;
         else normal = mult_vec(dir_rot, vnrm);
         R diffuseFactor = dot(normal, L.fwd);
         if (mat.present && mat.lighting_mode == T3D_LIGHTING_DOUBLE_SIDED) diffuseFactor = m_abs<R>(diffuseFactor);
@@ -482,10 +546,14 @@ void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_des
             }
         } else {
             V3<R> vertPos = v3<R>(0, 0, 0), vertPosWithNormal = v3<R>(0, 0, 0);
-            if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL)
+            if (skinned) {  // light.go:613-620
+                if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) vertPosWithNormal = add(add(vertPos, hmul(vnrm, cellSize)), bias);
+                else vertPos = add(vpos, bias);
+            } else if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) {
                 vertPosWithNormal = add(mult_vec(transform, add(vpos, hmul(vnrm, cellSize))), bias);
-            else
+            } else {
                 vertPos = add(mult_vec(transform, vpos), bias);
+            }
             // Dimensions.Contains (mesh.go:82-84)
             if (!(vertPos.x >= (R)d->vol_min[0] && vertPos.y >= (R)d->vol_min[1] && vertPos.z >= (R)d->vol_min[2] &&
                   vertPos.x <= (R)d->vol_max[0] && vertPos.y <= (R)d->vol_max[1] && vertPos.z <= (R)d->vol_max[2]))
@@ -504,6 +572,42 @@ void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_des
     default:
         break;
     }
+}
+
+// Mesh.VertexPositionWithShapeKeys / VertexNormalWithShapeKeys (mesh.go:796-822)
+// and, for a skinned model, Model.skinVertex (model.go:559-594).
+template <typename R>
+void altered_vertex(const t3d_scene_desc* sc, const t3d_model_desc& md, const t3d_mesh_desc& me, uint32_t v,
+                    V3<R>& pos, V3<R>& nrm) {
+    pos = v3<R>((R)me.positions[3 * v], (R)me.positions[3 * v + 1], (R)me.positions[3 * v + 2]);
+    nrm = v3<R>((R)me.normals[3 * v], (R)me.normals[3 * v + 1], (R)me.normals[3 * v + 2]);
+    for (uint32_t key = 0; key < me.num_shape_keys; key++) {
+        const R w = (R)me.shape_weights[key];
+        const size_t e = 3 * ((size_t)key * me.num_vertices + v);
+        pos.x += (R)me.shape_positions[e] * w;
+        pos.y += (R)me.shape_positions[e + 1] * w;
+        pos.z += (R)me.shape_positions[e + 2] * w;
+        nrm.x += (R)me.shape_normals[e] * w;
+        nrm.y += (R)me.shape_normals[e + 1] * w;
+        nrm.z += (R)me.shape_normals[e + 2] * w;
+    }
+    if (!md.skinned) return;
+    M4<R> skin;
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) skin.m[r][c] = 0;  // Matrix4.Clear
+    for (int i = 0; i < 4; i++) {
+        const R w = (R)me.weights[4 * (size_t)v + i];
+        if (w == 0) continue;
+        const float* bone = sc->bones + 16 * ((size_t)md.bone_first + me.joints[4 * (size_t)v + i]);
+        if (w == 1) {
+            skin = load_m<R>(bone);
+            break;
+        }
+        for (int q = 0; q < 16; q++) skin.m[q / 4][q % 4] = skin.m[q / 4][q % 4] + (R)bone[q] * w;  // Add(Scale(w))
+    }
+    pos = mult_vec(skin, pos);
+    skin.m[3][0] = 0; skin.m[3][1] = 0; skin.m[3][2] = 0; skin.m[3][3] = 1;
+    nrm = mult_vec(skin, nrm);
 }
 
 // The render closure (camera.go:1507-1827) with Model.ProcessVertices
@@ -529,20 +633,32 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
     V3<R> p, s; M4<R> r;
     decompose(inverted(modelTransform), p, s, r);  // model.go:629
     V3<R> invertedCamPos = add(mult_vec(r, camPos), hmul(p, v3<R>((R)1 / s.x, (R)1 / s.y, (R)1 / s.z)));  // :630
-    M4<R> mvp = mult(modelTransform, cam.vp);  // model.go:695
+    const bool skinned = md.skinned != 0;
+    // skinned vertices are in world space: VP alone (model.go:760-770)
+    const bool billboard = mat.present && mat.billboard && !skinned;
+    const bool unbillboarded = billboard && mat.billboard_depth == T3D_DEPTH_UNBILLBOARDED;
+    M4<R> base = billboard ? billboard_base(modelTransform, cam, mat) : modelTransform;
+    M4<R> mvp = skinned ? cam.vp : mult(base, cam.vp);  // model.go:695
+    M4<R> unalteredMVP = mult(modelTransform, cam.vp);   // model.go:700-703
 
     R minDepth = maxf<R>();   // model.go:710-711
     R maxDepth = -maxf<R>();
     R camNear = cam.near_, camFar = cam.far_;
 
-    if (S.clip.size() < me.num_vertices) S.clip.resize(me.num_vertices);
+    if (S.clip.size() < me.num_vertices) {
+        S.clip.resize(me.num_vertices);
+        S.apos.resize(me.num_vertices);
+        S.anrm.resize(me.num_vertices);
+        S.udepth.resize(me.num_vertices);
+    }
     uint32_t t_end = part.tri_start + part.tri_count;
     for (uint32_t t = part.tri_start; t < t_end; t++) {  // model.go:751-979
         uint32_t vidx[3] = {me.indices[3 * t], me.indices[3 * t + 1], me.indices[3 * t + 2]};
         for (int vi = 0; vi < 3; vi++) {
             uint32_t v = vidx[vi];
-            V3<R> vert = v3<R>((R)me.positions[3 * v], (R)me.positions[3 * v + 1], (R)me.positions[3 * v + 2]);
-            S.clip[v] = mult_vec_w(mvp, vert);  // model.go:808-811
+            altered_vertex<R>(sc, md, me, v, S.apos[v], S.anrm[v]);
+            S.clip[v] = mult_vec_w(mvp, S.apos[v]);  // model.go:808-811
+            if (unbillboarded) S.udepth[v] = mult_vec_w(unalteredMVP, S.apos[v]).z;  // model.go:800-801
         }
         bool outOfBounds = true;  // model.go:855-886
         V3<R> tv[3];
@@ -572,7 +688,16 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
         const float* pc = me.positions + 3 * (size_t)vidx[2];
         V3<R> center = v3<R>(((R)pa[0] + (R)pb[0] + (R)pc[0]) / (R)3, ((R)pa[1] + (R)pb[1] + (R)pc[1]) / (R)3,
                              ((R)pa[2] + (R)pb[2] + (R)pc[2]) / (R)3);
-        R dx = invertedCamPos.x - center.x, dy = invertedCamPos.y - center.y, dz = invertedCamPos.z - center.z;
+        V3<R> from = invertedCamPos;
+        if (skinned) {  // the skinned centre from the world camera (model.go:840-863, :941-946)
+            const V3<R>& a = S.apos[vidx[0]];
+            const V3<R>& b = S.apos[vidx[1]];
+            const V3<R>& c = S.apos[vidx[2]];
+            center = v3<R>((((R)0 + a.x) + b.x + c.x) / (R)3, (((R)0 + a.y) + b.y + c.y) / (R)3,
+                           (((R)0 + a.z) + b.z + c.z) / (R)3);
+            from = camPos;
+        }
+        R dx = from.x - center.x, dy = from.y - center.y, dz = from.z - center.z;
         R depth = dx * dx + dy * dy + dz * dz;  // model.go:950-953
         if (std::isnan(depth) || std::isinf(depth)) continue;
         if (depth < minDepth) minDepth = depth;
@@ -627,7 +752,8 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
                 ml.working = v3<R>(0, 0, 0);
                 ml.skip = false;
                 if (ml.l->type == T3D_LIGHT_POINT) {
-                    ml.working = add(mult_vec(ir, ml.l->wpos), hmul(ip, v3<R>((R)1 / is.x, (R)1 / is.y, (R)1 / is.z)));  // light.go:186
+                    if (skinned) ml.working = ml.l->wpos;  // light.go:183-184
+                    else ml.working = add(mult_vec(ir, ml.l->wpos), hmul(ip, v3<R>((R)1 / is.x, (R)1 / is.y, (R)1 / is.z)));  // light.go:186
                     if (ml.l->range > 0) {
                         R dist = maxSpan + ml.l->range;
                         if (dist2(modelPos, ml.l->wpos) > dist * dist) ml.skip = true;
@@ -645,7 +771,8 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
             for (auto& ml : mlights) {
                 if (ml.skip) continue;
                 for (int i = 0; i < 3; i++)
-                    vertex_light<R>(F, ml, part, me, modelTransform, dir_rot, vidx[i], S.vlight[vidx[i]]);
+                    vertex_light<R>(F, ml, part, skinned, modelTransform, dir_rot, S.apos[vidx[i]], S.anrm[vidx[i]],
+                                    S.vlight[vidx[i]]);
             }
         }
     }
@@ -683,7 +810,9 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
             if (lighting) { col.r *= S.vlight[v].r; col.g *= S.vlight[v].g; col.b *= S.vlight[v].b; }
             R depthOut = 0;
             if (cd->render_depth || cd->fog_on) {
-                R depth = (c.z + cam.margin) / cam.spread;
+                // camera.go:1760-1765 (RenderDepth) and :1785 (fog)
+                R vz = (cd->render_depth && unbillboarded) ? S.udepth[v] : c.z;
+                R depth = (vz + cam.margin) / cam.spread;
                 if (depth < 0) depth = 0;
                 else if (depth > 1) depth = 1;
                 depthOut = depth;
@@ -790,7 +919,7 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
     for (uint32_t i = 0; i < sc->num_models; i++) {
         const t3d_model_desc& md = sc->models[i];
         if (!md.visible) continue;
-        if (md.frustum_culling && !model_in_frustum(F.cam, F.models[i].transform, F.dims[md.mesh])) {
+        if (md.frustum_culling && !model_in_frustum(F.cam, F.models[i].transform, F.dims[md.mesh], md.skinned != 0)) {
             is_culled[i] = 1;
             culled++;
         }

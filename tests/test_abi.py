@@ -85,7 +85,9 @@ def test_constants_match_the_header():
         "T3D_LV_PER_OBJECT": abi.LV_PER_OBJECT, "T3D_LV_OFF": abi.LV_OFF, "T3D_LIGHT_AMBIENT": abi.LIGHT_AMBIENT,
         "T3D_LIGHT_POINT": abi.LIGHT_POINT, "T3D_LIGHT_DIRECTIONAL": abi.LIGHT_DIRECTIONAL,
         "T3D_LIGHT_VOLUME": abi.LIGHT_VOLUME, "T3D_FOG_ADD": abi.FOG_ADD, "T3D_FOG_SUB": abi.FOG_SUB,
-        "T3D_FOG_OVERWRITE": abi.FOG_OVERWRITE,
+        "T3D_FOG_OVERWRITE": abi.FOG_OVERWRITE, "T3D_BILLBOARD_UP_GLOBAL_Y": abi.BILLBOARD_UP_GLOBAL_Y,
+        "T3D_BILLBOARD_UP_CAMERA_Y": abi.BILLBOARD_UP_CAMERA_Y, "T3D_DEPTH_DEFAULT": abi.DEPTH_DEFAULT,
+        "T3D_DEPTH_UNBILLBOARDED": abi.DEPTH_UNBILLBOARDED,
     }
     for k, v in want.items():
         assert defs.get(k) == v, k

@@ -304,3 +304,98 @@ def test_max_light_count_matches_oracle(ctx, mixed):
             assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), f"keep {keep} mixed {mixed}")
         finally:
             ctx.release(sid)
+
+
+@pytest.mark.parametrize("variant", scenes.FEATURE_CAMERAS)
+def test_skinned_scene_matches_oracle(ctx, variant):
+    """Skinned models (bone blends, a 1.0 weight after a partial one), shape keys on skinned and
+    unskinned meshes, skinned meshes drawn unskinned, under every light and material option."""
+    sd = scenes.skinned_scene(7)
+    cam = scenes.feature_camera(variant)
+    ref = pyoracle.render(sd, cam)
+    assert ref.visible_tris > 0
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), ref, f"skinned/{variant}/mode{mode}")
+    finally:
+        ctx.release(sid)
+
+
+def test_bones_and_shape_weights_between_frames(ctx):
+    """New bone influences (all, then a sub-range) and shape-key weights between frames."""
+    sd = scenes.skinned_scene(8)
+    cam = scenes.feature_camera("persp")
+    nskin = int(sd.mv["skinned"].sum())
+    rng = np.random.default_rng(11)
+    pos = sd.mv["position"][:nskin, :3]
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), "initial")
+        sd.bones = scenes.tube_bones(rng, nskin, pos, bend=0.9)
+        ctx.set_bones(sid, sd.bones)
+        sd.meshes[3].shape_weights = np.array([0.2, 0.9], np.float32)
+        ctx.set_shape_weights(sid, 3, sd.meshes[3].shape_weights)
+        ctx.render(sid, cam)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), "new bones and weights")
+        part = scenes.tube_bones(rng, 2, pos[2:4], bend=1.2)
+        sd.bones = sd.bones.copy()
+        sd.bones[8:16] = part
+        ctx.set_bones(sid, part, first=8)
+        sd.meshes[2].shape_weights = np.array([-0.4], np.float32)
+        ctx.set_shape_weights(sid, 2, sd.meshes[2].shape_weights)
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), f"bone range, mode{mode}")
+    finally:
+        ctx.release(sid)
+
+
+def test_skinning_argument_errors(ctx):
+    lib = ctx.lib
+    sd = scenes.skinned_scene(7)
+    out = C.c_uint32()
+    bad = scenes.skinned_scene(7)
+    bad.mv["bone_first"][3] = bad.bones.shape[0] - 2  # joints 2, 3 past the last bone
+    d = bad.desc()
+    assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+    assert b"bone" in lib.t3d_last_error(ctx.h)
+    bad = scenes.skinned_scene(7)
+    bad.mv["skinned"][20] = 1
+    bad.mv["mesh"][20] = 4  # the cube has no joints
+    d = bad.desc()
+    assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+    sid = ctx.upload(sd)
+    try:
+        b = np.zeros((3, 16), np.float32)
+        nb = sd.bones.shape[0]
+        assert lib.t3d_scene_set_bones(ctx.h, sid, nb - 2, abi.fptr(b), 3) == abi.T3D_E_INVAL
+        w = np.zeros(3, np.float32)
+        assert lib.t3d_scene_set_shape_weights(ctx.h, sid, 3, abi.fptr(w), 3) == abi.T3D_E_INVAL
+        assert lib.t3d_scene_set_shape_weights(ctx.h, sid, 9, abi.fptr(w), 2) == abi.T3D_E_INVAL
+        m = (abi.ModelDesc * 1)(sd.models[5])
+        m[0].bone_first = nb
+        assert lib.t3d_scene_set_models(ctx.h, sid, 5, m, 1) == abi.T3D_E_INVAL
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), "after errors")
+    finally:
+        ctx.release(sid)
+
+
+@pytest.mark.parametrize("variant", scenes.FEATURE_CAMERAS + ["down"])
+def test_billboard_scene_matches_oracle(ctx, variant):
+    """Billboarded parts under every lock / up direction / depth mode, a LookAt straight up
+    (the `down` camera), a billboard material on a skinned model, in both forms."""
+    sd = scenes.billboard_scene(9)
+    cam = scenes.down_camera() if variant == "down" else scenes.feature_camera(variant)
+    ref = pyoracle.render(sd, cam)
+    assert ref.visible_tris > 0
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), ref, f"billboards/{variant}/mode{mode}")
+    finally:
+        ctx.release(sid)

@@ -64,6 +64,8 @@ def _noalloc(lib, sd, torch):
     for k, v in part["mat"].items():
         if k == "color":
             a.mat.color[:] = [float(c) for c in v]
+        elif k == "billboard_lock":
+            a.mat.billboard_lock[:] = [int(c) for c in v]
         else:
             setattr(a.mat, k, v)
     torch.cuda.synchronize()
@@ -89,10 +91,13 @@ def _grid_scene(seed):
     return sd
 
 
-@pytest.mark.parametrize("which", ["uv_sphere", "grid"])
+@pytest.mark.parametrize("which", ["uv_sphere", "grid", "billboard"])
 def test_noalloc_matches_context_api_twice(ctx, which):
     torch = pytest.importorskip("torch")
-    sd = scenes.uv_sphere_scene(5) if which == "uv_sphere" else _grid_scene(6)
+    sd = scenes.uv_sphere_scene(5) if which != "grid" else _grid_scene(6)
+    if which == "billboard":  # the turned part runs the kernel's altered-vertex loop
+        sd.meshes[0].parts[0]["mat"].update(billboard=1, billboard_lock=(0, 1, 0),
+                                             billboard_depth=abi.DEPTH_UNBILLBOARDED)
     ref = _reference(ctx, sd, sd.meshes[0])
     assert ref[0].shape[0] > 0
     for call in range(2):

@@ -26,6 +26,8 @@ LIGHTING_DEFAULT, LIGHTING_FIXED_NORMALS, LIGHTING_DOUBLE_SIDED = 0, 1, 2
 LV_PER_VERTEX, LV_PER_VERTEX_WITH_NORMAL, LV_PER_OBJECT, LV_OFF = 0, 1, 2, 3
 LIGHT_AMBIENT, LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_VOLUME = 0, 1, 2, 3
 FOG_ADD, FOG_SUB, FOG_OVERWRITE = 0, 1, 2
+BILLBOARD_UP_GLOBAL_Y, BILLBOARD_UP_CAMERA_Y = 0, 1
+DEPTH_DEFAULT, DEPTH_UNBILLBOARDED = 0, 1
 MODE_PLAIN, MODE_BATCHED = 0, 1
 
 f32p = C.POINTER(C.c_float)
@@ -37,7 +39,8 @@ class Material(C.Structure):
                 ("present", C.c_int32), ("backface_culling", C.c_int32), ("sort_mode", C.c_int32),
                 ("lighting_mode", C.c_int32), ("lv_shading_mode", C.c_int32), ("shadeless", C.c_int32),
                 ("visible", C.c_int32), ("transparency_mode", C.c_int32), ("blend_source_over", C.c_int32),
-                ("render_order", C.c_int32)]
+                ("render_order", C.c_int32), ("billboard", C.c_int32), ("billboard_lock", C.c_int32 * 3),
+                ("billboard_up", C.c_int32), ("billboard_depth", C.c_int32)]
 
 
 class PartDesc(C.Structure):
@@ -48,7 +51,9 @@ class MeshDesc(C.Structure):
     _fields_ = [("positions", f32p), ("normals", f32p), ("uvs", f32p), ("colors", f32p),
                 ("indices", u32p), ("parts", C.POINTER(PartDesc)),
                 ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32), ("num_parts", C.c_uint32),
-                ("has_dimensions", C.c_int32), ("dim_min", C.c_float * 3), ("dim_max", C.c_float * 3)]
+                ("has_dimensions", C.c_int32), ("dim_min", C.c_float * 3), ("dim_max", C.c_float * 3),
+                ("shape_positions", f32p), ("shape_normals", f32p), ("shape_weights", f32p),
+                ("num_shape_keys", C.c_uint32), ("reserved", C.c_uint32), ("joints", u32p), ("weights", f32p)]
 
 
 class ModelDesc(C.Structure):
@@ -56,7 +61,7 @@ class ModelDesc(C.Structure):
                 ("shadeless", C.c_int32), ("light_list", C.c_int32), ("use_trs", C.c_int32),
                 ("color", C.c_float * 4), ("transform", C.c_float * 16), ("world_rotation", C.c_float * 16),
                 ("position", C.c_float * 3), ("scale", C.c_float * 3), ("rotation", C.c_float * 16),
-                ("rotate_step", C.c_float * 16)]
+                ("rotate_step", C.c_float * 16), ("skinned", C.c_int32), ("bone_first", C.c_uint32)]
 
 
 class LightDesc(C.Structure):
@@ -72,7 +77,8 @@ class SceneDesc(C.Structure):
                 ("lights", C.POINTER(LightDesc)), ("volume_cells", f32p),
                 ("list_offsets", u32p), ("list_items", u32p),
                 ("num_meshes", C.c_uint32), ("num_models", C.c_uint32), ("num_lights", C.c_uint32),
-                ("num_volume_cells", C.c_uint32), ("num_lists", C.c_uint32), ("reserved", C.c_uint32)]
+                ("num_volume_cells", C.c_uint32), ("num_lists", C.c_uint32), ("num_bones", C.c_uint32),
+                ("bones", f32p)]
 
 
 class CameraDesc(C.Structure):
@@ -143,6 +149,8 @@ SIGNATURES = {
     "t3d_scene_set_models": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.POINTER(ModelDesc), C.c_uint32]),
     "t3d_scene_get_transforms": (C.c_int, [_VP, C.c_uint32, f32p, C.c_uint32]),
     "t3d_scene_bytes": (C.c_int, [_VP, C.c_uint32, C.POINTER(C.c_uint64)]),
+    "t3d_scene_set_bones": (C.c_int, [_VP, C.c_uint32, C.c_uint32, f32p, C.c_uint32]),
+    "t3d_scene_set_shape_weights": (C.c_int, [_VP, C.c_uint32, C.c_uint32, f32p, C.c_uint32]),
     "t3d_render": (C.c_int, [_VP, C.c_uint32, C.POINTER(CameraDesc), C.c_int, C.c_int, _VP]),
     "t3d_render_jobs": (C.c_int, [_VP, C.POINTER(JobDesc), C.c_uint32, C.c_int, C.c_int, _VP]),
     "t3d_frame_sync": (C.c_int, [_VP, C.POINTER(Stats)]),

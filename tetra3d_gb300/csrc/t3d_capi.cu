@@ -89,7 +89,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     drop_graph(ctx);
     for (auto& kv : ctx->scenes) kv.second->release();
     ctx->scenes.clear();
-    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum})
         b->release();
@@ -162,11 +162,18 @@ int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d
         set_err(ctx, "set_models: range [%u, %u) beyond %zu models", first, first + n, sc->models.size());
         return T3D_E_INVAL;
     }
-    for (uint32_t i = 0; i < n; i++)
+    for (uint32_t i = 0; i < n; i++) {
         if (models[i].mesh >= sc->meshes.size() || models[i].light_list >= (int32_t)sc->lists.size()) {
             set_err(ctx, "set_models: model %u has a bad mesh or light list", first + i);
             return T3D_E_INVAL;
         }
+        const SceneMesh& me = sc->meshes[models[i].mesh];
+        if (models[i].skinned && (!me.skin || (uint64_t)models[i].bone_first + me.max_joint >= sc->num_bones)) {
+            set_err(ctx, "set_models: skinned model %u without joints or with bones beyond the scene's %u", first + i,
+                    sc->num_bones);
+            return T3D_E_INVAL;
+        }
+    }
     cudaSetDevice(ctx->device);
     if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
     return scene_write_models(ctx, sc, first, models, n);
@@ -192,6 +199,38 @@ int t3d_scene_get_transforms(t3d_ctx* ctx, uint32_t scene, float* out, uint32_t 
             memcpy(out + 16 * (size_t)i, m.transform, 64);
         }
     }
+    return T3D_OK;
+}
+
+int t3d_scene_set_bones(t3d_ctx* ctx, uint32_t scene, uint32_t first, const float* influences, uint32_t n) {
+    if (!ctx || (n && !influences)) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    Scene* sc = it->second.get();
+    if ((uint64_t)first + n > sc->num_bones) {
+        set_err(ctx, "set_bones: range [%u, %u) beyond %u bones", first, first + n, sc->num_bones);
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    if (n) CKR(cudaMemcpy((char*)sc->bones.ptr + 64ull * first, influences, 64ull * n, cudaMemcpyHostToDevice));
+    return T3D_OK;
+}
+
+int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, const float* weights, uint32_t n) {
+    if (!ctx || (n && !weights)) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    Scene* sc = it->second.get();
+    if (mesh >= sc->meshes.size() || n != sc->meshes[mesh].nkeys) {
+        set_err(ctx, "set_shape_weights: mesh %u out of range or %u weights for its shape keys", mesh, n);
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    if (n)
+        CKR(cudaMemcpy((float*)sc->shape_w.ptr + sc->meshes[mesh].weight_first, weights, 4ull * n,
+                       cudaMemcpyHostToDevice));
     return T3D_OK;
 }
 
@@ -303,7 +342,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.algorithmic_bytes += 108ull * s.visible_tris;
     s.launches = ctx->launches;
     size_t scratch = 0;
-    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->vxyuv, &ctx->vrgba,
+    for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
         scratch += b->cap;
     s.scratch_bytes = scratch;

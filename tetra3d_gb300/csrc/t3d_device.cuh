@@ -32,6 +32,16 @@ enum : uint32_t {
     SEG_MULTI = 1u << 5,        // segment spans more than one tile
     SEG_WIDE = 1u << 6,         // vertex range above 65536: local vertex offsets do not fit 16 bits
     SEG_TRANSPARENT = 1u << 7,  // drawn in the transparent pass (no depth composite when rasterised)
+    SEG_SKINNED = 1u << 14,     // Model.skinned: world-space skinned vertices (records in valt)
+    SEG_SHAPES = 1u << 15,      // the mesh has shape keys
+    SEG_BILLBOARD = 1u << 16,   // Material.BillboardEnabled on an unskinned model
+    SEG_BB_LOCKX = 1u << 17,    // BillboardLockX
+    SEG_BB_LOCKY = 1u << 18,    // BillboardLockY
+    SEG_BB_LOCKZ = 1u << 19,    // BillboardLockZ
+    SEG_BB_CAMUP = 1u << 20,    // BillboardUpDirection == BillboardYUpCameraY
+    SEG_UNBB = 1u << 21,        // BillboardedDepthMode == DepthModeUnbillboarded on a billboard
+    // parts whose vertex records need more than the plain loop (their own loop, queue 5)
+    SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD,
 };
 constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }
@@ -39,13 +49,17 @@ __host__ __device__ inline uint32_t seg_light_mode(uint32_t f) { return (f >> 10
 __host__ __device__ inline uint32_t seg_lv_mode(uint32_t f) { return (f >> 12) & 3u; }
 
 // model flags
-enum : int32_t { MOD_VISIBLE = 1, MOD_FRUSTUM = 2, MOD_SHADELESS = 4, MOD_TRS = 8 };
+enum : int32_t { MOD_VISIBLE = 1, MOD_FRUSTUM = 2, MOD_SHADELESS = 4, MOD_TRS = 8, MOD_SKINNED = 16 };
 
 struct DevMesh {
     uint32_t vbase;      // first vertex in the scene pool
     uint32_t tbase;      // first triangle in the scene pool
     uint32_t nverts, ntris;
     float dmin[3], dmax[3];  // Mesh.Dimensions
+    uint32_t shape_first;    // key k, vertex v: shape pool entry shape_first + k * nverts + v
+    uint32_t nkeys;          // shape keys
+    uint32_t weight_first;   // key k's weight: shape_w[weight_first + k]
+    uint32_t pad;
 };
 
 // Resident, animatable model state.
@@ -59,7 +73,8 @@ struct DevModel {
     float color[4];
     uint32_t mesh;
     int32_t flags;
-    uint32_t pad[2];
+    uint32_t bone_first;    // skinned: the mesh's joint j uses bone bone_first + j
+    uint32_t pad;
 };
 
 // A light as one job sees it: beginRender results plus LightVolume geometry.
@@ -101,6 +116,12 @@ struct DevJob {
     DevModel* models;
     const float* cells;
     const DevLight* lights;
+    const float4* shape_a;  // per (key, vertex): position delta xyz, normal delta x
+    const float4* shape_b;  // per (key, vertex): normal delta y, z
+    const float* shape_w;   // key weights
+    const uint4* vjoint;    // per pool vertex: four joints (skinned meshes)
+    const float4* vweight;  // per pool vertex: their weights
+    const float4* bones;    // 4 rows per bone: Node.boneInfluence
 };
 
 // One (job, model) pair.
@@ -184,6 +205,7 @@ struct FrameParams {
     float4* vcull;                // per-vertex records: (cx, cy, clipZ, depth)
     float4* vxyuv;                // emitted screen position + UV
     float4* vrgba;                // emitted colour
+    float4* valt;                 // skinned pairs: world-space skinned position per record (depth key)
     // per multi-tile tile, tile_tris entries in blockDim/32 regions (one per warp of the
     // triangle phase, tile_tris/(blockDim/32) entries each, filled from the front)
     uint16_t* vis_idx;            // triangle within the tile (SEG_WIDE only)
@@ -204,9 +226,11 @@ struct FrameParams {
     uint32_t inst_begin, inst_end;
     uint32_t seg_begin, seg_end;
     uint32_t tile_begin, tile_end;
+    uint32_t tile_alt;                  // tiles of skinned parts: [tile_alt, tile_end)
     uint32_t mt_tile_begin, mt_tile_end;
     uint32_t mt_seg_begin, mt_seg_end;
     uint32_t vitem_begin, vitem_end;
+    uint32_t vitem_alt;                 // vertex items of shape-keyed or skinned parts: [vitem_alt, vitem_end)
     uint32_t tile_tris;           // triangles per tile
     uint32_t vchunk;              // vertices per vertex work item
     uint32_t has_multi;           // any multi-tile segment in range

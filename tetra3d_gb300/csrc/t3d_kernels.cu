@@ -98,12 +98,15 @@ __device__ __forceinline__ float clampf(float v, float lo, float hi) {  // math3
 
 // ------------------------------------------------------------------ P0 ----
 // Camera.SphereInFrustum (camera.go:933-983) on the frustum sphere that
-// Model.onTransformUpdate derives from the transform (model.go:142-182).
-__device__ bool model_in_frustum(const JobCam& c, const m4& M, const DevMesh& me) {
+// Model.onTransformUpdate derives from the transform (model.go:142-182); a
+// skinned model's sphere is centred on its position (model.go:158-161).
+__device__ bool model_in_frustum(const JobCam& c, const m4& M, const DevMesh& me, bool skinned) {
     f3 position, scale;
     m4 rotation;
     decompose(M, position, scale, rotation);
-    f3 center = mk3((me.dmax[0] + me.dmin[0]) / 2.0f, (me.dmax[1] + me.dmin[1]) / 2.0f, (me.dmax[2] + me.dmin[2]) / 2.0f);
+    f3 center = mk3(0.0f, 0.0f, 0.0f);
+    if (!skinned)
+        center = mk3((me.dmax[0] + me.dmin[0]) / 2.0f, (me.dmax[1] + me.dmin[1]) / 2.0f, (me.dmax[2] + me.dmin[2]) / 2.0f);
     center = mult_vec(rotation, center);
     position.x += center.x * scale.x;
     position.y += center.y * scale.y;
@@ -168,18 +171,22 @@ __device__ __noinline__ void phase_prep(const FrameParams& P) {
         }
         DevPrep& pr = P.preps[i];
         const JobCam& cam = J.cam;
+        const bool skinned = md->flags & MOD_SKINNED;
         m4 vp = load16(cam.vp);
-        store16(mult(M, vp), pr.mvp);  // model.go:695
+        // skinned vertices are already in world space: VP alone, and the depth
+        // key is measured from the world camera position (model.go:760-770, :941-946)
+        store16(skinned ? vp : mult(M, vp), pr.mvp);  // model.go:695
         store16(M, pr.M);
         InvFrame inv = inv_frame(M);   // model.go:629
-        f3 ic = to_model_space(inv, mk3(cam.pos[0], cam.pos[1], cam.pos[2]));  // model.go:630
+        f3 ic = skinned ? mk3(cam.pos[0], cam.pos[1], cam.pos[2])
+                        : to_model_space(inv, mk3(cam.pos[0], cam.pos[1], cam.pos[2]));  // model.go:630
         pr.invcam[0] = ic.x; pr.invcam[1] = ic.y; pr.invcam[2] = ic.z; pr.invcam[3] = 0.0f;
         for (int r = 0; r < 4; r++)
             for (int c = 0; c < 3; c++) pr.inv_r[4 * r + c] = inv.r.m[r][c];
         const f3 off = hmul3(inv.p, inv.inv_s);
         pr.inv_r[3] = off.x; pr.inv_r[7] = off.y; pr.inv_r[11] = off.z; pr.inv_r[15] = 0.0f;
         store16(transposed(inverted(WR)), pr.dirrot);  // light.go:326-330
-        bool culled = (md->flags & MOD_FRUSTUM) && !model_in_frustum(cam, M, me);
+        bool culled = (md->flags & MOD_FRUSTUM) && !model_in_frustum(cam, M, me, skinned);
         pr.culled = culled ? 1u : 0u;
         if (culled) {
             atomicAdd(&P.ctl->culled, 1u);
@@ -233,6 +240,8 @@ __device__ __forceinline__ f3 mult_vec_s(const float* m, f3 v) {
 
 // One light's contribution to one vertex (ILight.VertexLight, light.go:115-663).
 // M (model transform) and dirrot (workingModelRotation) live in shared memory.
+// For a skinned model vpos and vnrm are already in world space (light.go:334-343, :613-620).
+template <bool kSkin>
 __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3 vpos, f3 vnrm, const float* M,
                                              const float* dirrot, const float* __restrict__ cells, float& r, float& g,
                                              float& b) {
@@ -268,7 +277,9 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
     }
     case T3D_LIGHT_DIRECTIONAL: {
         f3 fwd = mk3(L.x, L.y, L.z);
-        f3 normal = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? fwd : mult_vec_s(dirrot, vnrm);
+        f3 normal = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? fwd
+                    : (kSkin && (flags & SEG_SKINNED))             ? vnrm
+                                                                   : mult_vec_s(dirrot, vnrm);
         float df = dot3(normal, fwd);
         if (mat && lmode == T3D_LIGHTING_DOUBLE_SIDED) df = fabsf(df);
         if (df <= 0.0f) return;
@@ -292,8 +303,14 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
             f3 cs = mk3(G.cell[0] / 2.0f, G.cell[1] / 2.0f, G.cell[2] / 2.0f);
             f3 bias = mk3(G.bias[0], G.bias[1], G.bias[2]);
             f3 vertPos = mk3(0.f, 0.f, 0.f), vertPosN = mk3(0.f, 0.f, 0.f);
-            if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) vertPosN = add3(mult_vec_s(M, add3(vpos, hmul3(vnrm, cs))), bias);
-            else vertPos = add3(mult_vec_s(M, vpos), bias);
+            if (kSkin && (flags & SEG_SKINNED)) {  // the zero vertPos plus the scaled normal (light.go:614-619)
+                if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) vertPosN = add3(add3(vertPos, hmul3(vnrm, cs)), bias);
+                else vertPos = add3(vpos, bias);
+            } else if (mode == T3D_LV_PER_VERTEX_WITH_NORMAL) {
+                vertPosN = add3(mult_vec_s(M, add3(vpos, hmul3(vnrm, cs))), bias);
+            } else {
+                vertPos = add3(mult_vec_s(M, vpos), bias);
+            }
             if (!(vertPos.x >= G.vmin[0] && vertPos.y >= G.vmin[1] && vertPos.z >= G.vmin[2] && vertPos.x <= G.vmax[0] &&
                   vertPos.y <= G.vmax[1] && vertPos.z <= G.vmax[2]))
                 return;
@@ -317,7 +334,7 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
 //   ModelSmem | TileSmem | whist[nwarps][kBins] | lidx u16[T] | depth f32[T] | bin u16[T]
 // Per work item constants of the emit path (camera, segment and stream bases).
 enum : uint32_t { EC_PERSP = 1, EC_PCORRECT = 2, EC_DEPTH = 4, EC_RDEPTH = 8, EC_FOG_ADD = 16, EC_FOG_SUB = 32,
-                  EC_LIT = 64, EC_COLORS = 128 };
+                  EC_LIT = 64, EC_COLORS = 128, EC_UNBB = 256 };
 struct EmitConst {
     float W, H, halfW, halfH;
     float margin, spread, tex_w, tex_h;
@@ -325,6 +342,7 @@ struct EmitConst {
     float fog0, fogspan, fog_r, fog_g;
     float fog_b;
     uint32_t flags, seg_flags, pad;
+    float uz[4];             // EC_UNBB: depth row of the unbillboarded MVP (model.go:700-803)
     const float4* va;        // vertex streams of the mesh (mesh vertex 0)
     const float4* vb;
     const float4* vc;
@@ -381,12 +399,16 @@ __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t 
 // Stages the model's matrices and (if lit) its light list in shared memory;
 // each thread runs ILight.beginModel for one light (light.go:175-189) and the
 // model-level point-range skip (camera.go:1625-1629).
+template <bool kSkin>
 __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJob& J, ModelSmem& ms) {
     const DevPrep& pr = P.preps[seg.inst];
     const DevInst& in = P.insts[seg.inst];
     float* mvpc = reinterpret_cast<float*>(ms.mvpc);
+    const bool bb = kSkin && (seg.flags & SEG_BILLBOARD);
     for (uint32_t k = threadIdx.x; k < 48; k += blockDim.x) {
-        if (k < 16) mvpc[4 * (k & 3) + (k >> 2)] = pr.mvp[k];
+        if (k < 16) {
+            if (!bb) mvpc[4 * (k & 3) + (k >> 2)] = pr.mvp[k];
+        }
         else if (k < 32) ms.M[k - 16] = pr.M[k - 16];
         else ms.dirrot[k - 32] = pr.dirrot[k - 32];
     }
@@ -410,6 +432,19 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
         if (!cam.render_depth && cam.fog_on && cam.fog_mode == T3D_FOG_SUB) f |= EC_FOG_SUB;
         if (seg.flags & SEG_LIT) f |= EC_LIT;
         if (seg.flags & SEG_COLORS) f |= EC_COLORS;
+        if (bb) {  // billboarded MVP of this part (model.go:634-695)
+            const m4 base = billboard_base(load16(pr.M), mk3(cam.pos[0], cam.pos[1], cam.pos[2]),
+                                           (seg.flags & SEG_BB_CAMUP) ? mk3(cam.up[0], cam.up[1], cam.up[2])
+                                                                      : mk3(0.f, 1.f, 0.f),
+                                           seg.flags & SEG_BB_LOCKX, seg.flags & SEG_BB_LOCKY, seg.flags & SEG_BB_LOCKZ);
+            const m4 mvp = mult(base, load16(cam.vp));
+            for (int r = 0; r < 4; r++)
+                for (int c = 0; c < 4; c++) mvpc[4 * c + r] = mvp.m[r][c];
+            if ((seg.flags & SEG_UNBB) && cam.render_depth) {
+                f |= EC_UNBB;
+                for (int r = 0; r < 4; r++) e.uz[r] = pr.mvp[4 * r + 2];
+            }
+        }
         e.flags = f;
         e.seg_flags = seg.flags;
         e.va = J.va + me.vbase;
@@ -428,6 +463,7 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
             const f3 q = mk3(r[0] * lp.x + r[4] * lp.y + r[8] * lp.z + r[12], r[1] * lp.x + r[5] * lp.y + r[9] * lp.z + r[13],
                              r[2] * lp.x + r[6] * lp.y + r[10] * lp.z + r[14]);
             w.x = q.x + r[3]; w.y = q.y + r[7]; w.z = q.z + r[11];
+            if (kSkin && (seg.flags & SEG_SKINNED)) { w.x = lp.x; w.y = lp.y; w.z = lp.z; }  // light.go:183-184
             if (L.range > 0.0f) {
                 const float dist = pr.maxspan + L.range;
                 if (dist2(mk3(pr.M[12], pr.M[13], pr.M[14]), lp) > dist * dist) w.w = 1.0f;
@@ -488,6 +524,7 @@ __device__ __forceinline__ float4 clip_of(const float4* mc, float x, float y, fl
 //   rgba  = vertex colour * model/material colour * light (camera.go:1726-1742)
 // Every value depends only on the vertex, the model, the part and the camera, so
 // computing it once per vertex gives the reference's per-corner values bit for bit.
+template <bool kSkin>
 __device__ __forceinline__ void vertex_record(const ModelSmem& ms, const float4 a, const float4 b, const float4 k,
                                               float4& cull, float4& xyuv, float4& rgba) {
     const EmitConst& e = ms.ec;
@@ -527,12 +564,14 @@ __device__ __forceinline__ void vertex_record(const ModelSmem& ms, const float4 
         float lr = 0.0f, lg = 0.0f, lb = 0.0f;
         const uint32_t nl = ms.nl;
         for (uint32_t k = 0; k < nl; k++)
-            light_vertex(ms.lights[k], e.seg_flags, vert, vnrm, ms.M, ms.dirrot, e.cells, lr, lg, lb);
+            light_vertex<kSkin>(ms.lights[k], e.seg_flags, vert, vnrm, ms.M, ms.dirrot, e.cells, lr, lg, lb);
         cr *= lr; cg *= lg; cb *= lb;
     }
     float depth = 0.0f;
     if (f & EC_DEPTH) {
-        depth = (c.z + e.margin) / e.spread;
+        float vz = c.z;
+        if (kSkin && (f & EC_UNBB)) vz = e.uz[0] * a.x + e.uz[1] * a.y + e.uz[2] * a.z + e.uz[3];
+        depth = (vz + e.margin) / e.spread;
         if (depth < 0.0f) depth = 0.0f;
         else if (depth > 1.0f) depth = 1.0f;
         if (f & (EC_FOG_ADD | EC_FOG_SUB)) {
@@ -731,10 +770,108 @@ __device__ __forceinline__ bool tri_visible(float nearp, float farp, bool backfa
         const float nor = (n0x * n1y) - (n1x * n0y);
         if (nor < 0.0f) return false;
     }
-    // squared distance from the model-space camera to tri.Center (model.go:950-953)
+    // squared distance from the model-space camera to tri.Center (model.go:950-953),
+    // or from the world camera to the skinned centre (model.go:941-946)
     const float ddx = ic.x - ctr.x, ddy = ic.y - ctr.y, ddz = ic.z - ctr.z;
     depth = ddx * ddx + ddy * ddy + ddz * ddz;
     return !(isnan(depth) || isinf(depth));
+}
+
+// Mesh.VertexPositionWithShapeKeys / VertexNormalWithShapeKeys (mesh.go:796-822)
+// and Model.skinVertex (model.go:559-594) for vertex v counted from the part's
+// first vertex; a = (px, py, pz, nx), b = (ny, nz, u, v).
+struct AlterSrc {
+    const float4* sa;     // key k, vertex v: sa[k * nverts + v] = position delta xyz, normal delta x
+    const float4* sb;     // normal delta y, z
+    const float* sw;      // key weights
+    const uint4* vj;      // joints of vertex v
+    const float4* vw;     // their weights
+    const float4* bones;  // the model's bone 0 (4 rows each)
+    uint32_t nkeys, nverts;
+};
+
+__device__ __forceinline__ void alter_vertex(const AlterSrc& ms, uint32_t flags, uint32_t v, float4& a, float4& b) {
+    const uint32_t nk = ms.nkeys;
+    for (uint32_t k = 0; k < nk; k++) {
+        const float w = ms.sw[k];
+        const float4 da = ms.sa[(size_t)k * ms.nverts + v];
+        const float4 db = ms.sb[(size_t)k * ms.nverts + v];
+        a.x += da.x * w; a.y += da.y * w; a.z += da.z * w;
+        a.w += da.w * w; b.x += db.x * w; b.y += db.y * w;
+    }
+    if (flags & SEG_SKINNED) {
+        const uint4 jv = ms.vj[v];
+        const float4 wv = ms.vw[v];
+        const uint32_t js[4] = {jv.x, jv.y, jv.z, jv.w};
+        const float ws[4] = {wv.x, wv.y, wv.z, wv.w};
+        float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0, s2 = s0, s3 = s0;  // skinMatrix.Clear()
+        for (int i = 0; i < 4; i++) {
+            const float w = ws[i];
+            if (w == 0.0f) continue;
+            const float4* B = ms.bones + 4 * (size_t)js[i];
+            const float4 b0 = B[0], b1 = B[1], b2 = B[2], b3 = B[3];
+            if (w == 1.0f) {
+                s0 = b0; s1 = b1; s2 = b2; s3 = b3;
+                break;
+            }
+            // skinMatrix.Add(boneInfluence.Scale(w)), element by element
+            s0.x = s0.x + b0.x * w; s0.y = s0.y + b0.y * w; s0.z = s0.z + b0.z * w; s0.w = s0.w + b0.w * w;
+            s1.x = s1.x + b1.x * w; s1.y = s1.y + b1.y * w; s1.z = s1.z + b1.z * w; s1.w = s1.w + b1.w * w;
+            s2.x = s2.x + b2.x * w; s2.y = s2.y + b2.y * w; s2.z = s2.z + b2.z * w; s2.w = s2.w + b2.w * w;
+            s3.x = s3.x + b3.x * w; s3.y = s3.y + b3.y * w; s3.z = s3.z + b3.z * w; s3.w = s3.w + b3.w * w;
+        }
+        const float px = a.x, py = a.y, pz = a.z, nx = a.w, ny = b.x, nz = b.y;
+        a.x = s0.x * px + s1.x * py + s2.x * pz + s3.x;
+        a.y = s0.y * px + s1.y * py + s2.y * pz + s3.y;
+        a.z = s0.z * px + s1.z * py + s2.z * pz + s3.z;
+        // the normal goes through the same matrix with its last row set to (0, 0, 0, 1)
+        a.w = s0.x * nx + s1.x * ny + s2.x * nz + 0.0f;
+        b.x = s0.y * nx + s1.y * ny + s2.y * nz + 0.0f;
+        b.y = s0.z * nx + s1.z * ny + s2.z * nz + 0.0f;
+    }
+}
+
+// The vertex records of a part whose mesh has shape keys or whose model is
+// skinned; a skinned part also leaves its world-space positions in valt for
+// the triangles' depth keys.
+__device__ __forceinline__ void vertex_chunk_altered(const FrameParams& P, const ModelSmem& ms, const DevSeg& seg,
+                                                     uint32_t v0, uint32_t v1) {
+    const float4* __restrict__ va = ms.ec.va + seg.vmin;
+    const float4* __restrict__ vb = ms.ec.vb + seg.vmin;
+    const float4* __restrict__ vc = ms.ec.vc + seg.vmin;
+    const bool colors = ms.ec.flags & EC_COLORS;
+    const bool skinned = seg.flags & SEG_SKINNED;
+    const DevJob& J = P.jobs[seg.job];
+    const DevMesh& me = J.meshes[seg.mesh];
+    AlterSrc src;
+    src.nkeys = (seg.flags & SEG_SHAPES) ? me.nkeys : 0u;
+    src.nverts = me.nverts;
+    src.sa = J.shape_a + me.shape_first + seg.vmin;
+    src.sb = J.shape_b + me.shape_first + seg.vmin;
+    src.sw = J.shape_w + me.weight_first;
+    src.vj = J.vjoint + me.vbase + seg.vmin;
+    src.vw = J.vweight + me.vbase + seg.vmin;
+    src.bones = J.bones + 4 * (size_t)J.models[P.insts[seg.inst].model].bone_first;
+    for (uint32_t lv = v0 + threadIdx.x; lv < v1; lv += blockDim.x) {
+        float4 a = va[lv], b = vb[lv], k = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (colors) k = vc[lv];
+        alter_vertex(src, seg.flags, lv, a, b);
+        float4 cull, xyuv, rgba;
+        vertex_record<true>(ms, a, b, k, cull, xyuv, rgba);
+        const uint32_t o = seg.vscratch + lv;
+        P.vcull[o] = cull;
+        P.vxyuv[o] = xyuv;
+        P.vrgba[o] = rgba;
+        if (skinned) P.valt[o] = make_float4(a.x, a.y, a.z, 0.0f);
+    }
+}
+
+// The skinned triangle centre, summed from zero over the corners' skinned
+// positions and divided by 3 (model.go:840-863, :941-946).
+__device__ __forceinline__ f3 skinned_centre(const float4* __restrict__ valt, uint32_t i0, uint32_t i1, uint32_t i2) {
+    const float4 p0 = rec_load(&valt[i0]), p1 = rec_load(&valt[i1]), p2 = rec_load(&valt[i2]);
+    return mk3((((0.0f + p0.x) + p1.x) + p2.x) / 3.0f, (((0.0f + p0.y) + p1.y) + p2.y) / 3.0f,
+               (((0.0f + p0.z) + p1.z) + p2.z) / 3.0f);
 }
 
 // PV: per (segment, vertex chunk) the vertex records of every vertex the
@@ -743,13 +880,13 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
     uint32_t item = P.vitem_begin + next_item(P.ctl, 6, s_item);
-    while (item < P.vitem_end) {
+    while (item < P.vitem_alt) {
         // the next item's queue slot is fetched now and read at the end of this one
         const uint32_t s = P.vitem_seg[item];
         const DevSeg seg = P.segs[s];
         if (!((seg.flags & SEG_SKIP) || P.preps[seg.inst].culled)) {
         const DevJob& J = P.jobs[seg.job];
-        stage_model(P, seg, J, ms);
+        stage_model<false>(P, seg, J, ms);
         __syncthreads();
         const uint32_t v0 = P.vitem_chunk[item] * P.vchunk;
         const uint32_t v1 = min(seg.vcount, v0 + P.vchunk);
@@ -775,7 +912,7 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
                 if (colors) nk = vc[nlv];
             }
             float4 cull, xyuv, rgba;
-            vertex_record(ms, a, b, k, cull, xyuv, rgba);
+            vertex_record<false>(ms, a, b, k, cull, xyuv, rgba);
             const uint32_t o = seg.vscratch + lv;
             P.vcull[o] = cull;
             P.vxyuv[o] = xyuv;
@@ -787,6 +924,23 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
         }
         }
         item = P.vitem_begin + next_item(P.ctl, 6, s_item);
+    }
+}
+
+// PV for the vertex items of parts with shape keys or skinning (queue 5).
+__device__ __noinline__ void phase_vertex_altered(const FrameParams& P, unsigned char* smem) {
+    ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
+    uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
+    uint32_t item = P.vitem_alt + next_item(P.ctl, 5, s_item);
+    while (item < P.vitem_end) {
+        const DevSeg seg = P.segs[P.vitem_seg[item]];
+        if (!((seg.flags & SEG_SKIP) || P.preps[seg.inst].culled)) {
+            stage_model<true>(P, seg, P.jobs[seg.job], ms);
+            __syncthreads();
+            const uint32_t v0 = P.vitem_chunk[item] * P.vchunk;
+            vertex_chunk_altered(P, ms, seg, v0, min(seg.vcount, v0 + P.vchunk));
+        }
+        item = P.vitem_alt + next_item(P.ctl, 5, s_item);
     }
 }
 
@@ -806,14 +960,21 @@ __device__ __noinline__ void prefetch_triangle_tile(const FrameParams& P, uint32
 }
 // P1: visibility and depth keys per tile; single-tile segments are sorted and
 // emitted right here, multi-tile segments leave their visible list in HBM.
-__device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char* smem) {
+// Tiles [first, end) from queue q; kSkinned: the tiles of skinned parts, whose
+// depth keys come from the skinned positions.
+template <bool kSkinned>
+__device__ __forceinline__ void triangle_tiles(const FrameParams& P, unsigned char* smem) {
+    // item ranges read from the launch parameters where they are used (no registers held)
+#define T3D_TILE_FIRST (kSkinned ? P.tile_alt : P.tile_begin)
+#define T3D_TILE_END (kSkinned ? P.tile_end : P.tile_alt)
+    constexpr int q = kSkinned ? 7 : 1;
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
     TileSmem& sm = *L.ts;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
-    while (item < P.tile_end) {
-        if (threadIdx.x == blockDim.x - 32 && item + gridDim.x < P.tile_end) prefetch_triangle_tile(P, item + gridDim.x);
+    uint32_t item = T3D_TILE_FIRST + next_item(P.ctl, q, &sm.item);
+    while (item < T3D_TILE_END) {
+        if (threadIdx.x == blockDim.x - 32 && item + gridDim.x < T3D_TILE_END) prefetch_triangle_tile(P, item + gridDim.x);
         // the next item's queue slot is fetched now and read at the end of this one
         const TileDesc td = P.tiles[item];
         const uint32_t s = td.seg;
@@ -832,6 +993,8 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
         const uint32_t* __restrict__ midx = J.idx + 3 * (size_t)td.tbase;
         const float* __restrict__ mctr = J.centers + 3 * (size_t)td.tbase;
         const float4* __restrict__ vcull = P.vcull + td.vscratch;
+        const float4* __restrict__ valt = P.valt + td.vscratch;
+        constexpr bool skinned = kSkinned;
         const uint32_t vm = td.vmin;
         const bool wide = td.flags & SEG_WIDE;
         const uint32_t t0 = td.t0;
@@ -851,11 +1014,13 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
             f3 ca = mk3(0.f, 0.f, 0.f), cb = ca;
             if (ha) {
                 ia0 = midx[3 * ta]; ia1 = midx[3 * ta + 1]; ia2 = midx[3 * ta + 2];
-                ca = mk3(mctr[3 * ta], mctr[3 * ta + 1], mctr[3 * ta + 2]);
+                if (!skinned) ca = mk3(mctr[3 * ta], mctr[3 * ta + 1], mctr[3 * ta + 2]);
+                else ca = skinned_centre(valt, ia0 - vm, ia1 - vm, ia2 - vm);
             }
             if (hb) {
                 ib0 = midx[3 * tb2]; ib1 = midx[3 * tb2 + 1]; ib2 = midx[3 * tb2 + 2];
-                cb = mk3(mctr[3 * tb2], mctr[3 * tb2 + 1], mctr[3 * tb2 + 2]);
+                if (!skinned) cb = mk3(mctr[3 * tb2], mctr[3 * tb2 + 1], mctr[3 * tb2 + 2]);
+                else cb = skinned_centre(valt, ib0 - vm, ib1 - vm, ib2 - vm);
             }
             float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f), pa1 = pa0, pa2 = pa0, pb0 = pa0, pb1 = pa0, pb2 = pa0;
             if (ha) { pa0 = rec_load(&vcull[ia0 - vm]); pa1 = rec_load(&vcull[ia1 - vm]); pa2 = rec_load(&vcull[ia2 - vm]); }
@@ -949,8 +1114,14 @@ __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char
         } else if (multi && threadIdx.x == 0) {
             P.tile_count[mt] = 0u;
         }
-        item = P.tile_begin + next_item(P.ctl, 1, &sm.item);
+        item = T3D_TILE_FIRST + next_item(P.ctl, q, &sm.item);
     }
+#undef T3D_TILE_FIRST
+#undef T3D_TILE_END
+}
+__device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char* smem) { triangle_tiles<false>(P, smem); }
+__device__ __noinline__ void phase_triangles_skinned(const FrameParams& P, unsigned char* smem) {
+    triangle_tiles<true>(P, smem);
 }
 
 // P2: bin histograms of the tiles of multi-tile segments, one warp per tile
@@ -1131,10 +1302,12 @@ __global__ void __launch_bounds__(256, T3D_MIN_BLOCKS) t3d_frame_kernel(const __
     if (!grid_barrier(P.ctl)) return;
     phase_start(since);
     phase_vertex(P, smem);
+    if (P.vitem_alt < P.vitem_end) phase_vertex_altered(P, smem);
     phase_done(P.ctl, 6, since);
     if (!grid_barrier(P.ctl)) return;
     phase_start(since);
     phase_triangles(P, smem);
+    if (P.tile_alt < P.tile_end) phase_triangles_skinned(P, smem);
     phase_done(P.ctl, 1, since);
     if (!P.has_multi) return;
     if (!grid_barrier(P.ctl)) return;

@@ -160,6 +160,64 @@ T3D_HD void decompose(const m4& M, f3& pos, f3& scl, m4& rot) {
     scl = mk3(mag3(row3(in, 0)), mag3(row3(in, 1)), mag3(row3(in, 2)));
 }
 
+// Vector3.Equals (vector.go:415-425): every component within 1e-4.
+T3D_HD bool equals3(f3 a, f3 b) {
+    return !(fabsf(a.x - b.x) > 1e-4f || fabsf(a.y - b.y) > 1e-4f || fabsf(a.z - b.z) > 1e-4f);
+}
+// Vector3.Cross (vector.go:164-175)
+T3D_HD f3 cross3(f3 a, f3 b) { return mk3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
+
+// NewMatrix4LookAt (matrix.go:788-815)
+T3D_HD m4 look_at(f3 from, f3 to, f3 up) {
+    if (equals3(from, to)) return ident();
+    const f3 z = unit3(sub3(to, from));
+    up = unit3(up);
+    if (equals3(z, up) || equals3(z, neg3(up))) up = !equals3(up, mk3(1.f, 0.f, 0.f)) ? mk3(1.f, 0.f, 0.f) : mk3(0.f, 0.f, 1.f);
+    const f3 x = unit3(cross3(up, z));
+    const f3 y = cross3(z, x);
+    m4 r = ident();
+    r.m[0][0] = x.x; r.m[0][1] = x.y; r.m[0][2] = x.z;
+    r.m[1][0] = y.x; r.m[1][1] = y.y; r.m[1][2] = y.z;
+    r.m[2][0] = z.x; r.m[2][1] = z.y; r.m[2][2] = z.z;
+    return r;
+}
+
+// Row i replaced by its Vector4.Unit (xyz over the xyz length, w kept; vector.go:1869-1877).
+T3D_HD void unit_row(m4& a, int i) {
+    const float x = a.m[i][0], y = a.m[i][1], z = a.m[i][2];
+    const float l = sqrt_rn(x * x + y * y + z * z);
+    if (l < 1e-8f || l == 1.0f) return;
+    a.m[i][0] = x / l; a.m[i][1] = y / l; a.m[i][2] = z / l;
+}
+
+// The billboarded model transform of ProcessVertices (model.go:634-688): the
+// LookAt from the model's world position to the camera, with locked axes, put
+// under the model's rotation and scale, at the model's position.
+T3D_HD m4 billboard_base(const m4& M, f3 cam_pos, f3 up, bool lock_x, bool lock_y, bool lock_z) {
+    m4 L = look_at(row3(M, 3), cam_pos, up);
+    if (lock_x) {
+        L.m[0][0] = 1.f; L.m[0][1] = 0.f; L.m[0][2] = 0.f; L.m[0][3] = 0.f;
+        L.m[1][0] = 0.f; unit_row(L, 1);
+        L.m[2][0] = 0.f; unit_row(L, 2);
+    }
+    if (lock_y) {
+        L.m[1][0] = 0.f; L.m[1][1] = 1.f; L.m[1][2] = 0.f; L.m[1][3] = 0.f;
+        L.m[0][1] = 0.f; unit_row(L, 0);
+        L.m[2][1] = 0.f; unit_row(L, 2);
+    }
+    if (lock_z) {
+        L.m[2][0] = 0.f; L.m[2][1] = 0.f; L.m[2][2] = 1.f; L.m[2][3] = 0.f;
+        L.m[0][2] = 0.f; unit_row(L, 0);
+        L.m[1][2] = 0.f; unit_row(L, 1);
+    }
+    f3 p, s;
+    m4 r;
+    decompose(M, p, s, r);
+    m4 base = mult(mult(r, scale_m(s.x, s.y, s.z)), L);
+    base.m[3][0] = p.x; base.m[3][1] = p.y; base.m[3][2] = p.z; base.m[3][3] = 1.f;
+    return base;
+}
+
 // Node.Transform for a parentless node (node.go:583-585): Scale * Rotation * Translate.
 T3D_HD m4 trs(f3 pos, f3 scl, const m4& rot) {
     m4 t = scale_m(scl.x, scl.y, scl.z);

@@ -210,6 +210,10 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
         fail(a, "bad camera size%s");
         return T3D_E_INVAL;
     }
+    if (a->model->skinned) {  // the part's vertices come without joints, weights or bones
+        fail(a, "skinned models need the scene path (t3d_scene_upload)%s");
+        return T3D_E_INVAL;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= 64) {
         fail(a, "bad device%s");
@@ -312,6 +316,7 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     flags |= (uint32_t)(mat.present ? mat.sort_mode & 3 : 0) << 8;
     flags |= (uint32_t)(mat.present ? mat.lighting_mode & 3 : 0) << 10;
     flags |= (uint32_t)(mat.present ? mat.lv_shading_mode & 3 : 0) << 12;
+    flags |= billboard_flags(mat, false);
     sg.flags = flags;
     for (int k = 0; k < 4; k++) sg.mp[k] = mat.present ? md.color[k] * mat.color[k] : md.color[k];
     sg.tex_w = mat.present ? mat.tex_w : 0.0f;
@@ -372,8 +377,8 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     P.accum = (unsigned long long*)(S + O_ACCUM);
     P.inst_begin = 0; P.inst_end = 1;
     P.seg_begin = 0; P.seg_end = 1;
-    P.tile_begin = 0; P.tile_end = ntiles;
-    P.vitem_begin = 0; P.vitem_end = nchunks;
+    P.tile_begin = 0; P.tile_end = ntiles; P.tile_alt = ntiles;
+    P.vitem_begin = 0; P.vitem_end = nchunks; P.vitem_alt = (flags & SEG_ALTERED) ? 0u : nchunks;
     P.mt_tile_begin = 0; P.mt_tile_end = ntiles > 1 ? ntiles : 0;
     P.mt_seg_begin = 0; P.mt_seg_end = ntiles > 1 ? 1 : 0;
     P.tile_tris = kNaTile;

@@ -316,7 +316,8 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         return T3D_E_INVAL;
     }
     auto sc = std::make_unique<Scene>();
-    uint64_t nv = 0, nt = 0;
+    uint64_t nv = 0, nt = 0, nshape = 0, nkeys_total = 0;
+    bool any_skin = false;
     for (uint32_t m = 0; m < d->num_meshes; m++) {
         const t3d_mesh_desc& me = d->meshes[m];
         if (!me.positions || !me.normals || !me.uvs || !me.indices || (me.num_parts && !me.parts)) {
@@ -329,6 +330,27 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         sm.nverts = me.num_vertices;
         sm.ntris = me.num_triangles;
         sm.colors = me.colors != nullptr;
+        if (me.num_shape_keys && (!me.shape_positions || !me.shape_normals || !me.shape_weights)) {
+            set_err(ctx, "mesh %u: shape keys without position, normal or weight arrays", m);
+            return T3D_E_INVAL;
+        }
+        if ((me.joints != nullptr) != (me.weights != nullptr)) {
+            set_err(ctx, "mesh %u: joints and weights must be given together", m);
+            return T3D_E_INVAL;
+        }
+        sm.nkeys = me.num_shape_keys;
+        sm.shape_first = (uint32_t)nshape;
+        sm.weight_first = (uint32_t)nkeys_total;
+        nshape += (uint64_t)me.num_shape_keys * me.num_vertices;
+        nkeys_total += me.num_shape_keys;
+        if (nshape > 0xFFFFFFF0ull) {
+            set_err(ctx, "scene too large: shape key deltas exceed 32-bit indexing");
+            return T3D_E_INVAL;
+        }
+        sm.skin = me.joints != nullptr;
+        any_skin |= sm.skin;
+        if (sm.skin)
+            for (uint64_t q = 0; q < 4ull * me.num_vertices; q++) sm.max_joint = std::max(sm.max_joint, me.joints[q]);
         for (uint32_t t = 0; t < 3ull * me.num_triangles; t++)
             if (me.indices[t] >= me.num_vertices) {
                 set_err(ctx, "mesh %u: index %u out of range (%u vertices)", m, me.indices[t], me.num_vertices);
@@ -389,6 +411,11 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
             set_err(ctx, "model %u: light list %d out of range", i, md.light_list);
             return T3D_E_INVAL;
         }
+        if (md.skinned && (!sc->meshes[md.mesh].skin ||
+                           (uint64_t)md.bone_first + sc->meshes[md.mesh].max_joint >= d->num_bones)) {
+            set_err(ctx, "model %u: skinned without joints or with bones beyond the %u scene bones", i, d->num_bones);
+            return T3D_E_INVAL;
+        }
         SceneModel sm;
         sm.d = md;
         sc->models.push_back(sm);
@@ -427,8 +454,21 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         (rc = sc->idx.ensure(ctx, nt * 12 + 256)) || (rc = sc->centers.ensure(ctx, nt * 12 + 256)) ||
         (rc = sc->dmeshes.ensure(ctx, sizeof(DevMesh) * std::max<size_t>(1, d->num_meshes))) ||
         (rc = sc->dmodels.ensure(ctx, sizeof(DevModel) * std::max<size_t>(1, d->num_models))) ||
-        (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))))
+        (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))) ||
+        (rc = sc->shape_a.ensure(ctx, 16 * std::max<uint64_t>(1, nshape))) ||
+        (rc = sc->shape_b.ensure(ctx, 16 * std::max<uint64_t>(1, nshape))) ||
+        (rc = sc->shape_w.ensure(ctx, 4 * std::max<uint64_t>(1, nkeys_total))) ||
+        (rc = sc->vjoint.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
+        (rc = sc->vweight.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
+        (rc = sc->bones.ensure(ctx, 64 * std::max<size_t>(1, d->num_bones))))
         return rc;
+    if (d->num_bones && !d->bones) {
+        set_err(ctx, "scene_upload: num_bones without bone matrices");
+        return T3D_E_INVAL;
+    }
+    sc->num_bones = d->num_bones;
+    sc->num_keys = (uint32_t)nkeys_total;
+    if (d->num_bones) CK(cudaMemcpy(sc->bones.ptr, d->bones, 64ull * d->num_bones, cudaMemcpyHostToDevice));
     std::vector<float4> a, b, c;
     std::vector<float> ctr;
     for (uint32_t m = 0; m < d->num_meshes; m++) {
@@ -464,6 +504,25 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         CK(cudaMemcpy((char*)sc->centers.ptr + (size_t)sc->meshes[m].tbase * 12, ctr.data(), me.num_triangles * 12ull,
                       cudaMemcpyHostToDevice));
         SceneMesh& smh = sc->meshes[m];
+        if (me.num_shape_keys) {  // deltas as float4 pairs: (px, py, pz, nx), (ny, nz, 0, 0)
+            const size_t ne = (size_t)me.num_shape_keys * me.num_vertices;
+            std::vector<float4> sa(ne), sb(ne);
+            for (size_t q = 0; q < ne; q++) {
+                const float* p = me.shape_positions + 3 * q;
+                const float* nn = me.shape_normals + 3 * q;
+                sa[q] = make_float4(p[0], p[1], p[2], nn[0]);
+                sb[q] = make_float4(nn[1], nn[2], 0.f, 0.f);
+            }
+            CK(cudaMemcpy((float4*)sc->shape_a.ptr + smh.shape_first, sa.data(), 16 * ne, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy((float4*)sc->shape_b.ptr + smh.shape_first, sb.data(), 16 * ne, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy((float*)sc->shape_w.ptr + smh.weight_first, me.shape_weights, 4ull * me.num_shape_keys,
+                          cudaMemcpyHostToDevice));
+        }
+        if (me.joints) {
+            CK(cudaMemcpy((uint4*)sc->vjoint.ptr + smh.vbase, me.joints, 16ull * me.num_vertices, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy((float4*)sc->vweight.ptr + smh.vbase, me.weights, 16ull * me.num_vertices,
+                          cudaMemcpyHostToDevice));
+        }
         const uint32_t nch = (me.num_triangles + kChunkTris - 1) / kChunkTris;
         smh.chunk_lo.assign(nch, 0xFFFFFFFFu);
         smh.chunk_hi.assign(nch, 0u);
@@ -478,6 +537,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     for (uint32_t m = 0; m < d->num_meshes; m++) {
         const SceneMesh& sm = sc->meshes[m];
         dm[m].vbase = sm.vbase; dm[m].tbase = sm.tbase; dm[m].nverts = sm.nverts; dm[m].ntris = sm.ntris;
+        dm[m].shape_first = sm.shape_first; dm[m].nkeys = sm.nkeys; dm[m].weight_first = sm.weight_first; dm[m].pad = 0;
         for (int k = 0; k < 3; k++) { dm[m].dmin[k] = sm.dmin[k]; dm[m].dmax[k] = sm.dmax[k]; }
     }
     if (d->num_meshes) CK(cudaMemcpy(sc->dmeshes.ptr, dm.data(), sizeof(DevMesh) * dm.size(), cudaMemcpyHostToDevice));
@@ -501,7 +561,7 @@ uint64_t next_version() {
 static bool same_model_structure(const t3d_model_desc& a, const t3d_model_desc& b) {
     return a.mesh == b.mesh && a.visible == b.visible && a.frustum_culling == b.frustum_culling &&
            a.shadeless == b.shadeless && a.light_list == b.light_list && a.use_trs == b.use_trs &&
-           memcmp(a.color, b.color, sizeof a.color) == 0;
+           a.skinned == b.skinned && a.bone_first == b.bone_first && memcmp(a.color, b.color, sizeof a.color) == 0;
 }
 
 int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n) {
@@ -525,7 +585,8 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
         memcpy(m.color, md.color, 16);
         m.mesh = md.mesh;
         m.flags = (md.visible ? MOD_VISIBLE : 0) | (md.frustum_culling ? MOD_FRUSTUM : 0) | (md.shadeless ? MOD_SHADELESS : 0) |
-                  (md.use_trs ? MOD_TRS : 0);
+                  (md.use_trs ? MOD_TRS : 0) | (md.skinned ? MOD_SKINNED : 0);
+        m.bone_first = md.bone_first;
         if (!structure && !same_model_structure(sc->models[first + i].d, md)) structure = true;
         sc->models[first + i].d = md;
     }
@@ -539,6 +600,21 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
 
 // ------------------------------------------------------------ frames ----
 // Builds the tables of one frame. Instances and segments are laid out per job.
+void order_altered_items(t3d_ctx* ctx, FrameTables& F);
+
+// Segment flags of a part's billboard options; a skinned model's vertices skip
+// the model matrix, so billboarding does not apply to it (model.go:760-770).
+uint32_t billboard_flags(const t3d_material& mat, bool skinned) {
+    if (!mat.present || !mat.billboard || skinned) return 0u;
+    uint32_t f = SEG_BILLBOARD;
+    if (mat.billboard_lock[0]) f |= SEG_BB_LOCKX;
+    if (mat.billboard_lock[1]) f |= SEG_BB_LOCKY;
+    if (mat.billboard_lock[2]) f |= SEG_BB_LOCKZ;
+    if (mat.billboard_up == T3D_BILLBOARD_UP_CAMERA_Y) f |= SEG_BB_CAMUP;
+    if (mat.billboard_depth == T3D_DEPTH_UNBILLBOARDED) f |= SEG_UNBB;
+    return f;
+}
+
 int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate) {
     FrameTables& F = ctx->tables;
     F.clear();
@@ -567,6 +643,12 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.meshes = (const DevMesh*)sc->dmeshes.ptr;
         dj.models = (DevModel*)sc->dmodels.ptr;
         dj.cells = (const float*)sc->cells.ptr;
+        dj.shape_a = (const float4*)sc->shape_a.ptr;
+        dj.shape_b = (const float4*)sc->shape_b.ptr;
+        dj.shape_w = (const float*)sc->shape_w.ptr;
+        dj.vjoint = (const uint4*)sc->vjoint.ptr;
+        dj.vweight = (const float4*)sc->vweight.ptr;
+        dj.bones = (const float4*)sc->bones.ptr;
         const uint32_t light_base = (uint32_t)F.lights.size();
         for (const auto& l : sc->lights) {
             DevLight L;
@@ -653,6 +735,10 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (mat.present) flags |= SEG_MAT;
             if (part.vcount > kLocalVerts) flags |= SEG_WIDE;
             if (is_transparent(m.d.color, mat)) flags |= SEG_TRANSPARENT;
+            if (m.d.skinned) { flags |= SEG_SKINNED; F.any_skinned = true; }
+            if (me.nkeys) flags |= SEG_SHAPES;
+            flags |= billboard_flags(mat, m.d.skinned != 0);
+            if (flags & SEG_ALTERED) F.any_altered = true;
             uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
             flags |= sort_mode << 8;
             flags |= (uint32_t)(mat.present ? mat.lighting_mode : 0) << 10;
@@ -718,8 +804,52 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         set_err(ctx, "frame too large for 32-bit slots");
         return T3D_E_INVAL;
     }
+    F.tile_alt = (uint32_t)F.tiles.size();
+    F.vitem_alt = (uint32_t)F.vitem_seg.size();
+    if (F.any_altered) order_altered_items(ctx, F);
     // point the jobs at their light tables (device address known after upload)
     return T3D_OK;
+}
+
+// Vertex items of parts with shape keys or skinning, and tiles of skinned
+// parts, move behind the others: the kernel runs them in loops of their own
+// (queues 5 and 7), so the loops of plain parts carry none of their code.
+// Each part's items stay contiguous and in order.
+void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
+    std::vector<TileDesc> tiles;
+    std::vector<uint32_t> vseg, vch;
+    tiles.reserve(F.tiles.size());
+    vseg.reserve(F.vitem_seg.size());
+    vch.reserve(F.vitem_chunk.size());
+    const uint32_t nseg = (uint32_t)F.segs.size();
+    std::vector<uint32_t> new_tile(nseg), new_vitem(nseg);
+    for (int pass = 0; pass < 2; pass++) {
+        for (uint32_t s = 0; s < nseg; s++) {
+            const DevSeg& sg = F.segs[s];
+            if (((sg.flags & SEG_SKINNED) != 0) == (pass == 1)) {
+                new_tile[s] = (uint32_t)tiles.size();
+                tiles.insert(tiles.end(), F.tiles.begin() + sg.tile_first, F.tiles.begin() + sg.tile_first + sg.ntiles);
+            }
+            if (((sg.flags & SEG_ALTERED) != 0) == (pass == 1)) {
+                const uint32_t nch = (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
+                const uint32_t f = F.seg_vitem_first[s];
+                new_vitem[s] = (uint32_t)vseg.size();
+                vseg.insert(vseg.end(), F.vitem_seg.begin() + f, F.vitem_seg.begin() + f + nch);
+                vch.insert(vch.end(), F.vitem_chunk.begin() + f, F.vitem_chunk.begin() + f + nch);
+            }
+        }
+        if (pass == 0) {
+            F.tile_alt = (uint32_t)tiles.size();
+            F.vitem_alt = (uint32_t)vseg.size();
+        }
+    }
+    for (uint32_t s = 0; s < nseg; s++) {
+        F.segs[s].tile_first = new_tile[s];
+        F.seg_vitem_first[s] = new_vitem[s];
+    }
+    F.tiles.swap(tiles);
+    F.vitem_seg.swap(vseg);
+    F.vitem_chunk.swap(vch);
 }
 
 template <typename T> static size_t bytes_of(const std::vector<T>& v) { return v.size() * sizeof(T); }
@@ -787,7 +917,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     const size_t nsc = std::max<uint64_t>(1, F.nscratch);
     const size_t nslots = std::max<uint64_t>(1, F.nslots);
     if ((rc = ctx->preps.ensure(ctx, sizeof(DevPrep) * ninst)) ||
-(rc = ctx->vcull.ensure(ctx, 16 * nsc)) ||
+(rc = ctx->vcull.ensure(ctx, 16 * nsc)) || (rc = ctx->valt.ensure(ctx, 16 * (F.any_skinned ? nsc : 1))) ||
         (rc = ctx->vxyuv.ensure(ctx, 16 * nsc)) || (rc = ctx->vrgba.ensure(ctx, 16 * nsc)) ||
         (rc = ctx->vis_idx.ensure(ctx, 2ull * nmt * ctx->tile_tris)) ||
         (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) ||
@@ -800,6 +930,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.preps = (DevPrep*)ctx->preps.ptr;
 
     P.vcull = (float4*)ctx->vcull.ptr;
+    P.valt = (float4*)ctx->valt.ptr;
     P.vxyuv = (float4*)ctx->vxyuv.ptr;
     P.vrgba = (float4*)ctx->vrgba.ptr;
     P.vis_idx = (uint16_t*)ctx->vis_idx.ptr;
@@ -867,6 +998,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
 
         P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
+        P.tile_alt = F.tile_alt; P.vitem_alt = F.vitem_alt;
         P.has_multi = F.mt_segs.empty() ? 0u : 1u;
         uint32_t items = (uint32_t)std::max({F.tiles.size(), F.mt_desc.size(), F.vitem_seg.size(),
                                              (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
@@ -883,7 +1015,9 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.seg_begin = (uint32_t)s; P.seg_end = (uint32_t)s + 1;
         P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
         P.vitem_begin = F.seg_vitem_first[s];
-        P.vitem_end = (s + 1 < F.segs.size()) ? F.seg_vitem_first[s + 1] : (uint32_t)F.vitem_seg.size();
+        P.vitem_end = P.vitem_begin + (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
+        P.tile_alt = (sg.flags & SEG_SKINNED) ? P.tile_begin : P.tile_end;
+        P.vitem_alt = (sg.flags & SEG_ALTERED) ? P.vitem_begin : P.vitem_end;
         if (sg.flags & SEG_MULTI) {
             P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles;
             P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;

@@ -38,6 +38,9 @@ struct SceneMesh {
     std::vector<ScenePart> parts;
     // per kChunkTris triangles: smallest and largest vertex index they use (prefetch ranges)
     std::vector<uint32_t> chunk_lo, chunk_hi;
+    uint32_t nkeys = 0, shape_first = 0, weight_first = 0;  // shape keys
+    bool skin = false;                                      // joints and weights present
+    uint32_t max_joint = 0;
 };
 struct SceneModel {
     t3d_model_desc d;  // host mirror (rotation advanced with every animated frame)
@@ -52,10 +55,14 @@ struct Scene {
     // tables are built from except transforms; model_ver with any model write
     uint64_t struct_ver = 0, model_ver = 0;
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
+    DevBuf shape_a, shape_b, shape_w, vjoint, vweight, bones;
+    uint32_t num_bones = 0, num_keys = 0;
     uint64_t device_bytes() const {
-        return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap;
+        return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap +
+               shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap;
     }
     void release() {
+        shape_a.release(); shape_b.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
         va.release(); vb.release(); vc.release(); idx.release(); centers.release();
         dmeshes.release(); dmodels.release(); cells.release();
     }
@@ -76,12 +83,14 @@ struct FrameTables {
     std::vector<uint32_t> mt_segs;
     std::vector<uint32_t> vitem_seg, vitem_chunk, seg_vitem_first;
     uint64_t nscratch = 0, nslots = 0;
+    bool any_skinned = false, any_altered = false;
+    uint32_t tile_alt = 0, vitem_alt = 0;  // first tile of a skinned part / vertex item of an altered part
     void clear() {
         jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
         insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
         seg_mt_seg.clear(); tiles.clear(); mt_desc.clear(); mt_segs.clear();
         vitem_seg.clear(); vitem_chunk.clear(); seg_vitem_first.clear();
-        nscratch = 0; nslots = 0;
+        nscratch = 0; nslots = 0; any_skinned = false; any_altered = false; tile_alt = 0; vitem_alt = 0;
     }
 };
 
@@ -114,6 +123,7 @@ struct t3d_ctx {
     bool order_dep = true;   // the draw order depends on model transforms (transparents, depth off)
     cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
     struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
+    t3d::DevBuf valt;
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
@@ -136,6 +146,7 @@ void build_light(const t3d_light_desc& d, DevLight& L);
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out);
 int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n);
 int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate);
+uint32_t billboard_flags(const t3d_material& mat, bool skinned);
 int upload_frame(t3d_ctx* ctx, cudaStream_t st);
 int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st);
 int configure(t3d_ctx* ctx);

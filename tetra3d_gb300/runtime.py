@@ -71,6 +71,16 @@ class Context:
         ptr = C.cast(C.byref(scene_data.models, first * C.sizeof(abi.ModelDesc)), C.POINTER(abi.ModelDesc))
         self._check(self.lib.t3d_scene_set_models(self.h, sid, first, ptr, n), "scene_set_models")
 
+    def set_bones(self, sid, bones, first=0):
+        """Bone influence matrices (n, 4, 4) of the scene's bones first..first+n."""
+        b = np.ascontiguousarray(bones, np.float32).reshape(-1, 16)
+        self._check(self.lib.t3d_scene_set_bones(self.h, sid, first, abi.fptr(b), b.shape[0]), "scene_set_bones")
+
+    def set_shape_weights(self, sid, mesh, weights):
+        w = np.ascontiguousarray(weights, np.float32).reshape(-1)
+        self._check(self.lib.t3d_scene_set_shape_weights(self.h, sid, mesh, abi.fptr(w), w.shape[0]),
+                    "scene_set_shape_weights")
+
     def transforms(self, sid, n):
         out = np.zeros((n, 16), np.float32)
         self._check(self.lib.t3d_scene_get_transforms(self.h, sid, abi.fptr(out), n), "scene_get_transforms")

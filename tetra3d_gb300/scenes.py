@@ -152,6 +152,9 @@ def default_material(**kw):
 
 
 class MeshData:
+    """A mesh's SoA streams. Optional: shape keys (shape_positions / shape_normals (K, V, 3) deltas,
+    shape_weights (K,)) and skinning joints / weights (V, 4)."""
+
     def __init__(self, positions, normals, uvs, indices, colors=None, parts=None, dims=None):
         self.positions = np.ascontiguousarray(positions, F32).reshape(-1, 3)
         self.normals = np.ascontiguousarray(normals, F32).reshape(-1, 3)
@@ -161,6 +164,8 @@ class MeshData:
         T = self.indices.shape[0]
         self.parts = parts if parts is not None else [dict(tri_start=0, tri_count=T, mat=default_material())]
         self.dims = dims  # None: UpdateDimensions
+        self.shape_positions = self.shape_normals = self.shape_weights = None
+        self.joints = self.weights = None
 
     @property
     def nverts(self):
@@ -340,6 +345,7 @@ class SceneData:
         self.cells = np.zeros((1, 4), F32) if cells is None or len(cells) == 0 else np.ascontiguousarray(cells, F32)
         self.ncells = 0 if cells is None else len(cells)
         self.camera = None
+        self.bones = None  # (NB, 16) Node.boneInfluence matrices
         self.meta = {}
         self._keep = []
 
@@ -355,6 +361,8 @@ class SceneData:
                 for f, v in mat.items():
                     if f == "color":
                         pa[k].mat.color[:] = [float(c) for c in v]
+                    elif f == "billboard_lock":
+                        pa[k].mat.billboard_lock[:] = [int(c) for c in v]
                     else:
                         setattr(pa[k].mat, f, v)
             keep.append(pa)
@@ -368,6 +376,18 @@ class SceneData:
                 d.has_dimensions = 1
                 d.dim_min[:] = [float(x) for x in m.dims[0]]
                 d.dim_max[:] = [float(x) for x in m.dims[1]]
+            if m.shape_weights is not None and len(m.shape_weights):
+                sp = np.ascontiguousarray(m.shape_positions, F32)
+                sn = np.ascontiguousarray(m.shape_normals, F32)
+                sw = np.ascontiguousarray(m.shape_weights, F32)
+                keep += [sp, sn, sw]
+                d.shape_positions, d.shape_normals, d.shape_weights = abi.fptr(sp), abi.fptr(sn), abi.fptr(sw)
+                d.num_shape_keys = len(sw)
+            if m.joints is not None:
+                jt = np.ascontiguousarray(m.joints, np.uint32)
+                wt = np.ascontiguousarray(m.weights, F32)
+                keep += [jt, wt]
+                d.joints, d.weights = abi.uptr(jt), abi.fptr(wt)
         offs = np.zeros(len(self.lists) + 1, np.uint32)
         for i, l in enumerate(self.lists):
             offs[i + 1] = offs[i] + len(l)
@@ -382,6 +402,10 @@ class SceneData:
         sd.list_items = abi.uptr(items)
         sd.num_meshes, sd.num_models, sd.num_lights = len(self.meshes), self.nmodels, self.nlights
         sd.num_volume_cells, sd.num_lists = self.ncells, len(self.lists)
+        if self.bones is not None and len(self.bones):
+            bones = np.ascontiguousarray(self.bones, F32).reshape(-1, 16)
+            keep.append(bones)
+            sd.bones, sd.num_bones = abi.fptr(bones), bones.shape[0]
         self._keep = keep
         return sd
 
@@ -689,6 +713,185 @@ def feature_scene(seed=5, n=48, w=1280, h=720):
     return sd
 
 
+def tube_mesh(rings=12, segments=10, height=3.0, radius=0.35):
+    """An open cylinder along +Y: (rings + 1) x segments vertices, smooth radial normals."""
+    r = np.arange(rings + 1)[:, None]
+    sg = np.arange(segments)[None, :]
+    ph = 2 * np.pi * sg / segments + 0 * r
+    y = height * r / rings + 0 * sg
+    pos = np.stack([radius * np.cos(ph), y, radius * np.sin(ph)], -1).reshape(-1, 3).astype(F32)
+    nrm = np.stack([np.cos(ph), 0 * ph, np.sin(ph)], -1).reshape(-1, 3).astype(F32)
+    uv = np.stack([sg / segments + 0 * r, r / rings + 0 * sg], -1).reshape(-1, 2).astype(F32)
+    q = (np.arange(rings)[:, None] * segments + np.arange(segments)[None, :]).reshape(-1)
+    nxt = (q // segments) * segments + (q + 1) % segments
+    idx = np.stack([q, nxt, q + segments, nxt, nxt + segments, q + segments], 1).reshape(-1, 3).astype(np.uint32)
+    idx = _orient_outward(pos, idx, center=None)
+    return MeshData(pos, nrm, uv, idx)
+
+
+def tube_skin(me, rng, nbones=4, height=3.0):
+    """Joints and weights of a tube along Y: each vertex blends the two nearest of `nbones` bones
+    spaced along the tube (exact 1.0 weights on the bone heights), unused slots hold other joints with
+    weight 0, and a few vertices carry a 1.0 weight after a partial one (Model.skinVertex stops there)."""
+    f = me.positions[:, 1].astype(np.float64) / height * (nbones - 1)
+    i0 = np.clip(np.floor(f), 0, nbones - 2).astype(np.uint32)
+    t = (f - i0).astype(F32)
+    V = me.nverts
+    joints = np.zeros((V, 4), np.uint32)
+    weights = np.zeros((V, 4), F32)
+    joints[:, 0], joints[:, 1] = i0, i0 + 1
+    weights[:, 0], weights[:, 1] = F32(1) - t, t
+    joints[:, 2:] = rng.integers(0, nbones, (V, 2))
+    weights[t == 0, :] = (1, 0, 0, 0)
+    weights[t == 1, :] = (0, 1, 0, 0)
+    odd = rng.choice(V, max(1, V // 12), replace=False)
+    weights[odd] = (0.25, 1.0, 0.5, 0.0)
+    return joints, weights
+
+
+def tube_bones(rng, n, pos, nbones=4, height=3.0, bend=0.5):
+    """Per model a chain of bone influence matrices bending a tube at `pos` (row-vector TRS)."""
+    out = []
+    for k in range(n):
+        for b in range(nbones):
+            ang = [float(rng.uniform(-bend, bend)) * b / max(nbones - 1, 1) for _ in range(2)]
+            rot = mult(rotate(1, 0, 0, ang[0]), rotate(0, 0, 1, ang[1]))
+            off = np.asarray(pos[k], F32) + np.array([0.3 * ang[1] * b, 0.0, 0.3 * ang[0] * b], F32)
+            s = F32(rng.uniform(0.8, 1.2))
+            out.append(trs(off.reshape(1, 3), np.full((1, 3), s, F32), rot.reshape(1, 4, 4))[0])
+    return np.asarray(out, F32).reshape(-1, 4, 4)
+
+
+def skinned_scene(seed=7, n=28, w=1280, h=720):
+    """Skinned and shape-keyed meshes under the feature scene's lights and random materials.
+
+    Meshes: a skinned tube (two copies with different part materials), a skinned tube that also has a
+    shape key, a UV sphere with two shape keys and a cube. Models: skinned tubes each bent by its own bone
+    chain (one behind the camera, culled on its model position), tubes drawn unskinned, shape-keyed spheres
+    under random transforms and a few cubes. Lights, light volumes and light lists as in feature_scene.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = feature_scene(seed, n=4)
+    nb = 4
+    tubes = []
+    for k in range(3):
+        t = tube_mesh()
+        T = t.ntris
+        cuts = sorted(set([0, T] + [int(c) for c in rng.integers(1, T, 2)]))
+        t.parts = [dict(tri_start=cuts[i], tri_count=cuts[i + 1] - cuts[i], mat=_random_material(rng))
+                   for i in range(len(cuts) - 1)]
+        t.joints, t.weights = tube_skin(t, rng, nb)
+        t.colors = rng.uniform(0.4, 1.0, (t.nverts, 4)).astype(F32) if k != 1 else None
+        tubes.append(t)
+    pinch = np.zeros((1, tubes[2].nverts, 3), F32)
+    pinch[0] = -0.3 * tubes[2].positions * np.array([1, 0, 1], F32) * np.sin(
+        tubes[2].positions[:, 1:2] * F32(np.pi / 3)).astype(F32)
+    tubes[2].shape_positions = pinch
+    tubes[2].shape_normals = rng.uniform(-0.2, 0.2, pinch.shape).astype(F32)
+    tubes[2].shape_weights = np.array([0.6], F32)
+    sph = uv_sphere(16, 8, 1.2)
+    sph.parts = [dict(tri_start=0, tri_count=sph.ntris, mat=_random_material(rng))]
+    bulge = (sph.normals * rng.uniform(0.0, 0.4, (sph.nverts, 1))).astype(F32)
+    sph.shape_positions = np.stack([bulge, rng.uniform(-0.15, 0.15, bulge.shape).astype(F32)])
+    sph.shape_normals = rng.uniform(-0.3, 0.3, (2, sph.nverts, 3)).astype(F32)
+    sph.shape_weights = np.array([0.7, -0.35], F32)
+    cube = cube_mesh(1.0, 1.0, 1.0)
+    cube.parts = [dict(tri_start=0, tri_count=cube.ntris, mat=_random_material(rng))]
+    meshes = tubes + [sph, cube]
+    nskin = n // 2
+    pos = np.stack([rng.uniform(-12, 12, n), rng.uniform(-6, 4, n), rng.uniform(-34, -6, n)], 1).astype(F32)
+    pos[1] = (0, 0, 150)  # skinned, behind the camera: culled on the model position
+    mesh_of = np.empty(n, np.uint32)
+    mesh_of[:nskin] = rng.integers(0, 3, nskin)
+    rest = n - nskin
+    mesh_of[nskin:] = rng.choice([0, 2, 3, 3, 3, 4], rest)
+    scl = np.repeat(rng.uniform(0.6, 2.0, (n, 1)), 3, 1).astype(F32)
+    rot = quat_to_mat(random_quats(rng, n))
+    sd = SceneData(meshes, n, [base.lights[i] for i in range(base.nlights)], base.lists,
+                   cells=base.cells[:base.ncells] if base.ncells else None, name=f"skinned{seed}")
+    set_models_trs(sd, mesh_of, pos, scl, rot,
+                   light_list=np.where(rng.random(n) < 0.5, -1, rng.integers(1, 4, n)).astype(np.int32))
+    sd.mv["skinned"][:nskin] = 1
+    sd.mv["bone_first"][:nskin] = np.arange(nskin, dtype=np.uint32) * nb
+    sd.mv["frustum_culling"] = (rng.random(n) < 0.85).astype(np.int32)
+    sd.mv["frustum_culling"][1] = 1
+    sd.mv["shadeless"] = (rng.random(n) < 0.08).astype(np.int32)
+    tint = rng.random(n) < 0.3
+    sd.mv["color"][tint, :3] = rng.uniform(0.3, 1.0, (int(tint.sum()), 3))
+    sd.bones = tube_bones(rng, nskin, pos[:nskin], nb)
+    sd.camera = feature_camera("persp", w, h)
+    return sd
+
+
+def quad_mesh(w=1.0, h=1.0):
+    """A w x h quad in the XY plane facing +Z (two triangles)."""
+    w2, h2 = F32(w) / F32(2), F32(h) / F32(2)
+    pos = np.array([(-w2, -h2, 0), (w2, -h2, 0), (w2, h2, 0), (-w2, h2, 0)], F32)
+    nrm = np.tile(np.array([0, 0, 1], F32), (4, 1))
+    uv = np.array([(0, 0), (1, 0), (1, 1), (0, 1)], F32)
+    return MeshData(pos, nrm, uv, np.array([(0, 1, 2), (0, 2, 3)], np.uint32))
+
+
+BILLBOARD_OPTIONS = [  # (locks, up, depth mode)
+    ((0, 0, 0), 0, 0), ((0, 1, 0), 0, 0), ((1, 0, 0), 0, 0), ((0, 0, 1), 0, 0), ((0, 0, 0), 1, 0),
+    ((0, 0, 0), 0, 1), ((1, 1, 0), 1, 1), ((0, 1, 1), 0, 1)]
+
+
+def billboard_scene(seed=9, n=40, w=1280, h=720):
+    """Billboarded parts under every lock, up direction and depth mode (Material.Billboard*),
+    next to plain parts of the same meshes, under the feature scene's lights.
+
+    Meshes: quads (two triangles, one part) and icospheres with two parts, one billboarded and one
+    not; each copy takes one option set of BILLBOARD_OPTIONS on top of a random material. Models: random
+    transforms in front of the camera, one directly below a camera at (0, 10, 0) (the LookAt's
+    degenerate-up branch for that camera) and a skinned tube with a billboard material (not turned).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = feature_scene(seed, n=4)
+    meshes = []
+    for k, (locks, up, depth) in enumerate(BILLBOARD_OPTIONS):
+        bb = dict(billboard=1, billboard_lock=locks, billboard_up=up, billboard_depth=depth)
+        q = quad_mesh(float(rng.uniform(0.8, 2.5)), float(rng.uniform(0.8, 2.5)))
+        q.parts = [dict(tri_start=0, tri_count=2, mat={**_random_material(rng), **bb, "present": 1, "visible": 1})]
+        q.colors = rng.uniform(0.4, 1.0, (4, 4)).astype(F32) if k % 2 else None
+        meshes.append(q)
+        ico = icosphere(1)
+        T = ico.ntris
+        cut = int(rng.integers(8, T - 8))
+        ico.parts = [dict(tri_start=0, tri_count=cut, mat={**_random_material(rng), **bb, "present": 1, "visible": 1}),
+                     dict(tri_start=cut, tri_count=T - cut, mat=_random_material(rng))]
+        meshes.append(ico)
+    tube = tube_mesh(rings=4, segments=6)
+    tube.joints, tube.weights = tube_skin(tube, rng, 4)
+    tube.parts = [dict(tri_start=0, tri_count=tube.ntris,
+                       mat=default_material(billboard=1, billboard_depth=1, backface_culling=0))]
+    meshes.append(tube)
+    nb = len(meshes) - 1
+    pos = np.stack([rng.uniform(-12, 12, n), rng.uniform(-6, 6, n), rng.uniform(-35, -5, n)], 1).astype(F32)
+    pos[0] = (0.0, 0.0, 0.0)   # below a camera at (0, 10, 0) looking down
+    pos[1] = (0.5, 1.0, -12.0)
+    mesh_of = np.concatenate([np.arange(nb), rng.integers(0, nb, n - nb - 1), [nb]]).astype(np.uint32)
+    scl = np.repeat(rng.uniform(0.6, 2.0, (n, 1)), 3, 1).astype(F32)
+    rot = quat_to_mat(random_quats(rng, n))
+    rot[0] = ident()
+    scl[0] = 3.0
+    sd = SceneData(meshes, n, [base.lights[i] for i in range(base.nlights)], base.lists,
+                   cells=base.cells[:base.ncells] if base.ncells else None, name=f"billboards{seed}")
+    set_models_trs(sd, mesh_of, pos, scl, rot,
+                   light_list=np.where(rng.random(n) < 0.5, -1, rng.integers(1, 4, n)).astype(np.int32))
+    sd.mv["frustum_culling"] = (rng.random(n) < 0.7).astype(np.int32)
+    sd.mv["frustum_culling"][0] = 0
+    sd.mv["skinned"][n - 1] = 1
+    sd.bones = tube_bones(rng, 1, pos[n - 1:], 4)
+    sd.camera = feature_camera("persp", w, h)
+    return sd
+
+
+def down_camera(w=1280, h=720):
+    """A camera at (0, 10, 0) looking straight down -Y."""
+    return camera(pos=(0.0, 10.0, 0.0), rot=rotate(1, 0, 0, deg2rad(-90.0)), w=w, h=h, fov=70.0, near=0.1, far=60.0)
+
+
 FEATURE_CAMERAS = ["persp", "ortho", "unlit", "fog_add", "fog_sub", "fog_overwrite", "corrected", "tilted"]
 
 
@@ -734,4 +937,5 @@ def subset(sd, models):
                     cells=sd.cells[:sd.ncells] if sd.ncells else None, name=sd.name + f"[{len(models)}]")
     out.mv[:] = sd.mv[models]
     out.camera = sd.camera
+    out.bones = sd.bones
     return out
