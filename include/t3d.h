@@ -150,7 +150,13 @@ typedef struct t3d_mesh_desc {
     /* Skinning (Model.skinVertex, model.go:559-596): four joint slots per vertex and
      * their weights (Mesh.VertexWeights); a skinned model maps joint j to scene bone
      * bone_first + j. NULL when no model skins this mesh. */
-    uint32_t             reserved;
+    /* Mesh.SetAutoSubdivide(true) (mesh.go:447-490): at upload every part triangle
+     * longer than the smallest MaximumTriangleSize of the scene's subdivision levels
+     * is split into up to max_subdivisions levels of 4-way subdivisions (new vertices
+     * appended after num_vertices); each frame a triangle draws the level its
+     * distance to the model-space camera selects (Triangle.handleSubdivision,
+     * mesh.go:1877-1949). Not with shape keys or on skinned models. */
+    int32_t              auto_subdivide;
     const uint32_t*      joints;          /* 4 * num_vertices */
     const float*         weights;         /* 4 * num_vertices */
 } t3d_mesh_desc;
@@ -221,6 +227,12 @@ typedef struct t3d_scene_desc {
     uint32_t              num_lists;
     uint32_t              num_bones;
     const float*          bones;          /* 16 per bone: initial Node.boneInfluence matrices */
+    /* Library.autosubdivisionLevels (library.go:206-209): DistanceSquared and
+     * MaximumTriangleSize per level; max_subdivisions = maxAutoSubdivisionCount
+     * (0: the library default, 3). */
+    const float*          subdivision_levels;     /* 2 * num_subdivision_levels */
+    uint32_t              num_subdivision_levels;
+    uint32_t              max_subdivisions;
 } t3d_scene_desc;
 
 /* Camera + World settings read by Render (camera.go:256-321, world.go:25-39).

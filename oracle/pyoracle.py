@@ -74,6 +74,16 @@ def render(scene_data, cam, light_mask=None, animate_frames=0, threads=1, f64=Fa
     sd = scene_data.desc()
     nseg_max = sum(len(scene_data.meshes[int(m)].parts) for m in scene_data.mv["mesh"]) + 1
     slots = max(1, scene_data.total_tris())
+    while True:
+        frame, rc, need = _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_max, slots)
+        if rc == 0:
+            return frame
+        if need <= slots:  # not a capacity problem
+            raise RuntimeError(f"oracle render failed: {rc}")
+        slots = need  # auto-subdivided meshes list more triangles than the scene holds
+
+
+def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_max, slots):
     dt = np.float64 if f64 else np.float32
     seg = {k: np.zeros(nseg_max, np.uint32) for k in ("model", "part", "base", "capacity", "count")}
     tri = np.zeros(slots, np.uint32)
@@ -95,13 +105,13 @@ def render(scene_data, cam, light_mask=None, animate_frames=0, threads=1, f64=Fa
     fn = lib.t3d_oracle_render_f64 if f64 else lib.t3d_oracle_render_f32
     rc = fn(C.byref(sd), C.byref(cam), mask, animate_frames, threads, C.byref(o))
     if rc != 0:
-        raise RuntimeError(f"oracle render failed: {rc}")
+        return None, rc, int(o.total_slots)
     n = o.num_segments
     segs = [dict(model=int(seg["model"][i]), part=int(seg["part"][i]), base=int(seg["base"][i]),
                  capacity=int(seg["capacity"][i]), count=int(seg["count"][i])) for i in range(n)]
     sel = np.concatenate([np.arange(s["base"], s["base"] + s["count"]) for s in segs] or [np.zeros(0, np.int64)])
     sel = sel.astype(np.int64)
-    return OracleFrame(segs, tri[sel], xyuv[sel], rgba[sel], depth[sel], o.culled_models)
+    return OracleFrame(segs, tri[sel], xyuv[sel], rgba[sel], depth[sel], o.culled_models), 0, slots
 
 
 def mat_inverted(m):

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <thread>
 #include <functional>
 #include <vector>
@@ -207,8 +208,174 @@ template <typename R> struct ModelState {
 // One render pair: model index + part index + draw-order slot.
 struct Pair { uint32_t model, part; float depth; int32_t order; };
 
+// Mesh.SetAutoSubdivide (mesh.go:447-490) restated: every part triangle,
+// then the triangles of its subdivision levels (forEachTri order,
+// mesh.go:2238-2256); new vertices appended; per listed triangle its centre
+// and, for handleSubdivision, the base's Normal, MaxSpan and level count.
+struct SubMesh {
+    std::vector<float> pos, nrm, uv, col;
+    std::vector<uint32_t> idx;
+    std::vector<float> ctr;
+    std::vector<float> bnormal, bspan;  // per listed triangle: its base triangle's Normal (3) and MaxSpan
+    std::vector<int> level, nlevels, base;  // level (-1: the base), the base's level count, the base's entry
+    std::vector<t3d_part_desc> parts;
+    t3d_mesh_desc desc;
+};
+
+struct Subdivision {  // Triangle.performSubdivision (mesh.go:1758-1864)
+    SubMesh& M;
+    bool colors;
+    float intended;
+    int max_count;
+    struct T { uint32_t a, b, c; float span; float ctr[3]; };
+    std::vector<std::vector<T>> lv;
+    void lerp3(std::vector<float>& v, int n, uint32_t i, uint32_t j) {  // Lerp(.., 0.5)
+        for (int k = 0; k < n; k++) {
+            float a = v[n * (size_t)i + k], b = v[n * (size_t)j + k];
+            v.push_back(a + ((b - a) * 0.5f));
+        }
+    }
+    T make(uint32_t a, uint32_t b, uint32_t c, float span) {
+        T t{a, b, c, span, {0, 0, 0}};
+        const float* P = M.pos.data();
+        for (int k = 0; k < 3; k++)  // Add(..).Add(..).Scale(1.0 / 3.0)
+            t.ctr[k] = ((P[3 * (size_t)a + k] + P[3 * (size_t)b + k]) + P[3 * (size_t)c + k]) * (float)(1.0 / 3.0);
+        return t;
+    }
+    void run(int level, T t) {
+        if (level == max_count || t.span <= intended) return;
+        const uint32_t s = (uint32_t)(M.pos.size() / 3);
+        const uint32_t e[3][2] = {{t.a, t.b}, {t.b, t.c}, {t.c, t.a}};
+        for (auto& q : e) lerp3(M.pos, 3, q[0], q[1]);
+        for (auto& q : e) lerp3(M.nrm, 3, q[0], q[1]);
+        for (auto& q : e) lerp3(M.uv, 2, q[0], q[1]);
+        if (colors)
+            for (auto& q : e) lerp3(M.col, 4, q[0], q[1]);
+        T A = make(t.a, s, s + 2, t.span / 2), B = make(s, t.b, s + 1, t.span / 2);
+        T C = make(s + 1, t.c, s + 2, t.span / 2), D = make(s, s + 1, s + 2, t.span / 2);
+        lv[level].insert(lv[level].end(), {A, B, C, D});
+        run(level + 1, A);
+        run(level + 1, B);
+        run(level + 1, C);
+        run(level + 1, D);
+    }
+};
+
+void build_submesh(const t3d_mesh_desc& me, const float* levels, uint32_t nlev, int max_count, SubMesh& M) {
+    M.pos.assign(me.positions, me.positions + 3 * (size_t)me.num_vertices);
+    M.nrm.assign(me.normals, me.normals + 3 * (size_t)me.num_vertices);
+    M.uv.assign(me.uvs, me.uvs + 2 * (size_t)me.num_vertices);
+    if (me.colors) M.col.assign(me.colors, me.colors + 4 * (size_t)me.num_vertices);
+    float smallest = std::numeric_limits<float>::max();
+    for (uint32_t i = 0; i < nlev; i++) smallest = std::min(smallest, levels[2 * i + 1]);
+    Subdivision div{M, me.colors != nullptr, smallest, max_count, {}};
+    auto cross3 = [](V3<float> a, V3<float> b) {  // Vector3.Cross, vector.go:164-175
+        return v3<float>(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+    };
+    for (uint32_t p = 0; p < me.num_parts; p++) {
+        t3d_part_desc part = me.parts[p];
+        uint32_t first = (uint32_t)(M.idx.size() / 3);
+        for (uint32_t t = me.parts[p].tri_start; t < me.parts[p].tri_start + me.parts[p].tri_count; t++) {
+            uint32_t a = me.indices[3 * (size_t)t], b = me.indices[3 * (size_t)t + 1], c = me.indices[3 * (size_t)t + 2];
+            V3<float> pa = v3<float>(M.pos[3 * (size_t)a], M.pos[3 * (size_t)a + 1], M.pos[3 * (size_t)a + 2]);
+            V3<float> pb = v3<float>(M.pos[3 * (size_t)b], M.pos[3 * (size_t)b + 1], M.pos[3 * (size_t)b + 2]);
+            V3<float> pc = v3<float>(M.pos[3 * (size_t)c], M.pos[3 * (size_t)c + 1], M.pos[3 * (size_t)c + 2]);
+            // MaxSpan = max of the edge lengths (mesh.go:2020-2024), Normal (mesh.go:2030-2037, :2171-2179)
+            float e0 = magnitude(sub(pa, pb)), e1 = magnitude(sub(pb, pc)), e2 = magnitude(sub(pc, pa));
+            float span = (std::isnan(e0) || std::isnan(e1) || std::isnan(e2)) ? NAN : std::max(std::max(e0, e1), e2);
+            V3<float> n = unit(cross3(sub(pb, pa), sub(pc, pb)));
+            if (!(std::fabs(n.x) > 1e-4f || std::fabs(n.y) > 1e-4f || std::fabs(n.z) > 1e-4f))
+                n = v3<float>(me.normals[3 * (size_t)a], me.normals[3 * (size_t)a + 1], me.normals[3 * (size_t)a + 2]);
+            int nl = span <= smallest ? 0 : max_count;
+            div.lv.assign(nl, {});
+            if (nl) div.run(0, Subdivision::T{a, b, c, span, {0, 0, 0}});
+            int baseEntry = (int)(M.idx.size() / 3);
+            auto push = [&](uint32_t x, uint32_t y, uint32_t z, const float* ctr, int level) {
+                M.idx.insert(M.idx.end(), {x, y, z});
+                M.ctr.insert(M.ctr.end(), {ctr[0], ctr[1], ctr[2]});
+                M.bnormal.insert(M.bnormal.end(), {n.x, n.y, n.z});
+                M.bspan.push_back(span);
+                M.level.push_back(level);
+                M.nlevels.push_back(nl);
+                M.base.push_back(baseEntry);
+            };
+            float c0[3] = {(pa.x + pb.x + pc.x) / 3.0f, (pa.y + pb.y + pc.y) / 3.0f, (pa.z + pb.z + pc.z) / 3.0f};
+            push(a, b, c, c0, -1);
+            for (int L = 0; L < nl; L++)
+                for (auto& st : div.lv[L]) push(st.a, st.b, st.c, st.ctr, L);
+        }
+        part.tri_start = first;
+        part.tri_count = (uint32_t)(M.idx.size() / 3) - first;
+        M.parts.push_back(part);
+    }
+    M.desc = me;
+    M.desc.positions = M.pos.data();
+    M.desc.normals = M.nrm.data();
+    M.desc.uvs = M.uv.data();
+    M.desc.colors = me.colors ? M.col.data() : nullptr;
+    M.desc.indices = M.idx.data();
+    M.desc.parts = M.parts.data();
+    M.desc.num_vertices = (uint32_t)(M.pos.size() / 3);
+    M.desc.num_triangles = (uint32_t)(M.idx.size() / 3);
+}
+
+// closestPointOnTri (colliderTriangles.go:177-281)
+template <typename R> V3<R> closest_on_line(V3<R> point, V3<R> start, V3<R> end) {
+    V3<R> diff = sub(end, start);
+    R d = dot(sub(point, start), diff) / dot(diff, diff);
+    if (d > 1) d = 1;
+    else if (d < 0) d = 0;
+    return add(start, v3<R>(diff.x * d, diff.y * d, diff.z * d));
+}
+template <typename R> V3<R> closest_on_tri(V3<R> point, V3<R> v0, V3<R> v1, V3<R> v2, V3<R> normal) {
+    R distance = dot(normal, v0);
+    R dist = dot(normal, point) - distance;
+    V3<R> planePoint = sub(point, v3<R>(normal.x * dist, normal.y * dist, normal.z * dist));
+    V3<R> ca = sub(v2, v0), ba = sub(v1, v0), pa = sub(planePoint, v0);
+    R dot00 = dot(ca, ca), dot01 = dot(ca, ba), dot02 = dot(ca, pa), dot11 = dot(ba, ba), dot12 = dot(ba, pa);
+    R invDenom = (R)1 / ((dot00 * dot11) - (dot01 * dot01));
+    R u = ((dot11 * dot02) - (dot01 * dot12)) * invDenom;
+    R v = ((dot00 * dot12) - (dot01 * dot02)) * invDenom;
+    if (u >= 0 && v >= 0 && u + v < 1) return planePoint;
+    V3<R> ab = closest_on_line(point, v0, v1), bc = closest_on_line(point, v1, v2), cap = closest_on_line(point, v2, v0);
+    V3<R> closest = ab;
+    R closestDist = dist2(point, ab), bcDist = dist2(point, bc), caDist = dist2(point, cap);
+    if (bcDist < closestDist) { closest = bc; closestDist = bcDist; }
+    if (caDist < closestDist) closest = cap;
+    return closest;
+}
+
+// Triangle.handleSubdivision (mesh.go:1877-1949) for listed triangle t: is it
+// the base (level -1) or on the level that the base triangle picks?
+template <typename R> bool subdiv_active(const t3d_scene_desc* sc, const SubMesh& M, uint32_t t, V3<R> camPos) {
+    const int nl = M.nlevels[t], level = M.level[t];
+    if (nl == 0) return level < 0;
+    const uint32_t b = (uint32_t)M.base[t];
+    V3<R> v[3];
+    for (int i = 0; i < 3; i++) {
+        const uint32_t k = M.idx[3 * (size_t)b + i];
+        v[i] = v3<R>((R)M.pos[3 * (size_t)k], (R)M.pos[3 * (size_t)k + 1], (R)M.pos[3 * (size_t)k + 2]);
+    }
+    V3<R> n = v3<R>((R)M.bnormal[3 * (size_t)t], (R)M.bnormal[3 * (size_t)t + 1], (R)M.bnormal[3 * (size_t)t + 2]);
+    R dist = dist2(camPos, closest_on_tri(camPos, v[0], v[1], v[2], n));
+    int active = -1;
+    R closestDistance = maxf<R>();
+    for (uint32_t i = 0; i < sc->num_subdivision_levels; i++) {
+        R d2 = (R)sc->subdivision_levels[2 * i];
+        if (dist < d2 && d2 < closestDistance) { closestDistance = d2; active = (int)i; }
+    }
+    if (active == -1) return level < 0;
+    R ms = (R)M.bspan[t];
+    int subIndex = -1;
+    while (ms > (R)sc->subdivision_levels[2 * active + 1]) { ms /= 2; subIndex++; }
+    if (subIndex >= nl) subIndex = nl - 1;
+    return subIndex >= 0 ? level == subIndex : level < 0;
+}
+
 template <typename R> struct Frame {
     const t3d_scene_desc* sc;
+    std::vector<std::unique_ptr<SubMesh>> sub;  // auto-subdivided meshes
+    std::vector<const t3d_mesh_desc*> mesh;     // the mesh each model draws (subdivided or as given)
     Camera<R> cam;
     std::vector<LightPrep<R>> lights;
     std::vector<ModelState<R>> models;
@@ -617,7 +784,8 @@ template <typename R, typename OutT>
 uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t slot, t3d_oracle_out* out) {
     const t3d_scene_desc* sc = F.sc;
     const t3d_model_desc& md = sc->models[rp.model];
-    const t3d_mesh_desc& me = sc->meshes[md.mesh];
+    const t3d_mesh_desc& me = *F.mesh[md.mesh];
+    const SubMesh* subm = F.sub[md.mesh].get();
     const t3d_part_desc& part = me.parts[rp.part];
     const t3d_material& mat = part.mat;
     const Camera<R>& cam = F.cam;
@@ -653,6 +821,8 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
     }
     uint32_t t_end = part.tri_start + part.tri_count;
     for (uint32_t t = part.tri_start; t < t_end; t++) {  // model.go:751-979
+        // auto-subdivision: only the triangles of the level handleSubdivision picked (model.go:753-755)
+        if (subm && !subdiv_active<R>(sc, *subm, t, invertedCamPos)) continue;
         uint32_t vidx[3] = {me.indices[3 * t], me.indices[3 * t + 1], me.indices[3 * t + 2]};
         for (int vi = 0; vi < 3; vi++) {
             uint32_t v = vidx[vi];
@@ -688,6 +858,8 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
         const float* pc = me.positions + 3 * (size_t)vidx[2];
         V3<R> center = v3<R>(((R)pa[0] + (R)pb[0] + (R)pc[0]) / (R)3, ((R)pa[1] + (R)pb[1] + (R)pc[1]) / (R)3,
                              ((R)pa[2] + (R)pb[2] + (R)pc[2]) / (R)3);
+        if (subm)  // subdivided triangles' centres come from the subdivision (mesh.go:1821-1845)
+            center = v3<R>((R)subm->ctr[3 * (size_t)t], (R)subm->ctr[3 * (size_t)t + 1], (R)subm->ctr[3 * (size_t)t + 2]);
         V3<R> from = invertedCamPos;
         if (skinned) {  // the skinned centre from the world camera (model.go:840-863, :941-946)
             const V3<R>& a = S.apos[vidx[0]];
@@ -843,6 +1015,18 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
     Frame<R> F;
     F.sc = sc;
     F.mask = mask;
+    const uint32_t nlev = sc->subdivision_levels ? sc->num_subdivision_levels : 0u;
+    F.sub.resize(sc->num_meshes);
+    F.mesh.resize(sc->num_meshes);
+    for (uint32_t m = 0; m < sc->num_meshes; m++) {
+        F.mesh[m] = &sc->meshes[m];
+        if (sc->meshes[m].auto_subdivide && nlev) {
+            F.sub[m] = std::make_unique<SubMesh>();
+            build_submesh(sc->meshes[m], sc->subdivision_levels, nlev,
+                          sc->max_subdivisions ? (int)sc->max_subdivisions : 3, *F.sub[m]);
+            F.mesh[m] = &F.sub[m]->desc;
+        }
+    }
     // the scene light list after the mask, then Camera.MaxLightCount (camera.go:1474-1497)
     if (sc->num_lists > 0)
         for (uint32_t q = sc->list_offsets[0]; q < sc->list_offsets[1]; q++)
@@ -923,7 +1107,7 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
             is_culled[i] = 1;
             culled++;
         }
-        const t3d_mesh_desc& me = sc->meshes[md.mesh];
+        const t3d_mesh_desc& me = *F.mesh[md.mesh];
         V3<R> mpos = row3(F.models[i].transform, 3);
         for (uint32_t p = 0; p < me.num_parts; p++) {
             const t3d_part_desc& part = me.parts[p];
@@ -958,7 +1142,7 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
     if (segs.size() > out->max_segments) return T3D_E_INVAL;
     uint64_t base = 0;
     for (size_t s = 0; s < segs.size(); s++) {
-        const t3d_mesh_desc& me = sc->meshes[sc->models[segs[s].model].mesh];
+        const t3d_mesh_desc& me = *F.mesh[sc->models[segs[s].model].mesh];
         out->seg_model[s] = segs[s].model;
         out->seg_part[s] = segs[s].part;
         out->seg_base[s] = (uint32_t)base;

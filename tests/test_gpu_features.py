@@ -399,3 +399,44 @@ def test_billboard_scene_matches_oracle(ctx, variant):
             assert_frames_equal(ctx.download(), ref, f"billboards/{variant}/mode{mode}")
     finally:
         ctx.release(sid)
+
+
+@pytest.mark.parametrize("variant", ["persp", "ortho", "tilted", "fog_add", "unlit"])
+def test_subdivision_scene_matches_oracle(ctx, variant):
+    """Auto-subdivided meshes: per-frame level choice per triangle (closest point on the
+    triangle to the model-space camera), subdivided vertices and centres, both forms."""
+    sd = scenes.subdivision_scene(10)
+    cam = scenes.feature_camera(variant)
+    ref = pyoracle.render(sd, cam)
+    assert ref.visible_tris > 0
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), ref, f"subdivision/{variant}/mode{mode}")
+        # the camera moves: triangles change level
+        for step in range(3):
+            cam2 = scenes.camera(pos=(0.0, 0.5, -4.0 - 8.0 * step), w=1280, h=720, fov=65.0, near=0.1, far=60.0)
+            ctx.render(sid, cam2)
+            assert_frames_equal(ctx.download(), pyoracle.render(sd, cam2), f"subdivision/moved{step}")
+    finally:
+        ctx.release(sid)
+
+
+def test_subdivision_argument_errors(ctx):
+    lib = ctx.lib
+    out = C.c_uint32()
+    bad = scenes.subdivision_scene(10)
+    bad.subdivision_levels = np.array([(36.0, 0.0)], np.float32)  # the level loop would not end
+    d = bad.desc()
+    assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+    bad = scenes.subdivision_scene(10)
+    bad.meshes[0].shape_positions = np.zeros((1, bad.meshes[0].nverts, 3), np.float32)
+    bad.meshes[0].shape_normals = np.zeros((1, bad.meshes[0].nverts, 3), np.float32)
+    bad.meshes[0].shape_weights = np.ones(1, np.float32)
+    d = bad.desc()
+    assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+    bad = scenes.subdivision_scene(10)
+    bad.max_subdivisions = 9
+    d = bad.desc()
+    assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL

@@ -53,7 +53,7 @@ class MeshDesc(C.Structure):
                 ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32), ("num_parts", C.c_uint32),
                 ("has_dimensions", C.c_int32), ("dim_min", C.c_float * 3), ("dim_max", C.c_float * 3),
                 ("shape_positions", f32p), ("shape_normals", f32p), ("shape_weights", f32p),
-                ("num_shape_keys", C.c_uint32), ("reserved", C.c_uint32), ("joints", u32p), ("weights", f32p)]
+                ("num_shape_keys", C.c_uint32), ("auto_subdivide", C.c_int32), ("joints", u32p), ("weights", f32p)]
 
 
 class ModelDesc(C.Structure):
@@ -78,7 +78,8 @@ class SceneDesc(C.Structure):
                 ("list_offsets", u32p), ("list_items", u32p),
                 ("num_meshes", C.c_uint32), ("num_models", C.c_uint32), ("num_lights", C.c_uint32),
                 ("num_volume_cells", C.c_uint32), ("num_lists", C.c_uint32), ("num_bones", C.c_uint32),
-                ("bones", f32p)]
+                ("bones", f32p), ("subdivision_levels", f32p), ("num_subdivision_levels", C.c_uint32),
+                ("max_subdivisions", C.c_uint32)]
 
 
 class CameraDesc(C.Structure):

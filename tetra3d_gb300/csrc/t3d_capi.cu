@@ -168,7 +168,7 @@ int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d
             return T3D_E_INVAL;
         }
         const SceneMesh& me = sc->meshes[models[i].mesh];
-        if (models[i].skinned && (!me.skin || (uint64_t)models[i].bone_first + me.max_joint >= sc->num_bones)) {
+        if (models[i].skinned && (!me.skin || me.subdiv || (uint64_t)models[i].bone_first + me.max_joint >= sc->num_bones)) {
             set_err(ctx, "set_models: skinned model %u without joints or with bones beyond the scene's %u", first + i,
                     sc->num_bones);
             return T3D_E_INVAL;

@@ -40,6 +40,9 @@ enum : uint32_t {
     SEG_BB_LOCKZ = 1u << 19,    // BillboardLockZ
     SEG_BB_CAMUP = 1u << 20,    // BillboardUpDirection == BillboardYUpCameraY
     SEG_UNBB = 1u << 21,        // BillboardedDepthMode == DepthModeUnbillboarded on a billboard
+    SEG_SUBDIV = 1u << 22,      // auto-subdivided mesh: triangles are candidates of a subdivision level
+    // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
+    SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
     SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD,
 };
@@ -122,6 +125,11 @@ struct DevJob {
     const uint4* vjoint;    // per pool vertex: four joints (skinned meshes)
     const float4* vweight;  // per pool vertex: their weights
     const float4* bones;    // 4 rows per bone: Node.boneInfluence
+    const float4* sub_info; // auto-subdivided meshes, per pool triangle: its base triangle's Normal and MaxSpan
+    const int4* sub_rel;    // (level or -1 for the base, the base's level count, entries back to the base, 0)
+    const float* sub_levels;  // AutoSubdivisionLevel: DistanceSquared, MaximumTriangleSize
+    uint32_t nsub_levels;
+    uint32_t pad_sub;
 };
 
 // One (job, model) pair.

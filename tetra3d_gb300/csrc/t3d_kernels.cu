@@ -866,6 +866,66 @@ __device__ __forceinline__ void vertex_chunk_altered(const FrameParams& P, const
     }
 }
 
+// ------------------------------------------------- auto-subdivision ----
+// closestPointOnTri with its plane and line helpers (colliderTriangles.go:177-182,
+// :206-281), in the model space of the camera position.
+__device__ __forceinline__ f3 closest_on_line(f3 point, f3 start, f3 end) {
+    const f3 diff = sub3(end, start);
+    float d = dot3(sub3(point, start), diff) / dot3(diff, diff);
+    if (d > 1.0f) d = 1.0f;
+    else if (d < 0.0f) d = 0.0f;
+    return add3(start, mk3(diff.x * d, diff.y * d, diff.z * d));
+}
+__device__ __forceinline__ f3 closest_on_tri(f3 point, f3 v0, f3 v1, f3 v2, f3 normal) {
+    const float dist = dot3(normal, point) - dot3(normal, v0);
+    const f3 pp = sub3(point, mk3(normal.x * dist, normal.y * dist, normal.z * dist));
+    // isPointInsideTriangle (colliderTriangles.go:240-265)
+    const f3 ca = sub3(v2, v0), ba = sub3(v1, v0), pa = sub3(pp, v0);
+    const float dot00 = dot3(ca, ca), dot01 = dot3(ca, ba), dot02 = dot3(ca, pa);
+    const float dot11 = dot3(ba, ba), dot12 = dot3(ba, pa);
+    const float inv = 1.0f / ((dot00 * dot11) - (dot01 * dot01));
+    const float u = ((dot11 * dot02) - (dot01 * dot12)) * inv;
+    const float v = ((dot00 * dot12) - (dot01 * dot02)) * inv;
+    if (u >= 0.0f && v >= 0.0f && u + v < 1.0f) return pp;
+    const f3 ab = closest_on_line(point, v0, v1);
+    const f3 bc = closest_on_line(point, v1, v2);
+    const f3 cl = closest_on_line(point, v2, v0);
+    f3 closest = ab;
+    float cd = dist2(point, ab);
+    const float bcd = dist2(point, bc), cad = dist2(point, cl);
+    if (bcd < cd) { closest = bc; cd = bcd; }
+    if (cad < cd) closest = cl;
+    return closest;
+}
+// Whether pool triangle t of an auto-subdivided part is drawn this frame:
+// Triangle.handleSubdivision (mesh.go:1877-1949) of its base triangle picks
+// the base itself or one subdivision level.
+__device__ __forceinline__ bool subdiv_active(const DevJob& J, const float4* __restrict__ va, uint32_t t, f3 ic) {
+    const int4 r = J.sub_rel[t];
+    if (r.y == 0) return r.x < 0;
+    const float4 inf = J.sub_info[t];
+    const uint32_t tb = t - (uint32_t)r.z;
+    const float4 A = va[J.idx[3 * (size_t)tb]], B = va[J.idx[3 * (size_t)tb + 1]], C = va[J.idx[3 * (size_t)tb + 2]];
+    const f3 cp = closest_on_tri(ic, mk3(A.x, A.y, A.z), mk3(B.x, B.y, B.z), mk3(C.x, C.y, C.z), mk3(inf.x, inf.y, inf.z));
+    const float dist = dist2(ic, cp);
+    int act = -1;
+    float closest = 3.402823466e38f;
+    for (uint32_t i = 0; i < J.nsub_levels; i++) {
+        const float d2 = J.sub_levels[2 * i];
+        if (dist < d2 && d2 < closest) { closest = d2; act = (int)i; }
+    }
+    if (act < 0) return r.x < 0;
+    const float size = J.sub_levels[2 * act + 1];
+    float ms = inf.w;
+    int sub = -1;
+    for (int it = 0; ms > size && it < 400; it++) {  // sizes are positive, so this ends within ~280 halvings
+        ms /= 2.0f;
+        sub++;
+    }
+    if (sub >= r.y) sub = r.y - 1;
+    return sub >= 0 ? r.x == sub : r.x < 0;
+}
+
 // The skinned triangle centre, summed from zero over the corners' skinned
 // positions and divided by 3 (model.go:840-863, :941-946).
 __device__ __forceinline__ f3 skinned_centre(const float4* __restrict__ valt, uint32_t i0, uint32_t i1, uint32_t i2) {
@@ -994,7 +1054,9 @@ __device__ __forceinline__ void triangle_tiles(const FrameParams& P, unsigned ch
         const float* __restrict__ mctr = J.centers + 3 * (size_t)td.tbase;
         const float4* __restrict__ vcull = P.vcull + td.vscratch;
         const float4* __restrict__ valt = P.valt + td.vscratch;
-        constexpr bool skinned = kSkinned;
+        const bool skinned = kSkinned && (td.flags & SEG_SKINNED);
+        const bool subdiv = kSkinned && (td.flags & SEG_SUBDIV);
+        const float4* __restrict__ sva = J.va + (subdiv ? J.meshes[P.segs[td.seg].mesh].vbase : 0u);
         const uint32_t vm = td.vmin;
         const bool wide = td.flags & SEG_WIDE;
         const uint32_t t0 = td.t0;
@@ -1009,7 +1071,11 @@ __device__ __forceinline__ void triangle_tiles(const FrameParams& P, unsigned ch
         // two triangles per lane per step (t and t + 32): both gathers are in flight together
         for (uint32_t tb = wt0; tb < wt1; tb += 64) {
             const uint32_t ta = tb + lane, tb2 = tb + 32 + lane;
-            const bool ha = ta < wt1, hb = tb2 < wt1;
+            bool ha = ta < wt1, hb = tb2 < wt1;
+            if (subdiv) {  // candidates of a level other than the chosen one are not drawn
+                if (ha) ha = subdiv_active(J, sva, td.tbase + ta, ic);
+                if (hb) hb = subdiv_active(J, sva, td.tbase + tb2, ic);
+            }
             uint32_t ia0 = vm, ia1 = vm, ia2 = vm, ib0 = vm, ib1 = vm, ib2 = vm;
             f3 ca = mk3(0.f, 0.f, 0.f), cb = ca;
             if (ha) {

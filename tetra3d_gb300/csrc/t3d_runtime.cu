@@ -305,6 +305,145 @@ static m4 host_transform(const SceneModel& m) {
 }
 
 // ------------------------------------------------------------ scenes ----
+// ------------------------------------------------------ auto-subdivision ----
+// Mesh.SetAutoSubdivide (mesh.go:447-490) with Triangle.performSubdivision
+// (mesh.go:1758-1864), done once at upload: every part lists each of its
+// triangles followed by that triangle's subdivision levels (forEachTri with
+// subdivisions, mesh.go:2238-2256), the new vertices appended after the mesh's
+// own. Per listed triangle: its centre, and for the per-frame level choice the
+// base triangle's Normal and MaxSpan, its level (-1: the base itself), the
+// base's level count and the distance back to the base's entry.
+struct SubdividedMesh {
+    std::vector<float> pos, nrm, uv, col;
+    std::vector<uint32_t> idx;
+    std::vector<float> ctr;
+    std::vector<float4> info;
+    std::vector<int4> rel;
+    std::vector<t3d_part_desc> parts;
+    t3d_mesh_desc desc;
+};
+
+namespace {
+struct SubTri { uint32_t a, b, c; float maxspan; float ctr[3]; };
+
+float edge_len(const float* p, const float* q) {  // Vector3.Sub + Magnitude
+    const float x = p[0] - q[0], y = p[1] - q[1], z = p[2] - q[2];
+    return sqrtf(x * x + y * y + z * z);
+}
+
+struct Subdivider {
+    SubdividedMesh& S;
+    bool colors;
+    float smallest;
+    uint32_t maxsub;
+    std::vector<std::vector<SubTri>>* levels;
+
+    uint32_t lerp_vertex(uint32_t i, uint32_t j) {  // Vector3/Vector2/Color4 Lerp(.., 0.5): a + ((b - a) * 0.5)
+        const uint32_t n = (uint32_t)(S.pos.size() / 3);
+        for (int k = 0; k < 3; k++) S.pos.push_back(S.pos[3 * (size_t)i + k] + ((S.pos[3 * (size_t)j + k] - S.pos[3 * (size_t)i + k]) * 0.5f));
+        for (int k = 0; k < 3; k++) S.nrm.push_back(S.nrm[3 * (size_t)i + k] + ((S.nrm[3 * (size_t)j + k] - S.nrm[3 * (size_t)i + k]) * 0.5f));
+        for (int k = 0; k < 2; k++) S.uv.push_back(S.uv[2 * (size_t)i + k] + ((S.uv[2 * (size_t)j + k] - S.uv[2 * (size_t)i + k]) * 0.5f));
+        if (colors)
+            for (int k = 0; k < 4; k++)
+                S.col.push_back(S.col[4 * (size_t)i + k] + ((S.col[4 * (size_t)j + k] - S.col[4 * (size_t)i + k]) * 0.5f));
+        return n;
+    }
+    SubTri child(uint32_t a, uint32_t b, uint32_t c, float maxspan) {
+        SubTri t{a, b, c, maxspan, {0.f, 0.f, 0.f}};
+        const float third = (float)(1.0 / 3.0);  // Vector3.Scale(1.0 / 3.0)
+        for (int k = 0; k < 3; k++)
+            t.ctr[k] = ((S.pos[3 * (size_t)a + k] + S.pos[3 * (size_t)b + k]) + S.pos[3 * (size_t)c + k]) * third;
+        return t;
+    }
+    void perform(uint32_t level, const SubTri& t) {
+        if (level == maxsub || t.maxspan <= smallest) return;
+        // the three edge midpoints in the order (a, b), (b, c), (c, a)
+        const uint32_t s = lerp_vertex(t.a, t.b);
+        lerp_vertex(t.b, t.c);
+        lerp_vertex(t.c, t.a);
+        const float half = t.maxspan / 2.0f;
+        const SubTri k[4] = {child(t.a, s, s + 2, half), child(s, t.b, s + 1, half), child(s + 1, t.c, s + 2, half),
+                             child(s, s + 1, s + 2, half)};
+        for (int q = 0; q < 4; q++) (*levels)[level].push_back(k[q]);
+        for (int q = 0; q < 4; q++) perform(level + 1, k[q]);
+    }
+};
+}  // namespace
+
+void subdivide_mesh(const t3d_mesh_desc& me, const float* lev, uint32_t nlev, uint32_t maxsub, SubdividedMesh& S) {
+    const size_t nv = me.num_vertices;
+    S.pos.assign(me.positions, me.positions + 3 * nv);
+    S.nrm.assign(me.normals, me.normals + 3 * nv);
+    S.uv.assign(me.uvs, me.uvs + 2 * nv);
+    if (me.colors) S.col.assign(me.colors, me.colors + 4 * nv);
+    float smallest = 3.402823466e38f;
+    for (uint32_t i = 0; i < nlev; i++)
+        if (lev[2 * i + 1] < smallest) smallest = lev[2 * i + 1];
+    std::vector<std::vector<SubTri>> levels;
+    Subdivider D{S, me.colors != nullptr, smallest, maxsub, &levels};
+    for (uint32_t p = 0; p < me.num_parts; p++) {
+        t3d_part_desc part = me.parts[p];
+        const uint32_t first = (uint32_t)(S.idx.size() / 3);
+        for (uint64_t t = me.parts[p].tri_start; t < (uint64_t)me.parts[p].tri_start + me.parts[p].tri_count; t++) {
+            const uint32_t a = me.indices[3 * t], b = me.indices[3 * t + 1], c = me.indices[3 * t + 2];
+            const float* pa = me.positions + 3 * (size_t)a;
+            const float* pb = me.positions + 3 * (size_t)b;
+            const float* pc = me.positions + 3 * (size_t)c;
+            // Triangle.RecalculateCenter / MaxSpan (mesh.go:1972-2026): Go's max of the three edges
+            const float e0 = edge_len(pa, pb), e1 = edge_len(pb, pc), e2 = edge_len(pc, pa);
+            float ms = e0;
+            if (e1 > ms) ms = e1;
+            if (e2 > ms) ms = e2;
+            if (e0 != e0 || e1 != e1 || e2 != e2) ms = NAN;
+            // Triangle.RecalculateNormal (mesh.go:2030-2037): Unit(Cross(B - A, C - B)), else A's vertex normal
+            const f3 v0 = sub3(mk3(pb[0], pb[1], pb[2]), mk3(pa[0], pa[1], pa[2]));
+            const f3 v1 = sub3(mk3(pc[0], pc[1], pc[2]), mk3(pb[0], pb[1], pb[2]));
+            f3 n = unit3(cross3(v0, v1));
+            if (!(fabsf(n.x) > 1e-4f || fabsf(n.y) > 1e-4f || fabsf(n.z) > 1e-4f))
+                n = mk3(me.normals[3 * (size_t)a], me.normals[3 * (size_t)a + 1], me.normals[3 * (size_t)a + 2]);
+            const int nl = (ms <= smallest) ? 0 : (int)maxsub;
+            levels.assign(nl, std::vector<SubTri>());
+            if (nl) D.perform(0, SubTri{a, b, c, ms, {0.f, 0.f, 0.f}});
+            const uint32_t base = (uint32_t)(S.idx.size() / 3);
+            const float4 info = make_float4(n.x, n.y, n.z, ms);
+            S.idx.insert(S.idx.end(), {a, b, c});
+            for (int k = 0; k < 3; k++) S.ctr.push_back((pa[k] + pb[k] + pc[k]) / 3.0f);
+            S.info.push_back(info);
+            S.rel.push_back(make_int4(-1, nl, 0, 0));
+            for (int L = 0; L < nl; L++)
+                for (const SubTri& st : levels[L]) {
+                    const uint32_t e = (uint32_t)(S.idx.size() / 3);
+                    S.idx.insert(S.idx.end(), {st.a, st.b, st.c});
+                    S.ctr.insert(S.ctr.end(), {st.ctr[0], st.ctr[1], st.ctr[2]});
+                    S.info.push_back(info);
+                    S.rel.push_back(make_int4(L, nl, (int)(e - base), 0));
+                }
+        }
+        part.tri_start = first;
+        part.tri_count = (uint32_t)(S.idx.size() / 3) - first;
+        S.parts.push_back(part);
+    }
+    S.desc = me;
+    S.desc.positions = S.pos.data();
+    S.desc.normals = S.nrm.data();
+    S.desc.uvs = S.uv.data();
+    S.desc.colors = me.colors ? S.col.data() : nullptr;
+    S.desc.indices = S.idx.data();
+    S.desc.parts = S.parts.data();
+    S.desc.num_vertices = (uint32_t)(S.pos.size() / 3);
+    S.desc.num_triangles = (uint32_t)(S.idx.size() / 3);
+    if (!me.has_dimensions) {  // Dimensions stay those of the mesh before subdividing
+        S.desc.has_dimensions = 1;
+        for (int c = 0; c < 3; c++) { S.desc.dim_min[c] = 3.402823466e38f; S.desc.dim_max[c] = -3.402823466e38f; }
+        for (size_t v = 0; v < nv; v++)
+            for (int c = 0; c < 3; c++) {
+                const float p = me.positions[3 * v + c];
+                if (S.desc.dim_min[c] > p) S.desc.dim_min[c] = p;
+                if (S.desc.dim_max[c] < p) S.desc.dim_max[c] = p;
+            }
+    }
+}
+
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     if (!d || !out || (d->num_meshes && !d->meshes) || (d->num_models && !d->models) ||
         (d->num_lights && !d->lights) || (d->num_volume_cells && !d->volume_cells)) {
@@ -317,14 +456,66 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     }
     auto sc = std::make_unique<Scene>();
     uint64_t nv = 0, nt = 0, nshape = 0, nkeys_total = 0;
-    bool any_skin = false;
+    bool any_skin = false, any_subdiv = false;
+    // auto-subdivided meshes are expanded first; the rest of the upload reads eff[m]
+    const uint32_t nlev = d->subdivision_levels ? d->num_subdivision_levels : 0u;
+    const uint32_t maxsub = d->max_subdivisions ? d->max_subdivisions : 3u;
+    if (d->num_subdivision_levels && !d->subdivision_levels) {
+        set_err(ctx, "scene_upload: subdivision levels without their array");
+        return T3D_E_INVAL;
+    }
+    for (uint32_t i = 0; i < nlev; i++)
+        if (!(d->subdivision_levels[2 * i + 1] > 0.0f)) {  // the level loop halves MaxSpan down to this size
+            set_err(ctx, "subdivision level %u: MaximumTriangleSize must be positive", i);
+            return T3D_E_INVAL;
+        }
+    if (maxsub > 8) {
+        set_err(ctx, "scene_upload: max_subdivisions %u above 8", maxsub);
+        return T3D_E_INVAL;
+    }
+    std::vector<std::unique_ptr<SubdividedMesh>> subs(d->num_meshes);
+    std::vector<const t3d_mesh_desc*> eff(d->num_meshes);
     for (uint32_t m = 0; m < d->num_meshes; m++) {
         const t3d_mesh_desc& me = d->meshes[m];
+        eff[m] = &me;
+        if (!me.auto_subdivide || nlev == 0) continue;
+        if (!me.positions || !me.normals || !me.uvs || !me.indices || (me.num_parts && !me.parts)) {
+            set_err(ctx, "mesh %u: null stream", m);
+            return T3D_E_INVAL;
+        }
+        if (me.num_shape_keys) {  // the new vertices have no shape-key deltas in the reference either
+            set_err(ctx, "mesh %u: auto-subdivision together with shape keys", m);
+            return T3D_E_INVAL;
+        }
+        for (uint64_t t = 0; t < 3ull * me.num_triangles; t++)
+            if (me.indices[t] >= me.num_vertices) {
+                set_err(ctx, "mesh %u: index %u out of range (%u vertices)", m, me.indices[t], me.num_vertices);
+                return T3D_E_INVAL;
+            }
+        for (uint32_t p = 0; p < me.num_parts; p++)
+            if ((uint64_t)me.parts[p].tri_start + me.parts[p].tri_count > me.num_triangles) {
+                set_err(ctx, "mesh %u part %u: triangle range out of bounds", m, p);
+                return T3D_E_INVAL;
+            }
+        subs[m] = std::make_unique<SubdividedMesh>();
+        subdivide_mesh(me, d->subdivision_levels, nlev, maxsub, *subs[m]);
+        if (subs[m]->pos.size() / 3 > 0xFFFFFFF0ull || subs[m]->idx.size() / 3 > 0x50000000ull) {
+            set_err(ctx, "mesh %u: subdivided mesh too large for 32-bit indexing", m);
+            return T3D_E_INVAL;
+        }
+        subs[m]->desc.joints = nullptr;  // no skinning on subdivided meshes
+        subs[m]->desc.weights = nullptr;
+        eff[m] = &subs[m]->desc;
+        any_subdiv = true;
+    }
+    for (uint32_t m = 0; m < d->num_meshes; m++) {
+        const t3d_mesh_desc& me = *eff[m];
         if (!me.positions || !me.normals || !me.uvs || !me.indices || (me.num_parts && !me.parts)) {
             set_err(ctx, "mesh %u: null stream", m);
             return T3D_E_INVAL;
         }
         SceneMesh sm;
+        sm.subdiv = subs[m] != nullptr;
         sm.vbase = (uint32_t)nv;
         sm.tbase = (uint32_t)nt;
         sm.nverts = me.num_vertices;
@@ -411,7 +602,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
             set_err(ctx, "model %u: light list %d out of range", i, md.light_list);
             return T3D_E_INVAL;
         }
-        if (md.skinned && (!sc->meshes[md.mesh].skin ||
+        if (md.skinned && (!sc->meshes[md.mesh].skin || sc->meshes[md.mesh].subdiv ||
                            (uint64_t)md.bone_first + sc->meshes[md.mesh].max_joint >= d->num_bones)) {
             set_err(ctx, "model %u: skinned without joints or with bones beyond the %u scene bones", i, d->num_bones);
             return T3D_E_INVAL;
@@ -460,8 +651,13 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         (rc = sc->shape_w.ensure(ctx, 4 * std::max<uint64_t>(1, nkeys_total))) ||
         (rc = sc->vjoint.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
         (rc = sc->vweight.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
-        (rc = sc->bones.ensure(ctx, 64 * std::max<size_t>(1, d->num_bones))))
+        (rc = sc->bones.ensure(ctx, 64 * std::max<size_t>(1, d->num_bones))) ||
+        (rc = sc->sub_info.ensure(ctx, 16 * (any_subdiv ? std::max<uint64_t>(1, nt) : 1))) ||
+        (rc = sc->sub_rel.ensure(ctx, 16 * (any_subdiv ? std::max<uint64_t>(1, nt) : 1))) ||
+        (rc = sc->sub_levels.ensure(ctx, 8 * std::max<uint32_t>(1, nlev))))
         return rc;
+    sc->num_sub_levels = nlev;
+    if (nlev) CK(cudaMemcpy(sc->sub_levels.ptr, d->subdivision_levels, 8ull * nlev, cudaMemcpyHostToDevice));
     if (d->num_bones && !d->bones) {
         set_err(ctx, "scene_upload: num_bones without bone matrices");
         return T3D_E_INVAL;
@@ -472,7 +668,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     std::vector<float4> a, b, c;
     std::vector<float> ctr;
     for (uint32_t m = 0; m < d->num_meshes; m++) {
-        const t3d_mesh_desc& me = d->meshes[m];
+        const t3d_mesh_desc& me = *eff[m];
         a.resize(me.num_vertices); b.resize(me.num_vertices); c.resize(me.num_vertices);
         for (uint32_t v = 0; v < me.num_vertices; v++) {
             const float* p = me.positions + 3 * (size_t)v;
@@ -494,12 +690,21 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         CK(cudaMemcpy((char*)sc->idx.ptr + (size_t)sc->meshes[m].tbase * 12, me.indices, me.num_triangles * 12ull,
                       cudaMemcpyHostToDevice));
         // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis in binary32
-        ctr.resize(3ull * me.num_triangles);
-        for (uint32_t t = 0; t < me.num_triangles; t++) {
-            const float* pa = me.positions + 3 * (size_t)me.indices[3 * (size_t)t];
-            const float* pb = me.positions + 3 * (size_t)me.indices[3 * (size_t)t + 1];
-            const float* pc = me.positions + 3 * (size_t)me.indices[3 * (size_t)t + 2];
-            for (int k = 0; k < 3; k++) ctr[3 * (size_t)t + k] = (pa[k] + pb[k] + pc[k]) / 3.0f;
+        if (subs[m]) {  // subdivided triangles carry their own centres (mesh.go:1821-1845)
+            ctr = subs[m]->ctr;
+            const size_t tb = sc->meshes[m].tbase;
+            CK(cudaMemcpy((float4*)sc->sub_info.ptr + tb, subs[m]->info.data(), 16ull * me.num_triangles,
+                          cudaMemcpyHostToDevice));
+            CK(cudaMemcpy((int4*)sc->sub_rel.ptr + tb, subs[m]->rel.data(), 16ull * me.num_triangles,
+                          cudaMemcpyHostToDevice));
+        } else {
+            ctr.resize(3ull * me.num_triangles);
+            for (uint32_t t = 0; t < me.num_triangles; t++) {
+                const float* pa = me.positions + 3 * (size_t)me.indices[3 * (size_t)t];
+                const float* pb = me.positions + 3 * (size_t)me.indices[3 * (size_t)t + 1];
+                const float* pc = me.positions + 3 * (size_t)me.indices[3 * (size_t)t + 2];
+                for (int k = 0; k < 3; k++) ctr[3 * (size_t)t + k] = (pa[k] + pb[k] + pc[k]) / 3.0f;
+            }
         }
         CK(cudaMemcpy((char*)sc->centers.ptr + (size_t)sc->meshes[m].tbase * 12, ctr.data(), me.num_triangles * 12ull,
                       cudaMemcpyHostToDevice));
@@ -649,6 +854,11 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.vjoint = (const uint4*)sc->vjoint.ptr;
         dj.vweight = (const float4*)sc->vweight.ptr;
         dj.bones = (const float4*)sc->bones.ptr;
+        dj.sub_info = (const float4*)sc->sub_info.ptr;
+        dj.sub_rel = (const int4*)sc->sub_rel.ptr;
+        dj.sub_levels = (const float*)sc->sub_levels.ptr;
+        dj.nsub_levels = sc->num_sub_levels;
+        dj.pad_sub = 0;
         const uint32_t light_base = (uint32_t)F.lights.size();
         for (const auto& l : sc->lights) {
             DevLight L;
@@ -737,8 +947,9 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (is_transparent(m.d.color, mat)) flags |= SEG_TRANSPARENT;
             if (m.d.skinned) { flags |= SEG_SKINNED; F.any_skinned = true; }
             if (me.nkeys) flags |= SEG_SHAPES;
+            if (me.subdiv) flags |= SEG_SUBDIV;
             flags |= billboard_flags(mat, m.d.skinned != 0);
-            if (flags & SEG_ALTERED) F.any_altered = true;
+            if (flags & (SEG_ALTERED | SEG_ALT_TILES)) F.any_altered = true;
             uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
             flags |= sort_mode << 8;
             flags |= (uint32_t)(mat.present ? mat.lighting_mode : 0) << 10;
@@ -826,7 +1037,7 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
     for (int pass = 0; pass < 2; pass++) {
         for (uint32_t s = 0; s < nseg; s++) {
             const DevSeg& sg = F.segs[s];
-            if (((sg.flags & SEG_SKINNED) != 0) == (pass == 1)) {
+            if (((sg.flags & SEG_ALT_TILES) != 0) == (pass == 1)) {
                 new_tile[s] = (uint32_t)tiles.size();
                 tiles.insert(tiles.end(), F.tiles.begin() + sg.tile_first, F.tiles.begin() + sg.tile_first + sg.ntiles);
             }
@@ -1016,7 +1227,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
         P.vitem_begin = F.seg_vitem_first[s];
         P.vitem_end = P.vitem_begin + (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
-        P.tile_alt = (sg.flags & SEG_SKINNED) ? P.tile_begin : P.tile_end;
+        P.tile_alt = (sg.flags & SEG_ALT_TILES) ? P.tile_begin : P.tile_end;
         P.vitem_alt = (sg.flags & SEG_ALTERED) ? P.vitem_begin : P.vitem_end;
         if (sg.flags & SEG_MULTI) {
             P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles;

@@ -41,6 +41,7 @@ struct SceneMesh {
     uint32_t nkeys = 0, shape_first = 0, weight_first = 0;  // shape keys
     bool skin = false;                                      // joints and weights present
     uint32_t max_joint = 0;
+    bool subdiv = false;  // auto-subdivided: parts list each triangle followed by its subdivision levels
 };
 struct SceneModel {
     t3d_model_desc d;  // host mirror (rotation advanced with every animated frame)
@@ -56,12 +57,15 @@ struct Scene {
     uint64_t struct_ver = 0, model_ver = 0;
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     DevBuf shape_a, shape_b, shape_w, vjoint, vweight, bones;
-    uint32_t num_bones = 0, num_keys = 0;
+    DevBuf sub_info, sub_rel, sub_levels;
+    uint32_t num_bones = 0, num_keys = 0, num_sub_levels = 0;
     uint64_t device_bytes() const {
         return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap +
-               shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap;
+               shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap + sub_info.cap + sub_rel.cap +
+               sub_levels.cap;
     }
     void release() {
+        sub_info.release(); sub_rel.release(); sub_levels.release();
         shape_a.release(); shape_b.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
         va.release(); vb.release(); vc.release(); idx.release(); centers.release();
         dmeshes.release(); dmodels.release(); cells.release();

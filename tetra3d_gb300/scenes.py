@@ -166,6 +166,7 @@ class MeshData:
         self.dims = dims  # None: UpdateDimensions
         self.shape_positions = self.shape_normals = self.shape_weights = None
         self.joints = self.weights = None
+        self.auto_subdivide = 0  # Mesh.SetAutoSubdivide
 
     @property
     def nverts(self):
@@ -346,6 +347,8 @@ class SceneData:
         self.ncells = 0 if cells is None else len(cells)
         self.camera = None
         self.bones = None  # (NB, 16) Node.boneInfluence matrices
+        self.subdivision_levels = None  # (L, 2) AutoSubdivisionLevel: DistanceSquared, MaximumTriangleSize
+        self.max_subdivisions = 0       # Library.maxAutoSubdivisionCount (0: 3)
         self.meta = {}
         self._keep = []
 
@@ -383,6 +386,7 @@ class SceneData:
                 keep += [sp, sn, sw]
                 d.shape_positions, d.shape_normals, d.shape_weights = abi.fptr(sp), abi.fptr(sn), abi.fptr(sw)
                 d.num_shape_keys = len(sw)
+            d.auto_subdivide = int(m.auto_subdivide)
             if m.joints is not None:
                 jt = np.ascontiguousarray(m.joints, np.uint32)
                 wt = np.ascontiguousarray(m.weights, F32)
@@ -406,6 +410,11 @@ class SceneData:
             bones = np.ascontiguousarray(self.bones, F32).reshape(-1, 16)
             keep.append(bones)
             sd.bones, sd.num_bones = abi.fptr(bones), bones.shape[0]
+        if self.subdivision_levels is not None and len(self.subdivision_levels):
+            lev = np.ascontiguousarray(self.subdivision_levels, F32).reshape(-1, 2)
+            keep.append(lev)
+            sd.subdivision_levels, sd.num_subdivision_levels = abi.fptr(lev), lev.shape[0]
+        sd.max_subdivisions = int(self.max_subdivisions)
         self._keep = keep
         return sd
 
@@ -887,6 +896,57 @@ def billboard_scene(seed=9, n=40, w=1280, h=720):
     return sd
 
 
+SUBDIVISION_LEVELS = [(36.0, 0.6), (144.0, 1.2), (576.0, 3.0)]  # (DistanceSquared, MaximumTriangleSize)
+
+
+def subdivision_scene(seed=10, n=24, w=1280, h=720, max_subdivisions=3):
+    """Auto-subdivided meshes (Mesh.SetAutoSubdivide) seen from 2 to 40 units away, so each draws
+    its base triangles or one of three subdivision levels, next to the same meshes unsubdivided.
+
+    Meshes: a coarse noise grid (large triangles), an icosahedron scaled up, a cube with vertex colours
+    and two parts, each once with auto-subdivision on and once off. Levels: SUBDIVISION_LEVELS; some
+    triangles are shorter than the smallest size (never subdivided) and some stop subdividing before
+    the last level (empty deeper lists).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = feature_scene(seed, n=4)
+    meshes = []
+    sseed = int(rng.integers(1 << 30))
+    grid = grid_mesh(6, 5, 6.0, 5.0, lambda X, Z, s=sseed: 0.8 * value_noise(s, X, Z, 2), x0=-3.0, z0=-2.5)
+    grid.colors = rng.uniform(0.4, 1.0, (grid.nverts, 4)).astype(F32)
+    ico = icosphere(0)
+    ico.positions = (ico.positions * F32(2.5)).astype(F32)
+    cube = cube_mesh(3.0, 0.5, 2.0)
+    cube.colors = rng.uniform(0.4, 1.0, (cube.nverts, 4)).astype(F32)
+    for b in (grid, ico, cube):
+        T = b.ntris
+        cut = int(rng.integers(1, T))
+        for sub in (1, 0):
+            m = MeshData(b.positions, b.normals, b.uvs, b.indices, colors=b.colors,
+                         parts=[dict(tri_start=0, tri_count=cut, mat=_random_material(rng)),
+                                dict(tri_start=cut, tri_count=T - cut, mat=_random_material(rng))])
+            for p in m.parts:
+                p["mat"].update(present=1, visible=1)
+            m.auto_subdivide = sub
+            meshes.append(m)
+    dist = rng.uniform(2.0, 40.0, n)
+    dirs = unit3(np.stack([rng.uniform(-0.5, 0.5, n), rng.uniform(-0.3, 0.3, n), -np.ones(n)], 1).astype(F32))
+    pos = (dirs * dist[:, None].astype(F32)).astype(F32)
+    mesh_of = rng.integers(0, len(meshes), n).astype(np.uint32)
+    mesh_of[:len(meshes)] = np.arange(len(meshes))
+    scl = np.repeat(rng.uniform(0.7, 1.5, (n, 1)), 3, 1).astype(F32)
+    rot = quat_to_mat(random_quats(rng, n))
+    sd = SceneData(meshes, n, [base.lights[i] for i in range(base.nlights)], base.lists,
+                   cells=base.cells[:base.ncells] if base.ncells else None, name=f"subdivision{seed}")
+    set_models_trs(sd, mesh_of, pos, scl, rot,
+                   light_list=np.where(rng.random(n) < 0.5, -1, rng.integers(1, 4, n)).astype(np.int32))
+    sd.mv["frustum_culling"] = (rng.random(n) < 0.7).astype(np.int32)
+    sd.subdivision_levels = np.array(SUBDIVISION_LEVELS, F32)
+    sd.max_subdivisions = max_subdivisions
+    sd.camera = feature_camera("persp", w, h)
+    return sd
+
+
 def down_camera(w=1280, h=720):
     """A camera at (0, 10, 0) looking straight down -Y."""
     return camera(pos=(0.0, 10.0, 0.0), rot=rotate(1, 0, 0, deg2rad(-90.0)), w=w, h=h, fov=70.0, near=0.1, far=60.0)
@@ -938,4 +998,6 @@ def subset(sd, models):
     out.mv[:] = sd.mv[models]
     out.camera = sd.camera
     out.bones = sd.bones
+    out.subdivision_levels = sd.subdivision_levels
+    out.max_subdivisions = sd.max_subdivisions
     return out
