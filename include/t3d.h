@@ -261,7 +261,7 @@ typedef struct t3d_camera_desc {
     int32_t max_light_count;
     int32_t focus_set;           /* MaxLightCountFocusPoint != nil */
     float   focus[3];            /* its WorldPosition(); otherwise the camera's is used */
-    float   reserved;
+    float   vertex_snapping;     /* Camera.VertexSnapping: > 0 rounds clip X, Y, Z to this grid (model.go:813-818) */
 } t3d_camera_desc;
 
 /* One unit of rendering work: one camera over one resident scene, optionally

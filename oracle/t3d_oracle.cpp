@@ -828,6 +828,12 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
             uint32_t v = vidx[vi];
             altered_vertex<R>(sc, md, me, v, S.apos[v], S.anrm[v]);
             S.clip[v] = mult_vec_w(mvp, S.apos[v]);  // model.go:808-811
+            if (cd->vertex_snapping > 0) {  // model.go:813-818
+                const R snap = (R)cd->vertex_snapping;
+                S.clip[v].x = m_round<R>(S.clip[v].x * snap) / snap;
+                S.clip[v].y = m_round<R>(S.clip[v].y * snap) / snap;
+                S.clip[v].z = m_round<R>(S.clip[v].z * snap) / snap;
+            }
             if (unbillboarded) S.udepth[v] = mult_vec_w(unalteredMVP, S.apos[v]).z;  // model.go:800-801
         }
         bool outOfBounds = true;  // model.go:855-886

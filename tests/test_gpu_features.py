@@ -440,3 +440,19 @@ def test_subdivision_argument_errors(ctx):
     bad.max_subdivisions = 9
     d = bad.desc()
     assert lib.t3d_scene_upload(ctx.h, C.byref(d), C.byref(out)) == abi.T3D_E_INVAL
+
+
+@pytest.mark.parametrize("variant", ["persp", "ortho", "fog_sub"])
+def test_vertex_snapping_matches_oracle(ctx, variant):
+    """Camera.VertexSnapping on the feature and billboard scenes, both forms."""
+    for sd in (scenes.feature_scene(5), scenes.billboard_scene(9)):
+        cam = scenes.feature_camera(variant)
+        cam.vertex_snapping = 8.0
+        ref = pyoracle.render(sd, cam)
+        sid = ctx.upload(sd)
+        try:
+            for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+                ctx.render(sid, cam, mode=mode)
+                assert_frames_equal(ctx.download(), ref, f"snap/{sd.name}/{variant}/mode{mode}")
+        finally:
+            ctx.release(sid)

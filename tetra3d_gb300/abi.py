@@ -89,7 +89,7 @@ class CameraDesc(C.Structure):
                 ("fog_on", C.c_int32), ("fog_mode", C.c_int32), ("fov_y", C.c_float), ("near_plane", C.c_float),
                 ("far_plane", C.c_float), ("ortho_scale", C.c_float), ("depth_margin", C.c_float),
                 ("fog_range", C.c_float * 2), ("fog_color", C.c_float * 4), ("max_light_count", C.c_int32),
-                ("focus_set", C.c_int32), ("focus", C.c_float * 3), ("reserved", C.c_float)]
+                ("focus_set", C.c_int32), ("focus", C.c_float * 3), ("vertex_snapping", C.c_float)]
 
 
 class JobDesc(C.Structure):

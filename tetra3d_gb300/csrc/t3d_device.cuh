@@ -41,10 +41,11 @@ enum : uint32_t {
     SEG_BB_CAMUP = 1u << 20,    // BillboardUpDirection == BillboardYUpCameraY
     SEG_UNBB = 1u << 21,        // BillboardedDepthMode == DepthModeUnbillboarded on a billboard
     SEG_SUBDIV = 1u << 22,      // auto-subdivided mesh: triangles are candidates of a subdivision level
+    SEG_SNAP = 1u << 23,        // Camera.VertexSnapping > 0
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
-    SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD,
+    SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD | SEG_SNAP,
 };
 constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }
@@ -101,7 +102,7 @@ struct JobCam {
     float sphere_tang, sphere_y, sphere_x, aspect;
     float near_, far_, W, H;
     float halfW, halfH, margin, spread;
-    float ortho_scale, pad0;
+    float ortho_scale, snap;  // snap: Camera.VertexSnapping
     float fog_range[2];
     float fog_color[4];
     int32_t perspective, render_depth, persp_correct, fog_on;

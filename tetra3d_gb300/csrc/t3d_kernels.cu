@@ -334,7 +334,7 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
 //   ModelSmem | TileSmem | whist[nwarps][kBins] | lidx u16[T] | depth f32[T] | bin u16[T]
 // Per work item constants of the emit path (camera, segment and stream bases).
 enum : uint32_t { EC_PERSP = 1, EC_PCORRECT = 2, EC_DEPTH = 4, EC_RDEPTH = 8, EC_FOG_ADD = 16, EC_FOG_SUB = 32,
-                  EC_LIT = 64, EC_COLORS = 128, EC_UNBB = 256 };
+                  EC_LIT = 64, EC_COLORS = 128, EC_UNBB = 256, EC_SNAP = 512 };
 struct EmitConst {
     float W, H, halfW, halfH;
     float margin, spread, tex_w, tex_h;
@@ -343,6 +343,7 @@ struct EmitConst {
     float fog_b;
     uint32_t flags, seg_flags, pad;
     float uz[4];             // EC_UNBB: depth row of the unbillboarded MVP (model.go:700-803)
+    float snap, pad2[3];     // EC_SNAP: Camera.VertexSnapping
     const float4* va;        // vertex streams of the mesh (mesh vertex 0)
     const float4* vb;
     const float4* vc;
@@ -432,6 +433,10 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
         if (!cam.render_depth && cam.fog_on && cam.fog_mode == T3D_FOG_SUB) f |= EC_FOG_SUB;
         if (seg.flags & SEG_LIT) f |= EC_LIT;
         if (seg.flags & SEG_COLORS) f |= EC_COLORS;
+        if (kSkin && (seg.flags & SEG_SNAP)) {
+            f |= EC_SNAP;
+            e.snap = cam.snap;
+        }
         if (bb) {  // billboarded MVP of this part (model.go:634-695)
             const m4 base = billboard_base(load16(pr.M), mk3(cam.pos[0], cam.pos[1], cam.pos[2]),
                                            (seg.flags & SEG_BB_CAMUP) ? mk3(cam.up[0], cam.up[1], cam.up[2])
@@ -529,7 +534,12 @@ __device__ __forceinline__ void vertex_record(const ModelSmem& ms, const float4 
                                               float4& cull, float4& xyuv, float4& rgba) {
     const EmitConst& e = ms.ec;
     const uint32_t f = e.flags;
-    const float4 c = clip_of(ms.mvpc, a.x, a.y, a.z);
+    float4 c = clip_of(ms.mvpc, a.x, a.y, a.z);
+    if (kSkin && (f & EC_SNAP)) {  // VertexSnapping (model.go:813-818): math32.Round = round half away from zero
+        c.x = roundf(c.x * e.snap) / e.snap;
+        c.y = roundf(c.y * e.snap) / e.snap;
+        c.z = roundf(c.z * e.snap) / e.snap;
+    }
     const float w1 = c.w < 0.0f ? 0.000001f : c.w;
     const float cx = c.x / w1, cy = c.y / w1;
     float w = c.w;

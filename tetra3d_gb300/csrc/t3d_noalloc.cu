@@ -317,6 +317,7 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     flags |= (uint32_t)(mat.present ? mat.lighting_mode & 3 : 0) << 10;
     flags |= (uint32_t)(mat.present ? mat.lv_shading_mode & 3 : 0) << 12;
     flags |= billboard_flags(mat, false);
+    if (a->camera->vertex_snapping > 0.0f) flags |= SEG_SNAP;
     sg.flags = flags;
     for (int k = 0; k < 4; k++) sg.mp[k] = mat.present ? md.color[k] * mat.color[k] : md.color[k];
     sg.tex_w = mat.present ? mat.tex_w : 0.0f;

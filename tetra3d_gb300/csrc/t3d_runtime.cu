@@ -267,6 +267,7 @@ void build_camera(const t3d_camera_desc& d, JobCam& c) {
     c.margin = (fr - nr) * d.depth_margin;
     c.spread = fr - nr + (c.margin * 2.0f);
     c.ortho_scale = d.ortho_scale;
+    c.snap = d.vertex_snapping > 0.0f ? d.vertex_snapping : 0.0f;
     c.fog_range[0] = d.fog_range[0]; c.fog_range[1] = d.fog_range[1];
     for (int i = 0; i < 4; i++) c.fog_color[i] = d.fog_color[i];
     c.perspective = d.perspective; c.render_depth = d.render_depth; c.persp_correct = d.perspective_corrected;
@@ -949,6 +950,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (me.nkeys) flags |= SEG_SHAPES;
             if (me.subdiv) flags |= SEG_SUBDIV;
             flags |= billboard_flags(mat, m.d.skinned != 0);
+            if (cd.vertex_snapping > 0.0f) flags |= SEG_SNAP;
             if (flags & (SEG_ALTERED | SEG_ALT_TILES)) F.any_altered = true;
             uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
             flags |= sort_mode << 8;
