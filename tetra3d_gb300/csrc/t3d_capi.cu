@@ -62,7 +62,8 @@ int t3d_create(int device, t3d_ctx** out) {
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_models, cudaEventDisableTiming) != cudaSuccess) {
         delete ctx;
         return T3D_E_CUDA;
     }
@@ -86,6 +87,8 @@ int t3d_destroy(t3d_ctx* ctx) {
     if (!ctx) return T3D_E_INVAL;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
+    if (ctx->ev_models) cudaEventSynchronize(ctx->ev_models);
     drop_graph(ctx);
     for (auto& kv : ctx->scenes) kv.second->release();
     ctx->scenes.clear();
@@ -97,6 +100,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     ctx->readback.release();
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
+    if (ctx->ev_models) cudaEventDestroy(ctx->ev_models);
     t3d_raster_release(ctx);
     ctx->model_host.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -175,7 +179,7 @@ int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d
         }
     }
     cudaSetDevice(ctx->device);
-    if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
+    // no host wait: the copy is queued behind the frames already issued (scene_write_models)
     return scene_write_models(ctx, sc, first, models, n);
 }
 
@@ -187,6 +191,7 @@ int t3d_scene_get_transforms(t3d_ctx* ctx, uint32_t scene, float* out, uint32_t 
     n = std::min<uint32_t>(n, (uint32_t)sc->models.size());
     cudaSetDevice(ctx->device);
     if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    if (ctx->ev_models) CKR(cudaEventSynchronize(ctx->ev_models));
     std::vector<DevModel> dm(n);
     if (n) CKR(cudaMemcpy(dm.data(), sc->dmodels.ptr, sizeof(DevModel) * n, cudaMemcpyDeviceToHost));
     for (uint32_t i = 0; i < n; i++) {
@@ -255,6 +260,10 @@ int t3d_render_jobs(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t num_jobs, i
     cudaSetDevice(ctx->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     if (ctx->last_stream && ctx->last_stream != st) CKR(cudaStreamSynchronize(ctx->last_stream));
+    {  // model writes to the scenes come first (a serving slot's scenes belong to its parent)
+        t3d_ctx* owner = ctx->scene_owner ? ctx->scene_owner : ctx;
+        if (owner->ev_models) CKR(cudaStreamWaitEvent(st, owner->ev_models, 0));
+    }
     ctx->frame_valid = false;
     // The launch tables depend on the jobs, the tuning and the scenes' structure,
     // and on model transforms only through the draw order of transparent pairs (or
@@ -433,6 +442,7 @@ int t3d_graph_capture(t3d_ctx* ctx, uint32_t scene, const t3d_camera_desc* cam, 
     job.light_mask[0] = job.light_mask[1] = ~0ull;
     job.camera = *cam;
     if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    if (ctx->ev_models) CKR(cudaEventSynchronize(ctx->ev_models));
     ctx->tables_ok = false;  // the arena now holds the captured frame's tables
     int rc = build_frame(ctx, &job, 1, animate);
     if (rc) return rc;
@@ -471,6 +481,7 @@ int t3d_graph_replay(t3d_ctx* ctx, uint32_t frames, void* stream) {
     }
     cudaSetDevice(ctx->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    if (ctx->ev_models) CKR(cudaStreamWaitEvent(st, ctx->ev_models, 0));
     for (uint32_t f = 0; f < frames; f++) CKR(cudaGraphLaunch(ctx->graph_exec, st));
     ctx->last_stream = st;
     ctx->frame_pending = true;

@@ -770,8 +770,14 @@ static bool same_model_structure(const t3d_model_desc& a, const t3d_model_desc& 
            a.skinned == b.skinned && a.bone_first == b.bone_first && memcmp(a.color, b.color, sizeof a.color) == 0;
 }
 
+// Model writes are asynchronous: the copy is queued on the stream of the last
+// render, behind the frames already issued (which read the previous models),
+// and ev_models marks its completion; the next render waits on it on the
+// device, and the next write waits on it on the host before reusing the
+// pinned staging buffer.
 int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n) {
     if (n == 0) return T3D_OK;
+    if (ctx->ev_models) CK(cudaEventSynchronize(ctx->ev_models));
     if (ctx->model_host.ensure(sizeof(DevModel) * n)) {
         set_err(ctx, "pinned model staging alloc failed");
         return T3D_E_OOM;
@@ -796,9 +802,11 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
         if (!structure && !same_model_structure(sc->models[first + i].d, md)) structure = true;
         sc->models[first + i].d = md;
     }
+    cudaStream_t st = ctx->last_stream ? ctx->last_stream : ctx->stream;
     CK(cudaMemcpyAsync((char*)sc->dmodels.ptr + sizeof(DevModel) * first, dv, sizeof(DevModel) * n,
-                       cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+                       cudaMemcpyHostToDevice, st));
+    if (ctx->ev_models) CK(cudaEventRecord(ctx->ev_models, st));
+    else CK(cudaStreamSynchronize(st));
     if (structure) sc->struct_ver = next_version();
     sc->model_ver = next_version();
     return T3D_OK;

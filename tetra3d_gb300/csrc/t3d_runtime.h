@@ -126,6 +126,7 @@ struct t3d_ctx {
     bool tables_ok = false;
     bool order_dep = true;   // the draw order depends on model transforms (transparents, depth off)
     cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
+    cudaEvent_t ev_models = nullptr;  // the last model write has reached the device (and left its staging)
     struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
     t3d::DevBuf valt;
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
