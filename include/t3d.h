@@ -348,6 +348,11 @@ int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out);
 int t3d_scene_set_bones(t3d_ctx* ctx, uint32_t scene, uint32_t first, const float* influences, uint32_t n);
 /* Shape-key weights of one mesh of a scene (ShapeKey.weight, mesh.go). */
 int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, const float* weights, uint32_t n);
+/* Lights [first, first + n) of a scene: moved, recoloured, re-ranged or of another
+ * kind, as Camera.Render reads them anew every frame (camera.go:1269-1300,
+ * light.go beginRender). The next render rebuilds its light tables; a
+ * captured graph is dropped (capture again). */
+int t3d_scene_set_lights(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d_light_desc* lights, uint32_t n);
 
 /* ---- rendering --------------------------------------------------------------- */
 /* Camera.Render over one scene: enqueue on `stream` (a cudaStream_t, NULL =

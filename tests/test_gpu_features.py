@@ -456,3 +456,35 @@ def test_vertex_snapping_matches_oracle(ctx, variant):
                 assert_frames_equal(ctx.download(), ref, f"snap/{sd.name}/{variant}/mode{mode}")
         finally:
             ctx.release(sid)
+
+
+def test_set_lights_between_frames(ctx):
+    """Lights moved, recoloured, re-ranged and switched off (energy 0) between frames, with and
+    without MaxLightCount; the launch tables are rebuilt and every frame matches the oracle."""
+    sd = scenes.feature_scene(6)
+    cam = scenes.feature_camera("persp")
+    rng = np.random.default_rng(5)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), "initial")
+        for step in range(3):
+            for i in range(sd.nlights):
+                L = sd.lights[i]
+                if L.type == abi.LIGHT_POINT:
+                    L.transform[12] += float(rng.uniform(-3, 3))
+                    L.transform[14] += float(rng.uniform(-3, 3))
+                    L.range = float(rng.uniform(5, 25))
+                L.color[0] = float(rng.uniform(0.2, 1.0))
+                L.energy = float(rng.uniform(0.0, 2.0)) if step < 2 else 0.0
+            first = 1 if step == 1 else 0
+            ctx.set_lights(sid, sd, first=first, n=sd.nlights - first)
+            cam.max_light_count = 4 if step == 1 else 0
+            ctx.render(sid, cam)
+            assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), f"lights step {step}")
+        bad = (abi.LightDesc * 1)(sd.lights[0])
+        bad[0].type = 7
+        assert ctx.lib.t3d_scene_set_lights(ctx.h, sid, 0, bad, 1) == abi.T3D_E_INVAL
+        assert ctx.lib.t3d_scene_set_lights(ctx.h, sid, sd.nlights, bad, 1) == abi.T3D_E_INVAL
+    finally:
+        ctx.release(sid)

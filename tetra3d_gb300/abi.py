@@ -151,6 +151,7 @@ SIGNATURES = {
     "t3d_scene_get_transforms": (C.c_int, [_VP, C.c_uint32, f32p, C.c_uint32]),
     "t3d_scene_bytes": (C.c_int, [_VP, C.c_uint32, C.POINTER(C.c_uint64)]),
     "t3d_scene_set_bones": (C.c_int, [_VP, C.c_uint32, C.c_uint32, f32p, C.c_uint32]),
+    "t3d_scene_set_lights": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.POINTER(LightDesc), C.c_uint32]),
     "t3d_scene_set_shape_weights": (C.c_int, [_VP, C.c_uint32, C.c_uint32, f32p, C.c_uint32]),
     "t3d_render": (C.c_int, [_VP, C.c_uint32, C.POINTER(CameraDesc), C.c_int, C.c_int, _VP]),
     "t3d_render_jobs": (C.c_int, [_VP, C.POINTER(JobDesc), C.c_uint32, C.c_int, C.c_int, _VP]),

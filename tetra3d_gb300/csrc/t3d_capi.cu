@@ -239,6 +239,40 @@ int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, con
     return T3D_OK;
 }
 
+int t3d_scene_set_lights(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d_light_desc* lights, uint32_t n) {
+    if (!ctx || (n && !lights)) return T3D_E_INVAL;
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return T3D_E_NOTFOUND;
+    Scene* sc = it->second.get();
+    if ((uint64_t)first + n > sc->lights.size()) {
+        set_err(ctx, "set_lights: range [%u, %u) beyond %zu lights", first, first + n, sc->lights.size());
+        return T3D_E_INVAL;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        const t3d_light_desc& l = lights[i];
+        if (l.type < 0 || l.type > 3) {
+            set_err(ctx, "set_lights: light %u has bad type %d", first + i, l.type);
+            return T3D_E_INVAL;
+        }
+        if (l.type == T3D_LIGHT_VOLUME) {
+            const uint64_t cells = (uint64_t)std::max(0, l.cell_count[0]) * std::max(0, l.cell_count[1]) *
+                                   std::max(0, l.cell_count[2]);
+            if ((uint64_t)l.cell_first + cells > sc->num_cells) {
+                set_err(ctx, "set_lights: light %u: volume cells out of range", first + i);
+                return T3D_E_INVAL;
+            }
+        }
+    }
+    cudaSetDevice(ctx->device);
+    // the light tables of frames in flight are already on the device; the next
+    // render builds new ones, so only a captured graph (which keeps its tables) goes
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    drop_graph(ctx);
+    for (uint32_t i = 0; i < n; i++) sc->lights[first + i] = lights[i];
+    sc->struct_ver = next_version();
+    return T3D_OK;
+}
+
 int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out) {
     if (!ctx || !bytes_out) return T3D_E_INVAL;
     auto it = ctx->scenes.find(scene);

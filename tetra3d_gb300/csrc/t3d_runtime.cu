@@ -664,6 +664,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         return T3D_E_INVAL;
     }
     sc->num_bones = d->num_bones;
+    sc->num_cells = d->num_volume_cells;
     sc->num_keys = (uint32_t)nkeys_total;
     if (d->num_bones) CK(cudaMemcpy(sc->bones.ptr, d->bones, 64ull * d->num_bones, cudaMemcpyHostToDevice));
     std::vector<float4> a, b, c;

@@ -58,7 +58,7 @@ struct Scene {
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     DevBuf shape_a, shape_b, shape_w, vjoint, vweight, bones;
     DevBuf sub_info, sub_rel, sub_levels;
-    uint32_t num_bones = 0, num_keys = 0, num_sub_levels = 0;
+    uint32_t num_bones = 0, num_keys = 0, num_sub_levels = 0, num_cells = 0;
     uint64_t device_bytes() const {
         return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap +
                shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap + sub_info.cap + sub_rel.cap +
@@ -152,6 +152,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out);
 int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_desc* models, uint32_t n);
 int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int animate);
 uint32_t billboard_flags(const t3d_material& mat, bool skinned);
+uint64_t next_version();
 int upload_frame(t3d_ctx* ctx, cudaStream_t st);
 int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st);
 int configure(t3d_ctx* ctx);

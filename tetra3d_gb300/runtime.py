@@ -76,6 +76,12 @@ class Context:
         b = np.ascontiguousarray(bones, np.float32).reshape(-1, 16)
         self._check(self.lib.t3d_scene_set_bones(self.h, sid, first, abi.fptr(b), b.shape[0]), "scene_set_bones")
 
+    def set_lights(self, sid, scene_data, first=0, n=None):
+        """Lights [first, first + n) of the scene from scene_data.lights."""
+        n = scene_data.nlights - first if n is None else n
+        ptr = C.cast(C.byref(scene_data.lights, first * C.sizeof(abi.LightDesc)), C.POINTER(abi.LightDesc))
+        self._check(self.lib.t3d_scene_set_lights(self.h, sid, first, ptr, n), "scene_set_lights")
+
     def set_shape_weights(self, sid, mesh, weights):
         w = np.ascontiguousarray(weights, np.float32).reshape(-1)
         self._check(self.lib.t3d_scene_set_shape_weights(self.h, sid, mesh, abi.fptr(w), w.shape[0]),
