@@ -469,7 +469,8 @@ def test_set_lights_between_frames(ctx):
         ctx.render(sid, cam)
         assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), "initial")
         for step in range(3):
-            for i in range(sd.nlights):
+            first = 1 if step == 1 else 0  # step 1 pushes (and changes) lights 1.. only
+            for i in range(first, sd.nlights):
                 L = sd.lights[i]
                 if L.type == abi.LIGHT_POINT:
                     L.transform[12] += float(rng.uniform(-3, 3))
@@ -477,7 +478,6 @@ def test_set_lights_between_frames(ctx):
                     L.range = float(rng.uniform(5, 25))
                 L.color[0] = float(rng.uniform(0.2, 1.0))
                 L.energy = float(rng.uniform(0.0, 2.0)) if step < 2 else 0.0
-            first = 1 if step == 1 else 0
             ctx.set_lights(sid, sd, first=first, n=sd.nlights - first)
             cam.max_light_count = 4 if step == 1 else 0
             ctx.render(sid, cam)
