@@ -186,6 +186,16 @@ typedef struct t3d_model_desc {
      * transform still places its frustum sphere and its point-light range test. */
     int32_t  skinned;
     uint32_t bone_first;       /* the mesh's joint j uses scene bone bone_first + j */
+    /* Dynamic batching (Model.DynamicBatchAdd, model.go:210-245): batched = 1 makes this
+     * model a member of model batch_owner's batch under that model's mesh part
+     * batch_part. Members draw only inside the batch: in the owner's place in the draw
+     * order, sorted far to near from the camera, each with its own frustum culling and
+     * all of its parts, in one flush (camera.go:1343-1457, :2068-2093); an owner draws
+     * no mesh of its own. */
+    int32_t  batched;
+    uint32_t batch_owner;
+    uint32_t batch_part;
+    uint32_t reserved;
 } t3d_model_desc;
 
 /* A light (light.go). transform = the light node's Transform(), world_rotation =
@@ -302,6 +312,8 @@ typedef struct t3d_segment_info {
     uint32_t base;           /* triangle slot */
     uint32_t capacity;       /* triangles in the part */
     uint32_t count;          /* visible triangles (valid after t3d_frame_sync) */
+    uint32_t draw;           /* flush this pair belongs to: pairs of one dynamic batch share it */
+    uint32_t draw_transparent; /* that flush is in the transparent pass (no depth composite) */
 } t3d_segment_info;
 
 typedef struct t3d_stats {

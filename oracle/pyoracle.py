@@ -23,7 +23,8 @@ class OracleOut(C.Structure):
                 ("seg_base", C.POINTER(C.c_uint32)), ("seg_capacity", C.POINTER(C.c_uint32)),
                 ("seg_count", C.POINTER(C.c_uint32)), ("max_tris", C.c_uint64), ("total_slots", C.c_uint64),
                 ("visible_tris", C.c_uint64), ("tri_index", C.POINTER(C.c_uint32)), ("xyuv", C.c_void_p),
-                ("rgba", C.c_void_p), ("depth", C.c_void_p), ("culled_models", C.c_uint32), ("reserved", C.c_uint32)]
+                ("rgba", C.c_void_p), ("depth", C.c_void_p), ("culled_models", C.c_uint32), ("reserved", C.c_uint32),
+                ("seg_draw", C.POINTER(C.c_uint32)), ("seg_draw_transparent", C.POINTER(C.c_uint32))]
 
 
 _lib = None
@@ -85,7 +86,8 @@ def render(scene_data, cam, light_mask=None, animate_frames=0, threads=1, f64=Fa
 
 def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_max, slots):
     dt = np.float64 if f64 else np.float32
-    seg = {k: np.zeros(nseg_max, np.uint32) for k in ("model", "part", "base", "capacity", "count")}
+    seg = {k: np.zeros(nseg_max, np.uint32) for k in ("model", "part", "base", "capacity", "count", "draw",
+                                                       "draw_transparent")}
     tri = np.zeros(slots, np.uint32)
     xyuv = np.zeros((slots, 3, 4), dt)
     rgba = np.zeros((slots, 3, 4), dt)
@@ -95,6 +97,7 @@ def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_ma
     u = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
     o.seg_model, o.seg_part, o.seg_base = u(seg["model"]), u(seg["part"]), u(seg["base"])
     o.seg_capacity, o.seg_count = u(seg["capacity"]), u(seg["count"])
+    o.seg_draw, o.seg_draw_transparent = u(seg["draw"]), u(seg["draw_transparent"])
     o.max_tris = slots
     o.tri_index = u(tri)
     o.xyuv, o.rgba, o.depth = xyuv.ctypes.data, rgba.ctypes.data, depth.ctypes.data
@@ -108,7 +111,8 @@ def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_ma
         return None, rc, int(o.total_slots)
     n = o.num_segments
     segs = [dict(model=int(seg["model"][i]), part=int(seg["part"][i]), base=int(seg["base"][i]),
-                 capacity=int(seg["capacity"][i]), count=int(seg["count"][i])) for i in range(n)]
+                 capacity=int(seg["capacity"][i]), count=int(seg["count"][i]), draw=int(seg["draw"][i]),
+                 draw_transparent=int(seg["draw_transparent"][i])) for i in range(n)]
     sel = np.concatenate([np.arange(s["base"], s["base"] + s["count"]) for s in segs] or [np.zeros(0, np.int64)])
     sel = sel.astype(np.int64)
     return OracleFrame(segs, tri[sel], xyuv[sel], rgba[sel], depth[sel], o.culled_models), 0, slots
@@ -180,15 +184,21 @@ def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, tran
     given = transparent
     transparent = np.zeros(max(1, len(frame.segments)), np.uint8)
     b = 0
+    flush = -1
     for k, s in enumerate(frame.segments):
-        pair[b:b + s["count"]] = k
+        # the pairs of one dynamic batch are one flush (one depth composite)
+        if k == 0 or "draw" not in s or s["draw"] != frame.segments[k - 1]["draw"]:
+            flush += 1
+        pair[b:b + s["count"]] = flush
         b += s["count"]
         if given is not None:
-            transparent[k] = bool(given[k])
+            transparent[flush] = bool(given[k])
+        elif "draw_transparent" in s:
+            transparent[flush] = bool(s["draw_transparent"])
         else:
             md = scene_data.mv[s["model"]]
             mat = scene_data.meshes[int(md["mesh"])].parts[s["part"]]["mat"]
-            transparent[k] = is_transparent(md, mat)
+            transparent[flush] = is_transparent(md, mat)
     xyuv = np.ascontiguousarray(frame.xyuv, np.float32).reshape(-1)
     rgba = np.ascontiguousarray(frame.rgba, np.float32).reshape(-1)
     depth = np.ascontiguousarray(frame.depth, np.float32).reshape(-1)

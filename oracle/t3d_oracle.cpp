@@ -11,6 +11,7 @@
 
 #include "t3d_oracle.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -206,7 +207,7 @@ template <typename R> struct ModelState {
 };
 
 // One render pair: model index + part index + draw-order slot.
-struct Pair { uint32_t model, part; float depth; int32_t order; };
+struct Pair { uint32_t model, part; float depth; int32_t order; bool batch = false; uint32_t draw = 0, draw_transparent = 0; };
 
 // Mesh.SetAutoSubdivide (mesh.go:447-490) restated: every part triangle,
 // then the triangles of its subdivision levels (forEachTri order,
@@ -1106,15 +1107,52 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
     std::vector<char> is_culled(sc->num_models, 0);
     uint32_t culled = 0;
     std::vector<Pair> solids, transparents;
+    // Model.DynamicBatchModels: owner -> (owner part -> members in model order)
+    std::vector<std::vector<std::pair<uint32_t, std::vector<uint32_t>>>> batch_of(sc->num_models);
+    for (uint32_t i = 0; i < sc->num_models; i++) {
+        const t3d_model_desc& md = sc->models[i];
+        if (!md.batched) continue;
+        auto& parts = batch_of[md.batch_owner];
+        auto it = std::find_if(parts.begin(), parts.end(), [&](const auto& e) { return e.first == md.batch_part; });
+        if (it == parts.end()) {
+            parts.push_back({md.batch_part, {}});
+            it = parts.end() - 1;
+        }
+        it->second.push_back(i);
+    }
+    for (auto& parts : batch_of)  // the owner's batch parts in ascending part order
+        std::sort(parts.begin(), parts.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
     for (uint32_t i = 0; i < sc->num_models; i++) {
         const t3d_model_desc& md = sc->models[i];
         if (!md.visible) continue;
+        // frustum culling of a batch member happens when its batch draws (camera.go:2083-2088)
         if (md.frustum_culling && !model_in_frustum(F.cam, F.models[i].transform, F.dims[md.mesh], md.skinned != 0)) {
             is_culled[i] = 1;
             culled++;
         }
+        if (md.batched) continue;  // camera.go:1346
         const t3d_mesh_desc& me = *F.mesh[md.mesh];
         V3<R> mpos = row3(F.models[i].transform, 3);
+        if (!batch_of[i].empty()) {  // a dynamic batcher: one pair per batch part (camera.go:1397-1451)
+            bool transparent = false;
+            for (const auto& bp : batch_of[i]) {
+                const t3d_material& bm = me.parts[bp.first].mat;
+                if (bm.present && !bm.visible) continue;
+                for (uint32_t c : bp.second) {
+                    const t3d_model_desc& cm = sc->models[c];
+                    if (!cm.visible || transparent) continue;
+                    const t3d_mesh_desc& cme = *F.mesh[cm.mesh];
+                    for (uint32_t q = 0; q < cme.num_parts && !transparent; q++)
+                        if (!(cme.parts[q].mat.present && !cme.parts[q].mat.visible) && is_transparent(cm, cme.parts[q]))
+                            transparent = true;
+                }
+                Pair rp{i, bp.first, 0.0f, bm.present ? bm.render_order : 0, true};
+                if (transparent || !cd->render_depth) rp.depth = (float)dist2(F.cam.pos, mpos);
+                if (transparent) transparents.push_back(rp);
+                else solids.push_back(rp);
+            }
+            continue;
+        }
         for (uint32_t p = 0; p < me.num_parts; p++) {
             const t3d_part_desc& part = me.parts[p];
             if (part.mat.present && !part.mat.visible) continue;  // MeshPart.isVisible, mesh.go:2402-2407
@@ -1142,14 +1180,40 @@ int render(const t3d_scene_desc* sc, const t3d_camera_desc* cd, const uint64_t* 
     };
     if (!cd->render_depth) stable_by(solids, by_order_then_far);  // camera.go:1461-1470
     stable_by(transparents, by_order_then_far);                   // camera.go:2050-2055
-    std::vector<Pair> segs(solids);
-    segs.insert(segs.end(), transparents.begin(), transparents.end());
+    std::vector<Pair> ordered(solids);
+    ordered.insert(ordered.end(), transparents.begin(), transparents.end());
+    // every pair is one flush; a batch draws its visible members far to near from the
+    // camera (camera.go:2072-2093; equal distances keep model order), all their parts
+    std::vector<Pair> segs;
+    for (size_t q = 0; q < ordered.size(); q++) {
+        Pair rp = ordered[q];
+        rp.draw = (uint32_t)q;
+        rp.draw_transparent = q >= solids.size() ? 1u : 0u;
+        if (!rp.batch) {
+            segs.push_back(rp);
+            continue;
+        }
+        std::vector<std::pair<R, uint32_t>> members;
+        for (const auto& bp : batch_of[rp.model])
+            if (bp.first == rp.part)
+                for (uint32_t c : bp.second)
+                    if (sc->models[c].visible) members.push_back({dist2(F.cam.pos, row3(F.models[c].transform, 3)), c});
+        std::stable_sort(members.begin(), members.end(),
+                         [](const std::pair<R, uint32_t>& a, const std::pair<R, uint32_t>& b) { return a.first > b.first; });
+        for (const auto& mc : members)
+            for (uint32_t p = 0; p < F.mesh[sc->models[mc.second].mesh]->num_parts; p++) {
+                Pair m{mc.second, p, 0.0f, 0, false, rp.draw, rp.draw_transparent};
+                segs.push_back(m);
+            }
+    }
 
     if (segs.size() > out->max_segments) return T3D_E_INVAL;
     uint64_t base = 0;
     for (size_t s = 0; s < segs.size(); s++) {
         const t3d_mesh_desc& me = *F.mesh[sc->models[segs[s].model].mesh];
         out->seg_model[s] = segs[s].model;
+        if (out->seg_draw) out->seg_draw[s] = segs[s].draw;
+        if (out->seg_draw_transparent) out->seg_draw_transparent[s] = segs[s].draw_transparent;
         out->seg_part[s] = segs[s].part;
         out->seg_base[s] = (uint32_t)base;
         out->seg_capacity[s] = me.parts[segs[s].part].tri_count;

@@ -44,6 +44,8 @@ typedef struct t3d_oracle_out {
     void*     depth;             /* [max_tris*3] */
     uint32_t  culled_models;     /* out */
     uint32_t  reserved;
+    uint32_t* seg_draw;          /* [max_segments] flush of each pair (a dynamic batch is one); may be NULL */
+    uint32_t* seg_draw_transparent; /* that flush is in the transparent pass; may be NULL */
 } t3d_oracle_out;
 
 /* Renders one frame. light_mask may be NULL (all lights). animate_frames

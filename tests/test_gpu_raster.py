@@ -33,6 +33,9 @@ CASES = [
     ("fog_over_incirc_dither", lambda: (scenes.feature_scene(7), _fog_depth_camera("over")),
      {"fog_curve": 2, "dither_size": 2.0}),
     ("fogless", lambda: (scenes.feature_scene(5), _fog_depth_camera("add")), {"fogless": 1}),
+    # dynamic batches: the members of a batch share one depth composite
+    ("batches", lambda: (scenes.batch_scene(11), scenes.feature_camera("persp")), {}),
+    ("batches_tilted_fog", lambda: (scenes.batch_scene(12), _fog_depth_camera("add")), {}),
 ]
 
 

@@ -61,7 +61,9 @@ class ModelDesc(C.Structure):
                 ("shadeless", C.c_int32), ("light_list", C.c_int32), ("use_trs", C.c_int32),
                 ("color", C.c_float * 4), ("transform", C.c_float * 16), ("world_rotation", C.c_float * 16),
                 ("position", C.c_float * 3), ("scale", C.c_float * 3), ("rotation", C.c_float * 16),
-                ("rotate_step", C.c_float * 16), ("skinned", C.c_int32), ("bone_first", C.c_uint32)]
+                ("rotate_step", C.c_float * 16), ("skinned", C.c_int32), ("bone_first", C.c_uint32),
+                ("batched", C.c_int32), ("batch_owner", C.c_uint32), ("batch_part", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class LightDesc(C.Structure):
@@ -104,7 +106,8 @@ class FrameView(C.Structure):
 
 class SegmentInfo(C.Structure):
     _fields_ = [("job", C.c_uint32), ("model", C.c_uint32), ("part", C.c_uint32), ("base", C.c_uint32),
-                ("capacity", C.c_uint32), ("count", C.c_uint32)]
+                ("capacity", C.c_uint32), ("count", C.c_uint32), ("draw", C.c_uint32),
+                ("draw_transparent", C.c_uint32)]
 
 
 class Stats(C.Structure):

@@ -171,6 +171,17 @@ int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d
             set_err(ctx, "set_models: model %u has a bad mesh or light list", first + i);
             return T3D_E_INVAL;
         }
+        if (models[i].batched) {
+            const uint32_t o = models[i].batch_owner;
+            const uint32_t omesh = (o >= first && o < first + n) ? models[o - first].mesh
+                                   : (o < sc->models.size() ? sc->models[o].d.mesh : 0xFFFFFFFFu);
+            if (o >= sc->models.size() || o == first + i || omesh >= sc->meshes.size() ||
+                models[i].batch_part >= sc->meshes[omesh].parts.size()) {
+                set_err(ctx, "set_models: model %u: batch owner %u or its part %u out of range", first + i, o,
+                        models[i].batch_part);
+                return T3D_E_INVAL;
+            }
+        }
         const SceneMesh& me = sc->meshes[models[i].mesh];
         if (models[i].skinned && (!me.skin || me.subdiv || (uint64_t)models[i].bone_first + me.max_joint >= sc->num_bones)) {
             set_err(ctx, "set_models: skinned model %u without joints or with bones beyond the scene's %u", first + i,

@@ -352,9 +352,11 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
     const uint32_t f0 = pstart[p], f1 = pstart[p + 1];
     uint32_t i = f0;
     while (i < f1) {
-        const uint32_t s = J.tri_seg[fvals[i]];
+        // the fragments of one flush: a render pair, or all pairs of a dynamic batch
+        // (pad[0] = flush number | transparent pass << 31)
+        const uint32_t fl = J.segs[J.tri_seg[fvals[i]]].pad[0];
         uint32_t e = i + 1;
-        while (e < f1 && J.tri_seg[fvals[e]] == s) e++;  // this pair's fragments
+        while (e < f1 && J.segs[J.tri_seg[fvals[e]]].pad[0] == fl) e++;
         if (J.render_depth) {
             uint32_t inter = 0u;
             for (uint32_t q = i; q < e; q++) {  // depth pass (camera.go:1882-1931)
@@ -389,7 +391,7 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
                     }
                     rc = blend_over(rc, r, g, b, a);
                 }
-                if (!(J.segs[s].flags & SEG_TRANSPARENT)) rd = inter;  // depth composite
+                if (!(fl >> 31)) rd = inter;  // depth composite unless the flush is transparent
             }
         } else {
             for (uint32_t q = i; q < e; q++) {  // plain draw, straight-alpha vertex colours

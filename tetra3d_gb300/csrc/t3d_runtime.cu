@@ -603,6 +603,12 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
             set_err(ctx, "model %u: light list %d out of range", i, md.light_list);
             return T3D_E_INVAL;
         }
+        if (md.batched && (md.batch_owner >= d->num_models || md.batch_owner == i ||
+                           d->models[md.batch_owner].mesh >= d->num_meshes ||
+                           md.batch_part >= d->meshes[d->models[md.batch_owner].mesh].num_parts)) {
+            set_err(ctx, "model %u: batch owner %u or its part %u out of range", i, md.batch_owner, md.batch_part);
+            return T3D_E_INVAL;
+        }
         if (md.skinned && (!sc->meshes[md.mesh].skin || sc->meshes[md.mesh].subdiv ||
                            (uint64_t)md.bone_first + sc->meshes[md.mesh].max_joint >= d->num_bones)) {
             set_err(ctx, "model %u: skinned without joints or with bones beyond the %u scene bones", i, d->num_bones);
@@ -768,7 +774,8 @@ uint64_t next_version() {
 static bool same_model_structure(const t3d_model_desc& a, const t3d_model_desc& b) {
     return a.mesh == b.mesh && a.visible == b.visible && a.frustum_culling == b.frustum_culling &&
            a.shadeless == b.shadeless && a.light_list == b.light_list && a.use_trs == b.use_trs &&
-           a.skinned == b.skinned && a.bone_first == b.bone_first && memcmp(a.color, b.color, sizeof a.color) == 0;
+           a.skinned == b.skinned && a.bone_first == b.bone_first && a.batched == b.batched &&
+           a.batch_owner == b.batch_owner && a.batch_part == b.batch_part && memcmp(a.color, b.color, sizeof a.color) == 0;
 }
 
 // Model writes are asynchronous: the copy is queued on the stream of the last
@@ -881,9 +888,17 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
 
         const t3d_camera_desc& cd = jobs[j].camera;
         f3 campos = row3(load16(cd.transform), 3);
-        struct Pair { uint32_t model, part; float depth; int32_t order; };
+        struct Pair { uint32_t model, part; float depth; int32_t order; bool batch; };
         std::vector<Pair> solids, transparents;
         std::vector<uint32_t> inst_of(sc->models.size(), 0xFFFFFFFFu);
+        // dynamic batches: the members of each (owner, owner part), in model order
+        std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>> batches;
+        std::vector<char> owner(sc->models.size(), 0);
+        for (uint32_t mi = 0; mi < sc->models.size(); mi++)
+            if (sc->models[mi].d.batched) {
+                batches[{sc->models[mi].d.batch_owner, sc->models[mi].d.batch_part}].push_back(mi);
+                owner[sc->models[mi].d.batch_owner] = 1;
+            }
         const std::vector<uint32_t> scene_lights = culled_scene_lights(sc, jobs[j]);
         for (uint32_t mi = 0; mi < sc->models.size(); mi++) {
             SceneModel& m = sc->models[mi];
@@ -917,10 +932,36 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             }
             m4 M = host_transform(m);
             float depth = dist2(campos, row3(M, 3));  // camera.go:1381
+            if (m.d.batched) continue;  // drawn inside its owner's batch (camera.go:1346)
+            if (owner[mi]) {
+                // one pair per batch part of the owner (camera.go:1397-1451); the
+                // transparency found for one part carries over to the later ones there
+                F.insts.back().bytes = 0;  // the owner's own mesh is not drawn
+                bool transparent = false;
+                for (auto it = batches.lower_bound({mi, 0u}); it != batches.end() && it->first.first == mi; ++it) {
+                    const t3d_material& bm = me.parts[it->first.second].d.mat;
+                    if (bm.present && !bm.visible) continue;
+                    for (uint32_t c : it->second) {
+                        const SceneModel& cm = sc->models[c];
+                        if (!cm.d.visible || transparent) continue;
+                        for (const ScenePart& cp : sc->meshes[cm.d.mesh].parts)
+                            if (!(cp.d.mat.present && !cp.d.mat.visible) && is_transparent(cm.d.color, cp.d.mat)) {
+                                transparent = true;
+                                break;
+                            }
+                    }
+                    Pair rp{mi, it->first.second, 0.0f, bm.present ? bm.render_order : 0, true};
+                    if (transparent || !cd.render_depth) rp.depth = depth;
+                    if (transparent) transparents.push_back(rp);
+                    else solids.push_back(rp);
+                }
+                ctx->order_dep = true;  // members are drawn far to near
+                continue;
+            }
             for (uint32_t p = 0; p < me.parts.size(); p++) {
                 const t3d_material& mat = me.parts[p].d.mat;
                 if (mat.present && !mat.visible) continue;
-                Pair rp{mi, p, depth, mat.present ? mat.render_order : 0};
+                Pair rp{mi, p, depth, mat.present ? mat.render_order : 0, false};
                 if (is_transparent(m.d.color, mat)) transparents.push_back(rp);
                 else solids.push_back(rp);
                 if (is_transparent(m.d.color, mat) || !cd.render_depth) ctx->order_dep = true;
@@ -931,8 +972,32 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         };
         if (!cd.render_depth) std::stable_sort(solids.begin(), solids.end(), by_order_then_far);
         std::stable_sort(transparents.begin(), transparents.end(), by_order_then_far);
+        const size_t nsolid = solids.size();
         solids.insert(solids.end(), transparents.begin(), transparents.end());
-        for (const Pair& rp : solids) {
+        // Draws: a plain pair is one flush; a batch pair draws its visible members far to
+        // near from the camera (camera.go:2072-2093; ties keep model order), every part of
+        // each, in one flush. Members outside the frustum are culled on the device.
+        struct Draw { uint32_t model, part, draw, transparent; };
+        std::vector<Draw> draws;
+        for (size_t q = 0; q < solids.size(); q++) {
+            const Pair& rp = solids[q];
+            const uint32_t dt = q >= nsolid ? 1u : 0u;
+            if (!rp.batch) {
+                draws.push_back({rp.model, rp.part, (uint32_t)q, dt});
+                continue;
+            }
+            std::vector<std::pair<float, uint32_t>> mem;
+            for (uint32_t c : batches[{rp.model, rp.part}]) {
+                if (!sc->models[c].d.visible) continue;
+                mem.push_back({dist2(campos, row3(host_transform(sc->models[c]), 3)), c});
+            }
+            std::stable_sort(mem.begin(), mem.end(), [](const std::pair<float, uint32_t>& a,
+                                                        const std::pair<float, uint32_t>& b) { return a.first > b.first; });
+            for (const auto& mc : mem)
+                for (uint32_t p = 0; p < sc->meshes[sc->models[mc.second].d.mesh].parts.size(); p++)
+                    draws.push_back({mc.second, p, (uint32_t)q, dt});
+        }
+        for (const Draw& rp : draws) {
             const SceneModel& m = sc->models[rp.model];
             const SceneMesh& me = sc->meshes[m.d.mesh];
             const ScenePart& part = me.parts[rp.part];
@@ -1014,9 +1079,11 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 if (ntiles > 1) F.mt_desc.push_back(td);
             }
 
+            sg.pad[0] = rp.draw | (rp.transparent << 31);  // flush and its pass, for the rasteriser
             F.segs.push_back(sg);
             t3d_segment_info si;
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
+            si.draw = rp.draw; si.draw_transparent = rp.transparent;
             F.seg_info.push_back(si);
             F.seg_mt_seg.push_back(ntiles > 1 ? (uint32_t)F.mt_segs.size() - 1 : 0xFFFFFFFFu);
         }

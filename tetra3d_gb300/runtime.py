@@ -109,8 +109,8 @@ class Context:
         self._check(self.lib.t3d_frame_segments(self.h, None, 0, C.byref(n)), "frame_segments")
         arr = (abi.SegmentInfo * max(1, n.value))()
         self._check(self.lib.t3d_frame_segments(self.h, arr, n.value, C.byref(n)), "frame_segments")
-        return [dict(job=s.job, model=s.model, part=s.part, base=s.base, capacity=s.capacity, count=s.count)
-                for s in arr[:n.value]]
+        return [dict(job=s.job, model=s.model, part=s.part, base=s.base, capacity=s.capacity, count=s.count,
+                     draw=s.draw, draw_transparent=s.draw_transparent) for s in arr[:n.value]]
 
     def download(self, stats=None):
         st = stats or self.sync()

@@ -947,6 +947,47 @@ def subdivision_scene(seed=10, n=24, w=1280, h=720, max_subdivisions=3):
     return sd
 
 
+def batch_scene(seed=11, n=72, w=1280, h=720):
+    """Dynamic batches (Model.DynamicBatchAdd): three owners, two of them batching under two
+    of their mesh parts, with members from the feature meshes scattered in front of the camera
+    (some invisible, some behind the camera with frustum culling, one half-transparent so one
+    batch goes to the transparent pass), next to unbatched models of the same meshes.
+    Owner 2 is itself a member of owner 0's batch (its own batch is never drawn)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = feature_scene(seed, n=8)
+    owner_mesh = cube_mesh(1.0, 1.0, 1.0)
+    owner_mesh.parts = [dict(tri_start=0, tri_count=6, mat=_random_material(rng)),
+                        dict(tri_start=6, tri_count=6, mat=_random_material(rng))]
+    for p in owner_mesh.parts:
+        p["mat"].update(present=1, visible=1, transparency_mode=abi.TRANSPARENCY_OPAQUE, render_order=0)
+    meshes = list(base.meshes[:6]) + [owner_mesh]
+    om = len(meshes) - 1
+    sd = SceneData(meshes, n, [base.lights[i] for i in range(base.nlights)], base.lists,
+                   cells=base.cells[:base.ncells] if base.ncells else None, name=f"batches{seed}")
+    pos = np.stack([rng.uniform(-14, 14, n), rng.uniform(-8, 8, n), rng.uniform(-45, -4, n)], 1).astype(F32)
+    mesh_of = rng.integers(0, 6, n).astype(np.uint32)
+    mesh_of[:3] = om
+    scl = np.repeat(rng.uniform(0.5, 2.0, (n, 1)), 3, 1).astype(F32)
+    rot = quat_to_mat(random_quats(rng, n))
+    set_models_trs(sd, mesh_of, pos, scl, rot,
+                   light_list=np.where(rng.random(n) < 0.5, -1, rng.integers(1, 4, n)).astype(np.int32))
+    mv = sd.mv
+    mv["frustum_culling"] = 1
+    members = np.arange(3, n - 10)
+    mv["batched"][members] = 1
+    mv["batch_owner"][members] = rng.integers(0, 2, len(members))
+    mv["batch_part"][members] = rng.integers(0, 2, len(members))
+    mv["batched"][2], mv["batch_owner"][2], mv["batch_part"][2] = 1, 0, 1   # a nested owner
+    mv["batched"][n - 12], mv["batch_owner"][n - 12], mv["batch_part"][n - 12] = 1, 2, 0
+    mv["visible"][[5, 9]] = 0
+    mv["position"][7] = (0.0, 0.0, 60.0)  # behind the camera: culled inside its batch
+    mv["color"][11] = (1.0, 1.0, 1.0, 0.5)  # makes its owner's later batch parts transparent
+    M = trs(mv["position"], mv["scale"], mv["rotation"].reshape(n, 4, 4))
+    mv["transform"] = M.reshape(n, 16)
+    sd.camera = feature_camera("persp", w, h)
+    return sd
+
+
 def down_camera(w=1280, h=720):
     """A camera at (0, 10, 0) looking straight down -Y."""
     return camera(pos=(0.0, 10.0, 0.0), rot=rotate(1, 0, 0, deg2rad(-90.0)), w=w, h=h, fov=70.0, near=0.1, far=60.0)
