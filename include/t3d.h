@@ -202,7 +202,7 @@ typedef struct t3d_model_desc {
  * its WorldRotation(). Volume fields describe a LightVolume (light.go:377-680):
  * its Dimensions, cell sizes, cell counts (as LightVolumeResize computed them),
  * offset, light bias and the index of its first cell colour (RGBA) in the
- * scene's cell table. Nested LightVolumeCell.useLights are not supported. */
+ * scene's cell table; the lights its cells use are in the scene desc. */
 typedef struct t3d_light_desc {
     int32_t  type;             /* T3D_LIGHT_* */
     int32_t  cell_count[3];
@@ -243,6 +243,13 @@ typedef struct t3d_scene_desc {
     const float*          subdivision_levels;     /* 2 * num_subdivision_levels */
     uint32_t              num_subdivision_levels;
     uint32_t              max_subdivisions;
+    /* LightVolumeCell.useLights (light.go:1381, :1509-1522): lights applied, in list
+     * order, to a vertex that falls into a cell in the per-vertex shading modes, before the
+     * cell's own colour (light.go:646-656). Cell c uses cell_use_items[cell_use_offsets[c] ..
+     * cell_use_offsets[c + 1]) (ambient, point or directional lights of this scene). NULL:
+     * no cell uses lights. Job light masks do not apply to them. */
+    const uint32_t*       cell_use_offsets;       /* num_volume_cells + 1 */
+    const uint32_t*       cell_use_items;
 } t3d_scene_desc;
 
 /* Camera + World settings read by Render (camera.go:256-321, world.go:25-39).

@@ -639,6 +639,7 @@ template <typename R> struct ModelLight {  // beginModel results for one model
     const LightPrep<R>* l;
     V3<R> working;          // point workingPosition
     bool skip;              // model-level point-range skip (camera.go:1625-1629)
+    const std::vector<ModelLight<R>>* nested = nullptr;  // every scene light after beginModel (cell useLights)
 };
 
 // LightVolume helpers (light.go:717-741, :1267-1272)
@@ -730,6 +731,12 @@ void vertex_light(const Frame<R>& F, const ModelLight<R>& ml, const t3d_part_des
             if (lv_cell(d, mode == T3D_LV_PER_VERTEX_WITH_NORMAL ? vertPosWithNormal : vertPos, idx)) {
                 const float* cc = F.sc->volume_cells + 4 * (size_t)(d->cell_first + idx);
                 cellColor.r = (R)cc[0]; cellColor.g = (R)cc[1]; cellColor.b = (R)cc[2]; cellColor.a = (R)cc[3];
+                if (F.sc->cell_use_offsets && ml.nested) {  // cell.useLights (light.go:652-654)
+                    const size_t c = (size_t)d->cell_first + (size_t)idx;
+                    for (uint32_t u = F.sc->cell_use_offsets[c]; u < F.sc->cell_use_offsets[c + 1]; u++)
+                        vertex_light<R>(F, (*ml.nested)[F.sc->cell_use_items[u]], part, skinned, transform, dir_rot, vpos,
+                                        vnrm, tgt);
+                }
             }
         }
         tgt.r += L.color.x * cellColor.r * L.energy;
@@ -911,6 +918,7 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
     // ---- lighting (camera.go:1521-1528, :1576-1644) ----
     bool lighting = cd->lighting_on && !(mat.present && mat.shadeless) && !md.shadeless;
     std::vector<ModelLight<R>> mlights;
+    std::vector<ModelLight<R>> nested_ml;  // beginModel of the lights light-volume cells use
     M4<R> dir_rot = identity<R>();
     if (lighting) {
         uint32_t list = md.light_list < 0 ? 0u : (uint32_t)md.light_list;
@@ -924,9 +932,22 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
             std::vector<uint32_t> items;
             if (list == 0) items = F.scene_lights;
             else for (uint32_t q = sc->list_offsets[list]; q < sc->list_offsets[list + 1]; q++) items.push_back(sc->list_items[q]);
+            if (sc->cell_use_offsets) {
+                nested_ml.resize(F.lights.size());
+                for (uint32_t li = 0; li < F.lights.size(); li++) {
+                    ModelLight<R>& nm = nested_ml[li];
+                    nm.l = &F.lights[li];
+                    nm.skip = false;
+                    nm.working = v3<R>(0, 0, 0);
+                    if (nm.l->type == T3D_LIGHT_POINT)
+                        nm.working = skinned ? nm.l->wpos
+                                             : add(mult_vec(ir, nm.l->wpos), hmul(ip, v3<R>((R)1 / is.x, (R)1 / is.y, (R)1 / is.z)));
+                }
+            }
             for (uint32_t li : items) {
                 if (li >= F.lights.size() || !light_enabled(F.mask, li)) continue;
                 ModelLight<R> ml;
+                ml.nested = nested_ml.empty() ? nullptr : &nested_ml;
                 ml.l = &F.lights[li];
                 ml.working = v3<R>(0, 0, 0);
                 ml.skip = false;

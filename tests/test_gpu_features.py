@@ -517,3 +517,24 @@ def test_dynamic_batches_match_oracle(ctx, variant):
         assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), f"batches/{variant}/moved")
     finally:
         ctx.release(sid)
+
+
+@pytest.mark.parametrize("variant", ["persp", "tilted", "fog_add", "corrected"])
+def test_cell_use_lights_match_oracle(ctx, variant):
+    """LightVolumeCell.useLights: lights applied to vertices inside light-volume cells, for
+    models lit by the scene list and by light groups, both forms; a used light cannot be
+    turned into a volume."""
+    sd = scenes.nested_light_scene(5)
+    cam = scenes.feature_camera(variant)
+    ref = pyoracle.render(sd, cam)
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), ref, f"nested/{variant}/mode{mode}")
+        used = sorted({x for c in sd.cell_uses for x in c})
+        bad = (abi.LightDesc * 1)(sd.lights[used[0]])
+        bad[0].type = abi.LIGHT_VOLUME
+        assert ctx.lib.t3d_scene_set_lights(ctx.h, sid, used[0], bad, 1) == abi.T3D_E_INVAL
+    finally:
+        ctx.release(sid)

@@ -81,7 +81,7 @@ class SceneDesc(C.Structure):
                 ("num_meshes", C.c_uint32), ("num_models", C.c_uint32), ("num_lights", C.c_uint32),
                 ("num_volume_cells", C.c_uint32), ("num_lists", C.c_uint32), ("num_bones", C.c_uint32),
                 ("bones", f32p), ("subdivision_levels", f32p), ("num_subdivision_levels", C.c_uint32),
-                ("max_subdivisions", C.c_uint32)]
+                ("max_subdivisions", C.c_uint32), ("cell_use_offsets", u32p), ("cell_use_items", u32p)]
 
 
 class CameraDesc(C.Structure):

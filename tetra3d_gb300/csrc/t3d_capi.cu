@@ -265,6 +265,10 @@ int t3d_scene_set_lights(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d
             set_err(ctx, "set_lights: light %u has bad type %d", first + i, l.type);
             return T3D_E_INVAL;
         }
+        if (l.type == T3D_LIGHT_VOLUME && sc->light_nested[first + i]) {
+            set_err(ctx, "set_lights: light %u is used by light-volume cells and cannot become a volume", first + i);
+            return T3D_E_INVAL;
+        }
         if (l.type == T3D_LIGHT_VOLUME) {
             const uint64_t cells = (uint64_t)std::max(0, l.cell_count[0]) * std::max(0, l.cell_count[1]) *
                                    std::max(0, l.cell_count[2]);
@@ -279,7 +283,16 @@ int t3d_scene_set_lights(t3d_ctx* ctx, uint32_t scene, uint32_t first, const t3d
     // render builds new ones, so only a captured graph (which keeps its tables) goes
     if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
     drop_graph(ctx);
-    for (uint32_t i = 0; i < n; i++) sc->lights[first + i] = lights[i];
+    for (uint32_t i = 0; i < n; i++) {
+        sc->lights[first + i] = lights[i];
+        const t3d_light_desc& l = lights[i];
+        sc->light_uses[first + i] = 0;  // a volume's cells keep their use lists; its cell range may move
+        if (l.type == T3D_LIGHT_VOLUME) {
+            const uint64_t cells = (uint64_t)std::max(0, l.cell_count[0]) * std::max(0, l.cell_count[1]) *
+                                   std::max(0, l.cell_count[2]);
+            sc->light_uses[first + i] = sc->cell_uses_between(l.cell_first, l.cell_first + cells);
+        }
+    }
     sc->struct_ver = next_version();
     return T3D_OK;
 }

@@ -42,10 +42,11 @@ enum : uint32_t {
     SEG_UNBB = 1u << 21,        // BillboardedDepthMode == DepthModeUnbillboarded on a billboard
     SEG_SUBDIV = 1u << 22,      // auto-subdivided mesh: triangles are candidates of a subdivision level
     SEG_SNAP = 1u << 23,        // Camera.VertexSnapping > 0
+    SEG_NESTED = 1u << 24,      // a light volume of the pair's list has cells that use lights
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
-    SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD | SEG_SNAP,
+    SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD | SEG_SNAP | SEG_NESTED,
 };
 constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }
@@ -131,6 +132,8 @@ struct DevJob {
     const float* sub_levels;  // AutoSubdivisionLevel: DistanceSquared, MaximumTriangleSize
     uint32_t nsub_levels;
     uint32_t pad_sub;
+    const uint32_t* cell_use_off;    // LightVolumeCell.useLights: cell c uses items [off[c], off[c + 1])
+    const uint32_t* cell_use_items;  // light indices of the job's light table
 };
 
 // One (job, model) pair.

@@ -238,13 +238,69 @@ __device__ __forceinline__ f3 mult_vec_s(const float* m, f3 v) {
                m[2] * v.x + m[6] * v.y + m[10] * v.z + m[14]);
 }
 
+// What the lights used by light-volume cells need (LightVolumeCell.useLights).
+struct NestedSrc {
+    const DevLight* lights;   // the job's light table
+    const uint32_t* off;      // cell c uses items [off[c], off[c + 1])
+    const uint32_t* items;
+    const float* inv_r;       // the model's Decompose(Inverted(M)) rows, for point-light positions
+};
+
+// A light used by a light-volume cell, lit at the vertex that fell into that cell
+// (light.go:652-654): its VertexLight as after its beginModel (light.go:175-189,
+// :326-330), without the model-level range skip of the scene's lights.
+__device__ __noinline__ void nested_light(const DevLight& N, uint32_t flags, f3 vpos, f3 vnrm, const float* dirrot,
+                                          const float* __restrict__ r_, float& r, float& g, float& b) {
+    const bool mat = flags & SEG_MAT;
+    const uint32_t lmode = seg_light_mode(flags);
+    const bool skinned = flags & SEG_SKINNED;
+    if (N.type == T3D_LIGHT_AMBIENT) {
+        r += N.amb[0]; g += N.amb[1]; b += N.amb[2];
+    } else if (N.type == T3D_LIGHT_POINT) {
+        const f3 lp = mk3(N.wpos[0], N.wpos[1], N.wpos[2]);
+        f3 work = lp;
+        if (!skinned) {  // the same model-space position as stage_model computes
+            const f3 q = mk3(r_[0] * lp.x + r_[4] * lp.y + r_[8] * lp.z + r_[12],
+                             r_[1] * lp.x + r_[5] * lp.y + r_[9] * lp.z + r_[13],
+                             r_[2] * lp.x + r_[6] * lp.y + r_[10] * lp.z + r_[14]);
+            work = mk3(q.x + r_[3], q.y + r_[7], q.z + r_[11]);
+        }
+        const float distance = dist2(work, vpos);
+        if (N.range > 0.0f) {
+            if (distance > N.range2) return;
+        } else {
+            if (1.0f / distance * N.energy < 0.001f) return;
+        }
+        const f3 lightVec = unit3(sub3(work, vpos));
+        const f3 n = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? lightVec : vnrm;
+        float diffuse = dot3(n, lightVec);
+        if (mat && lmode == T3D_LIGHTING_DOUBLE_SIDED) diffuse = fabsf(diffuse);
+        if (diffuse > 0.0f) {
+            float df = diffuse * (1.0f / (1.0f + (0.1f * distance))) * 2.0f;
+            if (N.range2 > 0.0f) df *= clampf((N.range2 - distance) / distance, 0.0f, 1.0f);
+            r += N.color[0] * df * N.energy;
+            g += N.color[1] * df * N.energy;
+            b += N.color[2] * df * N.energy;
+        }
+    } else if (N.type == T3D_LIGHT_DIRECTIONAL) {
+        const f3 fwd = mk3(N.fwd[0], N.fwd[1], N.fwd[2]);
+        const f3 normal = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? fwd : skinned ? vnrm : mult_vec_s(dirrot, vnrm);
+        float df = dot3(normal, fwd);
+        if (mat && lmode == T3D_LIGHTING_DOUBLE_SIDED) df = fabsf(df);
+        if (df <= 0.0f) return;
+        r += N.color[0] * df * N.energy;
+        g += N.color[1] * df * N.energy;
+        b += N.color[2] * df * N.energy;
+    }
+}
+
 // One light's contribution to one vertex (ILight.VertexLight, light.go:115-663).
 // M (model transform) and dirrot (workingModelRotation) live in shared memory.
 // For a skinned model vpos and vnrm are already in world space (light.go:334-343, :613-620).
 template <bool kSkin>
 __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3 vpos, f3 vnrm, const float* M,
-                                             const float* dirrot, const float* __restrict__ cells, float& r, float& g,
-                                             float& b) {
+                                             const float* dirrot, const float* __restrict__ cells, const NestedSrc& ns,
+                                             float& r, float& g, float& b) {
     const bool mat = flags & SEG_MAT;
     const uint32_t lmode = seg_light_mode(flags);
     switch (L.type) {
@@ -317,6 +373,11 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
             if (lv_cell(G, mode == T3D_LV_PER_VERTEX_WITH_NORMAL ? vertPosN : vertPos, idx)) {
                 const float* c = cells + 4 * (size_t)(G.cell_first + idx);
                 cr = c[0]; cg = c[1]; cb = c[2];
+                if (kSkin && (flags & SEG_NESTED)) {  // the cell's useLights, before its colour (light.go:650-656)
+                    const uint32_t cc = G.cell_first + idx;
+                    for (uint32_t u = ns.off[cc]; u < ns.off[cc + 1]; u++)
+                        nested_light(ns.lights[ns.items[u]], flags, vpos, vnrm, dirrot, ns.inv_r, r, g, b);
+                }
             }
         }
         r += L.cr * cr * L.energy;
@@ -359,6 +420,7 @@ struct ModelSmem {
     EmitConst ec;
     uint32_t nl;
     uint32_t pad[3];
+    NestedSrc nested;  // SEG_NESTED: lights used by light-volume cells
 };
 
 struct TileSmem {
@@ -433,6 +495,12 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
         if (!cam.render_depth && cam.fog_on && cam.fog_mode == T3D_FOG_SUB) f |= EC_FOG_SUB;
         if (seg.flags & SEG_LIT) f |= EC_LIT;
         if (seg.flags & SEG_COLORS) f |= EC_COLORS;
+        if (kSkin && (seg.flags & SEG_NESTED)) {
+            ms.nested.lights = J.lights;
+            ms.nested.off = J.cell_use_off;
+            ms.nested.items = J.cell_use_items;
+            ms.nested.inv_r = pr.inv_r;
+        }
         if (kSkin && (seg.flags & SEG_SNAP)) {
             f |= EC_SNAP;
             e.snap = cam.snap;
@@ -574,7 +642,7 @@ __device__ __forceinline__ void vertex_record(const ModelSmem& ms, const float4 
         float lr = 0.0f, lg = 0.0f, lb = 0.0f;
         const uint32_t nl = ms.nl;
         for (uint32_t k = 0; k < nl; k++)
-            light_vertex<kSkin>(ms.lights[k], e.seg_flags, vert, vnrm, ms.M, ms.dirrot, e.cells, lr, lg, lb);
+            light_vertex<kSkin>(ms.lights[k], e.seg_flags, vert, vnrm, ms.M, ms.dirrot, e.cells, ms.nested, lr, lg, lb);
         cr *= lr; cg *= lg; cb *= lb;
     }
     float depth = 0.0f;

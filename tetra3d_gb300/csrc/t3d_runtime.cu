@@ -664,6 +664,48 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         (rc = sc->sub_levels.ensure(ctx, 8 * std::max<uint32_t>(1, nlev))))
         return rc;
     sc->num_sub_levels = nlev;
+    // LightVolumeCell.useLights: offsets per cell, items are scene light indices
+    {
+        const uint32_t nc = d->num_volume_cells;
+        std::vector<uint32_t> off(nc + 1, 0u), items;
+        sc->light_uses.assign(d->num_lights, 0);
+        sc->light_nested.assign(d->num_lights, 0);
+        if (d->cell_use_offsets) {
+            if (!d->cell_use_items && d->cell_use_offsets[nc] > d->cell_use_offsets[0]) {
+                set_err(ctx, "scene_upload: cell_use_offsets without cell_use_items");
+                return T3D_E_INVAL;
+            }
+            for (uint32_t c = 0; c <= nc; c++) {
+                off[c] = d->cell_use_offsets[c] - d->cell_use_offsets[0];
+                if (c && off[c] < off[c - 1]) {
+                    set_err(ctx, "scene_upload: cell_use_offsets decrease at cell %u", c);
+                    return T3D_E_INVAL;
+                }
+            }
+            items.assign(d->cell_use_items + d->cell_use_offsets[0], d->cell_use_items + d->cell_use_offsets[nc]);
+            for (uint32_t li : items) {
+                if (li >= d->num_lights || d->lights[li].type == T3D_LIGHT_VOLUME) {
+                    set_err(ctx, "scene_upload: a cell uses light %u, which is not an ambient, point or directional light", li);
+                    return T3D_E_INVAL;
+                }
+                sc->light_nested[li] = 1;
+            }
+            for (uint32_t i = 0; i < d->num_lights; i++) {
+                const t3d_light_desc& l = d->lights[i];
+                if (l.type != T3D_LIGHT_VOLUME) continue;
+                const uint64_t cells = (uint64_t)std::max(0, l.cell_count[0]) * std::max(0, l.cell_count[1]) *
+                                       std::max(0, l.cell_count[2]);
+                sc->light_uses[i] = off[l.cell_first + cells] > off[l.cell_first];
+            }
+        }
+        if ((rc = sc->cell_use_off.ensure(ctx, 4ull * (nc + 1))) ||
+            (rc = sc->cell_use_items.ensure(ctx, 4ull * std::max<size_t>(1, items.size()))))
+            return rc;
+        CK(cudaMemcpy(sc->cell_use_off.ptr, off.data(), 4ull * (nc + 1), cudaMemcpyHostToDevice));
+        sc->cell_use_host = off;
+        if (!items.empty())
+            CK(cudaMemcpy(sc->cell_use_items.ptr, items.data(), 4ull * items.size(), cudaMemcpyHostToDevice));
+    }
     if (nlev) CK(cudaMemcpy(sc->sub_levels.ptr, d->subdivision_levels, 8ull * nlev, cudaMemcpyHostToDevice));
     if (d->num_bones && !d->bones) {
         set_err(ctx, "scene_upload: num_bones without bone matrices");
@@ -876,6 +918,8 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.sub_levels = (const float*)sc->sub_levels.ptr;
         dj.nsub_levels = sc->num_sub_levels;
         dj.pad_sub = 0;
+        dj.cell_use_off = (const uint32_t*)sc->cell_use_off.ptr;
+        dj.cell_use_items = (const uint32_t*)sc->cell_use_items.ptr;
         const uint32_t light_base = (uint32_t)F.lights.size();
         for (const auto& l : sc->lights) {
             DevLight L;
@@ -894,6 +938,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         // dynamic batches: the members of each (owner, owner part), in model order
         std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>> batches;
         std::vector<char> owner(sc->models.size(), 0);
+        std::vector<char> nested(sc->models.size(), 0);  // the model's lights include a volume whose cells use lights
         for (uint32_t mi = 0; mi < sc->models.size(); mi++)
             if (sc->models[mi].d.batched) {
                 batches[{sc->models[mi].d.batch_owner, sc->models[mi].d.batch_part}].push_back(mi);
@@ -915,6 +960,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             for (uint32_t li : list == 0 ? scene_lights : sc->lists[list]) {
                 if (!light_enabled(jobs[j].light_mask, li)) continue;
                 F.inst_light_idx.push_back(li);  // relative to the job's light table (DevJob.lights)
+                if (sc->light_uses[li]) nested[mi] = 1;
                 cnt++;
             }
             if (cnt > (uint32_t)kMaxLights) {
@@ -1015,6 +1061,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if ((m.d.color[3] == 0 && is_transparent(m.d.color, mat)) || part.d.tri_count == 0) flags |= SEG_SKIP;
             bool lit = cd.lighting_on && !(mat.present && mat.shadeless) && !m.d.shadeless;
             if (lit) flags |= SEG_LIT;
+            if (lit && nested[rp.model]) flags |= SEG_NESTED;
             if (mat.present && mat.backface_culling) flags |= SEG_BACKFACE;
             if (me.colors) flags |= SEG_COLORS;
             if (mat.present) flags |= SEG_MAT;

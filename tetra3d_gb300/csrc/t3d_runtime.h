@@ -57,15 +57,21 @@ struct Scene {
     uint64_t struct_ver = 0, model_ver = 0;
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     DevBuf shape_a, shape_b, shape_w, vjoint, vweight, bones;
-    DevBuf sub_info, sub_rel, sub_levels;
+    DevBuf sub_info, sub_rel, sub_levels, cell_use_off, cell_use_items;
+    std::vector<char> light_uses;    // per light: a volume whose cells use lights
+    std::vector<char> light_nested;  // per light: used by some cell (cannot become a volume)
+    std::vector<uint32_t> cell_use_host;  // host copy of the cell use offsets
+    bool cell_uses_between(uint64_t c0, uint64_t c1) const {
+        return c1 < cell_use_host.size() && cell_use_host[c1] > cell_use_host[c0];
+    }
     uint32_t num_bones = 0, num_keys = 0, num_sub_levels = 0, num_cells = 0;
     uint64_t device_bytes() const {
         return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap +
                shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap + sub_info.cap + sub_rel.cap +
-               sub_levels.cap;
+               sub_levels.cap + cell_use_off.cap + cell_use_items.cap;
     }
     void release() {
-        sub_info.release(); sub_rel.release(); sub_levels.release();
+        sub_info.release(); sub_rel.release(); sub_levels.release(); cell_use_off.release(); cell_use_items.release();
         shape_a.release(); shape_b.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
         va.release(); vb.release(); vc.release(); idx.release(); centers.release();
         dmeshes.release(); dmodels.release(); cells.release();

@@ -348,6 +348,7 @@ class SceneData:
         self.camera = None
         self.bones = None  # (NB, 16) Node.boneInfluence matrices
         self.subdivision_levels = None  # (L, 2) AutoSubdivisionLevel: DistanceSquared, MaximumTriangleSize
+        self.cell_uses = None           # per light-volume cell: light indices (LightVolumeCell.useLights)
         self.max_subdivisions = 0       # Library.maxAutoSubdivisionCount (0: 3)
         self.meta = {}
         self._keep = []
@@ -415,6 +416,13 @@ class SceneData:
             keep.append(lev)
             sd.subdivision_levels, sd.num_subdivision_levels = abi.fptr(lev), lev.shape[0]
         sd.max_subdivisions = int(self.max_subdivisions)
+        if self.cell_uses is not None:
+            offs = np.zeros(self.ncells + 1, np.uint32)
+            for c in range(self.ncells):
+                offs[c + 1] = offs[c] + len(self.cell_uses[c])
+            items = np.array([x for c in range(self.ncells) for x in self.cell_uses[c]] or [0], np.uint32)
+            keep += [offs, items]
+            sd.cell_use_offsets, sd.cell_use_items = abi.uptr(offs), abi.uptr(items)
         self._keep = keep
         return sd
 
@@ -993,6 +1001,19 @@ def down_camera(w=1280, h=720):
     return camera(pos=(0.0, 10.0, 0.0), rot=rotate(1, 0, 0, deg2rad(-90.0)), w=w, h=h, fov=70.0, near=0.1, far=60.0)
 
 
+def nested_light_scene(seed=5, n=48, w=1280, h=720):
+    """The feature scene with LightVolumeCell.useLights: about 70 % of the light-volume cells
+    use one to three of the scene's ambient, point and directional lights (the lights may also be
+    in the light lists)."""
+    sd = feature_scene(seed, n, w, h)
+    rng = np.random.Generator(np.random.PCG64([seed, 77]))
+    usable = [i for i in range(sd.nlights) if sd.lights[i].type != abi.LIGHT_VOLUME]
+    sd.cell_uses = [list(rng.choice(usable, int(rng.integers(1, 4)), replace=False)) if rng.random() < 0.7 else []
+                    for _ in range(sd.ncells)]
+    sd.name = f"nested{seed}"
+    return sd
+
+
 FEATURE_CAMERAS = ["persp", "ortho", "unlit", "fog_add", "fog_sub", "fog_overwrite", "corrected", "tilted"]
 
 
@@ -1041,4 +1062,5 @@ def subset(sd, models):
     out.bones = sd.bones
     out.subdivision_levels = sd.subdivision_levels
     out.max_subdivisions = sd.max_subdivisions
+    out.cell_uses = sd.cell_uses
     return out
