@@ -248,14 +248,16 @@ struct NestedSrc {
 
 // A light used by a light-volume cell, lit at the vertex that fell into that cell
 // (light.go:652-654): its VertexLight as after its beginModel (light.go:175-189,
-// :326-330), without the model-level range skip of the scene's lights.
-__device__ __noinline__ void nested_light(const DevLight& N, uint32_t flags, f3 vpos, f3 vnrm, const float* dirrot,
-                                          const float* __restrict__ r_, float& r, float& g, float& b) {
+// :326-330), without the model-level range skip of the scene's lights. Returns
+// the vertex's light sums (r, g, b) with this light added.
+__device__ __noinline__ float3 nested_light(const DevLight& N, uint32_t flags, f3 vpos, f3 vnrm, const float* dirrot,
+                                            const float* __restrict__ r_, float r, float g, float b) {
     const bool mat = flags & SEG_MAT;
     const uint32_t lmode = seg_light_mode(flags);
     const bool skinned = flags & SEG_SKINNED;
     if (N.type == T3D_LIGHT_AMBIENT) {
         r += N.amb[0]; g += N.amb[1]; b += N.amb[2];
+        return make_float3(r, g, b);
     } else if (N.type == T3D_LIGHT_POINT) {
         const f3 lp = mk3(N.wpos[0], N.wpos[1], N.wpos[2]);
         f3 work = lp;
@@ -267,9 +269,9 @@ __device__ __noinline__ void nested_light(const DevLight& N, uint32_t flags, f3 
         }
         const float distance = dist2(work, vpos);
         if (N.range > 0.0f) {
-            if (distance > N.range2) return;
+            if (distance > N.range2) return make_float3(r, g, b);
         } else {
-            if (1.0f / distance * N.energy < 0.001f) return;
+            if (1.0f / distance * N.energy < 0.001f) return make_float3(r, g, b);
         }
         const f3 lightVec = unit3(sub3(work, vpos));
         const f3 n = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? lightVec : vnrm;
@@ -287,11 +289,12 @@ __device__ __noinline__ void nested_light(const DevLight& N, uint32_t flags, f3 
         const f3 normal = (mat && lmode == T3D_LIGHTING_FIXED_NORMALS) ? fwd : skinned ? vnrm : mult_vec_s(dirrot, vnrm);
         float df = dot3(normal, fwd);
         if (mat && lmode == T3D_LIGHTING_DOUBLE_SIDED) df = fabsf(df);
-        if (df <= 0.0f) return;
+        if (df <= 0.0f) return make_float3(r, g, b);
         r += N.color[0] * df * N.energy;
         g += N.color[1] * df * N.energy;
         b += N.color[2] * df * N.energy;
     }
+    return make_float3(r, g, b);
 }
 
 // One light's contribution to one vertex (ILight.VertexLight, light.go:115-663).
@@ -376,7 +379,10 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
                 if (kSkin && (flags & SEG_NESTED)) {  // the cell's useLights, before its colour (light.go:650-656)
                     const uint32_t cc = G.cell_first + idx;
                     for (uint32_t u = ns.off[cc]; u < ns.off[cc + 1]; u++)
-                        nested_light(ns.lights[ns.items[u]], flags, vpos, vnrm, dirrot, ns.inv_r, r, g, b);
+                    {
+                        const float3 o = nested_light(ns.lights[ns.items[u]], flags, vpos, vnrm, dirrot, ns.inv_r, r, g, b);
+                        r = o.x; g = o.y; b = o.z;
+                    }
                 }
             }
         }
