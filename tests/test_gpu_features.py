@@ -538,3 +538,51 @@ def test_cell_use_lights_match_oracle(ctx, variant):
         assert ctx.lib.t3d_scene_set_lights(ctx.h, sid, used[0], bad, 1) == abi.T3D_E_INVAL
     finally:
         ctx.release(sid)
+
+
+def test_all_features_in_one_launch(ctx):
+    """Skinned, shape-keyed, billboarded, auto-subdivided, dynamically batched and cell-lit
+    scenes as four jobs of one batched launch (with light masks, MaxLightCount and vertex
+    snapping on some), and the same jobs one launch per pair: every job bit-exact."""
+    sk, bb = scenes.skinned_scene(7), scenes.billboard_scene(9)
+    sub, bat = scenes.subdivision_scene(10), scenes.batch_scene(11)
+    nested = scenes.nested_light_scene(6)
+    ids = [ctx.upload(x) for x in (sk, bb, sub, bat, nested)]
+    try:
+        c0 = scenes.feature_camera("tilted")
+        c1 = scenes.feature_camera("persp")
+        c1.vertex_snapping = 16.0
+        c2 = scenes.feature_camera("fog_sub")
+        c3 = scenes.feature_camera("persp")
+        c3.max_light_count = 3
+        c4 = scenes.feature_camera("ortho")
+        specs = [(ids[0], sk, c0, None), (ids[1], bb, c1, ((1 << 128) - 1) & ~(1 << 2)),
+                 (ids[2], sub, c2, None), (ids[3], bat, c3, None), (ids[4], nested, c4, ((1 << 128) - 1) & ~(1 << 1))]
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render_jobs([job(s, cam, mask) for s, _, cam, mask in specs], mode=mode)
+            parts = split_jobs(ctx.download(), len(specs))
+            for j, (s, sd, cam, mask) in enumerate(specs):
+                assert_frames_equal(parts[j], pyoracle.render(sd, cam, light_mask=mask), f"job{j}/mode{mode}")
+    finally:
+        for s in ids:
+            ctx.release(s)
+
+
+def test_graph_replay_follows_bone_updates(ctx):
+    """A captured frame of a skinned scene replayed after new bone influences: the graph reads
+    the bones from the device, so each replay matches the oracle with the current bones."""
+    sd = scenes.skinned_scene(8)
+    cam = scenes.feature_camera("persp")
+    nskin = int(sd.mv["skinned"].sum())
+    pos = sd.mv["position"][:nskin, :3]
+    rng = np.random.default_rng(21)
+    sid = ctx.upload(sd)
+    try:
+        ctx.graph_capture(sid, cam, animate=False)
+        for k in range(2):
+            ctx.graph_replay(1)
+            assert_frames_equal(ctx.download(), pyoracle.render(sd, cam), f"replay {k}")
+            sd.bones = scenes.tube_bones(rng, nskin, pos, bend=0.7)
+            ctx.set_bones(sid, sd.bones)
+    finally:
+        ctx.release(sid)
