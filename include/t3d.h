@@ -13,7 +13,15 @@
  *   Model.ProcessVertices       model.go:600-995     -> device vertex + triangle phases
  *   sortingTriangleBucket       sortingTriangles.go  -> device segmented 512-bin counting sort
  *   ILight.beginModel / Light   light.go:110-663     -> device model-prep + vertex phases
- *   flush (vertex lists)        camera.go:1829-2048  -> t3d_frame_* (resident device buffers)
+ *   flush (vertex lists)        camera.go:1829-2048  -> t3d_frame_* (resident device buffers),
+ *                                                       t3d_frame_raster (depth + colour passes)
+ *   Model.skinVertex, shape keys model.go:559-596,   -> device vertex phase
+ *                               mesh.go:796-822
+ *   billboarding                model.go:634-703     -> device vertex phase
+ *   Mesh.SetAutoSubdivide,      mesh.go:447-490,     -> t3d_scene_upload (subdivision) and
+ *   Triangle.handleSubdivision  mesh.go:1877-1949       the device triangle phase (level choice)
+ *   Model.DynamicBatchAdd       model.go:210-245,    -> t3d_model_desc.batched (draw order, flushes)
+ *                               camera.go:2068-2093
  *
  * Conventions
  *  - Matrices are Tetra3D Matrix4 values: 16 floats, row-major, row vectors
