@@ -188,8 +188,8 @@ def run_ours(args, rank, world, local_rank):
     if args.tune:
         from tetra3d_gb300 import autotune
         best, res = autotune.tune(ctx, sid, cam, frames=5, animate=False)
-        tuned = {"tile_tris": best[0], "block_threads": best[1],
-                 "sweep_ms": {f"{t}x{b}": round(v, 4) for (t, b), v in res.items()}}
+        tuned = {"tile_tris": best[0], "block_threads": best[1], "vertex_chunk": best[2],
+                 "sweep_ms": {"x".join(map(str, k)): round(v, 4) for k, v in res.items()}}
         ctx.set_models(sid, sd)  # restore the initial transforms after the sweep
     # ---- device-resident value: captured CUDA graph of the batched frame ----
     ctx.graph_capture(sid, cam, animate=animate)

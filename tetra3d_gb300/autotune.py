@@ -1,9 +1,10 @@
 """Autotuner for the batched frame kernel.
 
 Sweeps the launch shape knobs of the persistent kernel -- triangles per tile
-(the unit of the visibility / sort / emit work queues) and threads per block --
-on the caller's own scene and camera, timing captured-graph replays with CUDA
-events, and leaves the context on the fastest setting. The 512-bin sort itself
+(the unit of the visibility / sort / emit work queues) and threads per block,
+then vertices per vertex-phase work item -- on the caller's own scene and
+camera, timing captured-graph replays with CUDA events, and leaves the context
+on the fastest setting. The 512-bin sort itself
 is fixed by the reference's bucket sort (sortingTriangles.go:166-168), so its
 radix is not a free parameter.
 """
@@ -13,6 +14,7 @@ import time
 
 TILES = (1024, 2048, 4096)
 BLOCKS = (128, 256)
+CHUNKS = (2048, 4096, 8192)
 
 
 def time_config(ctx, sid, cam, tile, block, frames=10, warmup=3, animate=False):
@@ -31,8 +33,8 @@ def time_config(ctx, sid, cam, tile, block, frames=10, warmup=3, animate=False):
     return e0.elapsed_time(e1) / frames
 
 
-def tune(ctx, sid, cam, frames=10, tiles=TILES, blocks=BLOCKS, animate=False, verbose=False):
-    """Returns (best (tile, block), {config: ms per frame}); leaves ctx tuned to the best."""
+def tune(ctx, sid, cam, frames=10, tiles=TILES, blocks=BLOCKS, chunks=CHUNKS, animate=False, verbose=False):
+    """Returns (best (tile, block, vertex chunk), {config: ms per frame}); leaves ctx tuned to the best."""
     results = {}
     t0 = time.time()
     for tile, block in itertools.product(tiles, blocks):
@@ -47,6 +49,17 @@ def tune(ctx, sid, cam, frames=10, tiles=TILES, blocks=BLOCKS, animate=False, ve
             print(f"autotune: tile {tile:5d} block {block:3d}: {ms:.3f} ms/frame")
     best = min(results, key=results.get)
     ctx.set_tuning(tile_tris=best[0], block_threads=best[1])
+    # second stage: the vertex chunk at the best tile and block
+    chunk_ms = {}
+    for ch in chunks:
+        ctx.set_tuning(vertex_chunk=ch)
+        chunk_ms[ch] = time_config(ctx, sid, cam, best[0], best[1], frames=frames, animate=animate)
+        results[(best[0], best[1], ch)] = chunk_ms[ch]
+        if verbose:
+            print(f"autotune: tile {best[0]:5d} block {best[1]:3d} chunk {ch:5d}: {chunk_ms[ch]:.3f} ms/frame")
+    bch = min(chunk_ms, key=chunk_ms.get)
+    ctx.set_tuning(vertex_chunk=bch)
+    best = (best[0], best[1], bch)
     if verbose:
         print(f"autotune: best {best} in {time.time() - t0:.1f} s")
     return best, results
