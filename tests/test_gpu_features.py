@@ -586,3 +586,52 @@ def test_graph_replay_follows_bone_updates(ctx):
             ctx.set_bones(sid, sd.bones)
     finally:
         ctx.release(sid)
+
+
+def test_edge_cases_match_oracle(ctx):
+    """Empty and degenerate inputs: a scene without models, a frame where every model is culled,
+    a part with no triangles next to a one-triangle mesh, and a lit scene without lights."""
+    cam = scenes.feature_camera("persp")
+    # no models at all
+    empty = scenes.SceneData([scenes.cube_mesh()], 0, [], [[]], name="empty")
+    sid = ctx.upload(empty)
+    try:
+        ctx.render(sid, cam)
+        st = ctx.sync()
+        assert st.visible_tris == 0
+        assert ctx.download().visible_tris == 0
+    finally:
+        ctx.release(sid)
+    # every model behind the camera
+    sd = scenes.feature_scene(5)
+    sd.mv["position"][:, 2] = 80.0
+    n = sd.nmodels
+    sd.mv["transform"] = scenes.trs(sd.mv["position"], sd.mv["scale"], sd.mv["rotation"].reshape(n, 4, 4)).reshape(n, 16)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        got = ctx.download()
+        ref = pyoracle.render(sd, cam)
+        assert ref.visible_tris == 0
+        assert_frames_equal(got, ref, "all culled")
+    finally:
+        ctx.release(sid)
+    # an empty part and a single triangle, lit by an empty light list
+    tri = scenes.MeshData(np.array([(-1, -1, 0), (1, -1, 0), (0, 1, 0)], np.float32),
+                          np.tile(np.array([0, 0, 1], np.float32), (3, 1)), np.zeros((3, 2), np.float32),
+                          np.array([(0, 1, 2)], np.uint32))
+    cube = scenes.cube_mesh()
+    cube.parts = [dict(tri_start=0, tri_count=0, mat=scenes.default_material()),
+                  dict(tri_start=0, tri_count=12, mat=scenes.default_material(backface_culling=0))]
+    sd = scenes.SceneData([tri, cube], 2, [], [[]], name="degenerate")
+    scenes.set_models_trs(sd, [0, 1], np.array([(0, 0, -4), (2, 0, -6)], np.float32), np.ones((2, 3), np.float32),
+                          scenes.ident(2))
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            ref = pyoracle.render(sd, cam)
+            assert ref.visible_tris > 0
+            assert_frames_equal(ctx.download(), ref, f"degenerate/mode{mode}")
+    finally:
+        ctx.release(sid)
