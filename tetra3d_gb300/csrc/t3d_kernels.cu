@@ -1025,7 +1025,6 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
     uint32_t item = P.vitem_begin + next_item(P.ctl, 6, s_item);
     while (item < P.vitem_alt) {
-        // the next item's queue slot is fetched now and read at the end of this one
         const uint32_t s = P.vitem_seg[item];
         const DevSeg seg = P.segs[s];
         if (!((seg.flags & SEG_SKIP) || P.preps[seg.inst].culled)) {
@@ -1119,7 +1118,6 @@ __device__ __forceinline__ void triangle_tiles(const FrameParams& P, unsigned ch
     uint32_t item = T3D_TILE_FIRST + next_item(P.ctl, q, &sm.item);
     while (item < T3D_TILE_END) {
         if (threadIdx.x == blockDim.x - 32 && item + gridDim.x < T3D_TILE_END) prefetch_triangle_tile(P, item + gridDim.x);
-        // the next item's queue slot is fetched now and read at the end of this one
         const TileDesc td = P.tiles[item];
         const uint32_t s = td.seg;
         const bool multi = td.flags & SEG_MULTI;
