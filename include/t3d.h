@@ -427,7 +427,9 @@ typedef struct t3d_completion {
 
 /* hbm_budget_bytes bounds the device bytes of in-flight requests' outputs and
  * scratch; max_batch bounds the jobs per launch; streams = launch slots that
- * run concurrently. */
+ * run concurrently. The slots render the context's resident scenes: while a
+ * server runs, scenes are not uploaded, released or changed (set_models /
+ * set_bones / set_shape_weights / set_lights) on that context. */
 int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batch,
                       uint32_t streams, t3d_server** out);
 int t3d_server_destroy(t3d_server* srv);
