@@ -94,18 +94,23 @@ struct t3d_server {
         std::vector<uint64_t> vis(s.batch.size(), 0), sum(s.batch.size(), 1469598103934665603ull);
         if (rc == T3D_OK) {
             const auto& info = s.ctx->tables.seg_info;
-            std::vector<float> buf;
-            for (const auto& si : info) {
-                if (si.job >= s.batch.size()) continue;
-                vis[si.job] += si.count;
-                if (verify && si.count) {
-                    buf.resize(12ull * si.count);
-                    cudaMemcpy(buf.data(), (char*)s.ctx->out_xyuv.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
-                    sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
-                    cudaMemcpy(buf.data(), (char*)s.ctx->out_rgba.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost);
-                    sum[si.job] = fnv(buf.data(), 48ull * si.count, sum[si.job]);
-                    cudaMemcpy(buf.data(), (char*)s.ctx->out_depth.ptr + 12ull * si.base, 12ull * si.count, cudaMemcpyDeviceToHost);
-                    sum[si.job] = fnv(buf.data(), 12ull * si.count, sum[si.job]);
+            for (const auto& si : info)
+                if (si.job < s.batch.size()) vis[si.job] += si.count;
+            if (verify && !info.empty()) {
+                // one copy of each output stream for the whole batch, then the hashes of
+                // every pair's written slots in emit order
+                uint64_t slots = 0;
+                for (const auto& si : info) slots = std::max<uint64_t>(slots, (uint64_t)si.base + si.capacity);
+                std::vector<float> xy(12 * slots), rg(12 * slots), dp(3 * slots);
+                if (slots && (cudaMemcpy(xy.data(), s.ctx->out_xyuv.ptr, 48 * slots, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                              cudaMemcpy(rg.data(), s.ctx->out_rgba.ptr, 48 * slots, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                              cudaMemcpy(dp.data(), s.ctx->out_depth.ptr, 12 * slots, cudaMemcpyDeviceToHost) != cudaSuccess))
+                    rc = T3D_E_CUDA;
+                for (const auto& si : info) {
+                    if (rc != T3D_OK || si.job >= s.batch.size() || !si.count) continue;
+                    sum[si.job] = fnv(xy.data() + 12ull * si.base, 48ull * si.count, sum[si.job]);
+                    sum[si.job] = fnv(rg.data() + 12ull * si.base, 48ull * si.count, sum[si.job]);
+                    sum[si.job] = fnv(dp.data() + 3ull * si.base, 12ull * si.count, sum[si.job]);
                 }
             }
         }
