@@ -635,3 +635,40 @@ def test_edge_cases_match_oracle(ctx):
             assert_frames_equal(ctx.download(), ref, f"degenerate/mode{mode}")
     finally:
         ctx.release(sid)
+
+
+def test_multi_tile_altered_parts(ctx):
+    """Skinned, shape-keyed, billboarded and auto-subdivided parts large enough to span several
+    triangle tiles: their tiles go through the histogram / scan / rank phases like plain ones."""
+    rng = np.random.default_rng(31)
+    tube = scenes.tube_mesh(rings=120, segments=40, height=3.0)
+    tube.parts = [dict(tri_start=0, tri_count=tube.ntris, mat=scenes.default_material(backface_culling=0))]
+    tube.joints, tube.weights = scenes.tube_skin(tube, rng, 4)
+    tube.shape_positions = (0.05 * rng.standard_normal((1, tube.nverts, 3))).astype(np.float32)
+    tube.shape_normals = (0.05 * rng.standard_normal((1, tube.nverts, 3))).astype(np.float32)
+    tube.shape_weights = np.array([0.5], np.float32)
+    grid = scenes.grid_mesh(40, 40, 8.0, 8.0, lambda X, Z: 0.3 * np.sin(X) * np.cos(Z), x0=-4.0, z0=-4.0)
+    grid.parts = [dict(tri_start=0, tri_count=grid.ntris, mat=scenes.default_material(backface_culling=0))]
+    grid.auto_subdivide = 1
+    bb = scenes.grid_mesh(80, 80, 4.0, 4.0, lambda X, Z: 0.0 * X, x0=-2.0, z0=-2.0)
+    bb.parts = [dict(tri_start=0, tri_count=bb.ntris,
+                     mat=scenes.default_material(backface_culling=0, billboard=1, billboard_lock=(0, 1, 0)))]
+    base = scenes.feature_scene(5, n=4)
+    sd = scenes.SceneData([tube, grid, bb], 3, [base.lights[i] for i in range(base.nlights)], base.lists,
+                          cells=base.cells[:base.ncells], name="big_altered")
+    pos = np.array([(0.0, -1.5, -8.0), (0.0, -2.0, -7.0), (3.0, 1.0, -10.0)], np.float32)
+    scenes.set_models_trs(sd, [0, 1, 2], pos, np.ones((3, 3), np.float32), scenes.ident(3), frustum=0)
+    sd.mv["skinned"][0] = 1
+    sd.bones = scenes.tube_bones(rng, 1, pos[:1], 4, bend=0.8)
+    sd.subdivision_levels = np.array([(100.0, 0.05), (400.0, 0.2)], np.float32)
+    sd.max_subdivisions = 2
+    cam = scenes.feature_camera("persp")
+    ref = pyoracle.render(sd, cam)
+    assert max(s["capacity"] for s in ref.segments) > 2 * 2048
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), ref, f"big altered/mode{mode}")
+    finally:
+        ctx.release(sid)
