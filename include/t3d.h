@@ -353,7 +353,8 @@ int         t3d_create(int device, t3d_ctx** out);
 int         t3d_destroy(t3d_ctx* ctx);
 const char* t3d_last_error(const t3d_ctx* ctx);
 /* Tuning knobs (0 keeps the current value): triangles per tile (power of two,
- * 256..4096), a reserved value, threads per block (128 or 256). */
+ * 256..4096), vertices per vertex-phase work item (32..2^20), threads per block
+ * (128 or 256). */
 int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint32_t block_threads);
 
 /* ---- resident scenes --------------------------------------------------------- */
@@ -361,9 +362,10 @@ int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chu
  * per-frame reads of Mesh/Model/Light state. */
 int t3d_scene_upload(t3d_ctx* ctx, const t3d_scene_desc* desc, uint32_t* scene_out);
 int t3d_scene_release(t3d_ctx* ctx, uint32_t scene);
-/* Per-frame transform update (Node.Transform changes): n model descs'
- * transform/world_rotation/position/scale/rotation/rotate_step fields,
- * for models [first, first+n). */
+/* Per-frame model update (Node.Transform changes, visibility, colour, ...): the
+ * n model descs of models [first, first+n). The descs are copied during the call;
+ * the device copy is queued behind the frames already issued, so the call does
+ * not wait for them and the next render sees the new models. */
 int t3d_scene_set_models(t3d_ctx* ctx, uint32_t scene, uint32_t first,
                          const t3d_model_desc* models, uint32_t n);
 /* Reads back the current (possibly animated) per-model transforms, 16 floats each. */
