@@ -371,7 +371,9 @@ struct Subdivider {
 };
 }  // namespace
 
-void subdivide_mesh(const t3d_mesh_desc& me, const float* lev, uint32_t nlev, uint32_t maxsub, SubdividedMesh& S) {
+// Returns false (and stops) once the listed triangles pass `max_tris`.
+bool subdivide_mesh(const t3d_mesh_desc& me, const float* lev, uint32_t nlev, uint32_t maxsub, SubdividedMesh& S,
+                    uint64_t max_tris) {
     const size_t nv = me.num_vertices;
     S.pos.assign(me.positions, me.positions + 3 * nv);
     S.nrm.assign(me.normals, me.normals + 3 * nv);
@@ -419,6 +421,7 @@ void subdivide_mesh(const t3d_mesh_desc& me, const float* lev, uint32_t nlev, ui
                     S.info.push_back(info);
                     S.rel.push_back(make_int4(L, nl, (int)(e - base), 0));
                 }
+            if (S.idx.size() / 3 > max_tris || S.pos.size() / 3 > max_tris) return false;
         }
         part.tri_start = first;
         part.tri_count = (uint32_t)(S.idx.size() / 3) - first;
@@ -443,6 +446,7 @@ void subdivide_mesh(const t3d_mesh_desc& me, const float* lev, uint32_t nlev, ui
                 if (S.desc.dim_max[c] < p) S.desc.dim_max[c] = p;
             }
     }
+    return true;
 }
 
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
@@ -499,8 +503,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
                 return T3D_E_INVAL;
             }
         subs[m] = std::make_unique<SubdividedMesh>();
-        subdivide_mesh(me, d->subdivision_levels, nlev, maxsub, *subs[m]);
-        if (subs[m]->pos.size() / 3 > 0xFFFFFFF0ull || subs[m]->idx.size() / 3 > 0x50000000ull) {
+        if (!subdivide_mesh(me, d->subdivision_levels, nlev, maxsub, *subs[m], 0x40000000ull)) {
             set_err(ctx, "mesh %u: subdivided mesh too large for 32-bit indexing", m);
             return T3D_E_INVAL;
         }
