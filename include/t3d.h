@@ -122,6 +122,15 @@ typedef struct t3d_material {
     int32_t billboard_lock[3]; /* BillboardLockX, BillboardLockY, BillboardLockZ */
     int32_t billboard_up;      /* T3D_BILLBOARD_UP_* */
     int32_t billboard_depth;   /* T3D_DEPTH_* */
+    /* Rasteriser only (t3d_frame_raster): the material's texture when UseTexture is set
+     * (0 = the default white image, k = texture k - 1 of t3d_raster_set_textures), its
+     * TextureFilterMode (0 nearest, 1 bilinear), TextureMapMode (0 UV, 1 screen) and
+     * TextureMapScreenSizeMultiplierW/H (the reference's default is 1, 1). */
+    uint32_t texture;
+    int32_t  texture_filter;
+    int32_t  texture_map_mode;
+    float    texture_map_scale[2];
+    int32_t  reserved_tex;
 } t3d_material;
 
 /* A MeshPart (mesh.go:2183-2190): a contiguous triangle range with one material. */
@@ -448,18 +457,30 @@ int t3d_server_replay(t3d_server* srv, const t3d_request* reqs, uint32_t n, t3d_
 
 /* ---- rasterising the emitted stream ----------------------------------------- */
 /* The colour and depth passes of flush (camera.go:1829-2048) over one job of the
- * last rendered frame, on the device: per render pair in draw order, the depth pass
- * (camera.go:350-383: encodeDepth into an RGBA8 intermediate, tested against the depth
- * texture of the pairs before, composited into it unless the pair is transparent) and
- * the colour pass (shaders/base3d.kage: vertex colour times the default white texture,
- * alpha premultiplied, fog by the pair's depth with FogCurve and dithering, source-over
+ * last rendered frame, on the device: per flush (a render pair, or a dynamic batch) in
+ * draw order, the depth pass (camera.go:350-383: encodeDepth into an RGBA8
+ * intermediate, tested against the depth texture of the flushes before, composited
+ * into it unless the flush is transparent; for TransparencyModeAlphaClip the
+ * clip-alpha shader, camera.go:390-480, which drops fragments whose texture alpha is
+ * 0.8 or less) and the colour pass (shaders/base3d.kage: texture -- nearest or
+ * bilinear, wrapped, UV or screen mapped -- times the vertex colour, alpha
+ * premultiplied, fog by the flush's depth with FogCurve and dithering, source-over
  * blending); with RenderDepth off, the plain source-over triangle draw. The camera's
  * fog settings are the World's (FogOn, FogMode, FogRange, FogColor). Images are RGBA8,
  * premultiplied, row-major, camera width x height, cleared to 0 first, like ebiten
  * images. Coverage: pixel centres, top-left fill rule; attributes interpolated linearly
- * in screen space. Textures other than the default image, blend modes other than
- * source-over and custom fragment shaders are not supported. No reference counterpart
- * runs on the device: the reference hands these passes to ebiten. */
+ * in screen space; a texel is the one containing the sample point. Blend modes other
+ * than source-over, custom fragment shaders and textures under
+ * PerspectiveCorrectedTextureMapping (it needs the 1/w vertex attribute) are not
+ * supported. No reference counterpart runs on the device: the reference hands these
+ * passes to ebiten. */
+/* An RGBA8 texture as ebiten stores it (premultiplied, row-major). */
+typedef struct t3d_texture_desc {
+    const uint8_t* rgba8;
+    int32_t        width, height;
+} t3d_texture_desc;
+/* Replaces the context's raster texture table (materials refer to entry k as k + 1). */
+int t3d_raster_set_textures(t3d_ctx* ctx, const t3d_texture_desc* textures, uint32_t n);
 typedef struct t3d_raster_opts {
     int32_t fog_curve;     /* World.FogCurve: 0 linear, 1 out-circ, 2 in-circ */
     float   dither_size;   /* World.DitheredFogSize: > 0 enables Bayer-dithered fog */

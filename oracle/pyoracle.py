@@ -169,26 +169,64 @@ def is_transparent(model_row, mat):
     return bool(F(model_row["color"][3]) < F(0.999))
 
 
-def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, transparent=None):
+class OracleTextures(C.Structure):
+    _fields_ = [("flush_texture", C.POINTER(C.c_uint32)), ("flush_flags", C.POINTER(C.c_uint32)),
+                ("flush_scale", C.POINTER(C.c_float)), ("ntex", C.c_uint32), ("tex_offset", C.POINTER(C.c_uint32)),
+                ("tex_w", C.POINTER(C.c_int32)), ("tex_h", C.POINTER(C.c_int32)), ("texels", C.POINTER(C.c_uint32))]
+
+
+def flush_material(scene_data, seg):
+    """The material a flush draws with: a dynamic batch's members flush with the batch pair's
+    part (camera.go:2075-2100, flush at :1829-1845), anything else with its own."""
+    md = scene_data.mv[seg["model"]]
+    if int(md["batched"]):
+        owner = scene_data.mv[int(md["batch_owner"])]
+        return scene_data.meshes[int(owner["mesh"])].parts[int(md["batch_part"])]["mat"]
+    return scene_data.meshes[int(md["mesh"])].parts[seg["part"]]["mat"]
+
+
+def texture_state(mat):
+    """(texture, flags, (scale_w, scale_h)) of a flush material, as the device reads them."""
+    if not mat.get("present", 1):
+        return 0, 0, (0.0, 0.0)
+    flags = (1 if mat.get("texture_filter", 0) else 0) | (2 if mat.get("texture_map_mode", 0) == 1 else 0) | \
+        (4 if mat["transparency_mode"] == abi.TRANSPARENCY_ALPHA_CLIP else 0)
+    return int(mat.get("texture", 0)), flags, tuple(mat.get("texture_map_scale", (1.0, 1.0)))
+
+
+def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, transparent=None, textures=None,
+           flush_tex=None):
     """Oracle of t3d_frame_raster for a one-job frame (an OracleFrame or a downloaded frame, both
     compacted in draw order with .segments). Returns (colour, depth) RGBA8 (height, width, 4).
-    `transparent` (one flag per segment) replaces the flags derived from scene_data."""
+    `transparent` (one flag per segment) replaces the flags derived from scene_data; `textures`
+    is the texture table (premultiplied RGBA8 (height, width, 4) arrays, as given to
+    t3d_raster_set_textures); `flush_tex` (one (texture, flags, (scale_w, scale_h)) per segment)
+    replaces the texture state derived from the flush materials."""
     lib = load()
     fn = lib.t3d_oracle_raster
     u32p, f32p = C.POINTER(C.c_uint32), C.POINTER(C.c_float)
     fn.restype = C.c_int
     fn.argtypes = [C.POINTER(abi.CameraDesc), C.c_int32, C.c_float, C.c_int32, C.c_uint32, f32p, f32p, f32p, u32p,
-                   C.POINTER(C.c_uint8), u32p, u32p]
+                   C.POINTER(C.c_uint8), C.POINTER(OracleTextures), u32p, u32p]
     n = int(frame.xyuv.shape[0])
     pair = np.zeros(max(1, n), np.uint32)
     given = transparent
-    transparent = np.zeros(max(1, len(frame.segments)), np.uint8)
+    nseg = max(1, len(frame.segments))
+    transparent = np.zeros(nseg, np.uint8)
+    ftex, fflags, fscale = np.zeros(nseg, np.uint32), np.zeros(nseg, np.uint32), np.zeros((nseg, 2), np.float32)
     b = 0
     flush = -1
     for k, s in enumerate(frame.segments):
         # the pairs of one dynamic batch are one flush (one depth composite)
         if k == 0 or "draw" not in s or s["draw"] != frame.segments[k - 1]["draw"]:
             flush += 1
+            if flush_tex is not None:
+                st = flush_tex[k]
+            elif textures is not None and scene_data is not None:
+                st = texture_state(flush_material(scene_data, s))
+            else:
+                st = (0, 0, (0.0, 0.0))
+            ftex[flush], fflags[flush], fscale[flush] = st[0], st[1], st[2]
         pair[b:b + s["count"]] = flush
         b += s["count"]
         if given is not None:
@@ -205,9 +243,21 @@ def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, tran
     W, H = cam.width, cam.height
     col = np.zeros(W * H, np.uint32)
     dep = np.zeros(W * H, np.uint32)
+    texs = list(textures or [])
+    sizes = [(int(t.shape[1]), int(t.shape[0])) for t in texs]
+    offs = np.zeros(max(1, len(texs)), np.uint32)
+    offs[1:len(texs)] = np.cumsum([w * h for w, h in sizes])[:-1] if len(texs) > 1 else []
+    tw = np.array([w for w, _ in sizes] or [0], np.int32)
+    th = np.array([h for _, h in sizes] or [0], np.int32)
+    texels = np.concatenate([np.ascontiguousarray(t, np.uint8).reshape(-1, 4).view(np.uint32).reshape(-1)
+                             for t in texs]) if texs else np.zeros(1, np.uint32)
+    assert np.all(ftex[:flush + 1] <= len(texs)), "a flush names a texture beyond the table"
+    ts = OracleTextures(ftex.ctypes.data_as(u32p), fflags.ctypes.data_as(u32p), fscale.ctypes.data_as(f32p), len(texs),
+                        offs.ctypes.data_as(u32p), tw.ctypes.data_as(C.POINTER(C.c_int32)),
+                        th.ctypes.data_as(C.POINTER(C.c_int32)), texels.ctypes.data_as(u32p))
     rc = fn(C.byref(cam), fog_curve, dither_size, fogless, n, xyuv.ctypes.data_as(f32p), rgba.ctypes.data_as(f32p),
             depth.ctypes.data_as(f32p), pair.ctypes.data_as(u32p), transparent.ctypes.data_as(C.POINTER(C.c_uint8)),
-            col.ctypes.data_as(u32p), dep.ctypes.data_as(u32p))
+            C.byref(ts), col.ctypes.data_as(u32p), dep.ctypes.data_as(u32p))
     if rc != 0:
         raise RuntimeError(f"oracle raster failed: {rc}")
     return col.view(np.uint8).reshape(H, W, 4), dep.view(np.uint8).reshape(H, W, 4)

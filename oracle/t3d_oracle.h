@@ -58,13 +58,27 @@ int t3d_oracle_render_f64(const t3d_scene_desc* scene, const t3d_camera_desc* ca
                           const uint64_t* light_mask, uint32_t animate_frames,
                           uint32_t threads, t3d_oracle_out* out);
 
+/* The texture state of each flush and the texture table, for t3d_oracle_raster. */
+typedef struct t3d_oracle_textures {
+    const uint32_t* flush_texture;  /* per flush: 0 the white default image, k texture k - 1 */
+    const uint32_t* flush_flags;    /* per flush: bit 0 bilinear, bit 1 screen mapped, bit 2 alpha clip */
+    const float*    flush_scale;    /* per flush: TextureMapScreenSizeMultiplierW, H */
+    uint32_t        ntex;
+    const uint32_t* tex_offset;     /* texel k of texture t: texels[tex_offset[t] + k] (RGBA8 premultiplied) */
+    const int32_t*  tex_w;
+    const int32_t*  tex_h;
+    const uint32_t* texels;
+} t3d_oracle_textures;
+
 /* Rasterises n triangles of one job in draw order (3 corners each: xyuv, rgba, depth as
  * t3d_frame_download writes them) into RGBA8 colour and depth images of the camera size
- * (pixel = r | g << 8 | b << 16 | a << 24); tri_pair = render pair of each triangle,
- * pair_transparent indexed by that id. See t3d_oracle_raster.cpp. */
+ * (pixel = r | g << 8 | b << 16 | a << 24); tri_pair = flush of each triangle,
+ * pair_transparent indexed by that id; tex may be NULL (no textures, no alpha clip).
+ * See t3d_oracle_raster.cpp. */
 int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, float dither, int32_t fogless, uint32_t n,
                       const float* xyuv, const float* rgba, const float* depth, const uint32_t* tri_pair,
-                      const uint8_t* pair_transparent, uint32_t* color_out, uint32_t* depth_out);
+                      const uint8_t* pair_transparent, const t3d_oracle_textures* tex, uint32_t* color_out,
+                      uint32_t* depth_out);
 
 /* Matrix4 helpers (float32) for pinning against matrix_test.go. */
 void t3d_oracle_mat_mult(const float* a, const float* b, float* out);

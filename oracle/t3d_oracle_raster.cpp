@@ -5,9 +5,12 @@
 // the depth pass of the depth shader (camera.go:350-383) into a cleared RGBA8
 // intermediate, tested against the depth texture of the pairs before and
 // composited into it unless the pair is transparent; the colour pass of
-// shaders/base3d.kage:67-145 with the default white image (tetra3d.go:12, :38),
-// fog curves and Bayer dithering (camera.go:1257-1262); with RenderDepth off,
-// ebiten's plain draw with straight-alpha vertex colours. ebiten v2.9.7
+// shaders/base3d.kage:67-145: the flush material's texture (nearest or bilinear,
+// wrapped with mod, UV or screen mapped; the default white image, tetra3d.go:12,
+// :38, without one) times the vertex colour, fog curves and Bayer dithering
+// (camera.go:1257-1262); for TransparencyModeAlphaClip the clip-alpha shader
+// (camera.go:390-480) in the depth pass; with RenderDepth off, ebiten's plain
+// draw of the texture times straight-alpha vertex colours. ebiten v2.9.7
 // conventions restated: premultiplied RGBA8 images cleared to 0, fragments at
 // pixel centres, top-left fill rule, attributes interpolated linearly in
 // screen space, unorm8 writes rounded to nearest after clamping to [0, 1].
@@ -85,12 +88,70 @@ uint32_t blend_over(uint32_t dst, float r, float g, float b, float a) {
     return pack(q8(r + u8f(dst, 0) * k), q8(g + u8f(dst, 1) * k), q8(b + u8f(dst, 2) * k), q8(a + u8f(dst, 3) * k));
 }
 
+// ---- textures (shaders/base3d.kage:32-58 and the clip-alpha shader, camera.go:419-478) ----
+float gmod(float x, float y) { return x - y * floorf(x / y); }  // GLSL mod
+float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }  // GLSL mix
+struct Texel {
+    float r, g, b, a;
+};
+// the texel of texture t containing the point (px, py), clamped to the image
+Texel texel_at(const t3d_oracle_textures* tx, uint32_t t, float px, float py) {
+    const int w = tx->tex_w[t], h = tx->tex_h[t];
+    const float fx = floorf(px), fy = floorf(py);  // NaN reads texel 0
+    const int ix = !(fx >= 0.0f) ? 0 : (fx >= (float)w ? w - 1 : (int)fx);
+    const int iy = !(fy >= 0.0f) ? 0 : (fy >= (float)h ? h - 1 : (int)fy);
+    const uint32_t p = tx->texels[tx->tex_offset[t] + (size_t)iy * w + ix];
+    return {u8f(p, 0), u8f(p, 1), u8f(p, 2), u8f(p, 3)};
+}
+// nearestFilter / bilinearFilter
+Texel sample(const t3d_oracle_textures* tx, uint32_t t, bool bilinear, float px, float py) {
+    if (!bilinear) return texel_at(tx, t, px, py);
+    const float w = (float)tx->tex_w[t], h = (float)tx->tex_h[t];
+    const float p0x = gmod(px - 0.5f, w), p0y = gmod(py - 0.5f, h);
+    const float p1x = gmod(px + 0.5f, w), p1y = gmod(py + 0.5f, h);
+    const Texel c0 = texel_at(tx, t, p0x, p0y), c1 = texel_at(tx, t, p1x, p0y);
+    const Texel c2 = texel_at(tx, t, p0x, p1y), c3 = texel_at(tx, t, p1x, p1y);
+    const float rx = fractf(p1x), ry = fractf(p1y);
+    return {mixf(mixf(c0.r, c1.r, rx), mixf(c2.r, c3.r, rx), ry), mixf(mixf(c0.g, c1.g, rx), mixf(c2.g, c3.g, rx), ry),
+            mixf(mixf(c0.b, c1.b, rx), mixf(c2.b, c3.b, rx), ry), mixf(mixf(c0.a, c1.a, rx), mixf(c2.a, c3.a, rx), ry)};
+}
+// the source position of a fragment: SrcX/SrcY, or screen mapped (TextureMapMode 1)
+void src_pos(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v, float& px, float& py) {
+    px = u;
+    py = v;
+    if (tx->flush_flags[fl] & 2u) {
+        px = (x * tx->flush_scale[2 * fl]) + u;
+        py = (y * tx->flush_scale[2 * fl + 1]) + v;
+    }
+}
+// the colour pass's texel: wrapped with mod (base3d.kage:86); white without a texture
+Texel colour_texel(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v) {
+    if (!tx || tx->flush_texture[fl] == 0u) return {1.0f, 1.0f, 1.0f, 1.0f};
+    const uint32_t t = tx->flush_texture[fl] - 1;
+    float px, py;
+    src_pos(tx, fl, x, y, u, v, px, py);
+    px = gmod(px, (float)tx->tex_w[t]);
+    py = gmod(py, (float)tx->tex_h[t]);
+    return sample(tx, t, tx->flush_flags[fl] & 1u, px, py);
+}
+// the clip-alpha shader's texture alpha: wrapped with fract of the UV (camera.go:458-465)
+float clip_alpha(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v) {
+    if (tx->flush_texture[fl] == 0u) return 1.0f;
+    const uint32_t t = tx->flush_texture[fl] - 1;
+    const float w = (float)tx->tex_w[t], h = (float)tx->tex_h[t];
+    float px, py;
+    src_pos(tx, fl, x, y, u, v, px, py);
+    px = fractf(px / w) * w;
+    py = fractf(py / h) * h;
+    return sample(tx, t, tx->flush_flags[fl] & 1u, px, py).a;
+}
+
 }  // namespace
 
 extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, float dither, int32_t fogless,
                                  uint32_t n, const float* xyuv, const float* rgba, const float* depth,
-                                 const uint32_t* tri_pair, const uint8_t* pair_transparent, uint32_t* color_out,
-                                 uint32_t* depth_out) {
+                                 const uint32_t* tri_pair, const uint8_t* pair_transparent,
+                                 const t3d_oracle_textures* tex, uint32_t* color_out, uint32_t* depth_out) {
     const int W = cam->width, H = cam->height;
     if (W <= 0 || H <= 0) return -1;
     const int fog_mode = cam->fog_on ? cam->fog_mode : -1;
@@ -108,14 +169,16 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
         for (int px = 0; px < W; px++) {
             const float x = (float)px + 0.5f, y = (float)py + 0.5f;
             const std::vector<uint32_t>& L = lists[(size_t)py * W + px];
-            auto frag = [&](uint32_t c, float* out5) {
+            auto frag = [&](uint32_t c, float* out7) {  // depth, r, g, b, a, SrcX, SrcY
                 const Tri t = tri_of(xyuv, c, W, H);
                 float wa, wb, wc;
                 covers(t, x, y, wa, wb, wc);
                 const float* k = rgba + 12 * (size_t)c;
                 const float* d = depth + 3 * (size_t)c;
-                out5[0] = ((wa * d[0] + wb * d[1]) + wc * d[2]) / t.area;
-                for (int q = 0; q < 4; q++) out5[1 + q] = ((wa * k[q] + wb * k[4 + q]) + wc * k[8 + q]) / t.area;
+                const float* p = xyuv + 12 * (size_t)c;
+                out7[0] = ((wa * d[0] + wb * d[1]) + wc * d[2]) / t.area;
+                for (int q = 0; q < 4; q++) out7[1 + q] = ((wa * k[q] + wb * k[4 + q]) + wc * k[8 + q]) / t.area;
+                for (int q = 0; q < 2; q++) out7[5 + q] = ((wa * p[2 + q] + wb * p[6 + q]) + wc * p[10 + q]) / t.area;
             };
             uint32_t rc = 0, rd = 0;
             size_t i = 0;
@@ -123,19 +186,30 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
                 const uint32_t s = tri_pair[L[i]];
                 size_t e = i + 1;
                 while (e < L.size() && tri_pair[L[e]] == s) e++;
-                float f[5];
+                float f[7];
                 if (cam->render_depth) {
                     uint32_t inter = 0;
+                    const bool clip = tex && (tex->flush_flags[s] & 4u);
                     for (size_t q = i; q < e; q++) {
                         frag(L[q], f);
-                        if ((rd >> 24) == 0u || decode_depth(rd) > f[0]) inter = encode_depth(f[0]);
+                        if (clip) {  // discard at texture alpha <= 0.8; (encodeDepth.rgb, alpha) over the intermediate
+                            const float ta = clip_alpha(tex, s, x, y, f[5], f[6]);
+                            if (ta <= 0.8f) continue;
+                            if ((rd >> 24) == 0u || decode_depth(rd) > f[0]) {
+                                const uint32_t enc = encode_depth(f[0]);
+                                inter = blend_over(inter, u8f(enc, 0), u8f(enc, 1), u8f(enc, 2), ta);
+                            }
+                        } else if ((rd >> 24) == 0u || decode_depth(rd) > f[0]) {
+                            inter = encode_depth(f[0]);
+                        }
                     }
                     if ((inter >> 24) != 0u) {
                         for (size_t q = i; q < e; q++) {
                             frag(L[q], f);
-                            float r = f[1], g = f[2], b = f[3];
-                            const float a = f[4];
-                            r *= a; g *= a; b *= a;
+                            const Texel tc = colour_texel(tex, s, x, y, f[5], f[6]);
+                            float r = tc.r * f[1], g = tc.g * f[2], b = tc.b * f[3];
+                            const float a = tc.a * f[4];
+                            r *= f[4]; g *= f[4]; b *= f[4];
                             if (!fogless && fog_mode >= 0 && fog_mode <= 2) {
                                 const float dd = decode_depth(inter);
                                 float v = dd;
@@ -159,12 +233,15 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
                             }
                             rc = blend_over(rc, r, g, b, a);
                         }
-                        if (!pair_transparent[s]) rd = inter;
+                        // DrawImage of the intermediate: source-over
+                        if (!pair_transparent[s])
+                            rd = blend_over(rd, u8f(inter, 0), u8f(inter, 1), u8f(inter, 2), u8f(inter, 3));
                     }
                 } else {
                     for (size_t q = i; q < e; q++) {
                         frag(L[q], f);
-                        rc = blend_over(rc, f[1] * f[4], f[2] * f[4], f[3] * f[4], f[4]);
+                        const Texel tc = colour_texel(tex, s, x, y, f[5], f[6]);
+                        rc = blend_over(rc, tc.r * (f[1] * f[4]), tc.g * (f[2] * f[4]), tc.b * (f[3] * f[4]), tc.a * f[4]);
                     }
                 }
                 i = e;

@@ -70,3 +70,61 @@ def test_raster_second_job(ctx):
         ctx.release(sb)
     ocol, odep = pyoracle.raster(pyoracle.render(b, cam_b), b, cam_b)
     assert np.array_equal(col, ocol) and np.array_equal(dep, odep)
+
+
+# ---- textures and alpha clip: base3d.kage's filters and mappings, the clip-alpha shader ----
+
+TEX_CASES = [
+    ("textured_persp", lambda: (scenes.textured_scene(21), scenes.feature_camera("persp")), {}),
+    ("textured_tilted", lambda: (scenes.textured_scene(22), scenes.feature_camera("tilted")), {}),
+    ("textured_fog_outcirc", lambda: (scenes.textured_scene(23), _fog_depth_camera("add")), {"fog_curve": 1}),
+    ("textured_ortho", lambda: (scenes.textured_scene(24), scenes.feature_camera("ortho")), {}),
+    ("textured_no_depth", lambda: (scenes.textured_scene(25), scenes.feature_camera("fog_add")), {}),
+    ("textured_batches", lambda: (scenes.texture_materials(scenes.batch_scene(12), 12), scenes.feature_camera("persp")),
+     {}),
+]
+
+
+@pytest.mark.parametrize("name,make,opts", TEX_CASES, ids=[c[0] for c in TEX_CASES])
+def test_textured_raster_matches_oracle(ctx, name, make, opts):
+    sd, cam = make()
+    tex = scenes.raster_textures(seed=len(name))
+    ctx.set_textures(tex)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        col, dep = ctx.raster(**opts)
+    finally:
+        ctx.release(sid)
+        ctx.set_textures([])
+    f = pyoracle.render(sd, cam)
+    ocol, odep = pyoracle.raster(f, sd, cam, textures=tex, **opts)
+    plain, _ = pyoracle.raster(f, sd, cam, **opts)
+    assert (ocol[..., 3] > 0).sum() > 100, "the scene covers pixels"
+    assert np.any(ocol != plain), "the textures change the image"
+    bad = np.argwhere(np.any(col != ocol, axis=-1))
+    assert bad.size == 0, f"{name}: colour differs at {len(bad)} pixels, first {bad[:3].tolist()}: " \
+                          f"gpu {col[tuple(bad[0])]} oracle {ocol[tuple(bad[0])]}"
+    assert np.array_equal(dep, odep), f"{name}: depth image differs"
+
+
+def test_texture_errors(ctx):
+    sd = scenes.textured_scene(21)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, scenes.feature_camera("persp"))
+        ctx.set_textures(scenes.raster_textures()[:1])   # materials name textures 2 and 3 too
+        with pytest.raises(abi.T3DError):
+            ctx.raster()
+        ctx.set_textures(scenes.raster_textures())
+        ctx.render(sid, scenes.feature_camera("corrected"))  # textures need the 1/w attribute there
+        with pytest.raises(abi.T3DError):
+            ctx.raster()
+        ctx.render(sid, scenes.feature_camera("persp"))
+        col, _ = ctx.raster()
+        assert col[..., 3].any()
+    finally:
+        ctx.release(sid)
+        ctx.set_textures([])
+    with pytest.raises(abi.T3DError):
+        ctx.set_textures([np.zeros((0, 4, 4), np.uint8)])

@@ -40,7 +40,9 @@ class Material(C.Structure):
                 ("lighting_mode", C.c_int32), ("lv_shading_mode", C.c_int32), ("shadeless", C.c_int32),
                 ("visible", C.c_int32), ("transparency_mode", C.c_int32), ("blend_source_over", C.c_int32),
                 ("render_order", C.c_int32), ("billboard", C.c_int32), ("billboard_lock", C.c_int32 * 3),
-                ("billboard_up", C.c_int32), ("billboard_depth", C.c_int32)]
+                ("billboard_up", C.c_int32), ("billboard_depth", C.c_int32), ("texture", C.c_uint32),
+                ("texture_filter", C.c_int32), ("texture_map_mode", C.c_int32), ("texture_map_scale", C.c_float * 2),
+                ("reserved_tex", C.c_int32)]
 
 
 class PartDesc(C.Structure):
@@ -141,6 +143,10 @@ class RasterOpts(C.Structure):
     _fields_ = [("fog_curve", C.c_int32), ("dither_size", C.c_float), ("fogless", C.c_int32), ("reserved", C.c_int32)]
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("rgba8", C.POINTER(C.c_uint8)), ("width", C.c_int32), ("height", C.c_int32)]
+
+
 # name -> (restype, argtypes) for every entry point of include/t3d.h
 _VP = C.c_void_p
 SIGNATURES = {
@@ -173,6 +179,7 @@ SIGNATURES = {
     "t3d_server_replay": (C.c_int, [_VP, C.POINTER(Request), C.c_uint32, C.POINTER(Completion)]),
     "t3d_render_part_noalloc": (C.c_int, [C.c_int, C.POINTER(NoallocArgs), _VP]),
     "t3d_frame_raster": (C.c_int, [_VP, C.c_uint32, C.POINTER(RasterOpts), _VP]),
+    "t3d_raster_set_textures": (C.c_int, [_VP, C.POINTER(TextureDesc), C.c_uint32]),
     "t3d_frame_images": (C.c_int, [_VP, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32)]),
 }

@@ -53,7 +53,15 @@ __constant__ float kBayer[16] = {1.0f / 17.0f,  9.0f / 17.0f, 3.0f / 17.0f,  11.
                                  4.0f / 17.0f,  12.0f / 17.0f, 2.0f / 17.0f,  10.0f / 17.0f,
                                  16.0f / 17.0f, 8.0f / 17.0f, 14.0f / 17.0f, 6.0f / 17.0f};
 
+// One texture of the context's table: texels[offset + y * w + x], RGBA8 premultiplied.
+struct RasterTex {
+    uint32_t offset;
+    int32_t w, h, pad;
+};
+
 struct RasterJob {
+    const RasterTex* texs;      // texture k + 1 of a flush (DevSeg.pad[1]) is texs[k]
+    const uint32_t* texels;
     const float4* xyuv;
     const float4* rgba;
     const float* depth;
@@ -325,7 +333,7 @@ __device__ __forceinline__ uint32_t blend_over(uint32_t dst, float r, float g, f
 }
 
 struct Frag {
-    float d, r, g, b, a;
+    float d, r, g, b, a, u, v;
 };
 __device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t c, float x, float y) {
     const uint32_t slot = J.tri_slot[c];
@@ -340,7 +348,60 @@ __device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t c, float x
     f.g = ((wa * ka.y + wb * kb.y) + wc * kc.y) / t.area;
     f.b = ((wa * ka.z + wb * kb.z) + wc * kc.z) / t.area;
     f.a = ((wa * ka.w + wb * kb.w) + wc * kc.w) / t.area;
+    const float4 ua = J.xyuv[3 * (size_t)slot], ub = J.xyuv[3 * (size_t)slot + 1], uc = J.xyuv[3 * (size_t)slot + 2];
+    f.u = ((wa * ua.z + wb * ub.z) + wc * uc.z) / t.area;  // SrcX, SrcY
+    f.v = ((wa * ua.w + wb * ub.w) + wc * uc.w) / t.area;
     return f;
+}
+
+// ---- textures (shaders/base3d.kage:32-58, camera.go:419-478) -------------------
+__device__ __forceinline__ float gmod(float x, float y) { return x - y * floorf(x / y); }  // GLSL mod
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }  // GLSL mix
+// the texel containing (px, py)
+__device__ __forceinline__ float4 texel_at(const RasterJob& J, const RasterTex& T, float px, float py) {
+    const float fx = floorf(px), fy = floorf(py);  // NaN reads texel 0
+    const int ix = !(fx >= 0.0f) ? 0 : (fx >= (float)T.w ? T.w - 1 : (int)fx);
+    const int iy = !(fy >= 0.0f) ? 0 : (fy >= (float)T.h ? T.h - 1 : (int)fy);
+    const uint32_t p = J.texels[T.offset + (size_t)iy * T.w + ix];
+    return make_float4(u8f(p, 0), u8f(p, 1), u8f(p, 2), u8f(p, 3));
+}
+// nearestFilter / bilinearFilter at texel coordinates (tx, ty)
+__device__ float4 tex_sample(const RasterJob& J, const RasterTex& T, bool bilinear, float tx, float ty) {
+    if (!bilinear) return texel_at(J, T, tx, ty);
+    const float w = (float)T.w, h = (float)T.h;
+    const float p0x = gmod(tx - 0.5f, w), p0y = gmod(ty - 0.5f, h);
+    const float p1x = gmod(tx + 0.5f, w), p1y = gmod(ty + 0.5f, h);
+    const float4 c0 = texel_at(J, T, p0x, p0y), c1 = texel_at(J, T, p1x, p0y);
+    const float4 c2 = texel_at(J, T, p0x, p1y), c3 = texel_at(J, T, p1x, p1y);
+    const float rx = fractf(p1x), ry = fractf(p1y);
+    float4 r;
+    r.x = mixf(mixf(c0.x, c1.x, rx), mixf(c2.x, c3.x, rx), ry);
+    r.y = mixf(mixf(c0.y, c1.y, rx), mixf(c2.y, c3.y, rx), ry);
+    r.z = mixf(mixf(c0.z, c1.z, rx), mixf(c2.z, c3.z, rx), ry);
+    r.w = mixf(mixf(c0.w, c1.w, rx), mixf(c2.w, c3.w, rx), ry);
+    return r;
+}
+// The flush's texel for the colour pass (base3d.kage:79-100): UV or screen mapped,
+// wrapped with mod; the default white image when the flush has no texture.
+__device__ float4 colour_texel(const RasterJob& J, const DevSeg& sg, float x, float y, const Frag& f) {
+    if (sg.pad[1] == 0u) return make_float4(1.f, 1.f, 1.f, 1.f);
+    const RasterTex T = J.texs[sg.pad[1] - 1];
+    float tx = f.u, ty = f.v;
+    if (sg.pad[2] & 2u) { tx = (x * sg.pad2[0]) + f.u; ty = (y * sg.pad2[1]) + f.v; }
+    tx = gmod(tx, (float)T.w);
+    ty = gmod(ty, (float)T.h);
+    return tex_sample(J, T, sg.pad[2] & 1u, tx, ty);
+}
+// The clip-alpha shader's texture alpha (camera.go:440-474): wrapped with fract.
+__device__ float clip_alpha(const RasterJob& J, const DevSeg& sg, float x, float y, const Frag& f) {
+    if (sg.pad[1] == 0u) return 1.0f;
+    const RasterTex T = J.texs[sg.pad[1] - 1];
+    const float w = (float)T.w, h = (float)T.h;
+    float tx = f.u, ty = f.v;
+    if (sg.pad[2] & 2u) { tx = (x * sg.pad2[0]) + f.u; ty = (y * sg.pad2[1]) + f.v; }
+    tx = fractf(tx / w) * w;
+    ty = fractf(ty / h) * h;
+    return tex_sample(J, T, sg.pad[2] & 1u, tx, ty).w;
 }
 
 __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ fvals,
@@ -354,21 +415,33 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
     while (i < f1) {
         // the fragments of one flush: a render pair, or all pairs of a dynamic batch
         // (pad[0] = flush number | transparent pass << 31)
-        const uint32_t fl = J.segs[J.tri_seg[fvals[i]]].pad[0];
+        const DevSeg& sg = J.segs[J.tri_seg[fvals[i]]];  // the flush's state (the same on all its pairs)
+        const uint32_t fl = sg.pad[0];
         uint32_t e = i + 1;
         while (e < f1 && J.segs[J.tri_seg[fvals[e]]].pad[0] == fl) e++;
         if (J.render_depth) {
             uint32_t inter = 0u;
+            const bool clip = sg.pad[2] & 4u;
             for (uint32_t q = i; q < e; q++) {  // depth pass (camera.go:1882-1931)
                 const Frag f = fragment(J, fvals[q], x, y);
-                if ((rd >> 24) == 0u || decode_depth(rd) > f.d) inter = encode_depth(f.d);
+                if (clip) {  // clip-alpha shader: (encodeDepth.rgb, texture alpha), blended source-over
+                    const float ta = clip_alpha(J, sg, x, y, f);
+                    if (ta <= 0.8f) continue;
+                    if ((rd >> 24) == 0u || decode_depth(rd) > f.d) {
+                        const uint32_t enc = encode_depth(f.d);
+                        inter = blend_over(inter, u8f(enc, 0), u8f(enc, 1), u8f(enc, 2), ta);
+                    }
+                } else if ((rd >> 24) == 0u || decode_depth(rd) > f.d) {
+                    inter = encode_depth(f.d);
+                }
             }
             if ((inter >> 24) != 0u) {
                 for (uint32_t q = i; q < e; q++) {  // colour pass (base3d.kage:67-145)
                     const Frag f = fragment(J, fvals[q], x, y);
-                    float r = f.r, g = f.g, b = f.b;
-                    const float a = f.a;
-                    r *= a; g *= a; b *= a;
+                    const float4 tc = colour_texel(J, sg, x, y, f);
+                    float r = tc.x * f.r, g = tc.y * f.g, b = tc.z * f.b;
+                    const float a = tc.w * f.a;
+                    r *= f.a; g *= f.a; b *= f.a;
                     if (!J.fogless && J.fog_mode >= 0 && J.fog_mode <= 2) {
                         const float dd = decode_depth(inter);
                         float v = dd;
@@ -391,12 +464,14 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
                     }
                     rc = blend_over(rc, r, g, b, a);
                 }
-                if (!(fl >> 31)) rd = inter;  // depth composite unless the flush is transparent
+                // depth composite (DrawImage, source-over) unless the flush is transparent
+                if (!(fl >> 31)) rd = blend_over(rd, u8f(inter, 0), u8f(inter, 1), u8f(inter, 2), u8f(inter, 3));
             }
         } else {
-            for (uint32_t q = i; q < e; q++) {  // plain draw, straight-alpha vertex colours
+            for (uint32_t q = i; q < e; q++) {  // plain draw: texel times the premultiplied vertex colour
                 const Frag f = fragment(J, fvals[q], x, y);
-                rc = blend_over(rc, f.r * f.a, f.g * f.a, f.b * f.a, f.a);
+                const float4 tc = colour_texel(J, sg, x, y, f);
+                rc = blend_over(rc, tc.x * (f.r * f.a), tc.y * (f.g * f.a), tc.z * (f.b * f.a), tc.w * f.a);
             }
         }
         i = e;
@@ -421,6 +496,8 @@ struct t3d_raster_state {
     RasterScratch S;
     int32_t W = 0, H = 0;
     bool valid = false;
+    std::vector<RasterTex> tex;  // the texture table (host copy of `texs`)
+    DevBuf texs, texels;
 };
 
 namespace {
@@ -483,8 +560,23 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     J.rgba = (const float4*)ctx->out_rgba.ptr;
     J.depth = (const float*)ctx->out_depth.ptr;
     J.segs = ctx->params.segs;
+    J.texs = (const RasterTex*)R.texs.ptr;
+    J.texels = (const uint32_t*)R.texels.ptr;
     uint64_t cap = 0;
-    for (uint32_t s = seg_lo; s < seg_hi; s++) cap += F.segs[s].tri_count;
+    for (uint32_t s = seg_lo; s < seg_hi; s++) {
+        const DevSeg& sg = F.segs[s];
+        cap += sg.tri_count;
+        const uint32_t t = sg.pad[1];
+        if (!t) continue;
+        if (t > R.tex.size()) {
+            set_err(ctx, "frame_raster: texture %u of a material is not in the table of %zu", t, R.tex.size());
+            return T3D_E_INVAL;
+        }
+        if (cam.persp_correct) {
+            set_err(ctx, "frame_raster: textures under perspective-corrected mapping are not supported");
+            return T3D_E_INVAL;
+        }
+    }
     const uint64_t npx = (uint64_t)J.W * J.H;
     int rc;
     if ((rc = S.cbase.ensure(ctx, 4ull * (nseg + 1))) || (rc = S.tri_slot.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
@@ -552,6 +644,45 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     return T3D_OK;
 }
 
+int t3d_raster_set_textures(t3d_ctx* ctx, const t3d_texture_desc* textures, uint32_t n) {
+    if (!ctx || (n && !textures)) return T3D_E_INVAL;
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < n; k++) {
+        const t3d_texture_desc& d = textures[k];
+        if (!d.rgba8 || d.width <= 0 || d.height <= 0 || d.width > 32768 || d.height > 32768) {
+            set_err(ctx, "raster_set_textures: texture %u has no texels or a bad size %d x %d", k, d.width, d.height);
+            return T3D_E_INVAL;
+        }
+        total += (uint64_t)d.width * d.height;
+    }
+    if (total >= (1ull << 32)) {
+        set_err(ctx, "raster_set_textures: %llu texels is more than 32-bit offsets address", (unsigned long long)total);
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));  // a raster in flight reads the table
+    if (!ctx->raster) ctx->raster = new t3d_raster_state();
+    t3d_raster_state& R = *ctx->raster;
+    std::vector<RasterTex> tex(n);
+    uint64_t off = 0;
+    for (uint32_t k = 0; k < n; k++) {
+        tex[k].offset = (uint32_t)off;
+        tex[k].w = textures[k].width;
+        tex[k].h = textures[k].height;
+        tex[k].pad = 0;
+        off += (uint64_t)textures[k].width * textures[k].height;
+    }
+    int rc;
+    if ((rc = R.texs.ensure(ctx, sizeof(RasterTex) * std::max(1u, n))) || (rc = R.texels.ensure(ctx, 4 * std::max<uint64_t>(1, total))))
+        return rc;
+    if (n) CKR(cudaMemcpy(R.texs.ptr, tex.data(), sizeof(RasterTex) * n, cudaMemcpyHostToDevice));
+    for (uint32_t k = 0; k < n; k++)
+        CKR(cudaMemcpy((uint32_t*)R.texels.ptr + tex[k].offset, textures[k].rgba8,
+                       4ull * textures[k].width * textures[k].height, cudaMemcpyHostToDevice));
+    R.tex = std::move(tex);
+    return T3D_OK;
+}
+
 int t3d_frame_images(t3d_ctx* ctx, uint8_t* color_rgba8, uint8_t* depth_rgba8, int32_t* width, int32_t* height) {
     if (!ctx) return T3D_E_INVAL;
     if (!ctx->raster || !ctx->raster->valid) {
@@ -575,7 +706,7 @@ void t3d_raster_release(t3d_ctx* ctx) {
     RasterScratch& S = ctx->raster->S;
     for (DevBuf* b : {&S.cbase, &S.tri_slot, &S.tri_seg, &S.fcount, &S.foff, &S.keys, &S.vals, &S.keys2, &S.vals2,
                       &S.counts, &S.offsets, &S.partial[0], &S.partial[1], &S.partial[2], &S.pstart, &S.pcount, &S.color,
-                      &S.depth})
+                      &S.depth, &ctx->raster->texs, &ctx->raster->texels})
         b->release();
     delete ctx->raster;
     ctx->raster = nullptr;

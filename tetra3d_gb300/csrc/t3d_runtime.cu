@@ -1026,13 +1026,15 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         // Draws: a plain pair is one flush; a batch pair draws its visible members far to
         // near from the camera (camera.go:2072-2093; ties keep model order), every part of
         // each, in one flush. Members outside the frustum are culled on the device.
-        struct Draw { uint32_t model, part, draw, transparent; };
+        // fmat: the material of the flush (a batch flushes with its owner's part)
+        struct Draw { uint32_t model, part, draw, transparent; const t3d_material* fmat; };
         std::vector<Draw> draws;
         for (size_t q = 0; q < solids.size(); q++) {
             const Pair& rp = solids[q];
             const uint32_t dt = q >= nsolid ? 1u : 0u;
+            const t3d_material* fm = &sc->meshes[sc->models[rp.model].d.mesh].parts[rp.part].d.mat;
             if (!rp.batch) {
-                draws.push_back({rp.model, rp.part, (uint32_t)q, dt});
+                draws.push_back({rp.model, rp.part, (uint32_t)q, dt, fm});
                 continue;
             }
             std::vector<std::pair<float, uint32_t>> mem;
@@ -1044,7 +1046,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                                                         const std::pair<float, uint32_t>& b) { return a.first > b.first; });
             for (const auto& mc : mem)
                 for (uint32_t p = 0; p < sc->meshes[sc->models[mc.second].d.mesh].parts.size(); p++)
-                    draws.push_back({mc.second, p, (uint32_t)q, dt});
+                    draws.push_back({mc.second, p, (uint32_t)q, dt, fm});
         }
         for (const Draw& rp : draws) {
             const SceneModel& m = sc->models[rp.model];
@@ -1130,6 +1132,13 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             }
 
             sg.pad[0] = rp.draw | (rp.transparent << 31);  // flush and its pass, for the rasteriser
+            if (rp.fmat->present) {  // the flush's texture state (camera.go:1840-1876)
+                sg.pad[1] = rp.fmat->texture;
+                sg.pad[2] = (rp.fmat->texture_filter ? 1u : 0u) | (rp.fmat->texture_map_mode == 1 ? 2u : 0u) |
+                            (rp.fmat->transparency_mode == T3D_TRANSPARENCY_ALPHA_CLIP ? 4u : 0u);
+                sg.pad2[0] = rp.fmat->texture_map_scale[0];
+                sg.pad2[1] = rp.fmat->texture_map_scale[1];
+            }
             F.segs.push_back(sg);
             t3d_segment_info si;
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;

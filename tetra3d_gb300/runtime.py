@@ -150,6 +150,16 @@ class Context:
                                               C.byref(h)), "frame_images")
         return col, dep
 
+    def set_textures(self, textures):
+        """Replaces the raster texture table: premultiplied RGBA8 arrays of shape (height, width, 4);
+        a material's `texture` k names entry k - 1."""
+        keep = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        arr = (abi.TextureDesc * max(1, len(keep)))()
+        for k, t in enumerate(keep):
+            assert t.ndim == 3 and t.shape[2] == 4, "textures are (height, width, 4) RGBA8"
+            arr[k] = abi.TextureDesc(t.ctypes.data_as(C.POINTER(C.c_uint8)), t.shape[1], t.shape[0])
+        self._check(self.lib.t3d_raster_set_textures(self.h, arr, len(keep)), "raster_set_textures")
+
     def graph_capture(self, sid, cam, animate=True):
         self._check(self.lib.t3d_graph_capture(self.h, sid, C.byref(cam), int(animate)), "graph_capture")
 

@@ -146,7 +146,8 @@ def look_rotation(forward_row):
 def default_material(**kw):
     m = dict(color=(1, 1, 1, 1), tex_w=0.0, tex_h=0.0, present=1, backface_culling=1,
              sort_mode=abi.SORT_BACK_TO_FRONT, lighting_mode=abi.LIGHTING_DEFAULT, lv_shading_mode=abi.LV_PER_VERTEX,
-             shadeless=0, visible=1, transparency_mode=abi.TRANSPARENCY_AUTO, blend_source_over=1, render_order=0)
+             shadeless=0, visible=1, transparency_mode=abi.TRANSPARENCY_AUTO, blend_source_over=1, render_order=0,
+             texture=0, texture_filter=0, texture_map_mode=0, texture_map_scale=(1.0, 1.0))
     m.update(kw)
     return m
 
@@ -367,6 +368,8 @@ class SceneData:
                         pa[k].mat.color[:] = [float(c) for c in v]
                     elif f == "billboard_lock":
                         pa[k].mat.billboard_lock[:] = [int(c) for c in v]
+                    elif f == "texture_map_scale":
+                        pa[k].mat.texture_map_scale[:] = [float(c) for c in v]
                     else:
                         setattr(pa[k].mat, f, v)
             keep.append(pa)
@@ -953,6 +956,49 @@ def subdivision_scene(seed=10, n=24, w=1280, h=720, max_subdivisions=3):
     sd.max_subdivisions = max_subdivisions
     sd.camera = feature_camera("persp", w, h)
     return sd
+
+
+TEXTURE_SIZES = [(64, 32), (16, 16), (128, 64)]
+
+
+def raster_textures(seed=0, holes=True):
+    """Premultiplied RGBA8 textures of TEXTURE_SIZES: random colours, and with `holes` a band of
+    texels at or below the alpha clip's 0.8 (alpha 0 or 204) and a band just above it (230)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for w, h in TEXTURE_SIZES:
+        a = np.full((h, w), 255, np.uint8)
+        if holes:
+            a[:, : w // 4] = 0
+            a[: h // 4, :] = 204
+            a[h // 2: h // 2 + h // 8, :] = 230
+        rgb = np.floor(rng.integers(0, 256, (h, w, 3)) * (a[..., None] / 255.0)).astype(np.uint8)
+        out.append(np.ascontiguousarray(np.concatenate([rgb, a[..., None]], -1)))
+    return out
+
+
+def texture_materials(sd, seed):
+    """Textures a scene's materials in place: each names one of raster_textures (or the white
+    default) with its size, a random filter, UV or screen mapping with a random screen multiplier,
+    and alpha clip on some. Returns the scene."""
+    rng = np.random.Generator(np.random.PCG64(seed + 1000))
+    for m in sd.meshes:
+        for p in m.parts:
+            mat = p["mat"]
+            t = int(rng.integers(len(TEXTURE_SIZES) + 1))
+            tw, th = TEXTURE_SIZES[t - 1] if t else (0, 0)
+            mat.update(texture=t, tex_w=float(tw), tex_h=float(th), texture_filter=int(rng.random() < 0.5),
+                       texture_map_mode=int(rng.random() < 0.2),
+                       texture_map_scale=[(1.0, 1.0), (0.5, 0.25), (2.0, 1.5)][int(rng.integers(3))])
+            if rng.random() < 0.3:
+                mat["transparency_mode"] = abi.TRANSPARENCY_ALPHA_CLIP
+    sd.name = f"{sd.name}_textured"
+    return sd
+
+
+def textured_scene(seed=21, n=48, w=1280, h=720):
+    """The feature scene with textured materials (texture_materials)."""
+    return texture_materials(feature_scene(seed, n=n, w=w, h=h), seed)
 
 
 def batch_scene(seed=11, n=72, w=1280, h=720):
