@@ -485,7 +485,10 @@ typedef struct t3d_raster_opts {
     int32_t fog_curve;     /* World.FogCurve: 0 linear, 1 out-circ, 2 in-circ */
     float   dither_size;   /* World.DitheredFogSize: > 0 enables Bayer-dithered fog */
     int32_t fogless;       /* Material.Fogless, for every pair */
-    int32_t reserved;
+    /* Tuning: triangles whose pixel box exceeds 32 pixels are shared out to the whole grid in
+     * 1024-pixel chunks, up to this many per call (0 = 262144, negative = none); beyond it
+     * each warp rasterises its own. The images do not depend on it. */
+    int32_t shared_large_tris;
 } t3d_raster_opts;
 /* Rasterises job `job` (0-based, in the order given to t3d_render_jobs) of the last frame. */
 int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, void* stream);

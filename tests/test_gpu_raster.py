@@ -128,3 +128,23 @@ def test_texture_errors(ctx):
         ctx.set_textures([])
     with pytest.raises(abi.T3DError):
         ctx.set_textures([np.zeros((0, 4, 4), np.uint8)])
+
+
+@pytest.mark.parametrize("shared", [-1, 7, 0])
+def test_large_triangles_shared_or_per_warp(ctx, shared):
+    """Triangles with a pixel box over 32 pixels are shared out to the grid in 1024-pixel chunks
+    up to the list's capacity, and rasterised by their own warp past it (-1: none shared, 7: the
+    first seven): the images are the oracle's either way. The scene has thousands of such
+    triangles, hundreds over one chunk."""
+    sd, cam = scenes.textured_scene(21), scenes.feature_camera("tilted")
+    tex = scenes.raster_textures(seed=3)
+    ctx.set_textures(tex)
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        col, dep = ctx.raster(shared_large_tris=shared)
+    finally:
+        ctx.release(sid)
+        ctx.set_textures([])
+    ocol, odep = pyoracle.raster(pyoracle.render(sd, cam), sd, cam, textures=tex)
+    assert np.array_equal(col, ocol) and np.array_equal(dep, odep)

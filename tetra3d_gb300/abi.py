@@ -140,7 +140,8 @@ class NoallocArgs(C.Structure):
 
 
 class RasterOpts(C.Structure):
-    _fields_ = [("fog_curve", C.c_int32), ("dither_size", C.c_float), ("fogless", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("fog_curve", C.c_int32), ("dither_size", C.c_float), ("fogless", C.c_int32),
+                ("shared_large_tris", C.c_int32)]
 
 
 class TextureDesc(C.Structure):

@@ -47,6 +47,11 @@ constexpr int kSortChunk = kSortThreads * kSortPerThread;
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
 constexpr int kScanChunk = kScanThreads * kScanPer;
+constexpr int kFragThreads = 256;
+constexpr uint32_t kUnitTris = 512;        // triangles per warp unit of the fragment passes
+constexpr uint32_t kBigChunk = 256;        // pixels per shared (one-warp) work item of a large triangle
+constexpr uint32_t kBigTriCap = 1u << 18;  // large triangles the shared list holds
+constexpr uint32_t kChunkCap = 1u << 22;   // and their chunks
 
 __constant__ float kBayer[16] = {1.0f / 17.0f,  9.0f / 17.0f, 3.0f / 17.0f,  11.0f / 17.0f,
                                  13.0f / 17.0f, 5.0f / 17.0f, 15.0f / 17.0f, 7.0f / 17.0f,
@@ -65,8 +70,9 @@ struct RasterJob {
     const float4* xyuv;
     const float4* rgba;
     const float* depth;
-    const uint32_t* tri_slot;   // compacted triangle -> output slot
-    const uint32_t* tri_seg;    // compacted triangle -> render pair
+    const uint32_t* cbase;      // exclusive prefix of the job's per-pair visible counts (nseg + 1)
+    uint32_t seg_lo, nseg;      // the job's render pairs: segs[seg_lo, seg_lo + nseg)
+    uint32_t big_cap;           // large triangles the shared list takes (<= kBigTriCap)
     const DevSeg* segs;
     int32_t W, H;
     int32_t render_depth;
@@ -149,49 +155,103 @@ __global__ void k_seg_bases(const uint32_t* __restrict__ seg_count, uint32_t seg
     if (threadIdx.x == 0) cbase[nseg] = carry;
 }
 
-__global__ void k_tri_lists(const DevSeg* __restrict__ segs, const uint32_t* __restrict__ seg_count, uint32_t seg_lo,
-                            uint32_t nseg, const uint32_t* __restrict__ cbase, uint32_t* tri_slot, uint32_t* tri_seg) {
-    // one warp per render pair
-    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= nseg) return;
-    const uint32_t s = seg_lo + w, n = seg_count[s], b = cbase[w], ob = segs[s].out_base;
-    for (uint32_t i = lane; i < n; i += 32) {
-        tri_slot[b + i] = ob + i;
-        tri_seg[b + i] = s;
+// The render pair holding visible triangle c of the job (draw order), searched forward
+// from pair `from` (cbase[from] <= c): gallop to a pair past c, then bisect. Pairs with no
+// visible triangle share their successor's prefix and are never returned.
+__device__ __forceinline__ uint32_t find_pair(const RasterJob& J, uint32_t c, uint32_t from) {
+    uint32_t lo = from, hi = from + 1, step = 1;
+    while (hi < J.nseg && __ldg(&J.cbase[hi]) <= c) {  // cbase[nseg] = n > c
+        lo = hi;
+        step <<= 1;
+        hi = lo + step;
     }
+    if (hi > J.nseg) hi = J.nseg;
+    while (hi - lo > 1) {  // cbase[lo] <= c < cbase[hi]
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&J.cbase[mid]) <= c) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
-__global__ void k_frag_count(RasterJob J, uint32_t n, uint32_t* fcount) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const TriScreen t = tri_screen(J, J.tri_slot[c]);
+__device__ __forceinline__ uint32_t tri_fragments(const TriScreen& t) {
     uint32_t k = 0;
-    if (t.ok)
-        for (int y = t.y0; y <= t.y1; y++)
-            for (int x = t.x0; x <= t.x1; x++) {
-                float wa, wb, wc;
-                if (covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc)) k++;
-            }
-    fcount[c] = k;
+    for (int y = t.y0; y <= t.y1; y++)
+        for (int x = t.x0; x <= t.x1; x++) {
+            float wa, wb, wc;
+            if (covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc)) k++;
+        }
+    return k;
 }
 
-__global__ void k_frag_write(RasterJob J, uint32_t n, const uint32_t* __restrict__ foff, uint32_t* keys, uint32_t* vals) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const TriScreen t = tri_screen(J, J.tri_slot[c]);
-    uint32_t o = foff[c];
-    if (t.ok)
-        for (int y = t.y0; y <= t.y1; y++)
-            for (int x = t.x0; x <= t.x1; x++) {
-                float wa, wb, wc;
-                if (covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc)) {
-                    keys[o] = (uint32_t)y * (uint32_t)J.W + (uint32_t)x;
-                    vals[o] = c;
-                    o++;
-                }
-            }
+// Bounding-box pixels of a triangle (0 when it covers no pixel centre's row or column).
+__device__ __forceinline__ uint32_t bbox_pixels(const TriScreen& t) {
+    if (!t.ok || t.x1 < t.x0 || t.y1 < t.y0) return 0u;
+    return (uint32_t)(t.x1 - t.x0 + 1) * (uint32_t)(t.y1 - t.y0 + 1);
+}
+// Triangles with larger pixel boxes are shared out to the whole grid in kBigChunk-pixel
+// chunks (or, when the shared list is full, tested by their warp together); smaller ones are
+// tested by their own thread.
+constexpr uint32_t kBigBox = 32;
+
+// A large triangle shared by the grid: its pixel box (row-major) is cut into kBigChunk-pixel
+// chunks [chunk0, chunk0 + ceil(box / kBigChunk)); `hit` is its entry in the hit list and
+// `cursor` the next free fragment of its range (set by the write pass).
+struct BigTri {
+    uint32_t slot, seg, hit, unit, chunk0, cursor, pad0, pad1;
+};
+
+__device__ __forceinline__ uint32_t warp_exclusive(uint32_t v, uint32_t lane, uint32_t& total) {
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += u;
+    }
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - v;
 }
 
+// A warp's count of the pixel centres triangle t covers (lanes stride the box row-major).
+__device__ __forceinline__ uint32_t warp_fragments(const TriScreen& t, uint32_t lane) {
+    const uint32_t bw = (uint32_t)(t.x1 - t.x0 + 1), area = bbox_pixels(t);
+    uint32_t k = 0;
+    for (uint32_t i = lane; i < area; i += 32) {
+        float wa, wb, wc;
+        if (covers(t, (float)(t.x0 + (int)(i % bw)) + 0.5f, (float)(t.y0 + (int)(i / bw)) + 0.5f, wa, wb, wc)) k++;
+    }
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    return k;
+}
+
+// A fragment's attributes at pixel centre (x, y): depth, colour and SrcX/SrcY interpolated
+// linearly in screen space with the edge weights of `covers`.
+struct Frag {
+    float d, r, g, b, a, u, v;
+};
+struct TriAttr {
+    float4 ka, kb, kc;  // colour of the corners
+    float da, db, dc;   // depth
+    float ua, ub, uc, va, vb, vc;  // SrcX, SrcY
+};
+__device__ __forceinline__ TriAttr tri_attr(const RasterJob& J, uint32_t slot) {
+    TriAttr A;
+    A.ka = J.rgba[3 * (size_t)slot]; A.kb = J.rgba[3 * (size_t)slot + 1]; A.kc = J.rgba[3 * (size_t)slot + 2];
+    A.da = J.depth[3 * (size_t)slot]; A.db = J.depth[3 * (size_t)slot + 1]; A.dc = J.depth[3 * (size_t)slot + 2];
+    const float4 pa = J.xyuv[3 * (size_t)slot], pb = J.xyuv[3 * (size_t)slot + 1], pc = J.xyuv[3 * (size_t)slot + 2];
+    A.ua = pa.z; A.ub = pb.z; A.uc = pc.z; A.va = pa.w; A.vb = pb.w; A.vc = pc.w;
+    return A;
+}
+__device__ __forceinline__ Frag interp(const TriAttr& A, float area, float wa, float wb, float wc) {
+    Frag f;
+    f.d = ((wa * A.da + wb * A.db) + wc * A.dc) / area;
+    f.r = ((wa * A.ka.x + wb * A.kb.x) + wc * A.kc.x) / area;
+    f.g = ((wa * A.ka.y + wb * A.kb.y) + wc * A.kc.y) / area;
+    f.b = ((wa * A.ka.z + wb * A.kb.z) + wc * A.kc.z) / area;
+    f.a = ((wa * A.ka.w + wb * A.kb.w) + wc * A.kc.w) / area;
+    f.u = ((wa * A.ua + wb * A.ub) + wc * A.uc) / area;
+    f.v = ((wa * A.va + wb * A.vb) + wc * A.vc) / area;
+    return f;
+}
 // ---- device-wide exclusive scan of uint32 ------------------------------------
 __device__ uint32_t block_exclusive(uint32_t v, uint32_t* sh, uint32_t& total) {
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -243,6 +303,212 @@ __global__ void k_scan_add(uint32_t* out, uint32_t n, const uint32_t* __restrict
 #pragma unroll
     for (int k = 0; k < kScanPer; k++)
         if (base + k < n) out[base + k] += add;
+}
+
+// Fragment pass 1, one warp per unit of kUnitTris triangles in draw order: count the pixel
+// centres each covers and keep, in draw order, the triangles that may cover any:
+// hits[u * kUnitTris + i] = (output slot, render pair, count, shared-list index + 1 or 0),
+// uhits[u] of them, ufrags[u] fragments. A triangle whose box exceeds kBigBox pixels goes to
+// the shared list (k_big_count adds its count); when the list is full its warp counts it.
+// ctr[0] / ctr[1]: large triangles / chunks handed out.
+__global__ void __launch_bounds__(kFragThreads) k_frag_count(RasterJob J, uint32_t nunits, uint4* hits, uint32_t* uhits,
+                                                             uint32_t* ufrags, BigTri* big, uint32_t* chunk_tri,
+                                                             unsigned long long* ctr) {
+    const uint32_t lane = threadIdx.x & 31, u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= nunits) return;  // the whole warp
+    const uint32_t n = __ldg(&J.cbase[J.nseg]), base = u * kUnitTris;
+    uint32_t nh = 0, frags = 0, pr = 0;
+    for (uint32_t j = 0; j < kUnitTris && base + j < n; j += 32) {
+        const uint32_t c = base + j + lane;
+        uint32_t k = 0, slot = 0, seg = 0, ref = 0;
+        bool hit = false, own_big = false;
+        if (c < n) {
+            pr = find_pair(J, c, j ? pr : 0u);
+            seg = J.seg_lo + pr;
+            slot = J.segs[seg].out_base + (c - __ldg(&J.cbase[pr]));
+            const TriScreen t = tri_screen(J, slot);
+            const uint32_t box = bbox_pixels(t);
+            if (box > kBigBox) {
+                hit = true;
+                own_big = true;
+                const unsigned long long b = atomicAdd(&ctr[0], 1ull);
+                if (b < J.big_cap) {
+                    const uint32_t nct = (box + kBigChunk - 1) / kBigChunk;
+                    const unsigned long long ch0 = atomicAdd(&ctr[1], (unsigned long long)nct);
+                    const bool fits = ch0 + nct <= kChunkCap;
+                    // chunks below the cap always name their triangle, or none when it did not fit
+                    for (unsigned long long q = ch0; q < ch0 + nct && q < kChunkCap; q++)
+                        chunk_tri[q] = fits ? (uint32_t)b : 0xFFFFFFFFu;
+                    if (fits) {
+                        own_big = false;
+                        ref = (uint32_t)b + 1;
+                        BigTri& B = big[b];
+                        B.slot = slot;
+                        B.seg = seg;
+                        B.unit = u;
+                        B.chunk0 = (uint32_t)ch0;
+                    }
+                }
+            } else if (box) {
+                k = tri_fragments(t);
+                hit = k != 0;
+            }
+        }
+        // large triangles the shared list could not take: the warp counts their pixels
+        for (uint32_t m = __ballot_sync(0xffffffffu, own_big); m; m &= m - 1) {
+            const int l = __ffs(m) - 1;
+            const uint32_t cnt = warp_fragments(tri_screen(J, __shfl_sync(0xffffffffu, slot, l)), lane);
+            if (lane == (uint32_t)l) k = cnt;
+        }
+        frags += k;
+        const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const uint32_t pos = base + nh + __popc(hm & ((1u << lane) - 1u));
+            hits[pos] = make_uint4(slot, seg, k, ref);
+            if (ref) big[ref - 1].hit = pos;
+        }
+        nh += __popc(hm);
+    }
+    for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, o);
+    if (lane == 0) {
+        uhits[u] = nh;
+        ufrags[u] = frags;
+    }
+}
+
+__device__ __forceinline__ uint32_t shared_chunks(const unsigned long long* ctr) {
+    const unsigned long long c = ctr[1];
+    return c < kChunkCap ? (uint32_t)c : kChunkCap;
+}
+
+// Counts of the shared large triangles: the grid's warps take kBigChunk-pixel chunks in turn
+// and add each chunk's count to its triangle's hit and unit.
+__global__ void __launch_bounds__(kFragThreads) k_big_count(RasterJob J, const BigTri* __restrict__ big,
+                                                           const uint32_t* __restrict__ chunk_tri,
+                                                           const unsigned long long* __restrict__ ctr, uint4* hits,
+                                                           uint32_t* ufrags) {
+    const uint32_t lane = threadIdx.x & 31, nch = shared_chunks(ctr);
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t ch = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nch; ch += nw) {
+        const uint32_t b = chunk_tri[ch];
+        if (b == 0xFFFFFFFFu) continue;  // the same for the whole warp
+        const BigTri B = big[b];
+        const TriScreen t = tri_screen(J, B.slot);
+        const uint32_t bw = (uint32_t)(t.x1 - t.x0 + 1), area = bbox_pixels(t);
+        const uint32_t p0 = (ch - B.chunk0) * kBigChunk, p1 = min(p0 + kBigChunk, area);
+        uint32_t k = 0;
+        for (uint32_t i = p0 + lane; i < p1; i += 32) {
+            float wa, wb, wc;
+            if (covers(t, (float)(t.x0 + (int)(i % bw)) + 0.5f, (float)(t.y0 + (int)(i / bw)) + 0.5f, wa, wb, wc)) k++;
+        }
+        for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+        if (lane == 0 && k) {
+            atomicAdd(&hits[B.hit].z, k);
+            atomicAdd(&ufrags[B.unit], k);
+        }
+    }
+}
+
+// Fragment pass 2, one warp per unit: the unit's hits write their fragments (key = pixel,
+// value = the hit's index, which names its triangle) from ufoff[u] on, in draw order, so the
+// stable sort by pixel keeps draw order per pixel. A shared large triangle only sets its
+// cursor; k_big_write fills its range.
+__global__ void __launch_bounds__(kFragThreads) k_frag_write(RasterJob J, uint32_t nunits, const uint4* __restrict__ hits,
+                                                             const uint32_t* __restrict__ uhits,
+                                                             const uint32_t* __restrict__ ufoff, BigTri* big,
+                                                             uint32_t* keys, uint32_t* vals) {
+    const uint32_t lane = threadIdx.x & 31, u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= nunits) return;  // the whole warp
+    const uint32_t base = u * kUnitTris, nh = uhits[u];
+    uint32_t run = ufoff[u];
+    for (uint32_t j = 0; j < nh; j += 32) {
+        const uint32_t i = j + lane;
+        const uint4 h = i < nh ? hits[base + i] : make_uint4(0u, 0u, 0u, 0u);
+        uint32_t total;
+        const uint32_t o = run + warp_exclusive(h.z, lane, total);
+        run += total;
+        bool own_big = false;
+        if (h.z) {
+            if (h.w) {
+                big[h.w - 1].cursor = o;
+            } else {
+                const TriScreen t = tri_screen(J, h.x);
+                if (bbox_pixels(t) > kBigBox) {
+                    own_big = true;
+                } else {
+                    uint32_t q = o;
+                    for (int y = t.y0; y <= t.y1; y++)
+                        for (int x = t.x0; x <= t.x1; x++) {
+                            float wa, wb, wc;
+                            if (covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc)) {
+                                keys[q] = (uint32_t)y * (uint32_t)J.W + (uint32_t)x;
+                                vals[q] = base + i;
+                                q++;
+                            }
+                        }
+                }
+            }
+        }
+        // large triangles outside the shared list: the warp writes them, pixels row-major
+        for (uint32_t m = __ballot_sync(0xffffffffu, own_big); m; m &= m - 1) {
+            const int l = __ffs(m) - 1;
+            const uint32_t slot = __shfl_sync(0xffffffffu, h.x, l), hidx = base + j + (uint32_t)l;
+            uint32_t ob = __shfl_sync(0xffffffffu, o, l);
+            const TriScreen t = tri_screen(J, slot);
+            const uint32_t bw = (uint32_t)(t.x1 - t.x0 + 1), area = bbox_pixels(t);
+            for (uint32_t b0 = 0; b0 < area; b0 += 32) {
+                const uint32_t pi = b0 + lane;
+                const int x = t.x0 + (int)(pi % bw), y = t.y0 + (int)(pi / bw);
+                float wa, wb, wc;
+                const bool in = pi < area && covers(t, (float)x + 0.5f, (float)y + 0.5f, wa, wb, wc);
+                const uint32_t pm = __ballot_sync(0xffffffffu, in);
+                if (in) {
+                    const uint32_t q = ob + __popc(pm & ((1u << lane) - 1u));
+                    keys[q] = (uint32_t)y * (uint32_t)J.W + (uint32_t)x;
+                    vals[q] = hidx;
+                }
+                ob += __popc(pm);
+            }
+        }
+    }
+}
+
+// Fragments of the shared large triangles: the grid's warps take chunks in turn; a chunk
+// claims its part of the triangle's range with one atomic on the cursor. The order inside a
+// triangle's range does not matter: a triangle has at most one fragment per pixel.
+__global__ void __launch_bounds__(kFragThreads) k_big_write(RasterJob J, BigTri* big, const uint32_t* __restrict__ chunk_tri,
+                                                           const unsigned long long* __restrict__ ctr, uint32_t* keys,
+                                                           uint32_t* vals) {
+    const uint32_t lane = threadIdx.x & 31, nch = shared_chunks(ctr);
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t ch = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nch; ch += nw) {
+        const uint32_t b = chunk_tri[ch];
+        if (b == 0xFFFFFFFFu) continue;  // the same for the whole warp
+        const uint32_t slot = big[b].slot, hidx = big[b].hit, chunk0 = big[b].chunk0;
+        const TriScreen t = tri_screen(J, slot);
+        const uint32_t bw = (uint32_t)(t.x1 - t.x0 + 1), area = bbox_pixels(t);
+        const uint32_t p0 = (ch - chunk0) * kBigChunk, p1 = min(p0 + kBigChunk, area);
+        uint32_t mask = 0, cnt = 0;  // lane's pixels p0 + lane + 32 q
+        for (uint32_t q = 0, i = p0 + lane; q < kBigChunk / 32; q++, i += 32) {
+            float wa, wb, wc;
+            if (i < p1 && covers(t, (float)(t.x0 + (int)(i % bw)) + 0.5f, (float)(t.y0 + (int)(i / bw)) + 0.5f, wa, wb, wc)) {
+                mask |= 1u << q;
+                cnt++;
+            }
+        }
+        uint32_t total;
+        const uint32_t off = warp_exclusive(cnt, lane, total);
+        uint32_t base = 0;
+        if (lane == 0 && total) base = atomicAdd(&big[b].cursor, total);
+        uint32_t o = __shfl_sync(0xffffffffu, base, 0) + off;
+        for (uint32_t q = 0, i = p0 + lane; mask; q++, i += 32) {
+            if (!((mask >> q) & 1u)) continue;
+            mask &= ~(1u << q);
+            keys[o] = (uint32_t)(t.y0 + (int)(i / bw)) * (uint32_t)J.W + (uint32_t)(t.x0 + (int)(i % bw));
+            vals[o] = hidx;
+            o++;
+        }
+    }
 }
 
 // ---- stable LSD radix sort of (key, value) pairs by kSortBits-bit digits --------
@@ -332,28 +598,6 @@ __device__ __forceinline__ uint32_t blend_over(uint32_t dst, float r, float g, f
     return pack(q8(r + u8f(dst, 0) * k), q8(g + u8f(dst, 1) * k), q8(b + u8f(dst, 2) * k), q8(a + u8f(dst, 3) * k));
 }
 
-struct Frag {
-    float d, r, g, b, a, u, v;
-};
-__device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t c, float x, float y) {
-    const uint32_t slot = J.tri_slot[c];
-    const TriScreen t = tri_screen(J, slot);
-    float wa, wb, wc;
-    covers(t, x, y, wa, wb, wc);
-    const float4 ka = J.rgba[3 * (size_t)slot], kb = J.rgba[3 * (size_t)slot + 1], kc = J.rgba[3 * (size_t)slot + 2];
-    const float da = J.depth[3 * (size_t)slot], db = J.depth[3 * (size_t)slot + 1], dc = J.depth[3 * (size_t)slot + 2];
-    Frag f;
-    f.d = ((wa * da + wb * db) + wc * dc) / t.area;
-    f.r = ((wa * ka.x + wb * kb.x) + wc * kc.x) / t.area;
-    f.g = ((wa * ka.y + wb * kb.y) + wc * kc.y) / t.area;
-    f.b = ((wa * ka.z + wb * kb.z) + wc * kc.z) / t.area;
-    f.a = ((wa * ka.w + wb * kb.w) + wc * kc.w) / t.area;
-    const float4 ua = J.xyuv[3 * (size_t)slot], ub = J.xyuv[3 * (size_t)slot + 1], uc = J.xyuv[3 * (size_t)slot + 2];
-    f.u = ((wa * ua.z + wb * ub.z) + wc * uc.z) / t.area;  // SrcX, SrcY
-    f.v = ((wa * ua.w + wb * ub.w) + wc * uc.w) / t.area;
-    return f;
-}
-
 // ---- textures (shaders/base3d.kage:32-58, camera.go:419-478) -------------------
 __device__ __forceinline__ float gmod(float x, float y) { return x - y * floorf(x / y); }  // GLSL mod
 __device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }  // GLSL mix
@@ -404,8 +648,18 @@ __device__ float clip_alpha(const RasterJob& J, const DevSeg& sg, float x, float
     return tex_sample(J, T, sg.pad[2] & 1u, tx, ty).w;
 }
 
+// Fragment of the triangle in output slot `slot` at pixel centre (x, y).
+__device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t slot, float x, float y) {
+    const TriScreen t = tri_screen(J, slot);
+    float wa, wb, wc;
+    covers(t, x, y, wa, wb, wc);
+    return interp(tri_attr(J, slot), t.area, wa, wb, wc);
+}
+
+// One thread per pixel replays the pixel's fragments (sorted by pixel, draw order kept);
+// fvals[q] is the hit of fragment q's triangle: hits[fvals[q]] = (output slot, render pair, ...).
 __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ fvals,
-                         uint32_t* color, uint32_t* depth) {
+                         const uint4* __restrict__ hits, uint32_t* color, uint32_t* depth) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (uint32_t)(J.W * J.H)) return;
     const float x = (float)(p % (uint32_t)J.W) + 0.5f, y = (float)(p / (uint32_t)J.W) + 0.5f;
@@ -415,15 +669,15 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
     while (i < f1) {
         // the fragments of one flush: a render pair, or all pairs of a dynamic batch
         // (pad[0] = flush number | transparent pass << 31)
-        const DevSeg& sg = J.segs[J.tri_seg[fvals[i]]];  // the flush's state (the same on all its pairs)
+        const DevSeg& sg = J.segs[hits[fvals[i]].y];  // the flush's state (the same on all its pairs)
         const uint32_t fl = sg.pad[0];
         uint32_t e = i + 1;
-        while (e < f1 && J.segs[J.tri_seg[fvals[e]]].pad[0] == fl) e++;
+        while (e < f1 && J.segs[hits[fvals[e]].y].pad[0] == fl) e++;
         if (J.render_depth) {
             uint32_t inter = 0u;
             const bool clip = sg.pad[2] & 4u;
             for (uint32_t q = i; q < e; q++) {  // depth pass (camera.go:1882-1931)
-                const Frag f = fragment(J, fvals[q], x, y);
+                const Frag f = fragment(J, hits[fvals[q]].x, x, y);
                 if (clip) {  // clip-alpha shader: (encodeDepth.rgb, texture alpha), blended source-over
                     const float ta = clip_alpha(J, sg, x, y, f);
                     if (ta <= 0.8f) continue;
@@ -437,7 +691,7 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
             }
             if ((inter >> 24) != 0u) {
                 for (uint32_t q = i; q < e; q++) {  // colour pass (base3d.kage:67-145)
-                    const Frag f = fragment(J, fvals[q], x, y);
+                    const Frag f = fragment(J, hits[fvals[q]].x, x, y);
                     const float4 tc = colour_texel(J, sg, x, y, f);
                     float r = tc.x * f.r, g = tc.y * f.g, b = tc.z * f.b;
                     const float a = tc.w * f.a;
@@ -469,7 +723,7 @@ __global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const
             }
         } else {
             for (uint32_t q = i; q < e; q++) {  // plain draw: texel times the premultiplied vertex colour
-                const Frag f = fragment(J, fvals[q], x, y);
+                const Frag f = fragment(J, hits[fvals[q]].x, x, y);
                 const float4 tc = colour_texel(J, sg, x, y, f);
                 rc = blend_over(rc, tc.x * (f.r * f.a), tc.y * (f.g * f.a), tc.z * (f.b * f.a), tc.w * f.a);
             }
@@ -486,7 +740,7 @@ __global__ void k_pixel_count(const uint32_t* __restrict__ keys, uint32_t n, uin
 }
 
 struct RasterScratch {
-    DevBuf cbase, tri_slot, tri_seg, fcount, foff, keys, vals, keys2, vals2, counts, offsets, partial[3], pstart, pcount,
+    DevBuf cbase, hits, uhits, ufrags, ufoff, big, chunk_tri, ctr, keys, vals, keys2, vals2, counts, offsets, partial[3], pstart, pcount,
         color, depth;
 };
 
@@ -556,6 +810,10 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     J.fog_curve = opts ? opts->fog_curve : 0;
     J.fogless = opts ? opts->fogless : 0;
     J.dither = opts ? opts->dither_size : 0.0f;
+    {
+        const int32_t sl = opts ? opts->shared_large_tris : 0;
+        J.big_cap = sl == 0 ? kBigTriCap : (sl < 0 ? 0u : std::min<uint32_t>((uint32_t)sl, kBigTriCap));
+    }
     J.xyuv = (const float4*)ctx->out_xyuv.ptr;
     J.rgba = (const float4*)ctx->out_rgba.ptr;
     J.depth = (const float*)ctx->out_depth.ptr;
@@ -579,34 +837,37 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     }
     const uint64_t npx = (uint64_t)J.W * J.H;
     int rc;
-    if ((rc = S.cbase.ensure(ctx, 4ull * (nseg + 1))) || (rc = S.tri_slot.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
-        (rc = S.tri_seg.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
-        (rc = S.fcount.ensure(ctx, 4 * std::max<uint64_t>(1, cap))) ||
-        (rc = S.foff.ensure(ctx, 4 * std::max<uint64_t>(1, cap) + 4)) || (rc = S.pstart.ensure(ctx, 4 * (npx + 1))) ||
-        (rc = S.pcount.ensure(ctx, 4 * npx)) || (rc = S.color.ensure(ctx, 4 * npx)) || (rc = S.depth.ensure(ctx, 4 * npx)))
+    // the fragment passes run one warp per kUnitTris triangles of the job's capacity; the
+    // visible count n = cbase[nseg] stays on the device (units past it only record zeros)
+    const uint32_t nunits = (uint32_t)std::max<uint64_t>(1, (cap + kUnitTris - 1) / kUnitTris);
+    const uint32_t fblocks = (nunits + kFragThreads / 32 - 1) / (kFragThreads / 32);
+    const uint32_t bigblocks = (uint32_t)std::max(1, ctx->num_sms) * 4;
+    if ((rc = S.cbase.ensure(ctx, 4ull * (nseg + 1))) || (rc = S.hits.ensure(ctx, 16ull * kUnitTris * nunits)) ||
+        (rc = S.uhits.ensure(ctx, 4ull * nunits)) || (rc = S.ufrags.ensure(ctx, 4ull * nunits)) ||
+        (rc = S.ufoff.ensure(ctx, 4ull * nunits)) || (rc = S.big.ensure(ctx, sizeof(BigTri) * (size_t)kBigTriCap)) ||
+        (rc = S.chunk_tri.ensure(ctx, 4ull * kChunkCap)) || (rc = S.ctr.ensure(ctx, 16)) ||
+        (rc = S.pstart.ensure(ctx, 4 * (npx + 1))) || (rc = S.pcount.ensure(ctx, 4 * npx)) ||
+        (rc = S.color.ensure(ctx, 4 * npx)) || (rc = S.depth.ensure(ctx, 4 * npx)))
         return rc;
-    J.tri_slot = (const uint32_t*)S.tri_slot.ptr;
-    J.tri_seg = (const uint32_t*)S.tri_seg.ptr;
-    // 1. visible triangles of the job, compacted in draw order
+    J.cbase = (const uint32_t*)S.cbase.ptr;
+    J.seg_lo = seg_lo;
+    J.nseg = nseg;
+    BigTri* big = (BigTri*)S.big.ptr;
+    uint32_t* chunk_tri = (uint32_t*)S.chunk_tri.ptr;
+    unsigned long long* ctr = (unsigned long long*)S.ctr.ptr;
+    // 1. the job's visible triangles in draw order: per-pair prefix of the visible counts
     k_seg_bases<<<1, 1024, 0, st>>>((const uint32_t*)ctx->seg_count.ptr, seg_lo, nseg, (uint32_t*)S.cbase.ptr);
-    if (nseg)
-        k_tri_lists<<<(nseg * 32 + 255) / 256, 256, 0, st>>>(ctx->params.segs, (const uint32_t*)ctx->seg_count.ptr, seg_lo,
-                                                             nseg, (const uint32_t*)S.cbase.ptr, (uint32_t*)S.tri_slot.ptr,
-                                                             (uint32_t*)S.tri_seg.ptr);
-    uint32_t n = 0;
-    CKR(cudaMemcpyAsync(&n, (const uint32_t*)S.cbase.ptr + nseg, 4, cudaMemcpyDeviceToHost, st));
+    // 2. fragments in draw order: count and keep the covering triangles, then write
+    CKR(cudaMemsetAsync(ctr, 0, 16, st));
+    k_frag_count<<<fblocks, kFragThreads, 0, st>>>(J, nunits, (uint4*)S.hits.ptr, (uint32_t*)S.uhits.ptr,
+                                                   (uint32_t*)S.ufrags.ptr, big, chunk_tri, ctr);
+    k_big_count<<<bigblocks, kFragThreads, 0, st>>>(J, big, chunk_tri, ctr, (uint4*)S.hits.ptr, (uint32_t*)S.ufrags.ptr);
+    if ((rc = scan_u32(ctx, S, (const uint32_t*)S.ufrags.ptr, (uint32_t*)S.ufoff.ptr, nunits, st))) return rc;
+    uint32_t last[2];
+    CKR(cudaMemcpyAsync(&last[0], (const uint32_t*)S.ufoff.ptr + nunits - 1, 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(&last[1], (const uint32_t*)S.ufrags.ptr + nunits - 1, 4, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
-    // 2. fragments in draw order
-    uint32_t nf = 0;
-    if (n) {
-        k_frag_count<<<(n + 255) / 256, 256, 0, st>>>(J, n, (uint32_t*)S.fcount.ptr);
-        if ((rc = scan_u32(ctx, S, (const uint32_t*)S.fcount.ptr, (uint32_t*)S.foff.ptr, n, st))) return rc;
-        uint32_t last[2];
-        CKR(cudaMemcpyAsync(&last[0], (const uint32_t*)S.foff.ptr + n - 1, 4, cudaMemcpyDeviceToHost, st));
-        CKR(cudaMemcpyAsync(&last[1], (const uint32_t*)S.fcount.ptr + n - 1, 4, cudaMemcpyDeviceToHost, st));
-        CKR(cudaStreamSynchronize(st));
-        nf = last[0] + last[1];
-    }
+    const uint32_t nf = last[0] + last[1];
     const uint32_t nsb = std::max(1u, (nf + kSortChunk - 1) / kSortChunk);
     if ((rc = S.keys.ensure(ctx, 4ull * std::max(1u, nf))) || (rc = S.vals.ensure(ctx, 4ull * std::max(1u, nf))) ||
         (rc = S.keys2.ensure(ctx, 4ull * std::max(1u, nf))) || (rc = S.vals2.ensure(ctx, 4ull * std::max(1u, nf))) ||
@@ -615,7 +876,9 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     uint32_t *kin = (uint32_t*)S.keys.ptr, *vin = (uint32_t*)S.vals.ptr;
     uint32_t *kout = (uint32_t*)S.keys2.ptr, *vout = (uint32_t*)S.vals2.ptr;
     if (nf) {
-        k_frag_write<<<(n + 255) / 256, 256, 0, st>>>(J, n, (const uint32_t*)S.foff.ptr, kin, vin);
+        k_frag_write<<<fblocks, kFragThreads, 0, st>>>(J, nunits, (const uint4*)S.hits.ptr, (const uint32_t*)S.uhits.ptr,
+                                                       (const uint32_t*)S.ufoff.ptr, big, kin, vin);
+        k_big_write<<<bigblocks, kFragThreads, 0, st>>>(J, big, chunk_tri, ctr, kin, vin);
         // 3. stable sort by pixel
         int bits = 1;
         while ((1ull << bits) < npx) bits++;
@@ -634,7 +897,8 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     if ((rc = scan_u32(ctx, S, (const uint32_t*)S.pcount.ptr, (uint32_t*)S.pstart.ptr, (uint32_t)npx, st))) return rc;
     CKR(cudaMemcpyAsync((uint32_t*)S.pstart.ptr + npx, &nf, 4, cudaMemcpyHostToDevice, st));
     // 5. replay per pixel
-    k_pixels<<<(uint32_t)((npx + 255) / 256), 256, 0, st>>>(J, (const uint32_t*)S.pstart.ptr, vin, (uint32_t*)S.color.ptr,
+    k_pixels<<<(uint32_t)((npx + 255) / 256), 256, 0, st>>>(J, (const uint32_t*)S.pstart.ptr, vin,
+                                                           (const uint4*)S.hits.ptr, (uint32_t*)S.color.ptr,
                                                            (uint32_t*)S.depth.ptr);
     CKR(cudaGetLastError());
     CKR(cudaStreamSynchronize(st));
@@ -704,7 +968,7 @@ int t3d_frame_images(t3d_ctx* ctx, uint8_t* color_rgba8, uint8_t* depth_rgba8, i
 void t3d_raster_release(t3d_ctx* ctx) {
     if (!ctx->raster) return;
     RasterScratch& S = ctx->raster->S;
-    for (DevBuf* b : {&S.cbase, &S.tri_slot, &S.tri_seg, &S.fcount, &S.foff, &S.keys, &S.vals, &S.keys2, &S.vals2,
+    for (DevBuf* b : {&S.cbase, &S.hits, &S.uhits, &S.ufrags, &S.ufoff, &S.big, &S.chunk_tri, &S.ctr, &S.keys, &S.vals, &S.keys2, &S.vals2,
                       &S.counts, &S.offsets, &S.partial[0], &S.partial[1], &S.partial[2], &S.pstart, &S.pcount, &S.color,
                       &S.depth, &ctx->raster->texs, &ctx->raster->texels})
         b->release();

@@ -133,11 +133,12 @@ class Context:
         self._check(self.lib.t3d_frame_view_get(self.h, C.byref(v)), "frame_view_get")
         return v
 
-    def raster(self, job=0, fog_curve=0, dither_size=0.0, fogless=0, stream=None, download=True):
+    def raster(self, job=0, fog_curve=0, dither_size=0.0, fogless=0, stream=None, download=True, shared_large_tris=0):
         """Rasterises one job of the last frame (the colour and depth passes of flush) and returns
         (colour, depth) RGBA8 images of shape (height, width, 4), premultiplied (None, None without
-        download: the images stay on the device)."""
-        o = abi.RasterOpts(fog_curve, float(dither_size), fogless, 0)
+        download: the images stay on the device). `shared_large_tris` is the tuning knob of
+        t3d_raster_opts (0 default, negative none)."""
+        o = abi.RasterOpts(fog_curve, float(dither_size), fogless, int(shared_large_tris))
         self._check(self.lib.t3d_frame_raster(self.h, job, C.byref(o), stream), "frame_raster")
         if not download:
             return None, None
