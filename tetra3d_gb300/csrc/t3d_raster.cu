@@ -89,9 +89,8 @@ struct TriScreen {
     bool ok;
 };
 
-__device__ __forceinline__ TriScreen tri_screen(const RasterJob& J, uint32_t slot) {
+__device__ __forceinline__ TriScreen screen_of(const RasterJob& J, const float4 a, const float4 b, const float4 c) {
     TriScreen t;
-    const float4 a = J.xyuv[3 * (size_t)slot], b = J.xyuv[3 * (size_t)slot + 1], c = J.xyuv[3 * (size_t)slot + 2];
     t.ax = a.x; t.ay = a.y; t.bx = b.x; t.by = b.y; t.cx = c.x; t.cy = c.y;
     t.area = (t.bx - t.ax) * (t.cy - t.ay) - (t.by - t.ay) * (t.cx - t.ax);
     t.ok = t.area != 0.0f && isfinite(t.area);
@@ -104,6 +103,9 @@ __device__ __forceinline__ TriScreen tri_screen(const RasterJob& J, uint32_t slo
     t.y1 = (int)fmaxf(fminf((float)J.H - 1.0f, floorf(mxy - 0.5f)), -1.0f);
     if (!(mnx == mnx) || !(mny == mny) || !(mxx == mxx) || !(mxy == mxy)) t.ok = false;
     return t;
+}
+__device__ __forceinline__ TriScreen tri_screen(const RasterJob& J, uint32_t slot) {
+    return screen_of(J, J.xyuv[3 * (size_t)slot], J.xyuv[3 * (size_t)slot + 1], J.xyuv[3 * (size_t)slot + 2]);
 }
 
 // Edge weights of pixel centre (x, y): w_c for edge a->b, w_a for b->c, w_b for c->a.
@@ -192,7 +194,7 @@ __device__ __forceinline__ uint32_t bbox_pixels(const TriScreen& t) {
 // Triangles with larger pixel boxes are shared out to the whole grid in kBigChunk-pixel
 // chunks (or, when the shared list is full, tested by their warp together); smaller ones are
 // tested by their own thread.
-constexpr uint32_t kBigBox = 32;
+constexpr uint32_t kBigBox = 8;
 
 // A large triangle shared by the grid: its pixel box (row-major) is cut into kBigChunk-pixel
 // chunks [chunk0, chunk0 + ceil(box / kBigChunk)); `hit` is its entry in the hit list and
@@ -305,6 +307,66 @@ __global__ void k_scan_add(uint32_t* out, uint32_t n, const uint32_t* __restrict
         if (base + k < n) out[base + k] += add;
 }
 
+// One warp step of pass 1 over 32 triangles (`valid` lanes): classify each, count the small
+// boxes, register the large ones, and append the hits in draw order.
+__device__ __forceinline__ void count_step(const RasterJob& J, bool valid, const TriScreen& t, uint32_t slot, uint32_t seg,
+                                           uint32_t u, uint32_t base, uint32_t lane, uint4* hits, BigTri* big,
+                                           uint32_t* chunk_tri, unsigned long long* ctr, uint32_t& nh, uint32_t& frags) {
+    uint32_t k = 0, ref = 0;
+    bool hit = false, own_big = false;
+    const uint32_t box = valid ? bbox_pixels(t) : 0u;
+    const bool large = box > kBigBox;
+    const uint32_t lm = __ballot_sync(0xffffffffu, large);
+    unsigned long long b = 0, ch0 = 0;
+    uint32_t nct = 0;
+    if (lm) {  // one pair of atomics per warp for its large triangles
+        nct = large ? (box + kBigChunk - 1) / kBigChunk : 0u;
+        uint32_t tot;
+        const uint32_t before = warp_exclusive(nct, lane, tot);
+        unsigned long long b0 = 0, c0 = 0;
+        if (lane == 0) {
+            b0 = atomicAdd(&ctr[0], (unsigned long long)__popc(lm));
+            c0 = atomicAdd(&ctr[1], (unsigned long long)tot);
+        }
+        b = __shfl_sync(0xffffffffu, b0, 0) + __popc(lm & ((1u << lane) - 1u));
+        ch0 = __shfl_sync(0xffffffffu, c0, 0) + before;
+    }
+    if (large) {
+        hit = true;
+        own_big = true;
+        const bool fits = b < J.big_cap && ch0 + nct <= kChunkCap;
+        // the reserved chunks below the cap name their triangle, or none when it did not fit
+        for (unsigned long long q = ch0; q < ch0 + nct && q < kChunkCap; q++)
+            chunk_tri[q] = fits ? (uint32_t)b : 0xFFFFFFFFu;
+        if (fits) {
+            own_big = false;
+            ref = (uint32_t)b + 1;
+            BigTri& B = big[b];
+            B.slot = slot;
+            B.seg = seg;
+            B.unit = u;
+            B.chunk0 = (uint32_t)ch0;
+        }
+    } else if (box) {
+        k = tri_fragments(t);
+        hit = k != 0;
+    }
+    // large triangles the shared list could not take: the warp counts their pixels
+    for (uint32_t m = __ballot_sync(0xffffffffu, own_big); m; m &= m - 1) {
+        const int l = __ffs(m) - 1;
+        const uint32_t cnt = warp_fragments(tri_screen(J, __shfl_sync(0xffffffffu, slot, l)), lane);
+        if (lane == (uint32_t)l) k = cnt;
+    }
+    frags += k;
+    const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+    if (hit) {
+        const uint32_t pos = base + nh + __popc(hm & ((1u << lane) - 1u));
+        hits[pos] = make_uint4(slot, seg, k, ref);
+        if (ref) big[ref - 1].hit = pos;
+    }
+    nh += __popc(hm);
+}
+
 // Fragment pass 1, one warp per unit of kUnitTris triangles in draw order: count the pixel
 // centres each covers and keep, in draw order, the triangles that may cover any:
 // hits[u * kUnitTris + i] = (output slot, render pair, count, shared-list index + 1 or 0),
@@ -318,56 +380,25 @@ __global__ void __launch_bounds__(kFragThreads) k_frag_count(RasterJob J, uint32
     if (u >= nunits) return;  // the whole warp
     const uint32_t n = __ldg(&J.cbase[J.nseg]), base = u * kUnitTris;
     uint32_t nh = 0, frags = 0, pr = 0;
-    for (uint32_t j = 0; j < kUnitTris && base + j < n; j += 32) {
-        const uint32_t c = base + j + lane;
-        uint32_t k = 0, slot = 0, seg = 0, ref = 0;
-        bool hit = false, own_big = false;
-        if (c < n) {
-            pr = find_pair(J, c, j ? pr : 0u);
-            seg = J.seg_lo + pr;
-            slot = J.segs[seg].out_base + (c - __ldg(&J.cbase[pr]));
-            const TriScreen t = tri_screen(J, slot);
-            const uint32_t box = bbox_pixels(t);
-            if (box > kBigBox) {
-                hit = true;
-                own_big = true;
-                const unsigned long long b = atomicAdd(&ctr[0], 1ull);
-                if (b < J.big_cap) {
-                    const uint32_t nct = (box + kBigChunk - 1) / kBigChunk;
-                    const unsigned long long ch0 = atomicAdd(&ctr[1], (unsigned long long)nct);
-                    const bool fits = ch0 + nct <= kChunkCap;
-                    // chunks below the cap always name their triangle, or none when it did not fit
-                    for (unsigned long long q = ch0; q < ch0 + nct && q < kChunkCap; q++)
-                        chunk_tri[q] = fits ? (uint32_t)b : 0xFFFFFFFFu;
-                    if (fits) {
-                        own_big = false;
-                        ref = (uint32_t)b + 1;
-                        BigTri& B = big[b];
-                        B.slot = slot;
-                        B.seg = seg;
-                        B.unit = u;
-                        B.chunk0 = (uint32_t)ch0;
-                    }
-                }
-            } else if (box) {
-                k = tri_fragments(t);
-                hit = k != 0;
-            }
+    // 64 triangles a step, two per lane, both loaded before either is classified
+    for (uint32_t j = 0; j < kUnitTris && base + j < n; j += 64) {
+        const uint32_t c0 = base + j + lane, c1 = c0 + 32;
+        uint32_t slot0 = 0, seg0 = 0, slot1 = 0, seg1 = 0;
+        float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), b0 = a0, d0 = a0, a1 = a0, b1 = a0, d1 = a0;
+        if (c0 < n) {
+            pr = find_pair(J, c0, j ? pr : 0u);
+            seg0 = J.seg_lo + pr;
+            slot0 = J.segs[seg0].out_base + (c0 - __ldg(&J.cbase[pr]));
+            a0 = J.xyuv[3 * (size_t)slot0]; b0 = J.xyuv[3 * (size_t)slot0 + 1]; d0 = J.xyuv[3 * (size_t)slot0 + 2];
         }
-        // large triangles the shared list could not take: the warp counts their pixels
-        for (uint32_t m = __ballot_sync(0xffffffffu, own_big); m; m &= m - 1) {
-            const int l = __ffs(m) - 1;
-            const uint32_t cnt = warp_fragments(tri_screen(J, __shfl_sync(0xffffffffu, slot, l)), lane);
-            if (lane == (uint32_t)l) k = cnt;
+        if (c1 < n) {
+            pr = find_pair(J, c1, pr);
+            seg1 = J.seg_lo + pr;
+            slot1 = J.segs[seg1].out_base + (c1 - __ldg(&J.cbase[pr]));
+            a1 = J.xyuv[3 * (size_t)slot1]; b1 = J.xyuv[3 * (size_t)slot1 + 1]; d1 = J.xyuv[3 * (size_t)slot1 + 2];
         }
-        frags += k;
-        const uint32_t hm = __ballot_sync(0xffffffffu, hit);
-        if (hit) {
-            const uint32_t pos = base + nh + __popc(hm & ((1u << lane) - 1u));
-            hits[pos] = make_uint4(slot, seg, k, ref);
-            if (ref) big[ref - 1].hit = pos;
-        }
-        nh += __popc(hm);
+        count_step(J, c0 < n, screen_of(J, a0, b0, d0), slot0, seg0, u, base, lane, hits, big, chunk_tri, ctr, nh, frags);
+        count_step(J, c1 < n, screen_of(J, a1, b1, d1), slot1, seg1, u, base, lane, hits, big, chunk_tri, ctr, nh, frags);
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, o);
     if (lane == 0) {
