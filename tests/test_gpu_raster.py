@@ -148,3 +148,37 @@ def test_large_triangles_shared_or_per_warp(ctx, shared):
         ctx.set_textures([])
     ocol, odep = pyoracle.raster(pyoracle.render(sd, cam), sd, cam, textures=tex)
     assert np.array_equal(col, ocol) and np.array_equal(dep, odep)
+
+
+def test_raster_edge_cases(ctx):
+    """Nothing visible (the camera looks away): both images stay cleared. Images of 1x1, 3x2
+    and 7x5 pixels (fewer pixels than a block or a warp) and a 3x3 orthographic view against
+    the oracle. A job with no render pair (an empty scene) rasterises to cleared images."""
+    sd = scenes.uv_sphere_scene(1)
+    sid = ctx.upload(sd)
+    try:
+        away = scenes.camera(w=64, h=48, rot=scenes.rotate(0, 1, 0, float(np.pi)), fov=75.0)
+        ctx.render(sid, away)
+        assert ctx.sync().visible_tris == 0
+        col, dep = ctx.raster()
+        assert col.shape == (48, 64, 4) and not col.any() and not dep.any()
+        near = (0.0, 0.0, -3.0)  # two units from the sphere's centre: it fills the small views
+        cams = [scenes.camera(pos=near, w=w, h=h, fov=75.0) for w, h in ((1, 1), (3, 2), (7, 5))]
+        cams.append(scenes.camera(pos=near, w=3, h=3, perspective=0, ortho_scale=3.0))
+        for cam in cams:
+            ctx.render(sid, cam)
+            col, dep = ctx.raster()
+            ocol, odep = pyoracle.raster(pyoracle.render(sd, cam), sd, cam)
+            assert col.shape == (cam.height, cam.width, 4)
+            assert np.array_equal(col, ocol) and np.array_equal(dep, odep), (cam.width, cam.height)
+            assert ocol[..., 3].any(), "the sphere covers pixels"
+    finally:
+        ctx.release(sid)
+    empty = scenes.SceneData([scenes.quad_mesh(1.0, 1.0)], 0, [], [[]], name="empty")
+    eid = ctx.upload(empty)
+    try:
+        ctx.render(eid, scenes.camera(w=16, h=16))
+        col, dep = ctx.raster()
+        assert not col.any() and not dep.any()
+    finally:
+        ctx.release(eid)

@@ -200,7 +200,7 @@ constexpr uint32_t kBigBox = 8;
 // chunks [chunk0, chunk0 + ceil(box / kBigChunk)); `hit` is its entry in the hit list and
 // `cursor` the next free fragment of its range (set by the write pass).
 struct BigTri {
-    uint32_t slot, seg, hit, unit, chunk0, cursor, pad0, pad1;
+    uint32_t slot, hit, unit, chunk0, cursor, pad0, pad1, pad2;
 };
 
 __device__ __forceinline__ uint32_t warp_exclusive(uint32_t v, uint32_t lane, uint32_t& total) {
@@ -343,7 +343,6 @@ __device__ __forceinline__ void count_step(const RasterJob& J, bool valid, const
             ref = (uint32_t)b + 1;
             BigTri& B = big[b];
             B.slot = slot;
-            B.seg = seg;
             B.unit = u;
             B.chunk0 = (uint32_t)ch0;
         }
