@@ -171,7 +171,11 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl")
 
     sd = make_scene(args.workload, args.models)
+    if args.textured:  # raster textures on every material (the vertex stage does not change)
+        scenes.texture_materials(sd, 7)
     ctx = Context(local_rank)
+    if args.textured:
+        ctx.set_textures(scenes.raster_textures())
     sid = ctx.upload(sd)
     cam = sd.camera
     animate = args.workload == "batched"
@@ -305,7 +309,7 @@ def run_ours(args, rank, world, local_rank):
         # 108 B), the colour and depth images written once (8 B per pixel)
         rbytes = 108 * int(rst.visible_tris) + 8 * cam.width * cam.height
         rpeak, rpeak_kind = peaks()
-        raster = {"ms_per_frame": rms, "device_ms_per_frame": rdev, "image": f"{cam.width}x{cam.height}",
+        raster = {"textured": bool(args.textured), "ms_per_frame": rms, "device_ms_per_frame": rdev, "image": f"{cam.width}x{cam.height}",
                   "visible_tris": int(rst.visible_tris), "tris_per_s": int(rst.visible_tris) / (rms / 1e3),
                   "covered_pixels": int((col[..., 3] > 0).sum()),
                   "roofline": {"bound": "hbm", "achieved": rbytes / (rdev / 1e3) / 1e9, "peak": rpeak, "unit": "GB/s",
@@ -499,6 +503,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep in the default run")
     ap.add_argument("--no-raster", action="store_true", help="skip rasterising the last frame")
+    ap.add_argument("--textured", action="store_true",
+                    help="texture every material for the raster (three textures, both filters, UV and screen "
+                         "mapping, alpha clip on some)")
     ap.add_argument("--rates", default="100,1000,5000,20000", help="serving request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival span per serving rate")
     ap.add_argument("--serve-max-requests", type=int, default=8000)
