@@ -318,11 +318,19 @@ def run_ours(args, rank, world, local_rank):
                   "note": "t3d_frame_raster (fragments, stable sort by pixel, per-pixel passes): ms_per_frame is "
                           "wall time incl. its host syncs, device_ms_per_frame CUDA events on its stream"}
 
+    # ---- the frame with one vertex-stage feature on for every model ----
+    features = None
+    if rank == 0 and not args.no_features and args.workload == "batched" and args.models == 4096:
+        ctx.release(sid)
+        sid = None
+        features = feature_frames(ctx, stream, sh, ms_per_step)
+
     # ---- serving sweep (continuous batching over 64 resident scenes) ----
     serve = None
     if rank == 0 and not args.no_serving and args.workload == "batched":
-        ctx.release(sid)
-        sid = None
+        if sid is not None:
+            ctx.release(sid)
+            sid = None
         serve = serving_sweep(ctx, [int(r) for r in args.rates.split(",")], args.serve_seconds,
                               args.serve_max_requests)
 
@@ -364,6 +372,7 @@ def run_ours(args, rank, world, local_rank):
             "batched_over_plain": (value / max(1, world)) / plain["tris_per_s"] if plain else None,
             "serving": serve,
             "raster": raster,
+            "features": features,
         }
         print(json.dumps(line))
     ctx.close()
@@ -372,6 +381,38 @@ def run_ours(args, rank, world, local_rank):
 
 
 # -------------------------------------------------------------- serving ----
+def feature_frames(ctx, stream, sh, base_ms, frames=10, warmup=3):
+    """The 4096-model frame with one vertex-stage feature on for every model (scenes.frame_variant):
+    device time per animated frame (CUDA graph replays, CUDA events on the replay stream), visible
+    triangles per second, and the time relative to the plain frame."""
+    import torch
+    from tetra3d_gb300 import scenes
+    out = {}
+    for kind in scenes.FRAME_VARIANTS:
+        sd = scenes.frame_variant(kind)
+        sid = ctx.upload(sd)
+        try:
+            ctx.graph_capture(sid, sd.camera, animate=True)
+            ctx.graph_replay(warmup, stream=sh)
+            torch.cuda.synchronize()
+            v0, _ = ctx.counters()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.graph_replay(frames, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / frames
+            v1, _ = ctx.counters()
+            vis = (v1 - v0) / frames
+            out[kind] = {"ms_per_frame": round(ms, 4), "visible_tris": int(vis), "tris_per_s": vis / (ms / 1e3),
+                         "time_vs_plain_frame": round(ms / base_ms, 3)}
+        finally:
+            ctx.release(sid)
+    out["note"] = ("4096-model frame with the feature on every model, animated, CUDA graph replays; "
+                   "time_vs_plain_frame = ms / the plain frame's ms")
+    return out
+
+
 def serving_sweep(ctx, rates, seconds, max_requests, seed=7, baseline_requests=1000):
     """Continuous-batching server over 64 resident scenes at Poisson rates; then the same requests
     rendered one request per launch, synchronously (the plain request loop)."""
@@ -503,6 +544,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep in the default run")
     ap.add_argument("--no-raster", action="store_true", help="skip rasterising the last frame")
+    ap.add_argument("--no-features", action="store_true",
+                    help="skip the frame variants with shape keys, skinning, billboards, subdivision, batching")
     ap.add_argument("--textured", action="store_true",
                     help="texture every material for the raster (three textures, both filters, UV and screen "
                          "mapping, alpha clip on some)")

@@ -672,3 +672,20 @@ def test_multi_tile_altered_parts(ctx):
             assert_frames_equal(ctx.download(), ref, f"big altered/mode{mode}")
     finally:
         ctx.release(sid)
+
+
+@pytest.mark.parametrize("kind", scenes.FRAME_VARIANTS)
+def test_full_frame_variants_match_oracle(ctx, kind):
+    """The full 4096-model frame (69.7 M triangles, 1920x1080) with one feature on for every model
+    -- shape keys, skinning, billboards, auto-subdivision, dynamic batching -- bit for bit against
+    the oracle (run on all host threads)."""
+    import os
+    sd = scenes.frame_variant(kind)
+    ref = pyoracle.render(sd, sd.camera, threads=os.cpu_count() or 1)
+    assert ref.visible_tris > 20_000_000
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), ref, f"frame/{kind}")
+    finally:
+        ctx.release(sid)

@@ -996,6 +996,66 @@ def texture_materials(sd, seed):
     return sd
 
 
+FRAME_VARIANTS = ("shape_keys", "skinned", "billboard", "subdivision", "batched")
+
+
+def frame_variant(kind, seed=4, n=4096):
+    """The benchmark frame (batched_scene) with one vertex-stage feature switched on at scale:
+    'shape_keys' (two keys on every mesh), 'skinned' (every model skinned by a four-bone chain
+    bending it about its own axis), 'billboard' (every material billboarded, camera-Y up),
+    'subdivision' (the icospheres of up to 320 triangles auto-subdivided up to twice within 250
+    units) and 'batched' (the noise grids drawn in the dynamic batches of 16 icosphere owners)."""
+    sd = batched_scene(seed, n=n)
+    rng = np.random.Generator(np.random.PCG64(seed + 77))
+    if kind == "shape_keys":
+        for m in sd.meshes:
+            bulge = (m.normals * rng.uniform(0.0, 0.2, (m.nverts, 1))).astype(F32)
+            m.shape_positions = np.stack([bulge, rng.uniform(-0.05, 0.05, bulge.shape).astype(F32)])
+            m.shape_normals = rng.uniform(-0.1, 0.1, (2, m.nverts, 3)).astype(F32)
+            m.shape_weights = np.array([0.6, -0.3], F32)
+    elif kind == "skinned":
+        nb = 4
+        for m in sd.meshes:
+            y = m.positions[:, 1].astype(np.float64)
+            f = (y - y.min()) / max(y.max() - y.min(), 1e-6) * (nb - 1)
+            i0 = np.clip(np.floor(f), 0, nb - 2).astype(np.uint32)
+            t = (f - i0).astype(F32)
+            m.joints = np.zeros((m.nverts, 4), np.uint32)
+            m.weights = np.zeros((m.nverts, 4), F32)
+            m.joints[:, 0], m.joints[:, 1] = i0, i0 + 1
+            m.weights[:, 0], m.weights[:, 1] = F32(1) - t, t
+        M = sd.mv["transform"].reshape(n, 4, 4)
+        bones = np.empty((n * nb, 4, 4), F32)
+        for k in range(n):
+            for b in range(nb):
+                bend = mult(rotate(1, 0, 0, 0.15 * b), rotate(0, 0, 1, -0.1 * b))
+                bones[k * nb + b] = mult(bend, M[k])
+        sd.mv["skinned"] = 1
+        sd.mv["bone_first"] = np.arange(n, dtype=np.uint32) * nb
+        sd.bones = bones
+    elif kind == "billboard":
+        for m in sd.meshes:
+            for p in m.parts:
+                p["mat"].update(billboard=1, billboard_lock=(0, 0, 0), billboard_up=abi.BILLBOARD_UP_CAMERA_Y,
+                                billboard_depth=abi.DEPTH_DEFAULT)
+    elif kind == "subdivision":
+        for m in sd.meshes:
+            if m.ntris <= 320:
+                m.auto_subdivide = 1
+        sd.subdivision_levels = np.array([(250.0 * 250.0, 0.3)], F32)  # model-space triangle size
+        sd.max_subdivisions = 2
+    elif kind == "batched":
+        owners = np.arange(0, 32, 2)  # icospheres (even models)
+        members = np.arange(1, n, 2)  # noise grids
+        sd.mv["batched"][members] = 1
+        sd.mv["batch_owner"][members] = owners[rng.integers(0, len(owners), len(members))]
+        sd.mv["batch_part"][members] = 0
+    else:
+        raise ValueError(kind)
+    sd.name = f"{sd.name}_{kind}"
+    return sd
+
+
 def textured_scene(seed=21, n=48, w=1280, h=720):
     """The feature scene with textured materials (texture_materials)."""
     return texture_materials(feature_scene(seed, n=n, w=w, h=h), seed)
