@@ -867,9 +867,15 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     }
     const uint64_t npx = (uint64_t)J.W * J.H;
     int rc;
-    // the fragment passes run one warp per kUnitTris triangles of the job's capacity; the
-    // visible count n = cbase[nseg] stays on the device (units past it only record zeros)
-    const uint32_t nunits = (uint32_t)std::max<uint64_t>(1, (cap + kUnitTris - 1) / kUnitTris);
+    // the fragment passes run one warp per kUnitTris triangles: of the job's visible count
+    // when a frame sync has brought it to the host, else of its capacity (the device's count
+    // n = cbase[nseg] bounds the work either way; units past it only record zeros)
+    uint64_t span = cap;
+    if (ctx->frame_valid && !ctx->frame_pending) {
+        span = 0;
+        for (uint32_t s = seg_lo; s < seg_hi; s++) span += F.seg_info[s].count;
+    }
+    const uint32_t nunits = (uint32_t)std::max<uint64_t>(1, (span + kUnitTris - 1) / kUnitTris);
     const uint32_t fblocks = (nunits + kFragThreads / 32 - 1) / (kFragThreads / 32);
     const uint32_t bigblocks = (uint32_t)std::max(1, ctx->num_sms) * 4;
     if ((rc = S.cbase.ensure(ctx, 4ull * (nseg + 1))) || (rc = S.hits.ensure(ctx, 16ull * kUnitTris * nunits)) ||
