@@ -122,9 +122,10 @@ struct DevJob {
     const float* cells;
     const DevLight* lights;
     const float4* shape_a;  // per (key, vertex): position delta xyz, normal delta x
-    const float4* shape_b;  // per (key, vertex): normal delta y, z
+    const float2* shape_b;  // per (key, vertex): normal delta y, z
     const float* shape_w;   // key weights
     const uint4* vjoint;    // per pool vertex: four joints (skinned meshes)
+    const uint32_t* vjoint8;  // the same packed one byte each, when every joint of the scene is below 256 (else null)
     const float4* vweight;  // per pool vertex: their weights
     const float4* bones;    // 4 rows per bone: Node.boneInfluence
     const float4* sub_info; // auto-subdivided meshes, per pool triangle: its base triangle's Normal and MaxSpan

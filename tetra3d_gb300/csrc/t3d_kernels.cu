@@ -866,9 +866,10 @@ __device__ __forceinline__ bool tri_visible(float nearp, float farp, bool backfa
 // first vertex; a = (px, py, pz, nx), b = (ny, nz, u, v).
 struct AlterSrc {
     const float4* sa;     // key k, vertex v: sa[k * nverts + v] = position delta xyz, normal delta x
-    const float4* sb;     // normal delta y, z
+    const float2* sb;     // normal delta y, z
     const float* sw;      // key weights
     const uint4* vj;      // joints of vertex v
+    const uint32_t* vj8;  // or the same as bytes (null when not packed)
     const float4* vw;     // their weights
     const float4* bones;  // the model's bone 0 (4 rows each)
     uint32_t nkeys, nverts;
@@ -879,12 +880,18 @@ __device__ __forceinline__ void alter_vertex(const AlterSrc& ms, uint32_t flags,
     for (uint32_t k = 0; k < nk; k++) {
         const float w = ms.sw[k];
         const float4 da = ms.sa[(size_t)k * ms.nverts + v];
-        const float4 db = ms.sb[(size_t)k * ms.nverts + v];
+        const float2 db = ms.sb[(size_t)k * ms.nverts + v];
         a.x += da.x * w; a.y += da.y * w; a.z += da.z * w;
         a.w += da.w * w; b.x += db.x * w; b.y += db.y * w;
     }
     if (flags & SEG_SKINNED) {
-        const uint4 jv = ms.vj[v];
+        uint4 jv;
+        if (ms.vj8) {
+            const uint32_t p = ms.vj8[v];
+            jv = make_uint4(p & 255u, (p >> 8) & 255u, (p >> 16) & 255u, p >> 24);
+        } else {
+            jv = ms.vj[v];
+        }
         const float4 wv = ms.vw[v];
         const uint32_t js[4] = {jv.x, jv.y, jv.z, jv.w};
         const float ws[4] = {wv.x, wv.y, wv.z, wv.w};
@@ -934,6 +941,7 @@ __device__ __forceinline__ void vertex_chunk_altered(const FrameParams& P, const
     src.sb = J.shape_b + me.shape_first + seg.vmin;
     src.sw = J.shape_w + me.weight_first;
     src.vj = J.vjoint + me.vbase + seg.vmin;
+    src.vj8 = J.vjoint8 ? J.vjoint8 + me.vbase + seg.vmin : nullptr;
     src.vw = J.vweight + me.vbase + seg.vmin;
     src.bones = J.bones + 4 * (size_t)J.models[P.insts[seg.inst].model].bone_first;
     for (uint32_t lv = v0 + threadIdx.x; lv < v1; lv += blockDim.x) {

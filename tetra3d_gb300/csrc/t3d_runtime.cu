@@ -648,6 +648,11 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     }
     sc->nverts = nv;
     sc->ntris = nt;
+    // joints travel as bytes when the scene's largest joint fits one
+    bool joint8 = any_skin;
+    for (const SceneMesh& sm : sc->meshes)
+        if (sm.skin && sm.max_joint > 255u) joint8 = false;
+    sc->joint8 = joint8;
     // device pools
     int rc;
     if ((rc = sc->va.ensure(ctx, nv * 16)) || (rc = sc->vb.ensure(ctx, nv * 16)) || (rc = sc->vc.ensure(ctx, nv * 16)) ||
@@ -657,9 +662,9 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         (rc = sc->dmodels.ensure(ctx, sizeof(DevModel) * std::max<size_t>(1, d->num_models))) ||
         (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))) ||
         (rc = sc->shape_a.ensure(ctx, 16 * std::max<uint64_t>(1, nshape))) ||
-        (rc = sc->shape_b.ensure(ctx, 16 * std::max<uint64_t>(1, nshape))) ||
+        (rc = sc->shape_b.ensure(ctx, 8 * std::max<uint64_t>(1, nshape))) ||
         (rc = sc->shape_w.ensure(ctx, 4 * std::max<uint64_t>(1, nkeys_total))) ||
-        (rc = sc->vjoint.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
+        (rc = sc->vjoint.ensure(ctx, (joint8 ? 4 : 16) * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
         (rc = sc->vweight.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
         (rc = sc->bones.ensure(ctx, 64 * std::max<size_t>(1, d->num_bones))) ||
         (rc = sc->sub_info.ensure(ctx, 16 * (any_subdiv ? std::max<uint64_t>(1, nt) : 1))) ||
@@ -762,22 +767,33 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         CK(cudaMemcpy((char*)sc->centers.ptr + (size_t)sc->meshes[m].tbase * 12, ctr.data(), me.num_triangles * 12ull,
                       cudaMemcpyHostToDevice));
         SceneMesh& smh = sc->meshes[m];
-        if (me.num_shape_keys) {  // deltas as float4 pairs: (px, py, pz, nx), (ny, nz, 0, 0)
+        if (me.num_shape_keys) {  // deltas as (px, py, pz, nx) and (ny, nz)
             const size_t ne = (size_t)me.num_shape_keys * me.num_vertices;
-            std::vector<float4> sa(ne), sb(ne);
+            std::vector<float4> sa(ne);
+            std::vector<float2> sb(ne);
             for (size_t q = 0; q < ne; q++) {
                 const float* p = me.shape_positions + 3 * q;
                 const float* nn = me.shape_normals + 3 * q;
                 sa[q] = make_float4(p[0], p[1], p[2], nn[0]);
-                sb[q] = make_float4(nn[1], nn[2], 0.f, 0.f);
+                sb[q] = make_float2(nn[1], nn[2]);
             }
             CK(cudaMemcpy((float4*)sc->shape_a.ptr + smh.shape_first, sa.data(), 16 * ne, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy((float4*)sc->shape_b.ptr + smh.shape_first, sb.data(), 16 * ne, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy((float2*)sc->shape_b.ptr + smh.shape_first, sb.data(), 8 * ne, cudaMemcpyHostToDevice));
             CK(cudaMemcpy((float*)sc->shape_w.ptr + smh.weight_first, me.shape_weights, 4ull * me.num_shape_keys,
                           cudaMemcpyHostToDevice));
         }
-        if (me.joints) {
+        if (me.joints && sc->joint8) {
+            std::vector<uint32_t> packed(me.num_vertices);
+            for (uint32_t v = 0; v < me.num_vertices; v++) {
+                const uint32_t* jv = me.joints + 4 * (size_t)v;
+                packed[v] = jv[0] | (jv[1] << 8) | (jv[2] << 16) | (jv[3] << 24);
+            }
+            CK(cudaMemcpy((uint32_t*)sc->vjoint.ptr + smh.vbase, packed.data(), 4ull * me.num_vertices,
+                          cudaMemcpyHostToDevice));
+        } else if (me.joints) {
             CK(cudaMemcpy((uint4*)sc->vjoint.ptr + smh.vbase, me.joints, 16ull * me.num_vertices, cudaMemcpyHostToDevice));
+        }
+        if (me.joints) {
             CK(cudaMemcpy((float4*)sc->vweight.ptr + smh.vbase, me.weights, 16ull * me.num_vertices,
                           cudaMemcpyHostToDevice));
         }
@@ -911,9 +927,10 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.models = (DevModel*)sc->dmodels.ptr;
         dj.cells = (const float*)sc->cells.ptr;
         dj.shape_a = (const float4*)sc->shape_a.ptr;
-        dj.shape_b = (const float4*)sc->shape_b.ptr;
+        dj.shape_b = (const float2*)sc->shape_b.ptr;
         dj.shape_w = (const float*)sc->shape_w.ptr;
         dj.vjoint = (const uint4*)sc->vjoint.ptr;
+        dj.vjoint8 = sc->joint8 ? (const uint32_t*)sc->vjoint.ptr : nullptr;
         dj.vweight = (const float4*)sc->vweight.ptr;
         dj.bones = (const float4*)sc->bones.ptr;
         dj.sub_info = (const float4*)sc->sub_info.ptr;

@@ -57,6 +57,7 @@ struct Scene {
     uint64_t struct_ver = 0, model_ver = 0;
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     DevBuf shape_a, shape_b, shape_w, vjoint, vweight, bones;
+    bool joint8 = false;  // vjoint holds four 8-bit joints per vertex (every joint below 256)
     DevBuf sub_info, sub_rel, sub_levels, cell_use_off, cell_use_items;
     std::vector<char> light_uses;    // per light: a volume whose cells use lights
     std::vector<char> light_nested;  // per light: used by some cell (cannot become a volume)
