@@ -404,8 +404,11 @@ def feature_frames(ctx, stream, sh, base_ms, frames=10, warmup=3):
             ms = e0.elapsed_time(e1) / frames
             v1, _ = ctx.counters()
             vis = (v1 - v0) / frames
+            st = ctx.sync()
             out[kind] = {"ms_per_frame": round(ms, 4), "visible_tris": int(vis), "tris_per_s": vis / (ms / 1e3),
-                         "time_vs_plain_frame": round(ms / base_ms, 3)}
+                         "time_vs_plain_frame": round(ms / base_ms, 3),
+                         "phase_busy_us_last_frame": {k: round(float(v), 1) for k, v in zip(
+                             ("prep", "vertex", "triangles", "hist", "scan", "rank_emit"), st.phase_busy)}}
         finally:
             ctx.release(sid)
     out["note"] = ("4096-model frame with the feature on every model, animated, CUDA graph replays; "

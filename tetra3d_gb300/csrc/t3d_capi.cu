@@ -244,9 +244,13 @@ int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, con
     }
     cudaSetDevice(ctx->device);
     if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
-    if (n)
+    if (n) {
         CKR(cudaMemcpy((float*)sc->shape_w.ptr + sc->meshes[mesh].weight_first, weights, 4ull * n,
                        cudaMemcpyHostToDevice));
+        int rc;
+        if ((rc = bake_shapes(ctx, sc, mesh))) return rc;  // the mesh's keyed streams for the new weights
+        CKR(cudaStreamSynchronize(ctx->stream));
+    }
     return T3D_OK;
 }
 

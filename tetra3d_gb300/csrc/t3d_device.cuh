@@ -46,7 +46,7 @@ enum : uint32_t {
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
-    SEG_ALTERED = SEG_SKINNED | SEG_SHAPES | SEG_BILLBOARD | SEG_SNAP | SEG_NESTED,
+    SEG_ALTERED = SEG_SKINNED | SEG_BILLBOARD | SEG_SNAP | SEG_NESTED,
 };
 constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }
@@ -64,7 +64,7 @@ struct DevMesh {
     uint32_t shape_first;    // key k, vertex v: shape pool entry shape_first + k * nverts + v
     uint32_t nkeys;          // shape keys
     uint32_t weight_first;   // key k's weight: shape_w[weight_first + k]
-    uint32_t pad;
+    uint32_t sbase;          // with shape keys: first vertex of the mesh's keyed streams (vaS / vbS)
 };
 
 // Resident, animatable model state.
@@ -123,6 +123,8 @@ struct DevJob {
     const DevLight* lights;
     const float4* shape_a;  // per (key, vertex): position delta xyz, normal delta x
     const float2* shape_b;  // per (key, vertex): normal delta y, z
+    const float4* vaS;      // shape-keyed meshes: the keyed streams, baked per weight set (as va / vb)
+    const float4* vbS;
     const float* shape_w;   // key weights
     const uint4* vjoint;    // per pool vertex: four joints (skinned meshes)
     const uint32_t* vjoint8;  // the same packed one byte each, when every joint of the scene is below 256 (else null)

@@ -526,8 +526,9 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
         }
         e.flags = f;
         e.seg_flags = seg.flags;
-        e.va = J.va + me.vbase;
-        e.vb = J.vb + me.vbase;
+        // shape-keyed meshes read their keyed streams (baked once per weight set)
+        e.va = me.nkeys ? J.vaS + me.sbase : J.va + me.vbase;
+        e.vb = me.nkeys ? J.vbS + me.sbase : J.vb + me.vbase;
         e.vc = J.vc + me.vbase;
         e.idx = J.idx + 3 * (size_t)me.tbase;
         e.cells = J.cells;
@@ -861,29 +862,37 @@ __device__ __forceinline__ bool tri_visible(float nearp, float farp, bool backfa
     return !(isnan(depth) || isinf(depth));
 }
 
-// Mesh.VertexPositionWithShapeKeys / VertexNormalWithShapeKeys (mesh.go:796-822)
-// and Model.skinVertex (model.go:559-594) for vertex v counted from the part's
-// first vertex; a = (px, py, pz, nx), b = (ny, nz, u, v).
+// Model.skinVertex (model.go:559-594) for vertex v counted from the part's first
+// vertex (its shape keys are already in the streams); a = (px, py, pz, nx),
+// b = (ny, nz, u, v).
 struct AlterSrc {
-    const float4* sa;     // key k, vertex v: sa[k * nverts + v] = position delta xyz, normal delta x
-    const float2* sb;     // normal delta y, z
-    const float* sw;      // key weights
     const uint4* vj;      // joints of vertex v
     const uint32_t* vj8;  // or the same as bytes (null when not packed)
     const float4* vw;     // their weights
     const float4* bones;  // the model's bone 0 (4 rows each)
-    uint32_t nkeys, nverts;
 };
 
-__device__ __forceinline__ void alter_vertex(const AlterSrc& ms, uint32_t flags, uint32_t v, float4& a, float4& b) {
-    const uint32_t nk = ms.nkeys;
-    for (uint32_t k = 0; k < nk; k++) {
-        const float w = ms.sw[k];
-        const float4 da = ms.sa[(size_t)k * ms.nverts + v];
-        const float2 db = ms.sb[(size_t)k * ms.nverts + v];
+// Mesh.VertexPositionWithShapeKeys / VertexNormalWithShapeKeys (mesh.go:796-822):
+// a mesh's keyed streams, key by key in order, for one weight set. Every model of
+// the mesh reads them (the weights belong to the mesh).
+__global__ void k_bake_shapes(const float4* __restrict__ va, const float4* __restrict__ vb,
+                              const float4* __restrict__ sa, const float2* __restrict__ sb,
+                              const float* __restrict__ sw, uint32_t nverts, uint32_t nkeys, float4* oa, float4* ob) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nverts) return;
+    float4 a = va[v], b = vb[v];
+    for (uint32_t k = 0; k < nkeys; k++) {
+        const float w = sw[k];
+        const float4 da = sa[(size_t)k * nverts + v];  // position delta xyz, normal delta x
+        const float2 db = sb[(size_t)k * nverts + v];  // normal delta y, z
         a.x += da.x * w; a.y += da.y * w; a.z += da.z * w;
         a.w += da.w * w; b.x += db.x * w; b.y += db.y * w;
     }
+    oa[v] = a;
+    ob[v] = b;
+}
+
+__device__ __forceinline__ void alter_vertex(const AlterSrc& ms, uint32_t flags, uint32_t v, float4& a, float4& b) {
     if (flags & SEG_SKINNED) {
         uint4 jv;
         if (ms.vj8) {
@@ -935,11 +944,6 @@ __device__ __forceinline__ void vertex_chunk_altered(const FrameParams& P, const
     const DevJob& J = P.jobs[seg.job];
     const DevMesh& me = J.meshes[seg.mesh];
     AlterSrc src;
-    src.nkeys = (seg.flags & SEG_SHAPES) ? me.nkeys : 0u;
-    src.nverts = me.nverts;
-    src.sa = J.shape_a + me.shape_first + seg.vmin;
-    src.sb = J.shape_b + me.shape_first + seg.vmin;
-    src.sw = J.shape_w + me.weight_first;
     src.vj = J.vjoint + me.vbase + seg.vmin;
     src.vj8 = J.vjoint8 ? J.vjoint8 + me.vbase + seg.vmin : nullptr;
     src.vw = J.vweight + me.vbase + seg.vmin;
@@ -1107,7 +1111,11 @@ __device__ __noinline__ void prefetch_triangle_tile(const FrameParams& P, uint32
     const size_t t0 = (size_t)td.tbase + td.t0, nt = td.t1 - td.t0;
     l2_prefetch(J.idx + 3 * t0, 12 * nt);
     l2_prefetch(J.centers + 3 * t0, 12 * nt);
-    if (td.vhi > td.vlo) l2_prefetch(P.vcull + td.vlo, 16ull * (td.vhi - td.vlo));
+    if (td.vhi > td.vlo) {
+        l2_prefetch(P.vcull + td.vlo, 16ull * (td.vhi - td.vlo));
+        // skinned parts take their depth keys from the skinned positions
+        if (td.flags & SEG_SKINNED) l2_prefetch(P.valt + td.vlo, 16ull * (td.vhi - td.vlo));
+    }
 }
 // P1: visibility and depth keys per tile; single-tile segments are sorted and
 // emitted right here, multi-tile segments leave their visible list in HBM.
@@ -1484,6 +1492,14 @@ __global__ void __launch_bounds__(256, T3D_MIN_BLOCKS) t3d_frame_kernel(const __
 
 // Launch entry used by the runtime (same translation-unit linkage).
 extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel; }
+// The keyed streams of one mesh (k_bake_shapes) on stream st.
+extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
+                                       const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
+                                       float4* ob) {
+    if (nverts == 0) return cudaSuccess;
+    t3d::k_bake_shapes<<<(nverts + 255) / 256, 256, 0, st>>>(va, vb, sa, sb, sw, nverts, nkeys, oa, ob);
+    return cudaGetLastError();
+}
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads) {
     const size_t tiles = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + 4ull * (block_threads / 32) * t3d::kBins +
                          10ull * tile_tris + 16;

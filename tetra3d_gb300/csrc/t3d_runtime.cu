@@ -25,6 +25,9 @@
 #include "t3d_runtime.h"
 
 extern "C" const void* t3d_frame_kernel_ptr();
+extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
+                                       const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
+                                       float4* ob);
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads);
 
 namespace t3d {
@@ -449,6 +452,22 @@ bool subdivide_mesh(const t3d_mesh_desc& me, const float* lev, uint32_t nlev, ui
     return true;
 }
 
+// The keyed streams of shape-keyed mesh m for its current weights, queued on the
+// context's stream (the caller synchronises before the next frame reads them).
+int bake_shapes(t3d_ctx* ctx, Scene* sc, uint32_t m) {
+    const SceneMesh& sm = sc->meshes[m];
+    const cudaError_t e =
+        t3d_bake_shapes(ctx->stream, (const float4*)sc->va.ptr + sm.vbase, (const float4*)sc->vb.ptr + sm.vbase,
+                        (const float4*)sc->shape_a.ptr + sm.shape_first, (const float2*)sc->shape_b.ptr + sm.shape_first,
+                        (const float*)sc->shape_w.ptr + sm.weight_first, sm.nverts, sm.nkeys,
+                        (float4*)sc->vaS.ptr + sm.sbase, (float4*)sc->vbS.ptr + sm.sbase);
+    if (e != cudaSuccess) {
+        set_err(ctx, "shape key bake: %s", cudaGetErrorString(e));
+        return T3D_E_CUDA;
+    }
+    return T3D_OK;
+}
+
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     if (!d || !out || (d->num_meshes && !d->meshes) || (d->num_models && !d->models) ||
         (d->num_lights && !d->lights) || (d->num_volume_cells && !d->volume_cells)) {
@@ -460,7 +479,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         return T3D_E_INVAL;
     }
     auto sc = std::make_unique<Scene>();
-    uint64_t nv = 0, nt = 0, nshape = 0, nkeys_total = 0;
+    uint64_t nv = 0, nt = 0, nshape = 0, nkeys_total = 0, nshaped = 0;
     bool any_skin = false, any_subdiv = false;
     // auto-subdivided meshes are expanded first; the rest of the upload reads eff[m]
     const uint32_t nlev = d->subdivision_levels ? d->num_subdivision_levels : 0u;
@@ -534,6 +553,8 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
             return T3D_E_INVAL;
         }
         sm.nkeys = me.num_shape_keys;
+        sm.sbase = (uint32_t)nshaped;
+        if (me.num_shape_keys) nshaped += me.num_vertices;
         sm.shape_first = (uint32_t)nshape;
         sm.weight_first = (uint32_t)nkeys_total;
         nshape += (uint64_t)me.num_shape_keys * me.num_vertices;
@@ -663,6 +684,8 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
         (rc = sc->cells.ensure(ctx, 16 * std::max<size_t>(1, d->num_volume_cells))) ||
         (rc = sc->shape_a.ensure(ctx, 16 * std::max<uint64_t>(1, nshape))) ||
         (rc = sc->shape_b.ensure(ctx, 8 * std::max<uint64_t>(1, nshape))) ||
+        (rc = sc->vaS.ensure(ctx, 16 * std::max<uint64_t>(1, nshaped))) ||
+        (rc = sc->vbS.ensure(ctx, 16 * std::max<uint64_t>(1, nshaped))) ||
         (rc = sc->shape_w.ensure(ctx, 4 * std::max<uint64_t>(1, nkeys_total))) ||
         (rc = sc->vjoint.ensure(ctx, (joint8 ? 4 : 16) * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
         (rc = sc->vweight.ensure(ctx, 16 * (any_skin ? std::max<uint64_t>(1, nv) : 1))) ||
@@ -811,10 +834,14 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     for (uint32_t m = 0; m < d->num_meshes; m++) {
         const SceneMesh& sm = sc->meshes[m];
         dm[m].vbase = sm.vbase; dm[m].tbase = sm.tbase; dm[m].nverts = sm.nverts; dm[m].ntris = sm.ntris;
-        dm[m].shape_first = sm.shape_first; dm[m].nkeys = sm.nkeys; dm[m].weight_first = sm.weight_first; dm[m].pad = 0;
+        dm[m].shape_first = sm.shape_first; dm[m].nkeys = sm.nkeys; dm[m].weight_first = sm.weight_first;
+        dm[m].sbase = sm.sbase;
         for (int k = 0; k < 3; k++) { dm[m].dmin[k] = sm.dmin[k]; dm[m].dmax[k] = sm.dmax[k]; }
     }
     if (d->num_meshes) CK(cudaMemcpy(sc->dmeshes.ptr, dm.data(), sizeof(DevMesh) * dm.size(), cudaMemcpyHostToDevice));
+    for (uint32_t m = 0; m < d->num_meshes; m++)
+        if (sc->meshes[m].nkeys && (rc = bake_shapes(ctx, sc.get(), m))) return rc;
+    if (nshaped) CK(cudaStreamSynchronize(ctx->stream));
     if (d->num_volume_cells)
         CK(cudaMemcpy(sc->cells.ptr, d->volume_cells, 16ull * d->num_volume_cells, cudaMemcpyHostToDevice));
     rc = scene_write_models(ctx, sc.get(), 0, d->models, d->num_models);
@@ -928,6 +955,8 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.cells = (const float*)sc->cells.ptr;
         dj.shape_a = (const float4*)sc->shape_a.ptr;
         dj.shape_b = (const float2*)sc->shape_b.ptr;
+        dj.vaS = (const float4*)sc->vaS.ptr;
+        dj.vbS = (const float4*)sc->vbS.ptr;
         dj.shape_w = (const float*)sc->shape_w.ptr;
         dj.vjoint = (const uint4*)sc->vjoint.ptr;
         dj.vjoint8 = sc->joint8 ? (const uint32_t*)sc->vjoint.ptr : nullptr;

@@ -39,6 +39,7 @@ struct SceneMesh {
     // per kChunkTris triangles: smallest and largest vertex index they use (prefetch ranges)
     std::vector<uint32_t> chunk_lo, chunk_hi;
     uint32_t nkeys = 0, shape_first = 0, weight_first = 0;  // shape keys
+    uint32_t sbase = 0;                                     // first vertex of the keyed streams
     bool skin = false;                                      // joints and weights present
     uint32_t max_joint = 0;
     bool subdiv = false;  // auto-subdivided: parts list each triangle followed by its subdivision levels
@@ -57,6 +58,7 @@ struct Scene {
     uint64_t struct_ver = 0, model_ver = 0;
     DevBuf va, vb, vc, idx, centers, dmeshes, dmodels, cells;
     DevBuf shape_a, shape_b, shape_w, vjoint, vweight, bones;
+    DevBuf vaS, vbS;  // keyed streams of the shape-keyed meshes (baked per weight set)
     bool joint8 = false;  // vjoint holds four 8-bit joints per vertex (every joint below 256)
     DevBuf sub_info, sub_rel, sub_levels, cell_use_off, cell_use_items;
     std::vector<char> light_uses;    // per light: a volume whose cells use lights
@@ -67,13 +69,13 @@ struct Scene {
     }
     uint32_t num_bones = 0, num_keys = 0, num_sub_levels = 0, num_cells = 0;
     uint64_t device_bytes() const {
-        return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap +
+        return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap + vaS.cap + vbS.cap +
                shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap + sub_info.cap + sub_rel.cap +
                sub_levels.cap + cell_use_off.cap + cell_use_items.cap;
     }
     void release() {
         sub_info.release(); sub_rel.release(); sub_levels.release(); cell_use_off.release(); cell_use_items.release();
-        shape_a.release(); shape_b.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
+        shape_a.release(); shape_b.release(); vaS.release(); vbS.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
         va.release(); vb.release(); vc.release(); idx.release(); centers.release();
         dmeshes.release(); dmodels.release(); cells.release();
     }
@@ -163,4 +165,5 @@ uint64_t next_version();
 int upload_frame(t3d_ctx* ctx, cudaStream_t st);
 int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st);
 int configure(t3d_ctx* ctx);
+int bake_shapes(t3d_ctx* ctx, Scene* sc, uint32_t mesh);
 }  // namespace t3d
