@@ -384,7 +384,8 @@ int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out);
 /* Bone influence matrices [first, first + n) of a scene (16 floats each, Node.boneInfluence,
  * node.go), as an animation player updates them every frame. */
 int t3d_scene_set_bones(t3d_ctx* ctx, uint32_t scene, uint32_t first, const float* influences, uint32_t n);
-/* Shape-key weights of one mesh of a scene (ShapeKey.weight, mesh.go). */
+/* Shape-key weights of one mesh of a scene (ShapeKey.weight, mesh.go). The mesh's keyed
+ * vertices (shared by all its models) are recomputed on the device before this returns. */
 int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, const float* weights, uint32_t n);
 /* Lights [first, first + n) of a scene: moved, recoloured, re-ranged or of another
  * kind, as Camera.Render reads them anew every frame (camera.go:1269-1300,
