@@ -372,7 +372,7 @@ __device__ __forceinline__ void count_step(const RasterJob& J, bool valid, const
 // uhits[u] of them, ufrags[u] fragments. A triangle whose box exceeds kBigBox pixels goes to
 // the shared list (k_big_count adds its count); when the list is full its warp counts it.
 // ctr[0] / ctr[1]: large triangles / chunks handed out.
-__global__ void __launch_bounds__(kFragThreads) k_frag_count(RasterJob J, uint32_t nunits, uint4* hits, uint32_t* uhits,
+__global__ void __launch_bounds__(kFragThreads, 4) k_frag_count(RasterJob J, uint32_t nunits, uint4* hits, uint32_t* uhits,
                                                              uint32_t* ufrags, BigTri* big, uint32_t* chunk_tri,
                                                              unsigned long long* ctr) {
     const uint32_t lane = threadIdx.x & 31, u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -413,7 +413,7 @@ __device__ __forceinline__ uint32_t shared_chunks(const unsigned long long* ctr)
 
 // Counts of the shared large triangles: the grid's warps take kBigChunk-pixel chunks in turn
 // and add each chunk's count to its triangle's hit and unit.
-__global__ void __launch_bounds__(kFragThreads) k_big_count(RasterJob J, const BigTri* __restrict__ big,
+__global__ void __launch_bounds__(kFragThreads, 5) k_big_count(RasterJob J, const BigTri* __restrict__ big,
                                                            const uint32_t* __restrict__ chunk_tri,
                                                            const unsigned long long* __restrict__ ctr, uint4* hits,
                                                            uint32_t* ufrags) {
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(kFragThreads) k_big_count(RasterJob J, const B
 // value = the hit's index, which names its triangle) from ufoff[u] on, in draw order, so the
 // stable sort by pixel keeps draw order per pixel. A shared large triangle only sets its
 // cursor; k_big_write fills its range.
-__global__ void __launch_bounds__(kFragThreads) k_frag_write(RasterJob J, uint32_t nunits, const uint4* __restrict__ hits,
+__global__ void __launch_bounds__(kFragThreads, 4) k_frag_write(RasterJob J, uint32_t nunits, const uint4* __restrict__ hits,
                                                              const uint32_t* __restrict__ uhits,
                                                              const uint32_t* __restrict__ ufoff, BigTri* big,
                                                              uint32_t* keys, uint32_t* vals) {
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kFragThreads) k_frag_write(RasterJob J, uint32
 // Fragments of the shared large triangles: the grid's warps take chunks in turn; a chunk
 // claims its part of the triangle's range with one atomic on the cursor. The order inside a
 // triangle's range does not matter: a triangle has at most one fragment per pixel.
-__global__ void __launch_bounds__(kFragThreads) k_big_write(RasterJob J, BigTri* big, const uint32_t* __restrict__ chunk_tri,
+__global__ void __launch_bounds__(kFragThreads, 5) k_big_write(RasterJob J, BigTri* big, const uint32_t* __restrict__ chunk_tri,
                                                            const unsigned long long* __restrict__ ctr, uint32_t* keys,
                                                            uint32_t* vals) {
     const uint32_t lane = threadIdx.x & 31, nch = shared_chunks(ctr);
@@ -688,7 +688,7 @@ __device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t slot, floa
 
 // One thread per pixel replays the pixel's fragments (sorted by pixel, draw order kept);
 // fvals[q] is the hit of fragment q's triangle: hits[fvals[q]] = (output slot, render pair, ...).
-__global__ void k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ fvals,
+__global__ void __launch_bounds__(256, 5) k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ fvals,
                          const uint4* __restrict__ hits, uint32_t* color, uint32_t* depth) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (uint32_t)(J.W * J.H)) return;
@@ -877,7 +877,7 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     }
     const uint32_t nunits = (uint32_t)std::max<uint64_t>(1, (span + kUnitTris - 1) / kUnitTris);
     const uint32_t fblocks = (nunits + kFragThreads / 32 - 1) / (kFragThreads / 32);
-    const uint32_t bigblocks = (uint32_t)std::max(1, ctx->num_sms) * 4;
+    const uint32_t bigblocks = (uint32_t)std::max(1, ctx->num_sms) * 5;  // 5 resident blocks of 256 per SM
     if ((rc = S.cbase.ensure(ctx, 4ull * (nseg + 1))) || (rc = S.hits.ensure(ctx, 16ull * kUnitTris * nunits)) ||
         (rc = S.uhits.ensure(ctx, 4ull * nunits)) || (rc = S.ufrags.ensure(ctx, 4ull * nunits)) ||
         (rc = S.ufoff.ensure(ctx, 4ull * nunits)) || (rc = S.big.ensure(ctx, sizeof(BigTri) * (size_t)kBigTriCap)) ||
