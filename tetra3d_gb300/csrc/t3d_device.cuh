@@ -46,7 +46,8 @@ enum : uint32_t {
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
-    SEG_ALTERED = SEG_SKINNED | SEG_BILLBOARD | SEG_SNAP | SEG_NESTED,
+    // billboards with DepthModeUnbillboarded need the altered loop; others only a staged MVP
+    SEG_ALTERED = SEG_SKINNED | SEG_UNBB | SEG_SNAP | SEG_NESTED,
 };
 constexpr uint32_t kLocalVerts = 65536;  // vertex range of a segment whose offsets fit uint16
 __host__ __device__ inline uint32_t seg_sort_mode(uint32_t f) { return (f >> 8) & 3u; }

@@ -473,7 +473,7 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
     const DevPrep& pr = P.preps[seg.inst];
     const DevInst& in = P.insts[seg.inst];
     float* mvpc = reinterpret_cast<float*>(ms.mvpc);
-    const bool bb = kSkin && (seg.flags & SEG_BILLBOARD);
+    const bool bb = seg.flags & SEG_BILLBOARD;  // either loop: a billboard only changes the MVP
     for (uint32_t k = threadIdx.x; k < 48; k += blockDim.x) {
         if (k < 16) {
             if (!bb) mvpc[4 * (k & 3) + (k >> 2)] = pr.mvp[k];
