@@ -405,14 +405,22 @@ def feature_frames(ctx, stream, sh, base_ms, frames=10, warmup=3):
             v1, _ = ctx.counters()
             vis = (v1 - v0) / frames
             st = ctx.sync()
+            # the oracle (the reference's algorithm restated on the CPU) on the same frame, all host threads
+            from oracle import pyoracle
+            threads = os.cpu_count() or 1
+            c0 = time.perf_counter()
+            cpu_vis = pyoracle.render(sd, sd.camera, threads=threads).visible_tris
+            cpu_s = time.perf_counter() - c0
             out[kind] = {"ms_per_frame": round(ms, 4), "visible_tris": int(vis), "tris_per_s": vis / (ms / 1e3),
                          "time_vs_plain_frame": round(ms / base_ms, 3),
+                         "cpu_baseline": {"value": cpu_vis / cpu_s, "unit": "tris/s", "cores": threads, "kind": "port",
+                                          "sample": "the whole frame (static transforms), 1 render"},
                          "phase_busy_us_last_frame": {k: round(float(v), 1) for k, v in zip(
                              ("prep", "vertex", "triangles", "hist", "scan", "rank_emit"), st.phase_busy)}}
         finally:
             ctx.release(sid)
     out["note"] = ("4096-model frame with the feature on every model, animated, CUDA graph replays; "
-                   "time_vs_plain_frame = ms / the plain frame's ms")
+                   "time_vs_plain_frame = ms / the plain frame's ms; cpu_baseline = the oracle on all host threads")
     return out
 
 
