@@ -309,7 +309,15 @@ def run_ours(args, rank, world, local_rank):
         # 108 B), the colour and depth images written once (8 B per pixel)
         rbytes = 108 * int(rst.visible_tris) + 8 * cam.width * cam.height
         rpeak, rpeak_kind = peaks()
-        raster = {"textured": bool(args.textured), "ms_per_frame": rms, "device_ms_per_frame": rdev, "image": f"{cam.width}x{cam.height}",
+        # the raster oracle (one host thread) on the same stream, downloaded
+        from oracle import pyoracle
+        fr = ctx.download(rst)
+        c0 = time.perf_counter()
+        pyoracle.raster(fr, sd, cam, textures=scenes.raster_textures() if args.textured else None)
+        rcpu = {"value": int(rst.visible_tris) / (time.perf_counter() - c0), "unit": "tris/s", "cores": 1, "kind": "port",
+                "sample": "the whole frame's stream, 1 rasterisation"}
+        del fr
+        raster = {"textured": bool(args.textured), "cpu_baseline": rcpu, "ms_per_frame": rms, "device_ms_per_frame": rdev, "image": f"{cam.width}x{cam.height}",
                   "visible_tris": int(rst.visible_tris), "tris_per_s": int(rst.visible_tris) / (rms / 1e3),
                   "covered_pixels": int((col[..., 3] > 0).sum()),
                   "roofline": {"bound": "hbm", "achieved": rbytes / (rdev / 1e3) / 1e9, "peak": rpeak, "unit": "GB/s",
