@@ -182,3 +182,34 @@ def test_alpha_clip_lets_a_far_pair_show_through_the_holes():
                            flush_tex=[(1, 4, (1, 1)), (0, 0, (1, 1))])
     assert np.all(c[0:4, 0] == [0, 255, 0, 255])  # the hole: the far pair passes the depth test
     assert np.array_equal(c[0:4, 1:4], t[:, 1:4])
+
+
+def test_bilinear_wraps_across_the_texture_edge():
+    """A sample point on the seam between the last and the first column mixes the two (GLSL mod
+    wrapping of both taps, rate = fract(p1)); nearest takes the texel containing the point."""
+    t = _tex(w=4, h=1, seed=6)
+    # a one-pixel-high strip: pixel centres at x + 0.5 map to u = x + 0.5 + 3.5, i.e. on the seams
+    f = _uv_frame(_quad(0, 0, 4, 1, 3.5, 0.5, 7.5, 0.5))
+    c, _ = pyoracle.raster(f, None, _cam(w=4, h=1), transparent=[0], textures=[t], flush_tex=[(1, 1, (1, 1))])
+    row = t[0].astype(np.float64)
+    for x in range(4):
+        want = (row[(x + 3) % 4] + row[x % 4]) / 2.0
+        assert np.abs(c[0, x].astype(np.float64) - want).max() <= 1.0, x
+    c, _ = pyoracle.raster(f, None, _cam(w=4, h=1), transparent=[0], textures=[t], flush_tex=[(1, 0, (1, 1))])
+    assert np.array_equal(c[0], t[0, [0, 1, 2, 3]])
+
+
+def test_negative_coordinates_wrap_with_mod():
+    """u = -0.5 lands in the last texel (mod, not remainder)."""
+    t = _tex(w=4, h=4, seed=7)
+    f = _uv_frame(_quad(0, 0, 4, 4, -4, -4, 0, 0))
+    c, _ = pyoracle.raster(f, None, _cam(), transparent=[0], textures=[t], flush_tex=[(1, 0, (1, 1))])
+    assert np.array_equal(c[0:4, 0:4], t)
+
+
+def test_screen_mapping_scales_the_pixel_position():
+    """TextureMapMode 1 with multipliers (0.5, 0.5): two pixels per texel in each direction."""
+    t = _tex(w=4, h=4, seed=8)
+    f = _uv_frame(_quad(0, 0, 8, 8, 0, 0, 0, 0))
+    c, _ = pyoracle.raster(f, None, _cam(), transparent=[0], textures=[t], flush_tex=[(1, 2, (0.5, 0.5))])
+    assert np.array_equal(c[0:8, 0:8], np.repeat(np.repeat(t, 2, axis=0), 2, axis=1))
