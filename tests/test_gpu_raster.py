@@ -74,6 +74,14 @@ def test_raster_second_job(ctx):
 
 # ---- textures and alpha clip: base3d.kage's filters and mappings, the clip-alpha shader ----
 
+def _tiled_uvs(sd, lo=-1.0, hi=2.0):
+    """Mesh UVs spread over [lo, hi]: negative and past-the-edge texture coordinates that the
+    samplers wrap (mod in the colour pass, fract in the clip-alpha pass)."""
+    for m in sd.meshes:
+        m.uvs = np.ascontiguousarray(m.uvs * np.float32(hi - lo) + np.float32(lo), np.float32)
+    return sd
+
+
 TEX_CASES = [
     ("textured_persp", lambda: (scenes.textured_scene(21), scenes.feature_camera("persp")), {}),
     ("textured_tilted", lambda: (scenes.textured_scene(22), scenes.feature_camera("tilted")), {}),
@@ -82,6 +90,7 @@ TEX_CASES = [
     ("textured_no_depth", lambda: (scenes.textured_scene(25), scenes.feature_camera("fog_add")), {}),
     ("textured_batches", lambda: (scenes.texture_materials(scenes.batch_scene(12), 12), scenes.feature_camera("persp")),
      {}),
+    ("textured_tiled_uvs", lambda: (_tiled_uvs(scenes.textured_scene(26)), scenes.feature_camera("tilted")), {}),
 ]
 
 
