@@ -213,3 +213,15 @@ def test_screen_mapping_scales_the_pixel_position():
     f = _uv_frame(_quad(0, 0, 8, 8, 0, 0, 0, 0))
     c, _ = pyoracle.raster(f, None, _cam(), transparent=[0], textures=[t], flush_tex=[(1, 2, (0.5, 0.5))])
     assert np.array_equal(c[0:8, 0:8], np.repeat(np.repeat(t, 2, axis=0), 2, axis=1))
+
+
+def test_alpha_clip_on_a_transparent_flush_writes_no_depth():
+    """A transparent flush with alpha clip: the clipped texels still gate its colour pass, but
+    its depth intermediate is not composited into the depth texture."""
+    alpha = np.full((4, 4), 255, np.uint8)
+    alpha[:, :2] = 0
+    t = _tex(alpha=alpha, seed=9)
+    f = _uv_frame(_quad(0, 0, 4, 4, 0, 0, 4, 4))
+    c, d = pyoracle.raster(f, None, _cam(), transparent=[1], textures=[t], flush_tex=[(1, 4, (1, 1))])
+    assert d.max() == 0
+    assert c[0:4, 0:2].max() == 0 and np.array_equal(c[0:4, 2:4], t[:, 2:4])
