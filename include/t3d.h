@@ -519,7 +519,9 @@ typedef struct t3d_noalloc_args {
     const float*          uvs;
     const float*          colors;
     const uint32_t*       indices;       /* 3 * num_triangles, mesh-absolute */
-    const float*          volume_cells;  /* device RGBA cells for volume lights, or NULL */
+    const float*          volume_cells;  /* device RGBA cells for volume lights, or NULL; the lights a
+                                            cell uses (t3d_scene_desc.cell_use_*) are not carried
+                                            here, so cells light with their own colour only */
     /* outputs in device memory, room for tri_count triangles */
     float*                out_xyuv;      /* 3 * 4 floats per triangle */
     float*                out_rgba;      /* 3 * 4 floats per triangle */

@@ -118,3 +118,40 @@ def test_noalloc_rejects_oversize(ctx):
     rc = ctx.lib.t3d_render_part_noalloc(0, C.byref(a), None)
     assert rc == abi.T3D_E_INVAL
     assert b"no-alloc limits" in a.error
+
+
+def test_noalloc_reports_empty_mesh_and_part_outside(ctx):
+    sd = scenes.uv_sphere_scene(5)
+    for nv, nt, start, cnt, want in ((0, 10, 0, 10, b"empty mesh"), (100, 10, 8, 5, b"outside")):
+        a = abi.NoallocArgs()
+        a.model = C.pointer(sd.models[0])
+        a.camera = C.pointer(sd.camera)
+        a.positions = a.normals = a.uvs = a.indices = 1  # rejected before any device work
+        a.out_xyuv = a.out_rgba = a.out_depth = a.out_count = 1
+        a.num_vertices, a.num_triangles, a.tri_start, a.tri_count = nv, nt, start, cnt
+        assert ctx.lib.t3d_render_part_noalloc(0, C.byref(a), None) == abi.T3D_E_INVAL
+        assert want in a.error, a.error
+
+
+def test_context_with_larger_tiles_renders_after_noalloc_calls(ctx):
+    """The frame kernel's shared-memory limit is one attribute for the whole process: a
+    context tuned for 4096-triangle tiles (more shared memory than the allocation-free
+    entry uses) still launches after allocation-free calls."""
+    torch = pytest.importorskip("torch")
+    sd = _grid_scene(8)
+    _noalloc(ctx.lib, sd, torch)
+    ctx.set_tuning(tile_tris=4096)
+    try:
+        sid = ctx.upload(sd)
+        try:
+            ctx.render(sid, sd.camera)
+            ref = ctx.download()
+            _noalloc(ctx.lib, sd, torch)
+            ctx.render(sid, sd.camera)
+            got = ctx.download()
+        finally:
+            ctx.release(sid)
+        assert got.visible_tris == ref.visible_tris > 0
+        assert np.array_equal(bits(got.xyuv), bits(ref.xyuv))
+    finally:
+        ctx.set_tuning(tile_tris=2048)

@@ -27,7 +27,7 @@ namespace t3d {
 int configure(t3d_ctx* ctx) {
     ctx->smem_bytes = t3d_frame_smem_bytes(ctx->tile_tris, ctx->block_threads);
     const void* fn = t3d_frame_kernel_ptr();
-    CKR(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
+    CKR(raise_smem_limit(fn, ctx->smem_bytes));
     int per_sm = 0;
     CKR(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)ctx->block_threads, ctx->smem_bytes));
     if (per_sm < 1) {

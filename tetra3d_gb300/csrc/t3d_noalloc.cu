@@ -154,7 +154,7 @@ static int na_setup(int device, t3d_noalloc_args* a) {
     }
     d.smem = t3d_frame_smem_bytes(kNaTile, kNaBlock);
     const void* fn = t3d_frame_kernel_ptr();
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem)) != cudaSuccess) {
+    if ((e = raise_smem_limit(fn, d.smem)) != cudaSuccess) {
         fail(a, "kernel attribute: %s", cudaGetErrorString(e));
         return T3D_E_CUDA;
     }
@@ -199,11 +199,19 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
         fail(a, "null argument%s");
         return T3D_E_INVAL;
     }
-    if (a->num_vertices == 0 || a->num_vertices > kNaMaxV || a->num_triangles > kNaMaxT ||
-        (uint64_t)a->tri_start + a->tri_count > a->num_triangles || a->num_lights > kNaMaxL) {
+    if (a->num_vertices == 0) {
+        fail(a, "empty mesh: num_vertices is 0%s");
+        return T3D_E_INVAL;
+    }
+    if (a->num_vertices > kNaMaxV || a->num_triangles > kNaMaxT || a->num_lights > kNaMaxL) {
         snprintf(a->error, sizeof a->error,
                  "size beyond the no-alloc limits: %u vertices (max %u), %u triangles (max %u), %u lights (max %u)",
                  a->num_vertices, kNaMaxV, a->num_triangles, kNaMaxT, a->num_lights, kNaMaxL);
+        return T3D_E_INVAL;
+    }
+    if ((uint64_t)a->tri_start + a->tri_count > a->num_triangles) {
+        snprintf(a->error, sizeof a->error, "part [%u, %u + %u) lies outside the mesh's %u triangles", a->tri_start,
+                 a->tri_start, a->tri_count, a->num_triangles);
         return T3D_E_INVAL;
     }
     if (a->camera->width <= 0 || a->camera->height <= 0) {
@@ -220,6 +228,12 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
         return T3D_E_INVAL;
     }
     std::lock_guard<std::mutex> guard(g_mu);
+    // the caller's current device is restored on every return
+    struct DeviceGuard {
+        int prev = -1;
+        ~DeviceGuard() { if (prev >= 0) cudaSetDevice(prev); }
+    } dev_guard;
+    NA_CK(cudaGetDevice(&dev_guard.prev));
     NA_CK(cudaSetDevice(device));
     int rc = na_setup(device, a);
     if (rc) return rc;
@@ -387,7 +401,7 @@ extern "C" int t3d_render_part_noalloc(int device, t3d_noalloc_args* a, void* st
     P.has_multi = ntiles > 1 ? 1u : 0u;
 
     const void* fn = t3d_frame_kernel_ptr();
-    NA_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
+    NA_CK(raise_smem_limit(fn, d.smem));  // never lowers what a context configured
     uint32_t grid = std::max(1u, std::min(d.max_grid, std::max(ntiles, nchunks)));
     void* args[] = {&P};
     cudaLaunchConfig_t cfg;

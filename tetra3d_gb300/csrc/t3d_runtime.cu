@@ -33,6 +33,20 @@ extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_thread
 namespace t3d {
 
 // ------------------------------------------------------------ utilities ----
+// A kernel's dynamic shared-memory limit is one process-wide attribute shared by
+// every context and the allocation-free entry: it is only ever raised, so a
+// launch configured for more shared memory never fails after another caller
+// configured less.
+cudaError_t raise_smem_limit(const void* fn, size_t bytes) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> g(mu);
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+    if (e != cudaSuccess) return e;
+    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 void set_err(t3d_ctx* c, const char* fmt, ...) {
     if (!c) return;
     char buf[512];

@@ -155,6 +155,7 @@ struct t3d_ctx {
 
 namespace t3d {
 void set_err(t3d_ctx* c, const char* fmt, ...);
+cudaError_t raise_smem_limit(const void* fn, size_t bytes);
 void build_camera(const t3d_camera_desc& d, JobCam& c);
 void build_light(const t3d_light_desc& d, DevLight& L);
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out);
