@@ -365,6 +365,20 @@ const char* t3d_last_error(const t3d_ctx* ctx);
  * 256..4096), vertices per vertex-phase work item (32..2^20), threads per block
  * (128 or 256). */
 int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint32_t block_threads);
+/* Route of the vertex stage (no reference counterpart: the reference has one CPU
+ * path). enable = 1 (the default): render pairs that need nothing beyond the plain
+ * vertex loop (no skinning, shape keys, auto-subdivision, vertex snapping, lights
+ * used by volume cells or unbillboarded depth) read their part's meshlets -- runs of
+ * consecutive triangles with their distinct vertices stored contiguously, cut at
+ * scene upload -- and keep every per-vertex intermediate in shared memory.
+ * enable = 0: every pair writes and reads per-vertex records in device memory. The
+ * emitted stream is the same bit for bit either way. */
+int         t3d_set_meshlets(t3d_ctx* ctx, int enable);
+/* Bounded device waits (grid barriers, bulk-copy waits): polls before the frame
+ * gives up and t3d_frame_sync returns T3D_E_TIMEOUT (0 = the default, seconds).
+ * Meant for tests of the timeout path; the context stays usable and the next
+ * frame with the default renders normally. */
+int         t3d_set_wait_limit(t3d_ctx* ctx, uint32_t polls);
 
 /* ---- resident scenes --------------------------------------------------------- */
 /* Uploads meshes, models and lights to the device. Replaces Tetra3D's

@@ -187,6 +187,43 @@ def test_serving_same_bits_alone_and_in_mix(ctx):
             ctx.release(s)
 
 
+def test_serving_scenes_match_oracle_alone_and_in_mix(ctx):
+    """The serving workload's own scenes (sphere, 1000 and 250 cubes, 256^2 / 512^2 / 1024^2
+    terrains, the 48-model batched scene), random cameras on the 10-100 sphere at the three
+    resolutions and random light subsets: every request's stream alone and in the mix equals
+    the oracle's."""
+    from tetra3d_gb300 import serving
+    sds, centres = serving.serving_scenes(n=8)
+    sids = [ctx.upload(sd) for sd in sds]
+    rng = np.random.Generator(np.random.PCG64(77))
+    reqs = []
+    for rid in range(16):
+        s = rid % 8
+        reqs.append((rid, s, serving.random_camera(rng, centres[s]), serving.random_light_mask(rng, sds[s].nlights)))
+    assert {(c.width, c.height) for _, _, c, _ in reqs} == set(serving.RESOLUTIONS)
+    srv = Server(ctx, hbm_budget_bytes=32 << 30, max_batch=8, streams=2, verify=True)
+    try:
+        alone = {}
+        for rid, s, cam, mask in reqs:
+            assert srv.submit(job(sids[s], cam, mask), rid) == abi.T3D_OK
+            c = _drain(srv, 1)[rid]
+            assert c.status == abi.T3D_OK
+            alone[rid] = (c.checksum, c.visible_tris)
+        for rid, s, cam, mask in reqs:
+            assert srv.submit(job(sids[s], cam, mask), 100 + rid) == abi.T3D_OK
+        mix = _drain(srv, len(reqs))
+        for rid, s, cam, mask in reqs:
+            c = mix[100 + rid]
+            assert c.status == abi.T3D_OK
+            assert (c.checksum, c.visible_tris) == alone[rid], f"request {rid} differs in the mix"
+            ref = pyoracle.render(sds[s], cam, light_mask=mask, threads=8)
+            assert alone[rid] == (_fnv_frame(ref), ref.visible_tris), f"request {rid} (scene {s}) differs from the oracle"
+    finally:
+        srv.close()
+        for sid in sids:
+            ctx.release(sid)
+
+
 def test_serving_admission(ctx):
     sd = scenes.small_variant("batched", 14)
     sid = ctx.upload(sd)

@@ -1,11 +1,17 @@
-"""Full-size workloads on the GPU, checked through size-independent properties:
+"""Full-size workloads on the GPU against the oracle and through size-independent
+properties:
 
+- the whole 4096-model frame (69.7 M triangles), static and after three animated
+  graph replays, bit for bit against the oracle on all host threads;
 - render pairs are independent, so the oracle on a sample of the models (every
-  k-th) must reproduce, bit for bit, those models' pairs inside the full frame;
-- the plain form (one launch per pair) and the batched form give identical bits;
+  k-th) reproduces those models' pairs inside the full frame;
+- the plain form (one launch per pair) and the batched form give identical bits,
+  and so do the meshlet and per-vertex record routes;
 - a static frame rendered twice gives identical bits (idempotence);
 - visible counts add up (segments vs stats vs device counters).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -84,6 +90,34 @@ def test_batched_4096_models_animated_graph(ctx):
         got = ctx.download()
         _check_sample(got, sd, sd.camera, stride=64, animate_frames=3)
     finally:
+        ctx.release(sid)
+
+
+def test_batched_4096_models_whole_frame_matches_oracle(ctx):
+    """The benchmarked frame itself, every triangle of every pair: static, then after three
+    animated graph replays; and the per-vertex record route gives the same bits."""
+    sd = scenes.batched_scene(4)
+    threads = os.cpu_count() or 8
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, sd.camera, mode=abi.MODE_BATCHED)
+        got = ctx.download()
+        ref = pyoracle.render(sd, sd.camera, threads=threads)
+        assert_frames_equal(got, ref, "4096 models, static")
+        del ref
+        ctx.set_meshlets(0)
+        ctx.render(sid, sd.camera, mode=abi.MODE_BATCHED)
+        rec = ctx.download()
+        assert_frames_equal(rec, got, "record route vs meshlet route")
+        del rec, got
+        ctx.set_meshlets(1)
+        ctx.graph_capture(sid, sd.camera, animate=True)
+        ctx.graph_replay(3)
+        got = ctx.download()
+        assert_frames_equal(got, pyoracle.render(sd, sd.camera, animate_frames=3, threads=threads),
+                            "4096 models, 3 animated replays")
+    finally:
+        ctx.set_meshlets(1)
         ctx.release(sid)
 
 

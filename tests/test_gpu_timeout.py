@@ -1,0 +1,36 @@
+"""Failure detection without a GPU fault: every wait inside the frame kernel (the
+software grid barrier between phases and the bulk-copy waits of meshlet tiles) is
+bounded. A test limit of a few polls makes the waits give up on a frame that runs
+many blocks; the kernel records the timeout and every block leaves, the host
+reports T3D_E_TIMEOUT with a message, and the context stays usable: the next frame,
+with the default limit, is bit-identical to the oracle. Nothing faults, traps or
+hangs."""
+import pytest
+
+from tetra3d_gb300 import abi, scenes
+from oracle import pyoracle
+from tests.parity import assert_frames_equal
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("meshlets", [1, 0])
+@pytest.mark.parametrize("mode", [abi.MODE_BATCHED, abi.MODE_PLAIN])
+def test_bounded_waits_give_up_and_the_next_frame_renders(ctx, meshlets, mode):
+    sd = scenes.small_variant("batched", 21)
+    ctx.set_meshlets(meshlets)
+    sid = ctx.upload(sd)
+    try:
+        ctx.set_wait_limit(2)
+        ctx.render(sid, sd.camera, mode=mode)
+        with pytest.raises(abi.T3DError) as e:
+            ctx.sync()
+        assert e.value.code == abi.T3D_E_TIMEOUT
+        assert "error" in str(e.value)
+        ctx.set_wait_limit(0)
+        ctx.render(sid, sd.camera, mode=mode)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), f"after timeout, meshlets={meshlets}")
+    finally:
+        ctx.set_wait_limit(0)
+        ctx.set_meshlets(1)
+        ctx.release(sid)

@@ -10,7 +10,9 @@
 #include "t3d_runtime.h"
 
 extern "C" const void* t3d_frame_kernel_ptr();
+extern "C" const void* t3d_frame_kernel_mesh_ptr();
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads);
+extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_threads, uint32_t mesh_ucap);
 
 using namespace t3d;
 
@@ -35,6 +37,31 @@ int configure(t3d_ctx* ctx) {
         return T3D_E_INVAL;
     }
     ctx->max_grid = (uint32_t)(per_sm * ctx->num_sms);
+    // the meshlet kernel runs two blocks per SM (its register budget); its slot budget per
+    // meshlet is the largest (a multiple of 32) that the shared memory of two blocks holds
+    ctx->mesh_ucap = 0;
+    ctx->smem_mesh = 0;
+    ctx->max_grid_mesh = 0;
+    int sm_bytes = 0, reserved = 0, block_max = 0;
+    CKR(cudaDeviceGetAttribute(&sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+    CKR(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, ctx->device));
+    CKR(cudaDeviceGetAttribute(&block_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    const size_t budget = std::min<size_t>((size_t)block_max, (size_t)(sm_bytes / 2 - reserved));
+    uint32_t U = std::min<uint32_t>(3 * ctx->tile_tris, 65504u) & ~31u;
+    while (U >= 64 && t3d_frame_smem_bytes_mesh(ctx->tile_tris, ctx->block_threads, U) > budget) U -= 32;
+    if (U >= 64) {
+        const size_t smem = t3d_frame_smem_bytes_mesh(ctx->tile_tris, ctx->block_threads, U);
+        const void* fm = t3d_frame_kernel_mesh_ptr();
+        int per = 0;
+        if (raise_smem_limit(fm, smem) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fm, (int)ctx->block_threads, smem) == cudaSuccess &&
+            per >= 1) {
+            ctx->mesh_ucap = U;
+            ctx->smem_mesh = smem;
+            ctx->max_grid_mesh = (uint32_t)(per * ctx->num_sms);
+        }
+        cudaGetLastError();
+    }
     return T3D_OK;
 }
 }  // namespace t3d
@@ -94,7 +121,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     ctx->scenes.clear();
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
-                      &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum})
+                      &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights})
         b->release();
     ctx->table_host.release();
     ctx->readback.release();
@@ -134,6 +161,28 @@ int t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint
     }
     drop_graph(ctx);
     ctx->frame_valid = false;
+    return T3D_OK;
+}
+
+int t3d_set_meshlets(t3d_ctx* ctx, int enable) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    ctx->use_meshlets = enable != 0;
+    ctx->tables_ok = false;
+    drop_graph(ctx);
+    ctx->frame_valid = false;
+    return T3D_OK;
+}
+
+int t3d_set_wait_limit(t3d_ctx* ctx, uint32_t polls) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    ctx->spin_limit = polls;
+    ctx->params.spin_limit = polls;
+    ctx->tables_ok = false;  // the limit travels in the launch parameters
+    drop_graph(ctx);
     return T3D_OK;
 }
 
@@ -414,7 +463,8 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.launches = ctx->launches;
     size_t scratch = 0;
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
-                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count})
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count,
+                      &ctx->inst_lights})
         scratch += b->cap;
     s.scratch_bytes = scratch;
     s.h2d_bytes = ctx->last_h2d;

@@ -43,6 +43,7 @@ enum : uint32_t {
     SEG_SUBDIV = 1u << 22,      // auto-subdivided mesh: triangles are candidates of a subdivision level
     SEG_SNAP = 1u << 23,        // Camera.VertexSnapping > 0
     SEG_NESTED = 1u << 24,      // a light volume of the pair's list has cells that use lights
+    SEG_MESHLET = 1u << 25,     // tiles are meshlets: contiguous vertex blocks with 16-bit local indices
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
@@ -140,6 +141,27 @@ struct DevJob {
     const uint32_t* cell_use_items;  // light indices of the job's light table
 };
 
+// Meshlet tiles (SEG_MESHLET). At upload every mesh part is cut into runs of
+// consecutive triangles with at most tile_tris triangles and at most mesh_ucap
+// distinct vertices; each run is stored once, contiguous and 16-byte aligned:
+//   lidx  uint16 x 3 per triangle: slots of its corners in the run's vertex list
+//         (padded to 16 bytes)
+//   pos   float x 3 per slot (px, py, pz), slots padded to a multiple of 4 (the
+//         triangle phase copies lidx + pos)
+//   aos   per slot (px, py, pz, nx, ny, nz, u, v) and, when the mesh has colours,
+//         (r, g, b, a): 32 or 48 bytes (the rank phase copies this block)
+// A meshlet tile's TileDesc keeps t0/t1 (mesh-absolute triangles), the slot count
+// in `vmin`, the run's offset in 16-byte units in `vlo` and its device address in
+// `vhi` (low) / `pad1` (high). Only the vertex numbering changes: every emitted
+// value depends on vertex values alone, so the output is the same as through
+// mesh-absolute indices.
+__host__ __device__ inline uint32_t mlet_slots4(uint32_t nu) { return (nu + 3u) & ~3u; }
+__host__ __device__ inline uint32_t mlet_lidx_bytes(uint32_t nt) { return (6u * nt + 15u) & ~15u; }
+__host__ __device__ inline uint32_t mlet_aos_stride(bool colors) { return colors ? 48u : 32u; }
+__host__ __device__ inline uint64_t mlet_bytes(uint32_t nt, uint32_t nu, bool colors) {
+    return (uint64_t)mlet_lidx_bytes(nt) + (12ull + mlet_aos_stride(colors)) * mlet_slots4(nu);
+}
+
 // One (job, model) pair.
 struct DevInst {
     uint32_t job, model;
@@ -158,7 +180,8 @@ struct DevPrep {
     float inv_r[16];    // Decompose(Inverted(M)): rotation rows 0..3 (cols 0..2) and p * (1/s) in column 3
     float maxspan;      // Mesh.Dimensions.MaxSpan()
     uint32_t culled;
-    uint32_t pad[2];
+    uint32_t nl;        // lights staged for the instance in FrameParams.inst_lights (meshlet frames)
+    uint32_t pad;
 };
 
 // One render pair (model, mesh part) of one job.
@@ -194,7 +217,7 @@ constexpr uint32_t kChunkTris = 256;    // triangles per entry of a mesh's verte
 struct Ctl {
     uint32_t bar_count;
     uint32_t bar_gen;
-    uint32_t queue[8];
+    uint32_t queue[12];
     int32_t err;
     uint32_t err_info;
     unsigned long long bytes;       // algorithmic bytes of surviving models
@@ -204,7 +227,7 @@ struct Ctl {
     unsigned long long busy[8];     // sum over blocks of the time spent inside phase k (ns)
 };
 
-enum : int32_t { ERR_NONE = 0, ERR_BARRIER_TIMEOUT = 1, ERR_BAD_INDEX = 2, ERR_LIGHTS = 3 };
+enum : int32_t { ERR_NONE = 0, ERR_BARRIER_TIMEOUT = 1, ERR_BAD_INDEX = 2, ERR_LIGHTS = 3, ERR_COPY_TIMEOUT = 4 };
 
 struct FrameParams {
     const DevJob* jobs;
@@ -250,7 +273,18 @@ struct FrameParams {
     uint32_t tile_tris;           // triangles per tile
     uint32_t vchunk;              // vertices per vertex work item
     uint32_t has_multi;           // any multi-tile segment in range
+    uint32_t mesh_ucap;           // largest slot count of a meshlet tile
+    // meshlet tiles (SEG_MESHLET): tiles [mesh_begin, mesh_end), their multi-tile
+    // numbers [mt_mesh_begin, mt_mesh_end); zero ranges when the frame has none
+    uint32_t mesh_begin, mesh_end;
+    uint32_t mt_mesh_begin, mt_mesh_end;
+    uint32_t spin_limit;          // bounded waits: polls before giving up (0 = the default)
     uint32_t pad;
+    // meshlet frames: per instance, kMaxLights records of 56 bytes (the light list
+    // the vertex loop reads, staged once by the prep phase); null otherwise
+    float4* inst_lights;
 };
+// Dense visible list of a meshlet tile i: depth keys at vis_depth + i * tile_tris,
+// 3 slots per entry at vis_vloc + 3 * i * tile_tris, tile_count[i] entries.
 
 }  // namespace t3d

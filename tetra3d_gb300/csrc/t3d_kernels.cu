@@ -27,7 +27,8 @@ __device__ __forceinline__ int32_t vload(const int32_t* p) { return *(const vola
 
 // Sense-by-generation grid barrier with a bounded wait. On timeout it records
 // ERR_BARRIER_TIMEOUT; every block then leaves the kernel at its next barrier.
-__device__ bool grid_barrier(Ctl* ctl) {
+__device__ __forceinline__ uint32_t spin_limit(const FrameParams& P) { return P.spin_limit ? P.spin_limit : kSpinLimit; }
+__device__ bool grid_barrier(Ctl* ctl, uint32_t limit) {
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -42,7 +43,7 @@ __device__ bool grid_barrier(Ctl* ctl) {
             uint32_t spins = 0;
             while (vload(&ctl->bar_gen) == gen) {
                 if (vload(&ctl->err) != 0) break;
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     atomicCAS(&ctl->err, 0, ERR_BARRIER_TIMEOUT);
                     break;
                 }
@@ -53,6 +54,44 @@ __device__ bool grid_barrier(Ctl* ctl) {
     }
     __syncthreads();
     return vload(&ctl->err) == 0;
+}
+
+// ---- bulk copies into shared memory (cp.async.bulk completing on an mbarrier) ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// orders this thread's earlier shared-memory accesses before later bulk copies into the same bytes
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+// global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(smem_u32(b)), "r"(parity) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void mbar_inval(unsigned long long* b) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Waits for phase `parity` of barrier b with a bounded number of polls. On
+// timeout it records ERR_COPY_TIMEOUT and waits once more, with the default
+// bound, for the copy in flight, so that no copy lands in shared memory after
+// the block has moved on.
+__device__ __noinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, Ctl* ctl, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++)
+        if (mbar_try_wait(b, parity)) return true;
+    atomicCAS(&ctl->err, 0, ERR_COPY_TIMEOUT);
+    for (uint32_t i = 0; i < kSpinLimit; i++)
+        if (mbar_try_wait(b, parity)) break;
+    return false;
 }
 
 // Loads of per-vertex records. The records are written only in the vertex
@@ -141,6 +180,50 @@ __device__ bool model_in_frustum(const JobCam& c, const m4& M, const DevMesh& me
     return true;
 }
 
+// One light of the model's list as the emit loop reads it (56 bytes).
+// x, y, z: point = model-space workingPosition, ambient = result,
+// directional = workingForward. Volume geometry is read from `vol`.
+struct SLight {
+    int32_t type, skip;
+    float cr, cg, cb, energy, range, range2;
+    float x, y, z;
+    const DevLight* vol;
+};
+static_assert(sizeof(SLight) == 56, "staged light records are 56 bytes");
+// Bytes of a bulk copy of n staged lights (rounded up to 16; the regions hold kMaxLights records).
+__device__ __forceinline__ uint32_t slight_copy_bytes(uint32_t n) { return (56u * n + 15u) & ~15u; }
+
+// Model.ProcessVertices' light set-up for one light of an unskinned model as the
+// vertex loop reads it: ILight.beginModel (light.go:175-189, :326-330) and the
+// model-level point-light range skip (camera.go:1625-1629). r = the model's
+// Decompose(Inverted(M)) rows, M its transform, maxspan Mesh.Dimensions.MaxSpan.
+// (stage_model does the same per work item for the record path.)
+__device__ __forceinline__ SLight light_for_model(const DevLight& L, const float* r, const float* M, float maxspan) {
+    float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (L.type == T3D_LIGHT_POINT) {
+        const f3 lp = mk3(L.wpos[0], L.wpos[1], L.wpos[2]);
+        // Decompose(Inverted(M)): r.MultVec(lp) + p * (1/s)
+        const f3 q = mk3(r[0] * lp.x + r[4] * lp.y + r[8] * lp.z + r[12], r[1] * lp.x + r[5] * lp.y + r[9] * lp.z + r[13],
+                         r[2] * lp.x + r[6] * lp.y + r[10] * lp.z + r[14]);
+        w.x = q.x + r[3]; w.y = q.y + r[7]; w.z = q.z + r[11];
+        if (L.range > 0.0f) {
+            const float dist = maxspan + L.range;
+            if (dist2(mk3(M[12], M[13], M[14]), lp) > dist * dist) w.w = 1.0f;
+        }
+    }
+    SLight d;
+    d.type = L.type;
+    d.skip = (L.type == T3D_LIGHT_POINT && w.w != 0.0f) ? 1 : 0;
+    d.cr = L.color[0]; d.cg = L.color[1]; d.cb = L.color[2];
+    d.energy = L.energy; d.range = L.range; d.range2 = L.range2;
+    if (L.type == T3D_LIGHT_POINT) { d.x = w.x; d.y = w.y; d.z = w.z; }
+    else if (L.type == T3D_LIGHT_AMBIENT) { d.x = L.amb[0]; d.y = L.amb[1]; d.z = L.amb[2]; }
+    else { d.x = L.fwd[0]; d.y = L.fwd[1]; d.z = L.fwd[2]; }
+    d.vol = &L;
+    return d;
+}
+
+template <bool kM>
 __device__ __noinline__ void phase_prep(const FrameParams& P) {
     const uint32_t n = P.inst_end - P.inst_begin;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -196,6 +279,17 @@ __device__ __noinline__ void phase_prep(const FrameParams& P) {
         }
         // Mesh.Dimensions.MaxSpan for the model-level point-light skip (camera.go:1625-1629)
         pr.maxspan = mag3(mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]));
+        // meshlet frames: the model's light list as its render pairs' vertex loops read it, once
+        if (kM && P.inst_lights && !culled && !skinned) {
+            SLight* out = reinterpret_cast<SLight*>(P.inst_lights) + (size_t)i * kMaxLights;
+            const uint32_t nl = min(in.light_cnt, (uint32_t)kMaxLights);
+            uint32_t o = 0;
+            for (uint32_t k = 0; k < nl; k++) {
+                const SLight d = light_for_model(J.lights[P.inst_light_idx[in.light_off + k]], pr.inv_r, pr.M, pr.maxspan);
+                if (!d.skip) out[o++] = d;
+            }
+            pr.nl = o;
+        }
     }
     const uint32_t ns = P.seg_end - P.seg_begin;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += stride) {
@@ -205,17 +299,6 @@ __device__ __noinline__ void phase_prep(const FrameParams& P) {
         P.seg_count[s] = 0u;
     }
 }
-
-// ------------------------------------------------------------------ P1 ----
-// One light of the model's list as the emit loop reads it (48 bytes).
-// x, y, z: point = model-space workingPosition, ambient = result,
-// directional = workingForward. Volume geometry is read from `vol`.
-struct SLight {
-    int32_t type, skip;
-    float cr, cg, cb, energy, range, range2;
-    float x, y, z;
-    const DevLight* vol;
-};
 
 // LightVolume.convertToXYZIndices + getLightCell (light.go:717-741, :1267-1272)
 __device__ __forceinline__ int lv_index(float v) {
@@ -468,10 +551,10 @@ __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t 
 // Stages the model's matrices and (if lit) its light list in shared memory;
 // each thread runs ILight.beginModel for one light (light.go:175-189) and the
 // model-level point-range skip (camera.go:1625-1629).
+// The per-pair constants of the vertex loop: MVP columns (billboarded when the
+// material says so), model matrix, directional-light rotation and the emit constants.
 template <bool kSkin>
-__device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJob& J, ModelSmem& ms) {
-    const DevPrep& pr = P.preps[seg.inst];
-    const DevInst& in = P.insts[seg.inst];
+__device__ void stage_model_consts(const DevSeg& seg, const DevJob& J, const DevPrep& pr, ModelSmem& ms) {
     float* mvpc = reinterpret_cast<float*>(ms.mvpc);
     const bool bb = seg.flags & SEG_BILLBOARD;  // either loop: a billboard only changes the MVP
     for (uint32_t k = threadIdx.x; k < 48; k += blockDim.x) {
@@ -481,7 +564,6 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
         else if (k < 32) ms.M[k - 16] = pr.M[k - 16];
         else ms.dirrot[k - 32] = pr.dirrot[k - 32];
     }
-    const uint32_t nl = (seg.flags & SEG_LIT) ? min(in.light_cnt, (uint32_t)kMaxLights) : 0u;
     if (threadIdx.x == 0) {
         const JobCam& cam = J.cam;
         const DevMesh& me = J.meshes[seg.mesh];
@@ -533,6 +615,14 @@ __device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJo
         e.idx = J.idx + 3 * (size_t)me.tbase;
         e.cells = J.cells;
     }
+}
+
+template <bool kSkin>
+__device__ void stage_model(const FrameParams& P, const DevSeg& seg, const DevJob& J, ModelSmem& ms) {
+    const DevPrep& pr = P.preps[seg.inst];
+    const DevInst& in = P.insts[seg.inst];
+    stage_model_consts<kSkin>(seg, J, pr, ms);
+    const uint32_t nl = (seg.flags & SEG_LIT) ? min(in.light_cnt, (uint32_t)kMaxLights) : 0u;
     for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
         const DevLight& L = J.lights[P.inst_light_idx[in.light_off + k]];
         float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1032,6 +1122,7 @@ __device__ __forceinline__ f3 skinned_centre(const float4* __restrict__ valt, ui
 
 // PV: per (segment, vertex chunk) the vertex records of every vertex the
 // part's triangles use.
+template <bool kM>
 __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* smem) {
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
@@ -1083,6 +1174,7 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
 }
 
 // PV for the vertex items of parts with shape keys or skinning (queue 5).
+template <bool kM>
 __device__ __noinline__ void phase_vertex_altered(const FrameParams& P, unsigned char* smem) {
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
@@ -1283,23 +1375,31 @@ __device__ __forceinline__ void triangle_tiles(const FrameParams& P, unsigned ch
 #undef T3D_TILE_FIRST
 #undef T3D_TILE_END
 }
+template <bool kM>
 __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char* smem) { triangle_tiles<false>(P, smem); }
+template <bool kM>
 __device__ __noinline__ void phase_triangles_skinned(const FrameParams& P, unsigned char* smem) {
     triangle_tiles<true>(P, smem);
 }
 
 // P2: bin histograms of the tiles of multi-tile segments, one warp per tile
-// (each warp pulls its own tiles and owns a kBins-counter region of shared memory).
+// (each warp pulls its own tiles and owns a kBins-counter region of shared
+// memory). Queue slots run over the record-path tiles [mt_tile_begin,
+// mt_tile_end), then the meshlet tiles [mt_mesh_begin, mt_mesh_end), whose
+// lists are dense.
+template <bool kM>
 __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
     const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t per = T / nw;
+    const uint32_t n_rec = P.mt_tile_end - P.mt_tile_begin, n_all = n_rec + (P.mt_mesh_end - P.mt_mesh_begin);
     uint32_t* wh = L.whist + wid * kBins;
-    uint32_t i = 0;
-    if (lane == 0) i = atomicAdd(&P.ctl->queue[2], 1u);
-    i = P.mt_tile_begin + __shfl_sync(0xffffffffu, i, 0);
-    while (i < P.mt_tile_end) {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(&P.ctl->queue[2], 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    while (k < n_all) {
+        const uint32_t i = k < n_rec ? P.mt_tile_begin + k : P.mt_mesh_begin + (k - n_rec);
         const TileDesc& td = P.mt_desc[i];
         const uint32_t s = td.seg;
         const uint32_t n = __ldcg(&P.tile_count[i]);
@@ -1310,13 +1410,15 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
             const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
             const float range = range_of(mn, mx);
             const uint32_t sort_mode = seg_sort_mode(td.flags);
-            // the tile's list regions (one per warp of the triangle phase), 4 keys per load
-            for (uint32_t w = 0; w < nw; w++) {
-                const uint32_t c = __ldcg(&P.tile_wcnt[(size_t)i * kMaxWarps + w]);
+            const bool dense = td.flags & SEG_MESHLET;
+            // the tile's list: one dense region, or one region per warp of the triangle phase;
+            // 4 keys per load
+            for (uint32_t w = 0; w < (dense ? 1u : nw); w++) {
+                const uint32_t c = dense ? n : __ldcg(&P.tile_wcnt[(size_t)i * kMaxWarps + w]);
                 const float4* rd = reinterpret_cast<const float4*>(P.vis_depth + (size_t)i * T + w * per);
-                for (uint32_t k = lane; 4 * k < c; k += 32) {
-                    const float4 v = __ldcg(&rd[k]);
-                    const uint32_t j = 4 * k;
+                for (uint32_t q = lane; 4 * q < c; q += 32) {
+                    const float4 v = __ldcg(&rd[q]);
+                    const uint32_t j = 4 * q;
                     atomicAdd(&wh[bin_of(v.x, mn, range, sort_mode)], 1u);
                     if (j + 1 < c) atomicAdd(&wh[bin_of(v.y, mn, range, sort_mode)], 1u);
                     if (j + 2 < c) atomicAdd(&wh[bin_of(v.z, mn, range, sort_mode)], 1u);
@@ -1330,11 +1432,12 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         __syncwarp();
         uint32_t nx = 0;
         if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
-        i = P.mt_tile_begin + __shfl_sync(0xffffffffu, nx, 0);
+        k = __shfl_sync(0xffffffffu, nx, 0);
     }
 }
 
 // P3: per multi-tile segment, turn tile histograms into per-tile bin bases.
+template <bool kM>
 __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* smem) {
     const SmemLayout L = smem_layout(smem, P.tile_tris);
     TileSmem& sm = *L.ts;
@@ -1380,6 +1483,7 @@ __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* sme
 }
 
 // P4: stable rank and emission of the tiles of multi-tile segments.
+template <bool kM>
 __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
@@ -1435,6 +1539,446 @@ __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned cha
     }
 }
 
+// ------------------------------------------------------- meshlet tiles ----
+// Render pairs whose parts have meshlets (SEG_MESHLET) keep no per-vertex
+// records in HBM. The triangle phase bulk-copies a meshlet's local indices and
+// positions into shared memory (the next tile's copy in flight while this one
+// is processed), computes the clip values of its slots there, tests the
+// triangles and writes the tile's dense visible list; the rank phase copies the
+// meshlet's interleaved vertices, computes every slot's emitted corner
+// (transform, lighting, depth) in shared memory, ranks the visible list and
+// emits from shared memory. Every meshlet tile takes the multi-tile route
+// (histogram, cross-tile scan, rank), also when its pair has one tile.
+
+struct MeshHdr {
+    unsigned long long bar[4];   // mbarriers: triangle phase 0, 1 = copy buffers; rank phase
+                                 // 0 = list + bases, 1 = vertex block, 3 = lights
+    uint32_t item[2];            // work item whose copy is in buffer b
+    uint32_t copied[2];          // buffer b holds a copy in flight
+    uint32_t pad[4];
+    TileDesc td[2];              // descriptor of the tile in buffer b
+};
+static_assert(sizeof(MeshHdr) % 16 == 0, "MeshHdr keeps 16-byte alignment");
+// Device address of a meshlet tile's data (the host keeps it in the descriptor's vhi / pad1).
+__device__ __forceinline__ const unsigned char* mlet_addr(const TileDesc& td) {
+    return reinterpret_cast<const unsigned char*>(((uint64_t)td.pad1 << 32) | td.vhi);
+}
+
+__host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+// The head of a DevPrep record the triangle phase copies: mvp, M, dirrot, invcam.
+constexpr uint32_t kPrepHead = 208;
+static_assert(offsetof(DevPrep, invcam) + 16 == kPrepHead && sizeof(DevPrep) % 16 == 0, "DevPrep head layout");
+// Triangle phase: MeshHdr | TileSmem | buf[2] (the model's prep record up to the model-space
+// camera, then lidx + pos of one meshlet) | cx, cy, cz per slot | the tile's visible
+// entries per warp region (depth f32[T], slots u16[3T])
+struct MeshTriLayout { size_t ts, buf0, buf1, cx, cy, cz, sdep, svl, total; };
+__host__ __device__ __forceinline__ MeshTriLayout mesh_tri_layout(uint32_t T, uint32_t U) {
+    MeshTriLayout L;
+    size_t o = sizeof(MeshHdr);
+    L.ts = o; o += al16(sizeof(TileSmem));
+    const size_t buf = kPrepHead + (size_t)mlet_lidx_bytes(T) + 12ull * U;
+    L.buf0 = o; o += al16(buf);
+    L.buf1 = o; o += al16(buf);
+    L.cx = o; o += al16(4ull * U);
+    L.cy = o; o += al16(4ull * U);
+    L.cz = o; o += al16(4ull * U);
+    L.sdep = o; o += al16(4ull * T);
+    L.svl = o; o += al16(6ull * T);
+    L.total = o;
+    return L;
+}
+// Rank phase: MeshHdr | TileSmem | ModelSmem | bases u32[kBins] | depth f32[T] (later perm
+// u16[T]) | vloc u16[3T] | bin u16[T] | whist | records: 48 bytes per slot (xyuv float4,
+// rgba float4, depth float), computed in place over the copied vertex block
+struct MeshRankLayout { size_t ts, ms, hist, dep, vloc, bin, wh, rec, total; };
+constexpr uint32_t kRecBytes = 48;
+__host__ __device__ __forceinline__ MeshRankLayout mesh_rank_layout(uint32_t T, uint32_t U, uint32_t warps) {
+    MeshRankLayout L;
+    size_t o = sizeof(MeshHdr);
+    L.ts = o; o += al16(sizeof(TileSmem));
+    L.ms = o; o += al16(sizeof(ModelSmem));
+    L.hist = o; o += 4ull * kBins;
+    L.dep = o; o += al16(4ull * T);
+    L.vloc = o; o += al16(6ull * T);
+    L.bin = o; o += al16(2ull * T);
+    L.wh = o; o += 4ull * warps * kBins;
+    L.rec = o; o += (size_t)kRecBytes * U;
+    L.total = o;
+    return L;
+}
+
+// Thread 0: records the descriptor of the tile going into buf and starts the copy of
+// its model's prep head, local indices and positions (nothing for skipped pairs
+// and culled models).
+__device__ __forceinline__ uint32_t mesh_issue_tri(const FrameParams& P, const TileDesc& td, bool culled,
+                                                   unsigned char* buf, unsigned long long* bar, TileDesc* slot) {
+    *slot = td;
+    if ((td.flags & SEG_SKIP) || culled) return 0u;
+    const uint32_t bytes = mlet_lidx_bytes(td.t1 - td.t0) + 12u * mlet_slots4(td.vmin);
+    fence_proxy_async();
+    mbar_expect_tx(bar, kPrepHead + bytes);
+    bulk_g2s(buf, &P.preps[td.inst], kPrepHead, bar);
+    bulk_g2s(buf + kPrepHead, mlet_addr(td), bytes, bar);
+    return 1u;
+}
+
+// MultVecW (model.go:808-811) by MVP rows m (row-major), in the reference's order.
+__device__ __forceinline__ float4 clip_rows(const float* m, float x, float y, float z) {
+    float4 c;
+    c.x = m[0] * x + m[4] * y + m[8] * z + m[12];
+    c.y = m[1] * x + m[5] * y + m[9] * z + m[13];
+    c.z = m[2] * x + m[6] * y + m[10] * z + m[14];
+    c.w = m[3] * x + m[7] * y + m[11] * z + m[15];
+    return c;
+}
+
+// Thread 0 also reads, between the steps of a tile, what the copy of the block's
+// tile after next needs: the descriptor of queue slot `kn` (after the clip values)
+// and its model's culling flag (after the triangles), so their latency hides
+// behind work.
+struct NextTile {
+    uint32_t kn;       // queue slot taken for the tile after next
+    TileDesc td;
+    uint32_t culled;
+};
+__device__ __forceinline__ void next_desc(const FrameParams& P, NextTile& nx) {
+    if (threadIdx.x == 0 && nx.kn < P.mesh_end - P.mesh_begin) nx.td = P.tiles[P.mesh_begin + nx.kn];
+}
+__device__ __forceinline__ void next_culled(const FrameParams& P, NextTile& nx) {
+    if (threadIdx.x == 0 && nx.kn < P.mesh_end - P.mesh_begin) nx.culled = P.preps[nx.td.inst].culled;
+}
+
+// One meshlet tile of the triangle phase, its prep head + lidx + pos block in buf.
+__device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDesc& td, unsigned char* buf,
+                                              TileSmem& sm, float* scx, float* scy, float* scz, float* sdep,
+                                              uint16_t* svl, NextTile& nx) {
+    const uint32_t mt = td.mt;
+    const DevPrep& pr = *reinterpret_cast<const DevPrep*>(buf);  // its head: mvp, M, dirrot, invcam
+    float* mrow = reinterpret_cast<float*>(buf);
+    if (td.flags & SEG_BILLBOARD) {  // the part turns to the camera (model.go:634-695)
+        if (threadIdx.x == 0) {
+            const JobCam& cam = P.jobs[td.job].cam;
+            const m4 base = billboard_base(load16(pr.M), mk3(cam.pos[0], cam.pos[1], cam.pos[2]),
+                                           (td.flags & SEG_BB_CAMUP) ? mk3(cam.up[0], cam.up[1], cam.up[2])
+                                                                     : mk3(0.f, 1.f, 0.f),
+                                           td.flags & SEG_BB_LOCKX, td.flags & SEG_BB_LOCKY, td.flags & SEG_BB_LOCKZ);
+            store16(mult(base, load16(cam.vp)), mrow);
+        }
+        __syncthreads();
+    }
+    const uint32_t U = td.vmin, nt = td.t1 - td.t0;
+    const uint16_t* __restrict__ lidx = reinterpret_cast<const uint16_t*>(buf + kPrepHead);
+    const float* __restrict__ pos = reinterpret_cast<const float*>(buf + kPrepHead + mlet_lidx_bytes(nt));
+    for (uint32_t v = threadIdx.x; v < U; v += blockDim.x) {
+        // MultVecW and the x/y divide of the rejection tests (model.go:808-873)
+        const float4 c = clip_rows(mrow, pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]);
+        const float w1 = c.w < 0.0f ? 0.000001f : c.w;
+        scx[v] = c.x / w1;
+        scy[v] = c.y / w1;
+        scz[v] = c.z;
+    }
+    next_desc(P, nx);
+    __syncthreads();
+    const uint32_t T = P.tile_tris;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float* __restrict__ gd = P.vis_depth + (size_t)mt * T;
+    uint16_t* __restrict__ gv = P.vis_vloc + (size_t)mt * 3 * T;
+    const float nearp = td.nearp, farp = td.farp;
+    const bool backface = td.flags & SEG_BACKFACE;
+    const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
+    float lmin = 3.402823466e38f, lmax = 0.0f;
+    const uint32_t per = T / nw;
+    const uint32_t wt0 = wid * per, wt1 = min(nt, wt0 + per);
+    const uint32_t wbase = wid * per;
+    uint32_t cnt = 0;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t tb = wt0; tb < wt1; tb += 32) {
+        const uint32_t t = tb + lane;
+        bool vis = false;
+        float d = 0.0f;
+        uint32_t i0 = 0, i1 = 0, i2 = 0;
+        if (t < wt1) {
+            i0 = lidx[3 * t]; i1 = lidx[3 * t + 1]; i2 = lidx[3 * t + 2];
+            const float4 c0 = make_float4(scx[i0], scy[i0], scz[i0], 0.f);
+            const float4 c1 = make_float4(scx[i1], scy[i1], scz[i1], 0.f);
+            const float4 c2 = make_float4(scx[i2], scy[i2], scz[i2], 0.f);
+            // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis
+            const f3 ctr = mk3((pos[3 * i0] + pos[3 * i1] + pos[3 * i2]) / 3.0f,
+                               (pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]) / 3.0f,
+                               (pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]) / 3.0f);
+            vis = tri_visible(nearp, farp, backface, ic, c0, c1, c2, ctr, d);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, vis);
+        if (vis) {
+            const uint32_t p = wbase + cnt + __popc(bal & lt);
+            sdep[p] = d;
+            svl[3 * p] = (uint16_t)i0;
+            svl[3 * p + 1] = (uint16_t)i1;
+            svl[3 * p + 2] = (uint16_t)i2;
+            lmin = fminf(lmin, d);
+            lmax = fmaxf(lmax, d);
+        }
+        cnt += __popc(bal);
+    }
+    next_culled(P, nx);
+    for (int o = 16; o > 0; o >>= 1) {
+        lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+        lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    }
+    if (lane == 0) {
+        sm.wmin[wid] = lmin;
+        sm.wmax[wid] = lmax;
+        sm.warp_tot[wid] = cnt;
+    }
+    __syncthreads();
+    {  // the tile's list, dense and in triangle order: each warp copies its region after the ones before
+        uint32_t base = 0;
+        for (uint32_t w = 0; w < wid; w++) base += sm.warp_tot[w];
+        for (uint32_t q = lane; q < cnt; q += 32) gd[base + q] = sdep[wbase + q];
+        for (uint32_t q = lane; q < 3 * cnt; q += 32) gv[3 * base + q] = svl[3 * wbase + q];
+    }
+    if (threadIdx.x == 0) {
+        uint32_t n = 0;
+        float mn = sm.wmin[0], mx = sm.wmax[0];
+        for (uint32_t w = 0; w < nw; w++) n += sm.warp_tot[w];
+        for (uint32_t w = 1; w < nw; w++) { mn = fminf(mn, sm.wmin[w]); mx = fmaxf(mx, sm.wmax[w]); }
+        P.tile_count[mt] = n;
+        if (n > 0) {
+            atomicMin(&P.seg_minmax[2 * td.seg], __float_as_uint(mn));
+            atomicMax(&P.seg_minmax[2 * td.seg + 1], __float_as_uint(mx));
+            atomicAdd(&P.seg_count[td.seg], n);
+            atomicAdd(&P.accum[0], (unsigned long long)n);
+        }
+    }
+}
+
+// Triangle phase over meshlet tiles (queue 0). Work is taken two tiles ahead: while
+// a block processes the tile in one copy buffer, the copy of its next tile is in
+// flight into the other, and thread 0 spreads the queue slot, descriptor and
+// culling reads for the tile after that over the current tile's work.
+template <bool kM>
+__device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsigned char* smem) {
+    MeshHdr& H = *reinterpret_cast<MeshHdr*>(smem);
+    const MeshTriLayout L = mesh_tri_layout(P.tile_tris, P.mesh_ucap);
+    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem + L.ts);
+    unsigned char* buf[2] = {smem + L.buf0, smem + L.buf1};
+    float* scx = reinterpret_cast<float*>(smem + L.cx);
+    float* scy = reinterpret_cast<float*>(smem + L.cy);
+    float* scz = reinterpret_cast<float*>(smem + L.cz);
+    float* sdep = reinterpret_cast<float*>(smem + L.sdep);
+    uint16_t* svl = reinterpret_cast<uint16_t*>(smem + L.svl);
+    const uint32_t n = P.mesh_end - P.mesh_begin, limit = spin_limit(P);
+    uint32_t ph0 = 0, ph1 = 0;
+    // the barriers live in bytes that other phases use: set up here, invalidated at the end
+    if (threadIdx.x == 0) {
+        mbar_init(&H.bar[0], 1);
+        mbar_init(&H.bar[1], 1);
+        fence_mbar_init();
+        for (int b = 0; b < 2; b++) {
+            const uint32_t k = atomicAdd(&P.ctl->queue[0], 1u);
+            H.item[b] = k;
+            H.copied[b] = 0u;
+            if (k < n) {
+                const TileDesc td = P.tiles[P.mesh_begin + k];
+                H.copied[b] = mesh_issue_tri(P, td, P.preps[td.inst].culled != 0, buf[b], &H.bar[b], &H.td[b]);
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t cur = 0;
+    for (;;) {
+        const uint32_t k = H.item[cur];
+        if (k >= n) break;
+        NextTile nx;
+        nx.kn = 0xFFFFFFFFu;
+        nx.culled = 1u;
+        if (threadIdx.x == 0) nx.kn = atomicAdd(&P.ctl->queue[0], 1u);  // read after the clip values
+        bool ok = true;
+        if (H.copied[cur]) {
+            ok = mbar_wait(&H.bar[cur], cur ? ph1 : ph0, P.ctl, limit);
+            if (cur) ph1 ^= 1u; else ph0 ^= 1u;
+        }
+        if (!__syncthreads_and(ok)) {  // gave up: let the other buffer's copy land, then leave
+            if (H.copied[cur ^ 1]) mbar_wait(&H.bar[cur ^ 1], cur ? ph0 : ph1, P.ctl, kSpinLimit);
+            break;
+        }
+        const TileDesc& td = H.td[cur];
+        if (H.copied[cur]) {
+            mesh_tile_tri(P, td, buf[cur], sm, scx, scy, scz, sdep, svl, nx);
+        } else {  // skipped pair or culled model
+            if (threadIdx.x == 0) P.tile_count[td.mt] = 0u;
+            next_desc(P, nx);
+            next_culled(P, nx);
+        }
+        __syncthreads();  // buffer cur is free
+        if (threadIdx.x == 0) {
+            H.item[cur] = nx.kn;
+            H.copied[cur] = nx.kn < n ? mesh_issue_tri(P, nx.td, nx.culled != 0, buf[cur], &H.bar[cur], &H.td[cur]) : 0u;
+        }
+        __syncthreads();
+        cur ^= 1u;
+    }
+    __syncthreads();
+    // every copy issued was waited for (a queue slot past the end issues none)
+    if (threadIdx.x == 0) {
+        mbar_inval(&H.bar[0]);
+        mbar_inval(&H.bar[1]);
+    }
+    __syncthreads();
+}
+
+// Rank phase over meshlet tiles (queue 9). Thread 0 starts every copy of a tile at
+// once: the dense visible list and the tile's bin bases (barrier 0), the
+// meshlet's interleaved vertex block (barrier 1) and the model's staged lights
+// (barrier 3). The block stages the pair's constants meanwhile, bins the list,
+// turns the vertex block into emitted corners in place, ranks the list and emits
+// from shared memory. The block's next tile is taken at the start of a tile and
+// its data asked into L2 halfway through.
+template <bool kM>
+__device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned char* smem) {
+    MeshHdr& H = *reinterpret_cast<MeshHdr*>(smem);
+    const uint32_t T = P.tile_tris, nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const MeshRankLayout ML = mesh_rank_layout(T, P.mesh_ucap, nw);
+    SmemLayout L;
+    L.ts = reinterpret_cast<TileSmem*>(smem + ML.ts);
+    L.whist = reinterpret_cast<uint32_t*>(smem + ML.wh);
+    L.bin = reinterpret_cast<uint16_t*>(smem + ML.bin);
+    L.perm = reinterpret_cast<uint16_t*>(smem + ML.dep);  // the depth keys are dead once binned
+    L.vloc = reinterpret_cast<uint16_t*>(smem + ML.vloc);
+    L.depth = reinterpret_cast<float*>(smem + ML.dep);
+    L.lidx = nullptr;
+    TileSmem& sm = *L.ts;
+    ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem + ML.ms);
+    const uint32_t* hist = reinterpret_cast<const uint32_t*>(smem + ML.hist);
+    unsigned char* rec = smem + ML.rec;
+    const uint32_t limit = spin_limit(P);
+    uint32_t ph0 = 0, ph1 = 0, ph3 = 0;  // mbarrier phases
+    const uint32_t nmt = P.mt_mesh_end - P.mt_mesh_begin;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 4; b++) mbar_init(&H.bar[b], 1);
+        fence_mbar_init();
+    }
+    uint32_t k = next_item(P.ctl, 9, &sm.item);
+    while (k < nmt) {
+        const uint32_t i = P.mt_mesh_begin + k;
+        uint32_t kn = 0xFFFFFFFFu;
+        if (threadIdx.x == 0) kn = atomicAdd(&P.ctl->queue[9], 1u);
+        const uint32_t n = __ldcg(&P.tile_count[i]);
+        const TileDesc td = P.mt_desc[i];
+        if (n > 0) {
+        const uint32_t U = td.vmin, U4 = mlet_slots4(U), nt = td.t1 - td.t0;
+        const bool colors = td.flags & SEG_COLORS;
+        const uint32_t as = mlet_aos_stride(colors);
+        // the vertex block lands at the end of the record area: a slot's 48-byte record then
+        // only ever covers input bytes of its own or earlier slots
+        unsigned char* vin = rec + (size_t)(kRecBytes - as) * U4;
+        const bool lit = td.flags & SEG_LIT;
+        const DevPrep& pr = P.preps[td.inst];
+        const uint32_t nl = lit ? pr.nl : 0u;
+        if (threadIdx.x == 0) {
+            const uint32_t db = (4u * n + 15u) & ~15u, vb = (6u * n + 15u) & ~15u;
+            fence_proxy_async();
+            mbar_expect_tx(&H.bar[0], 4u * kBins + db + vb);
+            bulk_g2s(smem + ML.hist, P.tile_hist + (size_t)i * kBins, 4u * kBins, &H.bar[0]);
+            bulk_g2s(L.depth, P.vis_depth + (size_t)i * T, db, &H.bar[0]);
+            bulk_g2s(L.vloc, P.vis_vloc + (size_t)i * 3 * T, vb, &H.bar[0]);
+            mbar_expect_tx(&H.bar[1], as * U4);
+            bulk_g2s(vin, mlet_addr(td) + mlet_lidx_bytes(nt) + 12ull * U4, as * U4, &H.bar[1]);
+            if (nl) {
+                const unsigned char* src = reinterpret_cast<const unsigned char*>(P.inst_lights) +
+                                           (size_t)td.inst * kMaxLights * sizeof(SLight);
+                mbar_expect_tx(&H.bar[3], slight_copy_bytes(nl));
+                bulk_g2s(ms.lights, src, slight_copy_bytes(nl), &H.bar[3]);
+            }
+            ms.nl = nl;
+        }
+        const DevSeg seg = P.segs[td.seg];
+        stage_model_consts<false>(seg, P.jobs[td.job], pr, ms);
+        const uint32_t s = td.seg;
+        const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
+        const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
+        const float range = range_of(mn, mx);
+        const uint32_t sort_mode = seg_sort_mode(td.flags);
+        bool ok = mbar_wait(&H.bar[0], ph0, P.ctl, limit);
+        ph0 ^= 1u;
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) L.bin[j] = (uint16_t)bin_of(L.depth[j], mn, range, sort_mode);
+        uint32_t nn = 0;
+        TileDesc tn;
+        if (threadIdx.x == 0 && kn < nmt) {  // read now, used after the records
+            nn = __ldcg(&P.tile_count[P.mt_mesh_begin + kn]);
+            tn = P.mt_desc[P.mt_mesh_begin + kn];
+        }
+        if (nl) {
+            ok = mbar_wait(&H.bar[3], ph3, P.ctl, limit) && ok;
+            ph3 ^= 1u;
+        }
+        {  // the warps rank consecutive slices of the dense list
+            const uint32_t per = (n + nw - 1) / nw;
+            if (lane == 0) {
+                sm.wlo[wid] = min(n, wid * per);
+                sm.whi[wid] = min(n, wid * per + per);
+            }
+        }
+        ok = mbar_wait(&H.bar[1], ph1, P.ctl, limit) && ok;
+        ph1 ^= 1u;
+        // every slot's emitted corner, in place: a round of blockDim slots reads its inputs,
+        // then (after a barrier) writes its records
+        for (uint32_t v0 = 0; v0 < U; v0 += blockDim.x) {
+            const uint32_t v = v0 + threadIdx.x;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), bb = a, kc = a;
+            if (v < U) {
+                const float4* in = reinterpret_cast<const float4*>(vin + (size_t)as * v);
+                a = in[0];
+                bb = in[1];
+                if (colors) kc = in[2];
+            }
+            __syncthreads();
+            if (v < U) {
+                float4 cull, xyuv, rgba;
+                vertex_record<false>(ms, a, bb, kc, cull, xyuv, rgba);
+                float4* out = reinterpret_cast<float4*>(rec + (size_t)kRecBytes * v);
+                out[0] = xyuv;
+                out[1] = rgba;
+                out[2] = make_float4(cull.w, 0.f, 0.f, 0.f);
+            }
+        }
+        if (threadIdx.x == 0 && nn > 0) {  // the next tile's vertex block, list and bases into L2
+            const uint32_t u4n = mlet_slots4(tn.vmin), ntn = tn.t1 - tn.t0;
+            const uint32_t in_ = P.mt_mesh_begin + kn;
+            l2_prefetch(mlet_addr(tn) + mlet_lidx_bytes(ntn) + 12ull * u4n,
+                        (size_t)mlet_aos_stride(tn.flags & SEG_COLORS) * u4n);
+            l2_prefetch(P.vis_depth + (size_t)in_ * T, 4ull * nn);
+            l2_prefetch(P.vis_vloc + (size_t)in_ * 3 * T, 6ull * nn);
+            l2_prefetch(P.tile_hist + (size_t)in_ * kBins, 4ull * kBins);
+        }
+        if (__syncthreads_and(ok)) {
+            rank_tile(L, sort_mode);
+            float4* __restrict__ oxyuv = P.out_xyuv + 3 * (size_t)td.out_base;
+            float4* __restrict__ orgba = P.out_rgba + 3 * (size_t)td.out_base;
+            float* __restrict__ odepth = P.out_depth + 3 * (size_t)td.out_base;
+            for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {
+                const uint32_t r = q / 3u, cc = q - 3u * r;
+                const uint32_t j = L.perm[r];
+                const uint32_t bn = L.bin[j];
+                const uint32_t pos = hist[bn] + (r - sm.loc_walk[walk_pos(bn, sort_mode)]);
+                const float4* rc = reinterpret_cast<const float4*>(rec + (size_t)kRecBytes * L.vloc[3 * j + cc]);
+                oxyuv[3 * pos + cc] = rc[0];
+                orgba[3 * pos + cc] = rc[1];
+                odepth[3 * pos + cc] = reinterpret_cast<const float*>(rc + 2)[0];
+            }
+        }
+        }
+        __syncthreads();  // the shared arrays are free; the slot taken above becomes the current tile
+        if (threadIdx.x == 0) sm.item = kn;
+        __syncthreads();
+        k = sm.item;
+    }
+    if (threadIdx.x == 0) {  // every copy of the last tile was waited for
+        for (int b = 0; b < 4; b++) mbar_inval(&H.bar[b]);
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -1454,44 +1998,55 @@ __device__ __forceinline__ void phase_start(unsigned long long& since) {
 }
 
 #ifndef T3D_MIN_BLOCKS
-#define T3D_MIN_BLOCKS 4  // resident blocks of 256 threads per SM the register budget is sized for
+#define T3D_MIN_BLOCKS 4  // resident blocks of 256 threads per SM the record-path kernel's registers are sized for
 #endif
-__global__ void __launch_bounds__(256, T3D_MIN_BLOCKS) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
+#ifndef T3D_MESH_BLOCKS
+#define T3D_MESH_BLOCKS 2  // the same for the kernel with meshlet tiles (its shared memory allows 2 per SM)
+#endif
+// kM: the frame has meshlet tiles. Both instantiations run the record path for
+// the pairs that need it (skinning, shape keys, subdivision, snapping, ...).
+template <bool kM>
+__global__ void __launch_bounds__(256, kM ? T3D_MESH_BLOCKS : T3D_MIN_BLOCKS) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long since = 0;
+    const uint32_t limit = spin_limit(P);
     if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl->t_end[7] = global_ns();
     phase_start(since);
-    phase_prep(P);
+    phase_prep<kM>(P);
     phase_done(P.ctl, 0, since);
-    if (!grid_barrier(P.ctl)) return;
+    if (!grid_barrier(P.ctl, limit)) return;
     phase_start(since);
-    phase_vertex(P, smem);
-    if (P.vitem_alt < P.vitem_end) phase_vertex_altered(P, smem);
+    if (P.vitem_begin < P.vitem_alt) phase_vertex<kM>(P, smem);
+    if (P.vitem_alt < P.vitem_end) phase_vertex_altered<kM>(P, smem);
     phase_done(P.ctl, 6, since);
-    if (!grid_barrier(P.ctl)) return;
+    if (!grid_barrier(P.ctl, limit)) return;
     phase_start(since);
-    phase_triangles(P, smem);
-    if (P.tile_alt < P.tile_end) phase_triangles_skinned(P, smem);
+    if (kM && P.mesh_begin < P.mesh_end) phase_triangles_meshlet<kM>(P, smem);
+    if (P.tile_begin < P.tile_alt) phase_triangles<kM>(P, smem);
+    if (P.tile_alt < P.tile_end) phase_triangles_skinned<kM>(P, smem);
     phase_done(P.ctl, 1, since);
     if (!P.has_multi) return;
-    if (!grid_barrier(P.ctl)) return;
+    if (!grid_barrier(P.ctl, limit)) return;
     phase_start(since);
-    phase_hist(P, smem);
+    phase_hist<kM>(P, smem);
     phase_done(P.ctl, 2, since);
-    if (!grid_barrier(P.ctl)) return;
+    if (!grid_barrier(P.ctl, limit)) return;
     phase_start(since);
-    phase_scan(P, smem);
+    phase_scan<kM>(P, smem);
     phase_done(P.ctl, 3, since);
-    if (!grid_barrier(P.ctl)) return;
+    if (!grid_barrier(P.ctl, limit)) return;
     phase_start(since);
-    phase_rank_multi(P, smem);
+    if (P.mt_tile_begin < P.mt_tile_end) phase_rank_multi<kM>(P, smem);
+    if (kM && P.mt_mesh_begin < P.mt_mesh_end) phase_rank_meshlet<kM>(P, smem);
     phase_done(P.ctl, 4, since);
 }
 
 }  // namespace t3d
 
 // Launch entry used by the runtime (same translation-unit linkage).
-extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel; }
+extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel<false>; }
+// The instantiation for frames with meshlet tiles.
+extern "C" const void* t3d_frame_kernel_mesh_ptr() { return (const void*)&t3d::t3d_frame_kernel<true>; }
 // The keyed streams of one mesh (k_bake_shapes) on stream st.
 extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
                                        const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
@@ -1505,4 +2060,11 @@ extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_thread
                          10ull * tile_tris + 16;
     const size_t verts = sizeof(t3d::ModelSmem) + 16;
     return tiles > verts ? tiles : verts;
+}
+// Shared memory of the meshlet kernel: the record-path layouts and both meshlet phases.
+extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_threads, uint32_t mesh_ucap) {
+    const size_t a = t3d_frame_smem_bytes(tile_tris, block_threads);
+    const size_t b = t3d::mesh_tri_layout(tile_tris, mesh_ucap).total;
+    const size_t c = t3d::mesh_rank_layout(tile_tris, mesh_ucap, block_threads / 32).total;
+    return a > b ? (a > c ? a : c) : (b > c ? b : c);
 }

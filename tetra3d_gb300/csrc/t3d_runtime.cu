@@ -25,6 +25,7 @@
 #include "t3d_runtime.h"
 
 extern "C" const void* t3d_frame_kernel_ptr();
+extern "C" const void* t3d_frame_kernel_mesh_ptr();
 extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
                                        const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
                                        float4* ob);
@@ -482,6 +483,139 @@ int bake_shapes(t3d_ctx* ctx, Scene* sc, uint32_t m) {
     return T3D_OK;
 }
 
+// ------------------------------------------------------------ meshlets ----
+// Cuts triangles [t0, t1) of a mesh into runs of consecutive triangles with at
+// most T triangles and at most U distinct vertices (a run ends before the
+// triangle that would exceed either). `stamp` marks the vertices of the run.
+static void cut_meshlets(const uint32_t* idx, uint32_t t0, uint32_t t1, uint32_t T, uint32_t U,
+                         std::vector<uint32_t>& stamp, uint32_t& gen, std::vector<Meshlet>& out) {
+    uint32_t t = t0;
+    while (t < t1) {
+        if (++gen == 0) { std::fill(stamp.begin(), stamp.end(), 0u); gen = 1; }
+        const uint32_t s = t;
+        uint32_t nu = 0;
+        while (t < t1 && t - s < T) {
+            const uint32_t a = idx[3 * (size_t)t], b = idx[3 * (size_t)t + 1], c = idx[3 * (size_t)t + 2];
+            const uint32_t add = (stamp[a] != gen) + (stamp[b] != gen && b != a) + (stamp[c] != gen && c != a && c != b);
+            if (nu + add > U) break;
+            stamp[a] = stamp[b] = stamp[c] = gen;
+            nu += add;
+            t++;
+        }
+        out.push_back({s, t - s, nu, 0u});
+    }
+}
+
+// Writes one meshlet (layout in t3d_device.cuh): slots in order of first use.
+static void fill_meshlet(const Meshlet& ml, const uint32_t* idx, const float4* va, const float4* vb, const float4* vc,
+                         bool colors, std::vector<uint32_t>& stamp, std::vector<uint32_t>& slot, uint32_t& gen,
+                         std::vector<uint32_t>& verts, unsigned char* dst) {
+    if (++gen == 0) { std::fill(stamp.begin(), stamp.end(), 0u); gen = 1; }
+    verts.clear();
+    uint16_t* li = reinterpret_cast<uint16_t*>(dst);
+    for (uint32_t t = 0; t < ml.nt; t++)
+        for (int k = 0; k < 3; k++) {
+            const uint32_t v = idx[3 * ((size_t)ml.t0 + t) + k];
+            if (stamp[v] != gen) {
+                stamp[v] = gen;
+                slot[v] = (uint32_t)verts.size();
+                verts.push_back(v);
+            }
+            li[3 * t + k] = (uint16_t)slot[v];
+        }
+    memset(dst + 6ull * ml.nt, 0, mlet_lidx_bytes(ml.nt) - 6ull * ml.nt);
+    const uint32_t U4 = mlet_slots4(ml.nu);
+    float* pos = reinterpret_cast<float*>(dst + mlet_lidx_bytes(ml.nt));
+    float* aos = pos + 3ull * U4;
+    const uint32_t af = mlet_aos_stride(colors) / 4;
+    memset(pos, 0, (12ull + 4 * af) * U4);
+    for (uint32_t q = 0; q < (uint32_t)verts.size(); q++) {
+        const float4 a = va[verts[q]], b = vb[verts[q]];
+        pos[3 * q] = a.x; pos[3 * q + 1] = a.y; pos[3 * q + 2] = a.z;
+        float* r = aos + (size_t)af * q;
+        r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+        r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+        if (colors) {
+            const float4 c = vc[verts[q]];
+            r[8] = c.x; r[9] = c.y; r[10] = c.z; r[11] = c.w;
+        }
+    }
+}
+
+// Cuts every part of the scene's meshes into meshlets for a triangle budget T
+// and a vertex budget U and stores them in the scene's meshlet pool, from the
+// resident vertex and index streams. Meshes with shape keys (their keyed
+// streams change with the weights) and auto-subdivided meshes get none: their
+// pairs take the per-vertex record path.
+int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U) {
+    sc->mlet.release();
+    sc->mlet_T = sc->mlet_U = 0;
+    for (SceneMesh& me : sc->meshes) me.mparts.assign(me.parts.size(), {});
+    if (U < 3 || U > 65535u) return T3D_OK;
+    std::vector<uint32_t> stamp, slot, verts, idx;
+    uint32_t gen = 0;
+    uint64_t total16 = 0;
+    // pass 1: the cuts and their offsets
+    for (SceneMesh& me : sc->meshes) {
+        if (me.nkeys || me.subdiv || me.ntris == 0) continue;
+        idx.resize(3ull * me.ntris);
+        CK(cudaMemcpy(idx.data(), (const uint32_t*)sc->idx.ptr + 3ull * me.tbase, 12ull * me.ntris, cudaMemcpyDeviceToHost));
+        stamp.assign(me.nverts, 0u);
+        gen = 0;
+        for (size_t p = 0; p < me.parts.size(); p++) {
+            const t3d_part_desc& pd = me.parts[p].d;
+            cut_meshlets(idx.data(), pd.tri_start, pd.tri_start + pd.tri_count, T, U, stamp, gen, me.mparts[p]);
+            for (Meshlet& ml : me.mparts[p]) {
+                ml.off16 = (uint32_t)total16;
+                total16 += mlet_bytes(ml.nt, ml.nu, me.colors) / 16;
+                if (total16 > 0xFFFFFFF0ull) {
+                    set_err(ctx, "meshlet pool beyond 64 GB");
+                    return T3D_E_INVAL;
+                }
+            }
+        }
+    }
+    if (total16 == 0) {
+        sc->mlet_T = T;
+        sc->mlet_U = U;
+        return T3D_OK;
+    }
+    int rc;
+    if ((rc = sc->mlet.ensure(ctx, 16ull * total16))) return rc;
+    // pass 2: the data, one mesh at a time
+    std::vector<float4> va, vb, vc;
+    std::vector<unsigned char> data;
+    for (SceneMesh& me : sc->meshes) {
+        bool any = false;
+        for (const auto& v : me.mparts) any |= !v.empty();
+        if (!any) continue;
+        idx.resize(3ull * me.ntris);
+        va.resize(me.nverts); vb.resize(me.nverts); vc.resize(me.nverts);
+        CK(cudaMemcpy(idx.data(), (const uint32_t*)sc->idx.ptr + 3ull * me.tbase, 12ull * me.ntris, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(va.data(), (const float4*)sc->va.ptr + me.vbase, 16ull * me.nverts, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(vb.data(), (const float4*)sc->vb.ptr + me.vbase, 16ull * me.nverts, cudaMemcpyDeviceToHost));
+        if (me.colors) CK(cudaMemcpy(vc.data(), (const float4*)sc->vc.ptr + me.vbase, 16ull * me.nverts, cudaMemcpyDeviceToHost));
+        stamp.assign(me.nverts, 0u);
+        slot.assign(me.nverts, 0u);
+        gen = 0;
+        uint64_t lo = UINT64_MAX, hi = 0;
+        for (const auto& v : me.mparts)
+            for (const Meshlet& ml : v) {
+                lo = std::min<uint64_t>(lo, ml.off16);
+                hi = std::max<uint64_t>(hi, ml.off16 + mlet_bytes(ml.nt, ml.nu, me.colors) / 16);
+            }
+        data.assign(16 * (hi - lo), 0);
+        for (const auto& v : me.mparts)
+            for (const Meshlet& ml : v)
+                fill_meshlet(ml, idx.data(), va.data(), vb.data(), vc.data(), me.colors, stamp, slot, gen, verts,
+                             data.data() + 16 * (ml.off16 - lo));
+        CK(cudaMemcpy((unsigned char*)sc->mlet.ptr + 16 * lo, data.data(), data.size(), cudaMemcpyHostToDevice));
+    }
+    sc->mlet_T = T;
+    sc->mlet_U = U;
+    return T3D_OK;
+}
+
 int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     if (!d || !out || (d->num_meshes && !d->meshes) || (d->num_models && !d->models) ||
         (d->num_lights && !d->lights) || (d->num_volume_cells && !d->volume_cells)) {
@@ -861,6 +995,7 @@ int scene_upload(t3d_ctx* ctx, const t3d_scene_desc* d, uint32_t* out) {
     rc = scene_write_models(ctx, sc.get(), 0, d->models, d->num_models);
     if (rc) return rc;
     CK(cudaDeviceSynchronize());
+    if (ctx->use_meshlets && ctx->mesh_ucap && (rc = build_meshlets(ctx, sc.get(), ctx->tile_tris, ctx->mesh_ucap))) return rc;
     uint32_t id = ctx->next_scene++;
     *out = id;
     ctx->scenes[id] = std::move(sc);
@@ -983,6 +1118,13 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         dj.pad_sub = 0;
         dj.cell_use_off = (const uint32_t*)sc->cell_use_off.ptr;
         dj.cell_use_items = (const uint32_t*)sc->cell_use_items.ptr;
+        // meshlets cut for another tuning are rebuilt by the context that owns the scene
+        if (ctx->use_meshlets && ctx->mesh_ucap && !ctx->scene_owner && (sc->mlet_T != T || sc->mlet_U != ctx->mesh_ucap)) {
+            CK(cudaDeviceSynchronize());
+            int rc = build_meshlets(ctx, sc, T, ctx->mesh_ucap);
+            if (rc) return rc;
+        }
+        const bool mlet_ok = ctx->use_meshlets && ctx->mesh_ucap && sc->mlet_T == T && sc->mlet_U == ctx->mesh_ucap;
         const uint32_t light_base = (uint32_t)F.lights.size();
         for (const auto& l : sc->lights) {
             DevLight L;
@@ -1138,6 +1280,12 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             flags |= billboard_flags(mat, m.d.skinned != 0);
             if (cd.vertex_snapping > 0.0f) flags |= SEG_SNAP;
             if (flags & (SEG_ALTERED | SEG_ALT_TILES)) F.any_altered = true;
+            // pairs that need no more than the plain vertex loop take their part's meshlets
+            const std::vector<Meshlet>* mls = nullptr;
+            if (mlet_ok && !(flags & (SEG_ALTERED | SEG_ALT_TILES | SEG_SHAPES | SEG_SKIP)) &&
+                rp.part < me.mparts.size() && !me.mparts[rp.part].empty())
+                mls = &me.mparts[rp.part];
+            if (mls) { flags |= SEG_MESHLET; F.any_mesh = true; }
             uint32_t sort_mode = mat.present ? (uint32_t)mat.sort_mode : 0u;
             flags |= sort_mode << 8;
             flags |= (uint32_t)(mat.present ? mat.lighting_mode : 0) << 10;
@@ -1148,26 +1296,44 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                 sg.tex_w = mat.tex_w; sg.tex_h = mat.tex_h;
             }
             sg.vscratch = (uint32_t)F.nscratch;
-            F.nscratch += sg.vcount;
             F.seg_vitem_first.push_back((uint32_t)F.vitem_seg.size());
-            {
+            if (!mls) {  // per-vertex records and vertex work items: record path only
+                F.nscratch += sg.vcount;
                 const uint32_t nch = (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
                 for (uint32_t c = 0; c < nch; c++) { F.vitem_seg.push_back((uint32_t)F.segs.size()); F.vitem_chunk.push_back(c); }
             }
             sg.out_base = (uint32_t)F.nslots;
             F.nslots += sg.tri_count;
-            uint32_t ntiles = (sg.tri_count + T - 1) / T;
+            uint32_t ntiles = mls ? (uint32_t)mls->size() : (sg.tri_count + T - 1) / T;
             if (ntiles == 0) ntiles = 1;
             sg.tile_first = (uint32_t)F.tiles.size();
             sg.ntiles = ntiles;
             const uint32_t s = (uint32_t)F.segs.size();
-            if (ntiles > 1) {
+            if (ntiles > 1 || mls) {  // every meshlet pair takes the multi-tile route
                 flags |= SEG_MULTI;
                 sg.mt_first = (uint32_t)F.mt_desc.size();
                 F.mt_segs.push_back(s);
             }
             sg.flags = flags;
-            for (uint32_t t = 0; t < ntiles; t++) {
+            if (mls) {
+                for (uint32_t t = 0; t < ntiles; t++) {
+                    const Meshlet& ml = (*mls)[t];
+                    TileDesc td;
+                    memset(&td, 0, sizeof td);
+                    td.seg = s; td.inst = sg.inst; td.job = j; td.flags = flags;
+                    td.t0 = ml.t0; td.t1 = ml.t0 + ml.nt;
+                    td.tbase = me.tbase;
+                    td.vmin = ml.nu; td.vlo = ml.off16; td.out_base = sg.out_base;
+                    const uint64_t addr = (uint64_t)(uintptr_t)sc->mlet.ptr + 16ull * ml.off16;  // read by the kernel
+                    td.vhi = (uint32_t)addr;
+                    td.pad1 = (uint32_t)(addr >> 32);
+                    td.mt = sg.mt_first + t;
+                    td.nearp = dj.cam.near_; td.farp = dj.cam.far_;
+                    F.tiles.push_back(td);
+                    F.mt_desc.push_back(td);
+                }
+            }
+            for (uint32_t t = 0; t < (mls ? 0u : ntiles); t++) {
                 TileDesc td;
                 memset(&td, 0, sizeof td);
                 td.seg = s; td.inst = sg.inst; td.job = j; td.flags = flags;
@@ -1188,7 +1354,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                     if (hi >= lo) { td.vlo = sg.vscratch + (lo - sg.vmin); td.vhi = sg.vscratch + (hi - sg.vmin) + 1; }
                 }
                 F.tiles.push_back(td);
-                if (ntiles > 1) F.mt_desc.push_back(td);
+                if (flags & SEG_MULTI) F.mt_desc.push_back(td);
             }
 
             sg.pad[0] = rp.draw | (rp.transparent << 31);  // flush and its pass, for the rasteriser
@@ -1204,7 +1370,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
             si.draw = rp.draw; si.draw_transparent = rp.transparent;
             F.seg_info.push_back(si);
-            F.seg_mt_seg.push_back(ntiles > 1 ? (uint32_t)F.mt_segs.size() - 1 : 0xFFFFFFFFu);
+            F.seg_mt_seg.push_back((flags & SEG_MULTI) ? (uint32_t)F.mt_segs.size() - 1 : 0xFFFFFFFFu);
         }
         F.job_seg_end.push_back((uint32_t)F.segs.size());
     }
@@ -1212,9 +1378,10 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
         set_err(ctx, "frame too large for 32-bit slots");
         return T3D_E_INVAL;
     }
-    F.tile_alt = (uint32_t)F.tiles.size();
+    F.tile_alt = F.tile_mesh = (uint32_t)F.tiles.size();
     F.vitem_alt = (uint32_t)F.vitem_seg.size();
-    if (F.any_altered) order_altered_items(ctx, F);
+    F.mt_mesh = (uint32_t)F.mt_desc.size();
+    if (F.any_altered || F.any_mesh) order_altered_items(ctx, F);
     // point the jobs at their light tables (device address known after upload)
     return T3D_OK;
 }
@@ -1222,7 +1389,9 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
 // Vertex items of parts with shape keys or skinning, and tiles of skinned
 // parts, move behind the others: the kernel runs them in loops of their own
 // (queues 5 and 7), so the loops of plain parts carry none of their code.
-// Each part's items stay contiguous and in order.
+// Meshlet tiles go last (tiles: plain | altered | meshlet) and their multi-tile
+// numbers after the record path's (mt_desc: record path | meshlet); each part's
+// items stay contiguous and in order.
 void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
     std::vector<TileDesc> tiles;
     std::vector<uint32_t> vseg, vch;
@@ -1231,15 +1400,16 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
     vch.reserve(F.vitem_chunk.size());
     const uint32_t nseg = (uint32_t)F.segs.size();
     std::vector<uint32_t> new_tile(nseg), new_vitem(nseg);
-    for (int pass = 0; pass < 2; pass++) {
+    auto tile_class = [](uint32_t f) { return (f & SEG_MESHLET) ? 2 : (f & SEG_ALT_TILES) ? 1 : 0; };
+    for (int pass = 0; pass < 3; pass++) {
         for (uint32_t s = 0; s < nseg; s++) {
             const DevSeg& sg = F.segs[s];
-            if (((sg.flags & SEG_ALT_TILES) != 0) == (pass == 1)) {
+            if (tile_class(sg.flags) == pass) {
                 new_tile[s] = (uint32_t)tiles.size();
                 tiles.insert(tiles.end(), F.tiles.begin() + sg.tile_first, F.tiles.begin() + sg.tile_first + sg.ntiles);
             }
-            if (((sg.flags & SEG_ALTERED) != 0) == (pass == 1)) {
-                const uint32_t nch = (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
+            if (pass < 2 && ((sg.flags & SEG_ALTERED) != 0) == (pass == 1)) {
+                const uint32_t nch = (sg.flags & SEG_MESHLET) ? 0u : (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
                 const uint32_t f = F.seg_vitem_first[s];
                 new_vitem[s] = (uint32_t)vseg.size();
                 vseg.insert(vseg.end(), F.vitem_seg.begin() + f, F.vitem_seg.begin() + f + nch);
@@ -1249,6 +1419,8 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
         if (pass == 0) {
             F.tile_alt = (uint32_t)tiles.size();
             F.vitem_alt = (uint32_t)vseg.size();
+        } else if (pass == 1) {
+            F.tile_mesh = (uint32_t)tiles.size();
         }
     }
     for (uint32_t s = 0; s < nseg; s++) {
@@ -1258,6 +1430,25 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
     F.tiles.swap(tiles);
     F.vitem_seg.swap(vseg);
     F.vitem_chunk.swap(vch);
+    // multi-tile numbers: the record path's first, then the meshlet pairs'
+    std::vector<TileDesc> mt;
+    mt.reserve(F.mt_desc.size());
+    for (int pass = 0; pass < 2; pass++) {
+        for (uint32_t s = 0; s < nseg; s++) {
+            DevSeg& sg = F.segs[s];
+            if (!(sg.flags & SEG_MULTI) || ((sg.flags & SEG_MESHLET) != 0) != (pass == 1)) continue;
+            const uint32_t first = (uint32_t)mt.size();
+            for (uint32_t t = 0; t < sg.ntiles; t++) {
+                TileDesc td = F.mt_desc[sg.mt_first + t];
+                td.mt = first + t;
+                F.tiles[sg.tile_first + t].mt = first + t;
+                mt.push_back(td);
+            }
+            sg.mt_first = first;
+        }
+        if (pass == 0) F.mt_mesh = (uint32_t)mt.size();
+    }
+    F.mt_desc.swap(mt);
 }
 
 template <typename T> static size_t bytes_of(const std::vector<T>& v) { return v.size() * sizeof(T); }
@@ -1336,6 +1527,11 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
         return rc;
     P.preps = (DevPrep*)ctx->preps.ptr;
+    P.inst_lights = nullptr;
+    if (F.any_mesh) {  // the instances' staged light lists (meshlet rank phase)
+        if ((rc = ctx->inst_lights.ensure(ctx, 56ull * kMaxLights * ninst + 16))) return rc;
+        P.inst_lights = (float4*)ctx->inst_lights.ptr;
+    }
 
     P.vcull = (float4*)ctx->vcull.ptr;
     P.valt = (float4*)ctx->valt.ptr;
@@ -1355,19 +1551,25 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.accum = (unsigned long long*)ctx->accum.ptr;
     P.tile_tris = ctx->tile_tris;
     P.vchunk = ctx->vchunk;
+    P.mesh_ucap = ctx->mesh_ucap;
+    P.spin_limit = ctx->spin_limit;
     return T3D_OK;
 }
 
 static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items, cudaStream_t st) {
     P.ctl = ctl;
-    uint32_t grid = std::max(1u, std::min(ctx->max_grid, max_items));
-    const void* fn = t3d_frame_kernel_ptr();
+    // frames with meshlet tiles run the instantiation that has their phases
+    const bool mesh = P.mesh_begin < P.mesh_end;
+    const uint32_t cap = mesh ? ctx->max_grid_mesh : ctx->max_grid;
+    const size_t smem = mesh ? ctx->smem_mesh : ctx->smem_bytes;
+    uint32_t grid = std::max(1u, std::min(cap, max_items));
+    const void* fn = mesh ? t3d_frame_kernel_mesh_ptr() : t3d_frame_kernel_ptr();
     void* args[] = {&P};
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof cfg);
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(ctx->block_threads);
-    cfg.dynamicSmemBytes = ctx->smem_bytes;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -1377,7 +1579,7 @@ static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items,
     cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
     if (e != cudaSuccess) {
         set_err(ctx, "frame kernel launch failed: %s (grid %u, block %u, smem %zu)", cudaGetErrorString(e), grid,
-                ctx->block_threads, ctx->smem_bytes);
+                ctx->block_threads, smem);
         return T3D_E_CUDA;
     }
     ctx->launches++;
@@ -1401,8 +1603,10 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         FrameParams P = P0;
         P.inst_begin = 0; P.inst_end = (uint32_t)F.insts.size();
         P.seg_begin = 0; P.seg_end = (uint32_t)F.segs.size();
-        P.tile_begin = 0; P.tile_end = (uint32_t)F.tiles.size();
-        P.mt_tile_begin = 0; P.mt_tile_end = (uint32_t)F.mt_desc.size();
+        P.tile_begin = 0; P.tile_end = F.tile_mesh;
+        P.mesh_begin = F.tile_mesh; P.mesh_end = (uint32_t)F.tiles.size();
+        P.mt_tile_begin = 0; P.mt_tile_end = F.mt_mesh;
+        P.mt_mesh_begin = F.mt_mesh; P.mt_mesh_end = (uint32_t)F.mt_desc.size();
         P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
 
         P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
@@ -1421,19 +1625,26 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         FrameParams P = P0;
         P.inst_begin = sg.inst; P.inst_end = sg.inst + 1;
         P.seg_begin = (uint32_t)s; P.seg_end = (uint32_t)s + 1;
-        P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
-        P.vitem_begin = F.seg_vitem_first[s];
-        P.vitem_end = P.vitem_begin + (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
-        P.tile_alt = (sg.flags & SEG_ALT_TILES) ? P.tile_begin : P.tile_end;
-        P.vitem_alt = (sg.flags & SEG_ALTERED) ? P.vitem_begin : P.vitem_end;
-        if (sg.flags & SEG_MULTI) {
-            P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles;
-            P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;
-
-            P.has_multi = 1;
+        const bool mesh = sg.flags & SEG_MESHLET;
+        if (mesh) {
+            P.tile_begin = P.tile_alt = P.tile_end = 0;
+            P.mesh_begin = sg.tile_first; P.mesh_end = sg.tile_first + sg.ntiles;
+            P.vitem_begin = P.vitem_alt = P.vitem_end = 0;
         } else {
-            P.mt_tile_begin = P.mt_tile_end = 0; P.mt_seg_begin = P.mt_seg_end = 0; P.has_multi = 0;
-
+            P.tile_begin = sg.tile_first; P.tile_end = sg.tile_first + sg.ntiles;
+            P.mesh_begin = P.mesh_end = 0;
+            P.vitem_begin = F.seg_vitem_first[s];
+            P.vitem_end = P.vitem_begin + (sg.vcount + ctx->vchunk - 1) / ctx->vchunk;
+            P.tile_alt = (sg.flags & SEG_ALT_TILES) ? P.tile_begin : P.tile_end;
+            P.vitem_alt = (sg.flags & SEG_ALTERED) ? P.vitem_begin : P.vitem_end;
+        }
+        P.mt_tile_begin = P.mt_tile_end = 0; P.mt_mesh_begin = P.mt_mesh_end = 0;
+        P.mt_seg_begin = P.mt_seg_end = 0; P.has_multi = 0;
+        if (sg.flags & SEG_MULTI) {
+            if (mesh) { P.mt_mesh_begin = sg.mt_first; P.mt_mesh_end = sg.mt_first + sg.ntiles; }
+            else { P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles; }
+            P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;
+            P.has_multi = 1;
         }
         // animation must be applied once: host tables carry the flag on the instance,
         // so later pairs of the same model use a copy without it.

@@ -31,6 +31,11 @@ struct ScenePart {
     t3d_part_desc d;
     uint32_t vmin = 0, vcount = 0;  // vertex range referenced by the part's triangles
 };
+// One meshlet of a part (t3d_device.cuh): triangles [t0, t0 + nt) of the mesh with
+// nu distinct vertices, stored at byte 16 * off16 of the scene's meshlet pool.
+struct Meshlet {
+    uint32_t t0, nt, nu, off16;
+};
 struct SceneMesh {
     uint32_t vbase = 0, tbase = 0, nverts = 0, ntris = 0;
     bool colors = false;
@@ -43,6 +48,7 @@ struct SceneMesh {
     bool skin = false;                                      // joints and weights present
     uint32_t max_joint = 0;
     bool subdiv = false;  // auto-subdivided: parts list each triangle followed by its subdivision levels
+    std::vector<std::vector<Meshlet>> mparts;  // per part: its meshlets (empty: the part has none)
 };
 struct SceneModel {
     t3d_model_desc d;  // host mirror (rotation advanced with every animated frame)
@@ -61,6 +67,8 @@ struct Scene {
     DevBuf vaS, vbS;  // keyed streams of the shape-keyed meshes (baked per weight set)
     bool joint8 = false;  // vjoint holds four 8-bit joints per vertex (every joint below 256)
     DevBuf sub_info, sub_rel, sub_levels, cell_use_off, cell_use_items;
+    DevBuf mlet;                         // meshlet pool
+    uint32_t mlet_T = 0, mlet_U = 0;     // triangle and vertex budgets the meshlets were cut for (0: none)
     std::vector<char> light_uses;    // per light: a volume whose cells use lights
     std::vector<char> light_nested;  // per light: used by some cell (cannot become a volume)
     std::vector<uint32_t> cell_use_host;  // host copy of the cell use offsets
@@ -71,9 +79,10 @@ struct Scene {
     uint64_t device_bytes() const {
         return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap + vaS.cap + vbS.cap +
                shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap + sub_info.cap + sub_rel.cap +
-               sub_levels.cap + cell_use_off.cap + cell_use_items.cap;
+               sub_levels.cap + cell_use_off.cap + cell_use_items.cap + mlet.cap;
     }
     void release() {
+        mlet.release(); mlet_T = mlet_U = 0;
         sub_info.release(); sub_rel.release(); sub_levels.release(); cell_use_off.release(); cell_use_items.release();
         shape_a.release(); shape_b.release(); vaS.release(); vbS.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
         va.release(); vb.release(); vc.release(); idx.release(); centers.release();
@@ -96,14 +105,17 @@ struct FrameTables {
     std::vector<uint32_t> mt_segs;
     std::vector<uint32_t> vitem_seg, vitem_chunk, seg_vitem_first;
     uint64_t nscratch = 0, nslots = 0;
-    bool any_skinned = false, any_altered = false;
+    bool any_skinned = false, any_altered = false, any_mesh = false;
     uint32_t tile_alt = 0, vitem_alt = 0;  // first tile of a skinned part / vertex item of an altered part
+    uint32_t tile_mesh = 0;                // first meshlet tile (tiles: record-path plain | record-path altered | meshlet)
+    uint32_t mt_mesh = 0;                  // first meshlet multi-tile number (mt_desc: record path | meshlet)
     void clear() {
         jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
         insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
         seg_mt_seg.clear(); tiles.clear(); mt_desc.clear(); mt_segs.clear();
         vitem_seg.clear(); vitem_chunk.clear(); seg_vitem_first.clear();
-        nscratch = 0; nslots = 0; any_skinned = false; any_altered = false; tile_alt = 0; vitem_alt = 0;
+        nscratch = 0; nslots = 0; any_skinned = false; any_altered = false; any_mesh = false; tile_alt = 0; vitem_alt = 0;
+        tile_mesh = 0; mt_mesh = 0;
     }
 };
 
@@ -121,6 +133,12 @@ struct t3d_ctx {
     uint32_t tile_tris = 2048, vchunk = 4096, block_threads = 256;
     uint32_t max_grid = 0;   // co-resident blocks for the current tuning
     size_t smem_bytes = 0;
+    // the kernel instantiation for frames with meshlet tiles
+    uint32_t mesh_ucap = 0;       // distinct vertices per meshlet (0: meshlets off)
+    uint32_t max_grid_mesh = 0;
+    size_t smem_mesh = 0;
+    bool use_meshlets = true;     // t3d_set_meshlets: 0 sends every pair through the per-vertex record path
+    uint32_t spin_limit = 0;      // bounded device waits (0: the kernel's default)
     uint32_t next_scene = 1;
     std::map<uint32_t, std::unique_ptr<t3d::Scene>> scenes;
     t3d_ctx* scene_owner = nullptr;  // serving slots render the parent context's scenes
@@ -137,7 +155,7 @@ struct t3d_ctx {
     cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
     cudaEvent_t ev_models = nullptr;  // the last model write has reached the device (and left its staging)
     struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
-    t3d::DevBuf valt;
+    t3d::DevBuf valt, inst_lights;
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
@@ -167,4 +185,5 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st);
 int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st);
 int configure(t3d_ctx* ctx);
 int bake_shapes(t3d_ctx* ctx, Scene* sc, uint32_t mesh);
+int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U);
 }  // namespace t3d

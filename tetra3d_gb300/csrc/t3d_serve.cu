@@ -210,6 +210,8 @@ int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batc
         sl.ctx->tile_tris = ctx->tile_tris;
         sl.ctx->vchunk = ctx->vchunk;
         sl.ctx->block_threads = ctx->block_threads;
+        sl.ctx->use_meshlets = ctx->use_meshlets;
+        sl.ctx->spin_limit = ctx->spin_limit;
         configure(sl.ctx);
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
     }

@@ -55,6 +55,15 @@ class Context:
     def set_tuning(self, tile_tris=0, vertex_chunk=0, block_threads=0):
         self._check(self.lib.t3d_set_tuning(self.h, tile_tris, vertex_chunk, block_threads), "set_tuning")
 
+    def set_meshlets(self, enable):
+        """Meshlet route for plain render pairs (default on); off sends every pair through the
+        per-vertex record path. The emitted stream is the same either way."""
+        self._check(self.lib.t3d_set_meshlets(self.h, int(bool(enable))), "set_meshlets")
+
+    def set_wait_limit(self, polls):
+        """Polls a bounded device wait makes before the frame gives up (0: the default)."""
+        self._check(self.lib.t3d_set_wait_limit(self.h, int(polls)), "set_wait_limit")
+
     def upload(self, scene_data):
         sd = scene_data.desc()
         sid = C.c_uint32()
