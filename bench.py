@@ -45,17 +45,17 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(workload):
-    """DRAM bytes per launch of the frame kernel from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", f"t3d_frame_kernel_{workload}.md")
-    if not os.path.exists(p):
-        return None, None
-    with open(p) as f:
-        for line in f:
-            if line.startswith("traffic_bytes_per_launch:"):
-                v = line.split(":", 1)[1].strip().split()[0]
-                return float(v), os.path.relpath(p, ROOT)
-    return None, os.path.relpath(p, ROOT)
+def cpu_model():
+    """The host CPU's model name (lscpu), stated beside the CPU arms' core counts."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 class ClockSampler:
@@ -132,21 +132,16 @@ def workload_config(workload, sd):
     return base
 
 
-def cpu_sample(sd, workload):
-    """Bounded sample of the workload for the CPU arms: every k-th model."""
-    from tetra3d_gb300 import scenes
-    if workload == "batched":
-        idx = np.arange(0, sd.nmodels, 16)
-        return scenes.subset(sd, idx), f"{len(idx)} of {sd.nmodels} models (every 16th), 1 frame"
-    return sd, "full scene, 1 frame"
-
-
-def time_cpu(sd_sample, cam, threads, min_seconds=10.0, max_reps=50):
+def time_cpu(sd, cam, threads, animated, min_seconds=10.0, max_reps=50, first_frame=1):
+    """The oracle (the reference's path restated on the CPU) on whole frames of the workload:
+    frame k applies every model's animation step k times, as the k-th graph replay does.
+    Repeats until min_seconds have passed. Returns (visible tris/s, frames, seconds)."""
     from oracle import pyoracle
     reps, vis, t0 = 0, 0, time.perf_counter()
     while True:
-        f = pyoracle.render(sd_sample, cam, threads=threads)
+        f = pyoracle.render(sd, cam, animate_frames=(first_frame + reps) if animated else 0, threads=threads)
         vis += f.visible_tris
+        del f
         reps += 1
         el = time.perf_counter() - t0
         if el >= min_seconds or reps >= max_reps:
@@ -342,18 +337,17 @@ def run_ours(args, rank, world, local_rank):
         serve = serving_sweep(ctx, [int(r) for r in args.rates.split(",")], args.serve_seconds,
                               args.serve_max_requests)
 
-    # ---- CPU baseline (oracle port, 1 thread) ----
+    # ---- CPU baseline (the oracle port on all host threads, whole frames of the same workload) ----
     cpu = None
     if rank == 0 and not args.no_cpu:
-        sample, desc = cpu_sample(sd, args.workload)
-        rate, reps, el = time_cpu(sample, cam, threads=1, min_seconds=args.cpu_seconds)
-        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{desc}; {reps} repetitions in {el:.1f} s, static transforms"}
+        threads = os.cpu_count() or 1
+        rate, reps, el = time_cpu(sd, cam, threads, animate, min_seconds=args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "cpu_model": cpu_model(), "kind": "port",
+               "sample": f"{reps} whole frames ({sd.nmodels} models{', animated' if animate else ''}) in {el:.1f} s"}
 
     if rank == 0:
         peak, peak_kind = peaks()
         achieved = alg_bytes / (ms / 1e3) / 1e9 / max(1, world)
-        traffic, tsrc = profile_traffic(args.workload)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -361,9 +355,10 @@ def run_ours(args, rank, world, local_rank):
             "config": dict(workload_config(args.workload, sd), form="batched persistent kernel, CUDA graph replay",
                            animated=animate, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                         "frac": achieved / peak, "traffic": None, "peak_source": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_step": alg_bytes / args.steps / max(1, world),
-                         "traffic_source": tsrc},
+                         "traffic_note": "DRAM bytes per launch are not measurable inside this run (ncu only); "
+                                         "the capture of this kernel is summarised in profiles/"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk.summary(),
@@ -511,40 +506,35 @@ def run_serving(args, rank, world, local_rank):
 
 # ------------------------------------------------------------ reference ----
 def run_reference(args, rank, world):
+    """The reference's path for the same workload, config and metric on the host cores: the
+    oracle (Camera.Render restated on the CPU; the Go reference cannot run here) renders
+    every model of every frame, frame k with every model's animation step applied k times,
+    exactly the frames the GPU arm's graph replays render. Steps are whole frames."""
     if rank != 0:
         return
     sd = make_scene(args.workload, args.models)
-    sample, desc = cpu_sample(sd, args.workload)
     from oracle import pyoracle
-    from tetra3d_gb300 import scenes
     threads = os.cpu_count() or 1
-    # size each step so the whole run stays within about two minutes
-    budget = 120.0 / max(1, args.steps + args.warmup)
-    stride = 16
-    while True:
-        t0 = time.perf_counter()
-        pyoracle.render(sample, sd.camera, threads=threads)
-        dt = time.perf_counter() - t0
-        if dt <= budget or args.workload != "batched" or stride >= 1024:
-            break
-        stride *= 2
-        idx = np.arange(0, sd.nmodels, stride)
-        sample, desc = scenes.subset(sd, idx), f"{len(idx)} of {sd.nmodels} models (every {stride}th), 1 frame"
-    for _ in range(args.warmup):
-        pyoracle.render(sample, sd.camera, threads=threads)
+    animate = args.workload == "batched"
+    for w in range(args.warmup):
+        pyoracle.render(sd, sd.camera, animate_frames=(w + 1) if animate else 0, threads=threads)
     vis = 0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        vis += pyoracle.render(sample, sd.camera, threads=threads).visible_tris
+    for k in range(args.steps):
+        f = pyoracle.render(sd, sd.camera, animate_frames=(args.warmup + k + 1) if animate else 0, threads=threads)
+        vis += f.visible_tris
+        del f
     el = time.perf_counter() - t0
     value = vis / el
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": dict(workload_config(args.workload, sd), form="CPU restatement of Camera.Render"),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{desc} per step, render pairs split over {threads} host threads"},
+            "config": dict(workload_config(args.workload, sd), form="CPU restatement of Camera.Render",
+                           animated=animate),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "cpu_model": cpu_model(), "kind": "port",
+                             "sample": f"whole frames ({sd.nmodels} models{', animated' if animate else ''}), "
+                                       f"render pairs split over {threads} host threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
