@@ -456,7 +456,15 @@ def serving_sweep(ctx, rates, seconds, max_requests, seed=7, baseline_requests=1
         # saturation: the last rate's requests all arrive at once (the server's capacity)
         w0 = time.perf_counter()
         comps = srv.replay(jobs, np.zeros(len(jobs)))
-        out["burst"] = dict(**serving.latency_summary(comps), wall_s=round(time.perf_counter() - w0, 3))
+        bwall = time.perf_counter() - w0
+        out["burst"] = dict(**serving.latency_summary(comps), wall_s=round(bwall, 3))
+        # served roofline: the burst's algorithmic bytes over its wall time (all requests queued at
+        # once: the server's capacity), against the measured HBM bandwidth
+        peak, peak_kind = peaks()
+        gbs = out["burst"]["algorithmic_bytes"] / bwall / 1e9
+        out["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                           "peak_source": f"{peak_kind} hbm_gbs",
+                           "note": "burst of the last rate's requests: algorithmic bytes / wall time incl. host work"}
         # one request per launch, synchronously, over the last rate's requests
         jobs = jobs[:baseline_requests]
         lat, vis = [], 0

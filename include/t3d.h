@@ -449,11 +449,14 @@ typedef struct t3d_completion {
     double   admit_s;
     double   done_s;
     uint64_t checksum;        /* order-dependent hash of the emitted stream */
+    uint64_t model_bytes;     /* 48V+12T+64+48L bytes of the request's models that survived
+                                 frustum culling (with 108 per visible triangle: its algorithmic bytes) */
 } t3d_completion;
 
 /* hbm_budget_bytes bounds the device bytes of in-flight requests' outputs and
  * scratch; max_batch bounds the jobs per launch; streams = launch slots that
- * run concurrently. The slots render the context's resident scenes: while a
+ * run concurrently. Each slot's launches use 1/streams of the device's
+ * co-resident blocks, so the launches of all slots fit on the device together. The slots render the context's resident scenes: while a
  * server runs, scenes are not uploaded, released or changed (set_models /
  * set_bones / set_shape_weights / set_lights) on that context. */
 int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batch,

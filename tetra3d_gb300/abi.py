@@ -126,7 +126,7 @@ class Request(C.Structure):
 class Completion(C.Structure):
     _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
                 ("visible_tris", C.c_uint64), ("arrival_s", C.c_double), ("admit_s", C.c_double),
-                ("done_s", C.c_double), ("checksum", C.c_uint64)]
+                ("done_s", C.c_double), ("checksum", C.c_uint64), ("model_bytes", C.c_uint64)]
 
 
 class NoallocArgs(C.Structure):

@@ -283,6 +283,8 @@ struct FrameParams {
     // meshlet frames: per instance, kMaxLights records of 56 bytes (the light list
     // the vertex loop reads, staged once by the prep phase); null otherwise
     float4* inst_lights;
+    // per job: algorithmic bytes of its models that survive frustum culling (serving); may be null
+    unsigned long long* job_bytes;
 };
 // Dense visible list of a meshlet tile i: depth keys at vis_depth + i * tile_tris,
 // 3 slots per entry at vis_vloc + 3 * i * tile_tris, tile_count[i] entries.

@@ -276,6 +276,7 @@ __device__ __noinline__ void phase_prep(const FrameParams& P) {
         } else {
             atomicAdd(&P.ctl->bytes, (unsigned long long)in.bytes);
             atomicAdd(&P.accum[1], (unsigned long long)in.bytes);
+            if (P.job_bytes) atomicAdd(&P.job_bytes[in.job], (unsigned long long)in.bytes);
         }
         // Mesh.Dimensions.MaxSpan for the model-level point-light skip (camera.go:1625-1629)
         pr.maxspan = mag3(mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]));

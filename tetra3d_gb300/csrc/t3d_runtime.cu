@@ -1527,6 +1527,11 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
         return rc;
     P.preps = (DevPrep*)ctx->preps.ptr;
+    P.job_bytes = nullptr;
+    if (ctx->want_job_bytes) {
+        if ((rc = ctx->job_bytes.ensure(ctx, 8ull * std::max<size_t>(1, F.jobs.size())))) return rc;
+        P.job_bytes = (unsigned long long*)ctx->job_bytes.ptr;
+    }
     P.inst_lights = nullptr;
     if (F.any_mesh) {  // the instances' staged light lists (meshlet rank phase)
         if ((rc = ctx->inst_lights.ensure(ctx, 56ull * kMaxLights * ninst + 16))) return rc;
@@ -1560,7 +1565,7 @@ static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items,
     P.ctl = ctl;
     // frames with meshlet tiles run the instantiation that has their phases
     const bool mesh = P.mesh_begin < P.mesh_end;
-    const uint32_t cap = mesh ? ctx->max_grid_mesh : ctx->max_grid;
+    const uint32_t cap = std::max(1u, (mesh ? ctx->max_grid_mesh : ctx->max_grid) / ctx->grid_share);
     const size_t smem = mesh ? ctx->smem_mesh : ctx->smem_bytes;
     uint32_t grid = std::max(1u, std::min(cap, max_items));
     const void* fn = mesh ? t3d_frame_kernel_mesh_ptr() : t3d_frame_kernel_ptr();
@@ -1596,6 +1601,10 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
     if ((rc = ctx->ctl.ensure(ctx, sizeof(Ctl) * nlaunch))) return rc;
     cudaError_t e = cudaMemsetAsync(ctx->ctl.ptr, 0, sizeof(Ctl) * nlaunch, st);
     if (e != cudaSuccess) { set_err(ctx, "ctl memset: %s", cudaGetErrorString(e)); return T3D_E_CUDA; }
+    if (P0.job_bytes && (e = cudaMemsetAsync(ctx->job_bytes.ptr, 0, 8ull * std::max<size_t>(1, F.jobs.size()), st)) != cudaSuccess) {
+        set_err(ctx, "job bytes memset: %s", cudaGetErrorString(e));
+        return T3D_E_CUDA;
+    }
     Ctl* ctl = (Ctl*)ctx->ctl.ptr;
     ctx->nctl = (uint32_t)nlaunch;
     if (F.segs.empty() && F.insts.empty()) return T3D_OK;

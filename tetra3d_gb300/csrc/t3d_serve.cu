@@ -92,6 +92,10 @@ struct t3d_server {
         if (rc == T3D_OK) rc = t3d_frame_sync(s.ctx, &st);
         const double t = now();
         std::vector<uint64_t> vis(s.batch.size(), 0), sum(s.batch.size(), 1469598103934665603ull);
+        std::vector<unsigned long long> jb(s.batch.size(), 0ull);
+        if (rc == T3D_OK && !jb.empty() &&
+            cudaMemcpy(jb.data(), s.ctx->job_bytes.ptr, 8 * jb.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = T3D_E_CUDA;
         if (rc == T3D_OK) {
             const auto& info = s.ctx->tables.seg_info;
             for (const auto& si : info)
@@ -126,6 +130,7 @@ struct t3d_server {
             c.admit_s = s.batch[k].admit_abs;
             c.done_s = t;
             c.checksum = (verify && rc == T3D_OK) ? sum[k] : 0;
+            c.model_bytes = rc == T3D_OK ? jb[k] : 0;
             done.push_back(c);
         }
         inflight -= s.bytes;
@@ -168,10 +173,18 @@ struct t3d_server {
                 std::unique_lock<std::mutex> g(mu);
                 while (!admit(s)) {
                     if (stop.load() && queue.empty()) return;
-                    // sleep until a submit, a completion, or the next replayed arrival
-                    double wait_s = 200e-6;
-                    if (!queue.empty()) wait_s = std::min(wait_s, std::max(10e-6, queue.front().arrival_abs - now()));
-                    cv.wait_for(g, std::chrono::duration<double>(wait_s));
+                    // a replayed arrival due within 100 us is waited for by polling the clock (a timed
+                    // sleep overshoots by tens of microseconds); otherwise sleep until a submit, a
+                    // completion or shortly before the next arrival
+                    const double due = queue.empty() ? 1.0 : queue.front().arrival_abs - now();
+                    if (due < 100e-6) {
+                        g.unlock();
+                        const double until = now() + std::max(0.0, due);
+                        while (now() < until) std::this_thread::yield();
+                        g.lock();
+                        continue;
+                    }
+                    cv.wait_for(g, std::chrono::duration<double>(std::min(200e-6, due - 60e-6)));
                 }
                 inflight += s.bytes;
             }
@@ -212,6 +225,11 @@ int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batc
         sl.ctx->block_threads = ctx->block_threads;
         sl.ctx->use_meshlets = ctx->use_meshlets;
         sl.ctx->spin_limit = ctx->spin_limit;
+        sl.ctx->want_job_bytes = true;
+        // the slots' launches share the device: each takes 1/streams of the co-resident
+        // blocks, so every slot's cooperative grid fits beside the others' (grid barriers
+        // need all of a launch's blocks resident at once)
+        sl.ctx->grid_share = streams;
         configure(sl.ctx);
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
     }

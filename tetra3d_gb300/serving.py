@@ -83,7 +83,10 @@ def latency_summary(completions):
     lat = np.array([(c.done_s - c.arrival_s) * 1e3 for c in ok]) if ok else np.zeros(1)
     span = (max(c.done_s for c in ok) - min(c.arrival_s for c in ok)) if ok else 0.0
     tris = sum(int(c.visible_tris) for c in ok)
-    return {"requests": len(completions), "ok": len(ok),
+    # algorithmic bytes (48V+12T+64+48L of surviving models + 108 per visible triangle)
+    alg = sum(int(c.model_bytes) + 108 * int(c.visible_tris) for c in ok)
+    return {"requests": len(completions), "ok": len(ok), "algorithmic_bytes": alg,
+            "algorithmic_gb_per_s": alg / span / 1e9 if span > 0 else 0.0,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "max_ms": float(lat.max()), "tris_per_s": tris / span if span > 0 else 0.0,
             "req_per_s": len(ok) / span if span > 0 else 0.0, "visible_tris": tris}
