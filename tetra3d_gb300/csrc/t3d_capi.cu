@@ -47,7 +47,8 @@ int configure(t3d_ctx* ctx) {
     CKR(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, ctx->device));
     CKR(cudaDeviceGetAttribute(&block_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
     const size_t budget = std::min<size_t>((size_t)block_max, (size_t)(sm_bytes / 2 - reserved));
-    uint32_t U = std::min<uint32_t>(3 * ctx->tile_tris, 65504u) & ~31u;
+    // meshlet tiles hold at most 2048 triangles (their rank words keep 11-bit entry numbers)
+    uint32_t U = ctx->tile_tris <= 2048 ? std::min<uint32_t>(3 * ctx->tile_tris, 65504u) & ~31u : 0u;
     while (U >= 64 && t3d_frame_smem_bytes_mesh(ctx->tile_tris, ctx->block_threads, U) > budget) U -= 32;
     if (U >= 64) {
         const size_t smem = t3d_frame_smem_bytes_mesh(ctx->tile_tris, ctx->block_threads, U);
@@ -122,7 +123,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights,
-                      &ctx->job_bytes})
+                      &ctx->job_bytes, &ctx->vis_rank})
         b->release();
     ctx->table_host.release();
     ctx->readback.release();
@@ -465,7 +466,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     size_t scratch = 0;
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count,
-                      &ctx->inst_lights})
+                      &ctx->inst_lights, &ctx->vis_rank})
         scratch += b->cap;
     s.scratch_bytes = scratch;
     s.h2d_bytes = ctx->last_h2d;

@@ -44,6 +44,8 @@ enum : uint32_t {
     SEG_SNAP = 1u << 23,        // Camera.VertexSnapping > 0
     SEG_NESTED = 1u << 24,      // a light volume of the pair's list has cells that use lights
     SEG_MESHLET = 1u << 25,     // tiles are meshlets: contiguous vertex blocks with 16-bit local indices
+    SEG_SINGLE = 1u << 26,      // a meshlet pair of one tile: its output order is its rank order (no
+                                // histogram or cross-tile scan)
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
@@ -245,6 +247,9 @@ struct FrameParams {
     float4* vxyuv;                // emitted screen position + UV
     float4* vrgba;                // emitted colour
     float4* valt;                 // skinned pairs: world-space skinned position per record (depth key)
+    // meshlet tiles: per visible entry in the tile's output order, its list entry j (bits 0-10),
+    // bin (11-19) and position among the tile's entries of that bin (20-30), from the histogram phase
+    uint32_t* vis_rank;
     // per multi-tile tile, tile_tris entries in blockDim/32 regions (one per warp of the
     // triangle phase, tile_tris/(blockDim/32) entries each, filled from the front)
     uint16_t* vis_idx;            // triangle within the tile (SEG_WIDE only)

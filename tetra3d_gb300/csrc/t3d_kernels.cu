@@ -554,7 +554,8 @@ __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t 
 // model-level point-range skip (camera.go:1625-1629).
 // The per-pair constants of the vertex loop: MVP columns (billboarded when the
 // material says so), model matrix, directional-light rotation and the emit constants.
-template <bool kSkin>
+// kStreams = false (meshlet tiles): the vertex stream bases are not needed.
+template <bool kSkin, bool kStreams = true>
 __device__ void stage_model_consts(const DevSeg& seg, const DevJob& J, const DevPrep& pr, ModelSmem& ms) {
     float* mvpc = reinterpret_cast<float*>(ms.mvpc);
     const bool bb = seg.flags & SEG_BILLBOARD;  // either loop: a billboard only changes the MVP
@@ -567,7 +568,6 @@ __device__ void stage_model_consts(const DevSeg& seg, const DevJob& J, const Dev
     }
     if (threadIdx.x == 0) {
         const JobCam& cam = J.cam;
-        const DevMesh& me = J.meshes[seg.mesh];
         EmitConst& e = ms.ec;
         e.W = cam.W; e.H = cam.H; e.halfW = cam.halfW; e.halfH = cam.halfH;
         e.margin = cam.margin; e.spread = cam.spread; e.tex_w = seg.tex_w; e.tex_h = seg.tex_h;
@@ -609,11 +609,13 @@ __device__ void stage_model_consts(const DevSeg& seg, const DevJob& J, const Dev
         }
         e.flags = f;
         e.seg_flags = seg.flags;
-        // shape-keyed meshes read their keyed streams (baked once per weight set)
-        e.va = me.nkeys ? J.vaS + me.sbase : J.va + me.vbase;
-        e.vb = me.nkeys ? J.vbS + me.sbase : J.vb + me.vbase;
-        e.vc = J.vc + me.vbase;
-        e.idx = J.idx + 3 * (size_t)me.tbase;
+        if (kStreams) {  // shape-keyed meshes read their keyed streams (baked once per weight set)
+            const DevMesh& me = J.meshes[seg.mesh];
+            e.va = me.nkeys ? J.vaS + me.sbase : J.va + me.vbase;
+            e.vb = me.nkeys ? J.vbS + me.sbase : J.vb + me.vbase;
+            e.vc = J.vc + me.vbase;
+            e.idx = J.idx + 3 * (size_t)me.tbase;
+        }
         e.cells = J.cells;
     }
 }
@@ -1383,6 +1385,94 @@ __device__ __noinline__ void phase_triangles_skinned(const FrameParams& P, unsig
     triangle_tiles<true>(P, smem);
 }
 
+// P2 for one meshlet tile, by one warp: the tile's bin counts (written for the
+// cross-tile scan unless the pair has one tile), their exclusive scan in the
+// pair's walk order, then the stable ranking of its dense list (entries in
+// triangle order, 32 at a time, equal bins ranked by lane with match_any): entry
+// j of bin b at local rank r gets the word j | b << 11 | (r - first rank of b) << 20
+// at position r of the tile's rank list. wh and run: kBins counters each.
+__device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i, const TileDesc& td, uint32_t* wh,
+                                               uint32_t* run, uint16_t* sb) {
+    const uint32_t lane = threadIdx.x & 31, T = P.tile_tris;
+    const uint32_t n = __ldcg(&P.tile_count[i]);
+    const uint32_t s = td.seg;
+    const bool single = td.flags & SEG_SINGLE;
+    for (uint32_t b = lane; b < kBins; b += 32) { wh[b] = 0u; run[b] = 0u; }
+    __syncwarp();
+    const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
+    const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
+    const float range = range_of(mn, mx);
+    const uint32_t sort_mode = seg_sort_mode(td.flags);
+    {  // bins of the dense list (kept in sb for the ranking) and their counts; 4 loads in flight per lane
+        const float4* rd = reinterpret_cast<const float4*>(P.vis_depth + (size_t)i * T);
+        const uint32_t nq = (n + 3) / 4;
+        for (uint32_t q0 = lane; q0 < nq; q0 += 128) {
+            float4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (q0 + 32 * u < nq) v[u] = __ldcg(&rd[q0 + 32 * u]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t j = 4 * (q0 + 32 * u);
+                if (j >= n) break;
+                const float d[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    if (j + e < n) {
+                        const uint32_t b = bin_of(d[e], mn, range, sort_mode);
+                        sb[j + e] = (uint16_t)b;
+                        atomicAdd(&wh[b], 1u);
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (!single) {
+        uint32_t* out = P.tile_hist + (size_t)i * kBins;
+        for (uint32_t b = lane; b < kBins; b += 32) out[b] = wh[b];
+    }
+    // exclusive scan in walk order: lane l owns walk positions [16 l, 16 l + 16)
+    {
+        constexpr uint32_t kPer = kBins / 32;
+        uint32_t c[kPer], sum = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < kPer; u++) {
+            c[u] = wh[walk_pos(lane * kPer + u, sort_mode)];  // walk_pos maps walk positions to bins too
+            sum += c[u];
+        }
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        uint32_t base = incl - sum;
+        __syncwarp();
+#pragma unroll
+        for (uint32_t u = 0; u < kPer; u++) {
+            wh[walk_pos(lane * kPer + u, sort_mode)] = base;
+            base += c[u];
+        }
+    }
+    __syncwarp();
+    uint32_t* rk = P.vis_rank + (size_t)i * T;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t j0 = 0; j0 < n; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        const bool active = j < n;
+        const uint32_t mask = __ballot_sync(0xffffffffu, active);
+        if (active) {
+            const uint32_t b = sb[j];
+            const uint32_t peers = __match_any_sync(mask, b);
+            const uint32_t w = run[b] + __popc(peers & lt);
+            rk[wh[b] + w] = j | (b << 11) | (w << 20);
+            __syncwarp(mask);
+            if (lane == (uint32_t)(__ffs(peers) - 1)) run[b] += __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
 // P2: bin histograms of the tiles of multi-tile segments, one warp per tile
 // (each warp pulls its own tiles and owns a kBins-counter region of shared
 // memory). Queue slots run over the record-path tiles [mt_tile_begin,
@@ -1403,6 +1493,14 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         const uint32_t i = k < n_rec ? P.mt_tile_begin + k : P.mt_mesh_begin + (k - n_rec);
         const TileDesc& td = P.mt_desc[i];
         const uint32_t s = td.seg;
+        if (td.flags & SEG_MESHLET) {  // counts, cross-tile counts and the tile's stable ranking
+            hist_rank_meshlet(P, i, td, wh, wh + (size_t)nw * kBins,
+                              reinterpret_cast<uint16_t*>(L.whist + 2 * (size_t)nw * kBins) + (size_t)wid * T);
+            uint32_t nx = 0;
+            if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
+            k = __shfl_sync(0xffffffffu, nx, 0);
+            continue;
+        }
         const uint32_t n = __ldcg(&P.tile_count[i]);
         for (uint32_t b = lane; b < kBins; b += 32) wh[b] = 0u;
         __syncwarp();
@@ -1411,11 +1509,9 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
             const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
             const float range = range_of(mn, mx);
             const uint32_t sort_mode = seg_sort_mode(td.flags);
-            const bool dense = td.flags & SEG_MESHLET;
-            // the tile's list: one dense region, or one region per warp of the triangle phase;
-            // 4 keys per load
-            for (uint32_t w = 0; w < (dense ? 1u : nw); w++) {
-                const uint32_t c = dense ? n : __ldcg(&P.tile_wcnt[(size_t)i * kMaxWarps + w]);
+            // the tile's list regions (one per warp of the triangle phase), 4 keys per load
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t c = __ldcg(&P.tile_wcnt[(size_t)i * kMaxWarps + w]);
                 const float4* rd = reinterpret_cast<const float4*>(P.vis_depth + (size_t)i * T + w * per);
                 for (uint32_t q = lane; 4 * q < c; q += 32) {
                     const float4 v = __ldcg(&rd[q]);
@@ -1588,23 +1684,24 @@ __host__ __device__ __forceinline__ MeshTriLayout mesh_tri_layout(uint32_t T, ui
     L.total = o;
     return L;
 }
-// Rank phase: MeshHdr | TileSmem | ModelSmem | bases u32[kBins] | depth f32[T] (later perm
-// u16[T]) | vloc u16[3T] | bin u16[T] | whist | records: 48 bytes per slot (xyuv float4,
-// rgba float4, depth float), computed in place over the copied vertex block
-struct MeshRankLayout { size_t ts, ms, hist, dep, vloc, bin, wh, rec, total; };
+// Rank phase: MeshHdr | TileSmem | ModelSmem | bases u32[kBins] | ranks u32[T] | vloc u16[3T] |
+// staged records | records: 48 bytes per slot (xyuv float4, rgba float4, depth float),
+// computed in place over the copied vertex block
+struct MeshRankLayout { size_t ts, ms, hist, rk, vloc, stg, rec, total; };
 constexpr uint32_t kRecBytes = 48;
+constexpr uint32_t kMeshStageBytes = 768;  // sizeof(MeshStage)
 __host__ __device__ __forceinline__ MeshRankLayout mesh_rank_layout(uint32_t T, uint32_t U, uint32_t warps) {
     MeshRankLayout L;
     size_t o = sizeof(MeshHdr);
     L.ts = o; o += al16(sizeof(TileSmem));
     L.ms = o; o += al16(sizeof(ModelSmem));
     L.hist = o; o += 4ull * kBins;
-    L.dep = o; o += al16(4ull * T);
+    L.rk = o; o += al16(4ull * T);
     L.vloc = o; o += al16(6ull * T);
-    L.bin = o; o += al16(2ull * T);
-    L.wh = o; o += 4ull * warps * kBins;
+    L.stg = o; o += kMeshStageBytes;
     L.rec = o; o += (size_t)kRecBytes * U;
     L.total = o;
+    (void)warps;
     return L;
 }
 
@@ -1828,61 +1925,94 @@ __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsig
     __syncthreads();
 }
 
-// Rank phase over meshlet tiles (queue 9). Thread 0 starts every copy of a tile at
-// once: the dense visible list and the tile's bin bases (barrier 0), the
+// The records a meshlet tile's rank phase starts from, staged in shared memory
+// by bulk copies while the block's previous tile is processed.
+struct MeshStage {
+    TileDesc td;
+    DevSeg seg;
+    DevPrep pr;
+    unsigned char job[304];  // DevJob up to and including `cells`: the camera and the cell table
+    uint32_t n;              // visible entries of the tile
+    uint32_t pad[3];
+};
+static_assert(sizeof(MeshStage) == kMeshStageBytes, "MeshStage size");
+static_assert(sizeof(DevSeg) % 16 == 0 && sizeof(DevJob) % 16 == 0 && offsetof(DevJob, cells) + 8 <= 304 &&
+              offsetof(MeshStage, seg) % 16 == 0 && offsetof(MeshStage, pr) % 16 == 0 &&
+              offsetof(MeshStage, job) % 16 == 0 && sizeof(MeshStage) % 16 == 0, "MeshStage layout");
+
+// Thread 0: stages meshlet tile i (its descriptor and count read already) for the
+// block's next round: the pair, prep and job records travel by bulk copy.
+__device__ __forceinline__ void mesh_stage_tile(const FrameParams& P, const TileDesc& td, uint32_t n, MeshStage& S,
+                                                unsigned long long* bar) {
+    S.td = td;
+    S.n = n;
+    if (n == 0) return;
+    fence_proxy_async();
+    mbar_expect_tx(bar, (uint32_t)(sizeof(DevSeg) + sizeof(DevPrep) + 304));
+    bulk_g2s(&S.seg, &P.segs[td.seg], sizeof(DevSeg), bar);
+    bulk_g2s(&S.pr, &P.preps[td.inst], sizeof(DevPrep), bar);
+    bulk_g2s(S.job, &P.jobs[td.job], 304, bar);
+}
+
+// Rank phase over meshlet tiles (queue 9): the emit of tiles the histogram phase
+// has ranked. A tile's descriptor, pair, prep and job records are staged during
+// the block's previous tile; at its start thread 0 starts every copy at once:
+// the tile's rank list, visible corners' slots and bin bases (barrier 0), the
 // meshlet's interleaved vertex block (barrier 1) and the model's staged lights
-// (barrier 3). The block stages the pair's constants meanwhile, bins the list,
-// turns the vertex block into emitted corners in place, ranks the list and emits
-// from shared memory. The block's next tile is taken at the start of a tile and
-// its data asked into L2 halfway through.
+// (barrier 3). The block stages the pair's constants from shared memory, turns
+// the vertex block into emitted corners in place and writes the corners in
+// output order, one per thread. The next tile is taken at the start of a tile,
+// its data asked into L2 and its records staged halfway through.
 template <bool kM>
 __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned char* smem) {
     MeshHdr& H = *reinterpret_cast<MeshHdr*>(smem);
-    const uint32_t T = P.tile_tris, nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t T = P.tile_tris, nw = blockDim.x >> 5;
     const MeshRankLayout ML = mesh_rank_layout(T, P.mesh_ucap, nw);
-    SmemLayout L;
-    L.ts = reinterpret_cast<TileSmem*>(smem + ML.ts);
-    L.whist = reinterpret_cast<uint32_t*>(smem + ML.wh);
-    L.bin = reinterpret_cast<uint16_t*>(smem + ML.bin);
-    L.perm = reinterpret_cast<uint16_t*>(smem + ML.dep);  // the depth keys are dead once binned
-    L.vloc = reinterpret_cast<uint16_t*>(smem + ML.vloc);
-    L.depth = reinterpret_cast<float*>(smem + ML.dep);
-    L.lidx = nullptr;
-    TileSmem& sm = *L.ts;
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem + ML.ms);
+    MeshStage& S = *reinterpret_cast<MeshStage*>(smem + ML.stg);
     const uint32_t* hist = reinterpret_cast<const uint32_t*>(smem + ML.hist);
+    uint32_t* rk = reinterpret_cast<uint32_t*>(smem + ML.rk);
+    uint16_t* vloc = reinterpret_cast<uint16_t*>(smem + ML.vloc);
     unsigned char* rec = smem + ML.rec;
     const uint32_t limit = spin_limit(P);
-    uint32_t ph0 = 0, ph1 = 0, ph3 = 0;  // mbarrier phases
+    uint32_t ph0 = 0, ph1 = 0, ph2 = 0, ph3 = 0;  // mbarrier phases
     const uint32_t nmt = P.mt_mesh_end - P.mt_mesh_begin;
     if (threadIdx.x == 0) {
         for (int b = 0; b < 4; b++) mbar_init(&H.bar[b], 1);
         fence_mbar_init();
+        const uint32_t k0 = atomicAdd(&P.ctl->queue[9], 1u);
+        H.item[0] = k0;
+        if (k0 < nmt) mesh_stage_tile(P, P.mt_desc[P.mt_mesh_begin + k0], __ldcg(&P.tile_count[P.mt_mesh_begin + k0]), S, &H.bar[2]);
     }
-    uint32_t k = next_item(P.ctl, 9, &sm.item);
-    while (k < nmt) {
+    __syncthreads();
+    for (;;) {
+        const uint32_t k = H.item[0];
+        if (k >= nmt) break;
         const uint32_t i = P.mt_mesh_begin + k;
+        const TileDesc td = S.td;
+        const uint32_t n = S.n;
         uint32_t kn = 0xFFFFFFFFu;
         if (threadIdx.x == 0) kn = atomicAdd(&P.ctl->queue[9], 1u);
-        const uint32_t n = __ldcg(&P.tile_count[i]);
-        const TileDesc td = P.mt_desc[i];
+        bool ok = true;
         if (n > 0) {
         const uint32_t U = td.vmin, U4 = mlet_slots4(U), nt = td.t1 - td.t0;
         const bool colors = td.flags & SEG_COLORS;
+        const bool single = td.flags & SEG_SINGLE;
         const uint32_t as = mlet_aos_stride(colors);
         // the vertex block lands at the end of the record area: a slot's 48-byte record then
         // only ever covers input bytes of its own or earlier slots
         unsigned char* vin = rec + (size_t)(kRecBytes - as) * U4;
-        const bool lit = td.flags & SEG_LIT;
-        const DevPrep& pr = P.preps[td.inst];
-        const uint32_t nl = lit ? pr.nl : 0u;
+        ok = mbar_wait(&H.bar[2], ph2, P.ctl, limit);  // the staged records
+        ph2 ^= 1u;
+        const uint32_t nl = (td.flags & SEG_LIT) ? S.pr.nl : 0u;
         if (threadIdx.x == 0) {
-            const uint32_t db = (4u * n + 15u) & ~15u, vb = (6u * n + 15u) & ~15u;
+            const uint32_t rb = (4u * n + 15u) & ~15u, vb = (6u * n + 15u) & ~15u;
+            const uint32_t hb = single ? 0u : 4u * kBins;
             fence_proxy_async();
-            mbar_expect_tx(&H.bar[0], 4u * kBins + db + vb);
-            bulk_g2s(smem + ML.hist, P.tile_hist + (size_t)i * kBins, 4u * kBins, &H.bar[0]);
-            bulk_g2s(L.depth, P.vis_depth + (size_t)i * T, db, &H.bar[0]);
-            bulk_g2s(L.vloc, P.vis_vloc + (size_t)i * 3 * T, vb, &H.bar[0]);
+            mbar_expect_tx(&H.bar[0], hb + rb + vb);
+            if (hb) bulk_g2s(smem + ML.hist, P.tile_hist + (size_t)i * kBins, hb, &H.bar[0]);
+            bulk_g2s(rk, P.vis_rank + (size_t)i * T, rb, &H.bar[0]);
+            bulk_g2s(vloc, P.vis_vloc + (size_t)i * 3 * T, vb, &H.bar[0]);
             mbar_expect_tx(&H.bar[1], as * U4);
             bulk_g2s(vin, mlet_addr(td) + mlet_lidx_bytes(nt) + 12ull * U4, as * U4, &H.bar[1]);
             if (nl) {
@@ -1893,16 +2023,7 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
             }
             ms.nl = nl;
         }
-        const DevSeg seg = P.segs[td.seg];
-        stage_model_consts<false>(seg, P.jobs[td.job], pr, ms);
-        const uint32_t s = td.seg;
-        const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
-        const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
-        const float range = range_of(mn, mx);
-        const uint32_t sort_mode = seg_sort_mode(td.flags);
-        bool ok = mbar_wait(&H.bar[0], ph0, P.ctl, limit);
-        ph0 ^= 1u;
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) L.bin[j] = (uint16_t)bin_of(L.depth[j], mn, range, sort_mode);
+        stage_model_consts<false, false>(S.seg, *reinterpret_cast<const DevJob*>(S.job), S.pr, ms);
         uint32_t nn = 0;
         TileDesc tn;
         if (threadIdx.x == 0 && kn < nmt) {  // read now, used after the records
@@ -1913,15 +2034,9 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
             ok = mbar_wait(&H.bar[3], ph3, P.ctl, limit) && ok;
             ph3 ^= 1u;
         }
-        {  // the warps rank consecutive slices of the dense list
-            const uint32_t per = (n + nw - 1) / nw;
-            if (lane == 0) {
-                sm.wlo[wid] = min(n, wid * per);
-                sm.whi[wid] = min(n, wid * per + per);
-            }
-        }
         ok = mbar_wait(&H.bar[1], ph1, P.ctl, limit) && ok;
         ph1 ^= 1u;
+        __syncthreads();  // the constants are in place
         // every slot's emitted corner, in place: a round of blockDim slots reads its inputs,
         // then (after a barrier) writes its records
         for (uint32_t v0 = 0; v0 < U; v0 += blockDim.x) {
@@ -1943,37 +2058,48 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
                 out[2] = make_float4(cull.w, 0.f, 0.f, 0.f);
             }
         }
-        if (threadIdx.x == 0 && nn > 0) {  // the next tile's vertex block, list and bases into L2
-            const uint32_t u4n = mlet_slots4(tn.vmin), ntn = tn.t1 - tn.t0;
-            const uint32_t in_ = P.mt_mesh_begin + kn;
-            l2_prefetch(mlet_addr(tn) + mlet_lidx_bytes(ntn) + 12ull * u4n,
-                        (size_t)mlet_aos_stride(tn.flags & SEG_COLORS) * u4n);
-            l2_prefetch(P.vis_depth + (size_t)in_ * T, 4ull * nn);
-            l2_prefetch(P.vis_vloc + (size_t)in_ * 3 * T, 6ull * nn);
-            l2_prefetch(P.tile_hist + (size_t)in_ * kBins, 4ull * kBins);
+        if (threadIdx.x == 0) {
+            if (nn > 0) {  // the next tile's vertex block, lists and bases into L2
+                const uint32_t u4n = mlet_slots4(tn.vmin), ntn = tn.t1 - tn.t0;
+                const uint32_t in_ = P.mt_mesh_begin + kn;
+                l2_prefetch(mlet_addr(tn) + mlet_lidx_bytes(ntn) + 12ull * u4n,
+                            (size_t)mlet_aos_stride(tn.flags & SEG_COLORS) * u4n);
+                l2_prefetch(P.vis_rank + (size_t)in_ * T, 4ull * nn);
+                l2_prefetch(P.vis_vloc + (size_t)in_ * 3 * T, 6ull * nn);
+                if (!(tn.flags & SEG_SINGLE)) l2_prefetch(P.tile_hist + (size_t)in_ * kBins, 4ull * kBins);
+            }
+            if (kn < nmt) mesh_stage_tile(P, tn, nn, S, &H.bar[2]);  // the staged records are no longer read
         }
+        ok = mbar_wait(&H.bar[0], ph0, P.ctl, limit) && ok;  // ranks, slots, bases (landed long ago)
+        ph0 ^= 1u;
         if (__syncthreads_and(ok)) {
-            rank_tile(L, sort_mode);
             float4* __restrict__ oxyuv = P.out_xyuv + 3 * (size_t)td.out_base;
             float4* __restrict__ orgba = P.out_rgba + 3 * (size_t)td.out_base;
             float* __restrict__ odepth = P.out_depth + 3 * (size_t)td.out_base;
-            for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {
+            for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {  // one corner per thread, output order
                 const uint32_t r = q / 3u, cc = q - 3u * r;
-                const uint32_t j = L.perm[r];
-                const uint32_t bn = L.bin[j];
-                const uint32_t pos = hist[bn] + (r - sm.loc_walk[walk_pos(bn, sort_mode)]);
-                const float4* rc = reinterpret_cast<const float4*>(rec + (size_t)kRecBytes * L.vloc[3 * j + cc]);
+                const uint32_t w = rk[r];
+                const uint32_t j = w & 2047u, bn = (w >> 11) & 511u;
+                const uint32_t pos = single ? r : hist[bn] + (w >> 20);
+                const float4* rc = reinterpret_cast<const float4*>(rec + (size_t)kRecBytes * vloc[3 * j + cc]);
                 oxyuv[3 * pos + cc] = rc[0];
                 orgba[3 * pos + cc] = rc[1];
                 odepth[3 * pos + cc] = reinterpret_cast<const float*>(rc + 2)[0];
             }
         }
+        } else if (threadIdx.x == 0 && kn < nmt) {  // an empty tile: stage the next one now
+            mesh_stage_tile(P, P.mt_desc[P.mt_mesh_begin + kn], __ldcg(&P.tile_count[P.mt_mesh_begin + kn]), S,
+                            &H.bar[2]);
         }
         __syncthreads();  // the shared arrays are free; the slot taken above becomes the current tile
-        if (threadIdx.x == 0) sm.item = kn;
+        if (threadIdx.x == 0) H.item[0] = kn;
         __syncthreads();
-        k = sm.item;
+        if (!ok) {  // gave up: every issued copy was waited for; leave (the staged copy too)
+            if (threadIdx.x == 0 && kn < nmt && S.n > 0) mbar_wait(&H.bar[2], ph2, P.ctl, kSpinLimit);
+            break;
+        }
     }
+    __syncthreads();
     if (threadIdx.x == 0) {  // every copy of the last tile was waited for
         for (int b = 0; b < 4; b++) mbar_inval(&H.bar[b]);
     }
@@ -2067,5 +2193,9 @@ extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_t
     const size_t a = t3d_frame_smem_bytes(tile_tris, block_threads);
     const size_t b = t3d::mesh_tri_layout(tile_tris, mesh_ucap).total;
     const size_t c = t3d::mesh_rank_layout(tile_tris, mesh_ucap, block_threads / 32).total;
-    return a > b ? (a > c ? a : c) : (b > c ? b : c);
+    // the histogram phase's meshlet ranking: two counter arrays and the bins of a tile per warp
+    const size_t d = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + (block_threads / 32) * (8ull * t3d::kBins + 2ull * tile_tris);
+    size_t m = a > b ? a : b;
+    m = m > c ? m : c;
+    return m > d ? m : d;
 }

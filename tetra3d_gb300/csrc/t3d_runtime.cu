@@ -1312,7 +1312,8 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (ntiles > 1 || mls) {  // every meshlet pair takes the multi-tile route
                 flags |= SEG_MULTI;
                 sg.mt_first = (uint32_t)F.mt_desc.size();
-                F.mt_segs.push_back(s);
+                if (mls && ntiles == 1) flags |= SEG_SINGLE;  // ranked alone: no cross-tile scan
+                else F.mt_segs.push_back(s);
             }
             sg.flags = flags;
             if (mls) {
@@ -1370,7 +1371,8 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
             si.draw = rp.draw; si.draw_transparent = rp.transparent;
             F.seg_info.push_back(si);
-            F.seg_mt_seg.push_back((flags & SEG_MULTI) ? (uint32_t)F.mt_segs.size() - 1 : 0xFFFFFFFFu);
+            F.seg_mt_seg.push_back((flags & SEG_MULTI) && !(flags & SEG_SINGLE) ? (uint32_t)F.mt_segs.size() - 1
+                                                                                  : 0xFFFFFFFFu);
         }
         F.job_seg_end.push_back((uint32_t)F.segs.size());
     }
@@ -1533,9 +1535,13 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         P.job_bytes = (unsigned long long*)ctx->job_bytes.ptr;
     }
     P.inst_lights = nullptr;
-    if (F.any_mesh) {  // the instances' staged light lists (meshlet rank phase)
-        if ((rc = ctx->inst_lights.ensure(ctx, 56ull * kMaxLights * ninst + 16))) return rc;
+    P.vis_rank = nullptr;
+    if (F.any_mesh) {  // the instances' staged light lists and the meshlet tiles' rank lists
+        if ((rc = ctx->inst_lights.ensure(ctx, 56ull * kMaxLights * ninst + 16)) ||
+            (rc = ctx->vis_rank.ensure(ctx, 4ull * nmt * ctx->tile_tris)))
+            return rc;
         P.inst_lights = (float4*)ctx->inst_lights.ptr;
+        P.vis_rank = (uint32_t*)ctx->vis_rank.ptr;
     }
 
     P.vcull = (float4*)ctx->vcull.ptr;
@@ -1620,7 +1626,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
 
         P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
         P.tile_alt = F.tile_alt; P.vitem_alt = F.vitem_alt;
-        P.has_multi = F.mt_segs.empty() ? 0u : 1u;
+        P.has_multi = F.mt_desc.empty() ? 0u : 1u;
         uint32_t items = (uint32_t)std::max({F.tiles.size(), F.mt_desc.size(), F.vitem_seg.size(),
                                              (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
         return launch_one(ctx, P, ctl, items, st);
@@ -1652,7 +1658,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         if (sg.flags & SEG_MULTI) {
             if (mesh) { P.mt_mesh_begin = sg.mt_first; P.mt_mesh_end = sg.mt_first + sg.ntiles; }
             else { P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles; }
-            P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1;
+            if (!(sg.flags & SEG_SINGLE)) { P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1; }
             P.has_multi = 1;
         }
         // animation must be applied once: host tables carry the flag on the instance,
