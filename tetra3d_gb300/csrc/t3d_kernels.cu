@@ -1385,52 +1385,81 @@ __device__ __noinline__ void phase_triangles_skinned(const FrameParams& P, unsig
     triangle_tiles<true>(P, smem);
 }
 
-// P2 for one meshlet tile, by one warp: the tile's bin counts (written for the
-// cross-tile scan unless the pair has one tile), their exclusive scan in the
-// pair's walk order, then the stable ranking of its dense list (entries in
-// triangle order, 32 at a time, equal bins ranked by lane with match_any): entry
-// j of bin b at local rank r gets the word j | b << 11 | (r - first rank of b) << 20
-// at position r of the tile's rank list. wh and run: kBins counters each.
-__device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i, const TileDesc& td, uint32_t* wh,
-                                               uint32_t* run, uint16_t* sb) {
+// bin_of for keys in [mn, mn + range] without a divide per key: the quotient is
+// (d - mn) * RN(1 / range) with one Markstein correction, within one ulp of the
+// division's; its bin can differ only when 512 q lies within an ulp or two of an
+// integer, and such keys (|512 q - nearest integer| <= 2^-13, at least two ulps
+// for 512 q <= 512) take the exact division, as does every key of a range whose
+// reciprocal is passed as NaN.
+__device__ __noinline__ uint32_t bin_exact(float d, float mn, float range, uint32_t sort_mode) {
+    return bin_of(d, mn, range, sort_mode);
+}
+__device__ __forceinline__ uint32_t bin_fast(float d, float mn, float range, float rinv, uint32_t sort_mode) {
+    if (sort_mode == T3D_SORT_NONE) return 0u;
+    const float a = d - mn;
+    const float q0 = a * rinv;
+    const float q = __fmaf_rn(__fmaf_rn(-range, q0, a), rinv, q0);
+    const float x = q * (float)kBins;
+    if (!(fabsf(x - rintf(x)) > 0.0001220703125f) || !(x >= 0.0f && x <= (float)kBins)) return bin_exact(d, mn, range, sort_mode);
+    return (uint32_t)(int)clampf(x, 0.0f, (float)(kBins - 1));
+}
+
+// P2 for one meshlet tile, by one warp: the tile's stable ranking and bin counts.
+// One pass over the dense list (entries in triangle order, 32 at a time) bins
+// each entry and gives it its index among the earlier entries of its bin (equal
+// bins ranked by lane with match_any; one lane per distinct bin advances that
+// bin's count), keeping bin and index in shared memory. The counts go out for the
+// cross-tile scan (unless the pair has one tile); their exclusive scan in the
+// pair's walk order gives each bin's first local rank, and a second pass writes
+// entry j of bin b with index w to position first(b) + w of the tile's rank list
+// as j | b << 11 | w << 20. cnt: kBins counters; sb, sw: a bin and an index per entry.
+__device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i, const TileDesc& td, uint32_t* cnt,
+                                               uint16_t* sb, uint16_t* sw) {
     const uint32_t lane = threadIdx.x & 31, T = P.tile_tris;
     const uint32_t n = __ldcg(&P.tile_count[i]);
     const uint32_t s = td.seg;
-    const bool single = td.flags & SEG_SINGLE;
-    for (uint32_t b = lane; b < kBins; b += 32) { wh[b] = 0u; run[b] = 0u; }
-    __syncwarp();
+    for (uint32_t b = lane; b < kBins; b += 32) cnt[b] = 0u;
     const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
     const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
     const float range = range_of(mn, mx);
+    // ranges outside [2^-60, 2^60] (never met by depth keys) take the exact bins: a NaN reciprocal
+    const float rinv = (range >= 0x1p-60f && range <= 0x1p60f) ? 1.0f / range : __int_as_float(0x7fc00000);
     const uint32_t sort_mode = seg_sort_mode(td.flags);
-    {  // bins of the dense list (kept in sb for the ranking) and their counts; 4 loads in flight per lane
-        const float4* rd = reinterpret_cast<const float4*>(P.vis_depth + (size_t)i * T);
-        const uint32_t nq = (n + 3) / 4;
-        for (uint32_t q0 = lane; q0 < nq; q0 += 128) {
-            float4 v[4];
+    const float* dep = P.vis_depth + (size_t)i * T;
+    const uint32_t lt = (1u << lane) - 1u;
+    __syncwarp();
+    // pass 1: bins and indices within bins, the next four keys in flight per lane
+    float nxt[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++)
-                if (q0 + 32 * u < nq) v[u] = __ldcg(&rd[q0 + 32 * u]);
+    for (int u = 0; u < 4; u++) nxt[u] = (32u * u + lane < n) ? __ldcg(&dep[32u * u + lane]) : 0.0f;
+    for (uint32_t j0 = 0; j0 < n; j0 += 128) {
+        float cur[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const uint32_t j = 4 * (q0 + 32 * u);
-                if (j >= n) break;
-                const float d[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+        for (int u = 0; u < 4; u++) {
+            cur[u] = nxt[u];
+            const uint32_t jn = j0 + 128u + 32u * u + lane;
+            nxt[u] = jn < n ? __ldcg(&dep[jn]) : 0.0f;
+        }
 #pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    if (j + e < n) {
-                        const uint32_t b = bin_of(d[e], mn, range, sort_mode);
-                        sb[j + e] = (uint16_t)b;
-                        atomicAdd(&wh[b], 1u);
-                    }
-                }
+        for (int u = 0; u < 4; u++) {
+            const uint32_t j = j0 + 32u * u + lane;
+            const bool active = j < n;
+            const uint32_t mask = __ballot_sync(0xffffffffu, active);
+            if (active) {
+                const uint32_t bn = bin_fast(cur[u], mn, range, rinv, sort_mode);
+                const uint32_t peers = __match_any_sync(mask, bn);
+                const uint32_t w = cnt[bn] + __popc(peers & lt);
+                sb[j] = (uint16_t)bn;
+                sw[j] = (uint16_t)w;
+                __syncwarp(mask);
+                if (lane == (uint32_t)(__ffs(peers) - 1)) cnt[bn] += __popc(peers);
             }
+            __syncwarp();
         }
     }
-    __syncwarp();
-    if (!single) {
+    if (!(td.flags & SEG_SINGLE)) {
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
-        for (uint32_t b = lane; b < kBins; b += 32) out[b] = wh[b];
+        for (uint32_t b = lane; b < kBins; b += 32) out[b] = cnt[b];
     }
     // exclusive scan in walk order: lane l owns walk positions [16 l, 16 l + 16)
     {
@@ -1438,7 +1467,7 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
         uint32_t c[kPer], sum = 0;
 #pragma unroll
         for (uint32_t u = 0; u < kPer; u++) {
-            c[u] = wh[walk_pos(lane * kPer + u, sort_mode)];  // walk_pos maps walk positions to bins too
+            c[u] = cnt[walk_pos(lane * kPer + u, sort_mode)];  // walk_pos maps walk positions to bins too
             sum += c[u];
         }
         uint32_t incl = sum;
@@ -1450,26 +1479,16 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
         __syncwarp();
 #pragma unroll
         for (uint32_t u = 0; u < kPer; u++) {
-            wh[walk_pos(lane * kPer + u, sort_mode)] = base;
+            cnt[walk_pos(lane * kPer + u, sort_mode)] = base;
             base += c[u];
         }
     }
     __syncwarp();
+    // pass 2: each entry to its rank
     uint32_t* rk = P.vis_rank + (size_t)i * T;
-    const uint32_t lt = (1u << lane) - 1u;
-    for (uint32_t j0 = 0; j0 < n; j0 += 32) {
-        const uint32_t j = j0 + lane;
-        const bool active = j < n;
-        const uint32_t mask = __ballot_sync(0xffffffffu, active);
-        if (active) {
-            const uint32_t b = sb[j];
-            const uint32_t peers = __match_any_sync(mask, b);
-            const uint32_t w = run[b] + __popc(peers & lt);
-            rk[wh[b] + w] = j | (b << 11) | (w << 20);
-            __syncwarp(mask);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) run[b] += __popc(peers);
-        }
-        __syncwarp();
+    for (uint32_t j = lane; j < n; j += 32) {
+        const uint32_t bn = sb[j], w = sw[j];
+        rk[cnt[bn] + w] = j | (bn << 11) | (w << 20);
     }
 }
 
@@ -1494,8 +1513,8 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         const TileDesc& td = P.mt_desc[i];
         const uint32_t s = td.seg;
         if (td.flags & SEG_MESHLET) {  // counts, cross-tile counts and the tile's stable ranking
-            hist_rank_meshlet(P, i, td, wh, wh + (size_t)nw * kBins,
-                              reinterpret_cast<uint16_t*>(L.whist + 2 * (size_t)nw * kBins) + (size_t)wid * T);
+            uint16_t* sb = reinterpret_cast<uint16_t*>(L.whist + (size_t)nw * kBins) + 2 * (size_t)wid * T;
+            hist_rank_meshlet(P, i, td, wh, sb, sb + T);
             uint32_t nx = 0;
             if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
             k = __shfl_sync(0xffffffffu, nx, 0);
@@ -1666,9 +1685,9 @@ __host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(
 constexpr uint32_t kPrepHead = 208;
 static_assert(offsetof(DevPrep, invcam) + 16 == kPrepHead && sizeof(DevPrep) % 16 == 0, "DevPrep head layout");
 // Triangle phase: MeshHdr | TileSmem | buf[2] (the model's prep record up to the model-space
-// camera, then lidx + pos of one meshlet) | cx, cy, cz per slot | the tile's visible
+// camera, then lidx + pos of one meshlet) | (X/w, Y/w, Z, 0) per slot | the tile's visible
 // entries per warp region (depth f32[T], slots u16[3T])
-struct MeshTriLayout { size_t ts, buf0, buf1, cx, cy, cz, sdep, svl, total; };
+struct MeshTriLayout { size_t ts, buf0, buf1, clip, sdep, svl, total; };
 __host__ __device__ __forceinline__ MeshTriLayout mesh_tri_layout(uint32_t T, uint32_t U) {
     MeshTriLayout L;
     size_t o = sizeof(MeshHdr);
@@ -1676,9 +1695,7 @@ __host__ __device__ __forceinline__ MeshTriLayout mesh_tri_layout(uint32_t T, ui
     const size_t buf = kPrepHead + (size_t)mlet_lidx_bytes(T) + 12ull * U;
     L.buf0 = o; o += al16(buf);
     L.buf1 = o; o += al16(buf);
-    L.cx = o; o += al16(4ull * U);
-    L.cy = o; o += al16(4ull * U);
-    L.cz = o; o += al16(4ull * U);
+    L.clip = o; o += 16ull * U;
     L.sdep = o; o += al16(4ull * T);
     L.svl = o; o += al16(6ull * T);
     L.total = o;
@@ -1720,6 +1737,22 @@ __device__ __forceinline__ uint32_t mesh_issue_tri(const FrameParams& P, const T
     return 1u;
 }
 
+// x / 3 rounded to nearest even without a divide instruction: q0 = x * RN(1/3),
+// then one correction with the exact residual x - 3 q0 (Markstein's correction,
+// P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990). Inputs whose quotient is tiny or not
+// finite take the division itself. t3d_check_div3 compares it with IEEE division
+// for every float.
+__device__ __noinline__ float div3_slow(float x) { return x / 3.0f; }
+__device__ __forceinline__ float div3(float x) {
+    const float c = 0.3333333432674408f;  // RN(1/3)
+    const float q = x * c;
+    const float r = __fmaf_rn(-3.0f, q, x);  // exact
+    const float y = __fmaf_rn(r, c, q);
+    // tiny or non-finite quotients (never met by finite vertex positions) take the division
+    return (fabsf(q) >= 1.1754944e-36f && fabsf(q) <= 3.0e38f) ? y : div3_slow(x);
+}
+
 // MultVecW (model.go:808-811) by MVP rows m (row-major), in the reference's order.
 __device__ __forceinline__ float4 clip_rows(const float* m, float x, float y, float z) {
     float4 c;
@@ -1748,7 +1781,7 @@ __device__ __forceinline__ void next_culled(const FrameParams& P, NextTile& nx) 
 
 // One meshlet tile of the triangle phase, its prep head + lidx + pos block in buf.
 __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDesc& td, unsigned char* buf,
-                                              TileSmem& sm, float* scx, float* scy, float* scz, float* sdep,
+                                              TileSmem& sm, float4* sclip, float* sdep,
                                               uint16_t* svl, NextTile& nx) {
     const uint32_t mt = td.mt;
     const DevPrep& pr = *reinterpret_cast<const DevPrep*>(buf);  // its head: mvp, M, dirrot, invcam
@@ -1771,9 +1804,7 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
         // MultVecW and the x/y divide of the rejection tests (model.go:808-873)
         const float4 c = clip_rows(mrow, pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]);
         const float w1 = c.w < 0.0f ? 0.000001f : c.w;
-        scx[v] = c.x / w1;
-        scy[v] = c.y / w1;
-        scz[v] = c.z;
+        sclip[v] = make_float4(c.x / w1, c.y / w1, c.z, 0.0f);
     }
     next_desc(P, nx);
     __syncthreads();
@@ -1797,13 +1828,11 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
         uint32_t i0 = 0, i1 = 0, i2 = 0;
         if (t < wt1) {
             i0 = lidx[3 * t]; i1 = lidx[3 * t + 1]; i2 = lidx[3 * t + 2];
-            const float4 c0 = make_float4(scx[i0], scy[i0], scz[i0], 0.f);
-            const float4 c1 = make_float4(scx[i1], scy[i1], scz[i1], 0.f);
-            const float4 c2 = make_float4(scx[i2], scy[i2], scz[i2], 0.f);
+            const float4 c0 = sclip[i0], c1 = sclip[i1], c2 = sclip[i2];
             // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis
-            const f3 ctr = mk3((pos[3 * i0] + pos[3 * i1] + pos[3 * i2]) / 3.0f,
-                               (pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]) / 3.0f,
-                               (pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]) / 3.0f);
+            const f3 ctr = mk3(div3(pos[3 * i0] + pos[3 * i1] + pos[3 * i2]),
+                               div3(pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]),
+                               div3(pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]));
             vis = tri_visible(nearp, farp, backface, ic, c0, c1, c2, ctr, d);
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, vis);
@@ -1860,9 +1889,7 @@ __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsig
     const MeshTriLayout L = mesh_tri_layout(P.tile_tris, P.mesh_ucap);
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem + L.ts);
     unsigned char* buf[2] = {smem + L.buf0, smem + L.buf1};
-    float* scx = reinterpret_cast<float*>(smem + L.cx);
-    float* scy = reinterpret_cast<float*>(smem + L.cy);
-    float* scz = reinterpret_cast<float*>(smem + L.cz);
+    float4* sclip = reinterpret_cast<float4*>(smem + L.clip);
     float* sdep = reinterpret_cast<float*>(smem + L.sdep);
     uint16_t* svl = reinterpret_cast<uint16_t*>(smem + L.svl);
     const uint32_t n = P.mesh_end - P.mesh_begin, limit = spin_limit(P);
@@ -1902,7 +1929,7 @@ __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsig
         }
         const TileDesc& td = H.td[cur];
         if (H.copied[cur]) {
-            mesh_tile_tri(P, td, buf[cur], sm, scx, scy, scz, sdep, svl, nx);
+            mesh_tile_tri(P, td, buf[cur], sm, sclip, sdep, svl, nx);
         } else {  // skipped pair or culled model
             if (threadIdx.x == 0) P.tile_count[td.mt] = 0u;
             next_desc(P, nx);
@@ -2193,9 +2220,79 @@ extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_t
     const size_t a = t3d_frame_smem_bytes(tile_tris, block_threads);
     const size_t b = t3d::mesh_tri_layout(tile_tris, mesh_ucap).total;
     const size_t c = t3d::mesh_rank_layout(tile_tris, mesh_ucap, block_threads / 32).total;
-    // the histogram phase's meshlet ranking: two counter arrays and the bins of a tile per warp
-    const size_t d = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + (block_threads / 32) * (8ull * t3d::kBins + 2ull * tile_tris);
+    // the histogram phase's meshlet ranking: per warp kBins counters and a bin and an index per entry
+    const size_t d = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + (block_threads / 32) * (4ull * t3d::kBins + 4ull * tile_tris);
     size_t m = a > b ? a : b;
     m = m > c ? m : c;
     return m > d ? m : d;
+}
+
+// Compares div3 with IEEE division for every 32-bit pattern (NaNs match NaNs):
+// the number of differences and the first differing pattern found.
+__global__ void k_check_div3(unsigned long long* bad, unsigned int* first) {
+    for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < (1ull << 32);
+         k += (unsigned long long)gridDim.x * blockDim.x) {
+        const float x = __uint_as_float((unsigned int)k);
+        const float a = t3d::div3(x), b = x / 3.0f;
+        if (!(__float_as_uint(a) == __float_as_uint(b) || (isnan(a) && isnan(b)))) {
+            atomicAdd(bad, 1ull);
+            atomicMin(first, (unsigned int)k);
+        }
+    }
+}
+extern "C" int t3d_check_div3(unsigned long long* mismatches, unsigned int* first_pattern) {
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return -1;
+    cudaMemset(d, 0, 8);
+    cudaMemset((char*)d + 8, 0xFF, 4);
+    k_check_div3<<<4096, 256>>>(d, (unsigned int*)((char*)d + 8));
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *mismatches = h[0];
+    *first_pattern = (unsigned int)h[1];
+    return 0;
+}
+
+namespace t3d {
+// Compares bin_fast with bin_of on n keys per range for 4096 ranges from a seeded
+// generator (range magnitudes 1e-3 .. 1e6, keys spread over the range and placed
+// next to bin edges): the number of differing bins.
+__global__ void k_check_bins(unsigned long long seed, uint32_t n, unsigned long long* bad) {
+    const uint32_t g = blockIdx.x;  // one range per block
+    unsigned long long h = seed ^ (0x9E3779B97F4A7C15ull * (g + 1));
+    auto next = [&h]() { h ^= h << 13; h ^= h >> 7; h ^= h << 17; return (uint32_t)(h >> 32); };
+    const float mn = (float)(next() % 2000000u) * 0.37f - 3.0e5f;
+    const float range = range_of(0.0f, __powf(10.0f, -3.0f + 9.0f * (float)(next() % 100000u) / 100000.0f));
+    const float rinv = (range >= 0x1p-60f && range <= 0x1p60f) ? 1.0f / range : __int_as_float(0x7fc00000);
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        unsigned long long hk = h + 0xD1B54A32D192ED03ull * (k + 1);
+        hk ^= hk >> 29; hk *= 0xBF58476D1CE4E5B9ull; hk ^= hk >> 32;
+        float d;
+        if (k & 1) {  // next to the edge of bin b (a few ulps either side)
+            const float e = mn + range * ((float)(uint32_t)(hk % 513u) / 512.0f);
+            d = __uint_as_float(__float_as_uint(e) + (int)((hk >> 20) % 9u) - 4);
+        } else {
+            d = mn + range * ((float)(uint32_t)(hk >> 40) / 16777216.0f);
+        }
+        if (!(d >= mn) || !(d <= mn + range)) continue;
+        for (uint32_t m = 0; m < 2; m++)
+            if (bin_fast(d, mn, range, rinv, m) != bin_of(d, mn, range, m)) atomicAdd(bad, 1ull);
+    }
+}
+}  // namespace t3d
+extern "C" int t3d_check_bins(unsigned long long seed, unsigned int keys_per_range, unsigned long long* mismatches) {
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 8) != cudaSuccess) return -1;
+    cudaMemset(d, 0, 8);
+    t3d::k_check_bins<<<4096, 256>>>(seed, keys_per_range, d);
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, 8, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *mismatches = h;
+    return 0;
 }
