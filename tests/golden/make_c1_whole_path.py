@@ -1,0 +1,471 @@
+"""Generates tests/golden/c1_whole_path.npz: the emitted stream of the one-sphere scene
+(a UV sphere of 32 x 16 segments, 960 triangles, ambient + directional + point light,
+640x360, back-to-front sort), and of the same scene with a non-uniform scale and two more
+point lights, computed by a second restatement of the vertex stage written here in
+numpy binary32 arithmetic, independently of the C++ oracle, so the oracle can be
+checked against it bit for bit.
+
+Every operation is an elementwise IEEE binary32 operation (numpy float32 arrays, no
+fused multiply-add, no reductions), in the order the reference writes it:
+
+- Node.Transform (node.go:572-607), Matrix4.Mult (matrix_none.go:6-32; the amd64
+  assembly in matrix_amd64.s sums in the same order), Inverted (matrix.go:255-307),
+  Decompose (matrix.go:181-196), MultVec / MultVecW (matrix.go:619-637), the
+  projection and view matrices (matrix.go:588-607, camera.go:638-679);
+- Camera.SphereInFrustum (camera.go:933-984) for the model's culling sphere
+  (model.go:394-395, colliderSphere.go:51-58);
+- Model.ProcessVertices (model.go:600-995): MVP, near/far, the +-0.5 screen test,
+  2D backface test, the model-space camera distance to Triangle.Center
+  (mesh.go:1972-1982) as the depth key;
+- sortingTriangleBucket.Sort / ForEach (sortingTriangles.go:38-125), 512 bins;
+- lights: AmbientLight, PointLight, DirectionalLight beginRender / beginModel /
+  VertexLight (light.go:110-360) with the model-level point-light range skip
+  (camera.go:1613-1641);
+- the emit loop (camera.go:1646-1820): screen position, UV, colour x lighting, depth.
+
+Run from the repo root: python tests/golden/make_c1_whole_path.py
+"""
+import hashlib
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+F = np.float32
+BINS = 512
+
+
+# ---- Matrix4 (row-major 4x4 float32; m[r][c]) ----
+
+def ident():
+    return np.eye(4, dtype=F)
+
+
+def mmul(a, b):
+    """Matrix4.Mult: out[i][j] = ((a[i][0]*b[0][j] + a[i][1]*b[1][j]) + a[i][2]*b[2][j]) + a[i][3]*b[3][j]."""
+    a = a.astype(F)
+    b = b.astype(F)
+    return ((a[:, 0:1] * b[0:1, :] + a[:, 1:2] * b[1:2, :]) + a[:, 2:3] * b[2:3, :]) + a[:, 3:4] * b[3:4, :]
+
+
+def translate(x, y, z):
+    m = ident()
+    m[3, 0], m[3, 1], m[3, 2] = x, y, z
+    return m
+
+
+def scale(x, y, z):
+    m = ident()
+    m[0, 0], m[1, 1], m[2, 2] = x, y, z
+    return m
+
+
+def transposed(m):
+    return np.ascontiguousarray(m.T)
+
+
+def inverted(m):
+    """Matrix4.Inverted: 2x2 minors of the lower rows, cofactor expansion, one reciprocal."""
+    m = m.astype(F)
+    g = lambda r, c: m[r, c]
+    A2323 = g(2, 2) * g(3, 3) - g(2, 3) * g(3, 2)
+    A1323 = g(2, 1) * g(3, 3) - g(2, 3) * g(3, 1)
+    A1223 = g(2, 1) * g(3, 2) - g(2, 2) * g(3, 1)
+    A0323 = g(2, 0) * g(3, 3) - g(2, 3) * g(3, 0)
+    A0223 = g(2, 0) * g(3, 2) - g(2, 2) * g(3, 0)
+    A0123 = g(2, 0) * g(3, 1) - g(2, 1) * g(3, 0)
+    A2313 = g(1, 2) * g(3, 3) - g(1, 3) * g(3, 2)
+    A1313 = g(1, 1) * g(3, 3) - g(1, 3) * g(3, 1)
+    A1213 = g(1, 1) * g(3, 2) - g(1, 2) * g(3, 1)
+    A2312 = g(1, 2) * g(2, 3) - g(1, 3) * g(2, 2)
+    A1312 = g(1, 1) * g(2, 3) - g(1, 3) * g(2, 1)
+    A1212 = g(1, 1) * g(2, 2) - g(1, 2) * g(2, 1)
+    A0313 = g(1, 0) * g(3, 3) - g(1, 3) * g(3, 0)
+    A0213 = g(1, 0) * g(3, 2) - g(1, 2) * g(3, 0)
+    A0312 = g(1, 0) * g(2, 3) - g(1, 3) * g(2, 0)
+    A0212 = g(1, 0) * g(2, 2) - g(1, 2) * g(2, 0)
+    A0113 = g(1, 0) * g(3, 1) - g(1, 1) * g(3, 0)
+    A0112 = g(1, 0) * g(2, 1) - g(1, 1) * g(2, 0)
+    det = (((g(0, 0) * ((g(1, 1) * A2323 - g(1, 2) * A1323) + g(1, 3) * A1223)
+             - g(0, 1) * ((g(1, 0) * A2323 - g(1, 2) * A0323) + g(1, 3) * A0223))
+            + g(0, 2) * ((g(1, 0) * A1323 - g(1, 1) * A0323) + g(1, 3) * A0123))
+           - g(0, 3) * ((g(1, 0) * A1223 - g(1, 1) * A0223) + g(1, 2) * A0123))
+    det = F(1) / det
+
+    def c3(a, x, b, y, c, z):  # (a*x - b*y) + c*z, left to right
+        return (a * x - b * y) + c * z
+
+    o = ident()
+    o[0, 0] = det * c3(g(1, 1), A2323, g(1, 2), A1323, g(1, 3), A1223)
+    o[0, 1] = det * -c3(g(0, 1), A2323, g(0, 2), A1323, g(0, 3), A1223)
+    o[0, 2] = det * c3(g(0, 1), A2313, g(0, 2), A1313, g(0, 3), A1213)
+    o[0, 3] = det * -c3(g(0, 1), A2312, g(0, 2), A1312, g(0, 3), A1212)
+    o[1, 0] = det * -c3(g(1, 0), A2323, g(1, 2), A0323, g(1, 3), A0223)
+    o[1, 1] = det * c3(g(0, 0), A2323, g(0, 2), A0323, g(0, 3), A0223)
+    o[1, 2] = det * -c3(g(0, 0), A2313, g(0, 2), A0313, g(0, 3), A0213)
+    o[1, 3] = det * c3(g(0, 0), A2312, g(0, 2), A0312, g(0, 3), A0212)
+    o[2, 0] = det * c3(g(1, 0), A1323, g(1, 1), A0323, g(1, 3), A0123)
+    o[2, 1] = det * -c3(g(0, 0), A1323, g(0, 1), A0323, g(0, 3), A0123)
+    o[2, 2] = det * c3(g(0, 0), A1313, g(0, 1), A0313, g(0, 3), A0113)
+    o[2, 3] = det * -c3(g(0, 0), A1312, g(0, 1), A0312, g(0, 3), A0112)
+    o[3, 0] = det * -c3(g(1, 0), A1223, g(1, 1), A0223, g(1, 2), A0123)
+    o[3, 1] = det * c3(g(0, 0), A1223, g(0, 1), A0223, g(0, 2), A0123)
+    o[3, 2] = det * -c3(g(0, 0), A1213, g(0, 1), A0213, g(0, 2), A0113)
+    o[3, 3] = det * c3(g(0, 0), A1212, g(0, 1), A0212, g(0, 2), A0112)
+    return o
+
+
+def sqrt32(x):
+    """math32.Sqrt: the float64 square root rounded to float32 (the correctly rounded float32 root)."""
+    return F(math.sqrt(float(x)))
+
+
+def mag3(x, y, z):
+    return sqrt32((x * x + y * y) + z * z)
+
+
+def unit3(v):
+    """Vector3.Unit / Vector4.Unit (xyz only): unchanged when the length is < 1e-8 or exactly 1."""
+    x, y, z = F(v[0]), F(v[1]), F(v[2])
+    l = mag3(x, y, z)
+    if l < F(1e-8) or l == F(1):
+        return [x, y, z]
+    return [x / l, y / l, z / l]
+
+
+def decompose(m):
+    """Matrix4.Decompose: position = row 3, rotation rows = unit rows 0-2 (w kept), scale = row lengths
+    of m x rotation^T."""
+    pos = [m[3, 0], m[3, 1], m[3, 2]]
+    rot = ident()
+    for r in range(3):
+        ux, uy, uz = unit3(m[r, :3])
+        rot[r, 0], rot[r, 1], rot[r, 2], rot[r, 3] = ux, uy, uz, m[r, 3]
+    inn = mmul(m, transposed(rot))
+    scl = [mag3(inn[r, 0], inn[r, 1], inn[r, 2]) for r in range(3)]
+    return pos, scl, rot
+
+
+def multvec(m, v):
+    """MultVec: x' = ((m00 x + m10 y) + m20 z) + m30 (v may be arrays)."""
+    x, y, z = v
+    return [((m[0, c] * x + m[1, c] * y) + m[2, c] * z) + m[3, c] for c in range(3)]
+
+
+def multvecw(m, v):
+    x, y, z = v
+    return [((m[0, c] * x + m[1, c] * y) + m[2, c] * z) + m[3, c] for c in range(4)]
+
+
+def node_transform(pos, scl, rot):
+    """Node.Transform for a node without parent: Scale x Rotation x Translate."""
+    t = mmul(scale(*scl), rot)
+    return mmul(t, translate(*pos))
+
+
+def projection(fov, near, far, w, h):
+    """NewProjectionMatrix4Perspective; math32.Tan is the float64 tangent rounded to float32."""
+    aspect = F(w) / F(h)
+    t = F(math.tan(float((F(fov) * F(math.pi)) / F(360))))
+    b = -t
+    r = t * aspect
+    l = -r
+    near, far = F(near), F(far)
+    P = np.zeros((4, 4), F)
+    P[0, 0] = (F(2) * near) / (r - l)
+    P[0, 2] = (r + l) / (r - l)
+    P[1, 1] = (F(2) * near) / (t - b)
+    P[1, 2] = (t + b) / (t - b)
+    P[2, 2] = -((far + near) / (far - near))
+    P[2, 3] = -(((F(2) * far) * near) / (far - near))
+    P[3, 2] = F(-1)
+    return P
+
+
+# ---- the scene ----
+
+def scene_inputs(sd):
+    """The binary32 inputs the restatement reads from a one-model SceneData."""
+    from tetra3d_gb300 import abi
+    assert sd.nmodels == 1
+    mv = sd.mv[0]
+    me = sd.meshes[int(mv["mesh"])]
+    mat = me.parts[0]["mat"]
+    cam = sd.camera
+    lights = []
+    ll = int(mv["light_list"])  # -1: the scene's light list (list 0); k >= 1: LightGroup k
+    for k in sd.lists[ll if ll >= 0 else 0]:
+        L = sd.lights[k]
+        Lt = np.asarray(L.transform[:], F).reshape(4, 4)
+        lights.append(dict(type=int(L.type), color=np.asarray(L.color[:3], F), energy=F(L.energy),
+                           range=F(L.range), world_pos=[Lt[3, 0], Lt[3, 1], Lt[3, 2]],
+                           world_rot=np.asarray(L.world_rotation[:], F).reshape(4, 4)))
+    ct = np.asarray(cam.transform[:], F).reshape(4, 4)
+    return dict(
+        positions=me.positions.astype(F), normals=me.normals.astype(F), uvs=me.uvs.astype(F),
+        colors=None if me.colors is None else me.colors.astype(F), indices=me.indices.astype(np.int64),
+        model_pos=np.asarray(mv["position"], F), model_scale=np.asarray(mv["scale"], F),
+        model_rot=np.asarray(mv["rotation"], F).reshape(4, 4), model_color=np.asarray(mv["color"], F),
+        mat_color=np.asarray(mat["color"], F), tex=(F(mat["tex_w"]), F(mat["tex_h"])),
+        backface=bool(mat["backface_culling"]), sort_mode=int(mat["sort_mode"]),
+        lighting_mode=int(mat["lighting_mode"]), shadeless=bool(mat["shadeless"]) or bool(mv["shadeless"]),
+        lights=lights, cam_pos=[ct[3, 0], ct[3, 1], ct[3, 2]],
+        cam_rot=np.asarray(cam.world_rotation[:], F).reshape(4, 4), width=int(cam.width), height=int(cam.height),
+        fov=F(cam.fov_y), near=F(cam.near_plane), far=F(cam.far_plane), depth_margin=F(cam.depth_margin),
+        perspective=bool(cam.perspective), lighting_on=bool(cam.lighting_on), render_depth=bool(cam.render_depth),
+        abi=abi)
+
+
+def in_frustum(S, M, dmin, dmax):
+    """Camera.SphereInFrustum for the model's culling sphere as Model.onTransformUpdate places it
+    (model.go:141-181): position + (rotation x Dimensions.Center()) * scale, radius = MaxSpan of the
+    scaled Dimensions / 2; the sphere node itself is unscaled (colliderSphere.go:51-60)."""
+    pos, scl, rot = decompose(M)
+    centre = [(dmax[a] + dmin[a]) / F(2) for a in range(3)]
+    cr = multvec(rot, centre)
+    wpos = [pos[a] + cr[a] * scl[a] for a in range(3)]
+    lo = [dmin[a] * scl[a] for a in range(3)]
+    hi = [dmax[a] * scl[a] for a in range(3)]
+    radius = mag3(hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]) / F(2)
+    crot = S["cam_rot"]
+    fwd, right, up = unit3(crot[2, :3]), unit3(crot[0, :3]), unit3(crot[1, :3])
+    diff = [wpos[a] - S["cam_pos"][a] for a in range(3)]
+    dot = lambda a, b: (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
+    pcz = dot(diff, [-fwd[0], -fwd[1], -fwd[2]])
+    if pcz > S["far"] + radius or pcz < S["near"] - radius:
+        return False
+    angle = (S["fov"] * F(3.1415)) / F(360)
+    tang = F(math.tan(float(angle)))
+    fy = F(1) / F(math.cos(float(angle)))
+    aspect = F(S["width"]) / F(S["height"])
+    fx = F(1) / F(math.cos(float(F(math.atan(float(tang * aspect))))))
+    d = fy * radius
+    pcz = pcz * tang
+    pcy = dot(diff, up)
+    if pcy > pcz + d or pcy < -pcz - d:
+        return False
+    pcz = pcz * aspect
+    d = fx * radius
+    pcx = dot(diff, right)
+    return not (pcx > pcz + d or pcx < -pcz - d)
+
+
+def render(S):
+    """The vertex stage for the scene's one model and one mesh part: returns (triangle order, xyuv,
+    rgba, depth) of the visible triangles in draw order."""
+    abi = S["abi"]
+    P, N, UV, idx = S["positions"], S["normals"], S["uvs"], S["indices"]
+    W, H = S["width"], S["height"]
+    near, far = S["near"], S["far"]
+    # camera: view = T(-pos) x R^T, vp = view x projection (camera.go:638-648, :1329)
+    cp = S["cam_pos"]
+    view = mmul(translate(-cp[0], -cp[1], -cp[2]), transposed(S["cam_rot"]))
+    vp = mmul(view, projection(S["fov"], near, far, W, H))
+    # model transform and the culling sphere
+    M = node_transform(S["model_pos"], S["model_scale"], S["model_rot"])
+    dmin = [F(P[:, a].min()) for a in range(3)]  # Mesh.UpdateDimensions
+    dmax = [F(P[:, a].max()) for a in range(3)]
+    maxspan = mag3(dmax[0] - dmin[0], dmax[1] - dmin[1], dmax[2] - dmin[2])
+    if not in_frustum(S, M, dmin, dmax):
+        return np.zeros(0, np.int64), np.zeros((0, 3, 4), F), np.zeros((0, 3, 4), F), np.zeros((0, 3), F)
+    # ProcessVertices
+    mvp = mmul(M, vp)
+    ip, isc, ir = decompose(inverted(M))
+    rc = multvec(ir, cp)
+    icam = [rc[a] + ip[a] * (F(1) / isc[a]) for a in range(3)]
+    clip = multvecw(mvp, (P[:, 0], P[:, 1], P[:, 2]))  # per vertex, float32 arrays
+    X, Y, Z, Wc = clip
+    a, b, c = idx[:, 0], idx[:, 1], idx[:, 2]
+    inb = np.zeros(len(idx), bool)
+    for k in (a, b, c):
+        inb |= (Z[k] + F(1) >= near) & (Z[k] < far)
+    wq = np.where(Wc < 0, F(0.000001), Wc).astype(F)
+    sx, sy = X / wq, Y / wq
+    vis = inb.copy()
+    for comp in (sx, sy):
+        vis &= ~((comp[a] < F(-0.5)) & (comp[b] < F(-0.5)) & (comp[c] < F(-0.5)))
+        vis &= ~((comp[a] > F(0.5)) & (comp[b] > F(0.5)) & (comp[c] > F(0.5)))
+    if S["backface"]:
+        n0x, n0y = sx[a] - sx[b], sy[a] - sy[b]
+        n1x, n1y = sx[b] - sx[c], sy[b] - sy[c]
+        vis &= ~((n0x * n1y) - (n1x * n0y) < F(0))
+    ctr = [((P[a, k] + P[b, k]) + P[c, k]) / F(3) for k in range(3)]  # Triangle.RecalculateCenter
+    dx, dy, dz = icam[0] - ctr[0], icam[1] - ctr[1], icam[2] - ctr[2]
+    depth = (dx * dx + dy * dy) + dz * dz
+    vis &= np.isfinite(depth)
+    tris = np.nonzero(vis)[0]
+    # sortingTriangleBucket.Sort: bins of the accepted triangles, in triangle order within a bin
+    if len(tris):
+        mn, mx = F(depth[tris].min()), F(depth[tris].max())
+    else:
+        mn, mx = F(np.finfo(F).max), -F(np.finfo(F).max)
+    rng = mx - mn
+    if rng == F(0):
+        rng = rng + F(0.001)
+    if S["sort_mode"] != abi.SORT_NONE:
+        key = ((depth[tris] - mn) / rng) * F(BINS)
+        t = np.where(key < F(0), F(0), np.where(key > F(BINS - 1), F(BINS - 1), key))
+        bins = t.astype(np.int64)
+    else:
+        bins = np.zeros(len(tris), np.int64)
+    walk = (BINS - 1 - bins) if S["sort_mode"] == abi.SORT_BACK_TO_FRONT else bins
+    order = tris[np.argsort(walk, kind="stable")]
+    # lighting (camera.go:1521-1641; light.go:110-360), a sum over the model's lights in list order
+    lighting = S["lighting_on"] and not S["shadeless"]
+    nv = len(P)
+    lr = np.zeros(nv, F)
+    lg = np.zeros(nv, F)
+    lb = np.zeros(nv, F)
+    if lighting:
+        mpos = [M[3, 0], M[3, 1], M[3, 2]]  # Model.WorldPosition
+        mrot_inv_t = transposed(inverted(S["model_rot"]))  # DirectionalLight.beginModel
+        vx, vy, vz = P[:, 0], P[:, 1], P[:, 2]
+        nx, ny, nz = N[:, 0], N[:, 1], N[:, 2]
+        for L in S["lights"]:
+            col, e = L["color"], L["energy"]
+            if L["type"] == abi.LIGHT_AMBIENT:
+                res = [col[0] * e, col[1] * e, col[2] * e]  # beginRender
+                lr, lg, lb = lr + res[0], lg + res[1], lb + res[2]
+            elif L["type"] == abi.LIGHT_DIRECTIONAL:
+                fwd = unit3(L["world_rot"][2, :3])  # WorldRotation().Forward()
+                if S["lighting_mode"] == abi.LIGHTING_FIXED_NORMALS:
+                    wn = [np.full(nv, fwd[0], F), np.full(nv, fwd[1], F), np.full(nv, fwd[2], F)]
+                else:
+                    wn = multvec(mrot_inv_t, (nx, ny, nz))
+                df = (wn[0] * fwd[0] + wn[1] * fwd[1]) + wn[2] * fwd[2]
+                if S["lighting_mode"] == abi.LIGHTING_DOUBLE_SIDED:
+                    df = np.abs(df)
+                on = df > F(0)
+                lr = np.where(on, lr + (col[0] * df) * e, lr).astype(F)
+                lg = np.where(on, lg + (col[1] * df) * e, lg).astype(F)
+                lb = np.where(on, lb + (col[2] * df) * e, lb).astype(F)
+            elif L["type"] == abi.LIGHT_POINT:
+                R = L["range"]
+                R2 = R * R
+                lp = L["world_pos"]
+                if R > F(0):  # model-level skip (camera.go:1625-1629)
+                    dist = maxspan + R
+                    ddx, ddy, ddz = mpos[0] - lp[0], mpos[1] - lp[1], mpos[2] - lp[2]
+                    if (ddx * ddx + ddy * ddy) + ddz * ddz > dist * dist:
+                        continue
+                p_, s_, r_ = decompose(inverted(M))  # PointLight.beginModel
+                rq = multvec(r_, lp)
+                wp = [rq[k] + p_[k] * (F(1) / s_[k]) for k in range(3)]
+                ex, ey, ez = wp[0] - vx, wp[1] - vy, wp[2] - vz
+                dist2 = (ex * ex + ey * ey) + ez * ez
+                if R > F(0):
+                    on = ~(dist2 > R2)
+                else:
+                    on = ~((F(1) / dist2) * e < F(0.001))
+                l = np.sqrt(((ex * ex + ey * ey) + ez * ez).astype(np.float64)).astype(F)
+                keep = (l < F(1e-8)) | (l == F(1))
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    ux = np.where(keep, ex, ex / l).astype(F)
+                    uy = np.where(keep, ey, ey / l).astype(F)
+                    uz = np.where(keep, ez, ez / l).astype(F)
+                if S["lighting_mode"] == abi.LIGHTING_FIXED_NORMALS:
+                    qx, qy, qz = ux, uy, uz
+                else:
+                    qx, qy, qz = nx, ny, nz
+                dif = (qx * ux + qy * uy) + qz * uz
+                if S["lighting_mode"] == abi.LIGHTING_DOUBLE_SIDED:
+                    dif = np.abs(dif)
+                on &= dif > F(0)
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    dfac = (dif * (F(1) / (F(1) + (F(0.1) * dist2)))) * F(2)
+                    if R2 > F(0):
+                        q = (R2 - dist2) / dist2
+                        q = np.where(q < F(0), F(0), np.where(q > F(1), F(1), q)).astype(F)
+                        dfac = dfac * q
+                lr = np.where(on, lr + (col[0] * dfac) * e, lr).astype(F)
+                lg = np.where(on, lg + (col[1] * dfac) * e, lg).astype(F)
+                lb = np.where(on, lb + (col[2] * dfac) * e, lb).astype(F)
+    # the emit loop, corner by corner in draw order
+    mp = S["model_color"] * S["mat_color"]  # Color4.MultiplyRGBA
+    margin = (far - near) * S["depth_margin"]
+    spread = (far - near) + (margin * F(2))
+    tw, th = S["tex"]
+    cor = idx[order]  # (n, 3) vertex per corner
+    w = Wc[cor] if S["perspective"] else np.ones(cor.shape, F)
+    w = np.where(w < F(0), F(0.001), w).astype(F)
+    xs = (X[cor] / w) * F(W) + F(W) / F(2)
+    ys = (Y[cor] / -w) * F(H) + F(H) / F(2)
+    u = UV[cor, 0] * tw
+    v = (F(1) - UV[cor, 1]) * th
+    if S["colors"] is not None:
+        col = S["colors"][cor] * mp
+    else:
+        col = np.broadcast_to(mp, cor.shape + (4,)).astype(F)
+    col = col.astype(F).copy()
+    if lighting:
+        col[..., 0] *= lr[cor]
+        col[..., 1] *= lg[cor]
+        col[..., 2] *= lb[cor]
+    dep = (Z[cor] + margin) / spread
+    dep = np.where(dep < F(0), F(0), np.where(dep > F(1), F(1), dep)).astype(F)
+    xyuv = np.stack([xs, ys, u, v], -1).astype(F)
+    return order, xyuv, col.astype(F), dep
+
+
+def scaled_variant():
+    """The one-sphere scene (same mesh, colours and rotation) with a non-uniform scale and two more
+    point lights: one near enough to light part of the sphere, one that the model-level range skip
+    leaves out."""
+    from tetra3d_gb300 import abi, scenes
+    rng = np.random.Generator(np.random.PCG64(1))
+    me = scenes.uv_sphere(32, 16, 1.0)
+    me.colors = rng.uniform(0.5, 1.0, (me.nverts, 4)).astype(F)
+    lights = [scenes.light(abi.LIGHT_AMBIENT, energy=0.2),
+              scenes.light(abi.LIGHT_DIRECTIONAL, energy=1.0,
+                           rot=scenes.look_rotation(scenes.unit3(np.array([1, 1, 1], F)))),
+              scenes.light(abi.LIGHT_POINT, energy=2.0, rng_=10.0, pos=(2, 2, -3)),
+              scenes.light(abi.LIGHT_POINT, color=(0.9, 0.4, 0.2), energy=1.5, rng_=3.0, pos=(-1.5, 0.5, -3.5)),
+              scenes.light(abi.LIGHT_POINT, color=(0.2, 0.8, 1.0), energy=3.0, rng_=2.0, pos=(30, 0, -5))]
+    sd = scenes.SceneData([me], 1, lights, [[0, 1, 2, 3, 4]], name="uv_sphere_scaled")
+    scenes.set_models_trs(sd, 0, [(0, 0, -5)], [(1.3, 0.7, 1.1)], scenes.quat_to_mat(scenes.random_quats(rng, 1)))
+    sd.camera = scenes.camera(w=640, h=360, fov=75.0)
+    return sd
+
+
+def cases():
+    from tetra3d_gb300 import scenes
+    return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant()}
+
+
+def input_digest(S):
+    h = hashlib.sha256()
+    for k in ("positions", "normals", "uvs", "colors", "indices", "model_pos", "model_scale", "model_rot",
+              "model_color", "mat_color", "cam_rot"):
+        if S[k] is not None:
+            h.update(np.ascontiguousarray(S[k]).tobytes())
+    for L in S["lights"]:
+        h.update(np.asarray([L["type"]], np.int64).tobytes())
+        h.update(np.asarray([*L["color"], L["energy"], L["range"], *L["world_pos"]], F).tobytes())
+        h.update(L["world_rot"].tobytes())
+    h.update(np.asarray([*S["cam_pos"], S["fov"], S["near"], S["far"], S["depth_margin"]], F).tobytes())
+    h.update(np.asarray([S["width"], S["height"], S["sort_mode"], S["backface"]], np.int64).tobytes())
+    return h.hexdigest()
+
+
+def main():
+    out = {}
+    for name, sd in cases().items():
+        S = scene_inputs(sd)
+        order, xyuv, rgba, depth = render(S)
+        out[f"{name}_order"] = order.astype(np.uint32)
+        out[f"{name}_xyuv"] = xyuv
+        out[f"{name}_rgba"] = rgba
+        out[f"{name}_depth"] = depth
+        out[f"{name}_digest"] = np.frombuffer(bytes.fromhex(input_digest(S)), np.uint8)
+        print(name, "visible", len(order))
+    np.savez_compressed(os.path.join(HERE, "c1_whole_path.npz"), **out)
+
+
+if __name__ == "__main__":
+    main()
