@@ -427,6 +427,12 @@ int t3d_frame_segments(t3d_ctx* ctx, t3d_segment_info* segs_out, uint32_t max_se
  * segment order (3 corners per triangle; xyuv/rgba 4 floats per corner). */
 int t3d_frame_download(t3d_ctx* ctx, float* xyuv, float* rgba, float* depth, uint64_t max_tris,
                        uint64_t* tris_out);
+/* Copies Custom0 of the last frame's visible corners (one float per corner, same
+ * order as t3d_frame_download): 1 / w under perspective-corrected texture mapping
+ * (Camera.PerspectiveCorrectedTextureMapping, camera.go:1700-1704; the colour pass
+ * divides the interpolated UV by it, shaders/base3d.kage:79-81); 0 for corners of
+ * jobs without it. T3D_E_INVAL when no job of the frame uses it. */
+int t3d_frame_download_custom0(t3d_ctx* ctx, float* custom0, uint64_t max_tris, uint64_t* tris_out);
 
 /* ---- CUDA graph replay (batched form) ------------------------------------- */
 /* Captures the frame of t3d_render(mode=BATCHED, animate) into a CUDA graph. */

@@ -24,7 +24,8 @@ class OracleOut(C.Structure):
                 ("seg_count", C.POINTER(C.c_uint32)), ("max_tris", C.c_uint64), ("total_slots", C.c_uint64),
                 ("visible_tris", C.c_uint64), ("tri_index", C.POINTER(C.c_uint32)), ("xyuv", C.c_void_p),
                 ("rgba", C.c_void_p), ("depth", C.c_void_p), ("culled_models", C.c_uint32), ("reserved", C.c_uint32),
-                ("seg_draw", C.POINTER(C.c_uint32)), ("seg_draw_transparent", C.POINTER(C.c_uint32))]
+                ("seg_draw", C.POINTER(C.c_uint32)), ("seg_draw_transparent", C.POINTER(C.c_uint32)),
+                ("custom0", C.c_void_p)]
 
 
 _lib = None
@@ -57,11 +58,12 @@ def load():
 
 
 class OracleFrame:
-    def __init__(self, segs, tri_index, xyuv, rgba, depth, culled):
+    def __init__(self, segs, tri_index, xyuv, rgba, depth, culled, custom0=None):
         self.segments = segs      # list of dicts model, part, base, capacity, count (draw order)
         self.tri_index = tri_index  # (n,) mesh-absolute triangle per visible triangle, in emit order
         self.xyuv, self.rgba, self.depth = xyuv, rgba, depth
         self.culled_models = culled
+        self.custom0 = custom0    # (n, 3) 1 / w per corner under perspective-corrected mapping, else None
 
     @property
     def visible_tris(self):
@@ -92,6 +94,7 @@ def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_ma
     xyuv = np.zeros((slots, 3, 4), dt)
     rgba = np.zeros((slots, 3, 4), dt)
     depth = np.zeros((slots, 3), dt)
+    custom0 = np.zeros((slots, 3), dt) if cam.perspective_corrected else None
     o = OracleOut()
     o.max_segments = nseg_max
     u = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
@@ -101,6 +104,7 @@ def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_ma
     o.max_tris = slots
     o.tri_index = u(tri)
     o.xyuv, o.rgba, o.depth = xyuv.ctypes.data, rgba.ctypes.data, depth.ctypes.data
+    o.custom0 = custom0.ctypes.data if custom0 is not None else None
     mask = None
     if light_mask is not None:
         m = (C.c_uint64 * 2)(light_mask & ((1 << 64) - 1), (light_mask >> 64) & ((1 << 64) - 1))
@@ -115,7 +119,8 @@ def _render_into(lib, sd, cam, light_mask, animate_frames, threads, f64, nseg_ma
                  draw_transparent=int(seg["draw_transparent"][i])) for i in range(n)]
     sel = np.concatenate([np.arange(s["base"], s["base"] + s["count"]) for s in segs] or [np.zeros(0, np.int64)])
     sel = sel.astype(np.int64)
-    return OracleFrame(segs, tri[sel], xyuv[sel], rgba[sel], depth[sel], o.culled_models), 0, slots
+    return OracleFrame(segs, tri[sel], xyuv[sel], rgba[sel], depth[sel], o.culled_models,
+                       custom0[sel] if custom0 is not None else None), 0, slots
 
 
 def mat_inverted(m):
@@ -207,7 +212,7 @@ def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, tran
     u32p, f32p = C.POINTER(C.c_uint32), C.POINTER(C.c_float)
     fn.restype = C.c_int
     fn.argtypes = [C.POINTER(abi.CameraDesc), C.c_int32, C.c_float, C.c_int32, C.c_uint32, f32p, f32p, f32p, u32p,
-                   C.POINTER(C.c_uint8), C.POINTER(OracleTextures), u32p, u32p]
+                   C.POINTER(C.c_uint8), C.POINTER(OracleTextures), u32p, u32p, f32p]
     n = int(frame.xyuv.shape[0])
     pair = np.zeros(max(1, n), np.uint32)
     given = transparent
@@ -240,6 +245,10 @@ def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, tran
     xyuv = np.ascontiguousarray(frame.xyuv, np.float32).reshape(-1)
     rgba = np.ascontiguousarray(frame.rgba, np.float32).reshape(-1)
     depth = np.ascontiguousarray(frame.depth, np.float32).reshape(-1)
+    custom0 = None
+    if cam.perspective_corrected:
+        assert getattr(frame, "custom0", None) is not None, "perspective-corrected frame without Custom0"
+        custom0 = np.ascontiguousarray(frame.custom0, np.float32).reshape(-1)
     W, H = cam.width, cam.height
     col = np.zeros(W * H, np.uint32)
     dep = np.zeros(W * H, np.uint32)
@@ -257,7 +266,8 @@ def raster(frame, scene_data, cam, fog_curve=0, dither_size=0.0, fogless=0, tran
                         th.ctypes.data_as(C.POINTER(C.c_int32)), texels.ctypes.data_as(u32p))
     rc = fn(C.byref(cam), fog_curve, dither_size, fogless, n, xyuv.ctypes.data_as(f32p), rgba.ctypes.data_as(f32p),
             depth.ctypes.data_as(f32p), pair.ctypes.data_as(u32p), transparent.ctypes.data_as(C.POINTER(C.c_uint8)),
-            C.byref(ts), col.ctypes.data_as(u32p), dep.ctypes.data_as(u32p))
+            C.byref(ts), col.ctypes.data_as(u32p), dep.ctypes.data_as(u32p),
+            custom0.ctypes.data_as(f32p) if custom0 is not None else None)
     if rc != 0:
         raise RuntimeError(f"oracle raster failed: {rc}")
     return col.view(np.uint8).reshape(H, W, 4), dep.view(np.uint8).reshape(H, W, 4)

@@ -984,6 +984,7 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
     OutT* oxyuv = (OutT*)out->xyuv;
     OutT* orgba = (OutT*)out->rgba;
     OutT* odepth = (OutT*)out->depth;
+    OutT* ocustom = cd->perspective_corrected ? (OutT*)out->custom0 : nullptr;
     uint32_t n = 0;
     for (uint32_t t : order) {
         size_t s_ = (size_t)slot + n;
@@ -1030,6 +1031,7 @@ uint32_t render_pair(const Frame<R>& F, Scratch<R>& S, const Pair& rp, uint32_t 
             oxyuv[4 * ci] = (OutT)dx; oxyuv[4 * ci + 1] = (OutT)dy; oxyuv[4 * ci + 2] = (OutT)uvU; oxyuv[4 * ci + 3] = (OutT)uvV;
             orgba[4 * ci] = (OutT)col.r; orgba[4 * ci + 1] = (OutT)col.g; orgba[4 * ci + 2] = (OutT)col.b; orgba[4 * ci + 3] = (OutT)col.a;
             odepth[ci] = (OutT)depthOut;
+            if (ocustom) ocustom[ci] = (OutT)((R)1 / w);  // Custom0 (camera.go:1700-1704)
         }
         n++;
     }

@@ -46,6 +46,8 @@ typedef struct t3d_oracle_out {
     uint32_t  reserved;
     uint32_t* seg_draw;          /* [max_segments] flush of each pair (a dynamic batch is one); may be NULL */
     uint32_t* seg_draw_transparent; /* that flush is in the transparent pass; may be NULL */
+    void*     custom0;           /* [max_tris*3] 1 / w per corner under perspective-corrected texture
+                                  * mapping (camera.go:1700-1704); may be NULL */
 } t3d_oracle_out;
 
 /* Renders one frame. light_mask may be NULL (all lights). animate_frames
@@ -73,12 +75,13 @@ typedef struct t3d_oracle_textures {
 /* Rasterises n triangles of one job in draw order (3 corners each: xyuv, rgba, depth as
  * t3d_frame_download writes them) into RGBA8 colour and depth images of the camera size
  * (pixel = r | g << 8 | b << 16 | a << 24); tri_pair = flush of each triangle,
- * pair_transparent indexed by that id; tex may be NULL (no textures, no alpha clip).
+ * pair_transparent indexed by that id; tex may be NULL (no textures, no alpha clip);
+ * custom0 (1 / w per corner) is read when the camera uses perspective-corrected mapping.
  * See t3d_oracle_raster.cpp. */
 int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, float dither, int32_t fogless, uint32_t n,
                       const float* xyuv, const float* rgba, const float* depth, const uint32_t* tri_pair,
                       const uint8_t* pair_transparent, const t3d_oracle_textures* tex, uint32_t* color_out,
-                      uint32_t* depth_out);
+                      uint32_t* depth_out, const float* custom0);
 
 /* Matrix4 helpers (float32) for pinning against matrix_test.go. */
 void t3d_oracle_mat_mult(const float* a, const float* b, float* out);

@@ -115,32 +115,39 @@ Texel sample(const t3d_oracle_textures* tx, uint32_t t, bool bilinear, float px,
     return {mixf(mixf(c0.r, c1.r, rx), mixf(c2.r, c3.r, rx), ry), mixf(mixf(c0.g, c1.g, rx), mixf(c2.g, c3.g, rx), ry),
             mixf(mixf(c0.b, c1.b, rx), mixf(c2.b, c3.b, rx), ry), mixf(mixf(c0.a, c1.a, rx), mixf(c2.a, c3.a, rx), ry)};
 }
-// the source position of a fragment: SrcX/SrcY, or screen mapped (TextureMapMode 1)
-void src_pos(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v, float& px, float& py) {
+// the source position of a fragment: SrcX/SrcY, screen mapped (TextureMapMode 1), or
+// under perspective correction times 1 / Custom0 (base3d.kage:77-81, camera.go:452-455);
+// c is null when the camera does not correct
+void src_pos(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v, const float* c, float& px,
+             float& py) {
     px = u;
     py = v;
     if (tx->flush_flags[fl] & 2u) {
         px = (x * tx->flush_scale[2 * fl]) + u;
         py = (y * tx->flush_scale[2 * fl + 1]) + v;
+    } else if (c) {
+        const float r = 1.0f / *c;
+        px = px * r;
+        py = py * r;
     }
 }
 // the colour pass's texel: wrapped with mod (base3d.kage:86); white without a texture
-Texel colour_texel(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v) {
+Texel colour_texel(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v, const float* c) {
     if (!tx || tx->flush_texture[fl] == 0u) return {1.0f, 1.0f, 1.0f, 1.0f};
     const uint32_t t = tx->flush_texture[fl] - 1;
     float px, py;
-    src_pos(tx, fl, x, y, u, v, px, py);
+    src_pos(tx, fl, x, y, u, v, c, px, py);
     px = gmod(px, (float)tx->tex_w[t]);
     py = gmod(py, (float)tx->tex_h[t]);
     return sample(tx, t, tx->flush_flags[fl] & 1u, px, py);
 }
 // the clip-alpha shader's texture alpha: wrapped with fract of the UV (camera.go:458-465)
-float clip_alpha(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v) {
+float clip_alpha(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, float u, float v, const float* c) {
     if (tx->flush_texture[fl] == 0u) return 1.0f;
     const uint32_t t = tx->flush_texture[fl] - 1;
     const float w = (float)tx->tex_w[t], h = (float)tx->tex_h[t];
     float px, py;
-    src_pos(tx, fl, x, y, u, v, px, py);
+    src_pos(tx, fl, x, y, u, v, c, px, py);
     px = fractf(px / w) * w;
     py = fractf(py / h) * h;
     return sample(tx, t, tx->flush_flags[fl] & 1u, px, py).a;
@@ -151,7 +158,8 @@ float clip_alpha(const t3d_oracle_textures* tx, uint32_t fl, float x, float y, f
 extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, float dither, int32_t fogless,
                                  uint32_t n, const float* xyuv, const float* rgba, const float* depth,
                                  const uint32_t* tri_pair, const uint8_t* pair_transparent,
-                                 const t3d_oracle_textures* tex, uint32_t* color_out, uint32_t* depth_out) {
+                                 const t3d_oracle_textures* tex, uint32_t* color_out, uint32_t* depth_out,
+                                 const float* custom0) {
     const int W = cam->width, H = cam->height;
     if (W <= 0 || H <= 0) return -1;
     const int fog_mode = cam->fog_on ? cam->fog_mode : -1;
@@ -169,7 +177,8 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
         for (int px = 0; px < W; px++) {
             const float x = (float)px + 0.5f, y = (float)py + 0.5f;
             const std::vector<uint32_t>& L = lists[(size_t)py * W + px];
-            auto frag = [&](uint32_t c, float* out7) {  // depth, r, g, b, a, SrcX, SrcY
+            const bool pc = cam->perspective_corrected && custom0;
+            auto frag = [&](uint32_t c, float* out7) {  // depth, r, g, b, a, SrcX, SrcY, Custom0
                 const Tri t = tri_of(xyuv, c, W, H);
                 float wa, wb, wc;
                 covers(t, x, y, wa, wb, wc);
@@ -179,6 +188,11 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
                 out7[0] = ((wa * d[0] + wb * d[1]) + wc * d[2]) / t.area;
                 for (int q = 0; q < 4; q++) out7[1 + q] = ((wa * k[q] + wb * k[4 + q]) + wc * k[8 + q]) / t.area;
                 for (int q = 0; q < 2; q++) out7[5 + q] = ((wa * p[2 + q] + wb * p[6 + q]) + wc * p[10 + q]) / t.area;
+                out7[7] = 0.0f;
+                if (pc) {
+                    const float* cw = custom0 + 3 * (size_t)c;
+                    out7[7] = ((wa * cw[0] + wb * cw[1]) + wc * cw[2]) / t.area;
+                }
             };
             uint32_t rc = 0, rd = 0;
             size_t i = 0;
@@ -186,14 +200,14 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
                 const uint32_t s = tri_pair[L[i]];
                 size_t e = i + 1;
                 while (e < L.size() && tri_pair[L[e]] == s) e++;
-                float f[7];
+                float f[8];
                 if (cam->render_depth) {
                     uint32_t inter = 0;
                     const bool clip = tex && (tex->flush_flags[s] & 4u);
                     for (size_t q = i; q < e; q++) {
                         frag(L[q], f);
                         if (clip) {  // discard at texture alpha <= 0.8; (encodeDepth.rgb, alpha) over the intermediate
-                            const float ta = clip_alpha(tex, s, x, y, f[5], f[6]);
+                            const float ta = clip_alpha(tex, s, x, y, f[5], f[6], pc ? &f[7] : nullptr);
                             if (ta <= 0.8f) continue;
                             if ((rd >> 24) == 0u || decode_depth(rd) > f[0]) {
                                 const uint32_t enc = encode_depth(f[0]);
@@ -206,7 +220,7 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
                     if ((inter >> 24) != 0u) {
                         for (size_t q = i; q < e; q++) {
                             frag(L[q], f);
-                            const Texel tc = colour_texel(tex, s, x, y, f[5], f[6]);
+                            const Texel tc = colour_texel(tex, s, x, y, f[5], f[6], pc ? &f[7] : nullptr);
                             float r = tc.r * f[1], g = tc.g * f[2], b = tc.b * f[3];
                             const float a = tc.a * f[4];
                             r *= f[4]; g *= f[4]; b *= f[4];
@@ -240,7 +254,7 @@ extern "C" int t3d_oracle_raster(const t3d_camera_desc* cam, int32_t fog_curve, 
                 } else {
                     for (size_t q = i; q < e; q++) {
                         frag(L[q], f);
-                        const Texel tc = colour_texel(tex, s, x, y, f[5], f[6]);
+                        const Texel tc = colour_texel(tex, s, x, y, f[5], f[6], pc ? &f[7] : nullptr);
                         rc = blend_over(rc, tc.r * (f[1] * f[4]), tc.g * (f[2] * f[4]), tc.b * (f[3] * f[4]), tc.a * f[4]);
                     }
                 }

@@ -726,3 +726,64 @@ def test_full_frame_variants_match_oracle(ctx, kind):
         assert_frames_equal(ctx.download(), ref, f"frame/{kind}")
     finally:
         ctx.release(sid)
+
+
+CUSTOM0_SCENES = [
+    ("sphere", lambda: scenes.uv_sphere_scene(1)),
+    ("cubes", lambda: scenes.small_variant("cubes", 3)),
+    ("features", lambda: scenes.feature_scene(5)),
+    ("skinned", lambda: scenes.skinned_scene(7)),
+    ("billboards", lambda: scenes.billboard_scene(9)),
+    ("subdivision", lambda: scenes.subdivision_scene(10)),
+    ("batches", lambda: scenes.batch_scene(11)),
+    ("nested_lights", lambda: scenes.nested_light_scene(6)),
+]
+
+
+@pytest.mark.parametrize("name,make", CUSTOM0_SCENES, ids=[c[0] for c in CUSTOM0_SCENES])
+@pytest.mark.parametrize("variant", ["persp", "tilted", "ortho"])
+def test_custom0_stream_matches_oracle(ctx, name, make, variant):
+    """Perspective-corrected texture mapping: every corner's UV / w and Custom0 = 1 / w
+    (camera.go:1689-1704) on the meshlet, record, skinned, billboard and subdivided routes,
+    both forms, bit for bit against the oracle."""
+    sd = make()
+    cam = scenes.corrected_camera(variant)
+    ref = pyoracle.render(sd, cam)
+    assert ref.custom0 is not None and ref.visible_tris > 0
+    sid = ctx.upload(sd)
+    try:
+        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+            ctx.render(sid, cam, mode=mode)
+            got = ctx.download()
+            assert_frames_equal(got, ref, f"custom0/{name}/{variant}/mode{mode}")
+            c0 = ctx.download_custom0()
+            assert np.array_equal(bits(c0), bits(ref.custom0)), f"custom0/{name}/{variant}/mode{mode}: Custom0"
+    finally:
+        ctx.release(sid)
+
+
+def test_custom0_only_for_corrected_jobs(ctx):
+    """Two jobs in one launch, one with perspective-corrected mapping: Custom0 holds 1 / w for
+    its corners and 0 for the other job's; a frame without the option has no Custom0."""
+    sd = scenes.feature_scene(5)
+    sid = ctx.upload(sd)
+    try:
+        cams = [scenes.corrected_camera("persp"), scenes.feature_camera("tilted")]
+        ctx.render_jobs([job(sid, c, None) for c in cams])
+        got = ctx.download()
+        c0 = ctx.download_custom0()
+        parts = split_jobs(got, 2)
+        for j, cam in enumerate(cams):
+            assert_frames_equal(parts[j], pyoracle.render(sd, cam), f"custom0 jobs/{j}")
+        b, sel = 0, [[], []]
+        for s in got.segments:
+            sel[s["job"]].extend(range(b, b + s["count"]))
+            b += s["count"]
+        assert np.array_equal(bits(c0[sel[0]]), bits(pyoracle.render(sd, cams[0]).custom0))
+        assert not c0[sel[1]].any()
+        ctx.render(sid, scenes.feature_camera("persp"))
+        ctx.sync()
+        with pytest.raises(abi.T3DError):
+            ctx.download_custom0()
+    finally:
+        ctx.release(sid)

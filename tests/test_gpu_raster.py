@@ -91,6 +91,13 @@ TEX_CASES = [
     ("textured_batches", lambda: (scenes.texture_materials(scenes.batch_scene(12), 12), scenes.feature_camera("persp")),
      {}),
     ("textured_tiled_uvs", lambda: (_tiled_uvs(scenes.textured_scene(26)), scenes.feature_camera("tilted")), {}),
+    # perspective-corrected texture mapping: UV / w and Custom0 = 1 / w interpolated, divided per pixel
+    ("textured_corrected", lambda: (scenes.textured_scene(27), scenes.feature_camera("corrected")), {}),
+    ("textured_corrected_tilted", lambda: (scenes.textured_scene(28), scenes.corrected_camera("tilted")), {}),
+    ("textured_corrected_ortho", lambda: (scenes.textured_scene(29), scenes.corrected_camera("ortho")), {}),
+    ("textured_corrected_no_depth", lambda: (scenes.textured_scene(30), scenes.corrected_camera("fog_add")), {}),
+    ("textured_corrected_tiled_uvs", lambda: (_tiled_uvs(scenes.textured_scene(31)), scenes.feature_camera("corrected")),
+     {}),
 ]
 
 
@@ -126,9 +133,6 @@ def test_texture_errors(ctx):
         with pytest.raises(abi.T3DError):
             ctx.raster()
         ctx.set_textures(scenes.raster_textures())
-        ctx.render(sid, scenes.feature_camera("corrected"))  # textures need the 1/w attribute there
-        with pytest.raises(abi.T3DError):
-            ctx.raster()
         ctx.render(sid, scenes.feature_camera("persp"))
         col, _ = ctx.raster()
         assert col[..., 3].any()

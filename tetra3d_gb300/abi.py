@@ -172,6 +172,7 @@ SIGNATURES = {
     "t3d_frame_view_get": (C.c_int, [_VP, C.POINTER(FrameView)]),
     "t3d_frame_segments": (C.c_int, [_VP, C.POINTER(SegmentInfo), C.c_uint32, C.POINTER(C.c_uint32)]),
     "t3d_frame_download": (C.c_int, [_VP, f32p, f32p, f32p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "t3d_frame_download_custom0": (C.c_int, [_VP, f32p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "t3d_graph_capture": (C.c_int, [_VP, C.c_uint32, C.POINTER(CameraDesc), C.c_int]),
     "t3d_graph_replay": (C.c_int, [_VP, C.c_uint32, _VP]),
     "t3d_server_create": (C.c_int, [_VP, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(_VP)]),

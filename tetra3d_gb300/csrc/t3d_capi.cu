@@ -123,7 +123,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights,
-                      &ctx->job_bytes, &ctx->vis_rank})
+                      &ctx->job_bytes, &ctx->vis_rank, &ctx->vinvw, &ctx->out_invw})
         b->release();
     ctx->table_host.release();
     ctx->readback.release();
@@ -466,7 +466,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     size_t scratch = 0;
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count,
-                      &ctx->inst_lights, &ctx->vis_rank})
+                      &ctx->inst_lights, &ctx->vis_rank, &ctx->vinvw})
         scratch += b->cap;
     s.scratch_bytes = scratch;
     s.h2d_bytes = ctx->last_h2d;
@@ -540,6 +540,37 @@ int t3d_frame_download(t3d_ctx* ctx, float* xyuv, float* rgba, float* depth, uin
         if (xyuv) CKR(cudaMemcpy(xyuv + 12 * n, (char*)ctx->out_xyuv.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost));
         if (rgba) CKR(cudaMemcpy(rgba + 12 * n, (char*)ctx->out_rgba.ptr + 48ull * si.base, 48ull * si.count, cudaMemcpyDeviceToHost));
         if (depth) CKR(cudaMemcpy(depth + 3 * n, (char*)ctx->out_depth.ptr + 12ull * si.base, 12ull * si.count, cudaMemcpyDeviceToHost));
+        n += si.count;
+    }
+    if (tris_out) *tris_out = n;
+    return T3D_OK;
+}
+
+int t3d_frame_download_custom0(t3d_ctx* ctx, float* custom0, uint64_t max_tris, uint64_t* tris_out) {
+    if (!ctx || !custom0) return T3D_E_INVAL;
+    if (!ctx->frame_valid) {
+        set_err(ctx, "frame_download_custom0: call t3d_frame_sync first");
+        return T3D_E_INVAL;
+    }
+    if (!ctx->tables.any_pcorrect) {
+        set_err(ctx, "frame_download_custom0: no job of the last frame uses perspective-corrected texture mapping");
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    uint64_t n = 0;
+    for (size_t k = 0; k < ctx->tables.seg_info.size(); k++) {
+        const auto& si = ctx->tables.seg_info[k];
+        if (!si.count) continue;
+        if (n + si.count > max_tris) {
+            set_err(ctx, "frame_download_custom0: %llu triangles do not fit %llu", (unsigned long long)(n + si.count),
+                    (unsigned long long)max_tris);
+            return T3D_E_INVAL;
+        }
+        if (ctx->tables.segs[k].flags & SEG_PCORRECT)
+            CKR(cudaMemcpy(custom0 + 3 * n, (char*)ctx->out_invw.ptr + 12ull * si.base, 12ull * si.count,
+                           cudaMemcpyDeviceToHost));
+        else
+            memset(custom0 + 3 * n, 0, 12ull * si.count);
         n += si.count;
     }
     if (tris_out) *tris_out = n;

@@ -46,6 +46,8 @@ enum : uint32_t {
     SEG_MESHLET = 1u << 25,     // tiles are meshlets: contiguous vertex blocks with 16-bit local indices
     SEG_SINGLE = 1u << 26,      // a meshlet pair of one tile: its output order is its rank order (no
                                 // histogram or cross-tile scan)
+    SEG_PCORRECT = 1u << 27,    // Camera.PerspectiveCorrectedTextureMapping: each corner also emits
+                                // Custom0 = 1 / w (camera.go:1700-1704)
     // parts whose tiles need more than the plain triangle loop (their own loop, queue 7)
     SEG_ALT_TILES = SEG_SKINNED | SEG_SUBDIV,
     // parts whose vertex records need more than the plain loop (their own loop, queue 5)
@@ -247,6 +249,7 @@ struct FrameParams {
     float4* vxyuv;                // emitted screen position + UV
     float4* vrgba;                // emitted colour
     float4* valt;                 // skinned pairs: world-space skinned position per record (depth key)
+    float* vinvw;                 // SEG_PCORRECT pairs: 1 / w per record (Custom0); may be null
     // meshlet tiles: per visible entry in the tile's output order, its list entry j (bits 0-10),
     // bin (11-19) and position among the tile's entries of that bin (20-30), from the histogram phase
     uint32_t* vis_rank;
@@ -264,6 +267,7 @@ struct FrameParams {
     float4* out_xyuv;
     float4* out_rgba;
     float* out_depth;
+    float* out_invw;              // Custom0 per corner, written for SEG_PCORRECT pairs; may be null
     Ctl* ctl;
     unsigned long long* accum;    // [0] visible triangles, [1] model bytes; cumulative across frames
     // ranges processed by this launch
@@ -284,7 +288,9 @@ struct FrameParams {
     uint32_t mesh_begin, mesh_end;
     uint32_t mt_mesh_begin, mt_mesh_end;
     uint32_t spin_limit;          // bounded waits: polls before giving up (0 = the default)
-    uint32_t pad;
+    // phases this launch runs (bit 0 prep, 1 vertex records, 2 triangles, 3 histogram, 4 scan,
+    // 5 rank + emit), with grid barriers only between phases of the same launch; 0 = all
+    uint32_t phases;
     // meshlet frames: per instance, kMaxLights records of 56 bytes (the light list
     // the vertex loop reads, staged once by the prep phase); null otherwise
     float4* inst_lights;

@@ -31,6 +31,7 @@ __device__ __forceinline__ uint32_t spin_limit(const FrameParams& P) { return P.
 __device__ bool grid_barrier(Ctl* ctl, uint32_t limit) {
     __threadfence();
     __syncthreads();
+    if (gridDim.x == 1) return vload(&ctl->err) == 0;  // one block: the block barrier is the grid barrier
     if (threadIdx.x == 0) {
         uint32_t gen = vload(&ctl->bar_gen);
         __threadfence();
@@ -765,6 +766,15 @@ __device__ __forceinline__ void vertex_record(const ModelSmem& ms, const float4 
     rgba = make_float4(cr, cg, cb, ca);
 }
 
+// Custom0 of a corner under perspective-corrected texture mapping (camera.go:1669-1704):
+// 1 / w with the emit loop's w (1 for an orthographic camera, 0.001 when negative).
+__device__ __forceinline__ float corner_invw(const ModelSmem& ms, const float4 a) {
+    float w = clip_of(ms.mvpc, a.x, a.y, a.z).w;
+    if (!(ms.ec.flags & EC_PERSP)) w = 1.0f;
+    if (w < 0.0f) w = 0.001f;
+    return 1.0f / w;
+}
+
 __device__ __forceinline__ uint32_t walk_pos(uint32_t b, uint32_t sort_mode) {
     return sort_mode == T3D_SORT_BACK_TO_FRONT ? (uint32_t)(kBins - 1) - b : b;
 }
@@ -879,6 +889,7 @@ __device__ void tile_emit(const FrameParams& P, const TileDesc& td, const SmemLa
     float4* __restrict__ oxyuv = P.out_xyuv + 3 * (size_t)td.out_base;
     float4* __restrict__ orgba = P.out_rgba + 3 * (size_t)td.out_base;
     float* __restrict__ odepth = P.out_depth + 3 * (size_t)td.out_base;
+    const bool pcorrect = td.flags & SEG_PCORRECT;
     const uint32_t vs = td.vscratch, vm = td.vmin, t0 = td.t0;
     const uint32_t total = 3 * n, B = blockDim.x;
     for (uint32_t q0 = threadIdx.x; q0 < total; q0 += kILP * B) {
@@ -924,6 +935,7 @@ __device__ void tile_emit(const FrameParams& P, const TileDesc& td, const SmemLa
                 orgba[oc[u]] = k[u];
                 odepth[oc[u]] = d[u];
 #endif
+                if (pcorrect) P.out_invw[3 * (size_t)td.out_base + oc[u]] = rec_load(&P.vinvw[o[u]]);
             }
         }
     }
@@ -1052,6 +1064,7 @@ __device__ __forceinline__ void vertex_chunk_altered(const FrameParams& P, const
         P.vxyuv[o] = xyuv;
         P.vrgba[o] = rgba;
         if (skinned) P.valt[o] = make_float4(a.x, a.y, a.z, 0.0f);
+        if (seg.flags & SEG_PCORRECT) P.vinvw[o] = corner_invw(ms, a);
     }
 }
 
@@ -1166,6 +1179,7 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
             P.vcull[o] = cull;
             P.vxyuv[o] = xyuv;
             P.vrgba[o] = rgba;
+            if (seg.flags & SEG_PCORRECT) P.vinvw[o] = corner_invw(ms, a);
             a = na;
             b = nb;
             k = nk;
@@ -2025,6 +2039,7 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
         const uint32_t U = td.vmin, U4 = mlet_slots4(U), nt = td.t1 - td.t0;
         const bool colors = td.flags & SEG_COLORS;
         const bool single = td.flags & SEG_SINGLE;
+        const bool pcorrect = td.flags & SEG_PCORRECT;
         const uint32_t as = mlet_aos_stride(colors);
         // the vertex block lands at the end of the record area: a slot's 48-byte record then
         // only ever covers input bytes of its own or earlier slots
@@ -2082,7 +2097,7 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
                 float4* out = reinterpret_cast<float4*>(rec + (size_t)kRecBytes * v);
                 out[0] = xyuv;
                 out[1] = rgba;
-                out[2] = make_float4(cull.w, 0.f, 0.f, 0.f);
+                out[2] = make_float4(cull.w, pcorrect ? corner_invw(ms, a) : 0.f, 0.f, 0.f);
             }
         }
         if (threadIdx.x == 0) {
@@ -2112,6 +2127,7 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
                 oxyuv[3 * pos + cc] = rc[0];
                 orgba[3 * pos + cc] = rc[1];
                 odepth[3 * pos + cc] = reinterpret_cast<const float*>(rc + 2)[0];
+                if (pcorrect) P.out_invw[3 * ((size_t)td.out_base + pos) + cc] = reinterpret_cast<const float*>(rc + 2)[1];
             }
         }
         } else if (threadIdx.x == 0 && kn < nmt) {  // an empty tile: stage the next one now
@@ -2164,35 +2180,50 @@ __global__ void __launch_bounds__(256, kM ? T3D_MESH_BLOCKS : T3D_MIN_BLOCKS) t3
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long since = 0;
     const uint32_t limit = spin_limit(P);
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl->t_end[7] = global_ns();
-    phase_start(since);
-    phase_prep<kM>(P);
-    phase_done(P.ctl, 0, since);
-    if (!grid_barrier(P.ctl, limit)) return;
-    phase_start(since);
-    if (P.vitem_begin < P.vitem_alt) phase_vertex<kM>(P, smem);
-    if (P.vitem_alt < P.vitem_end) phase_vertex_altered<kM>(P, smem);
-    phase_done(P.ctl, 6, since);
-    if (!grid_barrier(P.ctl, limit)) return;
-    phase_start(since);
-    if (kM && P.mesh_begin < P.mesh_end) phase_triangles_meshlet<kM>(P, smem);
-    if (P.tile_begin < P.tile_alt) phase_triangles<kM>(P, smem);
-    if (P.tile_alt < P.tile_end) phase_triangles_skinned<kM>(P, smem);
-    phase_done(P.ctl, 1, since);
+    const uint32_t ph = P.phases ? P.phases : 0x3Fu;
+    // a grid barrier after phase bit b when this launch also runs a later phase
+    auto barrier_after = [&](uint32_t b) { return !(ph & b) || !(ph & ~(2u * b - 1u)) || grid_barrier(P.ctl, limit); };
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (ph & 1u)) P.ctl->t_end[7] = global_ns();
+    if (ph & 1u) {
+        phase_start(since);
+        phase_prep<kM>(P);
+        phase_done(P.ctl, 0, since);
+    }
+    if (!barrier_after(1u)) return;
+    if (ph & 2u) {
+        phase_start(since);
+        if (P.vitem_begin < P.vitem_alt) phase_vertex<kM>(P, smem);
+        if (P.vitem_alt < P.vitem_end) phase_vertex_altered<kM>(P, smem);
+        phase_done(P.ctl, 6, since);
+    }
+    if (!barrier_after(2u)) return;
+    if (ph & 4u) {
+        phase_start(since);
+        if (kM && P.mesh_begin < P.mesh_end) phase_triangles_meshlet<kM>(P, smem);
+        if (P.tile_begin < P.tile_alt) phase_triangles<kM>(P, smem);
+        if (P.tile_alt < P.tile_end) phase_triangles_skinned<kM>(P, smem);
+        phase_done(P.ctl, 1, since);
+    }
     if (!P.has_multi) return;
-    if (!grid_barrier(P.ctl, limit)) return;
-    phase_start(since);
-    phase_hist<kM>(P, smem);
-    phase_done(P.ctl, 2, since);
-    if (!grid_barrier(P.ctl, limit)) return;
-    phase_start(since);
-    phase_scan<kM>(P, smem);
-    phase_done(P.ctl, 3, since);
-    if (!grid_barrier(P.ctl, limit)) return;
-    phase_start(since);
-    if (P.mt_tile_begin < P.mt_tile_end) phase_rank_multi<kM>(P, smem);
-    if (kM && P.mt_mesh_begin < P.mt_mesh_end) phase_rank_meshlet<kM>(P, smem);
-    phase_done(P.ctl, 4, since);
+    if (!barrier_after(4u)) return;
+    if (ph & 8u) {
+        phase_start(since);
+        phase_hist<kM>(P, smem);
+        phase_done(P.ctl, 2, since);
+    }
+    if (!barrier_after(8u)) return;
+    if (ph & 16u) {
+        phase_start(since);
+        phase_scan<kM>(P, smem);
+        phase_done(P.ctl, 3, since);
+    }
+    if (!barrier_after(16u)) return;
+    if (ph & 32u) {
+        phase_start(since);
+        if (P.mt_tile_begin < P.mt_tile_end) phase_rank_multi<kM>(P, smem);
+        if (kM && P.mt_mesh_begin < P.mt_mesh_end) phase_rank_meshlet<kM>(P, smem);
+        phase_done(P.ctl, 4, since);
+    }
 }
 
 }  // namespace t3d

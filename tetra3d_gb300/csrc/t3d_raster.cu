@@ -70,6 +70,7 @@ struct RasterJob {
     const float4* xyuv;
     const float4* rgba;
     const float* depth;
+    const float* custom0;       // 1 / w per corner (perspective-corrected texture mapping), else null
     const uint32_t* cbase;      // exclusive prefix of the job's per-pair visible counts (nseg + 1)
     uint32_t seg_lo, nseg;      // the job's render pairs: segs[seg_lo, seg_lo + nseg)
     uint32_t big_cap;           // large triangles the shared list takes (<= kBigTriCap)
@@ -229,11 +230,13 @@ __device__ __forceinline__ uint32_t warp_fragments(const TriScreen& t, uint32_t 
 // linearly in screen space with the edge weights of `covers`.
 struct Frag {
     float d, r, g, b, a, u, v;
+    float c;  // Custom0 (perspective-corrected texture mapping only)
 };
 struct TriAttr {
     float4 ka, kb, kc;  // colour of the corners
     float da, db, dc;   // depth
     float ua, ub, uc, va, vb, vc;  // SrcX, SrcY
+    float ca, cb, cc;   // Custom0
 };
 __device__ __forceinline__ TriAttr tri_attr(const RasterJob& J, uint32_t slot) {
     TriAttr A;
@@ -241,10 +244,15 @@ __device__ __forceinline__ TriAttr tri_attr(const RasterJob& J, uint32_t slot) {
     A.da = J.depth[3 * (size_t)slot]; A.db = J.depth[3 * (size_t)slot + 1]; A.dc = J.depth[3 * (size_t)slot + 2];
     const float4 pa = J.xyuv[3 * (size_t)slot], pb = J.xyuv[3 * (size_t)slot + 1], pc = J.xyuv[3 * (size_t)slot + 2];
     A.ua = pa.z; A.ub = pb.z; A.uc = pc.z; A.va = pa.w; A.vb = pb.w; A.vc = pc.w;
+    A.ca = A.cb = A.cc = 0.0f;
+    if (J.custom0) {
+        A.ca = J.custom0[3 * (size_t)slot]; A.cb = J.custom0[3 * (size_t)slot + 1]; A.cc = J.custom0[3 * (size_t)slot + 2];
+    }
     return A;
 }
 __device__ __forceinline__ Frag interp(const TriAttr& A, float area, float wa, float wb, float wc) {
     Frag f;
+    f.c = ((wa * A.ca + wb * A.cb) + wc * A.cc) / area;
     f.d = ((wa * A.da + wb * A.db) + wc * A.dc) / area;
     f.r = ((wa * A.ka.x + wb * A.kb.x) + wc * A.kc.x) / area;
     f.g = ((wa * A.ka.y + wb * A.kb.y) + wc * A.kc.y) / area;
@@ -661,7 +669,12 @@ __device__ float4 colour_texel(const RasterJob& J, const DevSeg& sg, float x, fl
     if (sg.pad[1] == 0u) return make_float4(1.f, 1.f, 1.f, 1.f);
     const RasterTex T = J.texs[sg.pad[1] - 1];
     float tx = f.u, ty = f.v;
-    if (sg.pad[2] & 2u) { tx = (x * sg.pad2[0]) + f.u; ty = (y * sg.pad2[1]) + f.v; }
+    if (sg.pad[2] & 2u) {
+        tx = (x * sg.pad2[0]) + f.u; ty = (y * sg.pad2[1]) + f.v;
+    } else if (J.custom0) {  // tx *= 1.0 / custom.x (base3d.kage:79-81)
+        const float r = 1.0f / f.c;
+        tx = tx * r; ty = ty * r;
+    }
     tx = gmod(tx, (float)T.w);
     ty = gmod(ty, (float)T.h);
     return tex_sample(J, T, sg.pad[2] & 1u, tx, ty);
@@ -672,7 +685,12 @@ __device__ float clip_alpha(const RasterJob& J, const DevSeg& sg, float x, float
     const RasterTex T = J.texs[sg.pad[1] - 1];
     const float w = (float)T.w, h = (float)T.h;
     float tx = f.u, ty = f.v;
-    if (sg.pad[2] & 2u) { tx = (x * sg.pad2[0]) + f.u; ty = (y * sg.pad2[1]) + f.v; }
+    if (sg.pad[2] & 2u) {
+        tx = (x * sg.pad2[0]) + f.u; ty = (y * sg.pad2[1]) + f.v;
+    } else if (J.custom0) {  // camera.go:454-455
+        const float r = 1.0f / f.c;
+        tx = tx * r; ty = ty * r;
+    }
     tx = fractf(tx / w) * w;
     ty = fractf(ty / h) * h;
     return tex_sample(J, T, sg.pad[2] & 1u, tx, ty).w;
@@ -847,6 +865,7 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     J.xyuv = (const float4*)ctx->out_xyuv.ptr;
     J.rgba = (const float4*)ctx->out_rgba.ptr;
     J.depth = (const float*)ctx->out_depth.ptr;
+    J.custom0 = cam.persp_correct ? (const float*)ctx->out_invw.ptr : nullptr;
     J.segs = ctx->params.segs;
     J.texs = (const RasterTex*)R.texs.ptr;
     J.texels = (const uint32_t*)R.texels.ptr;
@@ -858,10 +877,6 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
         if (!t) continue;
         if (t > R.tex.size()) {
             set_err(ctx, "frame_raster: texture %u of a material is not in the table of %zu", t, R.tex.size());
-            return T3D_E_INVAL;
-        }
-        if (cam.persp_correct) {
-            set_err(ctx, "frame_raster: textures under perspective-corrected mapping are not supported");
             return T3D_E_INVAL;
         }
     }

@@ -1279,6 +1279,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (me.subdiv) flags |= SEG_SUBDIV;
             flags |= billboard_flags(mat, m.d.skinned != 0);
             if (cd.vertex_snapping > 0.0f) flags |= SEG_SNAP;
+            if (cd.perspective_corrected) { flags |= SEG_PCORRECT; F.any_pcorrect = true; }
             if (flags & (SEG_ALTERED | SEG_ALT_TILES)) F.any_altered = true;
             // pairs that need no more than the plain vertex loop take their part's meshlets
             const std::vector<Meshlet>* mls = nullptr;
@@ -1544,6 +1545,13 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         P.vis_rank = (uint32_t*)ctx->vis_rank.ptr;
     }
 
+    P.vinvw = nullptr;
+    P.out_invw = nullptr;
+    if (F.any_pcorrect) {  // Custom0: 1 / w per record and per emitted corner
+        if ((rc = ctx->vinvw.ensure(ctx, 4 * nsc)) || (rc = ctx->out_invw.ensure(ctx, 12 * nslots))) return rc;
+        P.vinvw = (float*)ctx->vinvw.ptr;
+        P.out_invw = (float*)ctx->out_invw.ptr;
+    }
     P.vcull = (float4*)ctx->vcull.ptr;
     P.valt = (float4*)ctx->valt.ptr;
     P.vxyuv = (float4*)ctx->vxyuv.ptr;
@@ -1582,11 +1590,14 @@ static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items,
     cfg.blockDim = dim3(ctx->block_threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
+    // grid barriers need every block resident: a cooperative launch when more than one block
+    // runs more than one phase (one block, or one phase per launch, needs none)
+    const bool coop = grid > 1 && (P.phases == 0 || (P.phases & (P.phases - 1)) != 0);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.attrs = coop ? attr : nullptr;
+    cfg.numAttrs = coop ? 1 : 0;
     cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
     if (e != cudaSuccess) {
         set_err(ctx, "frame kernel launch failed: %s (grid %u, block %u, smem %zu)", cudaGetErrorString(e), grid,
@@ -1631,9 +1642,12 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
                                              (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
         return launch_one(ctx, P, ctl, items, st);
     }
-    // Plain: one launch per render pair, in draw order (render + flush per pair,
-    // camera.go:2061-2106). A model's prep (and animation step) runs with its
-    // first pair; its later pairs recompute the same prep without animating.
+    // Plain: render pairs one after another, in draw order (render + flush per pair,
+    // camera.go:2061-2106). A pair of one tile is one launch of one block (its phases
+    // separated by block barriers); a pair of several tiles is a sequence of launches of
+    // one phase each (prep, vertex records, triangles, histogram, scan, rank + emit), so
+    // no launch waits on a grid barrier. A model's prep (and animation step) runs with
+    // its first pair; its later pairs recompute the same prep without animating.
     std::vector<char> animated(F.insts.size(), 0);
     for (size_t s = 0; s < F.segs.size(); s++) {
         const DevSeg& sg = F.segs[s];
@@ -1668,8 +1682,19 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
             P.insts = ctx->insts_noanim;
         }
         animated[sg.inst] = 1;
-        uint32_t items = std::max({sg.ntiles, P.vitem_end - P.vitem_begin, 1u});
-        if ((rc = launch_one(ctx, P, ctl + s, items, st))) return rc;
+        if (sg.ntiles <= 1) {
+            P.phases = 0;
+            if ((rc = launch_one(ctx, P, ctl + s, 1u, st))) return rc;
+            continue;
+        }
+        const uint32_t vitems = P.vitem_end - P.vitem_begin;
+        const bool scan = P.mt_seg_begin < P.mt_seg_end;
+        const uint32_t seq[6][2] = {{1u, 1u}, {2u, vitems}, {4u, sg.ntiles}, {8u, sg.ntiles}, {16u, 1u}, {32u, sg.ntiles}};
+        for (const auto& q : seq) {
+            if ((q[0] == 2u && vitems == 0) || (q[0] >= 8u && !P.has_multi) || (q[0] == 16u && !scan)) continue;
+            P.phases = q[0];
+            if ((rc = launch_one(ctx, P, ctl + s, q[1], st))) return rc;
+        }
     }
     return T3D_OK;
 }

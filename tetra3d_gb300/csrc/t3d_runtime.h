@@ -106,6 +106,7 @@ struct FrameTables {
     std::vector<uint32_t> vitem_seg, vitem_chunk, seg_vitem_first;
     uint64_t nscratch = 0, nslots = 0;
     bool any_skinned = false, any_altered = false, any_mesh = false;
+    bool any_pcorrect = false;             // a job's camera uses perspective-corrected texture mapping
     uint32_t tile_alt = 0, vitem_alt = 0;  // first tile of a skinned part / vertex item of an altered part
     uint32_t tile_mesh = 0;                // first meshlet tile (tiles: record-path plain | record-path altered | meshlet)
     uint32_t mt_mesh = 0;                  // first meshlet multi-tile number (mt_desc: record path | meshlet)
@@ -114,7 +115,8 @@ struct FrameTables {
         insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
         seg_mt_seg.clear(); tiles.clear(); mt_desc.clear(); mt_segs.clear();
         vitem_seg.clear(); vitem_chunk.clear(); seg_vitem_first.clear();
-        nscratch = 0; nslots = 0; any_skinned = false; any_altered = false; any_mesh = false; tile_alt = 0; vitem_alt = 0;
+        nscratch = 0; nslots = 0; any_skinned = false; any_altered = false; any_mesh = false; any_pcorrect = false;
+        tile_alt = 0; vitem_alt = 0;
         tile_mesh = 0; mt_mesh = 0;
     }
 };
@@ -155,7 +157,7 @@ struct t3d_ctx {
     cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
     cudaEvent_t ev_models = nullptr;  // the last model write has reached the device (and left its staging)
     struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
-    t3d::DevBuf valt, inst_lights, job_bytes, vis_rank;
+    t3d::DevBuf valt, inst_lights, job_bytes, vis_rank, vinvw, out_invw;
     bool want_job_bytes = false;  // serving slots: per-job algorithmic bytes (FrameParams.job_bytes)
     uint32_t grid_share = 1;      // serving slots: launches use 1/grid_share of the co-resident blocks
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,

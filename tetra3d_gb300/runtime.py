@@ -132,6 +132,17 @@ class Context:
                                                 C.byref(got)), "frame_download")
         return Frame(xyuv[:n], rgba[:n], depth[:n], self.segments(), st)
 
+    def download_custom0(self, stats=None):
+        """Custom0 (1 / w) of the last frame's visible corners, (n, 3) float32, same order as
+        download(); the frame must use perspective-corrected texture mapping."""
+        st = stats or self.sync()
+        n = int(st.visible_tris)
+        out = np.zeros((max(1, n), 3), np.float32)
+        got = C.c_uint64()
+        self._check(self.lib.t3d_frame_download_custom0(self.h, abi.fptr(out), n, C.byref(got)),
+                    "frame_download_custom0")
+        return out[:n]
+
     def counters(self):
         v, b = C.c_uint64(), C.c_uint64()
         self._check(self.lib.t3d_frame_counters(self.h, C.byref(v), C.byref(b)), "frame_counters")

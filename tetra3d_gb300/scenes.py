@@ -1145,6 +1145,13 @@ def feature_camera(variant, w=1280, h=720):
     return c
 
 
+def corrected_camera(variant, w=1280, h=720):
+    """feature_camera(variant) with Camera.PerspectiveCorrectedTextureMapping on."""
+    c = feature_camera(variant, w, h)
+    c.perspective_corrected = 1
+    return c
+
+
 def small_variant(kind, seed):
     """Reduced-size versions of the workloads for oracle comparisons."""
     if kind == "sphere":
