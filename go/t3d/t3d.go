@@ -169,6 +169,18 @@ func (c *Context) Download(maxTris uint64) (xyuv, rgba, depth []float32, err err
 	return xyuv[:12*n], rgba[:12*n], depth[:3*n], c.err(rc)
 }
 
+// DownloadCustom0 copies ebiten.Vertex.Custom0 of every downloaded corner (same order as
+// Download): 1 / w when Camera.PerspectiveCorrectedTextureMapping is on (camera.go:1700-1704).
+func (c *Context) DownloadCustom0(maxTris uint64) ([]float32, error) {
+	if maxTris == 0 {
+		return nil, nil
+	}
+	out := make([]float32, 3*maxTris)
+	var n C.uint64_t
+	rc := C.t3d_frame_download_custom0(c.h, (*C.float)(unsafe.Pointer(&out[0])), C.uint64_t(maxTris), &n)
+	return out[:3*n], c.err(rc)
+}
+
 // UpdateArmature copies the boneInfluence matrices of bones first..first+n.
 func (c *Context) UpdateArmature(scene uint32, first int, influences []tetra3d.Matrix4) error {
 	if len(influences) == 0 {

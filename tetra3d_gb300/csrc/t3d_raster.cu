@@ -454,9 +454,9 @@ __global__ void __launch_bounds__(kFragThreads, 5) k_big_count(RasterJob J, cons
 __global__ void __launch_bounds__(kFragThreads, 4) k_frag_write(RasterJob J, uint32_t nunits, const uint4* __restrict__ hits,
                                                              const uint32_t* __restrict__ uhits,
                                                              const uint32_t* __restrict__ ufoff, BigTri* big,
-                                                             uint32_t* keys, uint32_t* vals) {
+                                                             uint32_t* keys, uint32_t* vals, const uint32_t* fcount) {
     const uint32_t lane = threadIdx.x & 31, u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (u >= nunits) return;  // the whole warp
+    if (u >= nunits || fcount[1] == 0u) return;  // the whole warp; nothing when the buffers are too small
     const uint32_t base = u * kUnitTris, nh = uhits[u];
     uint32_t run = ufoff[u];
     for (uint32_t j = 0; j < nh; j += 32) {
@@ -516,8 +516,8 @@ __global__ void __launch_bounds__(kFragThreads, 4) k_frag_write(RasterJob J, uin
 // triangle's range does not matter: a triangle has at most one fragment per pixel.
 __global__ void __launch_bounds__(kFragThreads, 5) k_big_write(RasterJob J, BigTri* big, const uint32_t* __restrict__ chunk_tri,
                                                            const unsigned long long* __restrict__ ctr, uint32_t* keys,
-                                                           uint32_t* vals) {
-    const uint32_t lane = threadIdx.x & 31, nch = shared_chunks(ctr);
+                                                           uint32_t* vals, const uint32_t* fcount) {
+    const uint32_t lane = threadIdx.x & 31, nch = fcount[1] ? shared_chunks(ctr) : 0u;
     const uint32_t nw = gridDim.x * (blockDim.x >> 5);
     for (uint32_t ch = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nch; ch += nw) {
         const uint32_t b = chunk_tri[ch];
@@ -550,7 +550,9 @@ __global__ void __launch_bounds__(kFragThreads, 5) k_big_write(RasterJob J, BigT
 }
 
 // ---- stable LSD radix sort of (key, value) pairs by kSortBits-bit digits --------
-__global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t nblocks, uint32_t* counts) {
+__global__ void k_sort_hist(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ fcount, int shift,
+                            uint32_t nblocks, uint32_t* counts) {
+    const uint32_t n = fcount[1];
     __shared__ uint32_t h[kSortDigits];
     for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) h[d] = 0;
     __syncthreads();
@@ -563,8 +565,10 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int s
     for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) counts[(size_t)d * nblocks + blockIdx.x] = h[d];
 }
 
-__global__ void k_sort_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, int shift,
-                               uint32_t nblocks, const uint32_t* __restrict__ offsets, uint32_t* okeys, uint32_t* ovals) {
+__global__ void k_sort_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                               const uint32_t* __restrict__ fcount, int shift, uint32_t nblocks,
+                               const uint32_t* __restrict__ offsets, uint32_t* okeys, uint32_t* ovals) {
+    const uint32_t n = fcount[1];
     constexpr int kWarps = kSortThreads / 32;
     __shared__ uint32_t running[kSortDigits];
     __shared__ uint32_t wcount[kWarps][kSortDigits];
@@ -782,20 +786,33 @@ __global__ void __launch_bounds__(256, 5) k_pixels(RasterJob J, const uint32_t* 
     depth[p] = rd;
 }
 
-__global__ void k_pixel_count(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* pcount) {
+__global__ void k_pixel_count(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ fcount, uint32_t* pcount) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&pcount[keys[i]], 1u);
+    if (i < fcount[1]) atomicAdd(&pcount[keys[i]], 1u);
+}
+
+// The job's fragment total from the per-unit offsets: fcount[0] = total, fcount[1] = the total
+// when it fits the `cap` entries of the fragment buffers, else 0 (the passes after it then do
+// nothing and the host grows the buffers and rasterises again); pstart[npx] = fcount[1].
+__global__ void k_frag_total(const uint32_t* __restrict__ ufoff, const uint32_t* __restrict__ ufrags, uint32_t nunits,
+                             uint32_t cap, uint32_t* fcount, uint32_t* pstart_end) {
+    const uint64_t nf = (uint64_t)ufoff[nunits - 1] + ufrags[nunits - 1];
+    const uint32_t fit = nf <= cap ? (uint32_t)nf : 0u;
+    fcount[0] = nf > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)nf;
+    fcount[1] = fit;
+    *pstart_end = fit;
 }
 
 struct RasterScratch {
     DevBuf cbase, hits, uhits, ufrags, ufoff, big, chunk_tri, ctr, keys, vals, keys2, vals2, counts, offsets, partial[3], pstart, pcount,
-        color, depth;
+        color, depth, fcount;
 };
 
 }  // namespace
 
 struct t3d_raster_state {
     RasterScratch S;
+    uint32_t frag_cap = 1u << 22;  // fragments the sort buffers hold (grow-only)
     int32_t W = 0, H = 0;
     bool valid = false;
     std::vector<RasterTex> tex;  // the texture table (host copy of `texs`)
@@ -914,45 +931,56 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
                                                    (uint32_t*)S.ufrags.ptr, big, chunk_tri, ctr);
     k_big_count<<<bigblocks, kFragThreads, 0, st>>>(J, big, chunk_tri, ctr, (uint4*)S.hits.ptr, (uint32_t*)S.ufrags.ptr);
     if ((rc = scan_u32(ctx, S, (const uint32_t*)S.ufrags.ptr, (uint32_t*)S.ufoff.ptr, nunits, st))) return rc;
-    uint32_t last[2];
-    CKR(cudaMemcpyAsync(&last[0], (const uint32_t*)S.ufoff.ptr + nunits - 1, 4, cudaMemcpyDeviceToHost, st));
-    CKR(cudaMemcpyAsync(&last[1], (const uint32_t*)S.ufrags.ptr + nunits - 1, 4, cudaMemcpyDeviceToHost, st));
-    CKR(cudaStreamSynchronize(st));
-    const uint32_t nf = last[0] + last[1];
-    const uint32_t nsb = std::max(1u, (nf + kSortChunk - 1) / kSortChunk);
-    if ((rc = S.keys.ensure(ctx, 4ull * std::max(1u, nf))) || (rc = S.vals.ensure(ctx, 4ull * std::max(1u, nf))) ||
-        (rc = S.keys2.ensure(ctx, 4ull * std::max(1u, nf))) || (rc = S.vals2.ensure(ctx, 4ull * std::max(1u, nf))) ||
-        (rc = S.counts.ensure(ctx, 4ull * kSortDigits * nsb)) || (rc = S.offsets.ensure(ctx, 4ull * kSortDigits * nsb)))
+    // the fragment total stays on the device: the buffers after this point hold `fcap` fragments
+    // (the last raster's total and an eighth more, grow-only); a larger total is found at the
+    // end of the call, which then grows them and runs again
+    const uint32_t fcap = R.frag_cap;
+    const uint32_t nsb = std::max(1u, (fcap + kSortChunk - 1) / kSortChunk);
+    if ((rc = S.keys.ensure(ctx, 4ull * fcap)) || (rc = S.vals.ensure(ctx, 4ull * fcap)) ||
+        (rc = S.keys2.ensure(ctx, 4ull * fcap)) || (rc = S.vals2.ensure(ctx, 4ull * fcap)) ||
+        (rc = S.counts.ensure(ctx, 4ull * kSortDigits * nsb)) || (rc = S.offsets.ensure(ctx, 4ull * kSortDigits * nsb)) ||
+        (rc = S.fcount.ensure(ctx, 16)))
         return rc;
+    uint32_t* fcount = (uint32_t*)S.fcount.ptr;
+    k_frag_total<<<1, 1, 0, st>>>((const uint32_t*)S.ufoff.ptr, (const uint32_t*)S.ufrags.ptr, nunits, fcap, fcount,
+                                  (uint32_t*)S.pstart.ptr + npx);
     uint32_t *kin = (uint32_t*)S.keys.ptr, *vin = (uint32_t*)S.vals.ptr;
     uint32_t *kout = (uint32_t*)S.keys2.ptr, *vout = (uint32_t*)S.vals2.ptr;
-    if (nf) {
-        k_frag_write<<<fblocks, kFragThreads, 0, st>>>(J, nunits, (const uint4*)S.hits.ptr, (const uint32_t*)S.uhits.ptr,
-                                                       (const uint32_t*)S.ufoff.ptr, big, kin, vin);
-        k_big_write<<<bigblocks, kFragThreads, 0, st>>>(J, big, chunk_tri, ctr, kin, vin);
-        // 3. stable sort by pixel
-        int bits = 1;
-        while ((1ull << bits) < npx) bits++;
-        for (int shift = 0; shift < bits; shift += kSortBits) {
-            k_sort_hist<<<nsb, kSortThreads, 0, st>>>(kin, nf, shift, nsb, (uint32_t*)S.counts.ptr);
-            if ((rc = scan_u32(ctx, S, (const uint32_t*)S.counts.ptr, (uint32_t*)S.offsets.ptr, kSortDigits * nsb, st)))
-                return rc;
-            k_sort_scatter<<<nsb, kSortThreads, 0, st>>>(kin, vin, nf, shift, nsb, (const uint32_t*)S.offsets.ptr, kout, vout);
-            std::swap(kin, kout);
-            std::swap(vin, vout);
-        }
+    k_frag_write<<<fblocks, kFragThreads, 0, st>>>(J, nunits, (const uint4*)S.hits.ptr, (const uint32_t*)S.uhits.ptr,
+                                                   (const uint32_t*)S.ufoff.ptr, big, kin, vin, fcount);
+    k_big_write<<<bigblocks, kFragThreads, 0, st>>>(J, big, chunk_tri, ctr, kin, vin, fcount);
+    // 3. stable sort by pixel
+    int bits = 1;
+    while ((1ull << bits) < npx) bits++;
+    for (int shift = 0; shift < bits; shift += kSortBits) {
+        k_sort_hist<<<nsb, kSortThreads, 0, st>>>(kin, fcount, shift, nsb, (uint32_t*)S.counts.ptr);
+        if ((rc = scan_u32(ctx, S, (const uint32_t*)S.counts.ptr, (uint32_t*)S.offsets.ptr, kSortDigits * nsb, st)))
+            return rc;
+        k_sort_scatter<<<nsb, kSortThreads, 0, st>>>(kin, vin, fcount, shift, nsb, (const uint32_t*)S.offsets.ptr, kout, vout);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
     }
-    // 4. per-pixel fragment ranges
+    // 4. per-pixel fragment ranges (pstart[npx], the total, was written by k_frag_total)
     CKR(cudaMemsetAsync(S.pcount.ptr, 0, 4 * npx, st));
-    if (nf) k_pixel_count<<<(nf + 255) / 256, 256, 0, st>>>(kin, nf, (uint32_t*)S.pcount.ptr);
+    k_pixel_count<<<(fcap + 255) / 256, 256, 0, st>>>(kin, fcount, (uint32_t*)S.pcount.ptr);
     if ((rc = scan_u32(ctx, S, (const uint32_t*)S.pcount.ptr, (uint32_t*)S.pstart.ptr, (uint32_t)npx, st))) return rc;
-    CKR(cudaMemcpyAsync((uint32_t*)S.pstart.ptr + npx, &nf, 4, cudaMemcpyHostToDevice, st));
     // 5. replay per pixel
     k_pixels<<<(uint32_t)((npx + 255) / 256), 256, 0, st>>>(J, (const uint32_t*)S.pstart.ptr, vin,
                                                            (const uint4*)S.hits.ptr, (uint32_t*)S.color.ptr,
                                                            (uint32_t*)S.depth.ptr);
     CKR(cudaGetLastError());
+    uint32_t fc[2] = {0u, 0u};
+    CKR(cudaMemcpyAsync(fc, fcount, 8, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
+    if (fc[0] != 0u && fc[1] == 0u) {  // more fragments than the buffers hold: grow them, rasterise again
+        if (fc[0] > 0xF0000000u) {
+            set_err(ctx, "frame_raster: %u fragments exceed 32-bit fragment indices", fc[0]);
+            return T3D_E_INVAL;
+        }
+        R.frag_cap = fc[0] + fc[0] / 8 + 1024;
+        return t3d_frame_raster(ctx, job, opts, stream);
+    }
+    R.frag_cap = std::max(R.frag_cap, fc[0] + fc[0] / 8);
     R.W = J.W;
     R.H = J.H;
     R.valid = true;
@@ -1021,7 +1049,7 @@ void t3d_raster_release(t3d_ctx* ctx) {
     RasterScratch& S = ctx->raster->S;
     for (DevBuf* b : {&S.cbase, &S.hits, &S.uhits, &S.ufrags, &S.ufoff, &S.big, &S.chunk_tri, &S.ctr, &S.keys, &S.vals, &S.keys2, &S.vals2,
                       &S.counts, &S.offsets, &S.partial[0], &S.partial[1], &S.partial[2], &S.pstart, &S.pcount, &S.color,
-                      &S.depth, &ctx->raster->texs, &ctx->raster->texels})
+                      &S.depth, &S.fcount, &ctx->raster->texs, &ctx->raster->texels})
         b->release();
     delete ctx->raster;
     ctx->raster = nullptr;
