@@ -483,7 +483,7 @@ __device__ __forceinline__ void light_vertex(const SLight& L, uint32_t flags, f3
 
 // ------------------------------------------------------- tile phases ----
 // Shared memory of one block while it works on a tile:
-//   ModelSmem | TileSmem | whist[nwarps][kBins] | lidx u16[T] | depth f32[T] | bin u16[T]
+//   ModelSmem | TileSmem | whist[nwarps][kBinsPadded] | lidx u16[T] | depth f32[T] | bin u16[T]
 // Per work item constants of the emit path (camera, segment and stream bases).
 enum : uint32_t { EC_PERSP = 1, EC_PCORRECT = 2, EC_DEPTH = 4, EC_RDEPTH = 8, EC_FOG_ADD = 16, EC_FOG_SUB = 32,
                   EC_LIT = 64, EC_COLORS = 128, EC_UNBB = 256, EC_SNAP = 512 };
@@ -522,6 +522,11 @@ struct TileSmem {
     uint32_t loc_walk[kBins];   // per-bin first position within this tile's own output order (walk order)
 };
 
+// Per-warp bin counter regions hold kBinsPadded words: the meshlet ranking keeps counter b
+// at pad_bin(b) (one padding word after every 16), the per-vertex route's at b.
+constexpr uint32_t kBinsPadded = kBins + kBins / 16;
+__device__ __forceinline__ uint32_t pad_bin(uint32_t b) { return b + (b >> 4); }
+
 struct SmemLayout {
     TileSmem* ts;
     uint32_t* whist;
@@ -538,7 +543,7 @@ __device__ __forceinline__ SmemLayout smem_layout(unsigned char* smem, uint32_t 
     L.ts = (TileSmem*)(smem + o);
     o += (sizeof(TileSmem) + 15) & ~(size_t)15;  // 16-byte alignment for the vector accesses below
     L.whist = (uint32_t*)(smem + o);
-    o += sizeof(uint32_t) * (blockDim.x >> 5) * kBins;
+    o += sizeof(uint32_t) * (blockDim.x >> 5) * kBinsPadded;
     L.depth = (float*)(smem + o);
     o += 4 * (size_t)tile;
     L.lidx = (uint16_t*)(smem + o);
@@ -962,6 +967,23 @@ __device__ __forceinline__ bool tri_visible(float nearp, float farp, bool backfa
     }
     // squared distance from the model-space camera to tri.Center (model.go:950-953),
     // or from the world camera to the skinned centre (model.go:941-946)
+    const float ddx = ic.x - ctr.x, ddy = ic.y - ctr.y, ddz = ic.z - ctr.z;
+    depth = ddx * ddx + ddy * ddy + ddz * ddz;
+    return !(isnan(depth) || isinf(depth));
+}
+
+// tri_visible for corners whose per-corner test outcomes are bits in .w (1 inside near/far,
+// 2 / 4 / 8 / 16 off the left / right / bottom / top of the screen): some corner inside
+// near/far, not all three off one side, the backface test and the depth key as there.
+__device__ __forceinline__ bool tri_visible_bits(bool backface, f3 ic, float4 c0, float4 c1, float4 c2, f3 ctr,
+                                                 float& depth) {
+    const uint32_t f0 = __float_as_uint(c0.w), f1 = __float_as_uint(c1.w), f2 = __float_as_uint(c2.w);
+    if (!((f0 | f1 | f2) & 1u) || (f0 & f1 & f2 & 30u)) return false;
+    if (backface) {
+        const float n0x = c0.x - c1.x, n0y = c0.y - c1.y;
+        const float n1x = c1.x - c2.x, n1y = c1.y - c2.y;
+        if ((n0x * n1y) - (n1x * n0y) < 0.0f) return false;
+    }
     const float ddx = ic.x - ctr.x, ddy = ic.y - ctr.y, ddz = ic.z - ctr.z;
     depth = ddx * ddx + ddy * ddy + ddz * ddz;
     return !(isnan(depth) || isinf(depth));
@@ -1426,13 +1448,15 @@ __device__ __forceinline__ uint32_t bin_fast(float d, float mn, float range, flo
 // cross-tile scan (unless the pair has one tile); their exclusive scan in the
 // pair's walk order gives each bin's first local rank, and a second pass writes
 // entry j of bin b with index w to position first(b) + w of the tile's rank list
-// as j | b << 11 | w << 20. cnt: kBins counters; sb, sw: a bin and an index per entry.
+// as j | b << 11 | w << 20. cnt: kBins counters, counter b at pad_bin(b) (a padding word
+// after every 16, so the lanes' 16-bin runs of the scan fall in distinct banks); sb, sw: a
+// bin and an index per entry.
 __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i, const TileDesc& td, uint32_t* cnt,
                                                uint16_t* sb, uint16_t* sw) {
     const uint32_t lane = threadIdx.x & 31, T = P.tile_tris;
     const uint32_t n = __ldcg(&P.tile_count[i]);
     const uint32_t s = td.seg;
-    for (uint32_t b = lane; b < kBins; b += 32) cnt[b] = 0u;
+    for (uint32_t b = lane; b < kBinsPadded; b += 32) cnt[b] = 0u;
     const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
     const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
     const float range = range_of(mn, mx);
@@ -1462,18 +1486,18 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
             if (active) {
                 const uint32_t bn = bin_fast(cur[u], mn, range, rinv, sort_mode);
                 const uint32_t peers = __match_any_sync(mask, bn);
-                const uint32_t w = cnt[bn] + __popc(peers & lt);
+                const uint32_t w = cnt[pad_bin(bn)] + __popc(peers & lt);
                 sb[j] = (uint16_t)bn;
                 sw[j] = (uint16_t)w;
                 __syncwarp(mask);
-                if (lane == (uint32_t)(__ffs(peers) - 1)) cnt[bn] += __popc(peers);
+                if (lane == (uint32_t)(__ffs(peers) - 1)) cnt[pad_bin(bn)] += __popc(peers);
             }
             __syncwarp();
         }
     }
     if (!(td.flags & SEG_SINGLE)) {
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
-        for (uint32_t b = lane; b < kBins; b += 32) out[b] = cnt[b];
+        for (uint32_t b = lane; b < kBins; b += 32) out[b] = cnt[pad_bin(b)];
     }
     // exclusive scan in walk order: lane l owns walk positions [16 l, 16 l + 16)
     {
@@ -1481,7 +1505,7 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
         uint32_t c[kPer], sum = 0;
 #pragma unroll
         for (uint32_t u = 0; u < kPer; u++) {
-            c[u] = cnt[walk_pos(lane * kPer + u, sort_mode)];  // walk_pos maps walk positions to bins too
+            c[u] = cnt[pad_bin(walk_pos(lane * kPer + u, sort_mode))];  // walk_pos maps walk positions to bins too
             sum += c[u];
         }
         uint32_t incl = sum;
@@ -1493,7 +1517,7 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
         __syncwarp();
 #pragma unroll
         for (uint32_t u = 0; u < kPer; u++) {
-            cnt[walk_pos(lane * kPer + u, sort_mode)] = base;
+            cnt[pad_bin(walk_pos(lane * kPer + u, sort_mode))] = base;
             base += c[u];
         }
     }
@@ -1502,7 +1526,7 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
     uint32_t* rk = P.vis_rank + (size_t)i * T;
     for (uint32_t j = lane; j < n; j += 32) {
         const uint32_t bn = sb[j], w = sw[j];
-        rk[cnt[bn] + w] = j | (bn << 11) | (w << 20);
+        rk[cnt[pad_bin(bn)] + w] = j | (bn << 11) | (w << 20);
     }
 }
 
@@ -1518,7 +1542,7 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
     const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t per = T / nw;
     const uint32_t n_rec = P.mt_tile_end - P.mt_tile_begin, n_all = n_rec + (P.mt_mesh_end - P.mt_mesh_begin);
-    uint32_t* wh = L.whist + wid * kBins;
+    uint32_t* wh = L.whist + wid * kBinsPadded;
     uint32_t k = 0;
     if (lane == 0) k = atomicAdd(&P.ctl->queue[2], 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
@@ -1527,7 +1551,7 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         const TileDesc& td = P.mt_desc[i];
         const uint32_t s = td.seg;
         if (td.flags & SEG_MESHLET) {  // counts, cross-tile counts and the tile's stable ranking
-            uint16_t* sb = reinterpret_cast<uint16_t*>(L.whist + (size_t)nw * kBins) + 2 * (size_t)wid * T;
+            uint16_t* sb = reinterpret_cast<uint16_t*>(L.whist + (size_t)nw * kBinsPadded) + 2 * (size_t)wid * T;
             hist_rank_meshlet(P, i, td, wh, sb, sb + T);
             uint32_t nx = 0;
             if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
@@ -1814,11 +1838,17 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
     const uint32_t U = td.vmin, nt = td.t1 - td.t0;
     const uint16_t* __restrict__ lidx = reinterpret_cast<const uint16_t*>(buf + kPrepHead);
     const float* __restrict__ pos = reinterpret_cast<const float*>(buf + kPrepHead + mlet_lidx_bytes(nt));
+    const float nearp = td.nearp, farp = td.farp;
     for (uint32_t v = threadIdx.x; v < U; v += blockDim.x) {
-        // MultVecW and the x/y divide of the rejection tests (model.go:808-873)
+        // MultVecW and the x/y divide of the rejection tests (model.go:808-873), and the
+        // per-corner outcomes of those tests as bits: 1 inside near/far, 2 / 4 left / right of
+        // the screen (X/w < -0.5 / > 0.5), 8 / 16 below / above it
         const float4 c = clip_rows(mrow, pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]);
         const float w1 = c.w < 0.0f ? 0.000001f : c.w;
-        sclip[v] = make_float4(c.x / w1, c.y / w1, c.z, 0.0f);
+        const float sx = c.x / w1, sy = c.y / w1;
+        const uint32_t f = ((c.z + 1.0f >= nearp && c.z < farp) ? 1u : 0u) | (sx < -0.5f ? 2u : 0u) |
+                           (sx > 0.5f ? 4u : 0u) | (sy < -0.5f ? 8u : 0u) | (sy > 0.5f ? 16u : 0u);
+        sclip[v] = make_float4(sx, sy, c.z, __uint_as_float(f));
     }
     next_desc(P, nx);
     __syncthreads();
@@ -1826,7 +1856,6 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     float* __restrict__ gd = P.vis_depth + (size_t)mt * T;
     uint16_t* __restrict__ gv = P.vis_vloc + (size_t)mt * 3 * T;
-    const float nearp = td.nearp, farp = td.farp;
     const bool backface = td.flags & SEG_BACKFACE;
     const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
     float lmin = 3.402823466e38f, lmax = 0.0f;
@@ -1847,7 +1876,7 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
             const f3 ctr = mk3(div3(pos[3 * i0] + pos[3 * i1] + pos[3 * i2]),
                                div3(pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]),
                                div3(pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]));
-            vis = tri_visible(nearp, farp, backface, ic, c0, c1, c2, ctr, d);
+            vis = tri_visible_bits(backface, ic, c0, c1, c2, ctr, d);
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, vis);
         if (vis) {
@@ -2241,7 +2270,7 @@ extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const 
     return cudaGetLastError();
 }
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads) {
-    const size_t tiles = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + 4ull * (block_threads / 32) * t3d::kBins +
+    const size_t tiles = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + 4ull * (block_threads / 32) * t3d::kBinsPadded +
                          10ull * tile_tris + 16;
     const size_t verts = sizeof(t3d::ModelSmem) + 16;
     return tiles > verts ? tiles : verts;
@@ -2252,7 +2281,7 @@ extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_t
     const size_t b = t3d::mesh_tri_layout(tile_tris, mesh_ucap).total;
     const size_t c = t3d::mesh_rank_layout(tile_tris, mesh_ucap, block_threads / 32).total;
     // the histogram phase's meshlet ranking: per warp kBins counters and a bin and an index per entry
-    const size_t d = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + (block_threads / 32) * (4ull * t3d::kBins + 4ull * tile_tris);
+    const size_t d = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) + (block_threads / 32) * (4ull * t3d::kBinsPadded + 4ull * tile_tris);
     size_t m = a > b ? a : b;
     m = m > c ? m : c;
     return m > d ? m : d;
