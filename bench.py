@@ -362,7 +362,8 @@ def run_ours(args, rank, world, local_rank):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk.summary(),
-            "gpu_launches": int(args.steps),
+            "gpu_launches": int(args.steps) * int(st_last.launches),
+            "launches_per_frame": int(st_last.launches),
             "visible_tris_per_step": vis / args.steps / max(1, world),
             "culled_models_last_frame": int(st_last.culled_models),
             "phase_us_last_frame": {k: round(float(v), 1) for k, v in

@@ -374,6 +374,14 @@ int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chu
  * enable = 0: every pair writes and reads per-vertex records in device memory. The
  * emitted stream is the same bit for bit either way. */
 int         t3d_set_meshlets(t3d_ctx* ctx, int enable);
+/* Launch shape of a batched frame (no reference counterpart: the reference has one
+ * CPU path). enable = 1 (the default): one launch per phase (model prep, vertex
+ * records, triangles, histogram, scan, rank + emit), each kernel compiled with its
+ * own register budget and sized to its own co-resident blocks, the launch boundary
+ * ordering the phases. enable = 0: the whole frame in one cooperative persistent
+ * launch whose phases are separated by grid barriers. The emitted stream is the same
+ * bit for bit either way; the autotuner picks the faster. */
+int         t3d_set_split_phases(t3d_ctx* ctx, int enable);
 /* Bounded device waits (grid barriers, bulk-copy waits): polls before the frame
  * gives up and t3d_frame_sync returns T3D_E_TIMEOUT (0 = the default, seconds).
  * Meant for tests of the timeout path; the context stays usable and the next

@@ -17,21 +17,27 @@ from tests.parity import assert_frames_equal, bits
 pytestmark = pytest.mark.gpu
 
 
+# batched as one launch per phase (the default), batched as one cooperative launch, plain
+FORMS = [(abi.MODE_BATCHED, 1), (abi.MODE_BATCHED, 0), (abi.MODE_PLAIN, 1)]
+
+
 @pytest.mark.parametrize("variant", scenes.FEATURE_CAMERAS)
-@pytest.mark.parametrize("mode", [abi.MODE_BATCHED, abi.MODE_PLAIN])
-def test_feature_scenes_match_oracle(ctx, variant, mode):
+@pytest.mark.parametrize("mode,split", FORMS)
+def test_feature_scenes_match_oracle(ctx, variant, mode, split):
     for seed in (5, 6):
         sd = scenes.feature_scene(seed)
         cam = scenes.feature_camera(variant)
         sid = ctx.upload(sd)
         try:
+            ctx.set_split_phases(split)
             ctx.render(sid, cam, mode=mode)
             got = ctx.download()
         finally:
+            ctx.set_split_phases(1)
             ctx.release(sid)
         ref = pyoracle.render(sd, cam)
         assert ref.visible_tris > 0
-        assert_frames_equal(got, ref, f"features{seed}/{variant}/mode{mode}")
+        assert_frames_equal(got, ref, f"features{seed}/{variant}/mode{mode}/split{split}")
 
 
 class _JobFrame:
@@ -595,12 +601,15 @@ def test_all_features_in_one_launch(ctx):
         c4 = scenes.feature_camera("ortho")
         specs = [(ids[0], sk, c0, None), (ids[1], bb, c1, ((1 << 128) - 1) & ~(1 << 2)),
                  (ids[2], sub, c2, None), (ids[3], bat, c3, None), (ids[4], nested, c4, ((1 << 128) - 1) & ~(1 << 1))]
-        for mode in (abi.MODE_BATCHED, abi.MODE_PLAIN):
+        for mode, split in FORMS:
+            ctx.set_split_phases(split)
             ctx.render_jobs([job(s, cam, mask) for s, _, cam, mask in specs], mode=mode)
             parts = split_jobs(ctx.download(), len(specs))
             for j, (s, sd, cam, mask) in enumerate(specs):
-                assert_frames_equal(parts[j], pyoracle.render(sd, cam, light_mask=mask), f"job{j}/mode{mode}")
+                assert_frames_equal(parts[j], pyoracle.render(sd, cam, light_mask=mask),
+                                    f"job{j}/mode{mode}/split{split}")
     finally:
+        ctx.set_split_phases(1)
         for s in ids:
             ctx.release(s)
 

@@ -6,7 +6,8 @@ properties:
 - render pairs are independent, so the oracle on a sample of the models (every
   k-th) reproduces those models' pairs inside the full frame;
 - the plain form (one launch per pair) and the batched form give identical bits,
-  and so do the meshlet and per-vertex record routes;
+  and so do the meshlet and per-vertex record routes and the batched frame as one
+  cooperative launch or as one launch per phase;
 - a static frame rendered twice gives identical bits (idempotence);
 - visible counts add up (segments vs stats vs device counters).
 """
@@ -105,6 +106,12 @@ def test_batched_4096_models_whole_frame_matches_oracle(ctx):
         ref = pyoracle.render(sd, sd.camera, threads=threads)
         assert_frames_equal(got, ref, "4096 models, static")
         del ref
+        ctx.set_split_phases(0)
+        ctx.render(sid, sd.camera, mode=abi.MODE_BATCHED)
+        coop = ctx.download()
+        assert_frames_equal(coop, got, "one cooperative launch vs one launch per phase")
+        del coop
+        ctx.set_split_phases(1)
         ctx.set_meshlets(0)
         ctx.render(sid, sd.camera, mode=abi.MODE_BATCHED)
         rec = ctx.download()
@@ -118,6 +125,7 @@ def test_batched_4096_models_whole_frame_matches_oracle(ctx):
                             "4096 models, 3 animated replays")
     finally:
         ctx.set_meshlets(1)
+        ctx.set_split_phases(1)
         ctx.release(sid)
 
 

@@ -13,6 +13,8 @@ extern "C" const void* t3d_frame_kernel_ptr();
 extern "C" const void* t3d_frame_kernel_mesh_ptr();
 extern "C" size_t t3d_frame_smem_bytes(uint32_t tile_tris, uint32_t block_threads);
 extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_threads, uint32_t mesh_ucap);
+extern "C" const void* t3d_phase_kernel_ptr(int mesh, int k);
+extern "C" size_t t3d_phase_smem_bytes(int mesh, int k, uint32_t tile_tris, uint32_t block_threads, uint32_t mesh_ucap);
 
 using namespace t3d;
 
@@ -62,6 +64,25 @@ int configure(t3d_ctx* ctx) {
             ctx->max_grid_mesh = (uint32_t)(per * ctx->num_sms);
         }
         cudaGetLastError();
+    }
+    // the one-phase kernels: each with the shared memory of its own phase and its own
+    // co-resident blocks (no grid barrier: nothing needs them all resident at once)
+    for (int m = 0; m < 2; m++) {
+        for (int k = 0; k < 6; k++) {
+            ctx->phase_smem[m][k] = 0;
+            ctx->phase_grid[m][k] = 0;
+            if (m == 1 && !ctx->mesh_ucap) continue;
+            const size_t smem = t3d_phase_smem_bytes(m, k, ctx->tile_tris, ctx->block_threads, ctx->mesh_ucap);
+            const void* fp = t3d_phase_kernel_ptr(m, k);
+            int per = 0;
+            if (raise_smem_limit(fp, smem) == cudaSuccess &&
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fp, (int)ctx->block_threads, smem) == cudaSuccess &&
+                per >= 1) {
+                ctx->phase_smem[m][k] = smem;
+                ctx->phase_grid[m][k] = (uint32_t)(per * ctx->num_sms);
+            }
+            cudaGetLastError();
+        }
     }
     return T3D_OK;
 }
@@ -125,6 +146,7 @@ int t3d_destroy(t3d_ctx* ctx) {
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights,
                       &ctx->job_bytes, &ctx->vis_rank, &ctx->vinvw, &ctx->out_invw})
         b->release();
+    cudaStreamSynchronize(ctx->stream);  // stream-ordered frees of a pooled context have run
     ctx->table_host.release();
     ctx->readback.release();
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
@@ -174,6 +196,15 @@ int t3d_set_meshlets(t3d_ctx* ctx, int enable) {
     ctx->tables_ok = false;
     drop_graph(ctx);
     ctx->frame_valid = false;
+    return T3D_OK;
+}
+
+int t3d_set_split_phases(t3d_ctx* ctx, int enable) {
+    if (!ctx) return T3D_E_INVAL;
+    cudaSetDevice(ctx->device);
+    if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
+    ctx->split_phases = enable != 0;
+    drop_graph(ctx);
     return T3D_OK;
 }
 
@@ -449,7 +480,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
         if (ctls[i].err) {
             set_err(ctx, "frame kernel reported error %d (launch %u)", ctls[i].err, i);
             ctx->frame_valid = false;
-            return ctls[i].err == ERR_BARRIER_TIMEOUT ? T3D_E_TIMEOUT : T3D_E_CUDA;
+            return (ctls[i].err == ERR_BARRIER_TIMEOUT || ctls[i].err == ERR_COPY_TIMEOUT) ? T3D_E_TIMEOUT : T3D_E_CUDA;
         }
         s.algorithmic_bytes += ctls[i].bytes;
         s.culled_models += ctls[i].culled;
@@ -480,7 +511,9 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
                 s.phase_us[i] = (double)(t - prev) / 1e3;
                 prev = t;
             }
-            s.phase_busy[i] = ctx->last_grid ? (double)c.busy[order[i]] / 1e3 / ctx->last_grid : 0.0;
+            // order[i] is the timer slot of phase i (prep, vertex, triangles, hist, scan, rank + emit)
+            const uint32_t g = ctx->phase_grid_used[i];
+            s.phase_busy[i] = g ? (double)c.busy[order[i]] / 1e3 / g : 0.0;
         }
     }
     s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl;

@@ -224,7 +224,7 @@ __device__ __forceinline__ SLight light_for_model(const DevLight& L, const float
     return d;
 }
 
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_prep(const FrameParams& P) {
     const uint32_t n = P.inst_end - P.inst_begin;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -282,7 +282,7 @@ __device__ __noinline__ void phase_prep(const FrameParams& P) {
         // Mesh.Dimensions.MaxSpan for the model-level point-light skip (camera.go:1625-1629)
         pr.maxspan = mag3(mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]));
         // meshlet frames: the model's light list as its render pairs' vertex loops read it, once
-        if (kM && P.inst_lights && !culled && !skinned) {
+        if ((kV & 1) && P.inst_lights && !culled && !skinned) {
             SLight* out = reinterpret_cast<SLight*>(P.inst_lights) + (size_t)i * kMaxLights;
             const uint32_t nl = min(in.light_cnt, (uint32_t)kMaxLights);
             uint32_t o = 0;
@@ -1160,7 +1160,7 @@ __device__ __forceinline__ f3 skinned_centre(const float4* __restrict__ valt, ui
 
 // PV: per (segment, vertex chunk) the vertex records of every vertex the
 // part's triangles use.
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* smem) {
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
@@ -1213,7 +1213,7 @@ __device__ __noinline__ void phase_vertex(const FrameParams& P, unsigned char* s
 }
 
 // PV for the vertex items of parts with shape keys or skinning (queue 5).
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_vertex_altered(const FrameParams& P, unsigned char* smem) {
     ModelSmem& ms = *reinterpret_cast<ModelSmem*>(smem);
     uint32_t* s_item = reinterpret_cast<uint32_t*>(smem + sizeof(ModelSmem));
@@ -1414,9 +1414,9 @@ __device__ __forceinline__ void triangle_tiles(const FrameParams& P, unsigned ch
 #undef T3D_TILE_FIRST
 #undef T3D_TILE_END
 }
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_triangles(const FrameParams& P, unsigned char* smem) { triangle_tiles<false>(P, smem); }
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_triangles_skinned(const FrameParams& P, unsigned char* smem) {
     triangle_tiles<true>(P, smem);
 }
@@ -1535,7 +1535,7 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
 // memory). Queue slots run over the record-path tiles [mt_tile_begin,
 // mt_tile_end), then the meshlet tiles [mt_mesh_begin, mt_mesh_end), whose
 // lists are dense.
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
@@ -1591,7 +1591,7 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
 }
 
 // P3: per multi-tile segment, turn tile histograms into per-tile bin bases.
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* smem) {
     const SmemLayout L = smem_layout(smem, P.tile_tris);
     TileSmem& sm = *L.ts;
@@ -1637,7 +1637,7 @@ __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* sme
 }
 
 // P4: stable rank and emission of the tiles of multi-tile segments.
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_rank_multi(const FrameParams& P, unsigned char* smem) {
     const uint32_t T = P.tile_tris;
     const SmemLayout L = smem_layout(smem, T);
@@ -1722,20 +1722,21 @@ __host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(
 // The head of a DevPrep record the triangle phase copies: mvp, M, dirrot, invcam.
 constexpr uint32_t kPrepHead = 208;
 static_assert(offsetof(DevPrep, invcam) + 16 == kPrepHead && sizeof(DevPrep) % 16 == 0, "DevPrep head layout");
-// Triangle phase: MeshHdr | TileSmem | buf[2] (the model's prep record up to the model-space
-// camera, then lidx + pos of one meshlet) | (X/w, Y/w, Z, 0) per slot | the tile's visible
-// entries per warp region (depth f32[T], slots u16[3T])
-struct MeshTriLayout { size_t ts, buf0, buf1, clip, sdep, svl, total; };
+// Triangle phase: MeshHdr | per-round warp counts (two rounds' worth) and per-warp depth
+// range | buf (the model's prep record up to the model-space camera, then lidx + pos of one
+// meshlet) | (X/w, Y/w, Z, test bits) per slot
+struct MeshTriWarp {
+    uint32_t cnt[2][kMaxWarps];
+    float mn[kMaxWarps], mx[kMaxWarps];
+};
+struct MeshTriLayout { size_t wc, buf, clip, total; };
 __host__ __device__ __forceinline__ MeshTriLayout mesh_tri_layout(uint32_t T, uint32_t U) {
     MeshTriLayout L;
     size_t o = sizeof(MeshHdr);
-    L.ts = o; o += al16(sizeof(TileSmem));
+    L.wc = o; o += al16(sizeof(MeshTriWarp));
     const size_t buf = kPrepHead + (size_t)mlet_lidx_bytes(T) + 12ull * U;
-    L.buf0 = o; o += al16(buf);
-    L.buf1 = o; o += al16(buf);
+    L.buf = o; o += al16(buf);
     L.clip = o; o += 16ull * U;
-    L.sdep = o; o += al16(4ull * T);
-    L.svl = o; o += al16(6ull * T);
     L.total = o;
     return L;
 }
@@ -1817,10 +1818,19 @@ __device__ __forceinline__ void next_culled(const FrameParams& P, NextTile& nx) 
     if (threadIdx.x == 0 && nx.kn < P.mesh_end - P.mesh_begin) nx.culled = P.preps[nx.td.inst].culled;
 }
 
-// One meshlet tile of the triangle phase, its prep head + lidx + pos block in buf.
-__device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDesc& td, unsigned char* buf,
-                                              TileSmem& sm, float4* sclip, float* sdep,
-                                              uint16_t* svl, NextTile& nx) {
+// Triangle steps of 32 that a warp holds in registers per round (a round covers
+// blockDim / 32 * kTriSteps * 32 triangles of the tile).
+constexpr uint32_t kTriSteps = 4;
+
+// One meshlet tile of the triangle phase, its prep head + lidx + pos block in buf. The
+// tile's triangles go in rounds; in a round each warp tests 32 * kTriSteps consecutive
+// triangles and keeps its visible ones in registers, the warps exchange their counts,
+// and every lane writes its entries straight to their places in the tile's dense list
+// (triangle order). After the last round's reads of buf, thread 0 starts the copy of
+// the block's next tile into it (nx: its queue slot, descriptor and culling flag).
+__device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDesc td, unsigned char* buf,
+                                              MeshTriWarp& wc, float4* sclip, NextTile& nx, MeshHdr& H,
+                                              uint32_t nitems) {
     const uint32_t mt = td.mt;
     const DevPrep& pr = *reinterpret_cast<const DevPrep*>(buf);  // its head: mvp, M, dirrot, invcam
     float* mrow = reinterpret_cast<float*>(buf);
@@ -1851,147 +1861,159 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
         sclip[v] = make_float4(sx, sy, c.z, __uint_as_float(f));
     }
     next_desc(P, nx);
+    const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
     __syncthreads();
     const uint32_t T = P.tile_tris;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     float* __restrict__ gd = P.vis_depth + (size_t)mt * T;
     uint16_t* __restrict__ gv = P.vis_vloc + (size_t)mt * 3 * T;
     const bool backface = td.flags & SEG_BACKFACE;
-    const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
     float lmin = 3.402823466e38f, lmax = 0.0f;
-    const uint32_t per = T / nw;
-    const uint32_t wt0 = wid * per, wt1 = min(nt, wt0 + per);
-    const uint32_t wbase = wid * per;
-    uint32_t cnt = 0;
     const uint32_t lt = (1u << lane) - 1u;
-    for (uint32_t tb = wt0; tb < wt1; tb += 32) {
-        const uint32_t t = tb + lane;
-        bool vis = false;
-        float d = 0.0f;
-        uint32_t i0 = 0, i1 = 0, i2 = 0;
-        if (t < wt1) {
-            i0 = lidx[3 * t]; i1 = lidx[3 * t + 1]; i2 = lidx[3 * t + 2];
-            const float4 c0 = sclip[i0], c1 = sclip[i1], c2 = sclip[i2];
-            // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis
-            const f3 ctr = mk3(div3(pos[3 * i0] + pos[3 * i1] + pos[3 * i2]),
-                               div3(pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]),
-                               div3(pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]));
-            vis = tri_visible_bits(backface, ic, c0, c1, c2, ctr, d);
+    const uint32_t span = nw * 32u * kTriSteps;
+    const uint32_t rounds = (nt + span - 1) / span;
+    uint32_t base = 0;  // entries of the earlier rounds
+    for (uint32_t r = 0; r < rounds; r++) {
+        float d[kTriSteps];
+        uint32_t s01[kTriSteps], s2[kTriSteps];
+        uint32_t vm = 0, wcnt = 0;
+#pragma unroll
+        for (uint32_t it = 0; it < kTriSteps; it++) {
+            const uint32_t t = r * span + (wid * kTriSteps + it) * 32u + lane;
+            bool vis = false;
+            d[it] = 0.0f;
+            s01[it] = 0u;
+            s2[it] = 0u;
+            if (t < nt) {
+                const uint32_t i0 = lidx[3 * t], i1 = lidx[3 * t + 1], i2 = lidx[3 * t + 2];
+                const float4 c0 = sclip[i0], c1 = sclip[i1], c2 = sclip[i2];
+                // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis
+                const f3 ctr = mk3(div3(pos[3 * i0] + pos[3 * i1] + pos[3 * i2]),
+                                   div3(pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]),
+                                   div3(pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]));
+                vis = tri_visible_bits(backface, ic, c0, c1, c2, ctr, d[it]);
+                s01[it] = i0 | (i1 << 16);
+                s2[it] = i2;
+            }
+            if (vis) {
+                vm |= 1u << it;
+                lmin = fminf(lmin, d[it]);
+                lmax = fmaxf(lmax, d[it]);
+            }
+            wcnt += __popc(__ballot_sync(0xffffffffu, vis));
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, vis);
-        if (vis) {
-            const uint32_t p = wbase + cnt + __popc(bal & lt);
-            sdep[p] = d;
-            svl[3 * p] = (uint16_t)i0;
-            svl[3 * p + 1] = (uint16_t)i1;
-            svl[3 * p + 2] = (uint16_t)i2;
-            lmin = fminf(lmin, d);
-            lmax = fmaxf(lmax, d);
+        if (r == 0) next_culled(P, nx);
+        const bool last = r + 1 == rounds;
+        if (last) {
+            for (int o = 16; o > 0; o >>= 1) {
+                lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+                lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            }
         }
-        cnt += __popc(bal);
-    }
-    next_culled(P, nx);
-    for (int o = 16; o > 0; o >>= 1) {
-        lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
-        lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-    }
-    if (lane == 0) {
-        sm.wmin[wid] = lmin;
-        sm.wmax[wid] = lmax;
-        sm.warp_tot[wid] = cnt;
-    }
-    __syncthreads();
-    {  // the tile's list, dense and in triangle order: each warp copies its region after the ones before
-        uint32_t base = 0;
-        for (uint32_t w = 0; w < wid; w++) base += sm.warp_tot[w];
-        for (uint32_t q = lane; q < cnt; q += 32) gd[base + q] = sdep[wbase + q];
-        for (uint32_t q = lane; q < 3 * cnt; q += 32) gv[3 * base + q] = svl[3 * wbase + q];
+        uint32_t* cnt = wc.cnt[r & 1u];
+        if (lane == 0) {
+            cnt[wid] = wcnt;
+            if (last) {
+                wc.mn[wid] = lmin;
+                wc.mx[wid] = lmax;
+            }
+        }
+        __syncthreads();  // the round's counts are in; after the last round buf is no longer read
+        if (last && threadIdx.x == 0) {
+            H.item[0] = nx.kn;
+            H.copied[0] = nx.kn < nitems ? mesh_issue_tri(P, nx.td, nx.culled != 0, buf, &H.bar[0], &H.td[0]) : 0u;
+        }
+        uint32_t p = base, tot = 0;
+        for (uint32_t w = 0; w < nw; w++) {
+            const uint32_t c = cnt[w];
+            p += w < wid ? c : 0u;
+            tot += c;
+        }
+#pragma unroll
+        for (uint32_t it = 0; it < kTriSteps; it++) {
+            const bool vis = (vm >> it) & 1u;
+            const uint32_t bal = __ballot_sync(0xffffffffu, vis);
+            if (vis) {
+                const uint32_t q = p + __popc(bal & lt);
+                gd[q] = d[it];
+                gv[3 * q] = (uint16_t)(s01[it] & 0xFFFFu);
+                gv[3 * q + 1] = (uint16_t)(s01[it] >> 16);
+                gv[3 * q + 2] = (uint16_t)s2[it];
+            }
+            p += __popc(bal);
+        }
+        base += tot;
     }
     if (threadIdx.x == 0) {
-        uint32_t n = 0;
-        float mn = sm.wmin[0], mx = sm.wmax[0];
-        for (uint32_t w = 0; w < nw; w++) n += sm.warp_tot[w];
-        for (uint32_t w = 1; w < nw; w++) { mn = fminf(mn, sm.wmin[w]); mx = fmaxf(mx, sm.wmax[w]); }
-        P.tile_count[mt] = n;
-        if (n > 0) {
+        P.tile_count[mt] = base;
+        if (base > 0) {
+            float mn = wc.mn[0], mx = wc.mx[0];
+            for (uint32_t w = 1; w < nw; w++) { mn = fminf(mn, wc.mn[w]); mx = fmaxf(mx, wc.mx[w]); }
             atomicMin(&P.seg_minmax[2 * td.seg], __float_as_uint(mn));
             atomicMax(&P.seg_minmax[2 * td.seg + 1], __float_as_uint(mx));
-            atomicAdd(&P.seg_count[td.seg], n);
-            atomicAdd(&P.accum[0], (unsigned long long)n);
+            atomicAdd(&P.seg_count[td.seg], base);
+            atomicAdd(&P.accum[0], (unsigned long long)base);
         }
     }
 }
 
-// Triangle phase over meshlet tiles (queue 0). Work is taken two tiles ahead: while
-// a block processes the tile in one copy buffer, the copy of its next tile is in
-// flight into the other, and thread 0 spreads the queue slot, descriptor and
-// culling reads for the tile after that over the current tile's work.
-template <bool kM>
+// Triangle phase over meshlet tiles (queue 0). One copy buffer: a tile's copy is started
+// as soon as the previous tile's triangles have been read (its list writes overlap the
+// copy), and the blocks on an SM cover each other's waits; thread 0 spreads the queue
+// slot, descriptor and culling reads for the next tile over the current tile's work.
+template <int kV>
 __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsigned char* smem) {
     MeshHdr& H = *reinterpret_cast<MeshHdr*>(smem);
     const MeshTriLayout L = mesh_tri_layout(P.tile_tris, P.mesh_ucap);
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem + L.ts);
-    unsigned char* buf[2] = {smem + L.buf0, smem + L.buf1};
+    MeshTriWarp& wc = *reinterpret_cast<MeshTriWarp*>(smem + L.wc);
+    unsigned char* buf = smem + L.buf;
     float4* sclip = reinterpret_cast<float4*>(smem + L.clip);
-    float* sdep = reinterpret_cast<float*>(smem + L.sdep);
-    uint16_t* svl = reinterpret_cast<uint16_t*>(smem + L.svl);
     const uint32_t n = P.mesh_end - P.mesh_begin, limit = spin_limit(P);
-    uint32_t ph0 = 0, ph1 = 0;
-    // the barriers live in bytes that other phases use: set up here, invalidated at the end
+    uint32_t ph0 = 0;
+    // the barrier lives in bytes that other phases use: set up here, invalidated at the end
     if (threadIdx.x == 0) {
         mbar_init(&H.bar[0], 1);
-        mbar_init(&H.bar[1], 1);
         fence_mbar_init();
-        for (int b = 0; b < 2; b++) {
-            const uint32_t k = atomicAdd(&P.ctl->queue[0], 1u);
-            H.item[b] = k;
-            H.copied[b] = 0u;
-            if (k < n) {
-                const TileDesc td = P.tiles[P.mesh_begin + k];
-                H.copied[b] = mesh_issue_tri(P, td, P.preps[td.inst].culled != 0, buf[b], &H.bar[b], &H.td[b]);
-            }
+        const uint32_t k = atomicAdd(&P.ctl->queue[0], 1u);
+        H.item[0] = k;
+        H.copied[0] = 0u;
+        if (k < n) {
+            const TileDesc td = P.tiles[P.mesh_begin + k];
+            H.copied[0] = mesh_issue_tri(P, td, P.preps[td.inst].culled != 0, buf, &H.bar[0], &H.td[0]);
         }
     }
     __syncthreads();
-    uint32_t cur = 0;
     for (;;) {
-        const uint32_t k = H.item[cur];
+        const uint32_t k = H.item[0];
         if (k >= n) break;
         NextTile nx;
         nx.kn = 0xFFFFFFFFu;
         nx.culled = 1u;
         if (threadIdx.x == 0) nx.kn = atomicAdd(&P.ctl->queue[0], 1u);  // read after the clip values
+        const bool copied = H.copied[0] != 0u;
         bool ok = true;
-        if (H.copied[cur]) {
-            ok = mbar_wait(&H.bar[cur], cur ? ph1 : ph0, P.ctl, limit);
-            if (cur) ph1 ^= 1u; else ph0 ^= 1u;
+        if (copied) {
+            ok = mbar_wait(&H.bar[0], ph0, P.ctl, limit);  // on giving up it has let the copy land
+            ph0 ^= 1u;
         }
-        if (!__syncthreads_and(ok)) {  // gave up: let the other buffer's copy land, then leave
-            if (H.copied[cur ^ 1]) mbar_wait(&H.bar[cur ^ 1], cur ? ph0 : ph1, P.ctl, kSpinLimit);
-            break;
-        }
-        const TileDesc& td = H.td[cur];
-        if (H.copied[cur]) {
-            mesh_tile_tri(P, td, buf[cur], sm, sclip, sdep, svl, nx);
+        if (!__syncthreads_and(ok)) break;
+        const TileDesc td = H.td[0];
+        if (copied) {
+            mesh_tile_tri(P, td, buf, wc, sclip, nx, H, n);
         } else {  // skipped pair or culled model
-            if (threadIdx.x == 0) P.tile_count[td.mt] = 0u;
             next_desc(P, nx);
             next_culled(P, nx);
+            if (threadIdx.x == 0) {
+                P.tile_count[td.mt] = 0u;
+                H.item[0] = nx.kn;
+                H.copied[0] = nx.kn < n ? mesh_issue_tri(P, nx.td, nx.culled != 0, buf, &H.bar[0], &H.td[0]) : 0u;
+            }
         }
-        __syncthreads();  // buffer cur is free
-        if (threadIdx.x == 0) {
-            H.item[cur] = nx.kn;
-            H.copied[cur] = nx.kn < n ? mesh_issue_tri(P, nx.td, nx.culled != 0, buf[cur], &H.bar[cur], &H.td[cur]) : 0u;
-        }
-        __syncthreads();
-        cur ^= 1u;
+        __syncthreads();  // the next tile's slot, descriptor and copy state are in place
     }
     __syncthreads();
     // every copy issued was waited for (a queue slot past the end issues none)
-    if (threadIdx.x == 0) {
-        mbar_inval(&H.bar[0]);
-        mbar_inval(&H.bar[1]);
-    }
+    if (threadIdx.x == 0) mbar_inval(&H.bar[0]);
     __syncthreads();
 }
 
@@ -2033,7 +2055,7 @@ __device__ __forceinline__ void mesh_stage_tile(const FrameParams& P, const Tile
 // the vertex block into emitted corners in place and writes the corners in
 // output order, one per thread. The next tile is taken at the start of a tile,
 // its data asked into L2 and its records staged halfway through.
-template <bool kM>
+template <int kV>
 __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned char* smem) {
     MeshHdr& H = *reinterpret_cast<MeshHdr*>(smem);
     const uint32_t T = P.tile_tris, nw = blockDim.x >> 5;
@@ -2202,57 +2224,89 @@ __device__ __forceinline__ void phase_start(unsigned long long& since) {
 #ifndef T3D_MESH_BLOCKS
 #define T3D_MESH_BLOCKS 2  // the same for the kernel with meshlet tiles (its shared memory allows 2 per SM)
 #endif
-// kM: the frame has meshlet tiles. Both instantiations run the record path for
-// the pairs that need it (skinning, shape keys, subdivision, snapping, ...).
-template <bool kM>
-__global__ void __launch_bounds__(256, kM ? T3D_MESH_BLOCKS : T3D_MIN_BLOCKS) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
-    extern __shared__ __align__(16) unsigned char smem[];
+// Blocks of 256 threads per SM that the one-phase kernels are compiled for (registers:
+// 65536 / (256 blocks)), per phase: prep, vertex records, triangles, histogram, scan,
+// rank + emit; for frames with meshlet tiles and for the others.
+#ifndef T3D_PHASE_BLOCKS_MESH
+#define T3D_PHASE_BLOCKS_MESH 2, 2, 3, 2, 2, 2
+#endif
+#ifndef T3D_PHASE_BLOCKS_REC
+#define T3D_PHASE_BLOCKS_REC 4, 4, 4, 4, 4, 4
+#endif
+constexpr int kPhaseBlocks[2][6] = {{T3D_PHASE_BLOCKS_REC}, {T3D_PHASE_BLOCKS_MESH}};
+// The phases of one launch (ph: bit 0 prep, 1 vertex records, 2 triangles, 3 histogram,
+// 4 scan, 5 rank + emit), with a grid barrier between two phases of the same launch.
+// kV & 1: the frame has meshlet tiles; the other bits tell the instantiations apart, so
+// every kernel below compiles its own copy of its phases under its own register budget.
+// A launch of a single phase after an earlier one has failed does nothing.
+template <int kV>
+__device__ __forceinline__ void frame_body(const FrameParams& P, unsigned char* smem, const uint32_t ph) {
+    constexpr bool kM = kV & 1;
     unsigned long long since = 0;
     const uint32_t limit = spin_limit(P);
-    const uint32_t ph = P.phases ? P.phases : 0x3Fu;
     // a grid barrier after phase bit b when this launch also runs a later phase
     auto barrier_after = [&](uint32_t b) { return !(ph & b) || !(ph & ~(2u * b - 1u)) || grid_barrier(P.ctl, limit); };
+    if (!(ph & 1u) && vload(&P.ctl->err) != 0) return;
     if (blockIdx.x == 0 && threadIdx.x == 0 && (ph & 1u)) P.ctl->t_end[7] = global_ns();
     if (ph & 1u) {
         phase_start(since);
-        phase_prep<kM>(P);
+        phase_prep<kV>(P);
         phase_done(P.ctl, 0, since);
     }
     if (!barrier_after(1u)) return;
     if (ph & 2u) {
         phase_start(since);
-        if (P.vitem_begin < P.vitem_alt) phase_vertex<kM>(P, smem);
-        if (P.vitem_alt < P.vitem_end) phase_vertex_altered<kM>(P, smem);
+        if (P.vitem_begin < P.vitem_alt) phase_vertex<kV>(P, smem);
+        if (P.vitem_alt < P.vitem_end) phase_vertex_altered<kV>(P, smem);
         phase_done(P.ctl, 6, since);
     }
     if (!barrier_after(2u)) return;
     if (ph & 4u) {
         phase_start(since);
-        if (kM && P.mesh_begin < P.mesh_end) phase_triangles_meshlet<kM>(P, smem);
-        if (P.tile_begin < P.tile_alt) phase_triangles<kM>(P, smem);
-        if (P.tile_alt < P.tile_end) phase_triangles_skinned<kM>(P, smem);
+        if (kM && P.mesh_begin < P.mesh_end) phase_triangles_meshlet<kV>(P, smem);
+        if (P.tile_begin < P.tile_alt) phase_triangles<kV>(P, smem);
+        if (P.tile_alt < P.tile_end) phase_triangles_skinned<kV>(P, smem);
         phase_done(P.ctl, 1, since);
     }
     if (!P.has_multi) return;
     if (!barrier_after(4u)) return;
     if (ph & 8u) {
         phase_start(since);
-        phase_hist<kM>(P, smem);
+        phase_hist<kV>(P, smem);
         phase_done(P.ctl, 2, since);
     }
     if (!barrier_after(8u)) return;
     if (ph & 16u) {
         phase_start(since);
-        phase_scan<kM>(P, smem);
+        phase_scan<kV>(P, smem);
         phase_done(P.ctl, 3, since);
     }
     if (!barrier_after(16u)) return;
     if (ph & 32u) {
         phase_start(since);
-        if (P.mt_tile_begin < P.mt_tile_end) phase_rank_multi<kM>(P, smem);
-        if (kM && P.mt_mesh_begin < P.mt_mesh_end) phase_rank_meshlet<kM>(P, smem);
+        if (P.mt_tile_begin < P.mt_tile_end) phase_rank_multi<kV>(P, smem);
+        if (kM && P.mt_mesh_begin < P.mt_mesh_end) phase_rank_meshlet<kV>(P, smem);
         phase_done(P.ctl, 4, since);
     }
+}
+
+// The whole frame in one cooperative launch (every block resident, phases separated by
+// grid barriers), or the phases P.phases names. kM: the frame has meshlet tiles. Both
+// instantiations run the record path for the pairs that need it (skinning, shape keys,
+// subdivision, snapping, ...).
+template <bool kM>
+__global__ void __launch_bounds__(256, kM ? T3D_MESH_BLOCKS : T3D_MIN_BLOCKS) t3d_frame_kernel(const __grid_constant__ FrameParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    frame_body<kM ? 1 : 0>(P, smem, P.phases ? P.phases : 0x3Fu);
+}
+
+// One phase per launch (kPh one phase bit): a frame is a sequence of these launches, no
+// block waits on another, and each phase runs under its own register budget and
+// blocks per SM (kBlocks).
+template <int kV, uint32_t kPh, int kBlocks>
+__global__ void __launch_bounds__(256, kBlocks) t3d_phase_kernel(const __grid_constant__ FrameParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    frame_body<kV>(P, smem, kPh);
 }
 
 }  // namespace t3d
@@ -2261,6 +2315,26 @@ __global__ void __launch_bounds__(256, kM ? T3D_MESH_BLOCKS : T3D_MIN_BLOCKS) t3
 extern "C" const void* t3d_frame_kernel_ptr() { return (const void*)&t3d::t3d_frame_kernel<false>; }
 // The instantiation for frames with meshlet tiles.
 extern "C" const void* t3d_frame_kernel_mesh_ptr() { return (const void*)&t3d::t3d_frame_kernel<true>; }
+namespace t3d {
+template <int kM>
+const void* phase_kernel_ptr(int k) {
+    switch (k) {
+        case 0: return (const void*)&t3d_phase_kernel<kM | 2, 1u, kPhaseBlocks[kM][0]>;
+        case 1: return (const void*)&t3d_phase_kernel<kM | 4, 2u, kPhaseBlocks[kM][1]>;
+        case 2: return (const void*)&t3d_phase_kernel<kM | 6, 4u, kPhaseBlocks[kM][2]>;
+        case 3: return (const void*)&t3d_phase_kernel<kM | 8, 8u, kPhaseBlocks[kM][3]>;
+        case 4: return (const void*)&t3d_phase_kernel<kM | 10, 16u, kPhaseBlocks[kM][4]>;
+        case 5: return (const void*)&t3d_phase_kernel<kM | 12, 32u, kPhaseBlocks[kM][5]>;
+        default: return nullptr;
+    }
+}
+}  // namespace t3d
+// The one-phase kernel of phase k (0 prep .. 5 rank + emit), for frames with meshlet tiles
+// (mesh != 0) or without; and the blocks per SM it is compiled for.
+extern "C" const void* t3d_phase_kernel_ptr(int mesh, int k) {
+    return mesh ? t3d::phase_kernel_ptr<1>(k) : t3d::phase_kernel_ptr<0>(k);
+}
+extern "C" int t3d_phase_kernel_blocks(int mesh, int k) { return (k >= 0 && k < 6) ? t3d::kPhaseBlocks[mesh ? 1 : 0][k] : 0; }
 // The keyed streams of one mesh (k_bake_shapes) on stream st.
 extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
                                        const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
@@ -2285,6 +2359,21 @@ extern "C" size_t t3d_frame_smem_bytes_mesh(uint32_t tile_tris, uint32_t block_t
     size_t m = a > b ? a : b;
     m = m > c ? m : c;
     return m > d ? m : d;
+}
+
+// Shared memory of the one-phase kernel of phase k (0 prep .. 5 rank + emit): the
+// record-path layout of that phase and, for frames with meshlet tiles, the meshlet one.
+extern "C" size_t t3d_phase_smem_bytes(int mesh, int k, uint32_t tile_tris, uint32_t block_threads, uint32_t mesh_ucap) {
+    if (k == 0) return 0;
+    const size_t a = t3d_frame_smem_bytes(tile_tris, block_threads);
+    if (!mesh) return a;
+    size_t b = 0;
+    if (k == 2) b = t3d::mesh_tri_layout(tile_tris, mesh_ucap).total;
+    if (k == 3)
+        b = ((sizeof(t3d::TileSmem) + 15) & ~(size_t)15) +
+            (block_threads / 32) * (4ull * t3d::kBinsPadded + 4ull * tile_tris);
+    if (k == 5) b = t3d::mesh_rank_layout(tile_tris, mesh_ucap, block_threads / 32).total;
+    return a > b ? a : b;
 }
 
 // Compares div3 with IEEE division for every 32-bit pattern (NaNs match NaNs):

@@ -26,6 +26,7 @@
 
 extern "C" const void* t3d_frame_kernel_ptr();
 extern "C" const void* t3d_frame_kernel_mesh_ptr();
+extern "C" const void* t3d_phase_kernel_ptr(int mesh, int k);
 extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
                                        const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
                                        float4* ob);
@@ -69,24 +70,27 @@ void set_err(t3d_ctx* c, const char* fmt, ...) {
 
 int DevBuf::ensure(t3d_ctx* ctx, size_t bytes) {
     if (bytes <= cap) return T3D_OK;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
+    release();
     size_t want = std::max(bytes, (size_t)256);
     want = want + want / 4;
-    cudaError_t e = cudaMalloc(&ptr, want);
+    cudaError_t e = ctx->pool ? cudaMallocFromPoolAsync(&ptr, want, ctx->pool, ctx->stream) : cudaMalloc(&ptr, want);
     if (e != cudaSuccess) {
         ptr = nullptr;
-        set_err(ctx, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+        set_err(ctx, "device allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
         return T3D_E_OOM;
     }
+    pooled = ctx->pool ? ctx->stream : nullptr;
     cap = want;
     return T3D_OK;
 }
 void DevBuf::release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+        if (pooled) cudaFreeAsync(ptr, pooled);  // after the work already queued on the stream
+        else cudaFree(ptr);
+    }
     ptr = nullptr;
     cap = 0;
+    pooled = nullptr;
 }
 
 int HostBuf::ensure(size_t bytes) {
@@ -1579,10 +1583,15 @@ static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items,
     P.ctl = ctl;
     // frames with meshlet tiles run the instantiation that has their phases
     const bool mesh = P.mesh_begin < P.mesh_end;
-    const uint32_t cap = std::max(1u, (mesh ? ctx->max_grid_mesh : ctx->max_grid) / ctx->grid_share);
-    const size_t smem = mesh ? ctx->smem_mesh : ctx->smem_bytes;
+    // a launch of one phase runs that phase's own kernel (when split launches are on)
+    const uint32_t ph = P.phases;
+    const int pk = (ph && !(ph & (ph - 1))) ? __builtin_ctz(ph) : -1;
+    const bool one = pk >= 0 && pk < 6 && ctx->split_phases && ctx->phase_grid[mesh][pk];
+    const uint32_t cap = std::max(1u, (one ? ctx->phase_grid[mesh][pk] : mesh ? ctx->max_grid_mesh : ctx->max_grid) /
+                                          ctx->grid_share);
+    const size_t smem = one ? ctx->phase_smem[mesh][pk] : mesh ? ctx->smem_mesh : ctx->smem_bytes;
     uint32_t grid = std::max(1u, std::min(cap, max_items));
-    const void* fn = mesh ? t3d_frame_kernel_mesh_ptr() : t3d_frame_kernel_ptr();
+    const void* fn = one ? t3d_phase_kernel_ptr(mesh, pk) : mesh ? t3d_frame_kernel_mesh_ptr() : t3d_frame_kernel_ptr();
     void* args[] = {&P};
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof cfg);
@@ -1606,6 +1615,8 @@ static int launch_one(t3d_ctx* ctx, FrameParams P, Ctl* ctl, uint32_t max_items,
     }
     ctx->launches++;
     ctx->last_grid = grid;
+    for (int k = 0; k < 6; k++)
+        if (one ? k == pk : (ph == 0 || (ph >> k) & 1u)) ctx->phase_grid_used[k] = grid;
     return T3D_OK;
 }
 
@@ -1638,9 +1649,27 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
         P.tile_alt = F.tile_alt; P.vitem_alt = F.vitem_alt;
         P.has_multi = F.mt_desc.empty() ? 0u : 1u;
-        uint32_t items = (uint32_t)std::max({F.tiles.size(), F.mt_desc.size(), F.vitem_seg.size(),
-                                             (F.insts.size() + ctx->block_threads - 1) / ctx->block_threads});
-        return launch_one(ctx, P, ctl, items, st);
+        const uint32_t inst_blocks = (uint32_t)((F.insts.size() + ctx->block_threads - 1) / ctx->block_threads);
+        if (!ctx->split_phases) {
+            uint32_t items = (uint32_t)std::max({F.tiles.size(), F.mt_desc.size(), F.vitem_seg.size(), (size_t)inst_blocks});
+            return launch_one(ctx, P, ctl, items, st);
+        }
+        // one launch per phase, each sized to its own work (the prep phase spreads its models
+        // one per block over every SM; the histogram phase ranks one tile per warp); phases
+        // with no work are left out
+        const uint32_t nmt = (uint32_t)F.mt_desc.size(), warps = ctx->block_threads / 32;
+        const uint32_t seq[6][2] = {{1u, std::max<uint32_t>(1u, (uint32_t)std::max(F.insts.size(), F.segs.size()))},
+                                    {2u, (uint32_t)F.vitem_seg.size()},
+                                    {4u, (uint32_t)F.tiles.size()},
+                                    {8u, (nmt + warps - 1) / warps},
+                                    {16u, (uint32_t)F.mt_segs.size()},
+                                    {32u, nmt}};
+        for (const auto& q : seq) {
+            if (q[1] == 0 || (q[0] >= 8u && !P.has_multi)) continue;
+            P.phases = q[0];
+            if ((rc = launch_one(ctx, P, ctl, q[1], st))) return rc;
+        }
+        return T3D_OK;
     }
     // Plain: render pairs one after another, in draw order (render + flush per pair,
     // camera.go:2061-2106). A pair of one tile is one launch of one block (its phases

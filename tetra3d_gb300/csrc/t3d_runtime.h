@@ -13,9 +13,13 @@
 namespace t3d {
 
 // Grow-only device buffer.
+// Grow-only device buffer. In a context with a memory pool (serving slots) it grows by
+// stream-ordered allocation on the context's stream, which does not synchronize the
+// device the way cudaMalloc / cudaFree do.
 struct DevBuf {
     void* ptr = nullptr;
     size_t cap = 0;
+    cudaStream_t pooled = nullptr;  // stream of the stream-ordered allocation (null: cudaMalloc)
     int ensure(t3d_ctx* ctx, size_t bytes);
     void release();
 };
@@ -140,6 +144,12 @@ struct t3d_ctx {
     uint32_t max_grid_mesh = 0;
     size_t smem_mesh = 0;
     bool use_meshlets = true;     // t3d_set_meshlets: 0 sends every pair through the per-vertex record path
+    // batched frames as one launch per phase (t3d_set_split_phases); per phase kernel
+    // ([0] frames without meshlet tiles, [1] with; phases prep .. rank + emit): its shared
+    // memory and its co-resident blocks
+    bool split_phases = true;
+    size_t phase_smem[2][6] = {};
+    uint32_t phase_grid[2][6] = {};
     uint32_t spin_limit = 0;      // bounded device waits (0: the kernel's default)
     uint32_t next_scene = 1;
     std::map<uint32_t, std::unique_ptr<t3d::Scene>> scenes;
@@ -160,12 +170,14 @@ struct t3d_ctx {
     t3d::DevBuf valt, inst_lights, job_bytes, vis_rank, vinvw, out_invw;
     bool want_job_bytes = false;  // serving slots: per-job algorithmic bytes (FrameParams.job_bytes)
     uint32_t grid_share = 1;      // serving slots: launches use 1/grid_share of the co-resident blocks
+    cudaMemPool_t pool = nullptr; // serving slots: the server's pool for stream-ordered buffer growth
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
         seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
     uint64_t last_h2d = 0;
     uint32_t launches = 0;
     uint32_t last_grid = 0;
+    uint32_t phase_grid_used[6] = {};  // blocks of the last launch that ran each phase
     bool frame_pending = false;
     bool frame_valid = false;
     t3d_stats stats{};

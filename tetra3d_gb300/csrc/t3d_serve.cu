@@ -11,7 +11,9 @@
 // builds overlap each other and the GPU work of the other slots -- so requests
 // arriving while others are on the GPU are admitted as soon as a slot and
 // memory free up. Each request's output is written only by its own job's
-// segments, so its result does not depend on what it was batched with.
+// segments, so its result does not depend on what it was batched with. A slot's
+// buffers grow in stream order from the server's memory pool, so a batch larger
+// than any before does not stall the other slots.
 // Scenes must not be uploaded or released while a server runs.
 
 #include <cuda_runtime.h>
@@ -63,6 +65,7 @@ uint64_t fnv(const void* p, size_t n, uint64_t h) {
 
 struct t3d_server {
     t3d_ctx* owner = nullptr;
+    cudaMemPool_t pool = nullptr;  // the slots' scratch and outputs grow in this pool, in stream order
     uint64_t budget = 0;
     uint32_t max_batch = 1;
     std::vector<Slot> slots;
@@ -94,7 +97,9 @@ struct t3d_server {
         std::vector<uint64_t> vis(s.batch.size(), 0), sum(s.batch.size(), 1469598103934665603ull);
         std::vector<unsigned long long> jb(s.batch.size(), 0ull);
         if (rc == T3D_OK && !jb.empty() &&
-            cudaMemcpy(jb.data(), s.ctx->job_bytes.ptr, 8 * jb.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+            (cudaMemcpyAsync(jb.data(), s.ctx->job_bytes.ptr, 8 * jb.size(), cudaMemcpyDeviceToHost, s.ctx->stream) !=
+                 cudaSuccess ||
+             cudaStreamSynchronize(s.ctx->stream) != cudaSuccess))
             rc = T3D_E_CUDA;
         if (rc == T3D_OK) {
             const auto& info = s.ctx->tables.seg_info;
@@ -211,25 +216,51 @@ int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batc
     s->max_batch = max_batch;
     s->t0 = Clock::now();
     s->slots.resize(streams);
+    // A batch larger than any before grows its slot's buffers. Grown with cudaMalloc / cudaFree
+    // that would wait for every slot's work on the device (a latency spike for all requests in
+    // flight); grown from this pool in the slot's stream order it waits for nothing. The pool
+    // keeps freed memory for reuse.
+    {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = ctx->device;
+        cudaSetDevice(ctx->device);
+        if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess) {
+            delete s;
+            return T3D_E_CUDA;
+        }
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     for (uint32_t i = 0; i < streams; i++) {
         Slot& sl = s->slots[i];
         int rc = t3d_create(ctx->device, &sl.ctx);
         if (rc != T3D_OK) {
             for (uint32_t k = 0; k < i; k++) { cudaEventDestroy(s->slots[k].ev); t3d_destroy(s->slots[k].ctx); }
+            cudaMemPoolDestroy(s->pool);
             delete s;
             return rc;
         }
+        sl.ctx->pool = s->pool;
+        // pinned staging of launch tables and read-backs, sized once (a pinned allocation
+        // during serving would also synchronize the device)
+        sl.ctx->table_host.ensure(32ull << 20);
+        sl.ctx->readback.ensure(4ull << 20);
         sl.ctx->scene_owner = ctx;
         sl.ctx->tile_tris = ctx->tile_tris;
         sl.ctx->vchunk = ctx->vchunk;
         sl.ctx->block_threads = ctx->block_threads;
         sl.ctx->use_meshlets = ctx->use_meshlets;
+        sl.ctx->split_phases = ctx->split_phases;
         sl.ctx->spin_limit = ctx->spin_limit;
         sl.ctx->want_job_bytes = true;
-        // the slots' launches share the device: each takes 1/streams of the co-resident
-        // blocks, so every slot's cooperative grid fits beside the others' (grid barriers
-        // need all of a launch's blocks resident at once)
-        sl.ctx->grid_share = streams;
+        // With one launch per phase no block waits on another, so every slot launches full
+        // grids and the device interleaves the slots' blocks (a lone request gets every SM).
+        // A frame as one cooperative launch needs all its blocks resident at once: each slot
+        // then takes 1/streams of the co-resident blocks, so the slots' grids fit side by side.
+        sl.ctx->grid_share = ctx->split_phases ? 1u : streams;
         configure(sl.ctx);
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
     }
@@ -248,6 +279,7 @@ int t3d_server_destroy(t3d_server* s) {
         cudaEventDestroy(x.ev);
         t3d_destroy(x.ctx);
     }
+    cudaMemPoolDestroy(s->pool);
     delete s;
     return T3D_OK;
 }
