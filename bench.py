@@ -183,13 +183,19 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
             torch.cuda.synchronize()
 
+    # the autotuner picks the launch shape (one launch per phase or one cooperative launch) and
+    # the tile size on this scene before the timed region
     tuned = None
-    if args.tune:
+    if not args.no_tune:
         from tetra3d_gb300 import autotune
-        best, res = autotune.tune(ctx, sid, cam, frames=5, animate=False)
-        tuned = {"tile_tris": best[0], "block_threads": best[1], "vertex_chunk": best[2],
-                 "sweep_ms": {"x".join(map(str, k)): round(v, 4) for k, v in res.items()}}
+        a0 = time.perf_counter()
+        best, res = autotune.tune(ctx, sid, cam, frames=5, animate=False, chunks=())
+        tuned = {"tile_tris": best[0], "block_threads": best[1], "split_phases": best[2],
+                 "sweep_ms": {f"tile{k[0]}_block{k[1]}_split{k[2]}": round(v, 4) for k, v in res.items()},
+                 "seconds": round(time.perf_counter() - a0, 1)}
         ctx.set_models(sid, sd)  # restore the initial transforms after the sweep
+    split_used = tuned["split_phases"] if tuned else 1
+    tile_used = tuned["tile_tris"] if tuned else 2048
     # ---- device-resident value: captured CUDA graph of the batched frame ----
     ctx.graph_capture(sid, cam, animate=animate)
     ctx.graph_replay(args.warmup, stream=sh)
@@ -352,8 +358,11 @@ def run_ours(args, rank, world, local_rank):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": dict(workload_config(args.workload, sd), form="batched persistent kernel, CUDA graph replay",
-                           animated=animate, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "config": dict(workload_config(args.workload, sd),
+                           form=("batched: one persistent launch per phase" if split_used else
+                                 "batched: one cooperative persistent launch") + ", CUDA graph replay",
+                           tile_tris=tile_used, animated=animate,
+                           parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_step": alg_bytes / args.steps / max(1, world),
@@ -557,7 +566,8 @@ def main():
     ap.add_argument("--workload", default="batched", choices=["batched", "terrain", "cubes", "sphere", "serving"])
     ap.add_argument("--models", type=int, default=4096, help="models in the batched scene (4096 = the full workload)")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--tune", action="store_true", help="run the autotuner before the timed region")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default tuning: 2048-triangle "
+                                                              "tiles, one launch per phase)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep in the default run")

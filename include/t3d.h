@@ -457,7 +457,7 @@ typedef struct t3d_request {
 typedef struct t3d_completion {
     uint64_t id;
     int32_t  status;
-    uint32_t reserved;
+    uint32_t batch;           /* requests in the launch that rendered it */
     uint64_t visible_tris;
     double   arrival_s;
     double   admit_s;
@@ -465,14 +465,18 @@ typedef struct t3d_completion {
     uint64_t checksum;        /* order-dependent hash of the emitted stream */
     uint64_t model_bytes;     /* 48V+12T+64+48L bytes of the request's models that survived
                                  frustum culling (with 108 per visible triangle: its algorithmic bytes) */
+    double   launch_s;        /* its batch's launch tables built and its kernels queued */
 } t3d_completion;
 
 /* hbm_budget_bytes bounds the device bytes of in-flight requests' outputs and
  * scratch; max_batch bounds the jobs per launch; streams = launch slots that
- * run concurrently. Each slot's launches use 1/streams of the device's
- * co-resident blocks, so the launches of all slots fit on the device together. The slots render the context's resident scenes: while a
- * server runs, scenes are not uploaded, released or changed (set_models /
- * set_bones / set_shape_weights / set_lights) on that context. */
+ * run concurrently. With one launch per phase (t3d_set_split_phases, the default)
+ * every slot launches full grids and the device interleaves them; a context set to
+ * one cooperative launch per frame gives each slot 1/streams of the device's
+ * co-resident blocks, so the launches of all slots fit on the device together. The
+ * slots render the context's resident scenes: while a server runs, scenes are not
+ * uploaded, released or changed (set_models / set_bones / set_shape_weights /
+ * set_lights) on that context. */
 int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batch,
                       uint32_t streams, t3d_server** out);
 int t3d_server_destroy(t3d_server* srv);
@@ -481,6 +485,12 @@ int t3d_server_submit(t3d_server* srv, const t3d_request* req);
 /* verify = 1 (default) hashes every request's emitted stream into
  * t3d_completion.checksum (costs a device-to-host copy per request). */
 int t3d_server_set_verify(t3d_server* srv, int verify);
+/* Bounds the render pairs (visible model parts) of one batch (0 = no bound; default
+ * 4096): a batch's launch tables are built on the host in time proportional to its
+ * pairs, so the bound keeps one batch of many-model requests from holding its slot
+ * (and the requests queued behind it) for milliseconds. A request is admitted alone
+ * when it exceeds the bound by itself. */
+int t3d_server_set_batch_pairs(t3d_server* srv, uint32_t max_pairs);
 /* Non-blocking poll of finished requests. */
 int t3d_server_poll(t3d_server* srv, t3d_completion* out, uint32_t max, uint32_t* n_out);
 /* Replays requests at their arrival_s offsets from a driver thread and blocks

@@ -183,7 +183,16 @@ def test_serving_same_bits_alone_and_in_mix(ctx):
             c = mix[100 + rid]
             assert c.status == abi.T3D_OK
             assert (c.checksum, c.visible_tris) == alone[rid], f"request {rid} differs in the mix"
-            assert c.admit_s >= c.arrival_s and c.done_s >= c.admit_s
+            assert c.admit_s >= c.arrival_s and c.done_s >= c.launch_s >= c.admit_s and c.batch >= 1
+        # a bound of one render pair per batch: every request goes alone, with the same bits
+        ctx.lib.t3d_server_set_batch_pairs(srv.h, 1)
+        for rid, sid, sd, cam in reqs:
+            assert srv.submit(job(sid, cam), 200 + rid) == abi.T3D_OK
+        one = _drain(srv, len(reqs))
+        for rid, sid, sd, cam in reqs:
+            c = one[200 + rid]
+            assert c.status == abi.T3D_OK and c.batch == 1
+            assert (c.checksum, c.visible_tris) == alone[rid], f"request {rid} differs batched alone"
         for rid, sid, sd, cam in reqs[:4]:  # the checksum is over the oracle's bits
             ref = pyoracle.render(sd, cam)
             assert alone[rid] == (_fnv_frame(ref), ref.visible_tris)
@@ -795,4 +804,23 @@ def test_custom0_only_for_corrected_jobs(ctx):
         with pytest.raises(abi.T3DError):
             ctx.download_custom0()
     finally:
+        ctx.release(sid)
+
+
+def test_autotune_leaves_a_bit_exact_tuning(ctx):
+    """The autotuner sweeps launch shape x tile size (re-cutting the meshlets) and the vertex
+    chunk, leaves the context on the fastest setting, and that setting renders the oracle's bits."""
+    from tetra3d_gb300 import autotune
+    sd = scenes.small_variant("batched", 21)
+    sid = ctx.upload(sd)
+    try:
+        best, res = autotune.tune(ctx, sid, sd.camera, frames=2, tiles=(1024, 2048), splits=(1, 0), chunks=(2048, 4096))
+        shapes = {k: v for k, v in res.items() if len(k) == 3}
+        assert len(shapes) == 4 and best[:3] in shapes
+        assert shapes[best[:3]] == min(shapes.values())
+        ctx.render(sid, sd.camera)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, sd.camera), f"after autotune {best}")
+    finally:
+        ctx.set_tuning(tile_tris=2048, block_threads=256, vertex_chunk=4096)
+        ctx.set_split_phases(1)
         ctx.release(sid)

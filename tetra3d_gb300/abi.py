@@ -124,9 +124,10 @@ class Request(C.Structure):
 
 
 class Completion(C.Structure):
-    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("batch", C.c_uint32),
                 ("visible_tris", C.c_uint64), ("arrival_s", C.c_double), ("admit_s", C.c_double),
-                ("done_s", C.c_double), ("checksum", C.c_uint64), ("model_bytes", C.c_uint64)]
+                ("done_s", C.c_double), ("checksum", C.c_uint64), ("model_bytes", C.c_uint64),
+                ("launch_s", C.c_double)]
 
 
 class NoallocArgs(C.Structure):
@@ -179,6 +180,7 @@ SIGNATURES = {
     "t3d_server_create": (C.c_int, [_VP, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(_VP)]),
     "t3d_server_destroy": (C.c_int, [_VP]),
     "t3d_server_set_verify": (C.c_int, [_VP, C.c_int]),
+    "t3d_server_set_batch_pairs": (C.c_int, [_VP, C.c_uint32]),
     "t3d_server_submit": (C.c_int, [_VP, C.POINTER(Request)]),
     "t3d_server_poll": (C.c_int, [_VP, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),
     "t3d_server_replay": (C.c_int, [_VP, C.POINTER(Request), C.c_uint32, C.POINTER(Completion)]),

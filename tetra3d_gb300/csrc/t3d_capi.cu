@@ -466,13 +466,21 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     cudaStream_t st = ctx->last_stream ? ctx->last_stream : ctx->stream;
     FrameTables& F = ctx->tables;
     const size_t nseg = F.segs.size();
-    const size_t rb = 4 * nseg + sizeof(Ctl) * ctx->nctl + 64;
+    // one read-back: per-pair counts, the launch control blocks and (serving slots) the
+    // per-job algorithmic bytes
+    const size_t njb = (ctx->want_job_bytes && ctx->params.job_bytes) ? F.jobs.size() : 0;
+    const size_t ctl_off = (4 * nseg + 63) & ~(size_t)63;
+    const size_t jb_off = ctl_off + sizeof(Ctl) * ctx->nctl;
+    const size_t rb = jb_off + 8 * njb + 64;
     if (ctx->readback.ensure(rb)) { set_err(ctx, "pinned readback alloc failed"); return T3D_E_OOM; }
     uint32_t* counts = (uint32_t*)ctx->readback.ptr;
-    Ctl* ctls = (Ctl*)((char*)ctx->readback.ptr + ((4 * nseg + 63) & ~(size_t)63));
+    Ctl* ctls = (Ctl*)((char*)ctx->readback.ptr + ctl_off);
+    unsigned long long* jbh = (unsigned long long*)((char*)ctx->readback.ptr + jb_off);
     if (nseg) CKR(cudaMemcpyAsync(counts, ctx->seg_count.ptr, 4 * nseg, cudaMemcpyDeviceToHost, st));
     if (ctx->nctl) CKR(cudaMemcpyAsync(ctls, ctx->ctl.ptr, sizeof(Ctl) * ctx->nctl, cudaMemcpyDeviceToHost, st));
+    if (njb) CKR(cudaMemcpyAsync(jbh, ctx->job_bytes.ptr, 8 * njb, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
+    ctx->job_bytes_host.assign(jbh, jbh + njb);
     ctx->frame_pending = false;
     t3d_stats s;
     memset(&s, 0, sizeof s);
@@ -516,7 +524,7 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
             s.phase_busy[i] = g ? (double)c.busy[order[i]] / 1e3 / g : 0.0;
         }
     }
-    s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl;
+    s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl + 8 * njb;
     ctx->stats = s;
     ctx->frame_valid = true;
     if (stats_out) *stats_out = s;

@@ -169,6 +169,7 @@ struct t3d_ctx {
     struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
     t3d::DevBuf valt, inst_lights, job_bytes, vis_rank, vinvw, out_invw;
     bool want_job_bytes = false;  // serving slots: per-job algorithmic bytes (FrameParams.job_bytes)
+    std::vector<unsigned long long> job_bytes_host;  // their values, read back by t3d_frame_sync
     uint32_t grid_share = 1;      // serving slots: launches use 1/grid_share of the co-resident blocks
     cudaMemPool_t pool = nullptr; // serving slots: the server's pool for stream-ordered buffer growth
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,

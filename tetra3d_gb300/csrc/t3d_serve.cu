@@ -24,6 +24,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -41,6 +42,7 @@ struct Pending {
     double arrival_abs;  // seconds since server start
     double admit_abs = 0;
     uint64_t bytes = 0;
+    uint32_t pairs = 0;  // render pairs of its scene (model parts), the size of its host table build
 };
 
 struct Slot {
@@ -49,6 +51,8 @@ struct Slot {
     std::thread worker;
     std::vector<Pending> batch;
     uint64_t bytes = 0;
+    uint64_t pairs = 0;
+    double launch_abs = 0;  // the batch's tables built and its kernels queued
 };
 
 // FNV-1a over the raw bytes of a request's emitted stream, in emit order.
@@ -68,6 +72,7 @@ struct t3d_server {
     cudaMemPool_t pool = nullptr;  // the slots' scratch and outputs grow in this pool, in stream order
     uint64_t budget = 0;
     uint32_t max_batch = 1;
+    uint32_t max_pairs = 4096;  // render pairs per batch (0: no bound)
     std::vector<Slot> slots;
     std::mutex mu;
     std::condition_variable cv;
@@ -89,18 +94,33 @@ struct t3d_server {
         return 116ull * sc->ntris + 48ull * sc->nverts + 1024ull * (sc->models.size() + 4);
     }
 
+    // render pairs of a request's scene (counted once per scene: scenes do not change while
+    // the server runs); called without the lock held
+    std::mutex pairs_mu;
+    std::map<uint32_t, uint32_t> scene_pairs;
+    uint32_t request_pairs(const t3d_request& r) {
+        std::lock_guard<std::mutex> g(pairs_mu);
+        auto c = scene_pairs.find(r.job.scene);
+        if (c != scene_pairs.end()) return c->second;
+        auto it = owner->scenes.find(r.job.scene);
+        if (it == owner->scenes.end()) return 0;
+        uint64_t n = 0;
+        for (const auto& m : it->second->models) n += it->second->meshes[m.d.mesh].parts.size();
+        const uint32_t v = (uint32_t)std::min<uint64_t>(n, 0xFFFFFFFFull);
+        scene_pairs[r.job.scene] = v;
+        return v;
+    }
+
     // Completions of the slot's finished launch (called without the lock held).
     void finish(Slot& s, int rc) {
         t3d_stats st;
         if (rc == T3D_OK) rc = t3d_frame_sync(s.ctx, &st);
         const double t = now();
         std::vector<uint64_t> vis(s.batch.size(), 0), sum(s.batch.size(), 1469598103934665603ull);
+        // per-job algorithmic bytes, read back with the counts by t3d_frame_sync
         std::vector<unsigned long long> jb(s.batch.size(), 0ull);
-        if (rc == T3D_OK && !jb.empty() &&
-            (cudaMemcpyAsync(jb.data(), s.ctx->job_bytes.ptr, 8 * jb.size(), cudaMemcpyDeviceToHost, s.ctx->stream) !=
-                 cudaSuccess ||
-             cudaStreamSynchronize(s.ctx->stream) != cudaSuccess))
-            rc = T3D_E_CUDA;
+        if (rc == T3D_OK)
+            for (size_t k = 0; k < jb.size() && k < s.ctx->job_bytes_host.size(); k++) jb[k] = s.ctx->job_bytes_host[k];
         if (rc == T3D_OK) {
             const auto& info = s.ctx->tables.seg_info;
             for (const auto& si : info)
@@ -133,6 +153,8 @@ struct t3d_server {
             c.visible_tris = rc == T3D_OK ? vis[k] : 0;
             c.arrival_s = s.batch[k].arrival_abs;
             c.admit_s = s.batch[k].admit_abs;
+            c.launch_s = s.launch_abs;
+            c.batch = (uint32_t)s.batch.size();
             c.done_s = t;
             c.checksum = (verify && rc == T3D_OK) ? sum[k] : 0;
             c.model_bytes = rc == T3D_OK ? jb[k] : 0;
@@ -140,6 +162,7 @@ struct t3d_server {
         }
         inflight -= s.bytes;
         s.bytes = 0;
+        s.pairs = 0;
         s.batch.clear();
     }
 
@@ -161,8 +184,10 @@ struct t3d_server {
                 continue;
             }
             if (inflight + s.bytes + p.bytes > budget) break;  // wait for memory
+            if (max_pairs && !s.batch.empty() && s.pairs + p.pairs > max_pairs) break;  // the next batch takes it
             p.admit_abs = t;
             s.bytes += p.bytes;
+            s.pairs += p.pairs;
             s.batch.push_back(p);
             queue.pop_front();
         }
@@ -196,9 +221,8 @@ struct t3d_server {
             jobs.resize(s.batch.size());
             for (size_t k = 0; k < s.batch.size(); k++) jobs[k] = s.batch[k].req.job;
             int rc = t3d_render_jobs(s.ctx, jobs.data(), (uint32_t)jobs.size(), T3D_MODE_BATCHED, 0, nullptr);
-            if (rc == T3D_OK) rc = cudaEventRecord(s.ev, s.ctx->stream) == cudaSuccess ? T3D_OK : T3D_E_CUDA;
-            if (rc == T3D_OK) rc = cudaEventSynchronize(s.ev) == cudaSuccess ? T3D_OK : T3D_E_CUDA;
-            finish(s, rc);
+            s.launch_abs = now();
+            finish(s, rc);  // its read-back waits for the launch
             cv.notify_all();  // memory and the slot are free again
         }
     }
@@ -264,6 +288,19 @@ int t3d_server_create(t3d_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_batc
         configure(sl.ctx);
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
     }
+    // Back the pool with memory now (1 GB per slot, within the budget): a slot's first large
+    // batch then draws on it instead of mapping new memory while requests wait.
+    {
+        const size_t per = (size_t)std::min<uint64_t>(1ull << 30, hbm_budget_bytes / streams);
+        std::vector<void*> warm(streams, nullptr);
+        cudaStream_t st = s->slots[0].ctx->stream;
+        for (uint32_t i = 0; i < streams; i++)
+            if (cudaMallocFromPoolAsync(&warm[i], per, s->pool, st) != cudaSuccess) warm[i] = nullptr;
+        for (void* p : warm)
+            if (p) cudaFreeAsync(p, st);
+        cudaStreamSynchronize(st);
+        cudaGetLastError();
+    }
     for (auto& sl : s->slots) sl.worker = std::thread([s, &sl] { s->slot_loop(sl); });
     *out = s;
     return T3D_OK;
@@ -298,6 +335,7 @@ int t3d_server_submit(t3d_server* s, const t3d_request* req) {
     Pending p;
     p.req = *req;
     p.bytes = s->request_bytes(*req);
+    p.pairs = s->request_pairs(*req);
     if (p.bytes > s->budget) return T3D_E_ADMIT;
     {
         std::lock_guard<std::mutex> g(s->mu);
@@ -305,6 +343,13 @@ int t3d_server_submit(t3d_server* s, const t3d_request* req) {
         s->queue.push_back(p);
     }
     s->cv.notify_all();
+    return T3D_OK;
+}
+
+int t3d_server_set_batch_pairs(t3d_server* s, uint32_t max_pairs) {
+    if (!s) return T3D_E_INVAL;
+    std::lock_guard<std::mutex> g(s->mu);
+    s->max_pairs = max_pairs;
     return T3D_OK;
 }
 
@@ -325,19 +370,24 @@ int t3d_server_replay(t3d_server* s, const t3d_request* reqs, uint32_t n, t3d_co
         if (reqs[i].job.camera.width <= 0 || reqs[i].job.camera.height <= 0) return T3D_E_INVAL;
     }
     // Enqueue everything with future arrival times; the scheduler admits each
-    // request only once its arrival time has passed.
+    // request only once its arrival time has passed. The requests are prepared
+    // before the lock is taken, so the slots keep admitting meanwhile.
+    std::vector<Pending> add(n);
+    for (uint32_t i = 0; i < n; i++) {
+        add[i].req = reqs[i];
+        add[i].arrival_abs = reqs[i].arrival_s;
+        add[i].bytes = s->request_bytes(reqs[i]);
+        add[i].pairs = s->request_pairs(reqs[i]);
+    }
+    std::stable_sort(add.begin(), add.end(), [](const Pending& a, const Pending& b) { return a.arrival_abs < b.arrival_abs; });
     {
         std::lock_guard<std::mutex> g(s->mu);
-        double base = s->now() + 0.002;
-        for (uint32_t i = 0; i < n; i++) {
-            Pending p;
-            p.req = reqs[i];
-            p.arrival_abs = base + reqs[i].arrival_s;
-            p.bytes = s->request_bytes(reqs[i]);
-            s->queue.push_back(p);
-        }
-        std::stable_sort(s->queue.begin(), s->queue.end(),
-                         [](const Pending& a, const Pending& b) { return a.arrival_abs < b.arrival_abs; });
+        const double base = s->now() + 0.002;
+        for (auto& p : add) p.arrival_abs += base;
+        std::deque<Pending> merged;
+        std::merge(s->queue.begin(), s->queue.end(), add.begin(), add.end(), std::back_inserter(merged),
+                   [](const Pending& a, const Pending& b) { return a.arrival_abs < b.arrival_abs; });
+        s->queue.swap(merged);
     }
     s->cv.notify_all();
     std::vector<t3d_completion> got;

@@ -208,12 +208,14 @@ def job(sid, cam, light_mask=None):
 class Server:
     """Continuous-batching render server over a Context's resident scenes."""
 
-    def __init__(self, ctx, hbm_budget_bytes=150 << 30, max_batch=64, streams=4, verify=True):
+    def __init__(self, ctx, hbm_budget_bytes=150 << 30, max_batch=64, streams=4, verify=True, max_pairs=None):
         self.ctx = ctx
         h = C.c_void_p()
         ctx._check(ctx.lib.t3d_server_create(ctx.h, hbm_budget_bytes, max_batch, streams, C.byref(h)), "server_create")
         self.h = h
         ctx.lib.t3d_server_set_verify(self.h, int(verify))
+        if max_pairs is not None:
+            ctx._check(ctx.lib.t3d_server_set_batch_pairs(self.h, int(max_pairs)), "server_set_batch_pairs")
 
     def close(self):
         if self.h:

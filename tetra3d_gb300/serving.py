@@ -85,8 +85,19 @@ def latency_summary(completions):
     tris = sum(int(c.visible_tris) for c in ok)
     # algorithmic bytes (48V+12T+64+48L of surviving models + 108 per visible triangle)
     alg = sum(int(c.model_bytes) + 108 * int(c.visible_tris) for c in ok)
+    # where the time goes: queue wait (arrival -> admission), launch-table build and launch
+    # (admission -> launch), device work and read-back (launch -> completion)
+    def pct(v, q):
+        return float(np.percentile(v, q)) if len(v) else 0.0
+    wait = [(c.admit_s - c.arrival_s) * 1e3 for c in ok]
+    build = [(c.launch_s - c.admit_s) * 1e3 for c in ok]
+    dev = [(c.done_s - c.launch_s) * 1e3 for c in ok]
     return {"requests": len(completions), "ok": len(ok), "algorithmic_bytes": alg,
             "algorithmic_gb_per_s": alg / span / 1e9 if span > 0 else 0.0,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "max_ms": float(lat.max()), "tris_per_s": tris / span if span > 0 else 0.0,
-            "req_per_s": len(ok) / span if span > 0 else 0.0, "visible_tris": tris}
+            "req_per_s": len(ok) / span if span > 0 else 0.0, "visible_tris": tris,
+            "mean_batch": float(np.mean([c.batch for c in ok])) if ok else 0.0,
+            "wait_ms_p50_p99": [pct(wait, 50), pct(wait, 99)],
+            "build_ms_p50_p99": [pct(build, 50), pct(build, 99)],
+            "device_ms_p50_p99": [pct(dev, 50), pct(dev, 99)]}
