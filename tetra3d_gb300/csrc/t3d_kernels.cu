@@ -1724,19 +1724,18 @@ constexpr uint32_t kPrepHead = 208;
 static_assert(offsetof(DevPrep, invcam) + 16 == kPrepHead && sizeof(DevPrep) % 16 == 0, "DevPrep head layout");
 // Triangle phase: MeshHdr | per-round warp counts (two rounds' worth) and per-warp depth
 // range | buf (the model's prep record up to the model-space camera, then lidx + pos of one
-// meshlet) | (X/w, Y/w, Z, test bits) per slot
+// meshlet); each slot's 12 bytes of position become its clip record (X/w, Y/w, test bits)
 struct MeshTriWarp {
     uint32_t cnt[2][kMaxWarps];
     float mn[kMaxWarps], mx[kMaxWarps];
 };
-struct MeshTriLayout { size_t wc, buf, clip, total; };
+struct MeshTriLayout { size_t wc, buf, total; };
 __host__ __device__ __forceinline__ MeshTriLayout mesh_tri_layout(uint32_t T, uint32_t U) {
     MeshTriLayout L;
     size_t o = sizeof(MeshHdr);
     L.wc = o; o += al16(sizeof(MeshTriWarp));
     const size_t buf = kPrepHead + (size_t)mlet_lidx_bytes(T) + 12ull * U;
     L.buf = o; o += al16(buf);
-    L.clip = o; o += 16ull * U;
     L.total = o;
     return L;
 }
@@ -1829,8 +1828,7 @@ constexpr uint32_t kTriSteps = 4;
 // (triangle order). After the last round's reads of buf, thread 0 starts the copy of
 // the block's next tile into it (nx: its queue slot, descriptor and culling flag).
 __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDesc td, unsigned char* buf,
-                                              MeshTriWarp& wc, float4* sclip, NextTile& nx, MeshHdr& H,
-                                              uint32_t nitems) {
+                                              MeshTriWarp& wc, NextTile& nx, MeshHdr& H, uint32_t nitems) {
     const uint32_t mt = td.mt;
     const DevPrep& pr = *reinterpret_cast<const DevPrep*>(buf);  // its head: mvp, M, dirrot, invcam
     float* mrow = reinterpret_cast<float*>(buf);
@@ -1847,18 +1845,27 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
     }
     const uint32_t U = td.vmin, nt = td.t1 - td.t0;
     const uint16_t* __restrict__ lidx = reinterpret_cast<const uint16_t*>(buf + kPrepHead);
-    const float* __restrict__ pos = reinterpret_cast<const float*>(buf + kPrepHead + mlet_lidx_bytes(nt));
+    // a slot's position (x, y, z), then, written over it by the same thread, its clip record
+    float* slot = reinterpret_cast<float*>(buf + kPrepHead + mlet_lidx_bytes(nt));
+    // Triangle.RecalculateCenter (mesh.go:1980-1982), ((A + B) + C) / 3 per axis, is a constant of
+    // the mesh: the scene keeps it per triangle (computed at upload in the same binary32
+    // operations); the tile's run is asked into L2 now and read by the triangle loop
+    const float* __restrict__ cen = P.jobs[td.job].centers + 3ull * ((size_t)td.tbase + td.t0);
+    if (threadIdx.x == 0) l2_prefetch(cen, 12ull * nt);
     const float nearp = td.nearp, farp = td.farp;
     for (uint32_t v = threadIdx.x; v < U; v += blockDim.x) {
         // MultVecW and the x/y divide of the rejection tests (model.go:808-873), and the
         // per-corner outcomes of those tests as bits: 1 inside near/far, 2 / 4 left / right of
         // the screen (X/w < -0.5 / > 0.5), 8 / 16 below / above it
-        const float4 c = clip_rows(mrow, pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]);
+        float* cl = slot + 3 * v;
+        const float4 c = clip_rows(mrow, cl[0], cl[1], cl[2]);
         const float w1 = c.w < 0.0f ? 0.000001f : c.w;
         const float sx = c.x / w1, sy = c.y / w1;
         const uint32_t f = ((c.z + 1.0f >= nearp && c.z < farp) ? 1u : 0u) | (sx < -0.5f ? 2u : 0u) |
                            (sx > 0.5f ? 4u : 0u) | (sy < -0.5f ? 8u : 0u) | (sy > 0.5f ? 16u : 0u);
-        sclip[v] = make_float4(sx, sy, c.z, __uint_as_float(f));
+        cl[0] = sx;
+        cl[1] = sy;
+        cl[2] = __uint_as_float(f);
     }
     next_desc(P, nx);
     const f3 ic = mk3(pr.invcam[0], pr.invcam[1], pr.invcam[2]);
@@ -1886,11 +1893,10 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
             s2[it] = 0u;
             if (t < nt) {
                 const uint32_t i0 = lidx[3 * t], i1 = lidx[3 * t + 1], i2 = lidx[3 * t + 2];
-                const float4 c0 = sclip[i0], c1 = sclip[i1], c2 = sclip[i2];
-                // Triangle.RecalculateCenter (mesh.go:1980-1982): ((A + B) + C) / 3 per axis
-                const f3 ctr = mk3(div3(pos[3 * i0] + pos[3 * i1] + pos[3 * i2]),
-                                   div3(pos[3 * i0 + 1] + pos[3 * i1 + 1] + pos[3 * i2 + 1]),
-                                   div3(pos[3 * i0 + 2] + pos[3 * i1 + 2] + pos[3 * i2 + 2]));
+                const float4 c0 = make_float4(slot[3 * i0], slot[3 * i0 + 1], 0.f, slot[3 * i0 + 2]);
+                const float4 c1 = make_float4(slot[3 * i1], slot[3 * i1 + 1], 0.f, slot[3 * i1 + 2]);
+                const float4 c2 = make_float4(slot[3 * i2], slot[3 * i2 + 1], 0.f, slot[3 * i2 + 2]);
+                const f3 ctr = mk3(__ldg(&cen[3 * t]), __ldg(&cen[3 * t + 1]), __ldg(&cen[3 * t + 2]));
                 vis = tri_visible_bits(backface, ic, c0, c1, c2, ctr, d[it]);
                 s01[it] = i0 | (i1 << 16);
                 s2[it] = i2;
@@ -1967,7 +1973,6 @@ __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsig
     const MeshTriLayout L = mesh_tri_layout(P.tile_tris, P.mesh_ucap);
     MeshTriWarp& wc = *reinterpret_cast<MeshTriWarp*>(smem + L.wc);
     unsigned char* buf = smem + L.buf;
-    float4* sclip = reinterpret_cast<float4*>(smem + L.clip);
     const uint32_t n = P.mesh_end - P.mesh_begin, limit = spin_limit(P);
     uint32_t ph0 = 0;
     // the barrier lives in bytes that other phases use: set up here, invalidated at the end
@@ -1999,7 +2004,7 @@ __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsig
         if (!__syncthreads_and(ok)) break;
         const TileDesc td = H.td[0];
         if (copied) {
-            mesh_tile_tri(P, td, buf, wc, sclip, nx, H, n);
+            mesh_tile_tri(P, td, buf, wc, nx, H, n);
         } else {  // skipped pair or culled model
             next_desc(P, nx);
             next_culled(P, nx);
@@ -2228,7 +2233,7 @@ __device__ __forceinline__ void phase_start(unsigned long long& since) {
 // 65536 / (256 blocks)), per phase: prep, vertex records, triangles, histogram, scan,
 // rank + emit; for frames with meshlet tiles and for the others.
 #ifndef T3D_PHASE_BLOCKS_MESH
-#define T3D_PHASE_BLOCKS_MESH 2, 2, 3, 2, 2, 2
+#define T3D_PHASE_BLOCKS_MESH 2, 2, 4, 2, 2, 2
 #endif
 #ifndef T3D_PHASE_BLOCKS_REC
 #define T3D_PHASE_BLOCKS_REC 4, 4, 4, 4, 4, 4
