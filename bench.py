@@ -3,8 +3,9 @@
 Default workload: the batched form -- 4096 models with log-uniform vertex
 counts in [24, 65536] (35.1M vertices, 69.7M triangles), 32 point lights +
 ambient with a random LightGroup per model, 1920x1080 camera, animated
-transforms -- rendered as one persistent-kernel launch per frame and replayed
-from a captured CUDA graph. A step is one frame over all 4096 models.
+transforms -- rendered as one persistent launch per phase (the launch shape and
+tile size picked by the autotuner) and replayed from a captured CUDA graph. A
+step is one frame over all 4096 models.
 
   value  visible triangles/s with the scene resident in HBM (graph replay)
   e2e    the same metric through the public C ABI with host buffers: per step

@@ -80,6 +80,12 @@ func (c *Context) UploadScene(desc *C.t3d_scene_desc) (uint32, error) {
 	return uint32(id), c.err(C.t3d_scene_upload(c.h, desc, &id))
 }
 
+// SetSplitPhases picks the launch shape of a frame: 1 (the default) one persistent launch
+// per phase, 0 a batched frame as one cooperative launch. The emitted stream is the same.
+func (c *Context) SetSplitPhases(mode int) error {
+	return c.err(C.t3d_set_split_phases(c.h, C.int(mode)))
+}
+
 // SetModels pushes changed model descriptors [first, first+len(models)) (Node.Transform
 // changes, visibility, colour). The copy is queued behind frames already issued.
 func (c *Context) SetModels(scene uint32, first int, models []C.t3d_model_desc) error {
@@ -245,6 +251,14 @@ func (c *Context) NewServer(hbmBudget uint64, maxBatch, streams uint32) (*Server
 		return nil, c.err(rc)
 	}
 	return &Server{c: c, h: h}, nil
+}
+
+// SetBatchPairs bounds the render pairs of one batch (0: no bound; the default is 4096).
+func (s *Server) SetBatchPairs(maxPairs uint32) error {
+	if rc := C.t3d_server_set_batch_pairs(s.h, C.uint32_t(maxPairs)); rc != C.T3D_OK {
+		return fmt.Errorf("t3d_server_set_batch_pairs: %d", int(rc))
+	}
+	return nil
 }
 
 // Submit queues one request (thread safe).

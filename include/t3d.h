@@ -92,7 +92,7 @@ extern "C" {
 
 /* render modes */
 #define T3D_MODE_PLAIN   0   /* one launch per model (the reference's per-model loop) */
-#define T3D_MODE_BATCHED 1   /* all models of all jobs in one persistent launch */
+#define T3D_MODE_BATCHED 1   /* all models of all jobs in one frame: a persistent launch per phase */
 
 /* Maximum lights one model may be lit by (length of its light list). */
 #define T3D_MAX_LIGHTS_PER_MODEL 128
@@ -374,14 +374,14 @@ int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chu
  * enable = 0: every pair writes and reads per-vertex records in device memory. The
  * emitted stream is the same bit for bit either way. */
 int         t3d_set_meshlets(t3d_ctx* ctx, int enable);
-/* Launch shape of a batched frame (no reference counterpart: the reference has one
- * CPU path). enable = 1 (the default): one launch per phase (model prep, vertex
+/* Launch shape of a frame (no reference counterpart: the reference has one CPU
+ * path). mode = 1 (the default): one persistent launch per phase (model prep, vertex
  * records, triangles, histogram, scan, rank + emit), each kernel compiled with its
  * own register budget and sized to its own co-resident blocks, the launch boundary
- * ordering the phases. enable = 0: the whole frame in one cooperative persistent
+ * ordering the phases. mode = 0: a batched frame in one cooperative persistent
  * launch whose phases are separated by grid barriers. The emitted stream is the same
  * bit for bit either way; the autotuner picks the faster. */
-int         t3d_set_split_phases(t3d_ctx* ctx, int enable);
+int         t3d_set_split_phases(t3d_ctx* ctx, int mode);
 /* Bounded device waits (grid barriers, bulk-copy waits): polls before the frame
  * gives up and t3d_frame_sync returns T3D_E_TIMEOUT (0 = the default, seconds).
  * Meant for tests of the timeout path; the context stays usable and the next

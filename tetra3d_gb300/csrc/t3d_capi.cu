@@ -199,11 +199,11 @@ int t3d_set_meshlets(t3d_ctx* ctx, int enable) {
     return T3D_OK;
 }
 
-int t3d_set_split_phases(t3d_ctx* ctx, int enable) {
-    if (!ctx) return T3D_E_INVAL;
+int t3d_set_split_phases(t3d_ctx* ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 1) return T3D_E_INVAL;
     cudaSetDevice(ctx->device);
     if (ctx->last_stream) CKR(cudaStreamSynchronize(ctx->last_stream));
-    ctx->split_phases = enable != 0;
+    ctx->split_phases = mode != 0;
     drop_graph(ctx);
     return T3D_OK;
 }

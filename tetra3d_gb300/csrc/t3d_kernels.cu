@@ -1,17 +1,18 @@
-// t3d_kernels.cu -- the GB300 vertex stage: one persistent kernel with phases.
+// t3d_kernels.cu -- the GB300 vertex stage: persistent kernels, one per phase.
 //
-//   P0 model prep   per (job, model): Node.Transform (+ animation step), MVP,
+//   prep            per (job, model): Node.Transform (+ animation step), MVP,
 //                   model-space camera, SphereInFrustum, light beginModel.
-//   P1 vertex       per (segment, vertex chunk): MultVecW, the cull record,
-//                   per-vertex lighting and the emitted corner attributes.
-//   P2 triangle     per (segment, tile): near/far, +-0.5 and backface rejection,
-//                   the depth key, a stable in-tile compaction and, for
-//                   single-tile segments, the whole bucket sort + emit.
-//   P3..P5          multi-tile segments only: tile histograms, cross-tile bin
-//                   scan, stable rank + emit.
-// Phases are separated by a bounded software grid barrier; the grid is sized so
-// that every block is co-resident (cooperative launch), and work items are
-// pulled from per-phase atomic queues so uneven models balance across SMs.
+//   vertex          per-vertex route only, per (segment, vertex chunk): MultVecW,
+//                   the cull record, lighting and the emitted corner attributes.
+//   triangles       per tile (a meshlet, or a run of the per-vertex route): near/far,
+//                   +-0.5 and backface rejection, the depth key, a stable in-tile
+//                   compaction (per-vertex single-tile segments: the whole sort + emit).
+//   histogram, scan, rank + emit: tile histograms and stable ranking, cross-tile
+//                   bin scan, emission of the corners in output order.
+// Each phase is a persistent kernel over its own atomic work queue (uneven models
+// balance across SMs), compiled with its own register budget and shared memory;
+// the launch boundary orders the phases. The same phases also run as one
+// cooperative launch with a bounded software grid barrier between them.
 //
 // Parity: compiled with -fmad=false and IEEE div/sqrt, every value follows the
 // reference's unfused binary32 operation order (see t3d_math.cuh).

@@ -60,10 +60,10 @@ class Context:
         per-vertex record path. The emitted stream is the same either way."""
         self._check(self.lib.t3d_set_meshlets(self.h, int(bool(enable))), "set_meshlets")
 
-    def set_split_phases(self, enable):
-        """Batched frames as one launch per phase (default on) or one cooperative launch with
-        grid barriers between the phases. The emitted stream is the same either way."""
-        self._check(self.lib.t3d_set_split_phases(self.h, int(bool(enable))), "set_split_phases")
+    def set_split_phases(self, mode):
+        """Launch shape: 1 (default) one persistent launch per phase, 0 a batched frame as one
+        cooperative launch with grid barriers between the phases. The stream is the same."""
+        self._check(self.lib.t3d_set_split_phases(self.h, int(mode)), "set_split_phases")
 
     def set_wait_limit(self, polls):
         """Polls a bounded device wait makes before the frame gives up (0: the default)."""
