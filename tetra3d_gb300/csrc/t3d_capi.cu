@@ -144,7 +144,7 @@ int t3d_destroy(t3d_ctx* ctx) {
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
                       &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
                       &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights,
-                      &ctx->job_bytes, &ctx->vis_rank, &ctx->vinvw, &ctx->out_invw})
+                      &ctx->job_bytes, &ctx->vis_rank, &ctx->vinvw, &ctx->out_invw, &ctx->live_tiles})
         b->release();
     cudaStreamSynchronize(ctx->stream);  // stream-ordered frees of a pooled context have run
     ctx->table_host.release();

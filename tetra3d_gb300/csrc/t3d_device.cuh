@@ -226,7 +226,8 @@ struct Ctl {
     uint32_t err_info;
     unsigned long long bytes;       // algorithmic bytes of surviving models
     uint32_t culled;
-    uint32_t pad[3];
+    uint32_t live;                  // meshlet tiles with visible triangles (FrameParams.live_tiles)
+    uint32_t pad[2];
     unsigned long long t_end[8];    // globaltimer when the last block finished phase k; [7] = kernel start
     unsigned long long busy[8];     // sum over blocks of the time spent inside phase k (ns)
 };
@@ -296,6 +297,10 @@ struct FrameParams {
     float4* inst_lights;
     // per job: algorithmic bytes of its models that survive frustum culling (serving); may be null
     unsigned long long* job_bytes;
+    // meshlet frames: the multi-tile numbers of the meshlet tiles with visible triangles, in the
+    // order the triangle phase finished them, from index mt_mesh_begin (Ctl.live of them); the
+    // histogram and emit phases take only these. Null: every tile of the range.
+    uint32_t* live_tiles;
 };
 // Dense visible list of a meshlet tile i: depth keys at vis_depth + i * tile_tris,
 // 3 slots per entry at vis_vloc + 3 * i * tile_tris, tile_count[i] entries.

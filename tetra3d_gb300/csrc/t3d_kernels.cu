@@ -124,6 +124,15 @@ __device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes) {
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)) : "memory");
 }
 
+// The k-th meshlet tile the histogram and emit phases take: the k-th entry of the list of
+// tiles with visible triangles, or the k-th tile of the range when there is no list.
+__device__ __forceinline__ uint32_t mesh_tile_at(const FrameParams& P, uint32_t k) {
+    return P.live_tiles ? __ldcg(&P.live_tiles[P.mt_mesh_begin + k]) : P.mt_mesh_begin + k;
+}
+__device__ __forceinline__ uint32_t mesh_tile_count(const FrameParams& P) {
+    return P.live_tiles ? vload(&P.ctl->live) : P.mt_mesh_end - P.mt_mesh_begin;
+}
+
 __device__ __forceinline__ uint32_t next_item(Ctl* ctl, int q, uint32_t* s_item) {
     __syncthreads();
     if (threadIdx.x == 0) *s_item = atomicAdd(&ctl->queue[q], 1u);
@@ -1542,13 +1551,14 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
     const SmemLayout L = smem_layout(smem, T);
     const uint32_t nw = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t per = T / nw;
-    const uint32_t n_rec = P.mt_tile_end - P.mt_tile_begin, n_all = n_rec + (P.mt_mesh_end - P.mt_mesh_begin);
+    const uint32_t n_rec = P.mt_tile_end - P.mt_tile_begin;
+    const uint32_t n_all = n_rec + (P.mt_mesh_begin < P.mt_mesh_end ? mesh_tile_count(P) : 0u);
     uint32_t* wh = L.whist + wid * kBinsPadded;
     uint32_t k = 0;
     if (lane == 0) k = atomicAdd(&P.ctl->queue[2], 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
     while (k < n_all) {
-        const uint32_t i = k < n_rec ? P.mt_tile_begin + k : P.mt_mesh_begin + (k - n_rec);
+        const uint32_t i = k < n_rec ? P.mt_tile_begin + k : mesh_tile_at(P, k - n_rec);
         const TileDesc& td = P.mt_desc[i];
         const uint32_t s = td.seg;
         if (td.flags & SEG_MESHLET) {  // counts, cross-tile counts and the tile's stable ranking
@@ -1818,6 +1828,13 @@ __device__ __forceinline__ void next_culled(const FrameParams& P, NextTile& nx) 
     if (threadIdx.x == 0 && nx.kn < P.mesh_end - P.mesh_begin) nx.culled = P.preps[nx.td.inst].culled;
 }
 
+// A meshlet tile with no visible triangle: its counts in the pair's cross-tile scan are
+// zeros (the histogram phase takes only the tiles with visible triangles).
+__device__ __forceinline__ void zero_tile_hist(const FrameParams& P, uint32_t mt) {
+    uint4* h = reinterpret_cast<uint4*>(P.tile_hist + (size_t)mt * kBins);
+    for (uint32_t b = threadIdx.x; b < kBins / 4; b += blockDim.x) h[b] = make_uint4(0u, 0u, 0u, 0u);
+}
+
 // Triangle steps of 32 that a warp holds in registers per round (a round covers
 // blockDim / 32 * kTriSteps * 32 triangles of the tile).
 constexpr uint32_t kTriSteps = 4;
@@ -1951,9 +1968,11 @@ __device__ __forceinline__ void mesh_tile_tri(const FrameParams& P, const TileDe
         }
         base += tot;
     }
+    if (base == 0 && !(td.flags & SEG_SINGLE)) zero_tile_hist(P, mt);
     if (threadIdx.x == 0) {
         P.tile_count[mt] = base;
         if (base > 0) {
+            if (P.live_tiles) P.live_tiles[P.mt_mesh_begin + atomicAdd(&P.ctl->live, 1u)] = mt;
             float mn = wc.mn[0], mx = wc.mx[0];
             for (uint32_t w = 1; w < nw; w++) { mn = fminf(mn, wc.mn[w]); mx = fmaxf(mx, wc.mx[w]); }
             atomicMin(&P.seg_minmax[2 * td.seg], __float_as_uint(mn));
@@ -2009,6 +2028,7 @@ __device__ __noinline__ void phase_triangles_meshlet(const FrameParams& P, unsig
         } else {  // skipped pair or culled model
             next_desc(P, nx);
             next_culled(P, nx);
+            if (!(td.flags & SEG_SINGLE)) zero_tile_hist(P, td.mt);
             if (threadIdx.x == 0) {
                 P.tile_count[td.mt] = 0u;
                 H.item[0] = nx.kn;
@@ -2074,19 +2094,22 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
     unsigned char* rec = smem + ML.rec;
     const uint32_t limit = spin_limit(P);
     uint32_t ph0 = 0, ph1 = 0, ph2 = 0, ph3 = 0;  // mbarrier phases
-    const uint32_t nmt = P.mt_mesh_end - P.mt_mesh_begin;
+    const uint32_t nmt = mesh_tile_count(P);
     if (threadIdx.x == 0) {
         for (int b = 0; b < 4; b++) mbar_init(&H.bar[b], 1);
         fence_mbar_init();
         const uint32_t k0 = atomicAdd(&P.ctl->queue[9], 1u);
         H.item[0] = k0;
-        if (k0 < nmt) mesh_stage_tile(P, P.mt_desc[P.mt_mesh_begin + k0], __ldcg(&P.tile_count[P.mt_mesh_begin + k0]), S, &H.bar[2]);
+        if (k0 < nmt) {
+            const uint32_t i0 = mesh_tile_at(P, k0);
+            mesh_stage_tile(P, P.mt_desc[i0], __ldcg(&P.tile_count[i0]), S, &H.bar[2]);
+        }
     }
     __syncthreads();
     for (;;) {
         const uint32_t k = H.item[0];
         if (k >= nmt) break;
-        const uint32_t i = P.mt_mesh_begin + k;
+        const uint32_t i = mesh_tile_at(P, k);
         const TileDesc td = S.td;
         const uint32_t n = S.n;
         uint32_t kn = 0xFFFFFFFFu;
@@ -2123,11 +2146,12 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
             ms.nl = nl;
         }
         stage_model_consts<false, false>(S.seg, *reinterpret_cast<const DevJob*>(S.job), S.pr, ms);
-        uint32_t nn = 0;
+        uint32_t nn = 0, in_ = 0;
         TileDesc tn;
         if (threadIdx.x == 0 && kn < nmt) {  // read now, used after the records
-            nn = __ldcg(&P.tile_count[P.mt_mesh_begin + kn]);
-            tn = P.mt_desc[P.mt_mesh_begin + kn];
+            in_ = mesh_tile_at(P, kn);
+            nn = __ldcg(&P.tile_count[in_]);
+            tn = P.mt_desc[in_];
         }
         if (nl) {
             ok = mbar_wait(&H.bar[3], ph3, P.ctl, limit) && ok;
@@ -2160,7 +2184,6 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
         if (threadIdx.x == 0) {
             if (nn > 0) {  // the next tile's vertex block, lists and bases into L2
                 const uint32_t u4n = mlet_slots4(tn.vmin), ntn = tn.t1 - tn.t0;
-                const uint32_t in_ = P.mt_mesh_begin + kn;
                 l2_prefetch(mlet_addr(tn) + mlet_lidx_bytes(ntn) + 12ull * u4n,
                             (size_t)mlet_aos_stride(tn.flags & SEG_COLORS) * u4n);
                 l2_prefetch(P.vis_rank + (size_t)in_ * T, 4ull * nn);
@@ -2188,8 +2211,8 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
             }
         }
         } else if (threadIdx.x == 0 && kn < nmt) {  // an empty tile: stage the next one now
-            mesh_stage_tile(P, P.mt_desc[P.mt_mesh_begin + kn], __ldcg(&P.tile_count[P.mt_mesh_begin + kn]), S,
-                            &H.bar[2]);
+            const uint32_t in2 = mesh_tile_at(P, kn);
+            mesh_stage_tile(P, P.mt_desc[in2], __ldcg(&P.tile_count[in2]), S, &H.bar[2]);
         }
         __syncthreads();  // the shared arrays are free; the slot taken above becomes the current tile
         if (threadIdx.x == 0) H.item[0] = kn;

@@ -1541,12 +1541,14 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     }
     P.inst_lights = nullptr;
     P.vis_rank = nullptr;
-    if (F.any_mesh) {  // the instances' staged light lists and the meshlet tiles' rank lists
+    P.live_tiles = nullptr;
+    if (F.any_mesh) {  // the instances' staged light lists, the meshlet tiles' rank lists and live list
         if ((rc = ctx->inst_lights.ensure(ctx, 56ull * kMaxLights * ninst + 16)) ||
-            (rc = ctx->vis_rank.ensure(ctx, 4ull * nmt * ctx->tile_tris)))
+            (rc = ctx->vis_rank.ensure(ctx, 4ull * nmt * ctx->tile_tris)) || (rc = ctx->live_tiles.ensure(ctx, 4 * nmt)))
             return rc;
         P.inst_lights = (float4*)ctx->inst_lights.ptr;
         P.vis_rank = (uint32_t*)ctx->vis_rank.ptr;
+        P.live_tiles = (uint32_t*)ctx->live_tiles.ptr;
     }
 
     P.vinvw = nullptr;

@@ -167,7 +167,7 @@ struct t3d_ctx {
     cudaEvent_t ev_upload = nullptr;  // the last table upload has left the pinned staging buffer
     cudaEvent_t ev_models = nullptr;  // the last model write has reached the device (and left its staging)
     struct t3d_raster_state* raster = nullptr;  // images and scratch of t3d_frame_raster
-    t3d::DevBuf valt, inst_lights, job_bytes, vis_rank, vinvw, out_invw;
+    t3d::DevBuf valt, inst_lights, job_bytes, vis_rank, vinvw, out_invw, live_tiles;
     bool want_job_bytes = false;  // serving slots: per-job algorithmic bytes (FrameParams.job_bytes)
     std::vector<unsigned long long> job_bytes_host;  // their values, read back by t3d_frame_sync
     uint32_t grid_share = 1;      // serving slots: launches use 1/grid_share of the co-resident blocks
