@@ -135,14 +135,16 @@ def workload_config(workload, sd):
 
 def time_cpu(sd, cam, threads, animated, min_seconds=10.0, max_reps=50, first_frame=1):
     """The oracle (the reference's path restated on the CPU) on whole frames of the workload:
-    frame k applies every model's animation step k times, as the k-th graph replay does.
-    Repeats until min_seconds have passed. Returns (visible tris/s, frames, seconds)."""
+    frame k applies every model's animation step k times, as the k-th graph replay does. The
+    output arrays are allocated and touched once before the timed frames (the reference's
+    render loop reuses its scratch and vertex lists). Repeats until min_seconds have passed.
+    Returns (visible tris/s, frames, seconds)."""
     from oracle import pyoracle
+    r = pyoracle.Renderer(sd, cam)
+    r.render(animate_frames=first_frame if animated else 0, threads=threads)
     reps, vis, t0 = 0, 0, time.perf_counter()
     while True:
-        f = pyoracle.render(sd, cam, animate_frames=(first_frame + reps) if animated else 0, threads=threads)
-        vis += f.visible_tris
-        del f
+        vis += r.render(animate_frames=(first_frame + reps) if animated else 0, threads=threads)
         reps += 1
         el = time.perf_counter() - t0
         if el >= min_seconds or reps >= max_reps:
@@ -345,12 +347,24 @@ def run_ours(args, rank, world, local_rank):
                               args.serve_max_requests)
 
     # ---- CPU baseline (the oracle port on all host threads, whole frames of the same workload) ----
-    cpu = None
+    cpu = cpu1 = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, reps, el = time_cpu(sd, cam, threads, animate, min_seconds=args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "cpu_model": cpu_model(), "kind": "port",
                "sample": f"{reps} whole frames ({sd.nmodels} models{', animated' if animate else ''}) in {el:.1f} s"}
+        # the reference's Render is one goroutine: the same port on one host thread, over every
+        # 8th model of the frame (render pairs are independent, so the sample's rate is the frame's)
+        from oracle import pyoracle
+        sub = scenes.subset(sd, np.arange(0, sd.nmodels, 8)) if sd.nmodels >= 64 else sd
+        r1 = pyoracle.Renderer(sub, cam)
+        r1.render(animate_frames=1 if animate else 0, threads=1)  # the output arrays touched once
+        c0 = time.perf_counter()
+        vis1 = r1.render(animate_frames=1 if animate else 0, threads=1)
+        el1 = time.perf_counter() - c0
+        del r1
+        cpu1 = {"value": vis1 / el1, "unit": UNIT, "cores": 1, "cpu_model": cpu_model(), "kind": "port",
+                "sample": f"one frame of every 8th model ({sub.nmodels} models) on one host thread, {el1:.1f} s"}
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -370,6 +384,7 @@ def run_ours(args, rank, world, local_rank):
                          "traffic_note": "DRAM bytes per launch are not measurable inside this run (ncu only); "
                                          "the capture of this kernel is summarised in profiles/"},
             "cpu_baseline": cpu,
+            "cpu_baseline_single_thread": cpu1,
             "e2e": e2e,
             "clocks": clk.summary(),
             "gpu_launches": int(args.steps) * int(st_last.launches),
@@ -419,12 +434,16 @@ def feature_frames(ctx, stream, sh, base_ms, frames=10, warmup=3):
             v1, _ = ctx.counters()
             vis = (v1 - v0) / frames
             st = ctx.sync()
-            # the oracle (the reference's algorithm restated on the CPU) on the same frame, all host threads
+            # the oracle (the reference's algorithm restated on the CPU) on the same frame, all host
+            # threads, its output arrays allocated and touched before the timed render
             from oracle import pyoracle
             threads = os.cpu_count() or 1
+            rc = pyoracle.Renderer(sd, sd.camera)
+            rc.render(threads=threads)
             c0 = time.perf_counter()
-            cpu_vis = pyoracle.render(sd, sd.camera, threads=threads).visible_tris
+            cpu_vis = rc.render(threads=threads)
             cpu_s = time.perf_counter() - c0
+            del rc
             out[kind] = {"ms_per_frame": round(ms, 4), "visible_tris": int(vis), "tris_per_s": vis / (ms / 1e3),
                          "time_vs_plain_frame": round(ms / base_ms, 3),
                          "cpu_baseline": {"value": cpu_vis / cpu_s, "unit": "tris/s", "cores": threads, "kind": "port",
@@ -449,9 +468,11 @@ def serving_sweep(ctx, rates, seconds, max_requests, seed=7, baseline_requests=1
     sids = [ctx.upload(sd) for sd in sds]
     tris = [sd.total_tris() for sd in sds]
     rng = np.random.Generator(np.random.PCG64(seed))
-    srv = Server(ctx, hbm_budget_bytes=150 << 30, max_batch=64, streams=4, verify=False)
+    slots = 8  # launch slots (host threads building and launching batches concurrently)
+    srv = Server(ctx, hbm_budget_bytes=150 << 30, max_batch=64, streams=slots, verify=False)
     out = {"scenes": len(sds), "scene_tris_min": int(min(tris)), "scene_tris_max": int(max(tris)),
-           "scene_tris_total": int(sum(tris)), "hbm_budget_gb": 150, "max_batch": 64, "slots": 4,
+           "scene_tris_total": int(sum(tris)), "hbm_budget_gb": 150, "max_batch": 64, "slots": slots,
+           "max_pairs_per_batch": 4096,
            "scene_gen_s": round(gen_s, 2), "rates": []}
     try:
         jobs, arr = serving.poisson_requests(rng, sids, sds, centres, 2000.0, 128)  # warm-up
@@ -535,14 +556,14 @@ def run_reference(args, rank, world):
     from oracle import pyoracle
     threads = os.cpu_count() or 1
     animate = args.workload == "batched"
+    # the output arrays are allocated once, as the reference's render loop reuses its scratch
+    r = pyoracle.Renderer(sd, sd.camera)
     for w in range(args.warmup):
-        pyoracle.render(sd, sd.camera, animate_frames=(w + 1) if animate else 0, threads=threads)
+        r.render(animate_frames=(w + 1) if animate else 0, threads=threads)
     vis = 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        f = pyoracle.render(sd, sd.camera, animate_frames=(args.warmup + k + 1) if animate else 0, threads=threads)
-        vis += f.visible_tris
-        del f
+        vis += r.render(animate_frames=(args.warmup + k + 1) if animate else 0, threads=threads)
     el = time.perf_counter() - t0
     value = vis / el
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
