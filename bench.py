@@ -11,7 +11,7 @@ step is one frame over all 4096 models.
   e2e    the same metric through the public C ABI with host buffers: per step
          the host pushes every model transform (t3d_scene_set_models), renders
          (t3d_render, batched) and reads the per-pair visible counts back
-         (t3d_frame_sync)
+         (t3d_frame_readback + t3d_frame_collect, pipelined one frame deep)
   plain  one launch per render pair (the reference's render + flush loop)
 
 python bench.py [--gpus N --steps K --warmup W] [--impl reference]
@@ -265,13 +265,16 @@ def run_ours(args, rank, world, local_rank):
             ctx.render(sid, cam, mode=abi.MODE_BATCHED, stream=sh)
             tm["render_call"] += time.perf_counter() - a2
 
-        # A game loop: while the GPU renders frame i the host advances the transforms of
-        # frame i + 1 (Node.Rotate) and pushes them (the copy waits for frame i on the
-        # device); then it reads frame i's result and starts frame i + 1.
+        # A pipelined game loop: frame i's read-back of its per-pair counts is queued right
+        # behind it; while the GPU renders frame i the host advances the transforms of frame
+        # i + 1 (Node.Rotate) and pushes them (the copy is queued behind frame i and its
+        # read-back), queues frame i + 1, and only then collects frame i's counts, so the GPU
+        # goes from one frame to the next without waiting for the host.
         t0 = time.perf_counter()
         push()
         render()
         for i in range(ek):
+            ctx.readback()
             a0 = time.perf_counter()
             nxt = scenes.mult(step, rot) if (animate and i + 1 < ek) else rot
             tm["game_loop_rotate"] += time.perf_counter() - a0
@@ -279,14 +282,14 @@ def run_ours(args, rank, world, local_rank):
                 rot = nxt
                 sd.mv["rotation"] = rot.reshape(n, 16)
                 push()
+                render()
             a1 = time.perf_counter()
-            st = ctx.sync()
+            st = ctx.collect()
             tm["sync"] += time.perf_counter() - a1
             ev += st.visible_tris
             h2d += n * C.sizeof(abi.ModelDesc) + st.h2d_bytes
             d2h += st.d2h_bytes
-            if i + 1 < ek:
-                render()
+        ctx.sync()
         el = time.perf_counter() - t0
         e2e = {"value": ev / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d // ek),
                "d2h_bytes_per_step": int(d2h // ek), "ms_per_step": el / ek * 1e3, "steps": ek,

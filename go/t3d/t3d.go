@@ -80,6 +80,16 @@ func (c *Context) UploadScene(desc *C.t3d_scene_desc) (uint32, error) {
 	return uint32(id), c.err(C.t3d_scene_upload(c.h, desc, &id))
 }
 
+// FrameReadback queues the read-back of the last frame's counts behind it; FrameCollect
+// waits for it and returns that frame's stats (a render loop can queue the next frame in
+// between, so the GPU does not wait for the host).
+func (c *Context) FrameReadback() error { return c.err(C.t3d_frame_readback(c.h)) }
+
+func (c *Context) FrameCollect() (C.t3d_stats, error) {
+	var st C.t3d_stats
+	return st, c.err(C.t3d_frame_collect(c.h, &st))
+}
+
 // SetSplitPhases picks the launch shape of a frame: 1 (the default) one persistent launch
 // per phase, 0 a batched frame as one cooperative launch. The emitted stream is the same.
 func (c *Context) SetSplitPhases(mode int) error {

@@ -425,6 +425,15 @@ int t3d_render_jobs(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t num_jobs,
                     int mode, int animate, void* stream);
 /* Waits for the last frame and fills the segment counts. */
 int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out);
+/* Deferred read-back for a pipelined render loop (no reference counterpart: the
+ * reference renders and flushes frame by frame). t3d_frame_readback enqueues a copy
+ * of the last frame's per-pair counts and launch status after it on its stream and
+ * returns; the caller may then push the next frame's models and render it, and
+ * t3d_frame_collect waits for the copy and returns the read-back frame's stats (the
+ * same as t3d_frame_sync would have, without updating the context's per-pair counts,
+ * which belong to the latest frame). One read-back can be in flight per context. */
+int t3d_frame_readback(t3d_ctx* ctx);
+int t3d_frame_collect(t3d_ctx* ctx, t3d_stats* stats_out);
 /* Cumulative counters since t3d_create over every frame (graph replays
  * included): visible triangles and the 48V+12T+64+48L bytes of models that
  * survived frustum culling. Waits for the last frame. */

@@ -824,3 +824,34 @@ def test_autotune_leaves_a_bit_exact_tuning(ctx):
         ctx.set_tuning(tile_tris=2048, block_threads=256, vertex_chunk=4096)
         ctx.set_split_phases(1)
         ctx.release(sid)
+
+
+def test_deferred_readback_pipelines_frames(ctx):
+    """t3d_frame_readback / t3d_frame_collect: with frame i + 1 queued before frame i's counts are
+    collected, every collected frame reports its own counts (those of the synchronous path)."""
+    sd = scenes.feature_scene(5)
+    sid = ctx.upload(sd)
+    try:
+        cams = [scenes.feature_camera(v) for v in ("persp", "tilted", "ortho", "persp")]
+        expect = []
+        for c in cams:
+            ctx.render(sid, c, mode=abi.MODE_BATCHED)
+            expect.append(int(ctx.sync().visible_tris))
+        assert len(set(expect)) > 1  # distinct counts, so a mix-up would show
+        got = []
+        ctx.render(sid, cams[0], mode=abi.MODE_BATCHED)
+        for k in range(len(cams)):
+            ctx.readback()
+            if k + 1 < len(cams):
+                ctx.render(sid, cams[k + 1], mode=abi.MODE_BATCHED)
+            got.append(int(ctx.collect().visible_tris))
+        assert got == expect
+        assert int(ctx.sync().visible_tris) == expect[-1]
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, cams[-1]), "after pipelined frames")
+        # one read-back at a time; a collect needs a read-back
+        ctx.readback()
+        assert ctx.lib.t3d_frame_readback(ctx.h) == abi.T3D_E_INVAL
+        ctx.collect()
+        assert ctx.lib.t3d_frame_collect(ctx.h, None) == abi.T3D_E_INVAL
+    finally:
+        ctx.release(sid)

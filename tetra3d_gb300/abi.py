@@ -158,6 +158,8 @@ SIGNATURES = {
     "t3d_set_tuning": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     "t3d_set_meshlets": (C.c_int, [_VP, C.c_int]),
     "t3d_set_split_phases": (C.c_int, [_VP, C.c_int]),
+    "t3d_frame_readback": (C.c_int, [_VP]),
+    "t3d_frame_collect": (C.c_int, [_VP, C.POINTER(Stats)]),
     "t3d_set_wait_limit": (C.c_int, [_VP, C.c_uint32]),
     "t3d_scene_upload": (C.c_int, [_VP, C.POINTER(SceneDesc), C.POINTER(C.c_uint32)]),
     "t3d_scene_release": (C.c_int, [_VP, C.c_uint32]),

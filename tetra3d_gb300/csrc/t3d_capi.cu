@@ -112,7 +112,8 @@ int t3d_create(int device, t3d_ctx** out) {
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_upload, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_models, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->ev_models, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_readback, cudaEventDisableTiming) != cudaSuccess) {
         delete ctx;
         return T3D_E_CUDA;
     }
@@ -152,6 +153,8 @@ int t3d_destroy(t3d_ctx* ctx) {
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
     if (ctx->ev_models) cudaEventDestroy(ctx->ev_models);
+    if (ctx->ev_readback) cudaEventDestroy(ctx->ev_readback);
+    ctx->readback2.release();
     t3d_raster_release(ctx);
     ctx->model_host.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -527,6 +530,76 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.d2h_bytes = 4 * nseg + sizeof(Ctl) * ctx->nctl + 8 * njb;
     ctx->stats = s;
     ctx->frame_valid = true;
+    if (stats_out) *stats_out = s;
+    return T3D_OK;
+}
+
+int t3d_frame_readback(t3d_ctx* ctx) {
+    if (!ctx) return T3D_E_INVAL;
+    if (!ctx->frame_pending && !ctx->frame_valid) {
+        set_err(ctx, "frame_readback: no frame rendered");
+        return T3D_E_INVAL;
+    }
+    if (ctx->rb2_pending) {
+        set_err(ctx, "frame_readback: the previous read-back was not collected");
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->last_stream ? ctx->last_stream : ctx->stream;
+    FrameTables& F = ctx->tables;
+    const size_t nseg = F.segs.size();
+    const size_t ctl_off = (4 * nseg + 63) & ~(size_t)63;
+    if (ctx->readback2.ensure(ctl_off + sizeof(Ctl) * ctx->nctl + 64)) {
+        set_err(ctx, "pinned readback alloc failed");
+        return T3D_E_OOM;
+    }
+    if (nseg) CKR(cudaMemcpyAsync(ctx->readback2.ptr, ctx->seg_count.ptr, 4 * nseg, cudaMemcpyDeviceToHost, st));
+    if (ctx->nctl)
+        CKR(cudaMemcpyAsync((char*)ctx->readback2.ptr + ctl_off, ctx->ctl.ptr, sizeof(Ctl) * ctx->nctl,
+                            cudaMemcpyDeviceToHost, st));
+    CKR(cudaEventRecord(ctx->ev_readback, st));
+    uint64_t total = 0;
+    for (const auto& si : F.seg_info) total += si.capacity;
+    ctx->rb2_nseg = nseg;
+    ctx->rb2_nctl = ctx->nctl;
+    ctx->rb2_launches = ctx->launches;
+    ctx->rb2_total = total;
+    ctx->rb2_h2d = ctx->last_h2d;
+    ctx->rb2_pending = true;
+    return T3D_OK;
+}
+
+int t3d_frame_collect(t3d_ctx* ctx, t3d_stats* stats_out) {
+    if (!ctx) return T3D_E_INVAL;
+    if (!ctx->rb2_pending) {
+        set_err(ctx, "frame_collect: no read-back in flight");
+        return T3D_E_INVAL;
+    }
+    cudaSetDevice(ctx->device);
+    ctx->rb2_pending = false;
+    CKR(cudaEventSynchronize(ctx->ev_readback));
+    const uint32_t* counts = (const uint32_t*)ctx->readback2.ptr;
+    const Ctl* ctls = (const Ctl*)((const char*)ctx->readback2.ptr + ((4 * ctx->rb2_nseg + 63) & ~(size_t)63));
+    t3d_stats s;
+    memset(&s, 0, sizeof s);
+    for (uint32_t i = 0; i < ctx->rb2_nctl; i++) {
+        if (ctls[i].err) {
+            set_err(ctx, "frame kernel reported error %d (launch %u)", ctls[i].err, i);
+            return (ctls[i].err == ERR_BARRIER_TIMEOUT || ctls[i].err == ERR_COPY_TIMEOUT) ? T3D_E_TIMEOUT : T3D_E_CUDA;
+        }
+        s.algorithmic_bytes += ctls[i].bytes;
+        s.culled_models += ctls[i].culled;
+    }
+    for (size_t k = 0; k < ctx->rb2_nseg; k++) {
+        s.visible_tris += counts[k];
+        if (counts[k]) s.drawn_parts++;
+    }
+    s.total_tris = ctx->rb2_total;
+    s.total_parts = (uint32_t)ctx->rb2_nseg;
+    s.algorithmic_bytes += 108ull * s.visible_tris;
+    s.launches = ctx->rb2_launches;
+    s.h2d_bytes = ctx->rb2_h2d;
+    s.d2h_bytes = 4 * ctx->rb2_nseg + sizeof(Ctl) * ctx->rb2_nctl;
     if (stats_out) *stats_out = s;
     return T3D_OK;
 }

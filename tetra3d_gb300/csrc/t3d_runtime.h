@@ -159,6 +159,14 @@ struct t3d_ctx {
     t3d::FrameParams params;
     const t3d::DevInst* insts_noanim = nullptr;  // same instances with animate = 0
     t3d::HostBuf table_host, readback, model_host;
+    // deferred read-back of one frame (t3d_frame_readback / t3d_frame_collect): its pinned copy of
+    // the per-pair counts and control blocks, the event after the copy, and the frame's sizes
+    t3d::HostBuf readback2;
+    cudaEvent_t ev_readback = nullptr;
+    bool rb2_pending = false;
+    size_t rb2_nseg = 0;
+    uint32_t rb2_nctl = 0, rb2_launches = 0;
+    uint64_t rb2_total = 0, rb2_h2d = 0;
     // launch tables of the last render (reused while nothing they depend on changed)
     std::vector<unsigned char> table_sig;
     std::vector<uint64_t> table_model_vers;

@@ -118,6 +118,16 @@ class Context:
         self._check(self.lib.t3d_frame_sync(self.h, C.byref(st)), "frame_sync")
         return st
 
+    def readback(self):
+        """Enqueues the read-back of the last frame's counts (collect() returns them)."""
+        self._check(self.lib.t3d_frame_readback(self.h), "frame_readback")
+
+    def collect(self):
+        """Waits for the read-back started by readback() and returns that frame's stats."""
+        st = abi.Stats()
+        self._check(self.lib.t3d_frame_collect(self.h, C.byref(st)), "frame_collect")
+        return st
+
     def segments(self):
         n = C.c_uint32()
         self._check(self.lib.t3d_frame_segments(self.h, None, 0, C.byref(n)), "frame_segments")
