@@ -291,16 +291,37 @@ __device__ __noinline__ void phase_prep(const FrameParams& P) {
         }
         // Mesh.Dimensions.MaxSpan for the model-level point-light skip (camera.go:1625-1629)
         pr.maxspan = mag3(mk3(me.dmax[0] - me.dmin[0], me.dmax[1] - me.dmin[1], me.dmax[2] - me.dmin[2]));
-        // meshlet frames: the model's light list as its render pairs' vertex loops read it, once
-        if ((kV & 1) && P.inst_lights && !culled && !skinned) {
+    }
+    // meshlet frames: each model's light list as its render pairs' vertex loops read it, staged
+    // once, by one warp per model of this block (the models k = blockIdx.x + gridDim.x * t whose
+    // prep records this block's threads just wrote): lane l stages lights l, l + 32, ..., and
+    // the kept ones (not skipped by the model-level range test) go out in list order
+    if ((kV & 1) && P.inst_lights) {
+        __syncthreads();
+        const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+        for (uint32_t t = threadIdx.x >> 5;; t += blockDim.x >> 5) {
+            const uint32_t k = blockIdx.x + gridDim.x * t;
+            if (k >= n) break;
+            const uint32_t i = P.inst_begin + k;
+            const DevInst in = P.insts[i];
+            DevPrep& pr = P.preps[i];
+            const DevJob& J = P.jobs[in.job];
+            if (pr.culled || (J.models[in.model].flags & MOD_SKINNED)) continue;
             SLight* out = reinterpret_cast<SLight*>(P.inst_lights) + (size_t)i * kMaxLights;
             const uint32_t nl = min(in.light_cnt, (uint32_t)kMaxLights);
             uint32_t o = 0;
-            for (uint32_t k = 0; k < nl; k++) {
-                const SLight d = light_for_model(J.lights[P.inst_light_idx[in.light_off + k]], pr.inv_r, pr.M, pr.maxspan);
-                if (!d.skip) out[o++] = d;
+            for (uint32_t k0 = 0; k0 < nl; k0 += 32) {
+                SLight d;
+                bool keep = false;
+                if (k0 + lane < nl) {
+                    d = light_for_model(J.lights[P.inst_light_idx[in.light_off + k0 + lane]], pr.inv_r, pr.M, pr.maxspan);
+                    keep = !d.skip;
+                }
+                const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) out[o + __popc(bal & lt)] = d;
+                o += __popc(bal);
             }
-            pr.nl = o;
+            if (lane == 0) pr.nl = o;
         }
     }
     const uint32_t ns = P.seg_end - P.seg_begin;
@@ -2160,25 +2181,34 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
         ok = mbar_wait(&H.bar[1], ph1, P.ctl, limit) && ok;
         ph1 ^= 1u;
         __syncthreads();  // the constants are in place
-        // every slot's emitted corner, in place: a round of blockDim slots reads its inputs,
-        // then (after a barrier) writes its records
-        for (uint32_t v0 = 0; v0 < U; v0 += blockDim.x) {
-            const uint32_t v = v0 + threadIdx.x;
-            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), bb = a, kc = a;
-            if (v < U) {
-                const float4* in = reinterpret_cast<const float4*>(vin + (size_t)as * v);
-                a = in[0];
-                bb = in[1];
-                if (colors) kc = in[2];
+        // every slot's emitted corner, in place: a round of two slots per thread reads its
+        // inputs, then (after a barrier) writes its records; a record covers only input bytes of
+        // its own or earlier slots, all read by the end of the round
+        for (uint32_t v0 = 0; v0 < U; v0 += 2 * blockDim.x) {
+            float4 a[2], bb[2], kc[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint32_t v = v0 + h * blockDim.x + threadIdx.x;
+                a[h] = make_float4(0.f, 0.f, 0.f, 0.f); bb[h] = a[h]; kc[h] = a[h];
+                if (v < U) {
+                    const float4* in = reinterpret_cast<const float4*>(vin + (size_t)as * v);
+                    a[h] = in[0];
+                    bb[h] = in[1];
+                    if (colors) kc[h] = in[2];
+                }
             }
             __syncthreads();
-            if (v < U) {
-                float4 cull, xyuv, rgba;
-                vertex_record<false>(ms, a, bb, kc, cull, xyuv, rgba);
-                float4* out = reinterpret_cast<float4*>(rec + (size_t)kRecBytes * v);
-                out[0] = xyuv;
-                out[1] = rgba;
-                out[2] = make_float4(cull.w, pcorrect ? corner_invw(ms, a) : 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint32_t v = v0 + h * blockDim.x + threadIdx.x;
+                if (v < U) {
+                    float4 cull, xyuv, rgba;
+                    vertex_record<false>(ms, a[h], bb[h], kc[h], cull, xyuv, rgba);
+                    float4* out = reinterpret_cast<float4*>(rec + (size_t)kRecBytes * v);
+                    out[0] = xyuv;
+                    out[1] = rgba;
+                    out[2] = make_float4(cull.w, pcorrect ? corner_invw(ms, a[h]) : 0.f, 0.f, 0.f);
+                }
             }
         }
         if (threadIdx.x == 0) {
