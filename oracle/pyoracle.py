@@ -133,13 +133,22 @@ class Renderer:
         self.scene_data = scene_data  # the descriptor points into its arrays
         self.sd = scene_data.desc()
         self.cam = cam
-        dt = np.float64 if f64 else np.float32
-        nseg_max = sum(len(scene_data.meshes[int(m)].parts) for m in scene_data.mv["mesh"]) + 1
-        slots = max(1, scene_data.total_tris())
+        self.dt = np.float64 if f64 else np.float32
+        self.nseg_max = sum(len(scene_data.meshes[int(m)].parts) for m in scene_data.mv["mesh"]) + 1
+        self.mask = None
+        if light_mask is not None:
+            self._m = (C.c_uint64 * 2)(light_mask & ((1 << 64) - 1), (light_mask >> 64) & ((1 << 64) - 1))
+            self.mask = C.cast(self._m, C.POINTER(C.c_uint64))
+        self.fn = self.lib.t3d_oracle_render_f64 if f64 else self.lib.t3d_oracle_render_f32
+        self._alloc(max(1, scene_data.total_tris()))
+
+    def _alloc(self, slots):
+        dt, nseg_max = self.dt, self.nseg_max
+        self.slots = slots
         self.count = np.zeros(nseg_max, np.uint32)
         self.arrays = [np.zeros(nseg_max, np.uint32) for _ in range(6)] + [np.zeros(slots, np.uint32)]
         self.out = [np.zeros((slots, 3, 4), dt), np.zeros((slots, 3, 4), dt), np.zeros((slots, 3), dt)]
-        self.custom0 = np.zeros((slots, 3), dt) if cam.perspective_corrected else None
+        self.custom0 = np.zeros((slots, 3), dt) if self.cam.perspective_corrected else None
         o = OracleOut()
         o.max_segments = nseg_max
         u = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
@@ -152,15 +161,14 @@ class Renderer:
         o.xyuv, o.rgba, o.depth = self.out[0].ctypes.data, self.out[1].ctypes.data, self.out[2].ctypes.data
         o.custom0 = self.custom0.ctypes.data if self.custom0 is not None else None
         self.o = o
-        self.mask = None
-        if light_mask is not None:
-            self._m = (C.c_uint64 * 2)(light_mask & ((1 << 64) - 1), (light_mask >> 64) & ((1 << 64) - 1))
-            self.mask = C.cast(self._m, C.POINTER(C.c_uint64))
-        self.fn = self.lib.t3d_oracle_render_f64 if f64 else self.lib.t3d_oracle_render_f32
 
     def render(self, animate_frames=0, threads=1):
         """Renders into the arrays; returns the visible triangles."""
         rc = self.fn(C.byref(self.sd), C.byref(self.cam), self.mask, animate_frames, threads, C.byref(self.o))
+        if rc != 0 and int(self.o.total_slots) > self.slots:
+            # auto-subdivided meshes list more triangles than the scene holds: grow once, render again
+            self._alloc(int(self.o.total_slots))
+            rc = self.fn(C.byref(self.sd), C.byref(self.cam), self.mask, animate_frames, threads, C.byref(self.o))
         if rc != 0:
             raise RuntimeError(f"oracle render failed: {rc}")
         return int(self.count[:self.o.num_segments].sum())

@@ -82,3 +82,17 @@ def test_subdivision_scene_draws_levels():
         if sd.meshes[m].auto_subdivide:
             counts[s["model"]] = counts.get(s["model"], 0) + s["count"]
     assert any(c > plain_caps[int(sd.mv["mesh"][k])] for k, c in counts.items())
+
+
+def test_timing_renderer_counts_like_render():
+    """pyoracle.Renderer, the CPU arms' timing path (output arrays allocated once and reused),
+    counts the visible triangles render() does, also for auto-subdivided meshes, which list more
+    triangles than the scene holds (its arrays grow once), and on repeated calls."""
+    from tetra3d_gb300 import scenes
+    for sd, cam in ((scenes.uv_sphere_scene(1), None), (scenes.subdivision_scene(10), scenes.feature_camera("persp"))):
+        cam = cam or sd.camera
+        r = pyoracle.Renderer(sd, cam)
+        want = pyoracle.render(sd, cam).visible_tris
+        assert want > 0
+        assert r.render() == want
+        assert r.render(threads=2) == want
