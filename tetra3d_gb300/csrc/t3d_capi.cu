@@ -334,6 +334,7 @@ int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, con
                        cudaMemcpyHostToDevice));
         int rc;
         if ((rc = bake_shapes(ctx, sc, mesh))) return rc;  // the mesh's keyed streams for the new weights
+        if ((rc = fill_keyed_meshlets(ctx, sc, mesh))) return rc;  // and its meshlets' vertex data
         CKR(cudaStreamSynchronize(ctx->stream));
     }
     return T3D_OK;

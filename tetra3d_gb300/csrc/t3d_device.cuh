@@ -162,6 +162,10 @@ struct DevJob {
 __host__ __device__ inline uint32_t mlet_slots4(uint32_t nu) { return (nu + 3u) & ~3u; }
 __host__ __device__ inline uint32_t mlet_lidx_bytes(uint32_t nt) { return (6u * nt + 15u) & ~15u; }
 __host__ __device__ inline uint32_t mlet_aos_stride(bool colors) { return colors ? 48u : 32u; }
+// A shape-keyed mesh's meshlet as the refill kernel reads it (same fields as the host's MletFill).
+struct MletFillDev {
+    uint32_t off16, nt, nu, vmap_off;
+};
 __host__ __device__ inline uint64_t mlet_bytes(uint32_t nt, uint32_t nu, bool colors) {
     return (uint64_t)mlet_lidx_bytes(nt) + (12ull + mlet_aos_stride(colors)) * mlet_slots4(nu);
 }

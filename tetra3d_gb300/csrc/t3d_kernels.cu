@@ -2394,6 +2394,31 @@ extern "C" const void* t3d_phase_kernel_ptr(int mesh, int k) {
     return mesh ? t3d::phase_kernel_ptr<1>(k) : t3d::phase_kernel_ptr<0>(k);
 }
 extern "C" int t3d_phase_kernel_blocks(int mesh, int k) { return (k >= 0 && k < 6) ? t3d::kPhaseBlocks[mesh ? 1 : 0][k] : 0; }
+// The vertex data of a shape-keyed mesh's meshlets from its keyed streams (one block per
+// meshlet, one thread per slot): positions and the interleaved records' position, normal and
+// UV (a mesh's colours are not keyed, so the colour part stays as cut).
+__global__ void k_fill_keyed(unsigned char* __restrict__ pool, const t3d::MletFillDev* __restrict__ fills,
+                             const uint32_t* __restrict__ vmap, const float4* __restrict__ va, const float4* __restrict__ vb,
+                             uint32_t colors) {
+    const t3d::MletFillDev f = fills[blockIdx.x];
+    float* pos = reinterpret_cast<float*>(pool + 16ull * f.off16 + t3d::mlet_lidx_bytes(f.nt));
+    const uint32_t U4 = t3d::mlet_slots4(f.nu), af = t3d::mlet_aos_stride(colors != 0) / 4;
+    float* aos = pos + 3ull * U4;
+    for (uint32_t s = threadIdx.x; s < f.nu; s += blockDim.x) {
+        const uint32_t v = vmap[f.vmap_off + s];
+        const float4 a = va[v], b = vb[v];
+        pos[3 * s] = a.x; pos[3 * s + 1] = a.y; pos[3 * s + 2] = a.z;
+        float* r = aos + (size_t)af * s;
+        r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+        r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+    }
+}
+extern "C" cudaError_t t3d_fill_keyed(cudaStream_t st, unsigned char* pool, const void* fills, uint32_t nfills,
+                                      const uint32_t* vmap, const float4* va, const float4* vb, uint32_t colors) {
+    if (nfills == 0) return cudaSuccess;
+    k_fill_keyed<<<nfills, 256, 0, st>>>(pool, (const t3d::MletFillDev*)fills, vmap, va, vb, colors);
+    return cudaGetLastError();
+}
 // The keyed streams of one mesh (k_bake_shapes) on stream st.
 extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
                                        const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,

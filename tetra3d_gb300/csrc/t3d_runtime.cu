@@ -27,6 +27,8 @@
 extern "C" const void* t3d_frame_kernel_ptr();
 extern "C" const void* t3d_frame_kernel_mesh_ptr();
 extern "C" const void* t3d_phase_kernel_ptr(int mesh, int k);
+extern "C" cudaError_t t3d_fill_keyed(cudaStream_t st, unsigned char* pool, const void* fills, uint32_t nfills,
+                                      const uint32_t* vmap, const float4* va, const float4* vb, uint32_t colors);
 extern "C" cudaError_t t3d_bake_shapes(cudaStream_t st, const float4* va, const float4* vb, const float4* sa,
                                        const float2* sb, const float* sw, uint32_t nverts, uint32_t nkeys, float4* oa,
                                        float4* ob);
@@ -548,20 +550,27 @@ static void fill_meshlet(const Meshlet& ml, const uint32_t* idx, const float4* v
 
 // Cuts every part of the scene's meshes into meshlets for a triangle budget T
 // and a vertex budget U and stores them in the scene's meshlet pool, from the
-// resident vertex and index streams. Meshes with shape keys (their keyed
-// streams change with the weights) and auto-subdivided meshes get none: their
-// pairs take the per-vertex record path.
+// resident vertex and index streams. Meshes with shape keys are cut from their
+// keyed streams (baked for the current weights), and each of their meshlets keeps
+// its slot -> vertex map so that fill_keyed_meshlets refills it when the weights
+// change. Auto-subdivided meshes get none: their pairs take the per-vertex record
+// path.
 int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U) {
     sc->mlet.release();
+    sc->mlet_kfill.release();
+    sc->mlet_vmap.release();
     sc->mlet_T = sc->mlet_U = 0;
-    for (SceneMesh& me : sc->meshes) me.mparts.assign(me.parts.size(), {});
+    for (SceneMesh& me : sc->meshes) {
+        me.mparts.assign(me.parts.size(), {});
+        me.kfill_first = me.kfill_count = 0;
+    }
     if (U < 3 || U > 65535u) return T3D_OK;
     std::vector<uint32_t> stamp, slot, verts, idx;
     uint32_t gen = 0;
     uint64_t total16 = 0;
     // pass 1: the cuts and their offsets
     for (SceneMesh& me : sc->meshes) {
-        if (me.nkeys || me.subdiv || me.ntris == 0) continue;
+        if (me.subdiv || me.ntris == 0) continue;
         idx.resize(3ull * me.ntris);
         CK(cudaMemcpy(idx.data(), (const uint32_t*)sc->idx.ptr + 3ull * me.tbase, 12ull * me.ntris, cudaMemcpyDeviceToHost));
         stamp.assign(me.nverts, 0u);
@@ -586,9 +595,11 @@ int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U) {
     }
     int rc;
     if ((rc = sc->mlet.ensure(ctx, 16ull * total16))) return rc;
-    // pass 2: the data, one mesh at a time
+    // pass 2: the data, one mesh at a time (shape-keyed meshes from their keyed streams)
     std::vector<float4> va, vb, vc;
     std::vector<unsigned char> data;
+    std::vector<MletFill> kfill;
+    std::vector<uint32_t> vmap;
     for (SceneMesh& me : sc->meshes) {
         bool any = false;
         for (const auto& v : me.mparts) any |= !v.empty();
@@ -596,8 +607,10 @@ int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U) {
         idx.resize(3ull * me.ntris);
         va.resize(me.nverts); vb.resize(me.nverts); vc.resize(me.nverts);
         CK(cudaMemcpy(idx.data(), (const uint32_t*)sc->idx.ptr + 3ull * me.tbase, 12ull * me.ntris, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(va.data(), (const float4*)sc->va.ptr + me.vbase, 16ull * me.nverts, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(vb.data(), (const float4*)sc->vb.ptr + me.vbase, 16ull * me.nverts, cudaMemcpyDeviceToHost));
+        const float4* sa = me.nkeys ? (const float4*)sc->vaS.ptr + me.sbase : (const float4*)sc->va.ptr + me.vbase;
+        const float4* sb = me.nkeys ? (const float4*)sc->vbS.ptr + me.sbase : (const float4*)sc->vb.ptr + me.vbase;
+        CK(cudaMemcpy(va.data(), sa, 16ull * me.nverts, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(vb.data(), sb, 16ull * me.nverts, cudaMemcpyDeviceToHost));
         if (me.colors) CK(cudaMemcpy(vc.data(), (const float4*)sc->vc.ptr + me.vbase, 16ull * me.nverts, cudaMemcpyDeviceToHost));
         stamp.assign(me.nverts, 0u);
         slot.assign(me.nverts, 0u);
@@ -609,14 +622,43 @@ int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U) {
                 hi = std::max<uint64_t>(hi, ml.off16 + mlet_bytes(ml.nt, ml.nu, me.colors) / 16);
             }
         data.assign(16 * (hi - lo), 0);
+        if (me.nkeys) me.kfill_first = (uint32_t)kfill.size();
         for (const auto& v : me.mparts)
-            for (const Meshlet& ml : v)
+            for (const Meshlet& ml : v) {
                 fill_meshlet(ml, idx.data(), va.data(), vb.data(), vc.data(), me.colors, stamp, slot, gen, verts,
                              data.data() + 16 * (ml.off16 - lo));
+                if (me.nkeys) {  // the meshlet's slot -> vertex map, for refills
+                    kfill.push_back({ml.off16, ml.nt, ml.nu, (uint32_t)vmap.size()});
+                    vmap.insert(vmap.end(), verts.begin(), verts.end());
+                }
+            }
+        if (me.nkeys) me.kfill_count = (uint32_t)kfill.size() - me.kfill_first;
         CK(cudaMemcpy((unsigned char*)sc->mlet.ptr + 16 * lo, data.data(), data.size(), cudaMemcpyHostToDevice));
+    }
+    if (!kfill.empty()) {
+        if ((rc = sc->mlet_kfill.ensure(ctx, sizeof(MletFill) * kfill.size())) ||
+            (rc = sc->mlet_vmap.ensure(ctx, 4ull * std::max<size_t>(1, vmap.size()))))
+            return rc;
+        CK(cudaMemcpy(sc->mlet_kfill.ptr, kfill.data(), sizeof(MletFill) * kfill.size(), cudaMemcpyHostToDevice));
+        if (!vmap.empty()) CK(cudaMemcpy(sc->mlet_vmap.ptr, vmap.data(), 4ull * vmap.size(), cudaMemcpyHostToDevice));
     }
     sc->mlet_T = T;
     sc->mlet_U = U;
+    return T3D_OK;
+}
+
+// Refills the meshlets of shape-keyed mesh m from its keyed streams (after a bake for new weights).
+int fill_keyed_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t m) {
+    const SceneMesh& me = sc->meshes[m];
+    if (!me.kfill_count || !sc->mlet.ptr) return T3D_OK;
+    const cudaError_t e = t3d_fill_keyed(ctx->stream, (unsigned char*)sc->mlet.ptr,
+                                         (const MletFill*)sc->mlet_kfill.ptr + me.kfill_first, me.kfill_count,
+                                         (const uint32_t*)sc->mlet_vmap.ptr, (const float4*)sc->vaS.ptr + me.sbase,
+                                         (const float4*)sc->vbS.ptr + me.sbase, me.colors ? 1u : 0u);
+    if (e != cudaSuccess) {
+        set_err(ctx, "keyed meshlet refill: %s", cudaGetErrorString(e));
+        return T3D_E_CUDA;
+    }
     return T3D_OK;
 }
 
@@ -1287,7 +1329,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             if (flags & (SEG_ALTERED | SEG_ALT_TILES)) F.any_altered = true;
             // pairs that need no more than the plain vertex loop take their part's meshlets
             const std::vector<Meshlet>* mls = nullptr;
-            if (mlet_ok && !(flags & (SEG_ALTERED | SEG_ALT_TILES | SEG_SHAPES | SEG_SKIP)) &&
+            if (mlet_ok && !(flags & (SEG_ALTERED | SEG_ALT_TILES | SEG_SKIP)) &&
                 rp.part < me.mparts.size() && !me.mparts[rp.part].empty())
                 mls = &me.mparts[rp.part];
             if (mls) { flags |= SEG_MESHLET; F.any_mesh = true; }

@@ -40,6 +40,12 @@ struct ScenePart {
 struct Meshlet {
     uint32_t t0, nt, nu, off16;
 };
+// A meshlet of a shape-keyed mesh, for refilling its vertex data from the keyed streams when
+// the weights change: its place in the pool (16-byte units), triangles, slots, and where its
+// slot -> mesh vertex map starts.
+struct MletFill {
+    uint32_t off16, nt, nu, vmap_off;
+};
 struct SceneMesh {
     uint32_t vbase = 0, tbase = 0, nverts = 0, ntris = 0;
     bool colors = false;
@@ -53,6 +59,7 @@ struct SceneMesh {
     uint32_t max_joint = 0;
     bool subdiv = false;  // auto-subdivided: parts list each triangle followed by its subdivision levels
     std::vector<std::vector<Meshlet>> mparts;  // per part: its meshlets (empty: the part has none)
+    uint32_t kfill_first = 0, kfill_count = 0;  // shape-keyed mesh: its MletFill records in the scene's list
 };
 struct SceneModel {
     t3d_model_desc d;  // host mirror (rotation advanced with every animated frame)
@@ -72,6 +79,7 @@ struct Scene {
     bool joint8 = false;  // vjoint holds four 8-bit joints per vertex (every joint below 256)
     DevBuf sub_info, sub_rel, sub_levels, cell_use_off, cell_use_items;
     DevBuf mlet;                         // meshlet pool
+    DevBuf mlet_kfill, mlet_vmap;        // shape-keyed meshes' meshlets: MletFill records, slot -> vertex maps
     uint32_t mlet_T = 0, mlet_U = 0;     // triangle and vertex budgets the meshlets were cut for (0: none)
     std::vector<char> light_uses;    // per light: a volume whose cells use lights
     std::vector<char> light_nested;  // per light: used by some cell (cannot become a volume)
@@ -83,10 +91,10 @@ struct Scene {
     uint64_t device_bytes() const {
         return va.cap + vb.cap + vc.cap + idx.cap + centers.cap + dmeshes.cap + dmodels.cap + cells.cap + shape_a.cap + vaS.cap + vbS.cap +
                shape_b.cap + shape_w.cap + vjoint.cap + vweight.cap + bones.cap + sub_info.cap + sub_rel.cap +
-               sub_levels.cap + cell_use_off.cap + cell_use_items.cap + mlet.cap;
+               sub_levels.cap + cell_use_off.cap + cell_use_items.cap + mlet.cap + mlet_kfill.cap + mlet_vmap.cap;
     }
     void release() {
-        mlet.release(); mlet_T = mlet_U = 0;
+        mlet.release(); mlet_kfill.release(); mlet_vmap.release(); mlet_T = mlet_U = 0;
         sub_info.release(); sub_rel.release(); sub_levels.release(); cell_use_off.release(); cell_use_items.release();
         shape_a.release(); shape_b.release(); vaS.release(); vbS.release(); shape_w.release(); vjoint.release(); vweight.release(); bones.release();
         va.release(); vb.release(); vc.release(); idx.release(); centers.release();
@@ -211,4 +219,5 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st);
 int configure(t3d_ctx* ctx);
 int bake_shapes(t3d_ctx* ctx, Scene* sc, uint32_t mesh);
 int build_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t T, uint32_t U);
+int fill_keyed_meshlets(t3d_ctx* ctx, Scene* sc, uint32_t m);
 }  // namespace t3d
