@@ -2181,10 +2181,13 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
         ok = mbar_wait(&H.bar[1], ph1, P.ctl, limit) && ok;
         ph1 ^= 1u;
         __syncthreads();  // the constants are in place
-        // every slot's emitted corner, in place: a round of two slots per thread reads its
-        // inputs, then (after a barrier) writes its records; a record covers only input bytes of
-        // its own or earlier slots, all read by the end of the round
-        for (uint32_t v0 = 0; v0 < U; v0 += 2 * blockDim.x) {
+        // a tile with fewer visible corners than slots computes each corner where it is written
+        // (from the vertex block, same function, same bits); the others compute every slot's
+        // emitted corner once, in place: a round of two slots per thread reads its inputs, then
+        // (after a barrier) writes its records; a record covers only input bytes of its own or
+        // earlier slots, all read by the end of the round
+        const bool sparse = 3u * n < U;
+        for (uint32_t v0 = 0; !sparse && v0 < U; v0 += 2 * blockDim.x) {
             float4 a[2], bb[2], kc[2];
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -2228,7 +2231,22 @@ __device__ __noinline__ void phase_rank_meshlet(const FrameParams& P, unsigned c
             float4* __restrict__ oxyuv = P.out_xyuv + 3 * (size_t)td.out_base;
             float4* __restrict__ orgba = P.out_rgba + 3 * (size_t)td.out_base;
             float* __restrict__ odepth = P.out_depth + 3 * (size_t)td.out_base;
-            for (uint32_t q = threadIdx.x; q < 3 * n; q += blockDim.x) {  // one corner per thread, output order
+            for (uint32_t q = threadIdx.x; sparse && q < 3 * n; q += blockDim.x) {  // corners computed here
+                const uint32_t r = q / 3u, cc = q - 3u * r;
+                const uint32_t w = rk[r];
+                const uint32_t j = w & 2047u, bn = (w >> 11) & 511u;
+                const uint32_t pos = single ? r : hist[bn] + (w >> 20);
+                const float4* in = reinterpret_cast<const float4*>(vin + (size_t)as * vloc[3 * j + cc]);
+                const float4 a = in[0], b = in[1];
+                const float4 kc = colors ? in[2] : make_float4(0.f, 0.f, 0.f, 0.f);
+                float4 cull, xyuv, rgba;
+                vertex_record<false>(ms, a, b, kc, cull, xyuv, rgba);
+                oxyuv[3 * pos + cc] = xyuv;
+                orgba[3 * pos + cc] = rgba;
+                odepth[3 * pos + cc] = cull.w;
+                if (pcorrect) P.out_invw[3 * ((size_t)td.out_base + pos) + cc] = corner_invw(ms, a);
+            }
+            for (uint32_t q = threadIdx.x; !sparse && q < 3 * n; q += blockDim.x) {  // one corner per thread, output order
                 const uint32_t r = q / 3u, cc = q - 3u * r;
                 const uint32_t w = rk[r];
                 const uint32_t j = w & 2047u, bn = (w >> 11) & 511u;
