@@ -143,8 +143,8 @@ int t3d_destroy(t3d_ctx* ctx) {
     for (auto& kv : ctx->scenes) kv.second->release();
     ctx->scenes.clear();
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
-                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax,
-                      &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights,
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist,
+                      &ctx->chunk_hist, &ctx->seg_minmax, &ctx->seg_count, &ctx->out_xyuv, &ctx->out_rgba, &ctx->out_depth, &ctx->accum, &ctx->inst_lights,
                       &ctx->job_bytes, &ctx->vis_rank, &ctx->vinvw, &ctx->out_invw, &ctx->live_tiles})
         b->release();
     cudaStreamSynchronize(ctx->stream);  // stream-ordered frees of a pooled context have run
@@ -508,8 +508,8 @@ int t3d_frame_sync(t3d_ctx* ctx, t3d_stats* stats_out) {
     s.launches = ctx->launches;
     size_t scratch = 0;
     for (DevBuf* b : {&ctx->table_dev, &ctx->ctl, &ctx->preps, &ctx->vcull, &ctx->valt, &ctx->vxyuv, &ctx->vrgba,
-                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist, &ctx->seg_minmax, &ctx->seg_count,
-                      &ctx->inst_lights, &ctx->vis_rank, &ctx->vinvw})
+                      &ctx->vis_idx, &ctx->vis_depth, &ctx->vis_vloc, &ctx->tile_count, &ctx->tile_wcnt, &ctx->tile_hist,
+                      &ctx->chunk_hist, &ctx->seg_minmax, &ctx->seg_count, &ctx->inst_lights, &ctx->vis_rank, &ctx->vinvw})
         scratch += b->cap;
     s.scratch_bytes = scratch;
     s.h2d_bytes = ctx->last_h2d;

@@ -220,6 +220,12 @@ struct TileDesc {
     uint32_t pad1;
 };
 constexpr uint32_t kChunkTris = 256;    // triangles per entry of a mesh's vertex-range table
+// A pair of more than kScanSplit tiles has its cross-tile scan split into chunks of kScanChunk
+// tiles (one scan work item each), the chunks' bin counts summed by the histogram phase. Pairs
+// of fewer tiles keep one item: there the chunk sums cost more than the shorter walk saves.
+constexpr uint32_t kScanChunk = 32;
+constexpr uint32_t kScanSplit = 64;
+constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
 
 // Launch control block (zeroed before every launch).
 struct Ctl {
@@ -305,6 +311,16 @@ struct FrameParams {
     // order the triangle phase finished them, from index mt_mesh_begin (Ctl.live of them); the
     // histogram and emit phases take only these. Null: every tile of the range.
     uint32_t* live_tiles;
+    // scan work items: per item (segment, first chunk, chunk, chunks); a pair of at most
+    // kScanChunk tiles is one item of one chunk (first chunk kNoChunk). Null: one item per
+    // segment of mt_segs.
+    const uint4* mt_scan;
+    // per multi-tile tile: its scan chunk (kNoChunk for pairs of one chunk); null: none
+    const uint32_t* mt_chunk;
+    // per chunk, kBins counts: the sum of its tiles' histograms (zeroed by the prep phase over
+    // chunks [chunk_zero_begin, chunk_zero_end))
+    uint32_t* chunk_hist;
+    uint32_t chunk_zero_begin, chunk_zero_end;
 };
 // Dense visible list of a meshlet tile i: depth keys at vis_depth + i * tile_tris,
 // 3 slots per entry at vis_vloc + 3 * i * tile_tris, tile_count[i] entries.

@@ -238,6 +238,12 @@ template <int kV>
 __device__ __noinline__ void phase_prep(const FrameParams& P) {
     const uint32_t n = P.inst_end - P.inst_begin;
     const uint32_t stride = gridDim.x * blockDim.x;
+    {  // the scan chunks' counts start from zero (the histogram phase adds to them)
+        uint4* z = reinterpret_cast<uint4*>(P.chunk_hist + (size_t)P.chunk_zero_begin * kBins);
+        const size_t nz = (size_t)(P.chunk_zero_end - P.chunk_zero_begin) * (kBins / 4);
+        for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nz; q += stride)
+            z[q] = make_uint4(0u, 0u, 0u, 0u);
+    }
     // model k runs on block k % grid: the serial per-model chains spread over every SM
     for (uint32_t k = blockIdx.x + gridDim.x * threadIdx.x; k < n; k += stride) {
         const uint32_t i = P.inst_begin + k;
@@ -1487,6 +1493,8 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
     const uint32_t lane = threadIdx.x & 31, T = P.tile_tris;
     const uint32_t n = __ldcg(&P.tile_count[i]);
     const uint32_t s = td.seg;
+    // the tile's scan chunk, read now so its latency hides behind the ranking
+    const uint32_t ch = (P.mt_chunk && !(td.flags & SEG_SINGLE)) ? __ldg(&P.mt_chunk[i]) : kNoChunk;
     for (uint32_t b = lane; b < kBinsPadded; b += 32) cnt[b] = 0u;
     const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
     const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
@@ -1528,7 +1536,11 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
     }
     if (!(td.flags & SEG_SINGLE)) {
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
-        for (uint32_t b = lane; b < kBins; b += 32) out[b] = cnt[pad_bin(b)];
+        for (uint32_t b = lane; b < kBins; b += 32) {
+            const uint32_t c = cnt[pad_bin(b)];
+            out[b] = c;
+            if (ch != kNoChunk && c) atomicAdd(&P.chunk_hist[(size_t)ch * kBins + b], c);
+        }
     }
     // exclusive scan in walk order: lane l owns walk positions [16 l, 16 l + 16)
     {
@@ -1591,6 +1603,7 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
             continue;
         }
         const uint32_t n = __ldcg(&P.tile_count[i]);
+        const uint32_t ch = P.mt_chunk ? __ldg(&P.mt_chunk[i]) : kNoChunk;  // read early: used at the end
         for (uint32_t b = lane; b < kBins; b += 32) wh[b] = 0u;
         __syncwarp();
         if (n > 0) {
@@ -1614,7 +1627,11 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         }
         __syncwarp();
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
-        for (uint32_t b = lane; b < kBins; b += 32) out[b] = wh[b];
+        for (uint32_t b = lane; b < kBins; b += 32) {
+            const uint32_t c = wh[b];
+            out[b] = c;
+            if (ch != kNoChunk && c) atomicAdd(&P.chunk_hist[(size_t)ch * kBins + b], c);
+        }
         __syncwarp();
         uint32_t nx = 0;
         if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
@@ -1622,7 +1639,10 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
     }
 }
 
-// P3: per multi-tile segment, turn tile histograms into per-tile bin bases.
+// P3: per multi-tile segment, turn tile histograms into per-tile bin bases. A pair of
+// several scan chunks (more than kScanSplit tiles) is several work items, one per chunk: each takes the pair's bin
+// totals and the counts of the chunks before its own from the chunk sums, then runs
+// through its own chunk's tiles.
 template <int kV>
 __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* smem) {
     const SmemLayout L = smem_layout(smem, P.tile_tris);
@@ -1630,9 +1650,54 @@ __device__ __noinline__ void phase_scan(const FrameParams& P, unsigned char* sme
     for (;;) {
         const uint32_t k = P.mt_seg_begin + next_item(P.ctl, 3, &sm.item);
         if (k >= P.mt_seg_end) break;
-        const uint32_t s = P.mt_segs[k];
+        const uint4 it = P.mt_scan ? P.mt_scan[k] : make_uint4(P.mt_segs[k], kNoChunk, 0u, 1u);
+        const uint32_t s = it.x;
         const DevSeg seg = P.segs[s];
         const uint32_t sort_mode = seg_sort_mode(seg.flags);
+        if (it.w > 1) {
+            const uint32_t c = it.z, nc = it.w;
+            const uint32_t* chb = P.chunk_hist + (size_t)it.y * kBins;
+            uint32_t* pre = L.whist;  // per bin: the counts of the chunks before this one
+            for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
+                uint32_t tot = 0, pb = 0, q = 0;
+                for (; q + 8 <= nc; q += 8) {
+                    uint32_t v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; u++) v[u] = __ldcg(&chb[(size_t)(q + u) * kBins + b]);
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        if (q + u == c) pb = tot;
+                        tot += v[u];
+                    }
+                }
+                for (; q < nc; q++) {
+                    if (q == c) pb = tot;
+                    tot += __ldcg(&chb[(size_t)q * kBins + b]);
+                }
+                pre[b] = pb;
+                sm.bins_walk[walk_pos(b, sort_mode)] = tot;
+            }
+            scan_bins(sm, sm.bins_walk);
+            const uint32_t t0 = c * kScanChunk, nt = min(seg.ntiles, t0 + kScanChunk) - t0;
+            for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
+                uint32_t run = sm.bins_walk[walk_pos(b, sort_mode)] + pre[b];
+                uint32_t* h = P.tile_hist + (size_t)(seg.mt_first + t0) * kBins + b;
+                uint32_t t = 0;
+                for (; t + 8 <= nt; t += 8) {
+                    uint32_t v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; u++) v[u] = __ldcg(&h[(size_t)(t + u) * kBins]);
+#pragma unroll
+                    for (int u = 0; u < 8; u++) { h[(size_t)(t + u) * kBins] = run; run += v[u]; }
+                }
+                for (; t < nt; t++) {
+                    const uint32_t cnt = __ldcg(&h[(size_t)t * kBins]);
+                    h[(size_t)t * kBins] = run;
+                    run += cnt;
+                }
+            }
+            continue;
+        }
         const uint32_t* hbase = P.tile_hist + (size_t)seg.mt_first * kBins;
         for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) {
             uint32_t tot = 0;

@@ -1356,12 +1356,23 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             sg.tile_first = (uint32_t)F.tiles.size();
             sg.ntiles = ntiles;
             const uint32_t s = (uint32_t)F.segs.size();
+            // the pair's cross-tile scan: one work item, or one per chunk of kScanChunk tiles
+            uint32_t scan_first = 0xFFFFFFFFu, nchunk = 1, chunk_first = kNoChunk;
             if (ntiles > 1 || mls) {  // every meshlet pair takes the multi-tile route
                 flags |= SEG_MULTI;
                 sg.mt_first = (uint32_t)F.mt_desc.size();
                 if (mls && ntiles == 1) flags |= SEG_SINGLE;  // ranked alone: no cross-tile scan
-                else F.mt_segs.push_back(s);
+                else {
+                    scan_first = (uint32_t)F.mt_scan.size();
+                    if (ntiles > kScanSplit) {
+                        nchunk = (ntiles + kScanChunk - 1) / kScanChunk;
+                        chunk_first = F.nchunks;
+                        F.nchunks += nchunk;
+                    }
+                    for (uint32_t c = 0; c < nchunk; c++) F.mt_scan.push_back(make_uint4(s, chunk_first, c, nchunk));
+                }
             }
+            auto tile_chunk = [&](uint32_t t) { return chunk_first == kNoChunk ? kNoChunk : chunk_first + t / kScanChunk; };
             sg.flags = flags;
             if (mls) {
                 for (uint32_t t = 0; t < ntiles; t++) {
@@ -1379,6 +1390,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                     td.nearp = dj.cam.near_; td.farp = dj.cam.far_;
                     F.tiles.push_back(td);
                     F.mt_desc.push_back(td);
+                    F.mt_chunk.push_back(tile_chunk(t));
                 }
             }
             for (uint32_t t = 0; t < (mls ? 0u : ntiles); t++) {
@@ -1402,7 +1414,10 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                     if (hi >= lo) { td.vlo = sg.vscratch + (lo - sg.vmin); td.vhi = sg.vscratch + (hi - sg.vmin) + 1; }
                 }
                 F.tiles.push_back(td);
-                if (flags & SEG_MULTI) F.mt_desc.push_back(td);
+                if (flags & SEG_MULTI) {
+                    F.mt_desc.push_back(td);
+                    F.mt_chunk.push_back(tile_chunk(t));
+                }
             }
 
             sg.pad[0] = rp.draw | (rp.transparent << 31);  // flush and its pass, for the rasteriser
@@ -1418,8 +1433,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
             si.draw = rp.draw; si.draw_transparent = rp.transparent;
             F.seg_info.push_back(si);
-            F.seg_mt_seg.push_back((flags & SEG_MULTI) && !(flags & SEG_SINGLE) ? (uint32_t)F.mt_segs.size() - 1
-                                                                                  : 0xFFFFFFFFu);
+            F.seg_mt_seg.push_back(scan_first);  // the pair's first scan item (none: all ones)
         }
         F.job_seg_end.push_back((uint32_t)F.segs.size());
     }
@@ -1481,7 +1495,9 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
     F.vitem_chunk.swap(vch);
     // multi-tile numbers: the record path's first, then the meshlet pairs'
     std::vector<TileDesc> mt;
+    std::vector<uint32_t> mtc;  // their scan chunks, in the same order
     mt.reserve(F.mt_desc.size());
+    mtc.reserve(F.mt_chunk.size());
     for (int pass = 0; pass < 2; pass++) {
         for (uint32_t s = 0; s < nseg; s++) {
             DevSeg& sg = F.segs[s];
@@ -1492,12 +1508,14 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
                 td.mt = first + t;
                 F.tiles[sg.tile_first + t].mt = first + t;
                 mt.push_back(td);
+                mtc.push_back(F.mt_chunk[sg.mt_first + t]);
             }
             sg.mt_first = first;
         }
         if (pass == 0) F.mt_mesh = (uint32_t)mt.size();
     }
     F.mt_desc.swap(mt);
+    F.mt_chunk.swap(mtc);
 }
 
 template <typename T> static size_t bytes_of(const std::vector<T>& v) { return v.size() * sizeof(T); }
@@ -1522,7 +1540,8 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     size_t o_segs = add(F.segs.data(), bytes_of(F.segs));
     size_t o_ts = add(F.tiles.data(), bytes_of(F.tiles));
     size_t o_mtt = add(F.mt_desc.data(), bytes_of(F.mt_desc));
-    size_t o_mts = add(F.mt_segs.data(), bytes_of(F.mt_segs));
+    size_t o_mts = add(F.mt_scan.data(), bytes_of(F.mt_scan));
+    size_t o_mtc = add(F.mt_chunk.data(), bytes_of(F.mt_chunk));
     size_t o_vs = add(F.vitem_seg.data(), bytes_of(F.vitem_seg));
     size_t o_vc = add(F.vitem_chunk.data(), bytes_of(F.vitem_chunk));
 
@@ -1554,7 +1573,9 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.segs = (const DevSeg*)(db + o_segs);
     P.tiles = (const TileDesc*)(db + o_ts);
     P.mt_desc = (const TileDesc*)(db + o_mtt);
-    P.mt_segs = (const uint32_t*)(db + o_mts);
+    P.mt_segs = nullptr;
+    P.mt_scan = (const uint4*)(db + o_mts);
+    P.mt_chunk = (const uint32_t*)(db + o_mtc);
     P.vitem_seg = (const uint32_t*)(db + o_vs);
     P.vitem_chunk = (const uint32_t*)(db + o_vc);
 
@@ -1571,7 +1592,9 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
         (rc = ctx->vis_depth.ensure(ctx, 4ull * nmt * ctx->tile_tris)) ||
         (rc = ctx->vis_vloc.ensure(ctx, 6ull * nmt * ctx->tile_tris)) || (rc = ctx->tile_count.ensure(ctx, 4 * nmt)) ||
         (rc = ctx->tile_wcnt.ensure(ctx, 4ull * kMaxWarps * nmt)) ||
-        (rc = ctx->tile_hist.ensure(ctx, 4ull * kBins * nmt)) || (rc = ctx->seg_minmax.ensure(ctx, 8 * nseg)) ||
+        (rc = ctx->tile_hist.ensure(ctx, 4ull * kBins * nmt)) ||
+        (rc = ctx->chunk_hist.ensure(ctx, 4ull * kBins * std::max<uint32_t>(1u, F.nchunks))) ||
+        (rc = ctx->seg_minmax.ensure(ctx, 8 * nseg)) ||
         (rc = ctx->seg_count.ensure(ctx, 4 * nseg)) || (rc = ctx->out_xyuv.ensure(ctx, 48 * nslots)) ||
         (rc = ctx->out_rgba.ensure(ctx, 48 * nslots)) || (rc = ctx->out_depth.ensure(ctx, 12 * nslots)))
         return rc;
@@ -1610,6 +1633,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.tile_wcnt = (uint32_t*)ctx->tile_wcnt.ptr;
     P.tile_count = (uint32_t*)ctx->tile_count.ptr;
     P.tile_hist = (uint32_t*)ctx->tile_hist.ptr;
+    P.chunk_hist = (uint32_t*)ctx->chunk_hist.ptr;
     P.seg_minmax = (uint32_t*)ctx->seg_minmax.ptr;
     P.seg_count = (uint32_t*)ctx->seg_count.ptr;
     P.out_xyuv = (float4*)ctx->out_xyuv.ptr;
@@ -1688,7 +1712,8 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         P.mesh_begin = F.tile_mesh; P.mesh_end = (uint32_t)F.tiles.size();
         P.mt_tile_begin = 0; P.mt_tile_end = F.mt_mesh;
         P.mt_mesh_begin = F.mt_mesh; P.mt_mesh_end = (uint32_t)F.mt_desc.size();
-        P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_segs.size();
+        P.mt_seg_begin = 0; P.mt_seg_end = (uint32_t)F.mt_scan.size();
+        P.chunk_zero_begin = 0; P.chunk_zero_end = F.nchunks;
 
         P.vitem_begin = 0; P.vitem_end = (uint32_t)F.vitem_seg.size();
         P.tile_alt = F.tile_alt; P.vitem_alt = F.vitem_alt;
@@ -1706,7 +1731,7 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
                                     {2u, (uint32_t)F.vitem_seg.size()},
                                     {4u, (uint32_t)F.tiles.size()},
                                     {8u, (nmt + warps - 1) / warps},
-                                    {16u, (uint32_t)F.mt_segs.size()},
+                                    {16u, (uint32_t)F.mt_scan.size()},
                                     {32u, nmt}};
         for (const auto& q : seq) {
             if (q[1] == 0 || (q[0] >= 8u && !P.has_multi)) continue;
@@ -1745,7 +1770,12 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         if (sg.flags & SEG_MULTI) {
             if (mesh) { P.mt_mesh_begin = sg.mt_first; P.mt_mesh_end = sg.mt_first + sg.ntiles; }
             else { P.mt_tile_begin = sg.mt_first; P.mt_tile_end = sg.mt_first + sg.ntiles; }
-            if (!(sg.flags & SEG_SINGLE)) { P.mt_seg_begin = F.seg_mt_seg[s]; P.mt_seg_end = F.seg_mt_seg[s] + 1; }
+            if (!(sg.flags & SEG_SINGLE)) {  // the pair's scan items, and its chunks' counts zeroed by its prep
+                const uint4 it = F.mt_scan[F.seg_mt_seg[s]];
+                P.mt_seg_begin = F.seg_mt_seg[s];
+                P.mt_seg_end = P.mt_seg_begin + it.w;
+                if (it.w > 1) { P.chunk_zero_begin = it.y; P.chunk_zero_end = it.y + it.w; }
+            }
             P.has_multi = 1;
         }
         // animation must be applied once: host tables carry the flag on the instance,
@@ -1762,7 +1792,8 @@ int launch_frame(t3d_ctx* ctx, int mode, cudaStream_t st) {
         }
         const uint32_t vitems = P.vitem_end - P.vitem_begin;
         const bool scan = P.mt_seg_begin < P.mt_seg_end;
-        const uint32_t seq[6][2] = {{1u, 1u}, {2u, vitems}, {4u, sg.ntiles}, {8u, sg.ntiles}, {16u, 1u}, {32u, sg.ntiles}};
+        const uint32_t seq[6][2] = {{1u, 1u}, {2u, vitems}, {4u, sg.ntiles}, {8u, sg.ntiles},
+                                    {16u, P.mt_seg_end - P.mt_seg_begin}, {32u, sg.ntiles}};
         for (const auto& q : seq) {
             if ((q[0] == 2u && vitems == 0) || (q[0] >= 8u && !P.has_multi) || (q[0] == 16u && !scan)) continue;
             P.phases = q[0];

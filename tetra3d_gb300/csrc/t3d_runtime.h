@@ -114,7 +114,11 @@ struct FrameTables {
     std::vector<t3d_segment_info> seg_info;
     std::vector<uint32_t> seg_mt_seg;
     std::vector<TileDesc> tiles, mt_desc;
-    std::vector<uint32_t> mt_segs;
+    // cross-tile scan work items (segment, first chunk, chunk, chunks) and each multi-tile
+    // tile's scan chunk (kNoChunk in pairs of one chunk); chunks numbered [0, nchunks)
+    std::vector<uint4> mt_scan;
+    std::vector<uint32_t> mt_chunk;
+    uint32_t nchunks = 0;
     std::vector<uint32_t> vitem_seg, vitem_chunk, seg_vitem_first;
     uint64_t nscratch = 0, nslots = 0;
     bool any_skinned = false, any_altered = false, any_mesh = false;
@@ -125,7 +129,7 @@ struct FrameTables {
     void clear() {
         jobs.clear(); job_scene.clear(); job_light_base.clear(); job_seg_end.clear(); lights.clear();
         insts.clear(); inst_light_idx.clear(); segs.clear(); seg_info.clear();
-        seg_mt_seg.clear(); tiles.clear(); mt_desc.clear(); mt_segs.clear();
+        seg_mt_seg.clear(); tiles.clear(); mt_desc.clear(); mt_scan.clear(); mt_chunk.clear(); nchunks = 0;
         vitem_seg.clear(); vitem_chunk.clear(); seg_vitem_first.clear();
         nscratch = 0; nslots = 0; any_skinned = false; any_altered = false; any_mesh = false; any_pcorrect = false;
         tile_alt = 0; vitem_alt = 0;
@@ -189,7 +193,7 @@ struct t3d_ctx {
     uint32_t grid_share = 1;      // serving slots: launches use 1/grid_share of the co-resident blocks
     cudaMemPool_t pool = nullptr; // serving slots: the server's pool for stream-ordered buffer growth
     t3d::DevBuf table_dev, ctl, preps, vcull, vxyuv, vrgba, vis_idx, vis_depth, vis_vloc, tile_count, tile_wcnt, tile_hist,
-        seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
+        chunk_hist, seg_minmax, seg_count, out_xyuv, out_rgba, out_depth, accum;
     uint32_t nctl = 0;
     uint64_t last_h2d = 0;
     uint32_t launches = 0;
