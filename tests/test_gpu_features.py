@@ -4,6 +4,7 @@ forms; several jobs with light masks in one launch; animation inside the launch 
 through CUDA graph replay; transform read-back; serving (same bits alone and in a
 mix); argument errors."""
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -854,4 +855,25 @@ def test_deferred_readback_pipelines_frames(ctx):
         ctx.collect()
         assert ctx.lib.t3d_frame_collect(ctx.h, None) == abi.T3D_E_INVAL
     finally:
+        ctx.release(sid)
+
+
+def test_parts_of_many_tiles_scan_in_chunks(ctx):
+    """A 1024^2 terrain alone: four parts of about 256 meshlet tiles each, far more than the
+    frame's tiles per block of the scan phase, so each pair's cross-tile scan runs as one work
+    item per chunk of 32 tiles (the chunks' bin counts summed by the histogram phase). Every form
+    and launch shape gives the oracle's stream."""
+    sd = scenes.terrain_scene(5, n=1024, w=1280, h=720)
+    cam = sd.camera
+    ref = pyoracle.render(sd, cam, threads=os.cpu_count() or 1)
+    assert ref.visible_tris > 100000
+    assert max(s["capacity"] for s in ref.segments) > 128 * 2048  # parts of more than 128 full tiles
+    sid = ctx.upload(sd)
+    try:
+        for mode, split in FORMS:
+            ctx.set_split_phases(split)
+            ctx.render(sid, cam, mode=mode)
+            assert_frames_equal(ctx.download(), ref, f"terrain1024/mode{mode}/split{split}")
+    finally:
+        ctx.set_split_phases(1)
         ctx.release(sid)

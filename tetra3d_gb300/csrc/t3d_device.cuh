@@ -220,9 +220,11 @@ struct TileDesc {
     uint32_t pad1;
 };
 constexpr uint32_t kChunkTris = 256;    // triangles per entry of a mesh's vertex-range table
-// A pair of more than kScanSplit tiles has its cross-tile scan split into chunks of kScanChunk
-// tiles (one scan work item each), the chunks' bin counts summed by the histogram phase. Pairs
-// of fewer tiles keep one item: there the chunk sums cost more than the shorter walk saves.
+// A pair whose cross-tile scan would run long beside the rest of the phase (more than
+// kScanSplit tiles, and more than four times the frame's multi-tile tiles per block) has it
+// split into chunks of kScanChunk tiles (one scan work item each), the chunks' bin counts
+// summed by the histogram phase. Other pairs keep one item: where the phase has enough other
+// work, the chunk sums cost more than the shorter walk saves.
 constexpr uint32_t kScanChunk = 32;
 constexpr uint32_t kScanSplit = 64;
 constexpr uint32_t kNoChunk = 0xFFFFFFFFu;

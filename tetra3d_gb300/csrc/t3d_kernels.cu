@@ -1640,7 +1640,7 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
 }
 
 // P3: per multi-tile segment, turn tile histograms into per-tile bin bases. A pair of
-// several scan chunks (more than kScanSplit tiles) is several work items, one per chunk: each takes the pair's bin
+// several scan chunks is several work items, one per chunk: each takes the pair's bin
 // totals and the counts of the chunks before its own from the chunk sums, then runs
 // through its own chunk's tiles.
 template <int kV>

@@ -1106,6 +1106,7 @@ int scene_write_models(t3d_ctx* ctx, Scene* sc, uint32_t first, const t3d_model_
 // ------------------------------------------------------------ frames ----
 // Builds the tables of one frame. Instances and segments are laid out per job.
 void order_altered_items(t3d_ctx* ctx, FrameTables& F);
+void plan_scan(t3d_ctx* ctx, FrameTables& F);
 
 // Segment flags of a part's billboard options; a skinned model's vertices skip
 // the model matrix, so billboarding does not apply to it (model.go:760-770).
@@ -1356,23 +1357,11 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             sg.tile_first = (uint32_t)F.tiles.size();
             sg.ntiles = ntiles;
             const uint32_t s = (uint32_t)F.segs.size();
-            // the pair's cross-tile scan: one work item, or one per chunk of kScanChunk tiles
-            uint32_t scan_first = 0xFFFFFFFFu, nchunk = 1, chunk_first = kNoChunk;
             if (ntiles > 1 || mls) {  // every meshlet pair takes the multi-tile route
                 flags |= SEG_MULTI;
                 sg.mt_first = (uint32_t)F.mt_desc.size();
                 if (mls && ntiles == 1) flags |= SEG_SINGLE;  // ranked alone: no cross-tile scan
-                else {
-                    scan_first = (uint32_t)F.mt_scan.size();
-                    if (ntiles > kScanSplit) {
-                        nchunk = (ntiles + kScanChunk - 1) / kScanChunk;
-                        chunk_first = F.nchunks;
-                        F.nchunks += nchunk;
-                    }
-                    for (uint32_t c = 0; c < nchunk; c++) F.mt_scan.push_back(make_uint4(s, chunk_first, c, nchunk));
-                }
             }
-            auto tile_chunk = [&](uint32_t t) { return chunk_first == kNoChunk ? kNoChunk : chunk_first + t / kScanChunk; };
             sg.flags = flags;
             if (mls) {
                 for (uint32_t t = 0; t < ntiles; t++) {
@@ -1390,7 +1379,6 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                     td.nearp = dj.cam.near_; td.farp = dj.cam.far_;
                     F.tiles.push_back(td);
                     F.mt_desc.push_back(td);
-                    F.mt_chunk.push_back(tile_chunk(t));
                 }
             }
             for (uint32_t t = 0; t < (mls ? 0u : ntiles); t++) {
@@ -1414,10 +1402,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
                     if (hi >= lo) { td.vlo = sg.vscratch + (lo - sg.vmin); td.vhi = sg.vscratch + (hi - sg.vmin) + 1; }
                 }
                 F.tiles.push_back(td);
-                if (flags & SEG_MULTI) {
-                    F.mt_desc.push_back(td);
-                    F.mt_chunk.push_back(tile_chunk(t));
-                }
+                if (flags & SEG_MULTI) F.mt_desc.push_back(td);
             }
 
             sg.pad[0] = rp.draw | (rp.transparent << 31);  // flush and its pass, for the rasteriser
@@ -1433,7 +1418,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
             si.job = j; si.model = rp.model; si.part = rp.part; si.base = sg.out_base; si.capacity = sg.tri_count; si.count = 0;
             si.draw = rp.draw; si.draw_transparent = rp.transparent;
             F.seg_info.push_back(si);
-            F.seg_mt_seg.push_back(scan_first);  // the pair's first scan item (none: all ones)
+            F.seg_mt_seg.push_back(0xFFFFFFFFu);  // the pair's first scan item (plan_scan)
         }
         F.job_seg_end.push_back((uint32_t)F.segs.size());
     }
@@ -1445,6 +1430,7 @@ int build_frame(t3d_ctx* ctx, const t3d_job_desc* jobs, uint32_t njobs, int anim
     F.vitem_alt = (uint32_t)F.vitem_seg.size();
     F.mt_mesh = (uint32_t)F.mt_desc.size();
     if (F.any_altered || F.any_mesh) order_altered_items(ctx, F);
+    plan_scan(ctx, F);
     // point the jobs at their light tables (device address known after upload)
     return T3D_OK;
 }
@@ -1495,9 +1481,7 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
     F.vitem_chunk.swap(vch);
     // multi-tile numbers: the record path's first, then the meshlet pairs'
     std::vector<TileDesc> mt;
-    std::vector<uint32_t> mtc;  // their scan chunks, in the same order
     mt.reserve(F.mt_desc.size());
-    mtc.reserve(F.mt_chunk.size());
     for (int pass = 0; pass < 2; pass++) {
         for (uint32_t s = 0; s < nseg; s++) {
             DevSeg& sg = F.segs[s];
@@ -1508,14 +1492,38 @@ void order_altered_items(t3d_ctx* ctx, FrameTables& F) {
                 td.mt = first + t;
                 F.tiles[sg.tile_first + t].mt = first + t;
                 mt.push_back(td);
-                mtc.push_back(F.mt_chunk[sg.mt_first + t]);
             }
             sg.mt_first = first;
         }
         if (pass == 0) F.mt_mesh = (uint32_t)mt.size();
     }
     F.mt_desc.swap(mt);
-    F.mt_chunk.swap(mtc);
+}
+
+// The cross-tile scan's work items, in pair order: one per pair of several tiles, or, for a
+// pair whose scan would run long beside the rest of the phase -- more than kScanSplit tiles
+// and more than four times the frame's multi-tile tiles per block of the scan phase -- one
+// per chunk of kScanChunk tiles (the histogram phase then sums each chunk's counts).
+void plan_scan(t3d_ctx* ctx, FrameTables& F) {
+    F.mt_scan.clear();
+    F.mt_chunk.assign(F.mt_desc.size(), kNoChunk);
+    F.nchunks = 0;
+    const uint64_t blocks = std::max<uint64_t>(1, 2ull * (uint64_t)ctx->num_sms);
+    const uint64_t split = std::max<uint64_t>(kScanSplit, 4ull * F.mt_desc.size() / blocks);
+    for (uint32_t s = 0; s < (uint32_t)F.segs.size(); s++) {
+        const DevSeg& sg = F.segs[s];
+        F.seg_mt_seg[s] = 0xFFFFFFFFu;
+        if (!(sg.flags & SEG_MULTI) || (sg.flags & SEG_SINGLE)) continue;
+        F.seg_mt_seg[s] = (uint32_t)F.mt_scan.size();
+        uint32_t nc = 1, cf = kNoChunk;
+        if (sg.ntiles > split) {
+            nc = (sg.ntiles + kScanChunk - 1) / kScanChunk;
+            cf = F.nchunks;
+            F.nchunks += nc;
+            for (uint32_t t = 0; t < sg.ntiles; t++) F.mt_chunk[sg.mt_first + t] = cf + t / kScanChunk;
+        }
+        for (uint32_t c = 0; c < nc; c++) F.mt_scan.push_back(make_uint4(s, cf, c, nc));
+    }
 }
 
 template <typename T> static size_t bytes_of(const std::vector<T>& v) { return v.size() * sizeof(T); }
@@ -1575,7 +1583,7 @@ int upload_frame(t3d_ctx* ctx, cudaStream_t st) {
     P.mt_desc = (const TileDesc*)(db + o_mtt);
     P.mt_segs = nullptr;
     P.mt_scan = (const uint4*)(db + o_mts);
-    P.mt_chunk = (const uint32_t*)(db + o_mtc);
+    P.mt_chunk = F.nchunks ? (const uint32_t*)(db + o_mtc) : nullptr;  // no chunk: no look-ups
     P.vitem_seg = (const uint32_t*)(db + o_vs);
     P.vitem_chunk = (const uint32_t*)(db + o_vc);
 
