@@ -1493,8 +1493,6 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
     const uint32_t lane = threadIdx.x & 31, T = P.tile_tris;
     const uint32_t n = __ldcg(&P.tile_count[i]);
     const uint32_t s = td.seg;
-    // the tile's scan chunk, read now so its latency hides behind the ranking
-    const uint32_t ch = (P.mt_chunk && !(td.flags & SEG_SINGLE)) ? __ldg(&P.mt_chunk[i]) : kNoChunk;
     for (uint32_t b = lane; b < kBinsPadded; b += 32) cnt[b] = 0u;
     const float mn = __uint_as_float(__ldcg(&P.seg_minmax[2 * s]));
     const float mx = __uint_as_float(__ldcg(&P.seg_minmax[2 * s + 1]));
@@ -1536,11 +1534,7 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
     }
     if (!(td.flags & SEG_SINGLE)) {
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
-        for (uint32_t b = lane; b < kBins; b += 32) {
-            const uint32_t c = cnt[pad_bin(b)];
-            out[b] = c;
-            if (ch != kNoChunk && c) atomicAdd(&P.chunk_hist[(size_t)ch * kBins + b], c);
-        }
+        for (uint32_t b = lane; b < kBins; b += 32) out[b] = cnt[pad_bin(b)];
     }
     // exclusive scan in walk order: lane l owns walk positions [16 l, 16 l + 16)
     {
@@ -1573,6 +1567,19 @@ __device__ __noinline__ void hist_rank_meshlet(const FrameParams& P, uint32_t i,
     }
 }
 
+// A tile of a pair whose scan runs in chunks adds its bin counts (just written to tile_hist by
+// the same lanes) to its chunk's sums. Kept out of the ranking code, whose schedule it
+// slowed even in frames without chunks.
+__device__ __noinline__ void add_chunk_counts(const FrameParams& P, uint32_t i) {
+    const uint32_t ch = __ldg(&P.mt_chunk[i]);
+    if (ch == kNoChunk) return;
+    const uint32_t* h = P.tile_hist + (size_t)i * kBins;
+    for (uint32_t b = threadIdx.x & 31; b < kBins; b += 32) {
+        const uint32_t c = h[b];
+        if (c) atomicAdd(&P.chunk_hist[(size_t)ch * kBins + b], c);
+    }
+}
+
 // P2: bin histograms of the tiles of multi-tile segments, one warp per tile
 // (each warp pulls its own tiles and owns a kBins-counter region of shared
 // memory). Queue slots run over the record-path tiles [mt_tile_begin,
@@ -1597,13 +1604,13 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         if (td.flags & SEG_MESHLET) {  // counts, cross-tile counts and the tile's stable ranking
             uint16_t* sb = reinterpret_cast<uint16_t*>(L.whist + (size_t)nw * kBinsPadded) + 2 * (size_t)wid * T;
             hist_rank_meshlet(P, i, td, wh, sb, sb + T);
+            if (P.mt_chunk && !(td.flags & SEG_SINGLE)) add_chunk_counts(P, i);
             uint32_t nx = 0;
             if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
             k = __shfl_sync(0xffffffffu, nx, 0);
             continue;
         }
         const uint32_t n = __ldcg(&P.tile_count[i]);
-        const uint32_t ch = P.mt_chunk ? __ldg(&P.mt_chunk[i]) : kNoChunk;  // read early: used at the end
         for (uint32_t b = lane; b < kBins; b += 32) wh[b] = 0u;
         __syncwarp();
         if (n > 0) {
@@ -1627,11 +1634,8 @@ __device__ __noinline__ void phase_hist(const FrameParams& P, unsigned char* sme
         }
         __syncwarp();
         uint32_t* out = P.tile_hist + (size_t)i * kBins;
-        for (uint32_t b = lane; b < kBins; b += 32) {
-            const uint32_t c = wh[b];
-            out[b] = c;
-            if (ch != kNoChunk && c) atomicAdd(&P.chunk_hist[(size_t)ch * kBins + b], c);
-        }
+        for (uint32_t b = lane; b < kBins; b += 32) out[b] = wh[b];
+        if (P.mt_chunk) add_chunk_counts(P, i);
         __syncwarp();
         uint32_t nx = 0;
         if (lane == 0) nx = atomicAdd(&P.ctl->queue[2], 1u);
