@@ -877,3 +877,30 @@ def test_parts_of_many_tiles_scan_in_chunks(ctx):
     finally:
         ctx.set_split_phases(1)
         ctx.release(sid)
+
+
+def test_shape_keyed_meshlets_follow_weight_changes(ctx):
+    """Shape-keyed meshes take the meshlet route, their meshlets cut from the keyed streams baked
+    for the current weights: new weights refill the meshlets, a re-cut for another tile size starts
+    from the current weights, and both routes at both tile sizes give the oracle's stream."""
+    sd = scenes.frame_variant("shape_keys", n=128)
+    cam = sd.camera
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam)
+        assert_frames_equal(ctx.download(), pyoracle.render(sd, cam, threads=os.cpu_count() or 1), "initial")
+        for step, w in enumerate(([0.1, 0.9], [-0.7, 0.25])):
+            for m in (0, len(sd.meshes) - 1):
+                sd.meshes[m].shape_weights = np.array(w, np.float32)
+                ctx.set_shape_weights(sid, m, sd.meshes[m].shape_weights)
+            ref = pyoracle.render(sd, cam, threads=os.cpu_count() or 1)
+            for tile in (2048, 1024):
+                ctx.set_tuning(tile_tris=tile)
+                for meshlets in (1, 0):
+                    ctx.set_meshlets(meshlets)
+                    ctx.render(sid, cam)
+                    assert_frames_equal(ctx.download(), ref, f"weights{step}/tile{tile}/meshlets{meshlets}")
+    finally:
+        ctx.set_meshlets(1)
+        ctx.set_tuning(tile_tris=2048)
+        ctx.release(sid)

@@ -254,7 +254,7 @@ struct FrameParams {
     const DevSeg* segs;
     const TileDesc* tiles;        // per tile
     const TileDesc* mt_desc;      // per multi-tile tile (a copy of its tile's record)
-    const uint32_t* mt_segs;      // multi-tile segments
+    const uint32_t* mt_segs;      // multi-tile segments, one scan item each (when mt_scan is null)
     const uint32_t* vitem_seg;    // vertex work item -> segment
     const uint32_t* vitem_chunk;  // vertex work item -> chunk of vchunk vertices
     // scratch
