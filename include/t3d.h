@@ -367,10 +367,11 @@ const char* t3d_last_error(const t3d_ctx* ctx);
 int         t3d_set_tuning(t3d_ctx* ctx, uint32_t tile_tris, uint32_t vertex_chunk, uint32_t block_threads);
 /* Route of the vertex stage (no reference counterpart: the reference has one CPU
  * path). enable = 1 (the default): render pairs that need nothing beyond the plain
- * vertex loop (no skinning, shape keys, auto-subdivision, vertex snapping, lights
- * used by volume cells or unbillboarded depth) read their part's meshlets -- runs of
- * consecutive triangles with their distinct vertices stored contiguously, cut at
- * scene upload -- and keep every per-vertex intermediate in shared memory.
+ * vertex loop (no skinning, auto-subdivision, vertex snapping, lights used by volume
+ * cells or unbillboarded depth; shape keys allowed) read their part's meshlets --
+ * runs of consecutive triangles with their distinct vertices stored contiguously, cut
+ * at scene upload (a shape-keyed mesh's from its keyed vertices, refilled when its
+ * weights change) -- and keep every per-vertex intermediate in shared memory.
  * enable = 0: every pair writes and reads per-vertex records in device memory. The
  * emitted stream is the same bit for bit either way. */
 int         t3d_set_meshlets(t3d_ctx* ctx, int enable);
@@ -407,7 +408,8 @@ int t3d_scene_bytes(t3d_ctx* ctx, uint32_t scene, uint64_t* bytes_out);
  * node.go), as an animation player updates them every frame. */
 int t3d_scene_set_bones(t3d_ctx* ctx, uint32_t scene, uint32_t first, const float* influences, uint32_t n);
 /* Shape-key weights of one mesh of a scene (ShapeKey.weight, mesh.go). The mesh's keyed
- * vertices (shared by all its models) are recomputed on the device before this returns. */
+ * vertices (shared by all its models) and its meshlets' vertex data are recomputed on the
+ * device before this returns. */
 int t3d_scene_set_shape_weights(t3d_ctx* ctx, uint32_t scene, uint32_t mesh, const float* weights, uint32_t n);
 /* Lights [first, first + n) of a scene: moved, recoloured, re-ranged or of another
  * kind, as Camera.Render reads them anew every frame (camera.go:1269-1300,
