@@ -14,9 +14,9 @@
 // rounded to nearest after clamping to [0, 1].
 //
 // Device work: every visible triangle of the job lists the pixels it covers
-// (fragments, written in draw order), a stable radix sort groups fragments by
-// pixel, and one thread per pixel replays its fragments in draw order with the
-// per-pair depth and colour logic.
+// (fragments), a counting sort groups fragments by pixel, and one thread per
+// pixel sorts its fragments into draw order (by hit index) and replays them with
+// the per-pair depth and colour logic.
 
 #include <cuda_runtime.h>
 
@@ -39,11 +39,6 @@ using namespace t3d;
 
 namespace {
 
-constexpr int kSortBits = 8;
-constexpr int kSortDigits = 1 << kSortBits;
-constexpr int kSortThreads = 256;
-constexpr int kSortPerThread = 16;
-constexpr int kSortChunk = kSortThreads * kSortPerThread;
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
 constexpr int kScanChunk = kScanThreads * kScanPer;
@@ -448,9 +443,8 @@ __global__ void __launch_bounds__(kFragThreads, 5) k_big_count(RasterJob J, cons
 }
 
 // Fragment pass 2, one warp per unit: the unit's hits write their fragments (key = pixel,
-// value = the hit's index, which names its triangle) from ufoff[u] on, in draw order, so the
-// stable sort by pixel keeps draw order per pixel. A shared large triangle only sets its
-// cursor; k_big_write fills its range.
+// value = the hit's index, which names its triangle and its place in draw order) from
+// ufoff[u] on. A shared large triangle only sets its cursor; k_big_write fills its range.
 __global__ void __launch_bounds__(kFragThreads, 4) k_frag_write(RasterJob J, uint32_t nunits, const uint4* __restrict__ hits,
                                                              const uint32_t* __restrict__ uhits,
                                                              const uint32_t* __restrict__ ufoff, BigTri* big,
@@ -549,66 +543,51 @@ __global__ void __launch_bounds__(kFragThreads, 5) k_big_write(RasterJob J, BigT
     }
 }
 
-// ---- stable LSD radix sort of (key, value) pairs by kSortBits-bit digits --------
-__global__ void k_sort_hist(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ fcount, int shift,
-                            uint32_t nblocks, uint32_t* counts) {
-    const uint32_t n = fcount[1];
-    __shared__ uint32_t h[kSortDigits];
-    for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) h[d] = 0;
-    __syncthreads();
-    const size_t base = (size_t)blockIdx.x * kSortChunk;
-    for (int k = 0; k < kSortPerThread; k++) {
-        const size_t i = base + (size_t)k * kSortThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kSortDigits - 1)], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) counts[(size_t)d * nblocks + blockIdx.x] = h[d];
+// ---- grouping fragments by pixel ------------------------------------------------
+// A counting sort: k_pixel_count counts each pixel's fragments, their exclusive prefix gives
+// each pixel its range, and k_pixel_scatter puts every fragment into its pixel's range through
+// an atomic cursor. The order inside a range is whatever the atomics gave; k_pixels restores
+// draw order by sorting the range by hit index (a triangle has at most one fragment per pixel,
+// so the indices of a range are distinct and the sorted order is unique).
+__global__ void k_pixel_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                const uint32_t* __restrict__ fcount, const uint32_t* __restrict__ pstart,
+                                uint32_t* cursor, uint32_t* ovals) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= fcount[1]) return;
+    const uint32_t p = keys[i];
+    ovals[pstart[p] + atomicAdd(&cursor[p], 1u)] = vals[i];
 }
 
-__global__ void k_sort_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                               const uint32_t* __restrict__ fcount, int shift, uint32_t nblocks,
-                               const uint32_t* __restrict__ offsets, uint32_t* okeys, uint32_t* ovals) {
-    const uint32_t n = fcount[1];
-    constexpr int kWarps = kSortThreads / 32;
-    __shared__ uint32_t running[kSortDigits];
-    __shared__ uint32_t wcount[kWarps][kSortDigits];
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < kSortDigits; d += blockDim.x) running[d] = offsets[(size_t)d * nblocks + blockIdx.x];
-    const size_t base = (size_t)blockIdx.x * kSortChunk;
-    const uint32_t lt = (1u << lane) - 1u;
-    for (int k = 0; k < kSortPerThread; k++) {
-        for (int q = threadIdx.x; q < kWarps * kSortDigits; q += blockDim.x) (&wcount[0][0])[q] = 0u;
-        __syncthreads();
-        // entries in order: round k covers [base + 256k, base + 256k + 256), warp w its 32-entry slice
-        const size_t i = base + (size_t)k * kSortThreads + threadIdx.x;
-        const bool active = i < n;
-        const uint32_t mask = __ballot_sync(0xffffffffu, active);
-        uint32_t key = 0, val = 0, d = 0, peers = 0;
-        if (active) {
-            key = keys[i];
-            val = vals[i];
-            d = (key >> shift) & (kSortDigits - 1);
-            peers = __match_any_sync(mask, d);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) wcount[wid][d] = __popc(peers);
+// Sorts v[0, n) ascending in place: insertion sort for short ranges, heapsort beyond.
+__device__ __forceinline__ void sort_range(uint32_t* v, uint32_t n) {
+    if (n <= 32) {
+        for (uint32_t i = 1; i < n; i++) {
+            const uint32_t x = v[i];
+            uint32_t j = i;
+            for (; j > 0 && v[j - 1] > x; j--) v[j] = v[j - 1];
+            v[j] = x;
         }
-        __syncthreads();
-        // per digit: exclusive prefix over warps (thread d owns digit d)
-        for (int dd = threadIdx.x; dd < kSortDigits; dd += blockDim.x) {
-            uint32_t run = running[dd];
-            for (int w = 0; w < kWarps; w++) {
-                const uint32_t t = wcount[w][dd];
-                wcount[w][dd] = run;
-                run += t;
-            }
-            running[dd] = run;
+        return;
+    }
+    auto sift = [&](uint32_t root, uint32_t end) {  // max-heap on v[0, end)
+        const uint32_t x = v[root];
+        uint32_t r = root;
+        for (;;) {
+            uint32_t c = 2 * r + 1;
+            if (c >= end) break;
+            if (c + 1 < end && v[c + 1] > v[c]) c++;
+            if (v[c] <= x) break;
+            v[r] = v[c];
+            r = c;
         }
-        __syncthreads();
-        if (active) {
-            const uint32_t pos = wcount[wid][d] + __popc(peers & lt);
-            okeys[pos] = key;
-            ovals[pos] = val;
-        }
-        __syncthreads();
+        v[r] = x;
+    };
+    for (uint32_t i = n / 2; i-- > 0;) sift(i, n);
+    for (uint32_t end = n - 1; end > 0; end--) {
+        const uint32_t t = v[0];
+        v[0] = v[end];
+        v[end] = t;
+        sift(0, end);
     }
 }
 
@@ -708,15 +687,18 @@ __device__ __forceinline__ Frag fragment(const RasterJob& J, uint32_t slot, floa
     return interp(tri_attr(J, slot), t.area, wa, wb, wc);
 }
 
-// One thread per pixel replays the pixel's fragments (sorted by pixel, draw order kept);
-// fvals[q] is the hit of fragment q's triangle: hits[fvals[q]] = (output slot, render pair, ...).
-__global__ void __launch_bounds__(256, 5) k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ fvals,
+// One thread per pixel replays the pixel's fragments in draw order (its range of fvals,
+// grouped by pixel, sorted here by hit index); fvals[q] is the hit of fragment q's triangle:
+// hits[fvals[q]] = (output slot, render pair, ...).
+__global__ void __launch_bounds__(256, 5) k_pixels(RasterJob J, const uint32_t* __restrict__ pstart, const uint32_t* fvals,
                          const uint4* __restrict__ hits, uint32_t* color, uint32_t* depth) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (uint32_t)(J.W * J.H)) return;
     const float x = (float)(p % (uint32_t)J.W) + 0.5f, y = (float)(p / (uint32_t)J.W) + 0.5f;
     uint32_t rc = 0u, rd = 0u;
     const uint32_t f0 = pstart[p], f1 = pstart[p + 1];
+    uint32_t* fv = const_cast<uint32_t*>(fvals);  // this thread's own range: draw order first
+    if (f1 - f0 > 1) sort_range(fv + f0, f1 - f0);
     uint32_t i = f0;
     while (i < f1) {
         // the fragments of one flush: a render pair, or all pairs of a dynamic batch
@@ -804,7 +786,7 @@ __global__ void k_frag_total(const uint32_t* __restrict__ ufoff, const uint32_t*
 }
 
 struct RasterScratch {
-    DevBuf cbase, hits, uhits, ufrags, ufoff, big, chunk_tri, ctr, keys, vals, keys2, vals2, counts, offsets, partial[3], pstart, pcount,
+    DevBuf cbase, hits, uhits, ufrags, ufoff, big, chunk_tri, ctr, keys, vals, vals2, partial[3], pstart, pcount,
         color, depth, fcount;
 };
 
@@ -935,37 +917,27 @@ int t3d_frame_raster(t3d_ctx* ctx, uint32_t job, const t3d_raster_opts* opts, vo
     // (the last raster's total and an eighth more, grow-only); a larger total is found at the
     // end of the call, which then grows them and runs again
     const uint32_t fcap = R.frag_cap;
-    const uint32_t nsb = std::max(1u, (fcap + kSortChunk - 1) / kSortChunk);
     if ((rc = S.keys.ensure(ctx, 4ull * fcap)) || (rc = S.vals.ensure(ctx, 4ull * fcap)) ||
-        (rc = S.keys2.ensure(ctx, 4ull * fcap)) || (rc = S.vals2.ensure(ctx, 4ull * fcap)) ||
-        (rc = S.counts.ensure(ctx, 4ull * kSortDigits * nsb)) || (rc = S.offsets.ensure(ctx, 4ull * kSortDigits * nsb)) ||
-        (rc = S.fcount.ensure(ctx, 16)))
+        (rc = S.vals2.ensure(ctx, 4ull * fcap)) || (rc = S.fcount.ensure(ctx, 16)))
         return rc;
     uint32_t* fcount = (uint32_t*)S.fcount.ptr;
     k_frag_total<<<1, 1, 0, st>>>((const uint32_t*)S.ufoff.ptr, (const uint32_t*)S.ufrags.ptr, nunits, fcap, fcount,
                                   (uint32_t*)S.pstart.ptr + npx);
-    uint32_t *kin = (uint32_t*)S.keys.ptr, *vin = (uint32_t*)S.vals.ptr;
-    uint32_t *kout = (uint32_t*)S.keys2.ptr, *vout = (uint32_t*)S.vals2.ptr;
+    uint32_t *kin = (uint32_t*)S.keys.ptr, *vin = (uint32_t*)S.vals.ptr, *vout = (uint32_t*)S.vals2.ptr;
     k_frag_write<<<fblocks, kFragThreads, 0, st>>>(J, nunits, (const uint4*)S.hits.ptr, (const uint32_t*)S.uhits.ptr,
                                                    (const uint32_t*)S.ufoff.ptr, big, kin, vin, fcount);
     k_big_write<<<bigblocks, kFragThreads, 0, st>>>(J, big, chunk_tri, ctr, kin, vin, fcount);
-    // 3. stable sort by pixel
-    int bits = 1;
-    while ((1ull << bits) < npx) bits++;
-    for (int shift = 0; shift < bits; shift += kSortBits) {
-        k_sort_hist<<<nsb, kSortThreads, 0, st>>>(kin, fcount, shift, nsb, (uint32_t*)S.counts.ptr);
-        if ((rc = scan_u32(ctx, S, (const uint32_t*)S.counts.ptr, (uint32_t*)S.offsets.ptr, kSortDigits * nsb, st)))
-            return rc;
-        k_sort_scatter<<<nsb, kSortThreads, 0, st>>>(kin, vin, fcount, shift, nsb, (const uint32_t*)S.offsets.ptr, kout, vout);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
-    // 4. per-pixel fragment ranges (pstart[npx], the total, was written by k_frag_total)
+    // 3. fragments grouped by pixel (pstart[npx], the total, was written by k_frag_total): counts,
+    // their prefix, then each fragment into its pixel's range (the counts zeroed again serve as
+    // the ranges' cursors)
     CKR(cudaMemsetAsync(S.pcount.ptr, 0, 4 * npx, st));
     k_pixel_count<<<(fcap + 255) / 256, 256, 0, st>>>(kin, fcount, (uint32_t*)S.pcount.ptr);
     if ((rc = scan_u32(ctx, S, (const uint32_t*)S.pcount.ptr, (uint32_t*)S.pstart.ptr, (uint32_t)npx, st))) return rc;
-    // 5. replay per pixel
-    k_pixels<<<(uint32_t)((npx + 255) / 256), 256, 0, st>>>(J, (const uint32_t*)S.pstart.ptr, vin,
+    CKR(cudaMemsetAsync(S.pcount.ptr, 0, 4 * npx, st));
+    k_pixel_scatter<<<(fcap + 255) / 256, 256, 0, st>>>(kin, vin, fcount, (const uint32_t*)S.pstart.ptr,
+                                                        (uint32_t*)S.pcount.ptr, vout);
+    // 4. replay per pixel, each pixel's range sorted into draw order first
+    k_pixels<<<(uint32_t)((npx + 255) / 256), 256, 0, st>>>(J, (const uint32_t*)S.pstart.ptr, vout,
                                                            (const uint4*)S.hits.ptr, (uint32_t*)S.color.ptr,
                                                            (uint32_t*)S.depth.ptr);
     CKR(cudaGetLastError());
@@ -1047,8 +1019,8 @@ int t3d_frame_images(t3d_ctx* ctx, uint8_t* color_rgba8, uint8_t* depth_rgba8, i
 void t3d_raster_release(t3d_ctx* ctx) {
     if (!ctx->raster) return;
     RasterScratch& S = ctx->raster->S;
-    for (DevBuf* b : {&S.cbase, &S.hits, &S.uhits, &S.ufrags, &S.ufoff, &S.big, &S.chunk_tri, &S.ctr, &S.keys, &S.vals, &S.keys2, &S.vals2,
-                      &S.counts, &S.offsets, &S.partial[0], &S.partial[1], &S.partial[2], &S.pstart, &S.pcount, &S.color,
+    for (DevBuf* b : {&S.cbase, &S.hits, &S.uhits, &S.ufrags, &S.ufoff, &S.big, &S.chunk_tri, &S.ctr, &S.keys, &S.vals, &S.vals2,
+                      &S.partial[0], &S.partial[1], &S.partial[2], &S.pstart, &S.pcount, &S.color,
                       &S.depth, &S.fcount, &ctx->raster->texs, &ctx->raster->texels})
         b->release();
     delete ctx->raster;
