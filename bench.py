@@ -330,7 +330,7 @@ def run_ours(args, rank, world, local_rank):
                   "roofline": {"bound": "hbm", "achieved": rbytes / (rdev / 1e3) / 1e9, "peak": rpeak, "unit": "GB/s",
                                "frac": rbytes / (rdev / 1e3) / 1e9 / rpeak, "algorithmic_bytes": rbytes,
                                "peak_source": f"{rpeak_kind} hbm_gbs"},
-                  "note": "t3d_frame_raster (fragments, stable sort by pixel, per-pixel passes): ms_per_frame is "
+                  "note": "t3d_frame_raster (fragments, counting sort by pixel, per-pixel draw-order passes): ms_per_frame is "
                           "wall time incl. its host syncs, device_ms_per_frame CUDA events on its stream"}
 
     # ---- the frame with one vertex-stage feature on for every model ----
