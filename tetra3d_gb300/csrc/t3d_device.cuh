@@ -162,7 +162,8 @@ struct DevJob {
 __host__ __device__ inline uint32_t mlet_slots4(uint32_t nu) { return (nu + 3u) & ~3u; }
 __host__ __device__ inline uint32_t mlet_lidx_bytes(uint32_t nt) { return (6u * nt + 15u) & ~15u; }
 __host__ __device__ inline uint32_t mlet_aos_stride(bool colors) { return colors ? 48u : 32u; }
-// A shape-keyed mesh's meshlet as the refill kernel reads it (same fields as the host's MletFill).
+// A meshlet of a shape-keyed mesh as the refill kernel reads it: its place in the pool (16-byte
+// units), triangles, slots, and where its slot -> mesh vertex map starts.
 struct MletFillDev {
     uint32_t off16, nt, nu, vmap_off;
 };

@@ -41,11 +41,8 @@ struct Meshlet {
     uint32_t t0, nt, nu, off16;
 };
 // A meshlet of a shape-keyed mesh, for refilling its vertex data from the keyed streams when
-// the weights change: its place in the pool (16-byte units), triangles, slots, and where its
-// slot -> mesh vertex map starts.
-struct MletFill {
-    uint32_t off16, nt, nu, vmap_off;
-};
+// the weights change (the record the refill kernel reads).
+using MletFill = MletFillDev;
 struct SceneMesh {
     uint32_t vbase = 0, tbase = 0, nverts = 0, ntris = 0;
     bool colors = false;
