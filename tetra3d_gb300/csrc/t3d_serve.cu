@@ -80,6 +80,11 @@ struct t3d_server {
     std::vector<t3d_completion> done;
     std::atomic<bool> stop{false};
     uint64_t inflight = 0;
+    // the slot that completed a batch last, and the slots with a batch in flight. While none is
+    // in flight only the last one watches the clock for the next replayed arrival, so at low load
+    // the slot whose host caches are warm takes the next request; otherwise every idle slot does.
+    const Slot* last_done = nullptr;
+    uint32_t nbusy = 0;
     Clock::time_point t0;
     bool verify = true;
     std::string err;
@@ -144,6 +149,8 @@ struct t3d_server {
             }
         }
         std::lock_guard<std::mutex> g(mu);
+        nbusy--;
+        last_done = &s;
         if (rc != T3D_OK && err.empty()) err = s.ctx->err;
         for (size_t k = 0; k < s.batch.size(); k++) {
             t3d_completion c;
@@ -207,15 +214,17 @@ struct t3d_server {
                     // sleep overshoots by tens of microseconds); otherwise sleep until a submit, a
                     // completion or shortly before the next arrival
                     const double due = queue.empty() ? 1.0 : queue.front().arrival_abs - now();
-                    if (due < 100e-6) {
+                    const bool may_poll = nbusy > 0 || last_done == nullptr || last_done == &s;
+                    if (due < 100e-6 && may_poll) {
                         g.unlock();
                         const double until = now() + std::max(0.0, due);
                         while (now() < until) std::this_thread::yield();
                         g.lock();
                         continue;
                     }
-                    cv.wait_for(g, std::chrono::duration<double>(std::min(200e-6, due - 60e-6)));
+                    cv.wait_for(g, std::chrono::duration<double>(std::max(50e-6, std::min(200e-6, due - 60e-6))));
                 }
+                nbusy++;
                 inflight += s.bytes;
             }
             jobs.resize(s.batch.size());
