@@ -1,9 +1,10 @@
 """Generates tests/golden/c1_whole_path.npz: the emitted stream of the one-sphere scene
 (a UV sphere of 32 x 16 segments, 960 triangles, ambient + directional + point light,
-640x360, back-to-front sort), and of the same scene with a non-uniform scale and two more
-point lights, computed by a second restatement of the vertex stage written here in
-numpy binary32 arithmetic, independently of the C++ oracle, so the oracle can be
-checked against it bit for bit.
+640x360, back-to-front sort), of the same scene with a non-uniform scale and two more
+point lights, and of that scene with a light volume (a grid of cells, an offset and a light
+bias) lighting the sphere per vertex, per vertex with the normal, and per object, computed by
+a second restatement of the vertex stage written here in numpy binary32 arithmetic,
+independently of the C++ oracle, so the oracle can be checked against it bit for bit.
 
 Every operation is an elementwise IEEE binary32 operation (numpy float32 arrays, no
 fused multiply-add, no reductions), in the order the reference writes it:
@@ -20,7 +21,9 @@ fused multiply-add, no reductions), in the order the reference writes it:
 - sortingTriangleBucket.Sort / ForEach (sortingTriangles.go:38-125), 512 bins;
 - lights: AmbientLight, PointLight, DirectionalLight beginRender / beginModel /
   VertexLight (light.go:110-360) with the model-level point-light range skip
-  (camera.go:1613-1641);
+  (camera.go:1613-1641); LightVolume.VertexLight (light.go:583-663) with the cell grid of
+  LightVolumeResize (light.go:459-513), convertToXYZIndices (light.go:716-724) and
+  Dimensions.Contains (mesh.go:82-84);
 - the emit loop (camera.go:1646-1820): screen position, UV, colour x lighting, depth.
 
 Run from the repo root: python tests/golden/make_c1_whole_path.py
@@ -205,7 +208,11 @@ def scene_inputs(sd):
         Lt = np.asarray(L.transform[:], F).reshape(4, 4)
         lights.append(dict(type=int(L.type), color=np.asarray(L.color[:3], F), energy=F(L.energy),
                            range=F(L.range), world_pos=[Lt[3, 0], Lt[3, 1], Lt[3, 2]],
-                           world_rot=np.asarray(L.world_rotation[:], F).reshape(4, 4)))
+                           world_rot=np.asarray(L.world_rotation[:], F).reshape(4, 4),
+                           vol_min=np.asarray(L.vol_min[:], F), vol_max=np.asarray(L.vol_max[:], F),
+                           cell_size=np.asarray(L.cell_size[:], F), offset=np.asarray(L.offset[:], F),
+                           bias=np.asarray(L.bias[:], F), cell_count=[int(c) for c in L.cell_count],
+                           cell_first=int(L.cell_first)))
     ct = np.asarray(cam.transform[:], F).reshape(4, 4)
     return dict(
         positions=me.positions.astype(F), normals=me.normals.astype(F), uvs=me.uvs.astype(F),
@@ -215,6 +222,7 @@ def scene_inputs(sd):
         mat_color=np.asarray(mat["color"], F), tex=(F(mat["tex_w"]), F(mat["tex_h"])),
         backface=bool(mat["backface_culling"]), sort_mode=int(mat["sort_mode"]),
         lighting_mode=int(mat["lighting_mode"]), shadeless=bool(mat["shadeless"]) or bool(mv["shadeless"]),
+        lv_mode=int(mat["lv_shading_mode"]), cells=np.asarray(sd.cells, F)[:max(0, sd.ncells)],
         lights=lights, cam_pos=[ct[3, 0], ct[3, 1], ct[3, 2]],
         cam_rot=np.asarray(cam.world_rotation[:], F).reshape(4, 4), width=int(cam.width), height=int(cam.height),
         fov=F(cam.fov_y), near=F(cam.near_plane), far=F(cam.far_plane), depth_margin=F(cam.depth_margin),
@@ -254,6 +262,75 @@ def in_frustum(S, M, dmin, dmax):
     d = fx * radius
     pcx = dot(diff, right)
     return not (pcx > pcz + d or pcx < -pcz - d)
+
+
+def grid_counts(vmin, vmax, cs):
+    """LightVolumeResize (light.go:485-513): cells along an axis from Min + size/2, stepping by the
+    size in binary32 while the position stays <= Max - size/2."""
+    out = []
+    for a in range(3):
+        n = 0
+        v = F(vmin[a]) + F(cs[a] / F(2))
+        top = F(vmax[a]) - F(cs[a] / F(2))
+        while v <= top:
+            n += 1
+            v = F(v + cs[a])
+        out.append(n)
+    return out
+
+
+def round_half_away(x):
+    """math32.Round: float32(math.Round(float64(x))), halves away from zero."""
+    x = np.asarray(x, np.float64)
+    return np.where(x < 0, -np.floor(-x + 0.5), np.floor(x + 0.5))
+
+
+def volume_cells(S, L, M, P, N):
+    """LightVolume.VertexLight (light.go:583-663) for every vertex of an unskinned model: the cell
+    colour each vertex takes (black where no cell) and whether the vertex adds anything (the light
+    returns early for vertices outside the volume's dimensions)."""
+    abi = S["abi"]
+    mode = S["lv_mode"]
+    nv = len(P)
+    if mode == abi.LV_OFF:  # LightVolume.Light skips the pair
+        z = np.zeros(nv, F)
+        return z, z, z, np.zeros(nv, bool)
+    vmin, vmax, cs, off, bias = L["vol_min"], L["vol_max"], L["cell_size"], L["offset"], L["bias"]
+    cnt = grid_counts(vmin, vmax, cs)
+    assert cnt == L["cell_count"], (cnt, L["cell_count"])
+    cells = S["cells"]
+
+    def cell_rgb(wx, wy, wz):
+        # convertToXYZIndices: int(Round(((w - offset - Min - size/2) / size)))
+        idx = []
+        for a, w in enumerate((wx, wy, wz)):
+            q = (((np.asarray(w, F) - off[a]) - vmin[a]) - (cs[a] / F(2))) / cs[a]
+            idx.append(round_half_away(q.astype(F)).astype(np.int64))
+        x, y, z = idx
+        inside = (x >= 0) & (y >= 0) & (z >= 0) & (x < cnt[0]) & (y < cnt[1]) & (z < cnt[2])
+        flat = np.where(inside, x + y * cnt[0] + z * cnt[0] * cnt[1], 0)
+        rgb = cells[L["cell_first"] + flat, :3].astype(F)
+        rgb = np.where(inside[..., None], rgb, F(0)).astype(F)
+        return rgb[..., 0], rgb[..., 1], rgb[..., 2]
+
+    if mode == abi.LV_PER_OBJECT:  # the cell at Model.WorldPosition, for every vertex
+        r, g, b = cell_rgb(np.full(nv, M[3, 0], F), np.full(nv, M[3, 1], F), np.full(nv, M[3, 2], F))
+        return r, g, b, np.ones(nv, bool)
+    half = [cs[a] / F(2) for a in range(3)]
+    if mode == abi.LV_PER_VERTEX_WITH_NORMAL:
+        # only vertPosWithNormal is set in this mode: the containment test reads vertPos, which
+        # stays the zero vector
+        q = [P[:, a] + N[:, a] * half[a] for a in range(3)]
+        t = multvec(M, (q[0], q[1], q[2]))
+        look = [t[a] + bias[a] for a in range(3)]
+        probe = [np.zeros(nv, F)] * 3
+    else:
+        t = multvec(M, (P[:, 0], P[:, 1], P[:, 2]))
+        look = probe = [t[a] + bias[a] for a in range(3)]
+    contains = ((probe[0] >= vmin[0]) & (probe[1] >= vmin[1]) & (probe[2] >= vmin[2]) &
+                (probe[0] <= vmax[0]) & (probe[1] <= vmax[1]) & (probe[2] <= vmax[2]))
+    r, g, b = cell_rgb(*look)
+    return r, g, b, contains
 
 
 def render(S):
@@ -386,6 +463,11 @@ def render(S):
                 lr = np.where(on, lr + (col[0] * dfac) * e, lr).astype(F)
                 lg = np.where(on, lg + (col[1] * dfac) * e, lg).astype(F)
                 lb = np.where(on, lb + (col[2] * dfac) * e, lb).astype(F)
+            elif L["type"] == abi.LIGHT_VOLUME:
+                cr_, cg_, cb_, on = volume_cells(S, L, M, P, N)
+                lr = np.where(on, lr + (col[0] * cr_) * e, lr).astype(F)
+                lg = np.where(on, lg + (col[1] * cg_) * e, lg).astype(F)
+                lb = np.where(on, lb + (col[2] * cb_) * e, lb).astype(F)
     # the emit loop, corner by corner in draw order
     mp = S["model_color"] * S["mat_color"]  # Color4.MultiplyRGBA
     margin = (far - near) * S["depth_margin"]
@@ -433,9 +515,38 @@ def scaled_variant():
     return sd
 
 
+def volume_variant(lv_mode):
+    """The scaled five-light scene plus a light volume around the sphere and the origin (the
+    containment test of the per-vertex-with-normal mode reads the zero vector): a 9 x 5 x 17 grid
+    of 0.4-unit cells with random colours, offset and light bias, lighting the sphere with the
+    material's LightVolumeShadingMode `lv_mode`."""
+    from tetra3d_gb300 import abi, scenes
+    sd = scaled_variant()
+    rng = np.random.Generator(np.random.PCG64(11))
+    vmin = np.array([-1.8, -1.0, -6.4], F)
+    vmax = np.array([1.8, 1.0, 0.4], F)
+    cs = np.array([0.4, 0.4, 0.4], F)
+    counts = scenes.light_volume_counts(vmin, vmax, cs)
+    cells = np.concatenate([rng.uniform(0.1, 1.0, (int(np.prod(counts)), 3)), np.ones((int(np.prod(counts)), 1))],
+                           1).astype(F)
+    vol = scenes.light(abi.LIGHT_VOLUME, color=(1.0, 0.9, 0.8), energy=0.7, vol=(vmin, vmax, cs, counts, 0))
+    vol.offset[:] = [0.05, -0.1, 0.15]
+    vol.bias[:] = [0.02, 0.0, -0.03]
+    lights = [sd.lights[i] for i in range(sd.nlights)] + [vol]
+    me = sd.meshes[0]
+    me.parts[0]["mat"] = dict(me.parts[0]["mat"], lv_shading_mode=lv_mode)
+    out = scenes.SceneData([me], 1, lights, [[0, 1, 2, 3, 4, 5]], cells=cells, name=f"uv_sphere_volume{lv_mode}")
+    out.mv[:] = sd.mv
+    out.camera = sd.camera
+    return out
+
+
 def cases():
-    from tetra3d_gb300 import scenes
-    return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant()}
+    from tetra3d_gb300 import abi, scenes
+    return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant(),
+            "c1_volume_vertex": volume_variant(abi.LV_PER_VERTEX),
+            "c1_volume_normal": volume_variant(abi.LV_PER_VERTEX_WITH_NORMAL),
+            "c1_volume_object": volume_variant(abi.LV_PER_OBJECT)}
 
 
 def input_digest(S):
@@ -448,6 +559,10 @@ def input_digest(S):
         h.update(np.asarray([L["type"]], np.int64).tobytes())
         h.update(np.asarray([*L["color"], L["energy"], L["range"], *L["world_pos"]], F).tobytes())
         h.update(L["world_rot"].tobytes())
+        if L["type"] == 3:  # a light volume: its grid and cells
+            h.update(np.concatenate([L["vol_min"], L["vol_max"], L["cell_size"], L["offset"], L["bias"]]).tobytes())
+            h.update(np.asarray([*L["cell_count"], L["cell_first"], S["lv_mode"]], np.int64).tobytes())
+            h.update(np.ascontiguousarray(S["cells"]).tobytes())
     h.update(np.asarray([*S["cam_pos"], S["fov"], S["near"], S["far"], S["depth_margin"]], F).tobytes())
     h.update(np.asarray([S["width"], S["height"], S["sort_mode"], S["backface"]], np.int64).tobytes())
     return h.hexdigest()

@@ -1,8 +1,9 @@
 """The C++ oracle against a second, independent restatement of the whole vertex stage
 (tests/golden/make_c1_whole_path.py: numpy binary32, written directly from model.go:600-995,
-light.go:110-360, sortingTriangles.go:38-125 and camera.go:1646-1820), on the one-sphere
-scene (960 triangles, ambient + directional + point light) and on the same sphere with a
-non-uniform scale and five lights: draw order and every emitted float, bit for bit."""
+light.go:110-360 and :459-724, sortingTriangles.go:38-125 and camera.go:1646-1820), on the
+one-sphere scene (960 triangles, ambient + directional + point light), on the same sphere
+rotated with a non-uniform scale and five lights, and on that scene with a light volume in each
+of its three shading modes: draw order and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -14,7 +15,7 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_c1_whole_path as G  # noqa: E402
 
 FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
-CASES = ["c1", "c1_scaled_5lights"]
+CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object"]
 
 
 @pytest.fixture(scope="module")
@@ -63,6 +64,17 @@ def test_scaled_case_exercises_the_added_lights(scenes_):
     four = G.render(dict(S, lights=S["lights"][:4]))[2]
     assert (full != three).any(-1).sum() > 100
     assert np.array_equal(_bits(full), _bits(four))
+
+
+@pytest.mark.parametrize("name", ["c1_volume_vertex", "c1_volume_normal", "c1_volume_object"])
+def test_volume_cases_exercise_the_volume(scenes_, name):
+    """The light volume changes the colours of most visible corners in each shading mode (per
+    vertex, per vertex with the normal, per object), so the fixture covers the cell grid, the
+    index rounding, the offset and bias and each mode's containment test."""
+    S = G.scene_inputs(scenes_[name])
+    with_volume = G.render(S)[2]
+    without = G.render(dict(S, lights=S["lights"][:5]))[2]
+    assert (with_volume != without).any(-1).sum() > 900
 
 
 @pytest.mark.gpu
