@@ -24,7 +24,9 @@ fused multiply-add, no reductions), in the order the reference writes it:
   (camera.go:1613-1641); LightVolume.VertexLight (light.go:583-663) with the cell grid of
   LightVolumeResize (light.go:459-513), convertToXYZIndices (light.go:716-724) and
   Dimensions.Contains (mesh.go:82-84);
-- the emit loop (camera.go:1646-1820): screen position, UV, colour x lighting, depth.
+- the emit loop (camera.go:1646-1820): screen position, UV, colour x lighting, depth, and
+  the world's fog added to or multiplied into the colour when the depth is not rendered
+  (camera.go:1785-1812).
 
 Run from the repo root: python tests/golden/make_c1_whole_path.py
 """
@@ -227,6 +229,8 @@ def scene_inputs(sd):
         cam_rot=np.asarray(cam.world_rotation[:], F).reshape(4, 4), width=int(cam.width), height=int(cam.height),
         fov=F(cam.fov_y), near=F(cam.near_plane), far=F(cam.far_plane), depth_margin=F(cam.depth_margin),
         perspective=bool(cam.perspective), lighting_on=bool(cam.lighting_on), render_depth=bool(cam.render_depth),
+        fog_on=bool(cam.fog_on), fog_mode=int(cam.fog_mode), fog_range=np.asarray(cam.fog_range[:], F),
+        fog_color=np.asarray(cam.fog_color[:3], F),
         abi=abi)
 
 
@@ -491,6 +495,19 @@ def render(S):
         col[..., 2] *= lb[cor]
     dep = (Z[cor] + margin) / spread
     dep = np.where(dep < F(0), F(0), np.where(dep > F(1), F(1), dep)).astype(F)
+    if not S["render_depth"] and S["fog_on"] and S["fog_mode"] in (abi.FOG_ADD, abi.FOG_SUB):
+        # FogRange[0] + ((FogRange[1] - FogRange[0]) * 1 - depth), then added to or multiplied
+        # into the colour channels (camera.go:1800-1811)
+        f0, f1 = S["fog_range"]
+        fd = f0 + ((f1 - f0) * F(1) - dep)
+        fc = S["fog_color"]
+        for k in range(3):
+            if S["fog_mode"] == abi.FOG_ADD:
+                col[..., k] = col[..., k] + fc[k] * fd
+            else:
+                col[..., k] = col[..., k] * (fc[k] * fd)
+    if not S["render_depth"] and not S["fog_on"]:
+        dep = np.zeros_like(dep)  # no depth is computed (the stream holds 0)
     xyuv = np.stack([xs, ys, u, v], -1).astype(F)
     return order, xyuv, col.astype(F), dep
 
@@ -541,12 +558,27 @@ def volume_variant(lv_mode):
     return out
 
 
+def fog_variant(mode):
+    """The scaled five-light scene seen without depth rendering, with the world's fog on in mode
+    `mode` (range 0.15-0.85, a blue-grey colour)."""
+    sd = scaled_variant()
+    cam = sd.camera
+    cam.render_depth = 0
+    cam.fog_on = 1
+    cam.fog_mode = mode
+    cam.fog_range[:] = [0.15, 0.85]
+    cam.fog_color[:] = [0.4, 0.5, 0.9, 1.0]
+    sd.name = f"uv_sphere_fog{mode}"
+    return sd
+
+
 def cases():
     from tetra3d_gb300 import abi, scenes
     return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant(),
             "c1_volume_vertex": volume_variant(abi.LV_PER_VERTEX),
             "c1_volume_normal": volume_variant(abi.LV_PER_VERTEX_WITH_NORMAL),
-            "c1_volume_object": volume_variant(abi.LV_PER_OBJECT)}
+            "c1_volume_object": volume_variant(abi.LV_PER_OBJECT),
+            "c1_fog_add": fog_variant(abi.FOG_ADD), "c1_fog_sub": fog_variant(abi.FOG_SUB)}
 
 
 def input_digest(S):
@@ -565,6 +597,9 @@ def input_digest(S):
             h.update(np.ascontiguousarray(S["cells"]).tobytes())
     h.update(np.asarray([*S["cam_pos"], S["fov"], S["near"], S["far"], S["depth_margin"]], F).tobytes())
     h.update(np.asarray([S["width"], S["height"], S["sort_mode"], S["backface"]], np.int64).tobytes())
+    if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)
+        h.update(np.asarray([S["render_depth"], S["fog_on"], S["fog_mode"]], np.int64).tobytes())
+        h.update(np.concatenate([S["fog_range"], S["fog_color"]]).tobytes())
     return h.hexdigest()
 
 

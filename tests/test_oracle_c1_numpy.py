@@ -2,8 +2,9 @@
 (tests/golden/make_c1_whole_path.py: numpy binary32, written directly from model.go:600-995,
 light.go:110-360 and :459-724, sortingTriangles.go:38-125 and camera.go:1646-1820), on the
 one-sphere scene (960 triangles, ambient + directional + point light), on the same sphere
-rotated with a non-uniform scale and five lights, and on that scene with a light volume in each
-of its three shading modes: draw order and every emitted float, bit for bit."""
+rotated with a non-uniform scale and five lights, on that scene with a light volume in each
+of its three shading modes, and on it with the world's fog added or multiplied in: draw order
+and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -15,7 +16,8 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_c1_whole_path as G  # noqa: E402
 
 FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
-CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object"]
+CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
+         "c1_fog_sub"]
 
 
 @pytest.fixture(scope="module")
@@ -75,6 +77,15 @@ def test_volume_cases_exercise_the_volume(scenes_, name):
     with_volume = G.render(S)[2]
     without = G.render(dict(S, lights=S["lights"][:5]))[2]
     assert (with_volume != without).any(-1).sum() > 900
+
+
+@pytest.mark.parametrize("name", ["c1_fog_add", "c1_fog_sub"])
+def test_fog_cases_change_every_corner(scenes_, name):
+    """Fog on without depth rendering changes the colour of every visible corner."""
+    S = G.scene_inputs(scenes_[name])
+    fogged = G.render(S)[2]
+    plain = G.render(dict(S, fog_on=False, render_depth=True))[2]
+    assert (fogged != plain).any(-1).all()
 
 
 @pytest.mark.gpu
