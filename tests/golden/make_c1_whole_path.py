@@ -2,7 +2,9 @@
 (a UV sphere of 32 x 16 segments, 960 triangles, ambient + directional + point light,
 640x360, back-to-front sort), of the same scene with a non-uniform scale and two more
 point lights, and of that scene with a light volume (a grid of cells, an offset and a light
-bias) lighting the sphere per vertex, per vertex with the normal, and per object, computed by
+bias) lighting the sphere per vertex, per vertex with the normal, and per object, with fog,
+with fixed-normal and double-sided lighting, without backface culling, front-to-back and
+unsorted, and lit by a LightGroup, computed by
 a second restatement of the vertex stage written here in numpy binary32 arithmetic,
 independently of the C++ oracle, so the oracle can be checked against it bit for bit.
 
@@ -572,13 +574,32 @@ def fog_variant(mode):
     return sd
 
 
+def material_variant(name, light_list=None, lists=None, **mat):
+    """The scaled five-light scene with material options `mat` (lighting mode, backface culling,
+    sort mode) and, optionally, the model lit by a LightGroup (`light_list` >= 1 of `lists`)."""
+    sd = scaled_variant()
+    me = sd.meshes[0]
+    me.parts[0]["mat"] = dict(me.parts[0]["mat"], **mat)
+    if lists is not None:
+        sd.lists = lists
+    if light_list is not None:
+        sd.mv["light_list"][0] = light_list
+    sd.name = name
+    return sd
+
+
 def cases():
     from tetra3d_gb300 import abi, scenes
     return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant(),
             "c1_volume_vertex": volume_variant(abi.LV_PER_VERTEX),
             "c1_volume_normal": volume_variant(abi.LV_PER_VERTEX_WITH_NORMAL),
             "c1_volume_object": volume_variant(abi.LV_PER_OBJECT),
-            "c1_fog_add": fog_variant(abi.FOG_ADD), "c1_fog_sub": fog_variant(abi.FOG_SUB)}
+            "c1_fog_add": fog_variant(abi.FOG_ADD), "c1_fog_sub": fog_variant(abi.FOG_SUB),
+            "c1_fixed_normals": material_variant("c1_fixed_normals", lighting_mode=abi.LIGHTING_FIXED_NORMALS),
+            "c1_double_sided_nocull": material_variant("c1_double_sided_nocull", lighting_mode=abi.LIGHTING_DOUBLE_SIDED,
+                                                       backface_culling=0, sort_mode=abi.SORT_FRONT_TO_BACK),
+            "c1_unsorted_group": material_variant("c1_unsorted_group", light_list=1,
+                                                  lists=[[0, 1, 2, 3, 4], [0, 2, 3]], sort_mode=abi.SORT_NONE)}
 
 
 def input_digest(S):
@@ -597,6 +618,8 @@ def input_digest(S):
             h.update(np.ascontiguousarray(S["cells"]).tobytes())
     h.update(np.asarray([*S["cam_pos"], S["fov"], S["near"], S["far"], S["depth_margin"]], F).tobytes())
     h.update(np.asarray([S["width"], S["height"], S["sort_mode"], S["backface"]], np.int64).tobytes())
+    if S["lighting_mode"]:
+        h.update(np.asarray([S["lighting_mode"]], np.int64).tobytes())
     if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)
         h.update(np.asarray([S["render_depth"], S["fog_on"], S["fog_mode"]], np.int64).tobytes())
         h.update(np.concatenate([S["fog_range"], S["fog_color"]]).tobytes())

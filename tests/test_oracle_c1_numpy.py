@@ -3,8 +3,9 @@
 light.go:110-360 and :459-724, sortingTriangles.go:38-125 and camera.go:1646-1820), on the
 one-sphere scene (960 triangles, ambient + directional + point light), on the same sphere
 rotated with a non-uniform scale and five lights, on that scene with a light volume in each
-of its three shading modes, and on it with the world's fog added or multiplied in: draw order
-and every emitted float, bit for bit."""
+of its three shading modes, with the world's fog added or multiplied in, with fixed-normal and
+double-sided lighting, without backface culling, front-to-back and unsorted, and lit by a
+LightGroup: draw order and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -17,7 +18,7 @@ import make_c1_whole_path as G  # noqa: E402
 
 FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
-         "c1_fog_sub"]
+         "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
 
 
 @pytest.fixture(scope="module")
@@ -86,6 +87,20 @@ def test_fog_cases_change_every_corner(scenes_, name):
     fogged = G.render(S)[2]
     plain = G.render(dict(S, fog_on=False, render_depth=True))[2]
     assert (fogged != plain).any(-1).all()
+
+
+def test_material_and_group_cases_differ_from_the_base(scenes_):
+    """Fixed normals change the lit colours; double-sided lighting without backface culling keeps
+    all 960 triangles, front to back; the unsorted LightGroup case keeps triangle order and drops
+    two lights."""
+    base = G.render(G.scene_inputs(scenes_["c1_scaled_5lights"]))
+    fixed = G.render(G.scene_inputs(scenes_["c1_fixed_normals"]))
+    assert np.array_equal(fixed[0], base[0]) and (fixed[2] != base[2]).any(-1).sum() > 300
+    both = G.render(G.scene_inputs(scenes_["c1_double_sided_nocull"]))
+    assert len(both[0]) == 960
+    grp = G.render(G.scene_inputs(scenes_["c1_unsorted_group"]))
+    assert np.array_equal(grp[0], np.sort(grp[0])) and not np.array_equal(grp[0], base[0])
+    assert len(G.scene_inputs(scenes_["c1_unsorted_group"])["lights"]) == 3
 
 
 @pytest.mark.gpu
