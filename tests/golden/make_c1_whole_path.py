@@ -4,7 +4,8 @@
 point lights, and of that scene with a light volume (a grid of cells, an offset and a light
 bias) lighting the sphere per vertex, per vertex with the normal, and per object, with fog,
 with fixed-normal and double-sided lighting, without backface culling, front-to-back and
-unsorted, and lit by a LightGroup, computed by
+unsorted, lit by a LightGroup, and seen with perspective-corrected texture mapping, vertex
+snapping or lighting off, computed by
 a second restatement of the vertex stage written here in numpy binary32 arithmetic,
 independently of the C++ oracle, so the oracle can be checked against it bit for bit.
 
@@ -232,7 +233,8 @@ def scene_inputs(sd):
         fov=F(cam.fov_y), near=F(cam.near_plane), far=F(cam.far_plane), depth_margin=F(cam.depth_margin),
         perspective=bool(cam.perspective), lighting_on=bool(cam.lighting_on), render_depth=bool(cam.render_depth),
         fog_on=bool(cam.fog_on), fog_mode=int(cam.fog_mode), fog_range=np.asarray(cam.fog_range[:], F),
-        fog_color=np.asarray(cam.fog_color[:3], F),
+        fog_color=np.asarray(cam.fog_color[:3], F), pcorrect=bool(cam.perspective_corrected),
+        snap=F(cam.vertex_snapping),
         abi=abi)
 
 
@@ -339,9 +341,10 @@ def volume_cells(S, L, M, P, N):
     return r, g, b, contains
 
 
-def render(S):
+def render(S, want_custom0=False):
     """The vertex stage for the scene's one model and one mesh part: returns (triangle order, xyuv,
-    rgba, depth) of the visible triangles in draw order."""
+    rgba, depth) of the visible triangles in draw order, and Custom0 (1 / w per corner under
+    perspective-corrected texture mapping, else None) when want_custom0."""
     abi = S["abi"]
     P, N, UV, idx = S["positions"], S["normals"], S["uvs"], S["indices"]
     W, H = S["width"], S["height"]
@@ -364,6 +367,11 @@ def render(S):
     icam = [rc[a] + ip[a] * (F(1) / isc[a]) for a in range(3)]
     clip = multvecw(mvp, (P[:, 0], P[:, 1], P[:, 2]))  # per vertex, float32 arrays
     X, Y, Z, Wc = clip
+    if S["snap"] > F(0):  # Camera.VertexSnapping (model.go:813-818): math32.Round = half away from zero
+        sn = S["snap"]
+        X = (round_half_away(X * sn).astype(F) / sn).astype(F)
+        Y = (round_half_away(Y * sn).astype(F) / sn).astype(F)
+        Z = (round_half_away(Z * sn).astype(F) / sn).astype(F)
     a, b, c = idx[:, 0], idx[:, 1], idx[:, 2]
     inb = np.zeros(len(idx), bool)
     for k in (a, b, c):
@@ -484,8 +492,14 @@ def render(S):
     w = np.where(w < F(0), F(0.001), w).astype(F)
     xs = (X[cor] / w) * F(W) + F(W) / F(2)
     ys = (Y[cor] / -w) * F(H) + F(H) / F(2)
-    u = UV[cor, 0] * tw
-    v = (F(1) - UV[cor, 1]) * th
+    if S["pcorrect"]:  # camera.go:1689-1704: UV over w, and Custom0 = 1 / w
+        u = (UV[cor, 0] / w) * tw
+        v = ((F(1) - UV[cor, 1]) / w) * th
+        custom0 = (F(1) / w).astype(F)
+    else:
+        u = UV[cor, 0] * tw
+        v = (F(1) - UV[cor, 1]) * th
+        custom0 = None
     if S["colors"] is not None:
         col = S["colors"][cor] * mp
     else:
@@ -511,6 +525,8 @@ def render(S):
     if not S["render_depth"] and not S["fog_on"]:
         dep = np.zeros_like(dep)  # no depth is computed (the stream holds 0)
     xyuv = np.stack([xs, ys, u, v], -1).astype(F)
+    if want_custom0:
+        return order, xyuv, col.astype(F), dep, custom0
     return order, xyuv, col.astype(F), dep
 
 
@@ -588,6 +604,27 @@ def material_variant(name, light_list=None, lists=None, **mat):
     return sd
 
 
+def camera_variant(name, tex=None, **cam):
+    """The scaled five-light scene with camera options `cam` (perspective-corrected texture
+    mapping, vertex snapping, lighting off) and, optionally, a texture size for the material."""
+    sd = scaled_variant()
+    if tex is not None:
+        me = sd.meshes[0]
+        me.parts[0]["mat"] = dict(me.parts[0]["mat"], tex_w=float(tex[0]), tex_h=float(tex[1]))
+    for k, v in cam.items():
+        setattr(sd.camera, k, v)
+    sd.name = name
+    return sd
+
+
+def cpu_cases():
+    """Cases checked against the C++ oracle on the CPU only (the GPU's parity for these camera
+    options is checked against the oracle by the feature-scene tests)."""
+    return {"c1_pcorrect": camera_variant("c1_pcorrect", tex=(256, 128), perspective_corrected=1),
+            "c1_snap": camera_variant("c1_snap", vertex_snapping=64.0),
+            "c1_unlit": camera_variant("c1_unlit", lighting_on=0)}
+
+
 def cases():
     from tetra3d_gb300 import abi, scenes
     return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant(),
@@ -620,6 +657,9 @@ def input_digest(S):
     h.update(np.asarray([S["width"], S["height"], S["sort_mode"], S["backface"]], np.int64).tobytes())
     if S["lighting_mode"]:
         h.update(np.asarray([S["lighting_mode"]], np.int64).tobytes())
+    if S["pcorrect"] or S["snap"] > F(0) or not S["lighting_on"]:
+        h.update(np.asarray([S["pcorrect"], S["lighting_on"]], np.int64).tobytes())
+        h.update(np.asarray([S["snap"], *S["tex"]], F).tobytes())
     if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)
         h.update(np.asarray([S["render_depth"], S["fog_on"], S["fog_mode"]], np.int64).tobytes())
         h.update(np.concatenate([S["fog_range"], S["fog_color"]]).tobytes())
@@ -628,13 +668,15 @@ def input_digest(S):
 
 def main():
     out = {}
-    for name, sd in cases().items():
+    for name, sd in {**cases(), **cpu_cases()}.items():
         S = scene_inputs(sd)
-        order, xyuv, rgba, depth = render(S)
+        order, xyuv, rgba, depth, custom0 = render(S, want_custom0=True)
         out[f"{name}_order"] = order.astype(np.uint32)
         out[f"{name}_xyuv"] = xyuv
         out[f"{name}_rgba"] = rgba
         out[f"{name}_depth"] = depth
+        if custom0 is not None:
+            out[f"{name}_custom0"] = custom0
         out[f"{name}_digest"] = np.frombuffer(bytes.fromhex(input_digest(S)), np.uint8)
         print(name, "visible", len(order))
     np.savez_compressed(os.path.join(HERE, "c1_whole_path.npz"), **out)

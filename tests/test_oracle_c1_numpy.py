@@ -4,8 +4,9 @@ light.go:110-360 and :459-724, sortingTriangles.go:38-125 and camera.go:1646-182
 one-sphere scene (960 triangles, ambient + directional + point light), on the same sphere
 rotated with a non-uniform scale and five lights, on that scene with a light volume in each
 of its three shading modes, with the world's fog added or multiplied in, with fixed-normal and
-double-sided lighting, without backface culling, front-to-back and unsorted, and lit by a
-LightGroup: draw order and every emitted float, bit for bit."""
+double-sided lighting, without backface culling, front-to-back and unsorted, lit by a
+LightGroup, and (oracle only) seen with perspective-corrected texture mapping (Custom0
+included), vertex snapping or lighting off: draw order and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -19,6 +20,9 @@ import make_c1_whole_path as G  # noqa: E402
 FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
          "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
+CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit"]  # the oracle only (the GPU's parity for these
+# camera options is checked against the oracle by the feature-scene tests)
+ALL = CASES + CPU_CASES
 
 
 @pytest.fixture(scope="module")
@@ -28,25 +32,26 @@ def fixture():
 
 @pytest.fixture(scope="module")
 def scenes_():
-    return G.cases()
+    return {**G.cases(), **G.cpu_cases()}
 
 
 def _bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", ALL)
 def test_restatement_reproduces_fixture(fixture, scenes_, name):
     S = G.scene_inputs(scenes_[name])
     assert bytes(fixture[f"{name}_digest"]).hex() == G.input_digest(S), "scene inputs changed"
-    order, xyuv, rgba, depth = G.render(S)
-    assert len(order) > 300
+    order, xyuv, rgba, depth, custom0 = G.render(S, want_custom0=True)
+    assert len(order) > 200
     assert np.array_equal(order, fixture[f"{name}_order"])
-    for k, v in (("xyuv", xyuv), ("rgba", rgba), ("depth", depth)):
-        assert np.array_equal(_bits(v), _bits(fixture[f"{name}_{k}"])), k
+    for k, v in (("xyuv", xyuv), ("rgba", rgba), ("depth", depth), ("custom0", custom0)):
+        if v is not None:
+            assert np.array_equal(_bits(v), _bits(fixture[f"{name}_{k}"])), k
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", ALL)
 def test_cpp_oracle_matches_numpy_restatement(built, fixture, scenes_, name):
     from oracle import pyoracle
     sd = scenes_[name]
@@ -55,6 +60,8 @@ def test_cpp_oracle_matches_numpy_restatement(built, fixture, scenes_, name):
     assert np.array_equal(ref.tri_index.astype(np.uint32), fixture[f"{name}_order"]), "draw order"
     for k in ("xyuv", "rgba", "depth"):
         assert np.array_equal(_bits(getattr(ref, k)), _bits(fixture[f"{name}_{k}"])), k
+    if f"{name}_custom0" in fixture:
+        assert np.array_equal(_bits(ref.custom0), _bits(fixture[f"{name}_custom0"])), "custom0"
 
 
 def test_scaled_case_exercises_the_added_lights(scenes_):
