@@ -5,7 +5,7 @@ point lights, and of that scene with a light volume (a grid of cells, an offset 
 bias) lighting the sphere per vertex, per vertex with the normal, and per object, with fog,
 with fixed-normal and double-sided lighting, without backface culling, front-to-back and
 unsorted, lit by a LightGroup, and seen with perspective-corrected texture mapping, vertex
-snapping or lighting off, computed by
+snapping or lighting off, or through an orthographic camera, computed by
 a second restatement of the vertex stage written here in numpy binary32 arithmetic,
 independently of the C++ oracle, so the oracle can be checked against it bit for bit.
 
@@ -196,6 +196,21 @@ def projection(fov, near, far, w, h):
     return P
 
 
+def projection_ortho(near, far, w, h, scale):
+    """Camera.Projection for an orthographic camera (camera.go:669-675): NewProjectionMatrix4Orthographic
+    (matrix.go:609-616) with right / left = +-orthoScale and top / bottom = +-(h / w) * orthoScale."""
+    asr = F(h) / F(w)
+    right, left = F(1) * scale, F(-1) * scale
+    top, bottom = asr * scale, -asr * scale
+    near, far = F(near), F(far)
+    P = np.zeros((4, 4), F)
+    P[0, 0] = F(2) / (right - left)
+    P[1, 1] = F(2) / (top - bottom)
+    P[2, 2] = F(-2) / (far - near)
+    P[3, 3] = F(1)
+    return P
+
+
 # ---- the scene ----
 
 def scene_inputs(sd):
@@ -234,7 +249,7 @@ def scene_inputs(sd):
         perspective=bool(cam.perspective), lighting_on=bool(cam.lighting_on), render_depth=bool(cam.render_depth),
         fog_on=bool(cam.fog_on), fog_mode=int(cam.fog_mode), fog_range=np.asarray(cam.fog_range[:], F),
         fog_color=np.asarray(cam.fog_color[:3], F), pcorrect=bool(cam.perspective_corrected),
-        snap=F(cam.vertex_snapping),
+        snap=F(cam.vertex_snapping), ortho_scale=F(cam.ortho_scale),
         abi=abi)
 
 
@@ -256,6 +271,14 @@ def in_frustum(S, M, dmin, dmax):
     pcz = dot(diff, [-fwd[0], -fwd[1], -fwd[2]])
     if pcz > S["far"] + radius or pcz < S["near"] - radius:
         return False
+    if not S["perspective"]:  # the orthographic box (camera.go:963-979)
+        width = S["ortho_scale"]
+        height = width / (F(S["width"]) / F(S["height"]))
+        pcy = dot(diff, up)
+        if -height / F(2) - radius > pcy or pcy > height / F(2) + radius:
+            return False
+        pcx = dot(diff, right)
+        return not (-width / F(2) - radius > pcx or pcx > width / F(2) + radius)
     angle = (S["fov"] * F(3.1415)) / F(360)
     tang = F(math.tan(float(angle)))
     fy = F(1) / F(math.cos(float(angle)))
@@ -352,7 +375,10 @@ def render(S, want_custom0=False):
     # camera: view = T(-pos) x R^T, vp = view x projection (camera.go:638-648, :1329)
     cp = S["cam_pos"]
     view = mmul(translate(-cp[0], -cp[1], -cp[2]), transposed(S["cam_rot"]))
-    vp = mmul(view, projection(S["fov"], near, far, W, H))
+    if S["perspective"]:
+        vp = mmul(view, projection(S["fov"], near, far, W, H))
+    else:
+        vp = mmul(view, projection_ortho(near, far, W, H, S["ortho_scale"]))
     # model transform and the culling sphere
     M = node_transform(S["model_pos"], S["model_scale"], S["model_rot"])
     dmin = [F(P[:, a].min()) for a in range(3)]  # Mesh.UpdateDimensions
@@ -622,7 +648,10 @@ def cpu_cases():
     options is checked against the oracle by the feature-scene tests)."""
     return {"c1_pcorrect": camera_variant("c1_pcorrect", tex=(256, 128), perspective_corrected=1),
             "c1_snap": camera_variant("c1_snap", vertex_snapping=64.0),
-            "c1_unlit": camera_variant("c1_unlit", lighting_on=0)}
+            "c1_unlit": camera_variant("c1_unlit", lighting_on=0),
+            "c1_ortho": camera_variant("c1_ortho", perspective=0, ortho_scale=3.0),
+            "c1_ortho_pcorrect": camera_variant("c1_ortho_pcorrect", tex=(64, 64), perspective=0, ortho_scale=2.5,
+                                                perspective_corrected=1)}
 
 
 def cases():
@@ -660,6 +689,8 @@ def input_digest(S):
     if S["pcorrect"] or S["snap"] > F(0) or not S["lighting_on"]:
         h.update(np.asarray([S["pcorrect"], S["lighting_on"]], np.int64).tobytes())
         h.update(np.asarray([S["snap"], *S["tex"]], F).tobytes())
+    if not S["perspective"]:
+        h.update(np.asarray([0, S["ortho_scale"]], F).tobytes())
     if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)
         h.update(np.asarray([S["render_depth"], S["fog_on"], S["fog_mode"]], np.int64).tobytes())
         h.update(np.concatenate([S["fog_range"], S["fog_color"]]).tobytes())

@@ -6,7 +6,8 @@ rotated with a non-uniform scale and five lights, on that scene with a light vol
 of its three shading modes, with the world's fog added or multiplied in, with fixed-normal and
 double-sided lighting, without backface culling, front-to-back and unsorted, lit by a
 LightGroup, and (oracle only) seen with perspective-corrected texture mapping (Custom0
-included), vertex snapping or lighting off: draw order and every emitted float, bit for bit."""
+included), vertex snapping, lighting off or an orthographic camera: draw order and every
+emitted float, bit for bit."""
 import os
 import sys
 
@@ -20,7 +21,7 @@ import make_c1_whole_path as G  # noqa: E402
 FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
          "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
-CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit"]  # the oracle only (the GPU's parity for these
+CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit", "c1_ortho", "c1_ortho_pcorrect"]  # the oracle only (the GPU's parity for these
 # camera options is checked against the oracle by the feature-scene tests)
 ALL = CASES + CPU_CASES
 
