@@ -5,7 +5,8 @@ point lights, and of that scene with a light volume (a grid of cells, an offset 
 bias) lighting the sphere per vertex, per vertex with the normal, and per object, with fog,
 with fixed-normal and double-sided lighting, without backface culling, front-to-back and
 unsorted, lit by a LightGroup, and seen with perspective-corrected texture mapping, vertex
-snapping or lighting off, or through an orthographic camera, computed by
+snapping or lighting off, or through an orthographic camera, and a frame of six such
+models (two outside the frustum, three lit by a LightGroup), computed by
 a second restatement of the vertex stage written here in numpy binary32 arithmetic,
 independently of the C++ oracle, so the oracle can be checked against it bit for bit.
 
@@ -213,11 +214,12 @@ def projection_ortho(near, far, w, h, scale):
 
 # ---- the scene ----
 
-def scene_inputs(sd):
-    """The binary32 inputs the restatement reads from a one-model SceneData."""
+def scene_inputs(sd, model=0):
+    """The binary32 inputs the restatement reads from a SceneData for one of its models (a model
+    of a one-part mesh)."""
     from tetra3d_gb300 import abi
-    assert sd.nmodels == 1
-    mv = sd.mv[0]
+    assert 0 <= model < sd.nmodels
+    mv = sd.mv[model]
     me = sd.meshes[int(mv["mesh"])]
     mat = me.parts[0]["mat"]
     cam = sd.camera
@@ -654,6 +656,38 @@ def cpu_cases():
                                                 perspective_corrected=1)}
 
 
+def render_frame(sd):
+    """Every model of a scene of opaque one-part models, depth rendered: the solid pass draws the
+    render pairs in model order (camera.go:1343-1457, :2057-2106), each pair's stream the
+    restatement's for that model (nothing for a model outside the frustum). Returns
+    [(model, triangle order, xyuv, rgba, depth)] in draw order."""
+    out = []
+    for m in range(sd.nmodels):
+        S = scene_inputs(sd, m)
+        assert S["render_depth"]
+        out.append((m,) + tuple(render(S)))
+    return out
+
+
+def multi_model_variant():
+    """Six spheres of the five-light scene's mesh: different positions (one behind the camera and
+    one far to the side, both culled by SphereInFrustum), non-uniform scales, rotations and model
+    colours, half of them lit by a LightGroup of three lights."""
+    from tetra3d_gb300 import scenes
+    base = scaled_variant()
+    rng = np.random.Generator(np.random.PCG64(5))
+    lights = [base.lights[i] for i in range(base.nlights)]
+    sd = scenes.SceneData([base.meshes[0]], 6, lights, [[0, 1, 2, 3, 4], [0, 2, 3]], name="six_spheres")
+    pos = np.array([(0, 0, -5), (-2.2, 0.8, -7), (2.5, -0.6, -9), (0, 0, 6), (40, 0, -6), (1.0, 1.4, -4)], F)
+    scl = rng.uniform(0.5, 1.4, (6, 3)).astype(F)
+    rot = scenes.quat_to_mat(scenes.random_quats(rng, 6))
+    scenes.set_models_trs(sd, np.zeros(6, np.uint32), pos, scl, rot)
+    sd.mv["color"] = np.concatenate([rng.uniform(0.6, 1.0, (6, 3)), np.ones((6, 1))], 1).astype(F)
+    sd.mv["light_list"] = np.array([-1, 1, -1, 1, -1, 1], np.int32)
+    sd.camera = base.camera
+    return sd
+
+
 def cases():
     from tetra3d_gb300 import abi, scenes
     return {"c1": scenes.uv_sphere_scene(1), "c1_scaled_5lights": scaled_variant(),
@@ -697,8 +731,23 @@ def input_digest(S):
     return h.hexdigest()
 
 
+def frame_cases():
+    """Multi-model cases, checked against the C++ oracle pair by pair."""
+    return {"six_spheres": multi_model_variant()}
+
+
 def main():
     out = {}
+    for name, sd in frame_cases().items():
+        parts = render_frame(sd)
+        out[f"{name}_counts"] = np.array([len(p[1]) for p in parts], np.uint32)
+        out[f"{name}_order"] = np.concatenate([p[1] for p in parts]).astype(np.uint32)
+        for k, i in (("xyuv", 2), ("rgba", 3), ("depth", 4)):
+            out[f"{name}_{k}"] = np.concatenate([p[i] for p in parts])
+        out[f"{name}_digest"] = np.frombuffer(bytes.fromhex(
+            hashlib.sha256("".join(input_digest(scene_inputs(sd, m)) for m in range(sd.nmodels)).encode()).hexdigest()),
+            np.uint8)
+        print(name, "visible per model", out[f"{name}_counts"].tolist())
     for name, sd in {**cases(), **cpu_cases()}.items():
         S = scene_inputs(sd)
         order, xyuv, rgba, depth, custom0 = render(S, want_custom0=True)
