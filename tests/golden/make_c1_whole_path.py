@@ -656,17 +656,42 @@ def cpu_cases():
                                                 perspective_corrected=1)}
 
 
+def is_transparent(md, mat):
+    """Model.isTransparent (model.go:1274-1282) with the default source-over blend."""
+    from tetra3d_gb300 import abi
+    a = F(md["color"][3])
+    if mat["present"]:
+        mat_t = (mat["transparency_mode"] == abi.TRANSPARENCY_TRANSPARENT or not mat["blend_source_over"] or
+                 (mat["transparency_mode"] == abi.TRANSPARENCY_AUTO and F(mat["color"][3]) < F(0.999)))
+        return bool(mat_t or (mat["transparency_mode"] != abi.TRANSPARENCY_OPAQUE and a < F(0.999)))
+    return bool(a < F(0.999))
+
+
 def render_frame(sd):
-    """Every model of a scene of opaque one-part models, depth rendered: the solid pass draws the
-    render pairs in model order (camera.go:1343-1457, :2057-2106), each pair's stream the
+    """Every model of a scene of one-part models, depth rendered: the solid pass draws its render
+    pairs in model order, then the transparent pass by RenderOrder ascending and, within one
+    order, by the squared camera distance to the model (Vector3.DistanceSquaredTo,
+    vector.go:242-247) far to near (camera.go:1343-1457, :2050-2106). Each pair's stream is the
     restatement's for that model (nothing for a model outside the frustum). Returns
     [(model, triangle order, xyuv, rgba, depth)] in draw order."""
-    out = []
+    solids, transparents = [], []
     for m in range(sd.nmodels):
         S = scene_inputs(sd, m)
         assert S["render_depth"]
-        out.append((m,) + tuple(render(S)))
-    return out
+        md = sd.mv[m]
+        mat = sd.meshes[int(md["mesh"])].parts[0]["mat"]
+        item = (m,) + tuple(render(S))
+        if is_transparent(md, mat):
+            wp = np.asarray(md["transform"], F).reshape(4, 4)[3, :3]  # Model.WorldPosition
+            cp = S["cam_pos"]
+            dx, dy, dz = F(cp[0] - wp[0]), F(cp[1] - wp[1]), F(cp[2] - wp[2])
+            dist = (dx * dx + dy * dy) + dz * dz
+            order = int(mat["render_order"]) if mat["present"] else 0
+            transparents.append(((order, -float(dist)), item))
+        else:
+            solids.append(item)
+    transparents.sort(key=lambda t: t[0])  # a strict weak order: any stable sort agrees
+    return solids + [t[1] for t in transparents]
 
 
 def multi_model_variant():
@@ -731,15 +756,26 @@ def input_digest(S):
     return h.hexdigest()
 
 
+def transparent_variant():
+    """The six-sphere frame with two models half transparent (model alpha 0.5): they move to the
+    transparent pass, far one first."""
+    sd = multi_model_variant()
+    sd.mv["color"][1, 3] = 0.5
+    sd.mv["color"][5, 3] = 0.5
+    sd.name = "six_spheres_transparent"
+    return sd
+
+
 def frame_cases():
     """Multi-model cases, checked against the C++ oracle pair by pair."""
-    return {"six_spheres": multi_model_variant()}
+    return {"six_spheres": multi_model_variant(), "six_spheres_transparent": transparent_variant()}
 
 
 def main():
     out = {}
     for name, sd in frame_cases().items():
         parts = render_frame(sd)
+        out[f"{name}_models"] = np.array([p[0] for p in parts], np.uint32)
         out[f"{name}_counts"] = np.array([len(p[1]) for p in parts], np.uint32)
         out[f"{name}_order"] = np.concatenate([p[1] for p in parts]).astype(np.uint32)
         for k, i in (("xyuv", 2), ("rgba", 3), ("depth", 4)):

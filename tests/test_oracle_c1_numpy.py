@@ -128,28 +128,34 @@ def test_gpu_matches_numpy_restatement(ctx, fixture, scenes_, name):
         ctx.release(sid)
 
 
-@pytest.mark.parametrize("name", ["six_spheres"])
+FRAMES = ["six_spheres", "six_spheres_transparent"]
+
+
+@pytest.mark.parametrize("name", FRAMES)
 def test_frame_restatement_reproduces_fixture(fixture, name):
     import hashlib
     sd = G.frame_cases()[name]
     digest = hashlib.sha256("".join(G.input_digest(G.scene_inputs(sd, m)) for m in range(sd.nmodels)).encode())
     assert bytes(fixture[f"{name}_digest"]).hex() == digest.hexdigest(), "scene inputs changed"
     parts = G.render_frame(sd)
+    assert np.array_equal(np.array([p[0] for p in parts], np.uint32), fixture[f"{name}_models"])
     assert np.array_equal(np.array([len(p[1]) for p in parts], np.uint32), fixture[f"{name}_counts"])
     assert np.array_equal(np.concatenate([p[1] for p in parts]).astype(np.uint32), fixture[f"{name}_order"])
     for k, i in (("xyuv", 2), ("rgba", 3), ("depth", 4)):
         assert np.array_equal(_bits(np.concatenate([p[i] for p in parts])), _bits(fixture[f"{name}_{k}"])), k
 
 
-@pytest.mark.parametrize("name", ["six_spheres"])
+@pytest.mark.parametrize("name", FRAMES)
 def test_cpp_oracle_matches_frame_restatement(built, fixture, name):
-    """Six models of one scene: the oracle's render pairs in draw order, the two the frustum test
-    drops empty, and every other pair's triangles and floats equal to the restatement's."""
+    """Six models of one scene (two of them transparent in the second frame): the oracle's render
+    pairs in draw order (solids in model order, then transparents far to near), the two the
+    frustum test drops empty, and every other pair's triangles and floats equal to the
+    restatement's."""
     from oracle import pyoracle
     sd = G.frame_cases()[name]
     ref = pyoracle.render(sd, sd.camera)
     assert ref.culled_models == 2
-    assert [s["model"] for s in ref.segments] == list(range(sd.nmodels))
+    assert np.array_equal(np.array([s["model"] for s in ref.segments], np.uint32), fixture[f"{name}_models"])
     assert np.array_equal(np.array([s["count"] for s in ref.segments], np.uint32), fixture[f"{name}_counts"])
     assert np.array_equal(ref.tri_index.astype(np.uint32), fixture[f"{name}_order"]), "draw order"
     for k in ("xyuv", "rgba", "depth"):
