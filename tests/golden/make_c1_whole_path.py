@@ -252,15 +252,20 @@ def scene_inputs(sd, model=0):
         fog_on=bool(cam.fog_on), fog_mode=int(cam.fog_mode), fog_range=np.asarray(cam.fog_range[:], F),
         fog_color=np.asarray(cam.fog_color[:3], F), pcorrect=bool(cam.perspective_corrected),
         snap=F(cam.vertex_snapping), ortho_scale=F(cam.ortho_scale),
+        skinned=bool(mv["skinned"]), bone_first=int(mv["bone_first"]),
+        joints=None if me.joints is None else np.asarray(me.joints, np.int64),
+        weights=None if me.weights is None else np.asarray(me.weights, F),
+        bones=None if not bool(mv["skinned"]) else np.asarray(sd.bones, F).reshape(-1, 4, 4),
         abi=abi)
 
 
-def in_frustum(S, M, dmin, dmax):
+def in_frustum(S, M, dmin, dmax, skinned=False):
     """Camera.SphereInFrustum for the model's culling sphere as Model.onTransformUpdate places it
     (model.go:141-181): position + (rotation x Dimensions.Center()) * scale, radius = MaxSpan of the
     scaled Dimensions / 2; the sphere node itself is unscaled (colliderSphere.go:51-60)."""
     pos, scl, rot = decompose(M)
-    centre = [(dmax[a] + dmin[a]) / F(2) for a in range(3)]
+    # a skinned model's sphere sits on the model position: its centre stays the zero vector
+    centre = [F(0)] * 3 if skinned else [(dmax[a] + dmin[a]) / F(2) for a in range(3)]
     cr = multvec(rot, centre)
     wpos = [pos[a] + cr[a] * scl[a] for a in range(3)]
     lo = [dmin[a] * scl[a] for a in range(3)]
@@ -295,6 +300,31 @@ def in_frustum(S, M, dmin, dmax):
     d = fx * radius
     pcx = dot(diff, right)
     return not (pcx > pcz + d or pcx < -pcz - d)
+
+
+def skin_vertices(S):
+    """Model.skinVertex (model.go:559-594) for every vertex: the skin matrix starts at zero, each
+    non-zero weight adds the bone influence scaled by it element by element (Matrix4.Add / Scale,
+    matrix.go:639-661), and a weight of exactly 1 replaces the sum and ends the loop; the
+    position goes through the matrix, the normal through it with its last row set to (0, 0, 0, 1)."""
+    P, N = S["positions"], S["normals"]
+    J, Wt, B = S["joints"], S["weights"], S["bones"]
+    nv = len(P)
+    m = np.zeros((nv, 4, 4), F)
+    done = np.zeros(nv, bool)
+    for k in range(4):
+        w = Wt[:, k]
+        bone = B[S["bone_first"] + J[:, k]]
+        one = ~done & (w == F(1))
+        add = ~done & (w != F(0)) & ~one
+        m = np.where(add[:, None, None], (m + bone * w[:, None, None]).astype(F), m)
+        m = np.where(one[:, None, None], bone, m)
+        done |= one
+    pos = [((P[:, 0] * m[:, 0, c] + P[:, 1] * m[:, 1, c]) + P[:, 2] * m[:, 2, c]) + m[:, 3, c] for c in range(3)]
+    mn = m.copy()
+    mn[:, 3, :] = np.array([0, 0, 0, 1], F)
+    nrm = [((N[:, 0] * mn[:, 0, c] + N[:, 1] * mn[:, 1, c]) + N[:, 2] * mn[:, 2, c]) + mn[:, 3, c] for c in range(3)]
+    return np.stack(pos, 1).astype(F), np.stack(nrm, 1).astype(F)
 
 
 def grid_counts(vmin, vmax, cs):
@@ -386,14 +416,19 @@ def render(S, want_custom0=False):
     dmin = [F(P[:, a].min()) for a in range(3)]  # Mesh.UpdateDimensions
     dmax = [F(P[:, a].max()) for a in range(3)]
     maxspan = mag3(dmax[0] - dmin[0], dmax[1] - dmin[1], dmax[2] - dmin[2])
-    if not in_frustum(S, M, dmin, dmax):
+    skinned = S["skinned"]
+    if not in_frustum(S, M, dmin, dmax, skinned):
         return np.zeros(0, np.int64), np.zeros((0, 3, 4), F), np.zeros((0, 3, 4), F), np.zeros((0, 3), F)
     # ProcessVertices
     mvp = mmul(M, vp)
     ip, isc, ir = decompose(inverted(M))
     rc = multvec(ir, cp)
     icam = [rc[a] + ip[a] * (F(1) / isc[a]) for a in range(3)]
-    clip = multvecw(mvp, (P[:, 0], P[:, 1], P[:, 2]))  # per vertex, float32 arrays
+    if skinned:  # world-space vertices through the skin, then VP alone (model.go:755-770)
+        Pw, Nw = skin_vertices(S)
+        clip = multvecw(vp, (Pw[:, 0], Pw[:, 1], Pw[:, 2]))
+    else:
+        clip = multvecw(mvp, (P[:, 0], P[:, 1], P[:, 2]))  # per vertex, float32 arrays
     X, Y, Z, Wc = clip
     if S["snap"] > F(0):  # Camera.VertexSnapping (model.go:813-818): math32.Round = half away from zero
         sn = S["snap"]
@@ -414,8 +449,12 @@ def render(S, want_custom0=False):
         n0x, n0y = sx[a] - sx[b], sy[a] - sy[b]
         n1x, n1y = sx[b] - sx[c], sy[b] - sy[c]
         vis &= ~((n0x * n1y) - (n1x * n0y) < F(0))
-    ctr = [((P[a, k] + P[b, k]) + P[c, k]) / F(3) for k in range(3)]  # Triangle.RecalculateCenter
-    dx, dy, dz = icam[0] - ctr[0], icam[1] - ctr[1], icam[2] - ctr[2]
+    if skinned:  # the skinned centre, summed from zero, against the world camera (model.go:839-863, :941-946)
+        ctr = [(((F(0) + Pw[a, k]) + Pw[b, k]) + Pw[c, k]) / F(3) for k in range(3)]
+        dx, dy, dz = cp[0] - ctr[0], cp[1] - ctr[1], cp[2] - ctr[2]
+    else:
+        ctr = [((P[a, k] + P[b, k]) + P[c, k]) / F(3) for k in range(3)]  # Triangle.RecalculateCenter
+        dx, dy, dz = icam[0] - ctr[0], icam[1] - ctr[1], icam[2] - ctr[2]
     depth = (dx * dx + dy * dy) + dz * dz
     vis &= np.isfinite(depth)
     tris = np.nonzero(vis)[0]
@@ -444,8 +483,12 @@ def render(S, want_custom0=False):
     if lighting:
         mpos = [M[3, 0], M[3, 1], M[3, 2]]  # Model.WorldPosition
         mrot_inv_t = transposed(inverted(S["model_rot"]))  # DirectionalLight.beginModel
-        vx, vy, vz = P[:, 0], P[:, 1], P[:, 2]
-        nx, ny, nz = N[:, 0], N[:, 1], N[:, 2]
+        if skinned:  # the lights work on the skinned world-space vertices (light.go:183-186, :334-343)
+            vx, vy, vz = Pw[:, 0], Pw[:, 1], Pw[:, 2]
+            nx, ny, nz = Nw[:, 0], Nw[:, 1], Nw[:, 2]
+        else:
+            vx, vy, vz = P[:, 0], P[:, 1], P[:, 2]
+            nx, ny, nz = N[:, 0], N[:, 1], N[:, 2]
         for L in S["lights"]:
             col, e = L["color"], L["energy"]
             if L["type"] == abi.LIGHT_AMBIENT:
@@ -455,6 +498,8 @@ def render(S, want_custom0=False):
                 fwd = unit3(L["world_rot"][2, :3])  # WorldRotation().Forward()
                 if S["lighting_mode"] == abi.LIGHTING_FIXED_NORMALS:
                     wn = [np.full(nv, fwd[0], F), np.full(nv, fwd[1], F), np.full(nv, fwd[2], F)]
+                elif skinned:
+                    wn = [nx, ny, nz]
                 else:
                     wn = multvec(mrot_inv_t, (nx, ny, nz))
                 df = (wn[0] * fwd[0] + wn[1] * fwd[1]) + wn[2] * fwd[2]
@@ -473,9 +518,12 @@ def render(S, want_custom0=False):
                     ddx, ddy, ddz = mpos[0] - lp[0], mpos[1] - lp[1], mpos[2] - lp[2]
                     if (ddx * ddx + ddy * ddy) + ddz * ddz > dist * dist:
                         continue
-                p_, s_, r_ = decompose(inverted(M))  # PointLight.beginModel
-                rq = multvec(r_, lp)
-                wp = [rq[k] + p_[k] * (F(1) / s_[k]) for k in range(3)]
+                if skinned:  # PointLight.beginModel: the light's own world position
+                    wp = [F(lp[0]), F(lp[1]), F(lp[2])]
+                else:
+                    p_, s_, r_ = decompose(inverted(M))  # PointLight.beginModel
+                    rq = multvec(r_, lp)
+                    wp = [rq[k] + p_[k] * (F(1) / s_[k]) for k in range(3)]
                 ex, ey, ez = wp[0] - vx, wp[1] - vy, wp[2] - vz
                 dist2 = (ex * ex + ey * ey) + ez * ez
                 if R > F(0):
@@ -645,6 +693,29 @@ def camera_variant(name, tex=None, **cam):
     return sd
 
 
+def skinned_variant(lighting_mode=0):
+    """A tube of 40 rings x 24 segments skinned by a chain of four bones (each vertex blending the
+    two nearest, exact 1.0 weights on the bone heights and a few 1.0 weights after a partial one),
+    lit by the five-light scene's lights, under material lighting mode `lighting_mode`."""
+    from tetra3d_gb300 import abi, scenes
+    base = scaled_variant()
+    rng = np.random.Generator(np.random.PCG64(9))
+    me = scenes.tube_mesh(rings=40, segments=24, height=3.0, radius=0.5)
+    me.colors = rng.uniform(0.5, 1.0, (me.nverts, 4)).astype(F)
+    me.joints, me.weights = scenes.tube_skin(me, rng, 4)
+    me.parts = [dict(tri_start=0, tri_count=me.ntris,
+                     mat=scenes.default_material(lighting_mode=lighting_mode, backface_culling=0))]
+    lights = [base.lights[i] for i in range(base.nlights)]
+    sd = scenes.SceneData([me], 1, lights, [[0, 1, 2, 3, 4]], name=f"skinned_tube{lighting_mode}")
+    pos = np.array([(0.3, -1.6, -5.5)], F)
+    scenes.set_models_trs(sd, 0, pos, [(1.0, 1.0, 1.0)], scenes.quat_to_mat(scenes.random_quats(rng, 1)))
+    sd.mv["skinned"][0] = 1
+    sd.mv["bone_first"][0] = 0
+    sd.bones = scenes.tube_bones(rng, 1, pos, 4, bend=0.9)
+    sd.camera = base.camera
+    return sd
+
+
 def cpu_cases():
     """Cases checked against the C++ oracle on the CPU only (the GPU's parity for these camera
     options is checked against the oracle by the feature-scene tests)."""
@@ -653,7 +724,8 @@ def cpu_cases():
             "c1_unlit": camera_variant("c1_unlit", lighting_on=0),
             "c1_ortho": camera_variant("c1_ortho", perspective=0, ortho_scale=3.0),
             "c1_ortho_pcorrect": camera_variant("c1_ortho_pcorrect", tex=(64, 64), perspective=0, ortho_scale=2.5,
-                                                perspective_corrected=1)}
+                                                perspective_corrected=1),
+            "skinned_tube": skinned_variant(), "skinned_tube_fixed": skinned_variant(1)}
 
 
 def is_transparent(md, mat):

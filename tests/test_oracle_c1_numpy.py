@@ -6,8 +6,9 @@ rotated with a non-uniform scale and five lights, on that scene with a light vol
 of its three shading modes, with the world's fog added or multiplied in, with fixed-normal and
 double-sided lighting, without backface culling, front-to-back and unsorted, lit by a
 LightGroup, and (oracle only) seen with perspective-corrected texture mapping (Custom0
-included), vertex snapping, lighting off or an orthographic camera: draw order and every
-emitted float, bit for bit."""
+included), vertex snapping, lighting off or an orthographic camera, and a tube skinned by a
+four-bone chain (default and fixed-normal lighting): draw order and every emitted float, bit
+for bit."""
 import os
 import sys
 
@@ -21,7 +22,8 @@ import make_c1_whole_path as G  # noqa: E402
 FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
          "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
-CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit", "c1_ortho", "c1_ortho_pcorrect"]  # the oracle only (the GPU's parity for these
+CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit", "c1_ortho", "c1_ortho_pcorrect", "skinned_tube",
+             "skinned_tube_fixed"]  # the oracle only (the GPU's parity for these
 # camera options is checked against the oracle by the feature-scene tests)
 ALL = CASES + CPU_CASES
 
@@ -126,6 +128,19 @@ def test_gpu_matches_numpy_restatement(ctx, fixture, scenes_, name):
                 assert np.array_equal(_bits(getattr(got, k)), _bits(fixture[f"{name}_{k}"])), (mode, k)
     finally:
         ctx.release(sid)
+
+
+def test_skinned_case_exercises_the_skin(scenes_):
+    """The skinned tube differs from the same tube drawn unskinned, and its weights hold blends,
+    exact 1.0 weights and 1.0 weights after a partial one (where Model.skinVertex stops)."""
+    S = G.scene_inputs(scenes_["skinned_tube"])
+    skinned = G.render(S)
+    plain = G.render(dict(S, skinned=False))
+    assert len(skinned[0]) == 1920 and not np.array_equal(_bits(skinned[1]), _bits(plain[1]))
+    w = S["weights"]
+    assert ((w > 0) & (w < 1)).any(1).sum() > 100 and (w == 1).any(1).sum() > 10
+    late = [(0 < w[v, :k]).any() and w[v, k] == 1 for v in range(len(w)) for k in range(1, 4)]
+    assert any(late)
 
 
 FRAMES = ["six_spheres", "six_spheres_transparent"]
