@@ -256,6 +256,9 @@ def scene_inputs(sd, model=0):
         joints=None if me.joints is None else np.asarray(me.joints, np.int64),
         weights=None if me.weights is None else np.asarray(me.weights, F),
         bones=None if not bool(mv["skinned"]) else np.asarray(sd.bones, F).reshape(-1, 4, 4),
+        shape_positions=None if me.shape_weights is None else np.asarray(me.shape_positions, F),
+        shape_normals=None if me.shape_weights is None else np.asarray(me.shape_normals, F),
+        shape_weights=None if me.shape_weights is None else np.asarray(me.shape_weights, F),
         abi=abi)
 
 
@@ -302,12 +305,22 @@ def in_frustum(S, M, dmin, dmax, skinned=False):
     return not (pcx > pcz + d or pcx < -pcz - d)
 
 
-def skin_vertices(S):
+def keyed_vertices(S):
+    """Mesh.VertexPositionWithShapeKeys / VertexNormalWithShapeKeys (mesh.go:796-822): each shape
+    key, in order, adds its delta times its weight to the base position and normal."""
+    P, N = S["positions"].copy(), S["normals"].copy()
+    if S["shape_weights"] is not None:
+        for k, w in enumerate(S["shape_weights"]):
+            P = (P + S["shape_positions"][k] * w).astype(F)
+            N = (N + S["shape_normals"][k] * w).astype(F)
+    return P, N
+
+
+def skin_vertices(S, P, N):
     """Model.skinVertex (model.go:559-594) for every vertex: the skin matrix starts at zero, each
     non-zero weight adds the bone influence scaled by it element by element (Matrix4.Add / Scale,
-    matrix.go:639-661), and a weight of exactly 1 replaces the sum and ends the loop; the
+    matrix.go:639-661), and a weight of exactly 1 replaces the sum and ends the loop; the (keyed)
     position goes through the matrix, the normal through it with its last row set to (0, 0, 0, 1)."""
-    P, N = S["positions"], S["normals"]
     J, Wt, B = S["joints"], S["weights"], S["bones"]
     nv = len(P)
     m = np.zeros((nv, 4, 4), F)
@@ -417,6 +430,8 @@ def render(S, want_custom0=False):
     dmax = [F(P[:, a].max()) for a in range(3)]
     maxspan = mag3(dmax[0] - dmin[0], dmax[1] - dmin[1], dmax[2] - dmin[2])
     skinned = S["skinned"]
+    # shape keys move the vertices; the dimensions and the triangle centres stay on the base mesh
+    Pk, Nk = keyed_vertices(S)
     if not in_frustum(S, M, dmin, dmax, skinned):
         return np.zeros(0, np.int64), np.zeros((0, 3, 4), F), np.zeros((0, 3, 4), F), np.zeros((0, 3), F)
     # ProcessVertices
@@ -425,10 +440,10 @@ def render(S, want_custom0=False):
     rc = multvec(ir, cp)
     icam = [rc[a] + ip[a] * (F(1) / isc[a]) for a in range(3)]
     if skinned:  # world-space vertices through the skin, then VP alone (model.go:755-770)
-        Pw, Nw = skin_vertices(S)
+        Pw, Nw = skin_vertices(S, Pk, Nk)
         clip = multvecw(vp, (Pw[:, 0], Pw[:, 1], Pw[:, 2]))
     else:
-        clip = multvecw(mvp, (P[:, 0], P[:, 1], P[:, 2]))  # per vertex, float32 arrays
+        clip = multvecw(mvp, (Pk[:, 0], Pk[:, 1], Pk[:, 2]))  # per vertex, float32 arrays
     X, Y, Z, Wc = clip
     if S["snap"] > F(0):  # Camera.VertexSnapping (model.go:813-818): math32.Round = half away from zero
         sn = S["snap"]
@@ -487,8 +502,8 @@ def render(S, want_custom0=False):
             vx, vy, vz = Pw[:, 0], Pw[:, 1], Pw[:, 2]
             nx, ny, nz = Nw[:, 0], Nw[:, 1], Nw[:, 2]
         else:
-            vx, vy, vz = P[:, 0], P[:, 1], P[:, 2]
-            nx, ny, nz = N[:, 0], N[:, 1], N[:, 2]
+            vx, vy, vz = Pk[:, 0], Pk[:, 1], Pk[:, 2]
+            nx, ny, nz = Nk[:, 0], Nk[:, 1], Nk[:, 2]
         for L in S["lights"]:
             col, e = L["color"], L["energy"]
             if L["type"] == abi.LIGHT_AMBIENT:
@@ -554,7 +569,7 @@ def render(S, want_custom0=False):
                 lg = np.where(on, lg + (col[1] * dfac) * e, lg).astype(F)
                 lb = np.where(on, lb + (col[2] * dfac) * e, lb).astype(F)
             elif L["type"] == abi.LIGHT_VOLUME:
-                cr_, cg_, cb_, on = volume_cells(S, L, M, P, N)
+                cr_, cg_, cb_, on = volume_cells(S, L, M, Pk, Nk)
                 lr = np.where(on, lr + (col[0] * cr_) * e, lr).astype(F)
                 lg = np.where(on, lg + (col[1] * cg_) * e, lg).astype(F)
                 lb = np.where(on, lb + (col[2] * cb_) * e, lb).astype(F)
@@ -716,6 +731,32 @@ def skinned_variant(lighting_mode=0):
     return sd
 
 
+def keyed_variant():
+    """The scaled five-light sphere with two shape keys: a bulge along the normals (weight 0.6)
+    and small random deltas (weight -0.3), with their normal deltas."""
+    sd = scaled_variant()
+    rng = np.random.Generator(np.random.PCG64(13))
+    me = sd.meshes[0]
+    bulge = (me.normals * rng.uniform(0.0, 0.25, (me.nverts, 1))).astype(F)
+    me.shape_positions = np.stack([bulge, rng.uniform(-0.05, 0.05, bulge.shape).astype(F)])
+    me.shape_normals = rng.uniform(-0.1, 0.1, (2, me.nverts, 3)).astype(F)
+    me.shape_weights = np.array([0.6, -0.3], F)
+    sd.name = "uv_sphere_keyed"
+    return sd
+
+
+def keyed_skinned_variant():
+    """The skinned tube with one shape key (weight 0.8) under its skin."""
+    sd = skinned_variant()
+    rng = np.random.Generator(np.random.PCG64(17))
+    me = sd.meshes[0]
+    me.shape_positions = (0.08 * rng.standard_normal((1, me.nverts, 3))).astype(F)
+    me.shape_normals = (0.05 * rng.standard_normal((1, me.nverts, 3))).astype(F)
+    me.shape_weights = np.array([0.8], F)
+    sd.name = "skinned_tube_keyed"
+    return sd
+
+
 def cpu_cases():
     """Cases checked against the C++ oracle on the CPU only (the GPU's parity for these camera
     options is checked against the oracle by the feature-scene tests)."""
@@ -725,7 +766,8 @@ def cpu_cases():
             "c1_ortho": camera_variant("c1_ortho", perspective=0, ortho_scale=3.0),
             "c1_ortho_pcorrect": camera_variant("c1_ortho_pcorrect", tex=(64, 64), perspective=0, ortho_scale=2.5,
                                                 perspective_corrected=1),
-            "skinned_tube": skinned_variant(), "skinned_tube_fixed": skinned_variant(1)}
+            "skinned_tube": skinned_variant(), "skinned_tube_fixed": skinned_variant(1),
+            "c1_shape_keys": keyed_variant(), "skinned_tube_keyed": keyed_skinned_variant()}
 
 
 def is_transparent(md, mat):
@@ -822,6 +864,13 @@ def input_digest(S):
         h.update(np.asarray([S["snap"], *S["tex"]], F).tobytes())
     if not S["perspective"]:
         h.update(np.asarray([0, S["ortho_scale"]], F).tobytes())
+    if S["skinned"]:
+        h.update(np.asarray([S["bone_first"]], np.int64).tobytes())
+        for k in ("joints", "weights", "bones"):
+            h.update(np.ascontiguousarray(S[k]).tobytes())
+    if S["shape_weights"] is not None:
+        for k in ("shape_positions", "shape_normals", "shape_weights"):
+            h.update(np.ascontiguousarray(S[k]).tobytes())
     if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)
         h.update(np.asarray([S["render_depth"], S["fog_on"], S["fog_mode"]], np.int64).tobytes())
         h.update(np.concatenate([S["fog_range"], S["fog_color"]]).tobytes())

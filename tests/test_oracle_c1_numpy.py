@@ -7,8 +7,8 @@ of its three shading modes, with the world's fog added or multiplied in, with fi
 double-sided lighting, without backface culling, front-to-back and unsorted, lit by a
 LightGroup, and (oracle only) seen with perspective-corrected texture mapping (Custom0
 included), vertex snapping, lighting off or an orthographic camera, and a tube skinned by a
-four-bone chain (default and fixed-normal lighting): draw order and every emitted float, bit
-for bit."""
+four-bone chain (default and fixed-normal lighting), the sphere with two shape keys and the
+skinned tube with one under its skin: draw order and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -23,7 +23,7 @@ FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
          "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
 CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit", "c1_ortho", "c1_ortho_pcorrect", "skinned_tube",
-             "skinned_tube_fixed"]  # the oracle only (the GPU's parity for these
+             "skinned_tube_fixed", "c1_shape_keys", "skinned_tube_keyed"]  # the oracle only (the GPU's parity for these
 # camera options is checked against the oracle by the feature-scene tests)
 ALL = CASES + CPU_CASES
 
@@ -141,6 +141,16 @@ def test_skinned_case_exercises_the_skin(scenes_):
     assert ((w > 0) & (w < 1)).any(1).sum() > 100 and (w == 1).any(1).sum() > 10
     late = [(0 < w[v, :k]).any() and w[v, k] == 1 for v in range(len(w)) for k in range(1, 4)]
     assert any(late)
+
+
+@pytest.mark.parametrize("name", ["c1_shape_keys", "skinned_tube_keyed"])
+def test_shape_key_cases_move_the_vertices(scenes_, name):
+    """The keys change what the stage emits (the triangle centres and dimensions stay on the
+    base mesh, the vertices move)."""
+    S = G.scene_inputs(scenes_[name])
+    keyed = G.render(S)
+    base = G.render(dict(S, shape_weights=None))
+    assert len(keyed[0]) != len(base[0]) or not np.array_equal(_bits(keyed[1]), _bits(base[1]))
 
 
 FRAMES = ["six_spheres", "six_spheres_transparent"]
