@@ -757,6 +757,18 @@ def keyed_skinned_variant():
     return sd
 
 
+def plain_colour_variant(shadeless=False):
+    """The scaled five-light sphere without a vertex colour channel (the model and material
+    colours alone), optionally with the model shadeless."""
+    sd = scaled_variant()
+    sd.meshes[0].colors = None
+    sd.mv["color"][0] = [0.9, 0.7, 0.5, 1.0]
+    if shadeless:
+        sd.mv["shadeless"][0] = 1
+    sd.name = "uv_sphere_plain" + ("_shadeless" if shadeless else "")
+    return sd
+
+
 def cpu_cases():
     """Cases checked against the C++ oracle on the CPU only (the GPU's parity for these camera
     options is checked against the oracle by the feature-scene tests)."""
@@ -767,7 +779,8 @@ def cpu_cases():
             "c1_ortho_pcorrect": camera_variant("c1_ortho_pcorrect", tex=(64, 64), perspective=0, ortho_scale=2.5,
                                                 perspective_corrected=1),
             "skinned_tube": skinned_variant(), "skinned_tube_fixed": skinned_variant(1),
-            "c1_shape_keys": keyed_variant(), "skinned_tube_keyed": keyed_skinned_variant()}
+            "c1_shape_keys": keyed_variant(), "skinned_tube_keyed": keyed_skinned_variant(),
+            "c1_no_colors": plain_colour_variant(), "c1_no_colors_shadeless": plain_colour_variant(True)}
 
 
 def is_transparent(md, mat):
@@ -871,6 +884,8 @@ def input_digest(S):
     if S["shape_weights"] is not None:
         for k in ("shape_positions", "shape_normals", "shape_weights"):
             h.update(np.ascontiguousarray(S[k]).tobytes())
+    if S["colors"] is None or S["shadeless"]:
+        h.update(np.asarray([S["colors"] is None, S["shadeless"]], np.int64).tobytes())
     if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)
         h.update(np.asarray([S["render_depth"], S["fog_on"], S["fog_mode"]], np.int64).tobytes())
         h.update(np.concatenate([S["fog_range"], S["fog_color"]]).tobytes())

@@ -8,7 +8,8 @@ double-sided lighting, without backface culling, front-to-back and unsorted, lit
 LightGroup, and (oracle only) seen with perspective-corrected texture mapping (Custom0
 included), vertex snapping, lighting off or an orthographic camera, and a tube skinned by a
 four-bone chain (default and fixed-normal lighting), the sphere with two shape keys and the
-skinned tube with one under its skin: draw order and every emitted float, bit for bit."""
+skinned tube with one under its skin, and the sphere without a vertex colour channel (lit and
+shadeless): draw order and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -23,7 +24,7 @@ FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
          "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
 CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit", "c1_ortho", "c1_ortho_pcorrect", "skinned_tube",
-             "skinned_tube_fixed", "c1_shape_keys", "skinned_tube_keyed"]  # the oracle only (the GPU's parity for these
+             "skinned_tube_fixed", "c1_shape_keys", "skinned_tube_keyed", "c1_no_colors", "c1_no_colors_shadeless"]  # the oracle only (the GPU's parity for these
 # camera options is checked against the oracle by the feature-scene tests)
 ALL = CASES + CPU_CASES
 
