@@ -223,18 +223,19 @@ def scene_inputs(sd, model=0):
     me = sd.meshes[int(mv["mesh"])]
     mat = me.parts[0]["mat"]
     cam = sd.camera
-    lights = []
-    ll = int(mv["light_list"])  # -1: the scene's light list (list 0); k >= 1: LightGroup k
-    for k in sd.lists[ll if ll >= 0 else 0]:
-        L = sd.lights[k]
+    def light_dict(L):
         Lt = np.asarray(L.transform[:], F).reshape(4, 4)
-        lights.append(dict(type=int(L.type), color=np.asarray(L.color[:3], F), energy=F(L.energy),
+        return dict(type=int(L.type), color=np.asarray(L.color[:3], F), energy=F(L.energy),
                            range=F(L.range), world_pos=[Lt[3, 0], Lt[3, 1], Lt[3, 2]],
                            world_rot=np.asarray(L.world_rotation[:], F).reshape(4, 4),
                            vol_min=np.asarray(L.vol_min[:], F), vol_max=np.asarray(L.vol_max[:], F),
                            cell_size=np.asarray(L.cell_size[:], F), offset=np.asarray(L.offset[:], F),
                            bias=np.asarray(L.bias[:], F), cell_count=[int(c) for c in L.cell_count],
-                           cell_first=int(L.cell_first)))
+                           cell_first=int(L.cell_first))
+    ll = int(mv["light_list"])  # -1: the scene's light list (list 0); k >= 1: LightGroup k
+    lights = [light_dict(sd.lights[k]) for k in sd.lists[ll if ll >= 0 else 0]]
+    all_lights = [light_dict(sd.lights[k]) for k in range(sd.nlights)]
+    cell_uses = None if sd.cell_uses is None else [list(map(int, u)) for u in sd.cell_uses]
     ct = np.asarray(cam.transform[:], F).reshape(4, 4)
     return dict(
         positions=me.positions.astype(F), normals=me.normals.astype(F), uvs=me.uvs.astype(F),
@@ -245,6 +246,7 @@ def scene_inputs(sd, model=0):
         backface=bool(mat["backface_culling"]), sort_mode=int(mat["sort_mode"]),
         lighting_mode=int(mat["lighting_mode"]), shadeless=bool(mat["shadeless"]) or bool(mv["shadeless"]),
         lv_mode=int(mat["lv_shading_mode"]), cells=np.asarray(sd.cells, F)[:max(0, sd.ncells)],
+        all_lights=all_lights, cell_uses=cell_uses,
         lights=lights, cam_pos=[ct[3, 0], ct[3, 1], ct[3, 2]],
         cam_rot=np.asarray(cam.world_rotation[:], F).reshape(4, 4), width=int(cam.width), height=int(cam.height),
         fov=F(cam.fov_y), near=F(cam.near_plane), far=F(cam.far_plane), depth_margin=F(cam.depth_margin),
@@ -363,14 +365,15 @@ def round_half_away(x):
 
 def volume_cells(S, L, M, P, N):
     """LightVolume.VertexLight (light.go:583-663) for every vertex of an unskinned model: the cell
-    colour each vertex takes (black where no cell) and whether the vertex adds anything (the light
-    returns early for vertices outside the volume's dimensions)."""
+    colour each vertex takes (black where no cell), whether the vertex adds anything (the light
+    returns early for vertices outside the volume's dimensions) and the scene cell whose
+    useLights light it first (-1: none)."""
     abi = S["abi"]
     mode = S["lv_mode"]
     nv = len(P)
     if mode == abi.LV_OFF:  # LightVolume.Light skips the pair
         z = np.zeros(nv, F)
-        return z, z, z, np.zeros(nv, bool)
+        return z, z, z, np.zeros(nv, bool), np.full(nv, -1)
     vmin, vmax, cs, off, bias = L["vol_min"], L["vol_max"], L["cell_size"], L["offset"], L["bias"]
     cnt = grid_counts(vmin, vmax, cs)
     assert cnt == L["cell_count"], (cnt, L["cell_count"])
@@ -387,11 +390,11 @@ def volume_cells(S, L, M, P, N):
         flat = np.where(inside, x + y * cnt[0] + z * cnt[0] * cnt[1], 0)
         rgb = cells[L["cell_first"] + flat, :3].astype(F)
         rgb = np.where(inside[..., None], rgb, F(0)).astype(F)
-        return rgb[..., 0], rgb[..., 1], rgb[..., 2]
+        return rgb[..., 0], rgb[..., 1], rgb[..., 2], np.where(inside, L["cell_first"] + flat, -1)
 
-    if mode == abi.LV_PER_OBJECT:  # the cell at Model.WorldPosition, for every vertex
-        r, g, b = cell_rgb(np.full(nv, M[3, 0], F), np.full(nv, M[3, 1], F), np.full(nv, M[3, 2], F))
-        return r, g, b, np.ones(nv, bool)
+    if mode == abi.LV_PER_OBJECT:  # the cell at Model.WorldPosition, for every vertex (no useLights)
+        r, g, b, _ = cell_rgb(np.full(nv, M[3, 0], F), np.full(nv, M[3, 1], F), np.full(nv, M[3, 2], F))
+        return r, g, b, np.ones(nv, bool), np.full(nv, -1)
     half = [cs[a] / F(2) for a in range(3)]
     if mode == abi.LV_PER_VERTEX_WITH_NORMAL:
         # only vertPosWithNormal is set in this mode: the containment test reads vertPos, which
@@ -405,8 +408,8 @@ def volume_cells(S, L, M, P, N):
         look = probe = [t[a] + bias[a] for a in range(3)]
     contains = ((probe[0] >= vmin[0]) & (probe[1] >= vmin[1]) & (probe[2] >= vmin[2]) &
                 (probe[0] <= vmax[0]) & (probe[1] <= vmax[1]) & (probe[2] <= vmax[2]))
-    r, g, b = cell_rgb(*look)
-    return r, g, b, contains
+    r, g, b, cell = cell_rgb(*look)
+    return r, g, b, contains, np.where(contains, cell, -1)
 
 
 def render(S, want_custom0=False):
@@ -504,12 +507,18 @@ def render(S, want_custom0=False):
         else:
             vx, vy, vz = Pk[:, 0], Pk[:, 1], Pk[:, 2]
             nx, ny, nz = Nk[:, 0], Nk[:, 1], Nk[:, 2]
-        for L in S["lights"]:
+        def add(lr, lg, lb, on, tr, tg, tb):
+            return (np.where(on, lr + tr, lr).astype(F), np.where(on, lg + tg, lg).astype(F),
+                    np.where(on, lb + tb, lb).astype(F))
+
+        def light_one(L, lr, lg, lb, mask, nested):
+            """One light's VertexLight on the vertices of `mask` (a cell's useLights when nested:
+            no model-level range skip, camera.go:1625-1629 applies to the scene's lights)."""
             col, e = L["color"], L["energy"]
             if L["type"] == abi.LIGHT_AMBIENT:
                 res = [col[0] * e, col[1] * e, col[2] * e]  # beginRender
-                lr, lg, lb = lr + res[0], lg + res[1], lb + res[2]
-            elif L["type"] == abi.LIGHT_DIRECTIONAL:
+                return add(lr, lg, lb, mask, res[0], res[1], res[2])
+            if L["type"] == abi.LIGHT_DIRECTIONAL:
                 fwd = unit3(L["world_rot"][2, :3])  # WorldRotation().Forward()
                 if S["lighting_mode"] == abi.LIGHTING_FIXED_NORMALS:
                     wn = [np.full(nv, fwd[0], F), np.full(nv, fwd[1], F), np.full(nv, fwd[2], F)]
@@ -520,19 +529,16 @@ def render(S, want_custom0=False):
                 df = (wn[0] * fwd[0] + wn[1] * fwd[1]) + wn[2] * fwd[2]
                 if S["lighting_mode"] == abi.LIGHTING_DOUBLE_SIDED:
                     df = np.abs(df)
-                on = df > F(0)
-                lr = np.where(on, lr + (col[0] * df) * e, lr).astype(F)
-                lg = np.where(on, lg + (col[1] * df) * e, lg).astype(F)
-                lb = np.where(on, lb + (col[2] * df) * e, lb).astype(F)
-            elif L["type"] == abi.LIGHT_POINT:
+                return add(lr, lg, lb, mask & (df > F(0)), (col[0] * df) * e, (col[1] * df) * e, (col[2] * df) * e)
+            if L["type"] == abi.LIGHT_POINT:
                 R = L["range"]
                 R2 = R * R
                 lp = L["world_pos"]
-                if R > F(0):  # model-level skip (camera.go:1625-1629)
+                if R > F(0) and not nested:  # model-level skip (camera.go:1625-1629)
                     dist = maxspan + R
                     ddx, ddy, ddz = mpos[0] - lp[0], mpos[1] - lp[1], mpos[2] - lp[2]
                     if (ddx * ddx + ddy * ddy) + ddz * ddz > dist * dist:
-                        continue
+                        return lr, lg, lb
                 if skinned:  # PointLight.beginModel: the light's own world position
                     wp = [F(lp[0]), F(lp[1]), F(lp[2])]
                 else:
@@ -541,13 +547,13 @@ def render(S, want_custom0=False):
                     wp = [rq[k] + p_[k] * (F(1) / s_[k]) for k in range(3)]
                 ex, ey, ez = wp[0] - vx, wp[1] - vy, wp[2] - vz
                 dist2 = (ex * ex + ey * ey) + ez * ez
-                if R > F(0):
-                    on = ~(dist2 > R2)
-                else:
-                    on = ~((F(1) / dist2) * e < F(0.001))
-                l = np.sqrt(((ex * ex + ey * ey) + ez * ez).astype(np.float64)).astype(F)
-                keep = (l < F(1e-8)) | (l == F(1))
-                with np.errstate(divide="ignore", invalid="ignore"):
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    if R > F(0):
+                        on = ~(dist2 > R2)
+                    else:
+                        on = ~((F(1) / dist2) * e < F(0.001))
+                    l = np.sqrt(((ex * ex + ey * ey) + ez * ez).astype(np.float64)).astype(F)
+                    keep = (l < F(1e-8)) | (l == F(1))
                     ux = np.where(keep, ex, ex / l).astype(F)
                     uy = np.where(keep, ey, ey / l).astype(F)
                     uz = np.where(keep, ez, ez / l).astype(F)
@@ -565,14 +571,21 @@ def render(S, want_custom0=False):
                         q = (R2 - dist2) / dist2
                         q = np.where(q < F(0), F(0), np.where(q > F(1), F(1), q)).astype(F)
                         dfac = dfac * q
-                lr = np.where(on, lr + (col[0] * dfac) * e, lr).astype(F)
-                lg = np.where(on, lg + (col[1] * dfac) * e, lg).astype(F)
-                lb = np.where(on, lb + (col[2] * dfac) * e, lb).astype(F)
-            elif L["type"] == abi.LIGHT_VOLUME:
-                cr_, cg_, cb_, on = volume_cells(S, L, M, Pk, Nk)
-                lr = np.where(on, lr + (col[0] * cr_) * e, lr).astype(F)
-                lg = np.where(on, lg + (col[1] * cg_) * e, lg).astype(F)
-                lb = np.where(on, lb + (col[2] * cb_) * e, lb).astype(F)
+                return add(lr, lg, lb, mask & on, (col[0] * dfac) * e, (col[1] * dfac) * e, (col[2] * dfac) * e)
+            if L["type"] == abi.LIGHT_VOLUME:
+                cr_, cg_, cb_, on, cell = volume_cells(S, L, M, Pk, Nk)
+                on &= mask
+                # the cell's useLights first, in list order, on the vertices in that cell (light.go:650-656)
+                if S["cell_uses"] is not None and not nested:
+                    for c in sorted(set(cell[on & (cell >= 0)].tolist())):
+                        for u in S["cell_uses"][c]:
+                            lr, lg, lb = light_one(S["all_lights"][u], lr, lg, lb, on & (cell == c), True)
+                return add(lr, lg, lb, on, (col[0] * cr_) * e, (col[1] * cg_) * e, (col[2] * cb_) * e)
+            return lr, lg, lb
+
+        every = np.ones(nv, bool)
+        for L in S["lights"]:
+            lr, lg, lb = light_one(L, lr, lg, lb, every, False)
     # the emit loop, corner by corner in draw order
     mp = S["model_color"] * S["mat_color"]  # Color4.MultiplyRGBA
     margin = (far - near) * S["depth_margin"]
@@ -769,6 +782,20 @@ def plain_colour_variant(shadeless=False):
     return sd
 
 
+def nested_variant():
+    """The per-vertex light-volume scene with LightVolumeCell.useLights: seven in ten cells each
+    light their vertices with one to three of the scene's other lights (ambient, directional and
+    point lights, in random order) before their own colour."""
+    from tetra3d_gb300 import abi
+    sd = volume_variant(abi.LV_PER_VERTEX)
+    rng = np.random.Generator(np.random.PCG64(19))
+    usable = [0, 1, 2, 3, 4]
+    sd.cell_uses = [list(map(int, rng.choice(usable, int(rng.integers(1, 4)), replace=False))) if rng.random() < 0.7
+                    else [] for _ in range(sd.ncells)]
+    sd.name = "uv_sphere_volume_nested"
+    return sd
+
+
 def cpu_cases():
     """Cases checked against the C++ oracle on the CPU only (the GPU's parity for these camera
     options is checked against the oracle by the feature-scene tests)."""
@@ -780,7 +807,8 @@ def cpu_cases():
                                                 perspective_corrected=1),
             "skinned_tube": skinned_variant(), "skinned_tube_fixed": skinned_variant(1),
             "c1_shape_keys": keyed_variant(), "skinned_tube_keyed": keyed_skinned_variant(),
-            "c1_no_colors": plain_colour_variant(), "c1_no_colors_shadeless": plain_colour_variant(True)}
+            "c1_no_colors": plain_colour_variant(), "c1_no_colors_shadeless": plain_colour_variant(True),
+            "c1_volume_nested": nested_variant()}
 
 
 def is_transparent(md, mat):
@@ -884,6 +912,8 @@ def input_digest(S):
     if S["shape_weights"] is not None:
         for k in ("shape_positions", "shape_normals", "shape_weights"):
             h.update(np.ascontiguousarray(S[k]).tobytes())
+    if S["cell_uses"] is not None:
+        h.update(repr(S["cell_uses"]).encode())
     if S["colors"] is None or S["shadeless"]:
         h.update(np.asarray([S["colors"] is None, S["shadeless"]], np.int64).tobytes())
     if S["fog_on"] or not S["render_depth"]:  # the fog and depth options (unchanged digests otherwise)

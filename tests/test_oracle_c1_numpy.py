@@ -9,7 +9,8 @@ LightGroup, and (oracle only) seen with perspective-corrected texture mapping (C
 included), vertex snapping, lighting off or an orthographic camera, and a tube skinned by a
 four-bone chain (default and fixed-normal lighting), the sphere with two shape keys and the
 skinned tube with one under its skin, and the sphere without a vertex colour channel (lit and
-shadeless): draw order and every emitted float, bit for bit."""
+shadeless), and the per-vertex light volume whose cells light their vertices with other lights
+first (LightVolumeCell.useLights): draw order and every emitted float, bit for bit."""
 import os
 import sys
 
@@ -24,7 +25,8 @@ FIXTURE = os.path.join(HERE, "golden", "c1_whole_path.npz")
 CASES = ["c1", "c1_scaled_5lights", "c1_volume_vertex", "c1_volume_normal", "c1_volume_object", "c1_fog_add",
          "c1_fog_sub", "c1_fixed_normals", "c1_double_sided_nocull", "c1_unsorted_group"]
 CPU_CASES = ["c1_pcorrect", "c1_snap", "c1_unlit", "c1_ortho", "c1_ortho_pcorrect", "skinned_tube",
-             "skinned_tube_fixed", "c1_shape_keys", "skinned_tube_keyed", "c1_no_colors", "c1_no_colors_shadeless"]  # the oracle only (the GPU's parity for these
+             "skinned_tube_fixed", "c1_shape_keys", "skinned_tube_keyed", "c1_no_colors", "c1_no_colors_shadeless",
+             "c1_volume_nested"]  # the oracle only (the GPU's parity for these
 # camera options is checked against the oracle by the feature-scene tests)
 ALL = CASES + CPU_CASES
 
@@ -152,6 +154,14 @@ def test_shape_key_cases_move_the_vertices(scenes_, name):
     keyed = G.render(S)
     base = G.render(dict(S, shape_weights=None))
     assert len(keyed[0]) != len(base[0]) or not np.array_equal(_bits(keyed[1]), _bits(base[1]))
+
+
+def test_nested_case_uses_the_cell_lights(scenes_):
+    """The cells' useLights change the colours of hundreds of corners."""
+    S = G.scene_inputs(scenes_["c1_volume_nested"])
+    nested = G.render(S)[2]
+    plain = G.render(dict(S, cell_uses=None))[2]
+    assert (nested != plain).any(-1).sum() > 300
 
 
 FRAMES = ["six_spheres", "six_spheres_transparent"]
