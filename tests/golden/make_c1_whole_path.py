@@ -830,10 +830,31 @@ def render_frame(sd):
     restatement's for that model (nothing for a model outside the frustum). Returns
     [(model, triangle order, xyuv, rgba, depth)] in draw order."""
     solids, transparents = [], []
+    # Model.DynamicBatchAdd: members draw only inside their owner's pair (opaque batches here)
+    batches = {}
     for m in range(sd.nmodels):
+        if int(sd.mv[m]["batched"]):
+            batches.setdefault(int(sd.mv[m]["batch_owner"]), []).append(m)
+    for m in range(sd.nmodels):
+        if int(sd.mv[m]["batched"]):
+            continue
         S = scene_inputs(sd, m)
         assert S["render_depth"]
         md = sd.mv[m]
+        if m in batches:
+            # the owner's pair: its members far to near from the camera (camera.go:2075-2093,
+            # Node.DistanceSquaredTo), each culled by its own sphere; the owner draws no mesh
+            cp = S["cam_pos"]
+
+            def d2(k):
+                wp = np.asarray(sd.mv[k]["transform"], F).reshape(4, 4)[3, :3]
+                dx, dy, dz = F(cp[0] - wp[0]), F(cp[1] - wp[1]), F(cp[2] - wp[2])
+                return float((dx * dx + dy * dy) + dz * dz)
+            dist = [d2(k) for k in batches[m]]
+            assert len(set(dist)) == len(dist), "sort.Slice is not stable: keep the distances distinct"
+            for k in sorted(batches[m], key=d2, reverse=True):
+                solids.append((k,) + tuple(render(scene_inputs(sd, k))))
+            continue
         mat = sd.meshes[int(md["mesh"])].parts[0]["mat"]
         item = (m,) + tuple(render(S))
         if is_transparent(md, mat):
@@ -932,9 +953,30 @@ def transparent_variant():
     return sd
 
 
+def batch_variant():
+    """Six spheres, four of them members of model 0's dynamic batch (one behind the camera, culled
+    inside the batch; two lit by a LightGroup), and one model drawn on its own after the batch."""
+    from tetra3d_gb300 import scenes
+    base = scaled_variant()
+    rng = np.random.Generator(np.random.PCG64(23))
+    lights = [base.lights[i] for i in range(base.nlights)]
+    sd = scenes.SceneData([base.meshes[0]], 6, lights, [[0, 1, 2, 3, 4], [0, 2, 3]], name="batch6")
+    pos = np.array([(0, 0, -5), (-2.0, 0.5, -8), (1.5, -0.5, -4.5), (2.5, 0.8, -11), (0, 0, 7), (-1.2, -1.0, -6)], F)
+    scl = rng.uniform(0.4, 1.0, (6, 3)).astype(F)
+    rot = scenes.quat_to_mat(scenes.random_quats(rng, 6))
+    scenes.set_models_trs(sd, np.zeros(6, np.uint32), pos, scl, rot)
+    sd.mv["batched"][1:5] = 1
+    sd.mv["batch_owner"][1:5] = 0
+    sd.mv["batch_part"][1:5] = 0
+    sd.mv["light_list"][[2, 3]] = 1
+    sd.camera = base.camera
+    return sd
+
+
 def frame_cases():
     """Multi-model cases, checked against the C++ oracle pair by pair."""
-    return {"six_spheres": multi_model_variant(), "six_spheres_transparent": transparent_variant()}
+    return {"six_spheres": multi_model_variant(), "six_spheres_transparent": transparent_variant(),
+            "batch6": batch_variant()}
 
 
 def main():

@@ -164,7 +164,8 @@ def test_nested_case_uses_the_cell_lights(scenes_):
     assert (nested != plain).any(-1).sum() > 300
 
 
-FRAMES = ["six_spheres", "six_spheres_transparent"]
+FRAMES = ["six_spheres", "six_spheres_transparent", "batch6"]
+CULLED = {"six_spheres": 2, "six_spheres_transparent": 2, "batch6": 1}
 
 
 @pytest.mark.parametrize("name", FRAMES)
@@ -183,14 +184,15 @@ def test_frame_restatement_reproduces_fixture(fixture, name):
 
 @pytest.mark.parametrize("name", FRAMES)
 def test_cpp_oracle_matches_frame_restatement(built, fixture, name):
-    """Six models of one scene (two of them transparent in the second frame): the oracle's render
-    pairs in draw order (solids in model order, then transparents far to near), the two the
-    frustum test drops empty, and every other pair's triangles and floats equal to the
+    """Six models of one scene (two of them transparent in the second frame; four members of a
+    dynamic batch in the third): the oracle's render pairs in draw order (solids in model order,
+    a batch's members far to near in its owner's place, then transparents far to near), the
+    models the frustum test drops empty, and every other pair's triangles and floats equal to the
     restatement's."""
     from oracle import pyoracle
     sd = G.frame_cases()[name]
     ref = pyoracle.render(sd, sd.camera)
-    assert ref.culled_models == 2
+    assert ref.culled_models == CULLED[name]
     assert np.array_equal(np.array([s["model"] for s in ref.segments], np.uint32), fixture[f"{name}_models"])
     assert np.array_equal(np.array([s["count"] for s in ref.segments], np.uint32), fixture[f"{name}_counts"])
     assert np.array_equal(ref.tri_index.astype(np.uint32), fixture[f"{name}_order"]), "draw order"
