@@ -214,14 +214,16 @@ def projection_ortho(near, far, w, h, scale):
 
 # ---- the scene ----
 
-def scene_inputs(sd, model=0):
-    """The binary32 inputs the restatement reads from a SceneData for one of its models (a model
-    of a one-part mesh)."""
+def scene_inputs(sd, model=0, part=0):
+    """The binary32 inputs the restatement reads from a SceneData for one render pair: a model and
+    one part of its mesh (the part's triangles and material; the mesh's vertices and
+    dimensions)."""
     from tetra3d_gb300 import abi
     assert 0 <= model < sd.nmodels
     mv = sd.mv[model]
     me = sd.meshes[int(mv["mesh"])]
-    mat = me.parts[0]["mat"]
+    mat = me.parts[part]["mat"]
+    t0, nt = int(me.parts[part]["tri_start"]), int(me.parts[part]["tri_count"])
     cam = sd.camera
     def light_dict(L):
         Lt = np.asarray(L.transform[:], F).reshape(4, 4)
@@ -239,7 +241,7 @@ def scene_inputs(sd, model=0):
     ct = np.asarray(cam.transform[:], F).reshape(4, 4)
     return dict(
         positions=me.positions.astype(F), normals=me.normals.astype(F), uvs=me.uvs.astype(F),
-        colors=None if me.colors is None else me.colors.astype(F), indices=me.indices.astype(np.int64),
+        colors=None if me.colors is None else me.colors.astype(F), indices=np.asarray(me.indices, np.int64).reshape(-1, 3)[t0:t0 + nt], tri_base=t0,
         model_pos=np.asarray(mv["position"], F), model_scale=np.asarray(mv["scale"], F),
         model_rot=np.asarray(mv["rotation"], F).reshape(4, 4), model_color=np.asarray(mv["color"], F),
         mat_color=np.asarray(mat["color"], F), tex=(F(mat["tex_w"]), F(mat["tex_h"])),
@@ -629,6 +631,7 @@ def render(S, want_custom0=False):
     if not S["render_depth"] and not S["fog_on"]:
         dep = np.zeros_like(dep)  # no depth is computed (the stream holds 0)
     xyuv = np.stack([xs, ys, u, v], -1).astype(F)
+    order = order + S["tri_base"]  # mesh-absolute triangle numbers
     if want_custom0:
         return order, xyuv, col.astype(F), dep, custom0
     return order, xyuv, col.astype(F), dep
@@ -827,8 +830,8 @@ def render_frame(sd):
     pairs in model order, then the transparent pass by RenderOrder ascending and, within one
     order, by the squared camera distance to the model (Vector3.DistanceSquaredTo,
     vector.go:242-247) far to near (camera.go:1343-1457, :2050-2106). Each pair's stream is the
-    restatement's for that model (nothing for a model outside the frustum). Returns
-    [(model, triangle order, xyuv, rgba, depth)] in draw order."""
+    restatement's for that model and part (nothing for a model outside the frustum). Returns
+    [(model, triangle order, xyuv, rgba, depth, part)] in draw order."""
     solids, transparents = [], []
     # Model.DynamicBatchAdd: members draw only inside their owner's pair (opaque batches here)
     batches = {}
@@ -838,9 +841,10 @@ def render_frame(sd):
     for m in range(sd.nmodels):
         if int(sd.mv[m]["batched"]):
             continue
+        md = sd.mv[m]
+        nparts = len(sd.meshes[int(md["mesh"])].parts)
         S = scene_inputs(sd, m)
         assert S["render_depth"]
-        md = sd.mv[m]
         if m in batches:
             # the owner's pair: its members far to near from the camera (camera.go:2075-2093,
             # Node.DistanceSquaredTo), each culled by its own sphere; the owner draws no mesh
@@ -853,19 +857,21 @@ def render_frame(sd):
             dist = [d2(k) for k in batches[m]]
             assert len(set(dist)) == len(dist), "sort.Slice is not stable: keep the distances distinct"
             for k in sorted(batches[m], key=d2, reverse=True):
-                solids.append((k,) + tuple(render(scene_inputs(sd, k))))
+                for q in range(len(sd.meshes[int(sd.mv[k]["mesh"])].parts)):
+                    solids.append((k,) + tuple(render(scene_inputs(sd, k, q))) + (q,))
             continue
-        mat = sd.meshes[int(md["mesh"])].parts[0]["mat"]
-        item = (m,) + tuple(render(S))
-        if is_transparent(md, mat):
-            wp = np.asarray(md["transform"], F).reshape(4, 4)[3, :3]  # Model.WorldPosition
-            cp = S["cam_pos"]
-            dx, dy, dz = F(cp[0] - wp[0]), F(cp[1] - wp[1]), F(cp[2] - wp[2])
-            dist = (dx * dx + dy * dy) + dz * dz
-            order = int(mat["render_order"]) if mat["present"] else 0
-            transparents.append(((order, -float(dist)), item))
-        else:
-            solids.append(item)
+        for q in range(nparts):  # one render pair per mesh part, in part order
+            mat = sd.meshes[int(md["mesh"])].parts[q]["mat"]
+            item = (m,) + tuple(render(scene_inputs(sd, m, q))) + (q,)
+            if is_transparent(md, mat):
+                wp = np.asarray(md["transform"], F).reshape(4, 4)[3, :3]  # Model.WorldPosition
+                cp = S["cam_pos"]
+                dx, dy, dz = F(cp[0] - wp[0]), F(cp[1] - wp[1]), F(cp[2] - wp[2])
+                dist = (dx * dx + dy * dy) + dz * dz
+                order = int(mat["render_order"]) if mat["present"] else 0
+                transparents.append(((order, -float(dist)), item))
+            else:
+                solids.append(item)
     transparents.sort(key=lambda t: t[0])  # a strict weak order: any stable sort agrees
     return solids + [t[1] for t in transparents]
 
@@ -973,10 +979,33 @@ def batch_variant():
     return sd
 
 
+def two_part_variant():
+    """Three models of a sphere cut into two mesh parts: the top half opaque with the default
+    material, the bottom half with fixed-normal lighting, front-to-back sorting and a material
+    alpha of 0.6 (so it is drawn in the transparent pass, far to near)."""
+    import copy
+    from tetra3d_gb300 import abi, scenes
+    base = scaled_variant()
+    rng = np.random.Generator(np.random.PCG64(29))
+    me = copy.deepcopy(base.meshes[0])
+    half = me.ntris // 2
+    m0 = dict(me.parts[0]["mat"])
+    m1 = dict(m0, lighting_mode=abi.LIGHTING_FIXED_NORMALS, sort_mode=abi.SORT_FRONT_TO_BACK, color=(1, 1, 1, 0.6))
+    me.parts = [dict(tri_start=0, tri_count=half, mat=m0), dict(tri_start=half, tri_count=me.ntris - half, mat=m1)]
+    lights = [base.lights[i] for i in range(base.nlights)]
+    sd = scenes.SceneData([me], 3, lights, [[0, 1, 2, 3, 4], [0, 2, 3]], name="two_parts")
+    pos = np.array([(0, 0, -6), (-1.8, 0.6, -4.5), (1.6, -0.4, -8)], F)
+    scl = rng.uniform(0.6, 1.2, (3, 3)).astype(F)
+    scenes.set_models_trs(sd, np.zeros(3, np.uint32), pos, scl, scenes.quat_to_mat(scenes.random_quats(rng, 3)))
+    sd.mv["light_list"][1] = 1
+    sd.camera = base.camera
+    return sd
+
+
 def frame_cases():
     """Multi-model cases, checked against the C++ oracle pair by pair."""
     return {"six_spheres": multi_model_variant(), "six_spheres_transparent": transparent_variant(),
-            "batch6": batch_variant()}
+            "batch6": batch_variant(), "two_parts": two_part_variant()}
 
 
 def main():
@@ -984,6 +1013,7 @@ def main():
     for name, sd in frame_cases().items():
         parts = render_frame(sd)
         out[f"{name}_models"] = np.array([p[0] for p in parts], np.uint32)
+        out[f"{name}_parts"] = np.array([p[5] for p in parts], np.uint32)
         out[f"{name}_counts"] = np.array([len(p[1]) for p in parts], np.uint32)
         out[f"{name}_order"] = np.concatenate([p[1] for p in parts]).astype(np.uint32)
         for k, i in (("xyuv", 2), ("rgba", 3), ("depth", 4)):

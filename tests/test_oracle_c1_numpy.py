@@ -164,8 +164,8 @@ def test_nested_case_uses_the_cell_lights(scenes_):
     assert (nested != plain).any(-1).sum() > 300
 
 
-FRAMES = ["six_spheres", "six_spheres_transparent", "batch6"]
-CULLED = {"six_spheres": 2, "six_spheres_transparent": 2, "batch6": 1}
+FRAMES = ["six_spheres", "six_spheres_transparent", "batch6", "two_parts"]
+CULLED = {"six_spheres": 2, "six_spheres_transparent": 2, "batch6": 1, "two_parts": 0}
 
 
 @pytest.mark.parametrize("name", FRAMES)
@@ -176,6 +176,7 @@ def test_frame_restatement_reproduces_fixture(fixture, name):
     assert bytes(fixture[f"{name}_digest"]).hex() == digest.hexdigest(), "scene inputs changed"
     parts = G.render_frame(sd)
     assert np.array_equal(np.array([p[0] for p in parts], np.uint32), fixture[f"{name}_models"])
+    assert np.array_equal(np.array([p[5] for p in parts], np.uint32), fixture[f"{name}_parts"])
     assert np.array_equal(np.array([len(p[1]) for p in parts], np.uint32), fixture[f"{name}_counts"])
     assert np.array_equal(np.concatenate([p[1] for p in parts]).astype(np.uint32), fixture[f"{name}_order"])
     for k, i in (("xyuv", 2), ("rgba", 3), ("depth", 4)):
@@ -185,7 +186,8 @@ def test_frame_restatement_reproduces_fixture(fixture, name):
 @pytest.mark.parametrize("name", FRAMES)
 def test_cpp_oracle_matches_frame_restatement(built, fixture, name):
     """Six models of one scene (two of them transparent in the second frame; four members of a
-    dynamic batch in the third): the oracle's render pairs in draw order (solids in model order,
+    dynamic batch in the third; a mesh cut into an opaque and a transparent part in the fourth):
+    the oracle's render pairs in draw order (solids in model and part order,
     a batch's members far to near in its owner's place, then transparents far to near), the
     models the frustum test drops empty, and every other pair's triangles and floats equal to the
     restatement's."""
@@ -194,6 +196,7 @@ def test_cpp_oracle_matches_frame_restatement(built, fixture, name):
     ref = pyoracle.render(sd, sd.camera)
     assert ref.culled_models == CULLED[name]
     assert np.array_equal(np.array([s["model"] for s in ref.segments], np.uint32), fixture[f"{name}_models"])
+    assert np.array_equal(np.array([s["part"] for s in ref.segments], np.uint32), fixture[f"{name}_parts"])
     assert np.array_equal(np.array([s["count"] for s in ref.segments], np.uint32), fixture[f"{name}_counts"])
     assert np.array_equal(ref.tri_index.astype(np.uint32), fixture[f"{name}_order"]), "draw order"
     for k in ("xyuv", "rgba", "depth"):
